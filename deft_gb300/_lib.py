@@ -1,0 +1,111 @@
+"""ctypes loader for the in-tree CUDA library libdeft_gb300.so.
+
+There is no CPU fallback: if the library is missing or cannot initialise a
+GPU, every call raises.
+"""
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libdeft_gb300.so")
+
+OK = 0
+ERR_ARG, ERR_CUDA, ERR_NAN, ERR_LINESEARCH, ERR_MAXITER, ERR_NOMEM = 1, 2, 3, 4, 5, 6
+TERM_HS, TERM_IDEAL, TERM_MU, TERM_VEXT, TERM_MASK = 1, 2, 4, 8, 16
+NTERMS = 6
+LS_SECANT, LS_QUADRATIC_REF = 0, 1
+
+# Every symbol include/deft_gb300.h declares.
+EXPORTS = (
+    "deft_strerror", "deft_last_error",
+    "deft_ctx_create", "deft_ctx_destroy", "deft_ctx_sync", "deft_ctx_stream",
+    "deft_grid_create", "deft_grid_create_dx", "deft_grid_destroy", "deft_grid_info",
+    "deft_grid_fft", "deft_grid_ifft",
+    "deft_fmt_create", "deft_fmt_destroy", "deft_fmt_set_params", "deft_fmt_set_vext",
+    "deft_fmt_set_mask", "deft_fmt_energy", "deft_fmt_energy_grad", "deft_fmt_weighted",
+    "deft_find_chemical_potential",
+    "deft_cg_create", "deft_cg_destroy", "deft_cg_set_x", "deft_cg_get_x", "deft_cg_x_device",
+    "deft_cg_step", "deft_cg_solve",
+)
+
+
+class DeftError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"deft_gb300 status {status}: {msg}")
+        self.status = status
+
+
+class FmtParams(ctypes.Structure):
+    _fields_ = [("R", ctypes.c_double), ("kT", ctypes.c_double), ("mu", ctypes.c_double),
+                ("terms", ctypes.c_int)]
+
+
+class CgParams(ctypes.Structure):
+    _fields_ = [("linesearch", ctypes.c_int), ("gtol", ctypes.c_double), ("maxiter", ctypes.c_int),
+                ("step", ctypes.c_double), ("precision", ctypes.c_double)]
+
+
+class CgStatus(ctypes.Structure):
+    _fields_ = [("iter", ctypes.c_int), ("evals", ctypes.c_int), ("energy", ctypes.c_double),
+                ("gnorm", ctypes.c_double), ("converged", ctypes.c_int), ("status", ctypes.c_int)]
+
+
+_lib = None
+_vp = ctypes.c_void_p
+_dp = ctypes.c_void_p  # data pointers are passed as raw addresses
+_pp = ctypes.POINTER(ctypes.c_void_p)
+
+
+def load():
+    """Load the library (building it first if it is absent and nvcc exists)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        from . import _build
+        _build.build()
+    L = ctypes.CDLL(LIB_PATH)
+    sig = {
+        "deft_strerror": (ctypes.c_char_p, [ctypes.c_int]),
+        "deft_last_error": (ctypes.c_char_p, []),
+        "deft_ctx_create": (ctypes.c_int, [ctypes.c_int, _pp]),
+        "deft_ctx_destroy": (ctypes.c_int, [_vp]),
+        "deft_ctx_sync": (ctypes.c_int, [_vp]),
+        "deft_ctx_stream": (_vp, [_vp]),
+        "deft_grid_create": (ctypes.c_int, [_vp, _dp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _pp]),
+        "deft_grid_create_dx": (ctypes.c_int, [_vp, _dp, ctypes.c_double, _pp]),
+        "deft_grid_destroy": (ctypes.c_int, [_vp]),
+        "deft_grid_info": (ctypes.c_int, [_vp, _dp, _dp, _dp, _dp]),
+        "deft_grid_fft": (ctypes.c_int, [_vp, _dp, _dp, ctypes.c_int]),
+        "deft_grid_ifft": (ctypes.c_int, [_vp, _dp, _dp, ctypes.c_int]),
+        "deft_fmt_create": (ctypes.c_int, [_vp, ctypes.POINTER(FmtParams), _pp]),
+        "deft_fmt_destroy": (ctypes.c_int, [_vp]),
+        "deft_fmt_set_params": (ctypes.c_int, [_vp, ctypes.POINTER(FmtParams)]),
+        "deft_fmt_set_vext": (ctypes.c_int, [_vp, _dp, ctypes.c_int]),
+        "deft_fmt_set_mask": (ctypes.c_int, [_vp, _dp, ctypes.c_int]),
+        "deft_fmt_energy": (ctypes.c_int, [_vp, _dp, ctypes.c_int, _dp, _dp]),
+        "deft_fmt_energy_grad": (ctypes.c_int, [_vp, _dp, ctypes.c_int, _dp, _dp, _dp]),
+        "deft_fmt_weighted": (ctypes.c_int, [_vp, _dp, ctypes.c_int, _dp]),
+        "deft_find_chemical_potential": (ctypes.c_int, [ctypes.c_double, ctypes.c_double,
+                                                        ctypes.c_double, _dp]),
+        "deft_cg_create": (ctypes.c_int, [_vp, ctypes.POINTER(CgParams), _pp]),
+        "deft_cg_destroy": (ctypes.c_int, [_vp]),
+        "deft_cg_set_x": (ctypes.c_int, [_vp, _dp, ctypes.c_int]),
+        "deft_cg_get_x": (ctypes.c_int, [_vp, _dp, ctypes.c_int]),
+        "deft_cg_x_device": (_vp, [_vp]),
+        "deft_cg_step": (ctypes.c_int, [_vp, ctypes.POINTER(CgStatus)]),
+        "deft_cg_solve": (ctypes.c_int, [_vp, ctypes.POINTER(CgStatus)]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def check(status):
+    if status != OK:
+        msg = load().deft_last_error().decode(errors="replace")
+        raise DeftError(status, msg)
+    return status

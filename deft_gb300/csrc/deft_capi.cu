@@ -1,0 +1,830 @@
+// C ABI of deft_gb300 (include/deft_gb300.h): context / grid / functional /
+// minimiser objects over the sm_103a engine in fmt_engine.cu, and the host
+// side of the conjugate-gradient minimisers.  The CG control flow runs on
+// the host; every vector operation and reduction runs on the GPU, and only
+// scalars (energies and dot products) come back.
+#include "../../include/deft_gb300.h"
+#include "fmt_engine.h"
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+using deft::Engine;
+
+struct deft_ctx {
+  int device;
+  cudaStream_t stream;
+};
+
+struct deft_grid {
+  deft_ctx *ctx;
+  deft::GridSpec spec;
+  Engine *eng;
+  double *in_buf;   // NR staging for host inputs
+  double *out_buf;  // NR staging for host outputs
+  double2 *c_buf;   // NC staging for spectra
+};
+
+struct deft_fmt {
+  deft_grid *grid;
+  deft_fmt_params p;
+  double *V;
+  double *mask;
+  double *g_buf;
+  double *w_buf;  // 5*NR, allocated on first deft_fmt_weighted
+};
+
+struct deft_cg {
+  deft_fmt *f;
+  deft_cg_params p;
+  double *x, *g, *d, *gold;
+  // shared state
+  int iter = 0, evals = 0;
+  // secant CG state
+  bool have_g = false;
+  double E = 0, gg = 0, ggold = 0, goldsqr = 0, s_prev = 0, alpha = 0;
+  // reference CG state (src/ConjugateGradient.cpp:20-45)
+  double step = 0, oldgradsqr = 0;
+  bool e_valid = false;
+  double e_cache = 0;
+  // Precision modifier state (src/Precision.cpp:23-48)
+  double dEdn = 0, log_ratio_avg = 0, deltaE = 0, err_est = 0;
+  bool done = false;
+};
+
+namespace {
+
+thread_local std::string g_err;
+
+int set_err(int code, const std::string &msg) {
+  g_err = msg;
+  return code;
+}
+
+int cuda_err(cudaError_t e, const char *what) {
+  g_err = std::string(what) + ": " + cudaGetErrorString(e);
+  return e == cudaErrorMemoryAllocation ? DEFT_ERR_NOMEM : DEFT_ERR_CUDA;
+}
+
+int eng_err(Engine *eng) {
+  g_err = eng->last_error();
+  return DEFT_ERR_CUDA;
+}
+
+deft::FmtSpec spec_of(const deft_fmt *f) {
+  deft::FmtSpec s;
+  s.R = f->p.R;
+  s.kT = f->p.kT;
+  s.mu = f->p.mu;
+  s.terms = f->p.terms;
+  if (!f->V) s.terms &= ~DEFT_TERM_VEXT;
+  if (!f->mask) s.terms &= ~DEFT_TERM_MASK;
+  return s;
+}
+
+size_t nr(const deft_grid *g) { return (size_t)g->eng->geom().NR; }
+
+// Stage a field: host input goes through the grid's staging buffer.
+int stage_in(deft_grid *g, const double *src, int on_device, double *dst, const double **out) {
+  if (on_device) {
+    *out = src;
+    return DEFT_OK;
+  }
+  cudaError_t e = cudaMemcpyAsync(dst, src, sizeof(double) * nr(g), cudaMemcpyHostToDevice,
+                                  g->ctx->stream);
+  if (e != cudaSuccess) return cuda_err(e, "host-to-device copy");
+  *out = dst;
+  return DEFT_OK;
+}
+
+int sync(deft_ctx *c) {
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  return e == cudaSuccess ? DEFT_OK : cuda_err(e, "stream");
+}
+
+int set_field(deft_fmt *f, double **slot, const double *src, int on_device) {
+  if (!src) {
+    cudaFree(*slot);
+    *slot = nullptr;
+    return DEFT_OK;
+  }
+  cudaSetDevice(f->grid->ctx->device);
+  if (!*slot) {
+    cudaError_t e = cudaMalloc((void **)slot, sizeof(double) * nr(f->grid));
+    if (e != cudaSuccess) return cuda_err(e, "cudaMalloc");
+  }
+  cudaError_t e = cudaMemcpyAsync(*slot, src, sizeof(double) * nr(f->grid),
+                                  on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                                  f->grid->ctx->stream);
+  if (e != cudaSuccess) return cuda_err(e, "field copy");
+  return sync(f->grid->ctx);
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *deft_strerror(int s) {
+  switch (s) {
+    case DEFT_OK: return "ok";
+    case DEFT_ERR_ARG: return "invalid argument";
+    case DEFT_ERR_CUDA: return "CUDA error";
+    case DEFT_ERR_NAN: return "energy or gradient is not finite";
+    case DEFT_ERR_LINESEARCH: return "line search failed";
+    case DEFT_ERR_MAXITER: return "iteration limit reached";
+    case DEFT_ERR_NOMEM: return "out of device memory";
+    default: return "unknown status";
+  }
+}
+
+const char *deft_last_error(void) { return g_err.c_str(); }
+
+int deft_ctx_create(int device, deft_ctx **out) {
+  if (!out) return set_err(DEFT_ERR_ARG, "out is NULL");
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess) return cuda_err(e, "cudaGetDeviceCount");
+  if (device < 0 || device >= n) return set_err(DEFT_ERR_ARG, "no such device");
+  e = cudaSetDevice(device);
+  if (e != cudaSuccess) return cuda_err(e, "cudaSetDevice");
+  deft_ctx *c = new deft_ctx();
+  c->device = device;
+  e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete c;
+    return cuda_err(e, "cudaStreamCreate");
+  }
+  *out = c;
+  return DEFT_OK;
+}
+
+int deft_ctx_destroy(deft_ctx *c) {
+  if (!c) return DEFT_OK;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  cudaStreamDestroy(c->stream);
+  delete c;
+  return DEFT_OK;
+}
+
+int deft_ctx_sync(deft_ctx *c) { return c ? sync(c) : set_err(DEFT_ERR_ARG, "ctx is NULL"); }
+
+void *deft_ctx_stream(deft_ctx *c) { return c ? (void *)c->stream : nullptr; }
+
+int deft_grid_create(deft_ctx *c, const double lat[9], int Nx, int Ny, int Nz, deft_grid **out) {
+  if (!c || !lat || !out) return set_err(DEFT_ERR_ARG, "NULL argument");
+  if (Nx < 1 || Ny < 1 || Nz < 1) return set_err(DEFT_ERR_ARG, "grid sizes must be positive");
+  cudaSetDevice(c->device);
+  deft::GridSpec s;
+  s.Nx = Nx;
+  s.Ny = Ny;
+  s.Nz = Nz;
+  memcpy(s.lat, lat, sizeof(s.lat));
+  std::string err;
+  Engine *eng = Engine::create(s, c->stream, &err);
+  if (!eng) return set_err(DEFT_ERR_ARG, err);
+  deft_grid *g = new deft_grid();
+  g->ctx = c;
+  g->spec = s;
+  g->eng = eng;
+  const deft::Geom &ge = eng->geom();
+  cudaError_t e = cudaMalloc((void **)&g->in_buf, sizeof(double) * ge.NR);
+  if (e == cudaSuccess) e = cudaMalloc((void **)&g->out_buf, sizeof(double) * ge.NR);
+  if (e == cudaSuccess) e = cudaMalloc((void **)&g->c_buf, sizeof(double2) * ge.NC);
+  if (e != cudaSuccess) {
+    deft_grid_destroy(g);
+    return cuda_err(e, "cudaMalloc");
+  }
+  *out = g;
+  return DEFT_OK;
+}
+
+int deft_grid_create_dx(deft_ctx *c, const double lat[9], double dx, deft_grid **out) {
+  if (!lat || !(dx > 0)) return set_err(DEFT_ERR_ARG, "bad lattice or dx");
+  int N[3];
+  for (int i = 0; i < 3; i++) {
+    const double L = std::sqrt(lat[3 * i] * lat[3 * i] + lat[3 * i + 1] * lat[3 * i + 1] +
+                               lat[3 * i + 2] * lat[3 * i + 2]);
+    N[i] = 1 + int(std::exp(1.0) / 100 + L / dx);
+  }
+  return deft_grid_create(c, lat, N[0], N[1], N[2], out);
+}
+
+int deft_grid_destroy(deft_grid *g) {
+  if (!g) return DEFT_OK;
+  cudaSetDevice(g->ctx->device);
+  cudaStreamSynchronize(g->ctx->stream);
+  cudaFree(g->in_buf);
+  cudaFree(g->out_buf);
+  cudaFree(g->c_buf);
+  delete g->eng;
+  delete g;
+  return DEFT_OK;
+}
+
+int deft_grid_info(const deft_grid *g, int N[3], double *dV, double *volume, double *scratch) {
+  if (!g) return set_err(DEFT_ERR_ARG, "grid is NULL");
+  const deft::Geom &ge = g->eng->geom();
+  if (N) {
+    N[0] = ge.Nx;
+    N[1] = ge.Ny;
+    N[2] = ge.Nz;
+  }
+  if (dV) *dV = ge.dV;
+  if (volume) *volume = ge.vol;
+  if (scratch)
+    *scratch = (double)g->eng->scratch_bytes() + sizeof(double) * 2.0 * ge.NR +
+               sizeof(double2) * (double)ge.NC;
+  return DEFT_OK;
+}
+
+int deft_grid_fft(deft_grid *g, const double *in, double *out, int on_device) {
+  if (!g || !in || !out) return set_err(DEFT_ERR_ARG, "NULL argument");
+  cudaSetDevice(g->ctx->device);
+  const double *src;
+  int s = stage_in(g, in, on_device, g->in_buf, &src);
+  if (s) return s;
+  double2 *dst = on_device ? (double2 *)out : g->c_buf;
+  if (g->eng->fft(src, dst)) return eng_err(g->eng);
+  if (!on_device) {
+    cudaError_t e = cudaMemcpyAsync(out, dst, sizeof(double2) * g->eng->geom().NC,
+                                    cudaMemcpyDeviceToHost, g->ctx->stream);
+    if (e != cudaSuccess) return cuda_err(e, "device-to-host copy");
+  }
+  return sync(g->ctx);
+}
+
+int deft_grid_ifft(deft_grid *g, const double *in, double *out, int on_device) {
+  if (!g || !in || !out) return set_err(DEFT_ERR_ARG, "NULL argument");
+  cudaSetDevice(g->ctx->device);
+  const double2 *src = (const double2 *)in;
+  if (!on_device) {
+    cudaError_t e = cudaMemcpyAsync(g->c_buf, in, sizeof(double2) * g->eng->geom().NC,
+                                    cudaMemcpyHostToDevice, g->ctx->stream);
+    if (e != cudaSuccess) return cuda_err(e, "host-to-device copy");
+    src = g->c_buf;
+  }
+  double *dst = on_device ? out : g->out_buf;
+  if (g->eng->ifft(src, dst)) return eng_err(g->eng);
+  if (!on_device) {
+    cudaError_t e = cudaMemcpyAsync(out, dst, sizeof(double) * nr(g), cudaMemcpyDeviceToHost,
+                                    g->ctx->stream);
+    if (e != cudaSuccess) return cuda_err(e, "device-to-host copy");
+  }
+  return sync(g->ctx);
+}
+
+int deft_fmt_create(deft_grid *g, const deft_fmt_params *p, deft_fmt **out) {
+  if (!g || !p || !out) return set_err(DEFT_ERR_ARG, "NULL argument");
+  if (!(p->R > 0) || !(p->kT > 0)) return set_err(DEFT_ERR_ARG, "R and kT must be positive");
+  cudaSetDevice(g->ctx->device);
+  deft_fmt *f = new deft_fmt();
+  f->grid = g;
+  f->p = *p;
+  cudaError_t e = cudaMalloc((void **)&f->g_buf, sizeof(double) * nr(g));
+  if (e != cudaSuccess) {
+    delete f;
+    return cuda_err(e, "cudaMalloc");
+  }
+  *out = f;
+  return DEFT_OK;
+}
+
+int deft_fmt_destroy(deft_fmt *f) {
+  if (!f) return DEFT_OK;
+  cudaSetDevice(f->grid->ctx->device);
+  cudaStreamSynchronize(f->grid->ctx->stream);
+  cudaFree(f->V);
+  cudaFree(f->mask);
+  cudaFree(f->g_buf);
+  cudaFree(f->w_buf);
+  delete f;
+  return DEFT_OK;
+}
+
+int deft_fmt_set_params(deft_fmt *f, const deft_fmt_params *p) {
+  if (!f || !p) return set_err(DEFT_ERR_ARG, "NULL argument");
+  if (!(p->R > 0) || !(p->kT > 0)) return set_err(DEFT_ERR_ARG, "R and kT must be positive");
+  f->p = *p;
+  return DEFT_OK;
+}
+
+int deft_fmt_set_vext(deft_fmt *f, const double *V, int on_device) {
+  if (!f) return set_err(DEFT_ERR_ARG, "fmt is NULL");
+  return set_field(f, &f->V, V, on_device);
+}
+
+int deft_fmt_set_mask(deft_fmt *f, const double *mask, int on_device) {
+  if (!f) return set_err(DEFT_ERR_ARG, "fmt is NULL");
+  return set_field(f, &f->mask, mask, on_device);
+}
+
+static int check_terms(const deft_fmt *f) {
+  if ((f->p.terms & DEFT_TERM_VEXT) && !f->V)
+    return set_err(DEFT_ERR_ARG, "DEFT_TERM_VEXT set but no external potential given");
+  if ((f->p.terms & DEFT_TERM_MASK) && !f->mask)
+    return set_err(DEFT_ERR_ARG, "DEFT_TERM_MASK set but no mask given");
+  return DEFT_OK;
+}
+
+int deft_fmt_energy(deft_fmt *f, const double *n, int on_device, double *E, double *terms) {
+  if (!f || !n || !E) return set_err(DEFT_ERR_ARG, "NULL argument");
+  if (int s = check_terms(f)) return s;
+  deft_grid *g = f->grid;
+  cudaSetDevice(g->ctx->device);
+  const double *src;
+  if (int s = stage_in(g, n, on_device, g->in_buf, &src)) return s;
+  if (g->eng->energy(spec_of(f), src, f->V, f->mask, E, terms)) return eng_err(g->eng);
+  if (!std::isfinite(*E)) return set_err(DEFT_ERR_NAN, "energy is not finite");
+  return DEFT_OK;
+}
+
+int deft_fmt_energy_grad(deft_fmt *f, const double *n, int on_device, double *E, double *grad,
+                         double *terms) {
+  if (!f || !n || !E || !grad) return set_err(DEFT_ERR_ARG, "NULL argument");
+  if (int s = check_terms(f)) return s;
+  deft_grid *g = f->grid;
+  cudaSetDevice(g->ctx->device);
+  const double *src;
+  if (int s = stage_in(g, n, on_device, g->in_buf, &src)) return s;
+  double *dst = on_device ? grad : f->g_buf;
+  if (g->eng->energy_grad(spec_of(f), src, f->V, f->mask, dst, E, terms)) return eng_err(g->eng);
+  if (!on_device) {
+    cudaError_t e = cudaMemcpyAsync(grad, dst, sizeof(double) * nr(g), cudaMemcpyDeviceToHost,
+                                    g->ctx->stream);
+    if (e != cudaSuccess) return cuda_err(e, "device-to-host copy");
+    if (int s = sync(g->ctx)) return s;
+  }
+  if (!std::isfinite(*E)) return set_err(DEFT_ERR_NAN, "energy is not finite");
+  return DEFT_OK;
+}
+
+int deft_fmt_weighted(deft_fmt *f, const double *n, int on_device, double *out5) {
+  if (!f || !n || !out5) return set_err(DEFT_ERR_ARG, "NULL argument");
+  deft_grid *g = f->grid;
+  cudaSetDevice(g->ctx->device);
+  const double *src;
+  if (int s = stage_in(g, n, on_device, g->in_buf, &src)) return s;
+  double *dst = out5;
+  if (!on_device) {
+    if (!f->w_buf) {
+      cudaError_t e = cudaMalloc((void **)&f->w_buf, 5 * sizeof(double) * nr(g));
+      if (e != cudaSuccess) return cuda_err(e, "cudaMalloc");
+    }
+    dst = f->w_buf;
+  }
+  if (g->eng->weighted(spec_of(f), src, dst)) return eng_err(g->eng);
+  if (!on_device) {
+    cudaError_t e = cudaMemcpyAsync(out5, dst, 5 * sizeof(double) * nr(g), cudaMemcpyDeviceToHost,
+                                    g->ctx->stream);
+    if (e != cudaSuccess) return cuda_err(e, "device-to-host copy");
+  }
+  return sync(g->ctx);
+}
+
+int deft_find_chemical_potential(double R, double kT, double nb, double *mu_out) {
+  if (!mu_out || !(R > 0) || !(kT > 0) || !(nb > 0))
+    return set_err(DEFT_ERR_ARG, "R, kT and nb must be positive");
+  // Homogeneous limit: n3 = nb 4/3 pi R^3, n2 = nb 4 pi R^2, vector shells 0
+  // (ConvolveWith::derive is w(0), src/Functional.h:390-392).
+  const double n3 = nb * (4 * M_PI / 3) * R * R * R, n2 = nb * 4 * M_PI * R * R;
+  const double omn3 = 1 - n3, l = std::log(omn3);
+  const double fpr = 4 * M_PI * R, fpr2 = 4 * M_PI * R * R;
+  double S, dS;
+  if (std::fabs(n3) < 1e-2) {
+    S = 1.5;
+    dS = 0;
+    double pw = 1;
+    for (int j = 1; j <= 12; j++) {
+      const double c = 2.0 / ((double)j * (j + 1) * (j + 2));
+      dS -= c * j * pw;
+      pw *= n3;
+      S -= c * pw;
+    }
+  } else {
+    const double gg = n3 + omn3 * omn3 * l, dg = n3 - 2 * omn3 * l;
+    S = gg / (n3 * n3);
+    dS = (dg * n3 - 2 * gg) / (n3 * n3 * n3);
+  }
+  const double f3 = S / (36 * M_PI * omn3 * omn3);
+  const double df3 = (dS * omn3 + 2 * S) / (36 * M_PI * omn3 * omn3 * omn3);
+  const double d3 = n2 / (fpr2 * omn3) + n2 * n2 / (fpr * omn3 * omn3) + df3 * n2 * n2 * n2;
+  const double d2 = -l / fpr2 + 2 * n2 / (fpr * omn3) + f3 * 3 * n2 * n2;
+  const double x = 18.01528 * 1822.8885 * kT / (2 * M_PI);
+  const double nQ = x * std::sqrt(x);
+  const double dfdn = kT * (d3 * (4 * M_PI / 3) * R * R * R + d2 * 4 * M_PI * R * R) +
+                      kT * std::log(nb / nQ);
+  *mu_out = -dfdn;
+  return DEFT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Minimiser
+
+int deft_cg_create(deft_fmt *f, const deft_cg_params *p, deft_cg **out) {
+  if (!f || !p || !out) return set_err(DEFT_ERR_ARG, "NULL argument");
+  if (p->linesearch != DEFT_LS_SECANT && p->linesearch != DEFT_LS_QUADRATIC_REF)
+    return set_err(DEFT_ERR_ARG, "unknown line search");
+  cudaSetDevice(f->grid->ctx->device);
+  deft_cg *c = new deft_cg();
+  c->f = f;
+  c->p = *p;
+  c->step = p->step;
+  c->alpha = p->step;
+  c->err_est = std::fmax(1.0, 2 * p->precision);
+  const size_t bytes = sizeof(double) * nr(f->grid);
+  cudaError_t e = cudaMalloc((void **)&c->x, bytes);
+  if (e == cudaSuccess) e = cudaMalloc((void **)&c->g, bytes);
+  if (e == cudaSuccess) e = cudaMalloc((void **)&c->d, bytes);
+  if (e == cudaSuccess) e = cudaMalloc((void **)&c->gold, bytes);
+  if (e == cudaSuccess) e = cudaMemsetAsync(c->d, 0, bytes, f->grid->ctx->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(c->gold, 0, bytes, f->grid->ctx->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(c->x, 0, bytes, f->grid->ctx->stream);
+  if (e != cudaSuccess) {
+    deft_cg_destroy(c);
+    return cuda_err(e, "cudaMalloc");
+  }
+  *out = c;
+  return sync(f->grid->ctx);
+}
+
+int deft_cg_destroy(deft_cg *c) {
+  if (!c) return DEFT_OK;
+  cudaSetDevice(c->f->grid->ctx->device);
+  cudaStreamSynchronize(c->f->grid->ctx->stream);
+  cudaFree(c->x);
+  cudaFree(c->g);
+  cudaFree(c->d);
+  cudaFree(c->gold);
+  delete c;
+  return DEFT_OK;
+}
+
+static void cg_reset(deft_cg *c) {
+  c->iter = 0;
+  c->evals = 0;
+  c->have_g = false;
+  c->e_valid = false;
+  c->goldsqr = 0;
+  c->oldgradsqr = 0;
+  c->s_prev = 0;
+  c->alpha = c->p.step;
+  c->step = c->p.step;
+  c->done = false;
+  c->dEdn = 0;
+  c->log_ratio_avg = 0;
+  c->deltaE = 0;
+  c->err_est = std::fmax(1.0, 2 * c->p.precision);
+  const size_t bytes = sizeof(double) * nr(c->f->grid);
+  cudaMemsetAsync(c->d, 0, bytes, c->f->grid->ctx->stream);
+  cudaMemsetAsync(c->gold, 0, bytes, c->f->grid->ctx->stream);
+}
+
+int deft_cg_set_x(deft_cg *c, const double *n, int on_device) {
+  if (!c || !n) return set_err(DEFT_ERR_ARG, "NULL argument");
+  deft_grid *g = c->f->grid;
+  cudaSetDevice(g->ctx->device);
+  cudaError_t e = cudaMemcpyAsync(c->x, n, sizeof(double) * nr(g),
+                                  on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                                  g->ctx->stream);
+  if (e != cudaSuccess) return cuda_err(e, "copy");
+  cg_reset(c);
+  return sync(g->ctx);
+}
+
+int deft_cg_get_x(deft_cg *c, double *n, int on_device) {
+  if (!c || !n) return set_err(DEFT_ERR_ARG, "NULL argument");
+  deft_grid *g = c->f->grid;
+  cudaSetDevice(g->ctx->device);
+  cudaError_t e = cudaMemcpyAsync(n, c->x, sizeof(double) * nr(g),
+                                  on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                                  g->ctx->stream);
+  if (e != cudaSuccess) return cuda_err(e, "copy");
+  return sync(g->ctx);
+}
+
+double *deft_cg_x_device(deft_cg *c) { return c ? c->x : nullptr; }
+
+namespace {
+
+Engine *eng_of(deft_cg *c) { return c->f->grid->eng; }
+
+// Energy + gradient at x into c->g, c->E.
+int cg_eval(deft_cg *c) {
+  double E;
+  if (eng_of(c)->energy_grad(spec_of(c->f), c->x, c->f->V, c->f->mask, c->g, &E, nullptr))
+    return eng_err(eng_of(c));
+  c->evals++;
+  c->E = E;
+  c->e_cache = E;
+  c->e_valid = true;
+  c->have_g = true;
+  return DEFT_OK;
+}
+
+// Minimizer::energy() (src/Minimizer.h:52), cached while x is unchanged.
+int cg_energy(deft_cg *c, double *E) {
+  if (!c->e_valid) {
+    if (eng_of(c)->energy(spec_of(c->f), c->x, c->f->V, c->f->mask, &c->e_cache, nullptr))
+      return eng_err(eng_of(c));
+    c->evals++;
+    c->e_valid = true;
+  }
+  *E = c->e_cache;
+  return DEFT_OK;
+}
+
+int cg_axpy(deft_cg *c, double a, const double *v) {
+  if (eng_of(c)->axpy(a, v, c->x)) return eng_err(eng_of(c));
+  c->e_valid = false;
+  c->have_g = false;
+  return DEFT_OK;
+}
+
+int dots3(deft_cg *c, double *s, double *gg, double *ggold) {
+  const double *a[3] = {c->g, c->g, c->g};
+  const double *b[3] = {c->d, c->g, c->gold};
+  double o[3];
+  if (eng_of(c)->dots(3, a, b, o)) return eng_err(eng_of(c));
+  *s = o[0];
+  *gg = o[1];
+  *ggold = o[2];
+  return DEFT_OK;
+}
+
+// Bracketing secant search on s(a) = grad(x + a d).d from s(0) = s0 < 0,
+// accepting |s| <= 0.1 |s0| with no energy rise beyond rounding.  Leaves x,
+// g, E, gg, ggold at the accepted point.
+int secant_search(deft_cg *c, double E0, double s0) {
+  double lo = 0, s_lo = s0, hi = -1, s_hi = 0, plo = 0, s_plo = s0;
+  double a = c->alpha, at = 0;
+  const double etol = 1e-12 * std::fabs(E0);
+  for (int it = 0; it < 40; it++) {
+    if (int st = cg_axpy(c, a - at, c->d)) return st;
+    at = a;
+    if (int st = cg_eval(c)) return st;
+    double s, gg, ggold;
+    if (int st = dots3(c, &s, &gg, &ggold)) return st;
+    const double E = c->E;
+    if (!std::isfinite(E) || !std::isfinite(s)) {
+      hi = a;
+      s_hi = 1e300;
+      a = lo + 0.5 * (a - lo);
+      continue;
+    }
+    if (std::fabs(s) <= 0.1 * std::fabs(s0) && E <= E0 + etol) {
+      c->alpha = a;
+      c->gg = gg;
+      c->ggold = ggold;
+      return DEFT_OK;
+    }
+    if (s < 0 && E <= E0 + etol) {
+      plo = lo;
+      s_plo = s_lo;
+      lo = a;
+      s_lo = s;
+      if (hi < 0) {
+        double an = 4 * a;
+        if (s - s_plo > 0) {
+          an = a - s * (a - plo) / (s - s_plo);
+          an = std::fmin(std::fmax(an, 1.5 * a), 4 * a);
+        }
+        a = an;
+        continue;
+      }
+    } else {
+      hi = a;
+      s_hi = s > 0 ? s : 1e300;
+    }
+    double an = 0.5 * (lo + hi);
+    if (s_hi < 1e299 && s_hi - s_lo > 0) an = lo - s_lo * (hi - lo) / (s_hi - s_lo);
+    const double w = hi - lo;
+    an = std::fmin(std::fmax(an, lo + 0.01 * w), hi - 0.01 * w);
+    a = an;
+  }
+  // return to the start point
+  cg_axpy(c, -at, c->d);
+  return set_err(DEFT_ERR_LINESEARCH, "secant line search did not converge in 40 evaluations");
+}
+
+int step_secant(deft_cg *c, deft_cg_status *st) {
+  if (!c->have_g) {
+    if (int s = cg_eval(c)) return s;
+    const double *a[2] = {c->g, c->g};
+    const double *b[2] = {c->g, c->gold};
+    double o[2];
+    if (eng_of(c)->dots(2, a, b, o)) return eng_err(eng_of(c));
+    c->gg = o[0];
+    c->ggold = o[1];
+  }
+  if (!std::isfinite(c->E) || !std::isfinite(c->gg))
+    return set_err(DEFT_ERR_NAN, "energy or gradient is not finite");
+  st->gnorm = std::sqrt(c->gg);
+  if (st->gnorm < c->p.gtol) {
+    c->done = true;
+    return DEFT_OK;
+  }
+  // Polak-Ribiere with reset (src/ConjugateGradient.cpp:77-91)
+  double beta = 0;
+  if (c->goldsqr > 0) {
+    beta = (c->gg - c->ggold) / c->goldsqr;
+    if (beta < 0 || beta != beta) beta = 0;
+  }
+  Engine *e = eng_of(c);
+  if (e->scal_add(beta, c->d, -1.0, c->g)) return eng_err(e);
+  double s0;
+  {
+    const double *a[1] = {c->g};
+    const double *b[1] = {c->d};
+    if (e->dots(1, a, b, &s0)) return eng_err(e);
+  }
+  if (!(s0 < 0)) {
+    if (e->scal_add(0.0, c->d, -1.0, c->g)) return eng_err(e);
+    s0 = -c->gg;
+  }
+  if (e->copy(c->g, c->gold)) return eng_err(e);
+  c->goldsqr = c->gg;
+  if (c->iter > 0 && s0 != 0) c->alpha *= c->s_prev / s0;
+  c->s_prev = s0;
+  c->iter++;
+  if (int s = secant_search(c, c->E, s0)) return s;
+  st->gnorm = std::sqrt(c->gg);
+  if (st->gnorm < c->p.gtol) c->done = true;
+  return DEFT_OK;
+}
+
+bool better(double a, double b) { return a < b || (b != b); }  // src/Minimizer.h:161-163
+
+// QuadraticLineMinimizerType::improve_energy, src/QuadraticLineMinimizer.cpp:27-198.
+int quad_linmin(deft_cg *c, double slope, double *step) {
+  double E0, Ex;
+  if (int s = cg_energy(c, &E0)) return s;
+  if (E0 != E0 || E0 > 1e307 || E0 < -1e307 || slope != slope || slope == 0) return DEFT_OK;
+  if (slope * (*step) > 0) *step *= -1;
+  double step1 = *step;
+  if (int s = cg_axpy(c, step1, c->d)) return s;
+  double Etried = -137;
+  for (int guard = 0;; guard++) {
+    if (guard > 1200) return set_err(DEFT_ERR_LINESEARCH, "quadratic line search: no step found");
+    step1 *= 0.5;
+    if (int s = cg_axpy(c, -step1, c->d)) return s;
+    if (int s = cg_energy(c, &Ex)) return s;
+    if (Ex == Etried) break;
+    Etried = Ex;
+    if (!better(E0, Ex)) break;
+  }
+  double E1;
+  if (int s = cg_energy(c, &E1)) return s;
+  const double curvature = 2.0 * (E1 - E0 - step1 * slope) / (step1 * step1);
+  const double step2 = -slope / curvature;
+  if (curvature <= 0.0) {
+    if (better(E0, E1)) return cg_axpy(c, -step1, c->d);
+    double Ebest = E0;
+    for (int guard = 0; guard < 2000; guard++) {
+      if (int s = cg_energy(c, &Ex)) return s;
+      if (!(Ex <= Ebest)) break;
+      Ebest = Ex;
+      if (int s = cg_axpy(c, step1, c->d)) return s;
+      step1 *= 2;
+    }
+    step1 *= 0.5;
+    if (int s = cg_axpy(c, -step1, c->d)) return s;
+    *step = step1;
+  } else if (E1 == E0) {
+    for (int guard = 0; guard < 2000; guard++) {
+      if (int s = cg_axpy(c, -step1, c->d)) return s;
+      step1 *= 2;
+      if (int s = cg_axpy(c, step1, c->d)) return s;
+      if (int s = cg_energy(c, &Ex)) return s;
+      if (Ex != E0) break;
+    }
+    if (int s = cg_energy(c, &Ex)) return s;
+    if (Ex > E0 || Ex != Ex) {
+      if (int s = cg_axpy(c, -step1, c->d)) return s;
+    }
+  } else {
+    *step = step2;
+    if (int s = cg_axpy(c, step2 - step1, c->d)) return s;
+    if (int s = cg_energy(c, &Ex)) return s;
+    if (better(E1, Ex) && better(E1, E0)) {
+      if (int s = cg_axpy(c, -(step2 - step1), c->d)) return s;
+    } else if (Ex > E0) {
+      if (int s = cg_axpy(c, -step2, c->d)) return s;
+    }
+  }
+  return DEFT_OK;
+}
+
+// ConjugateGradientType::improve_energy, src/ConjugateGradient.cpp:59-108.
+// Sets *more to its return value.
+int step_quadratic(deft_cg *c, bool *more) {
+  c->iter++;
+  // energy() then grad() at the same x: one fused evaluation gives both
+  if (!c->have_g)
+    if (int s = cg_eval(c)) return s;
+  const double E0 = c->E;
+  if (E0 != E0) {
+    *more = false;
+    return DEFT_OK;
+  }
+  Engine *e = eng_of(c);
+  // g = -grad; beta = g.(g - oldgrad)/oldgradsqr, with oldgrad stored as -grad
+  double o[2];
+  {
+    const double *a[2] = {c->g, c->g};
+    const double *b[2] = {c->g, c->gold};
+    if (e->dots(2, a, b, o)) return eng_err(e);
+  }
+  // with G = grad: g.g = G.G and g.oldgrad = -G.gold (gold holds oldgrad)
+  c->gg = o[0];
+  double beta = (o[0] + o[1]) / c->oldgradsqr;
+  if (e->scal_add(0.0, c->gold, -1.0, c->g)) return eng_err(e);  // oldgrad = -grad
+  if (beta < 0 || beta != beta || c->oldgradsqr == 0) beta = 0;
+  c->oldgradsqr = o[0];
+  if (e->scal_add(beta, c->d, 1.0, c->gold)) return eng_err(e);  // direction = g + beta dir
+  double gdotd;
+  {
+    const double *a[1] = {c->gold};
+    const double *b[1] = {c->d};
+    if (e->dots(1, a, b, &gdotd)) return eng_err(e);
+  }
+  if (gdotd < 0) {
+    if (e->copy(c->gold, c->d)) return eng_err(e);
+    gdotd = c->oldgradsqr;
+  }
+  if (int s = quad_linmin(c, -gdotd, &c->step)) return s;
+  double E;
+  if (int s = cg_energy(c, &E)) return s;
+  *more = E < E0;
+  return DEFT_OK;
+}
+
+}  // namespace
+
+int deft_cg_step(deft_cg *c, deft_cg_status *st) {
+  if (!c || !st) return set_err(DEFT_ERR_ARG, "NULL argument");
+  cudaSetDevice(c->f->grid->ctx->device);
+  if (int s = check_terms(c->f)) return s;
+  st->converged = 0;
+  st->status = DEFT_OK;
+  st->gnorm = 0;
+  int status = DEFT_OK;
+  if (!c->done) {
+    // Precision modifier bookkeeping (src/Precision.cpp:53-151)
+    double old_energy = 0;
+    const bool prec = c->p.precision > 0;
+    if (prec) status = cg_energy(c, &old_energy);
+    bool more = true;
+    if (!status) {
+      if (c->p.linesearch == DEFT_LS_SECANT) {
+        status = step_secant(c, st);
+        more = !c->done;
+      } else {
+        status = step_quadratic(c, &more);
+      }
+    }
+    if (!status && prec) {
+      double new_energy;
+      status = cg_energy(c, &new_energy);
+      if (!status) {
+        const double old_deltaE = c->deltaE;
+        c->deltaE = old_energy - new_energy;
+        c->dEdn = std::fmax(c->deltaE, old_deltaE);
+        const double w = 0.1;
+        const double nl = (c->deltaE && old_deltaE) ? std::log(std::fabs(c->deltaE / old_deltaE)) : 0;
+        c->log_ratio_avg = (1 - w) * c->log_ratio_avg + w * nl;
+        const double ratio = std::exp(c->log_ratio_avg);
+        double guess = std::fabs(std::fmax(c->dEdn, c->deltaE) / c->log_ratio_avg);
+        if (ratio >= 1) guess = c->p.precision + std::fabs(new_energy);
+        c->err_est = 2 * guess;
+        if (c->deltaE == 0 && old_deltaE == 0) more = false;
+        else if (!(more && !(c->err_est < c->p.precision))) more = false;
+      }
+    }
+    if (!status && !more) c->done = true;
+    if (!status && c->p.maxiter > 0 && c->iter >= c->p.maxiter && !c->done)
+      status = set_err(DEFT_ERR_MAXITER, "CG iteration limit reached");
+  }
+  double E = c->e_cache;
+  if (!c->e_valid && !status) status = cg_energy(c, &E);
+  st->iter = c->iter;
+  st->evals = c->evals;
+  st->energy = E;
+  if (st->gnorm == 0 && c->have_g) st->gnorm = std::sqrt(c->gg);
+  st->converged = c->done ? 1 : 0;
+  st->status = status;
+  return status;
+}
+
+int deft_cg_solve(deft_cg *c, deft_cg_status *st) {
+  if (!c || !st) return set_err(DEFT_ERR_ARG, "NULL argument");
+  for (;;) {
+    int s = deft_cg_step(c, st);
+    if (s) return s;
+    if (st->converged) return DEFT_OK;
+  }
+}
+
+}  // extern "C"

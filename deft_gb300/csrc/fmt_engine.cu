@@ -1,0 +1,997 @@
+// sm_103a kernels for deft's FMT hot path (FP64 form).
+//
+// One energy + gradient evaluation is nine launches over HBM-resident data:
+//   z_r2c      n -> half-complex along z (two real lines per complex FFT)
+//   y_fft(-1)  along y, tiles of contiguous kz columns
+//   x_conv_fwd along x, then x (weights w3, w2, i k_c wv) and inverse x for
+//              the five weighted densities (ConvolveWith::transform,
+//              src/Functional.h:376-381, for Step/Shell/x,y,zShell)
+//   y_fft(+1)  five fields
+//   z_phi      c2r of the five fields, White Bear phi + partials + ideal gas,
+//              mu and V_ext terms, per-block FP64 energy partials, then r2c
+//              of the five partials (src/HardSpheres.cpp:137-159 and the
+//              reverse-mode tree of src/Functional.cpp:439-633, fused)
+//   y_fft(-1)  five fields
+//   x_conv_adj along x, times the adjoint weights (odd ones negated,
+//              src/Functional.h:407-417), summed, inverse x
+//   y_fft(+1)  one field
+//   z_grad     c2r, + dV (kT ln(n/nQ) + mu + V), times mask
+//              (src/Functional.cpp:809-824)
+// The k-space weights (src/ReciprocalOperators.h:94-235) are evaluated
+// analytically once per (grid, R) into a table, with the convolution
+// normalisation dV/V folded in.
+#include "fft_smem.cuh"
+#include "fmt_engine.h"
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+namespace deft {
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr size_t kSmemBudget = 96 * 1024;
+
+// ---------------------------------------------------------------------------
+// Device helpers
+
+__device__ __forceinline__ int wrapm(int i, int N) { return i > N / 2 ? i - N : i; }
+
+__device__ __forceinline__ double kcomp(const Geom &g, int c, int x, int y, int z) {
+  return g.Bm[3 * c] * wrapm(x, g.Nx) + g.Bm[3 * c + 1] * wrapm(y, g.Ny) + g.Bm[3 * c + 2] * z;
+}
+
+// Analytic weights at |k| (src/ReciprocalOperators.h:94-142,162-235):
+// step w3, shell w2, and the radial factor wv of the vector shells, whose
+// weight is i k_c wv.
+__device__ void weights_at(double k2, double R, double dr, double &w3, double &w2, double &wv) {
+  const double kk = sqrt(k2);
+  const double kR = kk * R;
+  if (kR > 1e-3) {
+    const double kdr = kk * dr;
+    double s, c;
+    sincos(kR, &s, &c);
+    const double smear = exp(-6.0 * kdr * kdr);
+    w3 = smear * (4 * M_PI) * (s - kR * c) / (kk * kk * kk);
+    w2 = smear * (4 * M_PI) * R * s / kk;
+    wv = smear * (4 * M_PI) / (kk * kk) * (R * c - s / kk);
+  } else {
+    const double kR2 = kR * kR;
+    w3 = (4 * M_PI / 3) * R * R * R *
+         (kR2 * kR2 * kR2 * (-1.0 / 15120) + kR2 * kR2 * (1.0 / 280) + kR2 * (-1.0 / 10) + 1);
+    w2 = (4 * M_PI) * (R * R) *
+         (-kR2 * kR2 * kR2 * (1.0 / 120 / 6 / 7) + kR2 * kR2 * (1.0 / 120) - kR2 * (1.0 / 6) + 1);
+    wv = (4 * M_PI) * R * R * R *
+         (kR2 * kR2 * (1.0 / 5040 - 1.0 / 720) + kR2 * (1.0 / 24 - 1.0 / 120) - 1.0 / 3);
+  }
+}
+
+// S(eta) = (eta + (1-eta)^2 ln(1-eta)) / eta^2 and dS/deta; the phi3
+// prefactor of src/HardSpheres.cpp:153 is S / (36 pi (1-eta)^2).  The direct
+// form is 0/0 at eta -> 0, so |eta| < 1e-2 uses its Taylor series
+// S = 3/2 - sum_{j>=1} 2 eta^j / (j (j+1) (j+2)).
+__device__ __forceinline__ void phi3_S(double eta, double &S, double &dS) {
+  if (fabs(eta) < 1e-2) {
+    double s = 1.5, ds = 0, pw = 1;
+#pragma unroll
+    for (int j = 1; j <= 12; j++) {
+      const double c = 2.0 / ((double)j * (j + 1) * (j + 2));
+      ds -= c * j * pw;
+      pw *= eta;
+      s -= c * pw;
+    }
+    S = s;
+    dS = ds;
+  } else {
+    const double l = log(1 - eta);
+    const double gg = eta + (1 - eta) * (1 - eta) * l;
+    const double dg = eta - 2 * (1 - eta) * l;
+    S = gg / (eta * eta);
+    dS = (dg * eta - 2 * gg) / (eta * eta * eta);
+  }
+}
+
+// White Bear (no tensor) phi per kT, split as (phi3, phi1, phi2), and its
+// partials with respect to (n3, n2, n2x, n2y, n2z).
+__device__ __forceinline__ void phi_wb(double R, double n3, double n2, double vx, double vy,
+                                       double vz, double phi[3], double d[5]) {
+  const double v2 = vx * vx + vy * vy + vz * vz;
+  const double omn3 = 1 - n3;
+  const double l = log(omn3);
+  const double four_pi_r = 4 * M_PI * R, four_pi_r2 = 4 * M_PI * R * R;
+  double S, dS;
+  phi3_S(n3, S, dS);
+  const double inv = 1.0 / omn3;
+  const double f3 = S * inv * inv * (1.0 / (36 * M_PI));
+  const double df3 = (dS * omn3 + 2 * S) * inv * inv * inv * (1.0 / (36 * M_PI));
+  const double q = n2 * n2 - v2;
+  const double t3 = n2 * (n2 * n2 - 3 * v2);
+  phi[0] = f3 * t3;
+  phi[1] = -n2 * l / four_pi_r2;
+  phi[2] = q / (four_pi_r * omn3);
+  d[0] = n2 / (four_pi_r2 * omn3) + q / (four_pi_r * omn3 * omn3) + df3 * t3;
+  d[1] = -l / four_pi_r2 + 2 * n2 / (four_pi_r * omn3) + f3 * 3 * q;
+  const double cv = -2 / (four_pi_r * omn3) - 6 * f3 * n2;
+  d[2] = cv * vx;
+  d[3] = cv * vy;
+  d[4] = cv * vz;
+}
+
+// Deterministic block reduction of K doubles; thread 0 gets the sums.
+template <int K>
+__device__ void block_reduce(double (&v)[K], double *smem /* 32*K */) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < K; k++) {
+    double x = v[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    v[k] = x;
+  }
+  if (lane == 0)
+    for (int k = 0; k < K; k++) smem[warp * K + k] = v[k];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const int nw = (blockDim.x + 31) >> 5;
+    for (int k = 0; k < K; k++) {
+      double s = 0;
+      for (int w = 0; w < nw; w++) s += smem[w * K + k];
+      v[k] = s;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Kernels
+
+__global__ void k_weight_table(Geom g, double R, double *w3, double *w2, double *wv) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < g.NC; i += gridDim.x * blockDim.x) {
+    const int z = i % g.NzH;
+    const int t = i / g.NzH;
+    const int y = t % g.Ny;
+    const int x = t / g.Ny;
+    const double kx = kcomp(g, 0, x, y, z), ky = kcomp(g, 1, x, y, z), kz = kcomp(g, 2, x, y, z);
+    double a, b, c;
+    weights_at(kx * kx + ky * ky + kz * kz, R, g.dr, a, b, c);
+    w3[i] = a * g.scale;
+    w2[i] = b * g.scale;
+    wv[i] = c * g.scale;
+  }
+}
+
+// Packs two half-complex z-lines A (line l0) and B (line l0+1) into one
+// complex line Z = A + iB of full length (Hermitian extension); only the real
+// parts of the kz = 0 and Nyquist entries enter, as in a c2r of Hermitian data.
+template <typename T>
+__device__ __forceinline__ void pack_c2r(const typename Cplx<T>::type *__restrict__ in,
+                                         typename Cplx<T>::type *buf, const Geom &g, int p0,
+                                         int P) {
+  using C = typename Cplx<T>::type;
+  const int Nz = g.Nz, NzH = g.NzH;
+  for (int idx = threadIdx.x; idx < P * Nz; idx += blockDim.x) {
+    const int k = idx % Nz, pb = idx / Nz;
+    const int l0 = 2 * (p0 + pb), l1 = l0 + 1;
+    C A = C{0, 0}, B = C{0, 0};
+    if (k < NzH) {
+      if (l0 < g.lines) A = in[(size_t)l0 * NzH + k];
+      if (l1 < g.lines) B = in[(size_t)l1 * NzH + k];
+      if (k == 0 || 2 * k == Nz) {
+        A.y = 0;
+        B.y = 0;
+      }
+    } else {
+      const int kk = Nz - k;
+      if (l0 < g.lines) A = in[(size_t)l0 * NzH + kk];
+      if (l1 < g.lines) B = in[(size_t)l1 * NzH + kk];
+      A.y = -A.y;
+      B.y = -B.y;
+    }
+    buf[k * P + pb] = C{A.x - B.y, A.y + B.x};
+  }
+}
+
+// Unpacks the forward FFT Z of a + ib into the half spectra of a and b and
+// stores them (scaled by s) at lines 2(p0+pb), 2(p0+pb)+1.
+template <typename T>
+__device__ __forceinline__ void unpack_r2c_store(const typename Cplx<T>::type *res,
+                                                 typename Cplx<T>::type *__restrict__ out,
+                                                 const Geom &g, int p0, int P, T s) {
+  using C = typename Cplx<T>::type;
+  const int Nz = g.Nz, NzH = g.NzH;
+  for (int idx = threadIdx.x; idx < 2 * P * NzH; idx += blockDim.x) {
+    const int k = idx % NzH, ll = idx / NzH;
+    const int line = 2 * p0 + ll;
+    if (line >= g.lines) continue;
+    const int pb = ll >> 1;
+    const C zk = res[k * P + pb];
+    const C zm = res[((Nz - k) % Nz) * P + pb];
+    const T h = T(0.5) * s;
+    C o;
+    if ((ll & 1) == 0) o = C{h * (zk.x + zm.x), h * (zk.y - zm.y)};
+    else o = C{h * (zk.y + zm.y), -h * (zk.x - zm.x)};
+    out[(size_t)line * NzH + k] = o;
+  }
+}
+
+// Real fields -> half-complex along z.  grid.x = pair tiles, grid.y = field.
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_z_r2c(const T *__restrict__ in,
+                                                    typename Cplx<T>::type *__restrict__ out,
+                                                    Geom g, FftPlan pz, int P, T s) {
+  using C = typename Cplx<T>::type;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C *buf0 = reinterpret_cast<C *>(smem_raw);
+  C *buf1 = buf0 + g.Nz * P;
+  const int p0 = blockIdx.x * P;
+  in += (size_t)blockIdx.y * g.NR;
+  out += (size_t)blockIdx.y * g.NC;
+  for (int idx = threadIdx.x; idx < 2 * P * g.Nz; idx += blockDim.x) {
+    const int z = idx % g.Nz, ll = idx / g.Nz;
+    const int line = 2 * p0 + ll;
+    const T v = line < g.lines ? in[(size_t)line * g.Nz + z] : T(0);
+    reinterpret_cast<T *>(&buf0[z * P + (ll >> 1)])[ll & 1] = v;
+  }
+  C *res = fft_tile<T, -1>(buf0, buf1, P, pz);
+  unpack_r2c_store<T>(res, out, g, p0, P, s);
+}
+
+// Half-complex along z -> real fields.  grid.x = pair tiles, grid.y = field.
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_z_c2r(const typename Cplx<T>::type *__restrict__ in,
+                                                    T *__restrict__ out, Geom g, FftPlan pz, int P,
+                                                    T s) {
+  using C = typename Cplx<T>::type;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C *buf0 = reinterpret_cast<C *>(smem_raw);
+  C *buf1 = buf0 + g.Nz * P;
+  const int p0 = blockIdx.x * P;
+  in += (size_t)blockIdx.y * g.NC;
+  out += (size_t)blockIdx.y * g.NR;
+  pack_c2r<T>(in, buf0, g, p0, P);
+  C *res = fft_tile<T, +1>(buf0, buf1, P, pz);
+  for (int idx = threadIdx.x; idx < 2 * P * g.Nz; idx += blockDim.x) {
+    const int z = idx % g.Nz, ll = idx / g.Nz;
+    const int line = 2 * p0 + ll;
+    if (line >= g.lines) continue;
+    const C v = res[z * P + (ll >> 1)];
+    out[(size_t)line * g.Nz + z] = ((ll & 1) ? v.y : v.x) * s;
+  }
+}
+
+// FFT along y of complex fields.  grid = (kz tiles, Nx, fields).
+template <typename T, int SIGN>
+__global__ void __launch_bounds__(kThreads) k_y_fft(typename Cplx<T>::type *data, Geom g,
+                                                    FftPlan py, int B) {
+  using C = typename Cplx<T>::type;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C *buf0 = reinterpret_cast<C *>(smem_raw);
+  C *buf1 = buf0 + g.Ny * B;
+  const int kz0 = blockIdx.x * B;
+  C *base = data + (size_t)blockIdx.z * g.NC + (size_t)blockIdx.y * g.Ny * g.NzH;
+  for (int idx = threadIdx.x; idx < g.Ny * B; idx += blockDim.x) {
+    const int e = idx / B, b = idx % B;
+    const int kz = kz0 + b;
+    buf0[idx] = kz < g.NzH ? base[(size_t)e * g.NzH + kz] : C{0, 0};
+  }
+  C *res = fft_tile<T, SIGN>(buf0, buf1, B, py);
+  for (int idx = threadIdx.x; idx < g.Ny * B; idx += blockDim.x) {
+    const int e = idx / B, b = idx % B;
+    const int kz = kz0 + b;
+    if (kz < g.NzH) base[(size_t)e * g.NzH + kz] = res[idx];
+  }
+}
+
+// Plain FFT along x (stride Ny*NzH), optional scale.  grid.x = line tiles.
+template <typename T, int SIGN>
+__global__ void __launch_bounds__(kThreads) k_x_fft(typename Cplx<T>::type *data, Geom g,
+                                                    FftPlan px, int B, T s) {
+  using C = typename Cplx<T>::type;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C *buf0 = reinterpret_cast<C *>(smem_raw);
+  C *buf1 = buf0 + g.Nx * B;
+  const int J = g.Ny * g.NzH;
+  const int j0 = blockIdx.x * B;
+  for (int idx = threadIdx.x; idx < g.Nx * B; idx += blockDim.x) {
+    const int e = idx / B, j = j0 + idx % B;
+    buf0[idx] = j < J ? data[(size_t)e * J + j] : C{0, 0};
+  }
+  C *res = fft_tile<T, SIGN>(buf0, buf1, B, px);
+  for (int idx = threadIdx.x; idx < g.Nx * B; idx += blockDim.x) {
+    const int e = idx / B, j = j0 + idx % B;
+    if (j < J) data[(size_t)e * J + j] = c_scale(res[idx], s);
+  }
+}
+
+// x-FFT of n^, multiplication by the five weights, inverse x-FFT of each.
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_x_conv_fwd(
+    const typename Cplx<T>::type *__restrict__ in, typename Cplx<T>::type *__restrict__ out5,
+    const double *__restrict__ w3, const double *__restrict__ w2, const double *__restrict__ wv,
+    Geom g, FftPlan px, int B) {
+  using C = typename Cplx<T>::type;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C *bufA = reinterpret_cast<C *>(smem_raw);
+  C *bufB = bufA + g.Nx * B;
+  C *bufC = bufB + g.Nx * B;
+  const int J = g.Ny * g.NzH;
+  const int j0 = blockIdx.x * B;
+  for (int idx = threadIdx.x; idx < g.Nx * B; idx += blockDim.x) {
+    const int e = idx / B, j = j0 + idx % B;
+    bufA[idx] = j < J ? in[(size_t)e * J + j] : C{0, 0};
+  }
+  const C *R0 = fft_tile<T, -1>(bufA, bufB, B, px);
+  C *F1 = (R0 == bufA) ? bufB : bufA;
+  C *F2 = bufC;
+  for (int a = 0; a < 5; a++) {
+    for (int idx = threadIdx.x; idx < g.Nx * B; idx += blockDim.x) {
+      const int e = idx / B, j = j0 + idx % B;
+      C o = C{0, 0};
+      if (j < J) {
+        const size_t i = (size_t)e * J + j;
+        const C v = R0[idx];
+        if (a == 0) {
+          const T w = T(w3[i]);
+          o = C{v.x * w, v.y * w};
+        } else if (a == 1) {
+          const T w = T(w2[i]);
+          o = C{v.x * w, v.y * w};
+        } else {
+          const int y = j / g.NzH, z = j % g.NzH;
+          const T w = T(kcomp(g, a - 2, e, y, z) * wv[i]);
+          o = C{-v.y * w, v.x * w};  // times i w
+        }
+      }
+      F1[idx] = o;
+    }
+    const C *res = fft_tile<T, +1>(F1, F2, B, px);
+    C *dst = out5 + (size_t)a * g.NC;
+    for (int idx = threadIdx.x; idx < g.Nx * B; idx += blockDim.x) {
+      const int e = idx / B, j = j0 + idx % B;
+      if (j < J) dst[(size_t)e * J + j] = res[idx];
+    }
+    __syncthreads();
+  }
+}
+
+// x-FFT of the five partial spectra, times adjoint weights, summed, inverse x.
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_x_conv_adj(
+    const typename Cplx<T>::type *__restrict__ in5, typename Cplx<T>::type *__restrict__ out,
+    const double *__restrict__ w3, const double *__restrict__ w2, const double *__restrict__ wv,
+    Geom g, FftPlan px, int B) {
+  using C = typename Cplx<T>::type;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C *acc = reinterpret_cast<C *>(smem_raw);
+  C *F1 = acc + g.Nx * B;
+  C *F2 = F1 + g.Nx * B;
+  const int J = g.Ny * g.NzH;
+  const int j0 = blockIdx.x * B;
+  for (int idx = threadIdx.x; idx < g.Nx * B; idx += blockDim.x) acc[idx] = C{0, 0};
+  for (int a = 0; a < 5; a++) {
+    const C *src = in5 + (size_t)a * g.NC;
+    for (int idx = threadIdx.x; idx < g.Nx * B; idx += blockDim.x) {
+      const int e = idx / B, j = j0 + idx % B;
+      F1[idx] = j < J ? src[(size_t)e * J + j] : C{0, 0};
+    }
+    const C *res = fft_tile<T, -1>(F1, F2, B, px);
+    for (int idx = threadIdx.x; idx < g.Nx * B; idx += blockDim.x) {
+      const int e = idx / B, j = j0 + idx % B;
+      if (j >= J) continue;
+      const size_t i = (size_t)e * J + j;
+      const C v = res[idx];
+      C o = acc[idx];
+      if (a == 0) {
+        const T w = T(w3[i]);
+        o.x += v.x * w;
+        o.y += v.y * w;
+      } else if (a == 1) {
+        const T w = T(w2[i]);
+        o.x += v.x * w;
+        o.y += v.y * w;
+      } else {
+        const int y = j / g.NzH, z = j % g.NzH;
+        const T w = T(kcomp(g, a - 2, e, y, z) * wv[i]);
+        o.x += v.y * w;  // times -i w
+        o.y -= v.x * w;
+      }
+      acc[idx] = o;
+    }
+    __syncthreads();
+  }
+  const C *res = fft_tile<T, +1>(acc, F1, B, px);
+  for (int idx = threadIdx.x; idx < g.Nx * B; idx += blockDim.x) {
+    const int e = idx / B, j = j0 + idx % B;
+    if (j < J) out[(size_t)e * J + j] = res[idx];
+  }
+}
+
+struct LocalArgs {
+  double R, kT, mu, nQ, dV;
+  int terms;
+};
+
+// c2r of the five weighted densities, phi and local terms, per-block
+// energies, and (GRAD) r2c of the five partials dV kT dphi/dn_a in place.
+template <typename T, bool GRAD>
+__global__ void __launch_bounds__(kThreads) k_z_phi(typename Cplx<T>::type *S5,
+                                                    const T *__restrict__ n,
+                                                    const T *__restrict__ V, Geom g, FftPlan pz,
+                                                    int P, LocalArgs la, double *partials) {
+  using C = typename Cplx<T>::type;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C *buf0 = reinterpret_cast<C *>(smem_raw);
+  C *buf1 = buf0 + g.Nz * P;
+  T *rv = reinterpret_cast<T *>(buf1 + g.Nz * P);  // [5][2P][Nz]
+  __shared__ double red[32 * kNumTerms];
+  const int Nz = g.Nz;
+  const int LP = 2 * P * Nz;
+  const int p0 = blockIdx.x * P;
+  for (int a = 0; a < 5; a++) {
+    pack_c2r<T>(S5 + (size_t)a * g.NC, buf0, g, p0, P);
+    const C *res = fft_tile<T, +1>(buf0, buf1, P, pz);
+    T *dst = rv + a * LP;
+    for (int idx = threadIdx.x; idx < LP; idx += blockDim.x) {
+      const int z = idx % Nz, ll = idx / Nz;
+      const C v = res[z * P + (ll >> 1)];
+      dst[idx] = (ll & 1) ? v.y : v.x;
+    }
+    __syncthreads();
+  }
+  double acc[kNumTerms] = {0, 0, 0, 0, 0, 0};
+  const bool hs = la.terms & kTermHS;
+  for (int idx = threadIdx.x; idx < LP; idx += blockDim.x) {
+    const int z = idx % Nz, ll = idx / Nz;
+    const int line = 2 * p0 + ll;
+    double d[5] = {0, 0, 0, 0, 0};
+    if (line < g.lines) {
+      const size_t r = (size_t)line * Nz + z;
+      if (hs) {
+        double phi[3];
+        phi_wb(la.R, rv[idx], rv[LP + idx], rv[2 * LP + idx], rv[3 * LP + idx], rv[4 * LP + idx],
+               phi, d);
+        acc[0] += la.kT * phi[0];
+        acc[1] += la.kT * phi[1];
+        acc[2] += la.kT * phi[2];
+      }
+      const double nv = n[r];
+      if (la.terms & kTermIdeal) acc[3] += nv == 0 ? 0.0 : la.kT * nv * (log(nv / la.nQ) - 1);
+      if (la.terms & kTermMu) acc[4] += la.mu * nv;
+      if (la.terms & kTermVext) acc[5] += (double)V[r] * nv;
+    }
+    if (GRAD) {
+      const double c = la.dV * la.kT;
+#pragma unroll
+      for (int a = 0; a < 5; a++) rv[a * LP + idx] = T(c * d[a]);
+    }
+  }
+  block_reduce<kNumTerms>(acc, red);
+  if (threadIdx.x == 0)
+    for (int t = 0; t < kNumTerms; t++) partials[(size_t)blockIdx.x * kNumTerms + t] = acc[t];
+  if (!GRAD) return;
+  __syncthreads();
+  for (int a = 0; a < 5; a++) {
+    const T *src = rv + a * LP;
+    for (int idx = threadIdx.x; idx < P * Nz; idx += blockDim.x) {
+      const int pb = idx % P, z = idx / P;
+      buf0[idx] = C{src[(2 * pb) * Nz + z], src[(2 * pb + 1) * Nz + z]};
+    }
+    const C *res = fft_tile<T, -1>(buf0, buf1, P, pz);
+    unpack_r2c_store<T>(res, S5 + (size_t)a * g.NC, g, p0, P, T(1));
+    __syncthreads();
+  }
+}
+
+// c2r of the adjoint sum, + local gradient terms, masked.
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_z_grad(const typename Cplx<T>::type *__restrict__ in,
+                                                     const T *__restrict__ n,
+                                                     const T *__restrict__ V,
+                                                     const T *__restrict__ mask, T *__restrict__ grad,
+                                                     Geom g, FftPlan pz, int P, LocalArgs la) {
+  using C = typename Cplx<T>::type;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C *buf0 = reinterpret_cast<C *>(smem_raw);
+  C *buf1 = buf0 + g.Nz * P;
+  const int p0 = blockIdx.x * P;
+  const bool hs = la.terms & kTermHS;
+  const C *res = nullptr;
+  if (hs) {
+    pack_c2r<T>(in, buf0, g, p0, P);
+    res = fft_tile<T, +1>(buf0, buf1, P, pz);
+  }
+  for (int idx = threadIdx.x; idx < 2 * P * g.Nz; idx += blockDim.x) {
+    const int z = idx % g.Nz, ll = idx / g.Nz;
+    const int line = 2 * p0 + ll;
+    if (line >= g.lines) continue;
+    const size_t r = (size_t)line * g.Nz + z;
+    double conv = 0;
+    if (hs) {
+      const C v = res[z * P + (ll >> 1)];
+      conv = (ll & 1) ? v.y : v.x;
+    }
+    double loc = 0;
+    const double nv = n[r];
+    if (la.terms & kTermIdeal) loc += la.kT * log(nv / la.nQ);
+    if (la.terms & kTermMu) loc += la.mu;
+    if (la.terms & kTermVext) loc += (double)V[r];
+    double gr = conv + la.dV * loc;
+    if (la.terms & kTermMask) {
+      const double m = mask[r];
+      gr = m == 0 ? 0.0 : m * gr;
+    }
+    grad[r] = T(gr);
+  }
+}
+
+// Energy partials of the local terms only (no hard spheres).
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_local_energy(const T *__restrict__ n,
+                                                           const T *__restrict__ V, Geom g,
+                                                           LocalArgs la, double *partials) {
+  __shared__ double red[32 * kNumTerms];
+  double acc[kNumTerms] = {0, 0, 0, 0, 0, 0};
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < g.NR; r += gridDim.x * blockDim.x) {
+    const double nv = n[r];
+    if (la.terms & kTermIdeal) acc[3] += nv == 0 ? 0.0 : la.kT * nv * (log(nv / la.nQ) - 1);
+    if (la.terms & kTermMu) acc[4] += la.mu * nv;
+    if (la.terms & kTermVext) acc[5] += (double)V[r] * nv;
+  }
+  block_reduce<kNumTerms>(acc, red);
+  if (threadIdx.x == 0)
+    for (int t = 0; t < kNumTerms; t++) partials[(size_t)blockIdx.x * kNumTerms + t] = acc[t];
+}
+
+// Sums per-block energy partials in a fixed order: out[t] = dV sum, out[6] = E.
+__global__ void k_reduce_terms(const double *partials, int nblk, double dV, double *out) {
+  __shared__ double red[32 * kNumTerms];
+  double acc[kNumTerms] = {0, 0, 0, 0, 0, 0};
+  for (int b = threadIdx.x; b < nblk; b += blockDim.x)
+    for (int t = 0; t < kNumTerms; t++) acc[t] += partials[(size_t)b * kNumTerms + t];
+  block_reduce<kNumTerms>(acc, red);
+  if (threadIdx.x == 0) {
+    double E = 0;
+    for (int t = 0; t < kNumTerms; t++) {
+      out[t] = acc[t] * dV;
+      E += out[t];
+    }
+    out[kNumTerms] = E;
+  }
+}
+
+// Up to three dot products in one pass; the last block to finish reduces the
+// per-block partials in a fixed order (deterministic).
+__global__ void k_dots(int k, const double *a0, const double *b0, const double *a1,
+                       const double *b1, const double *a2, const double *b2, int n,
+                       double *partials, unsigned int *counter, double *out) {
+  __shared__ double red[32 * 3];
+  __shared__ bool last;
+  double acc[3] = {0, 0, 0};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    acc[0] += a0[i] * b0[i];
+    if (k > 1) acc[1] += a1[i] * b1[i];
+    if (k > 2) acc[2] += a2[i] * b2[i];
+  }
+  block_reduce<3>(acc, red);
+  if (threadIdx.x == 0) {
+    for (int t = 0; t < 3; t++) partials[(size_t)blockIdx.x * 3 + t] = acc[t];
+    __threadfence();
+    const unsigned int done = atomicAdd(counter, 1u);
+    last = (done == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  double s[3] = {0, 0, 0};
+  for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
+    for (int t = 0; t < 3; t++) s[t] += ((volatile double *)partials)[(size_t)b * 3 + t];
+  __syncthreads();
+  block_reduce<3>(s, red);
+  if (threadIdx.x == 0) {
+    for (int t = 0; t < 3; t++) out[t] = s[t];
+    *counter = 0;
+  }
+}
+
+__global__ void k_axpy(double alpha, const double *x, double *y, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    y[i] += alpha * x[i];
+}
+
+__global__ void k_scal_add(double beta, double *d, double alpha, const double *g, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    d[i] = alpha * g[i] + beta * d[i];
+}
+
+// ---------------------------------------------------------------------------
+// Host side
+
+bool factorize(int n, FftPlan &p) {
+  int k = 0;
+  p.n = n;
+  while (n % 8 == 0 && k < kMaxPasses) { p.radix[k++] = 8; n /= 8; }
+  while (n % 4 == 0 && k < kMaxPasses) { p.radix[k++] = 4; n /= 4; }
+  while (n % 2 == 0 && k < kMaxPasses) { p.radix[k++] = 2; n /= 2; }
+  const int primes[] = {3, 5, 7, 11, 13};
+  for (int q : primes)
+    while (n % q == 0 && k < kMaxPasses) { p.radix[k++] = q; n /= q; }
+  p.npass = k;
+  return n == 1;
+}
+
+double det3(const double m[9]) {
+  return m[0] * (m[4] * m[8] - m[5] * m[7]) - m[1] * (m[3] * m[8] - m[5] * m[6]) +
+         m[2] * (m[3] * m[7] - m[4] * m[6]);
+}
+
+double nQ_of(double kT) {
+  // find_nQ, src/IdealGas.cpp:54-59: (m kT / 2 pi)^(3/2), m = water mass
+  const double x = 18.01528 * 1822.8885 * kT / (2 * M_PI);
+  return x * std::sqrt(x);
+}
+
+template <typename K>
+void set_smem(K kernel, size_t bytes) {
+  cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+int tile_width(int lines, int L, size_t bytes_per_elem, int nbuf, int cap) {
+  int maxb = (int)(kSmemBudget / ((size_t)L * bytes_per_elem * nbuf));
+  if (maxb < 1) maxb = 1;
+  if (maxb > cap) maxb = cap;
+  const int ntiles = (lines + maxb - 1) / maxb;
+  return (lines + ntiles - 1) / ntiles;
+}
+
+}  // namespace
+
+class EngineImpl {
+ public:
+  Geom g{};
+  cudaStream_t stream = nullptr;
+  FftPlan px{}, py{}, pz{};
+  double2 *tw_x = nullptr, *tw_y = nullptr, *tw_z = nullptr;
+  double2 *S0 = nullptr, *S5 = nullptr;
+  double *w3 = nullptr, *w2 = nullptr, *wv = nullptr;
+  double table_R = -1;
+  double *partials = nullptr;
+  int max_blocks = 0;
+  double *results = nullptr;       // device, 8
+  double *results_host = nullptr;  // pinned, 8
+  double *dot_partials = nullptr;
+  unsigned int *dot_counter = nullptr;
+  int dot_blocks = 0;
+  int By = 0, Bx = 0, Pz = 0, Pphi = 0;
+  size_t smem_y = 0, smem_x2 = 0, smem_x3 = 0, smem_z = 0, smem_phi = 0;
+  size_t bytes = 0;
+  std::string err;
+
+  ~EngineImpl() {
+    cudaFree(tw_x);
+    cudaFree(tw_y);
+    cudaFree(tw_z);
+    cudaFree(S0);
+    cudaFree(S5);
+    cudaFree(w3);
+    cudaFree(w2);
+    cudaFree(wv);
+    cudaFree(partials);
+    cudaFree(results);
+    cudaFree(dot_partials);
+    cudaFree(dot_counter);
+    cudaFreeHost(results_host);
+  }
+
+  int fail(const char *what, cudaError_t e) {
+    err = std::string(what) + ": " + cudaGetErrorString(e);
+    return -1;
+  }
+  int check(const char *what) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(what, e);
+    return 0;
+  }
+
+  template <typename P>
+  int alloc(P **p, size_t n) {
+    cudaError_t e = cudaMalloc((void **)p, n);
+    if (e != cudaSuccess) return fail("cudaMalloc", e);
+    bytes += n;
+    return 0;
+  }
+
+  int make_plan(int n, FftPlan &p, double2 **tw) {
+    if (!factorize(n, p)) {
+      err = "grid size " + std::to_string(n) + " has a prime factor above 13";
+      return -1;
+    }
+    std::vector<double2> h(n);
+    const long double twopi = 6.283185307179586476925286766559005768L;
+    for (int t = 0; t < n; t++) {
+      const long double a = twopi * (long double)t / (long double)n;
+      h[t] = make_double2((double)cosl(a), (double)-sinl(a));
+    }
+    if (alloc(tw, sizeof(double2) * n)) return -1;
+    cudaError_t e = cudaMemcpy(*tw, h.data(), sizeof(double2) * n, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return fail("twiddle upload", e);
+    p.tw = *tw;
+    return 0;
+  }
+
+  int init(const GridSpec &s, cudaStream_t st) {
+    stream = st;
+    g.Nx = s.Nx;
+    g.Ny = s.Ny;
+    g.Nz = s.Nz;
+    g.NzH = s.Nz / 2 + 1;
+    g.lines = s.Nx * s.Ny;
+    const long long NR = (long long)s.Nx * s.Ny * s.Nz;
+    const long long NC = (long long)s.Nx * s.Ny * g.NzH;
+    if (NR > (1LL << 30) || 5 * NC > (1LL << 31) - 1) {
+      err = "grid too large";
+      return -1;
+    }
+    g.NR = (int)NR;
+    g.NC = (int)NC;
+    double R[9], fine[9];
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) R[3 * i + j] = s.lat[3 * j + i];
+    const int N[3] = {s.Nx, s.Ny, s.Nz};
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) fine[3 * i + j] = R[3 * i + j] / N[j];
+    g.vol = det3(R);
+    g.dV = det3(fine);
+    if (!(g.vol > 0)) {
+      err = "lattice vectors must be right-handed and non-degenerate";
+      return -1;
+    }
+    g.dr = std::pow(g.dV, 1.0 / 3);
+    g.scale = g.dV / g.vol;
+    double inv[9];
+    const double d = g.vol;
+    inv[0] = (R[4] * R[8] - R[5] * R[7]) / d;
+    inv[1] = (R[2] * R[7] - R[1] * R[8]) / d;
+    inv[2] = (R[1] * R[5] - R[2] * R[4]) / d;
+    inv[3] = (R[5] * R[6] - R[3] * R[8]) / d;
+    inv[4] = (R[0] * R[8] - R[2] * R[6]) / d;
+    inv[5] = (R[2] * R[3] - R[0] * R[5]) / d;
+    inv[6] = (R[3] * R[7] - R[4] * R[6]) / d;
+    inv[7] = (R[1] * R[6] - R[0] * R[7]) / d;
+    inv[8] = (R[0] * R[4] - R[1] * R[3]) / d;
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) g.Bm[3 * i + j] = 2 * M_PI * inv[3 * j + i];
+
+    if (make_plan(s.Nx, px, &tw_x) || make_plan(s.Ny, py, &tw_y) || make_plan(s.Nz, pz, &tw_z))
+      return -1;
+
+    // tile widths
+    const size_t cs = sizeof(double2);
+    By = tile_width(g.NzH, g.Ny, cs, 2, 16);
+    Bx = tile_width(g.Ny * g.NzH, g.Nx, cs, 3, 16);
+    const int pairs = (g.lines + 1) / 2;
+    Pz = tile_width(pairs, g.Nz, cs, 2, 16);
+    {
+      const size_t per_pair = (size_t)g.Nz * (2 * cs + 10 * sizeof(double));
+      int pm = (int)(kSmemBudget / per_pair);
+      if (pm < 1) pm = 1;
+      if (pm > 8) pm = 8;
+      const int nt = (pairs + pm - 1) / pm;
+      Pphi = (pairs + nt - 1) / nt;
+    }
+    smem_y = 2 * (size_t)g.Ny * By * cs;
+    smem_x2 = 2 * (size_t)g.Nx * Bx * cs;
+    smem_x3 = 3 * (size_t)g.Nx * Bx * cs;
+    smem_z = 2 * (size_t)g.Nz * Pz * cs;
+    smem_phi = (size_t)g.Nz * Pphi * (2 * cs + 10 * sizeof(double));
+    const size_t mx = 227 * 1024;
+    if (smem_y > mx || smem_x3 > mx || smem_z > mx || smem_phi > mx) {
+      err = "grid line too long for one shared-memory tile";
+      return -1;
+    }
+    set_smem(k_z_r2c<double>, smem_z);
+    set_smem(k_z_c2r<double>, smem_z);
+    set_smem(k_y_fft<double, -1>, smem_y);
+    set_smem(k_y_fft<double, +1>, smem_y);
+    set_smem(k_x_fft<double, -1>, smem_x2);
+    set_smem(k_x_fft<double, +1>, smem_x2);
+    set_smem(k_x_conv_fwd<double>, smem_x3);
+    set_smem(k_x_conv_adj<double>, smem_x3);
+    set_smem(k_z_phi<double, false>, smem_phi);
+    set_smem(k_z_phi<double, true>, smem_phi);
+    set_smem(k_z_grad<double>, smem_z);
+
+    if (alloc(&S0, cs * g.NC) || alloc(&S5, 5 * cs * g.NC) || alloc(&w3, sizeof(double) * g.NC) ||
+        alloc(&w2, sizeof(double) * g.NC) || alloc(&wv, sizeof(double) * g.NC))
+      return -1;
+    max_blocks = (pairs + Pphi - 1) / Pphi;
+    if (max_blocks < 1024) max_blocks = 1024;
+    if (alloc(&partials, sizeof(double) * kNumTerms * max_blocks)) return -1;
+    if (alloc(&results, sizeof(double) * 8)) return -1;
+    cudaError_t e = cudaMallocHost((void **)&results_host, sizeof(double) * 8);
+    if (e != cudaSuccess) return fail("cudaMallocHost", e);
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    dot_blocks = 2 * (sms > 0 ? sms : 148);
+    const int need = (g.NR + kThreads - 1) / kThreads;
+    if (dot_blocks > need) dot_blocks = need;
+    if (dot_blocks < 1) dot_blocks = 1;
+    if (alloc(&dot_partials, sizeof(double) * 3 * dot_blocks) || alloc(&dot_counter, sizeof(unsigned)))
+      return -1;
+    e = cudaMemset(dot_counter, 0, sizeof(unsigned));
+    if (e != cudaSuccess) return fail("cudaMemset", e);
+    return check("engine init");
+  }
+
+  int ensure_table(double R) {
+    if (R == table_R) return 0;
+    const int blocks = (g.NC + kThreads - 1) / kThreads;
+    k_weight_table<<<blocks < 4096 ? blocks : 4096, kThreads, 0, stream>>>(g, R, w3, w2, wv);
+    if (check("weight table")) return -1;
+    table_R = R;
+    return 0;
+  }
+
+  int pairs_tiles(int P) const { return ((g.lines + 1) / 2 + P - 1) / P; }
+
+  void y_fft(double2 *data, int nf, int sign) {
+    dim3 grid((g.NzH + By - 1) / By, g.Nx, nf);
+    if (sign < 0) k_y_fft<double, -1><<<grid, kThreads, smem_y, stream>>>(data, g, py, By);
+    else k_y_fft<double, +1><<<grid, kThreads, smem_y, stream>>>(data, g, py, By);
+  }
+  int x_tiles() const { return (g.Ny * g.NzH + Bx - 1) / Bx; }
+
+  int forward_weighted(const FmtSpec &f, const double *n) {
+    if (ensure_table(f.R)) return -1;
+    k_z_r2c<double><<<dim3(pairs_tiles(Pz), 1), kThreads, smem_z, stream>>>(n, S0, g, pz, Pz, 1.0);
+    y_fft(S0, 1, -1);
+    k_x_conv_fwd<double><<<x_tiles(), kThreads, smem_x3, stream>>>(S0, S5, w3, w2, wv, g, px, Bx);
+    y_fft(S5, 5, +1);
+    return check("forward convolution");
+  }
+
+  LocalArgs local_args(const FmtSpec &f) const {
+    LocalArgs la;
+    la.R = f.R;
+    la.kT = f.kT;
+    la.mu = f.mu;
+    la.nQ = nQ_of(f.kT);
+    la.dV = g.dV;
+    la.terms = f.terms;
+    return la;
+  }
+
+  int finish_energy(int nblk, double *E_host, double *terms_host) {
+    k_reduce_terms<<<1, kThreads, 0, stream>>>(partials, nblk, g.dV, results);
+    cudaMemcpyAsync(results_host, results, sizeof(double) * 8, cudaMemcpyDeviceToHost, stream);
+    cudaError_t e = cudaStreamSynchronize(stream);
+    if (e != cudaSuccess) return fail("energy", e);
+    if (E_host) *E_host = results_host[kNumTerms];
+    if (terms_host) memcpy(terms_host, results_host, sizeof(double) * kNumTerms);
+    return 0;
+  }
+
+  int eval(const FmtSpec &f, const double *n, const double *V, const double *mask, double *grad,
+           double *E_host, double *terms_host) {
+    const LocalArgs la = local_args(f);
+    int nblk;
+    if (f.terms & kTermHS) {
+      if (forward_weighted(f, n)) return -1;
+      nblk = pairs_tiles(Pphi);
+      if (grad)
+        k_z_phi<double, true><<<nblk, kThreads, smem_phi, stream>>>(S5, n, V, g, pz, Pphi, la,
+                                                                    partials);
+      else
+        k_z_phi<double, false><<<nblk, kThreads, smem_phi, stream>>>(S5, n, V, g, pz, Pphi, la,
+                                                                     partials);
+      if (check("phi")) return -1;
+      if (grad) {
+        y_fft(S5, 5, -1);
+        k_x_conv_adj<double><<<x_tiles(), kThreads, smem_x3, stream>>>(S5, S0, w3, w2, wv, g, px,
+                                                                       Bx);
+        y_fft(S0, 1, +1);
+      }
+    } else {
+      nblk = 4 * 152;
+      k_local_energy<double><<<nblk, kThreads, 0, stream>>>(n, V, g, la, partials);
+    }
+    if (grad)
+      k_z_grad<double><<<pairs_tiles(Pz), kThreads, smem_z, stream>>>(S0, n, V, mask, grad, g, pz,
+                                                                       Pz, la);
+    if (check("gradient")) return -1;
+    return finish_energy(nblk, E_host, terms_host);
+  }
+};
+
+Engine::Engine(EngineImpl *impl) : impl_(impl) {}
+Engine::~Engine() { delete impl_; }
+
+Engine *Engine::create(const GridSpec &g, cudaStream_t stream, std::string *err) {
+  EngineImpl *impl = new EngineImpl();
+  if (impl->init(g, stream)) {
+    if (err) *err = impl->err;
+    delete impl;
+    return nullptr;
+  }
+  return new Engine(impl);
+}
+
+const Geom &Engine::geom() const { return impl_->g; }
+cudaStream_t Engine::stream() const { return impl_->stream; }
+size_t Engine::scratch_bytes() const { return impl_->bytes; }
+const char *Engine::last_error() const { return impl_->err.c_str(); }
+
+int Engine::fft(const double *in, double2 *out) {
+  EngineImpl &e = *impl_;
+  k_z_r2c<double><<<dim3(e.pairs_tiles(e.Pz), 1), kThreads, e.smem_z, e.stream>>>(in, out, e.g, e.pz,
+                                                                                 e.Pz, 1.0);
+  e.y_fft(out, 1, -1);
+  k_x_fft<double, -1><<<e.x_tiles(), kThreads, e.smem_x2, e.stream>>>(out, e.g, e.px, e.Bx, e.g.dV);
+  return e.check("fft");
+}
+
+int Engine::ifft(const double2 *in, double *out) {
+  EngineImpl &e = *impl_;
+  cudaMemcpyAsync(e.S0, in, sizeof(double2) * e.g.NC, cudaMemcpyDeviceToDevice, e.stream);
+  k_x_fft<double, +1><<<e.x_tiles(), kThreads, e.smem_x2, e.stream>>>(e.S0, e.g, e.px, e.Bx, 1.0);
+  e.y_fft(e.S0, 1, +1);
+  k_z_c2r<double><<<dim3(e.pairs_tiles(e.Pz), 1), kThreads, e.smem_z, e.stream>>>(
+      e.S0, out, e.g, e.pz, e.Pz, 1.0 / e.g.vol);
+  return e.check("ifft");
+}
+
+int Engine::weighted(const FmtSpec &f, const double *n, double *out5) {
+  EngineImpl &e = *impl_;
+  if (e.forward_weighted(f, n)) return -1;
+  k_z_c2r<double><<<dim3(e.pairs_tiles(e.Pz), 5), kThreads, e.smem_z, e.stream>>>(e.S5, out5, e.g,
+                                                                                 e.pz, e.Pz, 1.0);
+  return e.check("weighted");
+}
+
+int Engine::energy(const FmtSpec &f, const double *n, const double *V, const double *mask,
+                   double *E_host, double *terms_host) {
+  return impl_->eval(f, n, V, mask, nullptr, E_host, terms_host);
+}
+
+int Engine::energy_grad(const FmtSpec &f, const double *n, const double *V, const double *mask,
+                        double *grad, double *E_host, double *terms_host) {
+  return impl_->eval(f, n, V, mask, grad, E_host, terms_host);
+}
+
+int Engine::dots(int k, const double *const *a, const double *const *b, double *out_host) {
+  EngineImpl &e = *impl_;
+  k_dots<<<e.dot_blocks, kThreads, 0, e.stream>>>(k, a[0], b[0], k > 1 ? a[1] : nullptr,
+                                                  k > 1 ? b[1] : nullptr, k > 2 ? a[2] : nullptr,
+                                                  k > 2 ? b[2] : nullptr, e.g.NR, e.dot_partials,
+                                                  e.dot_counter, e.results);
+  cudaMemcpyAsync(e.results_host, e.results, sizeof(double) * 3, cudaMemcpyDeviceToHost, e.stream);
+  cudaError_t err = cudaStreamSynchronize(e.stream);
+  if (err != cudaSuccess) return e.fail("dots", err);
+  for (int i = 0; i < k; i++) out_host[i] = e.results_host[i];
+  return 0;
+}
+
+int Engine::axpy(double alpha, const double *x, double *y) {
+  EngineImpl &e = *impl_;
+  k_axpy<<<e.dot_blocks, kThreads, 0, e.stream>>>(alpha, x, y, e.g.NR);
+  return e.check("axpy");
+}
+
+int Engine::scal_add(double beta, double *d, double alpha, const double *gv) {
+  EngineImpl &e = *impl_;
+  k_scal_add<<<e.dot_blocks, kThreads, 0, e.stream>>>(beta, d, alpha, gv, e.g.NR);
+  return e.check("scal_add");
+}
+
+int Engine::copy(const double *src, double *dst) {
+  EngineImpl &e = *impl_;
+  cudaError_t err =
+      cudaMemcpyAsync(dst, src, sizeof(double) * e.g.NR, cudaMemcpyDeviceToDevice, e.stream);
+  if (err != cudaSuccess) return e.fail("copy", err);
+  return 0;
+}
+
+}  // namespace deft

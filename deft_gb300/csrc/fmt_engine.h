@@ -1,0 +1,85 @@
+// FMT evaluation engine: host-side interface to the sm_103a kernels that
+// evaluate deft's White Bear functional (+ ideal gas, mu, V_ext, mask) and its
+// gradient on a periodic grid, plus the FP64 vector kernels the CG driver
+// needs.  Every pointer passed to Engine methods is a device pointer on the
+// engine's device; all work is queued on the engine's stream.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+
+namespace deft {
+
+enum TermFlags {
+  kTermHS = 1,
+  kTermIdeal = 2,
+  kTermMu = 4,
+  kTermVext = 8,
+  kTermMask = 16,
+};
+
+constexpr int kNumTerms = 6;  // phi3, phi1, phi2, ideal, mu, vext
+
+struct GridSpec {
+  int Nx, Ny, Nz;
+  double lat[9];  // a1 = lat[0..2], a2 = lat[3..5], a3 = lat[6..8]
+};
+
+struct FmtSpec {
+  double R, kT, mu;
+  int terms;
+};
+
+struct Geom {
+  int Nx, Ny, Nz, NzH;
+  int lines;  // Nx*Ny real z-lines
+  int NR;     // Nx*Ny*Nz real points
+  int NC;     // Nx*Ny*NzH complex points
+  double Bm[9];  // k_c = sum_d Bm[3c+d] m_d  (2 pi R^-T)
+  double dV, vol, dr, scale;  // scale = dV / vol (fft x dV then ifft x 1/V)
+};
+
+class EngineImpl;
+
+class Engine {
+ public:
+  // Returns nullptr and sets *err on failure.
+  static Engine *create(const GridSpec &g, cudaStream_t stream, std::string *err);
+  ~Engine();
+
+  const Geom &geom() const;
+  cudaStream_t stream() const;
+  size_t scratch_bytes() const;
+
+  // fft(gd, v): r2c x dV (src/Grid.cpp:470-478); ifft: c2r x 1/V
+  // (src/ReciprocalGrid.cpp:42-66).  out of fft / in of ifft: NC complex.
+  int fft(const double *in, double2 *out);
+  int ifft(const double2 *in, double *out);
+
+  // n3, n2, n2x, n2y, n2z (5*NR reals).
+  int weighted(const FmtSpec &f, const double *n, double *out5);
+
+  // Energy (terms_host gets the 6 per-term energies, may be null).
+  // V, mask may be null when the corresponding term flag is off.
+  int energy(const FmtSpec &f, const double *n, const double *V, const double *mask,
+             double *E_host, double *terms_host);
+  // Energy and masked gradient (grad: NR reals on device).
+  int energy_grad(const FmtSpec &f, const double *n, const double *V, const double *mask,
+                  double *grad, double *E_host, double *terms_host);
+
+  // Vector kernels (NR-long device vectors).
+  // out_host[i] = a_i . b_i for i < k (k <= 3), one pass, one sync.
+  int dots(int k, const double *const *a, const double *const *b, double *out_host);
+  int axpy(double alpha, const double *x, double *y);               // y += alpha x
+  int scal_add(double beta, double *d, double alpha, const double *g);  // d = alpha g + beta d
+  int copy(const double *src, double *dst);
+
+  const char *last_error() const;
+
+ private:
+  explicit Engine(EngineImpl *impl);
+  EngineImpl *impl_;
+};
+
+}  // namespace deft

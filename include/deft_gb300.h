@@ -1,0 +1,154 @@
+/* deft_gb300 -- C ABI of the GB300-native FMT functional + conjugate-gradient
+ * hot path of deft (droundy/deft).
+ *
+ * Plain pointers and sizes only.  Fields are FP64, row-major
+ * index x*Ny*Nz + y*Nz + z (the layout of Grid, src/Grid.h:37-42).  Every
+ * call that takes a field has an `on_device` flag: 0 = host pointer (the
+ * library copies), 1 = device pointer on the context's GPU (used in place).
+ * All calls return DEFT_OK (0) or a DEFT_ERR_* status; deft_last_error()
+ * gives a message.  A context owns one CUDA stream; objects made from a
+ * context must be used from one host thread at a time (the reference is not
+ * re-entrant either: src/Functional.h:223, src/Minimizer.h:80).
+ *
+ * Composition mirrored from the reference drivers
+ * (papers/contact/figs/walls.cpp:86-98):
+ *   f = constrain(mask, HardSpheresWBnotensor(R) + IdealGas()
+ *                       + ChemicalPotential(mu) + ExternalPotential(V))
+ * with each term switched on by a DEFT_TERM_* flag.
+ */
+#ifndef DEFT_GB300_H
+#define DEFT_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DEFT_OK 0
+#define DEFT_ERR_ARG 1         /* invalid argument or unsupported size */
+#define DEFT_ERR_CUDA 2        /* CUDA runtime error (message in deft_last_error) */
+#define DEFT_ERR_NAN 3         /* energy or gradient is not finite */
+#define DEFT_ERR_LINESEARCH 4  /* line search found no acceptable step */
+#define DEFT_ERR_MAXITER 5     /* iteration limit reached before the tolerance */
+#define DEFT_ERR_NOMEM 6       /* device allocation failed */
+
+/* Terms of the composed functional. */
+#define DEFT_TERM_HS 1     /* HardSpheresWBnotensor(R), src/HardSpheres.cpp:137-159 */
+#define DEFT_TERM_IDEAL 2  /* IdealGas(), src/IdealGas.cpp:68-72 */
+#define DEFT_TERM_MU 4     /* ChemicalPotential(mu), src/ChemicalPotential.cpp:19-22 */
+#define DEFT_TERM_VEXT 8   /* ExternalPotential(V), src/ExternalPotential.cpp:19-21 */
+#define DEFT_TERM_MASK 16  /* constrain(mask, f), src/Functional.cpp:834-838 */
+
+/* Number of per-term energies: phi3, phi1, phi2 (src/HardSpheres.cpp:156),
+ * ideal gas, chemical potential, external potential. */
+#define DEFT_NTERMS 6
+
+/* Line searches for the CG minimiser. */
+#define DEFT_LS_SECANT 0         /* derivative (secant) search on grad.d, reuses the gradient */
+#define DEFT_LS_QUADRATIC_REF 1  /* QuadraticLineMinimizer, src/QuadraticLineMinimizer.cpp:27-198 */
+
+typedef struct deft_ctx deft_ctx;
+typedef struct deft_grid deft_grid;
+typedef struct deft_fmt deft_fmt;
+typedef struct deft_cg deft_cg;
+
+typedef struct {
+  double R;   /* hard-sphere radius */
+  double kT;  /* temperature (the kT argument of Functional::integral, src/Functional.h:131) */
+  double mu;  /* ChemicalPotential coefficient (the tree adds mu*n) */
+  int terms;  /* DEFT_TERM_* bit set */
+} deft_fmt_params;
+
+typedef struct {
+  int linesearch;   /* DEFT_LS_* */
+  double gtol;      /* stop when |grad|_2 < gtol (grad includes dV, as integralgrad) */
+  int maxiter;      /* CG iteration limit */
+  double step;      /* initial step (ConjugateGradient's stepsize, src/LineMinimizer.h:18-19) */
+  double precision; /* >0: also stop by Precision(eps) (src/Precision.cpp:53-151) */
+} deft_cg_params;
+
+typedef struct {
+  int iter;          /* CG iterations done */
+  int evals;         /* functional evaluations (energy or energy+gradient) */
+  double energy;     /* current energy */
+  double gnorm;      /* |grad|_2 at the current point (secant search; 0 if unknown) */
+  int converged;     /* 1 if the stopping rule was met */
+  int status;        /* DEFT_OK or the error that ended the run */
+} deft_cg_status;
+
+/* ---- errors ---- */
+const char *deft_strerror(int status);
+/* Message of the last failing call on this host thread. */
+const char *deft_last_error(void);
+
+/* ---- context ----  (no reference counterpart: owns the device and stream) */
+int deft_ctx_create(int device, deft_ctx **out);
+int deft_ctx_destroy(deft_ctx *ctx);
+/* Synchronise the context's stream. */
+int deft_ctx_sync(deft_ctx *ctx);
+/* Raw cudaStream_t of the context (for callers that order their own work). */
+void *deft_ctx_stream(deft_ctx *ctx);
+
+/* ---- grid ----
+ * Replaces GridDescription(Lattice(a1,a2,a3), Nx, Ny, Nz)
+ * (src/GridDescription.cpp:6-25, src/lattice.cpp:13): lat holds a1, a2, a3
+ * (Cartesian rows).  Sizes must factor into primes <= 13. */
+int deft_grid_create(deft_ctx *ctx, const double lat[9], int Nx, int Ny, int Nz,
+                     deft_grid **out);
+/* Replaces GridDescription(lat, dx) (src/GridDescription.cpp:27-48):
+ * N_i = 1 + int(e/100 + |a_i|/dx). */
+int deft_grid_create_dx(deft_ctx *ctx, const double lat[9], double dx, deft_grid **out);
+int deft_grid_destroy(deft_grid *grid);
+/* N[3], dV (fineLat.volume()), cell volume, device scratch bytes held. */
+int deft_grid_info(const deft_grid *grid, int N[3], double *dV, double *volume,
+                   double *scratch_bytes);
+/* fft(gd, v): r2c times dV (src/Grid.cpp:470-478).  out: Nx*Ny*(Nz/2+1)
+ * interleaved complex. */
+int deft_grid_fft(deft_grid *grid, const double *in, double *out, int on_device);
+/* ifft(gd, v): c2r times 1/V (src/ReciprocalGrid.cpp:42-66); input kept. */
+int deft_grid_ifft(deft_grid *grid, const double *in, double *out, int on_device);
+
+/* ---- functional ---- */
+int deft_fmt_create(deft_grid *grid, const deft_fmt_params *p, deft_fmt **out);
+int deft_fmt_destroy(deft_fmt *f);
+int deft_fmt_set_params(deft_fmt *f, const deft_fmt_params *p);
+/* External potential field for DEFT_TERM_VEXT (NULL clears). */
+int deft_fmt_set_vext(deft_fmt *f, const double *V, int on_device);
+/* Constraint mask for DEFT_TERM_MASK (NULL clears). */
+int deft_fmt_set_mask(deft_fmt *f, const double *mask, int on_device);
+/* Functional::integral(kT, n) (src/Functional.h:131-143); terms_out
+ * (DEFT_NTERMS, may be NULL) gets the per-term energies (last_energy). */
+int deft_fmt_energy(deft_fmt *f, const double *n, int on_device, double *E_out,
+                    double *terms_out);
+/* Energy and Functional::integralgrad (src/Functional.h:147-149): grad_out is
+ * OVERWRITTEN with dE/dn (dV included, mask applied); the reference
+ * accumulates into caller-zeroed buffers. */
+int deft_fmt_energy_grad(deft_fmt *f, const double *n, int on_device, double *E_out,
+                         double *grad_out, double *terms_out);
+/* The weighted densities n3, n2, n2x, n2y, n2z (5 fields, out5), i.e.
+ * StepConvolve/ShellConvolve/x,y,zShellConvolve(R) (src/Gaussian.cpp:82-102). */
+int deft_fmt_weighted(deft_fmt *f, const double *n, int on_device, double *out5);
+/* find_chemical_potential(OfEffectivePotential(HS(R)+IdealGas()), kT, nb)
+ * (src/equation-of-state.cpp:189-192): the mu that makes nb the bulk density. */
+int deft_find_chemical_potential(double R, double kT, double nb, double *mu_out);
+
+/* ---- minimiser ----
+ * Replaces ConjugateGradient(f, gd, kT, &x, QuadraticLineMinimizer, step)
+ * (src/ConjugateGradient.cpp:59-108,166-169) wrapped in MaxIter / Precision
+ * (src/Minimizer.cpp:27-48, src/Precision.cpp:53-156).  The minimiser keeps
+ * its own device copy of x; get/set move it. */
+int deft_cg_create(deft_fmt *f, const deft_cg_params *p, deft_cg **out);
+int deft_cg_destroy(deft_cg *cg);
+int deft_cg_set_x(deft_cg *cg, const double *n, int on_device);
+int deft_cg_get_x(deft_cg *cg, double *n, int on_device);
+/* Device pointer of the minimiser's x (valid until deft_cg_destroy). */
+double *deft_cg_x_device(deft_cg *cg);
+/* One Minimizer::improve_energy() (src/Minimizer.h:44).  st->converged = 1
+ * and return DEFT_OK when the stopping rule holds. */
+int deft_cg_step(deft_cg *cg, deft_cg_status *st);
+/* improve_energy() until converged, an error, or maxiter. */
+int deft_cg_solve(deft_cg *cg, deft_cg_status *st);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

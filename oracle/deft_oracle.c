@@ -1,0 +1,607 @@
+/* deft_oracle -- plain-C FP64 restatement of deft's FMT functional + CG hot
+ * path.  TEST INFRASTRUCTURE ONLY (the checker): used by tests/, by
+ * __graft_entry__.smoke() and by bench.py's CPU baseline / reference arm.
+ * The product never links or calls it.
+ *
+ * What it restates (reference files are droundy/deft paths):
+ *   k-vectors        src/ReciprocalOperators.h:23-38, src/lattice.h:104-106
+ *   step weight      src/ReciprocalOperators.h:94-118
+ *   shell weight     src/ReciprocalOperators.h:120-142
+ *   vector shells    src/ReciprocalOperators.h:162-235
+ *   convolution      src/Functional.h:376-381 (fft x dV, ifft x 1/V:
+ *                    src/Grid.cpp:470-478, src/ReciprocalGrid.cpp:52-66)
+ *   adjoint          src/Functional.h:407-417 (odd weights negated)
+ *   White Bear phi   src/HardSpheres.cpp:21-28,137-159
+ *   ideal gas        src/IdealGas.cpp:54-72
+ *   mu, V_ext        src/ChemicalPotential.cpp:19-22, src/ExternalPotential.cpp:19-21
+ *   constraint       src/Functional.cpp:809-824 (gradient times mask)
+ *   CG               src/ConjugateGradient.cpp:59-108
+ *   quadratic search src/QuadraticLineMinimizer.cpp:27-198
+ *
+ * Two documented departures, both limits of the same formulas, applied
+ * identically by the GPU path:
+ *   - the phi3 prefactor (n3 + (1-n3)^2 ln(1-n3)) / (36 pi n3^2 (1-n3)^2) is
+ *     0/0 at n3 -> 0 (src/HardSpheres.cpp:153); for |n3| < 1e-2 its Taylor
+ *     series is used (limit 1/(24 pi));
+ *   - the ideal-gas integrand kT n (ln(n/nQ) - 1) is taken as 0 at n == 0
+ *     (the reference gives NaN there), and masked points get gradient 0.
+ * On inputs with n > 0 and n3 >= 1e-2 everywhere the formulas are the
+ * reference's own, which is how the restatement is pinned.
+ */
+#include "deft_oracle.h"
+#include "offt.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+static long long g_ffts = 0;
+long long oracle_fft_count(void) { return g_ffts; }
+
+static void r2c(const oracle_params *p, const double *in, double *out) {
+  g_ffts++;
+  offt_r2c_3d(p->Nx, p->Ny, p->Nz, in, out);
+}
+static void c2r(const oracle_params *p, const double *in, double *out) {
+  g_ffts++;
+  offt_c2r_3d(p->Nx, p->Ny, p->Nz, in, out);
+}
+
+static double det3(const double m[9]) {
+  /* m row-major: m[3*i + j] = component i of column j */
+  return m[0] * (m[4] * m[8] - m[5] * m[7]) - m[1] * (m[3] * m[8] - m[5] * m[6]) +
+         m[2] * (m[3] * m[7] - m[4] * m[6]);
+}
+
+/* R has the lattice vectors as columns (src/lattice.cpp:13-14). */
+static void lattice_matrix(const oracle_params *p, double R[9]) {
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) R[3 * i + j] = p->lat[3 * j + i];
+}
+
+double oracle_dvolume(const oracle_params *p) {
+  double R[9];
+  lattice_matrix(p, R);
+  const int N[3] = {p->Nx, p->Ny, p->Nz};
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) R[3 * i + j] /= N[j];
+  return det3(R); /* fineLat.volume(), src/GridDescription.cpp:12 */
+}
+
+static double volume(const oracle_params *p) {
+  double R[9];
+  lattice_matrix(p, R);
+  return det3(R);
+}
+
+/* B = 2 pi R^{-T}: k = B m  (Lattice::toReciprocal, src/lattice.h:104-106) */
+static void recip_matrix(const oracle_params *p, double B[9]) {
+  double R[9], inv[9];
+  lattice_matrix(p, R);
+  const double d = det3(R);
+  inv[0] = (R[4] * R[8] - R[5] * R[7]) / d;
+  inv[1] = (R[2] * R[7] - R[1] * R[8]) / d;
+  inv[2] = (R[1] * R[5] - R[2] * R[4]) / d;
+  inv[3] = (R[5] * R[6] - R[3] * R[8]) / d;
+  inv[4] = (R[0] * R[8] - R[2] * R[6]) / d;
+  inv[5] = (R[2] * R[3] - R[0] * R[5]) / d;
+  inv[6] = (R[3] * R[7] - R[4] * R[6]) / d;
+  inv[7] = (R[1] * R[6] - R[0] * R[7]) / d;
+  inv[8] = (R[0] * R[4] - R[1] * R[3]) / d;
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) B[3 * i + j] = 2 * M_PI * inv[3 * j + i];
+}
+
+static const double kSpreading = 6.0; /* src/ReciprocalOperators.h:92 */
+
+/* Analytic weights at one k-vector: step (w3), shell (w2) and the radial
+ * factor wv of the vector shells, whose weight is i * k_c * wv. */
+static void weights_at(const double k[3], double R, double dr, double *w3, double *w2,
+                       double *wv) {
+  const double k2 = k[0] * k[0] + k[1] * k[1] + k[2] * k[2];
+  const double kk = sqrt(k2);
+  const double kR = kk * R;
+  if (kR > 1e-3) {
+    const double kdr = kk * dr;
+    const double s = sin(kR), c = cos(kR);
+    const double smear = exp(-kSpreading * kdr * kdr);
+    *w3 = smear * (4 * M_PI) * (s - kR * c) / (kk * kk * kk);
+    *w2 = smear * (4 * M_PI) * R * s / kk;
+    *wv = smear * (4 * M_PI) / (kk * kk) * (R * c - s / kk);
+  } else {
+    const double kR2 = kR * kR;
+    *w3 = (4 * M_PI / 3) * R * R * R *
+          (kR2 * kR2 * kR2 * (-1.0 / 15120) + kR2 * kR2 * (1.0 / 280) + kR2 * (-1.0 / 10) + 1);
+    *w2 = (4 * M_PI) * (R * R) *
+          (-kR2 * kR2 * kR2 * (1.0 / 120 / 6 / 7) + kR2 * kR2 * (1.0 / 120) - kR2 * (1.0 / 6) + 1);
+    *wv = (4 * M_PI) * R * R * R *
+          (kR2 * kR2 * (1.0 / 5040 - 1.0 / 720) + kR2 * (1.0 / 24 - 1.0 / 120) - 1.0 / 3);
+  }
+}
+
+typedef struct {
+  size_t nr, nc;     /* real points, complex points */
+  double dV, V, dr, scale;
+  double *w3, *w2, *wv, *kv; /* per complex point; kv has 3 entries each */
+} kspace;
+
+static void kspace_init(const oracle_params *p, kspace *ks) {
+  const int Nx = p->Nx, Ny = p->Ny, Nz = p->Nz, NzH = Nz / 2 + 1;
+  ks->nr = (size_t)Nx * Ny * Nz;
+  ks->nc = (size_t)Nx * Ny * NzH;
+  ks->dV = oracle_dvolume(p);
+  ks->V = volume(p);
+  ks->dr = pow(ks->dV, 1.0 / 3);
+  ks->scale = ks->dV / ks->V;
+  ks->w3 = (double *)malloc(sizeof(double) * ks->nc);
+  ks->w2 = (double *)malloc(sizeof(double) * ks->nc);
+  ks->wv = (double *)malloc(sizeof(double) * ks->nc);
+  ks->kv = (double *)malloc(sizeof(double) * 3 * ks->nc);
+  double B[9];
+  recip_matrix(p, B);
+  size_t i = 0;
+  for (int x = 0; x < Nx; x++)
+    for (int y = 0; y < Ny; y++)
+      for (int z = 0; z < NzH; z++, i++) {
+        const double m[3] = {(double)(x > Nx / 2 ? x - Nx : x), (double)(y > Ny / 2 ? y - Ny : y),
+                             (double)z};
+        double k[3];
+        for (int c = 0; c < 3; c++) k[c] = B[3 * c] * m[0] + B[3 * c + 1] * m[1] + B[3 * c + 2] * m[2];
+        weights_at(k, p->R, ks->dr, &ks->w3[i], &ks->w2[i], &ks->wv[i]);
+        ks->kv[3 * i] = k[0];
+        ks->kv[3 * i + 1] = k[1];
+        ks->kv[3 * i + 2] = k[2];
+      }
+}
+
+static void kspace_free(kspace *ks) {
+  free(ks->w3);
+  free(ks->w2);
+  free(ks->wv);
+  free(ks->kv);
+}
+
+/* out5 = n3, n2, n2x, n2y, n2z */
+static void weighted(const oracle_params *p, const kspace *ks, const double *n, double *out5) {
+  double *nk = (double *)malloc(sizeof(double) * 2 * ks->nc);
+  double *tk = (double *)malloc(sizeof(double) * 2 * ks->nc);
+  r2c(p, n, nk);
+  for (int a = 0; a < 5; a++) {
+    for (size_t i = 0; i < ks->nc; i++) {
+      const double re = nk[2 * i] * ks->scale, im = nk[2 * i + 1] * ks->scale;
+      if (a < 2) {
+        const double w = a == 0 ? ks->w3[i] : ks->w2[i];
+        tk[2 * i] = re * w;
+        tk[2 * i + 1] = im * w;
+      } else {
+        const double w = ks->kv[3 * i + (a - 2)] * ks->wv[i]; /* weight = i*w */
+        tk[2 * i] = -im * w;
+        tk[2 * i + 1] = re * w;
+      }
+    }
+    c2r(p, tk, out5 + (size_t)a * ks->nr);
+  }
+  free(nk);
+  free(tk);
+}
+
+void oracle_weighted(const oracle_params *p, const double *n, double *out5) {
+  kspace ks;
+  kspace_init(p, &ks);
+  weighted(p, &ks, n, out5);
+  kspace_free(&ks);
+}
+
+/* S(eta) = (eta + (1-eta)^2 ln(1-eta)) / eta^2 and dS/deta.  The phi3
+ * prefactor is S / (36 pi (1-eta)^2).  Series for |eta| < 1e-2:
+ * S = 3/2 - sum_{j>=1} 2 eta^j / (j (j+1) (j+2)). */
+static void phi3_S(double eta, double *S, double *dS) {
+  if (fabs(eta) < 1e-2) {
+    double s = 1.5, ds = 0, pw = 1; /* pw = eta^(j-1) */
+    for (int j = 1; j <= 12; j++) {
+      const double c = 2.0 / ((double)j * (j + 1) * (j + 2));
+      ds -= c * j * pw;
+      pw *= eta;
+      s -= c * pw;
+    }
+    *S = s;
+    *dS = ds;
+  } else {
+    const double l = log(1 - eta);
+    const double g = eta + (1 - eta) * (1 - eta) * l;
+    const double dg = eta - 2 * (1 - eta) * l; /* d/deta of g */
+    *S = g / (eta * eta);
+    *dS = (dg * eta - 2 * g) / (eta * eta * eta);
+  }
+}
+
+/* White Bear (no tensor) excess free-energy density per kT, split into its
+ * three terms, and the partial derivatives with respect to n3, n2, n2v_c. */
+static void phi_wb(double R, double n3, double n2, double vx, double vy, double vz,
+                   double phi[3], double d[5]) {
+  const double v2 = vx * vx + vy * vy + vz * vz;
+  const double omn3 = 1 - n3;
+  const double l = log(omn3);
+  const double four_pi_r = 4 * M_PI * R, four_pi_r2 = 4 * M_PI * R * R;
+  double S, dS;
+  phi3_S(n3, &S, &dS);
+  const double f3 = S / (36 * M_PI * omn3 * omn3);
+  const double df3 = (dS * omn3 + 2 * S) / (36 * M_PI * omn3 * omn3 * omn3);
+  const double t3 = n2 * (n2 * n2 - 3 * v2);
+  phi[0] = f3 * t3;                            /* phi3 */
+  phi[1] = -n2 * l / four_pi_r2;               /* phi1 */
+  phi[2] = (n2 * n2 - v2) / (four_pi_r * omn3); /* phi2 */
+  d[0] = n2 / (four_pi_r2 * omn3) + (n2 * n2 - v2) / (four_pi_r * omn3 * omn3) + df3 * t3;
+  d[1] = -l / four_pi_r2 + 2 * n2 / (four_pi_r * omn3) + f3 * 3 * (n2 * n2 - v2);
+  const double cv = -2 / (four_pi_r * omn3) - 6 * f3 * n2;
+  d[2] = cv * vx;
+  d[3] = cv * vy;
+  d[4] = cv * vz;
+}
+
+static double nQ_of(double kT) {
+  /* find_nQ, src/IdealGas.cpp:54-59: (m kT / 2 pi)^(3/2), m = water mass */
+  const double x = 18.01528 * 1822.8885 * kT / (2 * M_PI);
+  return x * sqrt(x);
+}
+
+/* Shared energy (+ gradient) evaluation. */
+static double eval(const oracle_params *p, const double *n, const double *V, const double *mask,
+                   double *grad, double *terms6) {
+  kspace ks;
+  kspace_init(p, &ks);
+  const size_t nr = ks.nr, nc = ks.nc;
+  const double kT = p->kT, dV = ks.dV;
+  double t[ORACLE_NTERMS] = {0, 0, 0, 0, 0, 0};
+  double *wd = NULL, *part = NULL;
+  if (p->terms & ORACLE_HS) {
+    wd = (double *)malloc(sizeof(double) * 5 * nr);
+    weighted(p, &ks, n, wd);
+    if (grad) part = (double *)malloc(sizeof(double) * 5 * nr);
+    for (size_t i = 0; i < nr; i++) {
+      double phi[3], d[5];
+      phi_wb(p->R, wd[i], wd[nr + i], wd[2 * nr + i], wd[3 * nr + i], wd[4 * nr + i], phi, d);
+      t[0] += kT * phi[0];
+      t[1] += kT * phi[1];
+      t[2] += kT * phi[2];
+      if (part)
+        for (int a = 0; a < 5; a++) part[a * nr + i] = dV * kT * d[a];
+    }
+  }
+  const double nQ = nQ_of(kT);
+  for (size_t i = 0; i < nr; i++) {
+    if (p->terms & ORACLE_IDEAL) t[3] += n[i] == 0 ? 0.0 : kT * n[i] * (log(n[i] / nQ) - 1);
+    if (p->terms & ORACLE_MU) t[4] += p->mu * n[i];
+    if (p->terms & ORACLE_VEXT) t[5] += V[i] * n[i];
+  }
+  double E = 0;
+  for (int a = 0; a < ORACLE_NTERMS; a++) {
+    t[a] *= dV;
+    E += t[a];
+  }
+  if (terms6) memcpy(terms6, t, sizeof(t));
+  if (grad) {
+    memset(grad, 0, sizeof(double) * nr);
+    if (part) {
+      double *pk = (double *)malloc(sizeof(double) * 2 * nc);
+      double *gk = (double *)calloc(2 * nc, sizeof(double));
+      for (int a = 0; a < 5; a++) {
+        r2c(p, part + a * nr, pk);
+        for (size_t i = 0; i < nc; i++) {
+          const double re = pk[2 * i] * ks.scale, im = pk[2 * i + 1] * ks.scale;
+          if (a < 2) {
+            const double w = a == 0 ? ks.w3[i] : ks.w2[i];
+            gk[2 * i] += re * w;
+            gk[2 * i + 1] += im * w;
+          } else {
+            /* adjoint of an odd weight i*w is -i*w */
+            const double w = ks.kv[3 * i + (a - 2)] * ks.wv[i];
+            gk[2 * i] += im * w;
+            gk[2 * i + 1] -= re * w;
+          }
+        }
+      }
+      c2r(p, gk, grad);
+      free(pk);
+      free(gk);
+    }
+    for (size_t i = 0; i < nr; i++) {
+      double loc = 0;
+      if (p->terms & ORACLE_IDEAL) loc += kT * log(n[i] / nQ);
+      if (p->terms & ORACLE_MU) loc += p->mu;
+      if (p->terms & ORACLE_VEXT) loc += V[i];
+      double g = grad[i] + dV * loc;
+      if (p->terms & ORACLE_MASK) g = mask[i] == 0 ? 0.0 : mask[i] * g;
+      grad[i] = g;
+    }
+  }
+  free(wd);
+  free(part);
+  kspace_free(&ks);
+  return E;
+}
+
+double oracle_energy(const oracle_params *p, const double *n, const double *V, const double *mask,
+                     double *terms6) {
+  return eval(p, n, V, mask, NULL, terms6);
+}
+
+double oracle_energy_grad(const oracle_params *p, const double *n, const double *V,
+                          const double *mask, double *grad, double *terms6) {
+  return eval(p, n, V, mask, grad, terms6);
+}
+
+double oracle_homogeneous(double R, double kT, double mu, double nb) {
+  const double n3 = nb * (4 * M_PI / 3) * R * R * R, n2 = nb * 4 * M_PI * R * R;
+  double phi[3], d[5];
+  phi_wb(R, n3, n2, 0, 0, 0, phi, d);
+  return kT * (phi[0] + phi[1] + phi[2]) + kT * nb * (log(nb / nQ_of(kT)) - 1) + mu * nb;
+}
+
+double oracle_find_mu(double R, double kT, double nb) {
+  const double n3 = nb * (4 * M_PI / 3) * R * R * R, n2 = nb * 4 * M_PI * R * R;
+  double phi[3], d[5];
+  phi_wb(R, n3, n2, 0, 0, 0, phi, d);
+  const double dfdn = kT * (d[0] * (4 * M_PI / 3) * R * R * R + d[1] * 4 * M_PI * R * R) +
+                      kT * log(nb / nQ_of(kT));
+  return -dfdn;
+}
+
+/* ---------------------------------------------------------------------- */
+/* Minimisers                                                              */
+
+static double dot(const double *a, const double *b, size_t n) {
+  double s = 0;
+  for (size_t i = 0; i < n; i++) s += a[i] * b[i];
+  return s;
+}
+
+typedef struct {
+  const oracle_params *p;
+  const double *V, *mask;
+  double *x;
+  size_t n;
+  /* energy cache: the reference recomputes energy() on every call
+   * (src/Minimizer.h:52); caching a value of the same x changes nothing. */
+  int e_valid;
+  double e;
+  double *g;
+  int g_valid;
+} mstate;
+
+static double m_energy(mstate *m) {
+  if (!m->e_valid) {
+    m->e = oracle_energy(m->p, m->x, m->V, m->mask, NULL);
+    m->e_valid = 1;
+  }
+  return m->e;
+}
+static const double *m_grad(mstate *m) {
+  if (!m->g_valid) {
+    m->e = oracle_energy_grad(m->p, m->x, m->V, m->mask, m->g, NULL);
+    m->e_valid = 1;
+    m->g_valid = 1;
+  }
+  return m->g;
+}
+static void m_invalidate(mstate *m) {
+  m->e_valid = 0;
+  m->g_valid = 0;
+}
+static void m_axpy(mstate *m, double a, const double *d) {
+  for (size_t i = 0; i < m->n; i++) m->x[i] += a * d[i];
+  m_invalidate(m);
+}
+static int better(double a, double b) { return a < b || (b != b); } /* src/Minimizer.h:161-163 */
+
+/* QuadraticLineMinimizerType::improve_energy, src/QuadraticLineMinimizer.cpp:27-198 */
+static void quad_linmin(mstate *m, const double *dir, double slope, double *step) {
+  const double E0 = m_energy(m);
+  if (E0 != E0) return;
+  if (E0 > 1e307 || E0 < -1e307) return;
+  if (slope != slope) return;
+  if (slope == 0) return;
+  if (slope * (*step) > 0) *step *= -1;
+  double step1 = *step;
+  m_axpy(m, step1, dir);
+  double Etried = -137;
+  do {
+    step1 *= 0.5;
+    m_axpy(m, -step1, dir);
+    if (m_energy(m) == Etried) break;
+    Etried = m_energy(m);
+  } while (better(E0, m_energy(m)));
+  const double E1 = m_energy(m);
+  const double curvature = 2.0 * (E1 - E0 - step1 * slope) / (step1 * step1);
+  const double step2 = -slope / curvature;
+  if (curvature <= 0.0) {
+    if (better(E0, E1)) {
+      m_axpy(m, -step1, dir);
+      return;
+    } else {
+      double Ebest = E0;
+      while (m_energy(m) <= Ebest) {
+        Ebest = m_energy(m);
+        m_axpy(m, step1, dir);
+        step1 *= 2;
+      }
+      step1 *= 0.5;
+      m_axpy(m, -step1, dir);
+      *step = step1;
+    }
+  } else if (E1 == E0) {
+    do {
+      m_axpy(m, -step1, dir);
+      step1 *= 2;
+      m_axpy(m, step1, dir);
+    } while (m_energy(m) == E0);
+    if (m_energy(m) > E0) {
+      m_axpy(m, -step1, dir);
+      step1 = 0;
+    } else if (m_energy(m) != m_energy(m)) {
+      m_axpy(m, -step1, dir);
+      step1 = 0;
+    }
+  } else {
+    *step = step2;
+    m_axpy(m, step2 - step1, dir);
+    if (better(E1, m_energy(m)) && better(E1, E0)) {
+      m_axpy(m, -(step2 - step1), dir);
+    } else if (m_energy(m) > E0) {
+      m_axpy(m, -step2, dir);
+      return;
+    }
+  }
+}
+
+int oracle_cg_quadratic(const oracle_params *p, const double *V, const double *mask,
+                        double *n_inout, int iters, double step, double *energies) {
+  mstate m = {p, V, mask, n_inout, (size_t)p->Nx * p->Ny * p->Nz, 0, 0, NULL, 0};
+  m.g = (double *)malloc(sizeof(double) * m.n);
+  double *direction = (double *)calloc(m.n, sizeof(double));
+  double *oldgrad = (double *)calloc(m.n, sizeof(double));
+  double *g = (double *)malloc(sizeof(double) * m.n);
+  double oldgradsqr = 0;
+  int it = 0;
+  for (; it < iters; it++) {
+    /* ConjugateGradientType::improve_energy, src/ConjugateGradient.cpp:59-108 */
+    const double E0 = m_energy(&m);
+    int more;
+    if (E0 != E0) {
+      more = 0;
+    } else {
+      const double *gr = m_grad(&m);
+      for (size_t i = 0; i < m.n; i++) g[i] = -gr[i];
+      double num = 0;
+      for (size_t i = 0; i < m.n; i++) num += g[i] * (g[i] - oldgrad[i]);
+      double beta = num / oldgradsqr;
+      memcpy(oldgrad, g, sizeof(double) * m.n);
+      if (beta < 0 || beta != beta || oldgradsqr == 0) beta = 0;
+      oldgradsqr = dot(oldgrad, oldgrad, m.n);
+      for (size_t i = 0; i < m.n; i++) direction[i] = g[i] + beta * direction[i];
+      double gdotd = dot(oldgrad, direction, m.n);
+      if (gdotd < 0) {
+        memcpy(direction, oldgrad, sizeof(double) * m.n);
+        gdotd = dot(oldgrad, direction, m.n);
+      }
+      quad_linmin(&m, direction, -gdotd, &step);
+      more = m_energy(&m) < E0;
+    }
+    energies[it] = m_energy(&m);
+    if (!more) {
+      it++;
+      break;
+    }
+  }
+  free(m.g);
+  free(direction);
+  free(oldgrad);
+  free(g);
+  return it;
+}
+
+/* Derivative line search along d from x (slope s0 = g.d < 0): bracketing
+ * secant on s(a) = grad(x + a d).d until |s| <= 0.1 |s0|.  On return x and
+ * m->g hold the accepted point.  Returns the number of evaluations, or -1. */
+static int secant_linmin(mstate *m, const double *d, double E0, double s0, double *alpha) {
+  double lo = 0, s_lo = s0, hi = -1, s_hi = 0;
+  double plo = 0, s_plo = s0; /* previous lower point, for extrapolation */
+  double a = *alpha, at = 0;  /* at = where x currently sits */
+  int evals = 0;
+  for (int it = 0; it < 40; it++) {
+    m_axpy(m, a - at, d);
+    at = a;
+    const double *g = m_grad(m);
+    evals++;
+    const double E = m->e;
+    const double s = dot(g, d, m->n);
+    if (!(E == E) || !(s == s) || fabs(E) > 1e307) {
+      hi = a;
+      s_hi = 1e300;
+      a = lo + 0.5 * (a - lo);
+      continue;
+    }
+    if (fabs(s) <= 0.1 * fabs(s0) && E <= E0 + 1e-12 * fabs(E0)) {
+      *alpha = a;
+      return evals;
+    }
+    if (s < 0 && E <= E0 + 1e-12 * fabs(E0)) {
+      plo = lo;
+      s_plo = s_lo;
+      lo = a;
+      s_lo = s;
+      if (hi < 0) {
+        double an = 4 * a;
+        if (s - s_plo > 0) {
+          an = a - s * (a - plo) / (s - s_plo);
+          if (an < 1.5 * a) an = 1.5 * a;
+          if (an > 4 * a) an = 4 * a;
+        }
+        a = an;
+        continue;
+      }
+    } else {
+      hi = a;
+      s_hi = s > 0 ? s : 1e300; /* energy rose with negative slope: treat as overshoot */
+    }
+    /* bracketed: secant between lo and hi, kept inside the bracket */
+    double an = 0.5 * (lo + hi);
+    if (s_hi < 1e299 && s_hi - s_lo > 0) an = lo - s_lo * (hi - lo) / (s_hi - s_lo);
+    const double w = hi - lo;
+    if (an < lo + 0.01 * w) an = lo + 0.01 * w;
+    if (an > hi - 0.01 * w) an = hi - 0.01 * w;
+    a = an;
+  }
+  return -1;
+}
+
+int oracle_cg_solve(const oracle_params *p, const double *V, const double *mask, double *n_inout,
+                    double gtol, int maxiter, double step, double *out3) {
+  mstate m = {p, V, mask, n_inout, (size_t)p->Nx * p->Ny * p->Nz, 0, 0, NULL, 0};
+  m.g = (double *)malloc(sizeof(double) * m.n);
+  double *d = (double *)calloc(m.n, sizeof(double));
+  double *gold = (double *)calloc(m.n, sizeof(double));
+  double goldsqr = 0, s_prev = 0, alpha = step;
+  int evals = 0, it = 0;
+  m_grad(&m);
+  evals++;
+  for (; it < maxiter; it++) {
+    const double *g = m.g;
+    const double gg = dot(g, g, m.n);
+    if (sqrt(gg) < gtol) break;
+    /* Polak-Ribiere with reset, as src/ConjugateGradient.cpp:77-91 */
+    double beta = 0;
+    if (goldsqr > 0) {
+      double num = 0;
+      for (size_t i = 0; i < m.n; i++) num += g[i] * (g[i] - gold[i]);
+      beta = num / goldsqr;
+      if (beta < 0 || beta != beta) beta = 0;
+    }
+    for (size_t i = 0; i < m.n; i++) d[i] = -g[i] + beta * d[i];
+    double s0 = dot(g, d, m.n);
+    if (!(s0 < 0)) {
+      for (size_t i = 0; i < m.n; i++) d[i] = -g[i];
+      s0 = -gg;
+    }
+    memcpy(gold, g, sizeof(double) * m.n);
+    goldsqr = gg;
+    if (it > 0 && s0 != 0) alpha *= s_prev / s0;
+    s_prev = s0;
+    const double E0 = m.e;
+    const int ne = secant_linmin(&m, d, E0, s0, &alpha);
+    if (ne < 0) {
+      evals += 40;
+      break;
+    }
+    evals += ne;
+  }
+  if (out3) {
+    out3[0] = m.e;
+    out3[1] = sqrt(dot(m.g, m.g, m.n));
+    out3[2] = evals;
+  }
+  free(m.g);
+  free(d);
+  free(gold);
+  return it;
+}

@@ -1,0 +1,230 @@
+"""ctypes bindings for the oracle -- TEST INFRASTRUCTURE ONLY.
+
+Two CPU libraries live under oracle/:
+
+* ``liboracle.so`` -- the plain-C restatement of the FMT + CG hot path
+  (``deft_oracle.c``), built everywhere by ``make -C oracle liboracle``;
+* ``_ref/libdeft_ref.so`` -- the unmodified reference sources plus the
+  project's FFTW3-API shim, built only where the reference checkout exists
+  (``make -C oracle ref``).
+
+Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline /
+reference arm may import this module, as the checker.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_SO = os.path.join(HERE, "liboracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libdeft_ref.so")
+
+HS, IDEAL, MU, VEXT, MASK = 1, 2, 4, 8, 16
+NTERMS = 6
+TERM_NAMES = ("phi3", "phi1", "phi2", "ideal_gas", "chemical_potential", "external_potential")
+
+_dp = ctypes.POINTER(ctypes.c_double)
+
+
+def _ptr(a):
+    if a is None:
+        return None
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(_dp)
+
+
+class _Params(ctypes.Structure):
+    _fields_ = [
+        ("Nx", ctypes.c_int), ("Ny", ctypes.c_int), ("Nz", ctypes.c_int),
+        ("lat", ctypes.c_double * 9),
+        ("R", ctypes.c_double), ("kT", ctypes.c_double), ("mu", ctypes.c_double),
+        ("terms", ctypes.c_int),
+    ]
+
+
+def build(ref=False):
+    """Compile liboracle.so (and, if ref and the checkout exists, the reference)."""
+    import subprocess
+    targets = ["liboracle"]
+    if ref:
+        targets.append("ref")
+    subprocess.check_call(["make", "-s", "-C", HERE] + targets)
+
+
+_lib = None
+_ref = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(ORACLE_SO):
+            build()
+        L = ctypes.CDLL(ORACLE_SO)
+        P = ctypes.POINTER(_Params)
+        L.oracle_dvolume.restype = ctypes.c_double
+        L.oracle_dvolume.argtypes = [P]
+        L.oracle_weighted.argtypes = [P, _dp, _dp]
+        L.oracle_energy.restype = ctypes.c_double
+        L.oracle_energy.argtypes = [P, _dp, _dp, _dp, _dp]
+        L.oracle_energy_grad.restype = ctypes.c_double
+        L.oracle_energy_grad.argtypes = [P, _dp, _dp, _dp, _dp, _dp]
+        L.oracle_find_mu.restype = ctypes.c_double
+        L.oracle_find_mu.argtypes = [ctypes.c_double] * 3
+        L.oracle_homogeneous.restype = ctypes.c_double
+        L.oracle_homogeneous.argtypes = [ctypes.c_double] * 4
+        L.oracle_cg_quadratic.restype = ctypes.c_int
+        L.oracle_cg_quadratic.argtypes = [P, _dp, _dp, _dp, ctypes.c_int, ctypes.c_double, _dp]
+        L.oracle_cg_solve.restype = ctypes.c_int
+        L.oracle_cg_solve.argtypes = [P, _dp, _dp, _dp, ctypes.c_double, ctypes.c_int,
+                                      ctypes.c_double, _dp]
+        L.oracle_fft_count.restype = ctypes.c_longlong
+        L.offt_r2c_3d.argtypes = [ctypes.c_int] * 3 + [_dp, _dp]
+        L.offt_c2r_3d.argtypes = [ctypes.c_int] * 3 + [_dp, _dp]
+        _lib = L
+    return _lib
+
+
+def ref_available():
+    return os.path.exists(REF_SO)
+
+
+def ref():
+    """The unmodified reference build (only where it was compiled)."""
+    global _ref
+    if _ref is None:
+        L = ctypes.CDLL(REF_SO)
+        L.ref_eval.restype = ctypes.c_int
+        L.ref_eval.argtypes = [_dp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                               ctypes.c_double, ctypes.c_double, ctypes.c_int, _dp, _dp, _dp,
+                               _dp, _dp, _dp]
+        L.ref_weighted.argtypes = [_dp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                   ctypes.c_double, _dp, _dp]
+        L.ref_find_mu.restype = ctypes.c_double
+        L.ref_find_mu.argtypes = [ctypes.c_double] * 3
+        L.ref_homogeneous.restype = ctypes.c_double
+        L.ref_homogeneous.argtypes = [ctypes.c_double] * 4
+        L.ref_cg.restype = ctypes.c_int
+        L.ref_cg.argtypes = [_dp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                             ctypes.c_double, ctypes.c_double, ctypes.c_int, _dp, _dp, _dp,
+                             ctypes.c_int, ctypes.c_double, _dp]
+        L.ref_fd_test.restype = ctypes.c_int
+        L.ref_fd_test.argtypes = [_dp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                  ctypes.c_double, ctypes.c_double, ctypes.c_int, _dp, _dp]
+        L.ref_fft_count.restype = ctypes.c_longlong
+        _ref = L
+    return _ref
+
+
+class Problem:
+    """One evaluation setting: lattice (rows a1, a2, a3), grid, R, kT, mu, terms."""
+
+    def __init__(self, lat, N, R=1.0, kT=1.0, mu=0.0, terms=HS | IDEAL | MU, V=None, mask=None):
+        self.lat = np.ascontiguousarray(np.asarray(lat, dtype=np.float64).reshape(9))
+        self.N = tuple(int(v) for v in N)
+        self.R, self.kT, self.mu, self.terms = float(R), float(kT), float(mu), int(terms)
+        self.V = None if V is None else np.ascontiguousarray(V, dtype=np.float64).reshape(-1)
+        self.mask = None if mask is None else np.ascontiguousarray(mask, dtype=np.float64).reshape(-1)
+        if self.V is not None:
+            self.terms |= VEXT
+        if self.mask is not None:
+            self.terms |= MASK
+
+    @property
+    def size(self):
+        return self.N[0] * self.N[1] * self.N[2]
+
+    def params(self):
+        p = _Params()
+        p.Nx, p.Ny, p.Nz = self.N
+        for i in range(9):
+            p.lat[i] = self.lat[i]
+        p.R, p.kT, p.mu, p.terms = self.R, self.kT, self.mu, self.terms
+        return p
+
+    # -- restatement -------------------------------------------------------
+    def dvolume(self):
+        return lib().oracle_dvolume(ctypes.byref(self.params()))
+
+    def weighted(self, n):
+        n = np.ascontiguousarray(n, dtype=np.float64).reshape(-1)
+        out = np.empty(5 * self.size)
+        lib().oracle_weighted(ctypes.byref(self.params()), _ptr(n), _ptr(out))
+        return out.reshape(5, -1)
+
+    def energy(self, n, terms=False):
+        n = np.ascontiguousarray(n, dtype=np.float64).reshape(-1)
+        t = np.zeros(NTERMS)
+        E = lib().oracle_energy(ctypes.byref(self.params()), _ptr(n), _ptr(self.V),
+                                _ptr(self.mask), _ptr(t))
+        return (E, t) if terms else E
+
+    def energy_grad(self, n, terms=False):
+        n = np.ascontiguousarray(n, dtype=np.float64).reshape(-1)
+        g = np.empty(self.size)
+        t = np.zeros(NTERMS)
+        E = lib().oracle_energy_grad(ctypes.byref(self.params()), _ptr(n), _ptr(self.V),
+                                     _ptr(self.mask), _ptr(g), _ptr(t))
+        return (E, g, t) if terms else (E, g)
+
+    def cg_quadratic(self, n, iters, step=0.1):
+        x = np.array(n, dtype=np.float64).reshape(-1)
+        e = np.zeros(iters)
+        k = lib().oracle_cg_quadratic(ctypes.byref(self.params()), _ptr(self.V), _ptr(self.mask),
+                                      _ptr(x), iters, step, _ptr(e))
+        return x, e[:k]
+
+    def cg_solve(self, n, gtol=1e-9, maxiter=10000, step=1.0):
+        x = np.array(n, dtype=np.float64).reshape(-1)
+        out = np.zeros(3)
+        it = lib().oracle_cg_solve(ctypes.byref(self.params()), _ptr(self.V), _ptr(self.mask),
+                                   _ptr(x), gtol, maxiter, step, _ptr(out))
+        return x, {"iters": it, "energy": out[0], "gnorm": out[1], "evals": int(out[2])}
+
+    # -- unmodified reference ---------------------------------------------
+    def ref_energy_grad(self, n, grad=True):
+        n = np.ascontiguousarray(n, dtype=np.float64).reshape(-1)
+        E = ctypes.c_double(0)
+        t = np.zeros(8)
+        g = np.empty(self.size) if grad else None
+        nt = ref().ref_eval(_ptr(self.lat), *self.N, self.R, self.kT, self.mu, self.terms,
+                            _ptr(n), _ptr(self.V), _ptr(self.mask), ctypes.byref(E), _ptr(t), _ptr(g))
+        return E.value, g, t[:nt]
+
+    def ref_weighted(self, n):
+        n = np.ascontiguousarray(n, dtype=np.float64).reshape(-1)
+        out = np.empty(5 * self.size)
+        ref().ref_weighted(_ptr(self.lat), *self.N, self.R, _ptr(n), _ptr(out))
+        return out.reshape(5, -1)
+
+    def ref_cg(self, n, iters, step=0.1):
+        x = np.array(n, dtype=np.float64).reshape(-1)
+        e = np.zeros(iters)
+        k = ref().ref_cg(_ptr(self.lat), *self.N, self.R, self.kT, self.mu, self.terms,
+                         _ptr(self.V), _ptr(self.mask), _ptr(x), iters, step, _ptr(e))
+        return x, e[:k]
+
+
+def find_mu(R, kT, nb):
+    return lib().oracle_find_mu(R, kT, nb)
+
+
+def homogeneous(R, kT, mu, nb):
+    return lib().oracle_homogeneous(R, kT, mu, nb)
+
+
+def r2c_3d(x):
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    Nx, Ny, Nz = x.shape
+    out = np.empty((Nx, Ny, Nz // 2 + 1), dtype=np.complex128)
+    lib().offt_r2c_3d(Nx, Ny, Nz, _ptr(x), out.ctypes.data_as(_dp))
+    return out
+
+
+def c2r_3d(c, Nz):
+    c = np.ascontiguousarray(c, dtype=np.complex128)
+    Nx, Ny, _ = c.shape
+    out = np.empty((Nx, Ny, Nz))
+    lib().offt_c2r_3d(Nx, Ny, Nz, c.ctypes.data_as(_dp), _ptr(out))
+    return out

@@ -1,0 +1,162 @@
+// C-ABI wrapper around the UNMODIFIED reference sources (droundy/deft), built
+// by oracle/Makefile into oracle/_ref/libdeft_ref.so.  Test infrastructure
+// only: it runs the reference's own Functional tree so that the plain-C
+// restatement (oracle/deft_oracle.c) and the golden fixtures under
+// tests/golden/ are pinned to the reference's outputs.  FFTs go through
+// oracle/fftw_shim.c.
+//
+// The composed functional mirrors the drivers, e.g.
+// papers/contact/figs/walls.cpp:86-98:
+//   f = [constrain(mask,] HardSpheresWBnotensor(R) [+ IdealGas()]
+//       [+ ChemicalPotential(mu)] [+ ExternalPotential(V)] [)]
+// with HardSpheresWBnotensor at src/HardSpheres.cpp:137-159, IdealGas at
+// src/IdealGas.cpp:68-72, ChemicalPotential at src/ChemicalPotential.cpp:19-22,
+// ExternalPotential at src/ExternalPotential.cpp:19-21, constrain at
+// src/Functional.cpp:834-838.
+#include "Functionals.h"
+#include "Grid.h"
+#include "LineMinimizer.h"
+#include "Minimizer.h"
+#include "equation-of-state.h"
+
+#include <stdio.h>
+
+extern "C" long long deft_shim_fft_count(void);
+
+enum {
+  REF_HS = 1,
+  REF_IDEAL = 2,
+  REF_MU = 4,
+  REF_VEXT = 8,
+  REF_MASK = 16,
+};
+
+static Lattice make_lat(const double *lat) {
+  return Lattice(Cartesian(lat[0], lat[1], lat[2]), Cartesian(lat[3], lat[4], lat[5]),
+                 Cartesian(lat[6], lat[7], lat[8]));
+}
+
+static Functional make_sum(const GridDescription &gd, double R, double mu, int terms,
+                           const double *V) {
+  Functional f(0.0);
+  if (terms & REF_HS) f = HardSpheresWBnotensor(R);
+  if (terms & REF_IDEAL) f = f + IdealGas();
+  if (terms & REF_MU) f = f + ChemicalPotential(mu);
+  if (terms & REF_VEXT) {
+    VectorXd v(gd.NxNyNz);
+    for (int i = 0; i < gd.NxNyNz; i++) v[i] = V[i];
+    f = f + ExternalPotential(v);
+  }
+  return f;
+}
+
+extern "C" {
+
+long long ref_fft_count(void) { return deft_shim_fft_count(); }
+
+// Energy (Functional::integral, src/Functional.h:131-143), per-term energies
+// in sum order (phi3, phi1, phi2 for the hard spheres, then ideal gas, mu,
+// external potential -- src/HardSpheres.cpp:156 fixes the first three), and,
+// if grad != NULL, Functional::integralgrad (src/Functional.h:147-149) of the
+// (optionally constrained) functional.  Returns the number of terms written.
+int ref_eval(const double *lat, int Nx, int Ny, int Nz, double R, double kT, double mu,
+             int terms, const double *n, const double *V, const double *mask,
+             double *E_out, double *terms_out, double *grad) {
+  GridDescription gd(make_lat(lat), Nx, Ny, Nz);
+  Grid x(gd);
+  for (int i = 0; i < gd.NxNyNz; i++) x[i] = n[i];
+  Functional sum = make_sum(gd, R, mu, terms, V);
+  *E_out = sum.integral(kT, x);
+  int nt = 0;
+  for (const Functional *t = &sum; t; t = t->next()) {
+    if (terms_out) terms_out[nt] = t->justMeIntegral(gd, kT, x);
+    nt++;
+  }
+  if (grad) {
+    Functional f = sum;
+    if (terms & REF_MASK) {
+      Grid m(gd);
+      for (int i = 0; i < gd.NxNyNz; i++) m[i] = mask[i];
+      f = constrain(m, sum);
+    }
+    VectorXd g(gd.NxNyNz);
+    g.setZero();
+    f.integralgrad(kT, gd, x, &g);
+    for (int i = 0; i < gd.NxNyNz; i++) grad[i] = g[i];
+  }
+  return nt;
+}
+
+// The five weighted densities n3, n2, n2x, n2y, n2z of the White Bear
+// functional: StepConvolve / ShellConvolve / x,y,zShellConvolve
+// (src/Gaussian.cpp:82-102), each ifft(w(k) * fft(n)) (src/Functional.h:376-381).
+void ref_weighted(const double *lat, int Nx, int Ny, int Nz, double R, const double *n,
+                  double *out5) {
+  GridDescription gd(make_lat(lat), Nx, Ny, Nz);
+  Grid x(gd);
+  for (int i = 0; i < gd.NxNyNz; i++) x[i] = n[i];
+  Functional ops[5] = {StepConvolve(R), ShellConvolve(R), xShellConvolve(R),
+                       yShellConvolve(R), zShellConvolve(R)};
+  for (int a = 0; a < 5; a++) {
+    VectorXd w = ops[a](gd, 1.0, x);
+    for (int i = 0; i < gd.NxNyNz; i++) out5[(size_t)a * gd.NxNyNz + i] = w[i];
+  }
+}
+
+// Bulk chemical potential as the drivers compute it
+// (papers/contact/figs/walls.cpp:86-87, src/equation-of-state.cpp:189-192):
+// find_chemical_potential(OfEffectivePotential(HS(R) + IdealGas()), kT, nb).
+double ref_find_mu(double R, double kT, double nb) {
+  Functional f = OfEffectivePotential(HardSpheresWBnotensor(R) + IdealGas());
+  return find_chemical_potential(f, kT, nb);
+}
+
+// Homogeneous free-energy density of HS(R)+IdealGas()+ChemicalPotential(mu)
+// at density nb (Functional::operator()(kT, double), src/Functional.h:150-156).
+double ref_homogeneous(double R, double kT, double mu, double nb) {
+  Functional f = HardSpheresWBnotensor(R) + IdealGas() + ChemicalPotential(mu);
+  return f(kT, nb);
+}
+
+// Runs `iters` calls of ConjugateGradient(...).improve_energy()
+// (src/ConjugateGradient.cpp:59-108) with QuadraticLineMinimizer
+// (src/QuadraticLineMinimizer.cpp:27-198) on the constrained functional,
+// writing the energy after each call into energies[] and the final density
+// into n_inout.  Returns the number of calls made before improve_energy
+// returned false (or iters).
+int ref_cg(const double *lat, int Nx, int Ny, int Nz, double R, double kT, double mu,
+           int terms, const double *V, const double *mask, double *n_inout, int iters,
+           double step, double *energies) {
+  GridDescription gd(make_lat(lat), Nx, Ny, Nz);
+  Functional f = make_sum(gd, R, mu, terms, V);
+  if (terms & REF_MASK) {
+    Grid m(gd);
+    for (int i = 0; i < gd.NxNyNz; i++) m[i] = mask[i];
+    f = constrain(m, f);
+  }
+  Grid x(gd);
+  for (int i = 0; i < gd.NxNyNz; i++) x[i] = n_inout[i];
+  Minimizer min = ConjugateGradient(f, gd, kT, &x, QuadraticLineMinimizer, step);
+  int i = 0;
+  for (; i < iters; i++) {
+    bool more = min.improve_energy(false);
+    energies[i] = min.energy();
+    if (!more) { i++; break; }
+  }
+  for (int j = 0; j < gd.NxNyNz; j++) n_inout[j] = x[j];
+  return i;
+}
+
+// Functional::run_finite_difference_test (src/Functional.cpp:104-213) on the
+// unconstrained sum; returns its failure count (0 = pass).
+int ref_fd_test(const double *lat, int Nx, int Ny, int Nz, double R, double kT, double mu,
+                int terms, const double *V, const double *n) {
+  GridDescription gd(make_lat(lat), Nx, Ny, Nz);
+  Functional f = make_sum(gd, R, mu, terms, V);
+  Grid x(gd);
+  for (int i = 0; i < gd.NxNyNz; i++) x[i] = n[i];
+  fflush(stdout);
+  return f.run_finite_difference_test("oracle", kT, x);
+}
+
+}  // extern "C"

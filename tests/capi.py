@@ -1,0 +1,126 @@
+"""Thin test-side helpers that call the C ABI (include/deft_gb300.h) directly
+through ctypes with numpy buffers."""
+import ctypes
+
+import numpy as np
+
+from deft_gb300 import _lib
+from deft_gb300._lib import check
+
+
+class Ctx:
+    def __init__(self, device=0):
+        self.L = _lib.load()
+        h = ctypes.c_void_p()
+        check(self.L.deft_ctx_create(device, ctypes.byref(h)))
+        self.h = h
+
+    def close(self):
+        self.L.deft_ctx_destroy(self.h)
+
+
+class Grid:
+    def __init__(self, ctx, lat, N):
+        self.L = ctx.L
+        self.N = tuple(int(v) for v in N)
+        self.size = int(np.prod(self.N))
+        lat9 = np.ascontiguousarray(np.asarray(lat, dtype=np.float64).reshape(9))
+        h = ctypes.c_void_p()
+        check(self.L.deft_grid_create(ctx.h, lat9.ctypes.data, *self.N, ctypes.byref(h)))
+        self.h = h
+
+    def fft(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        out = np.empty((self.N[0], self.N[1], self.N[2] // 2 + 1), dtype=np.complex128)
+        check(self.L.deft_grid_fft(self.h, x.ctypes.data, out.ctypes.data, 0))
+        return out
+
+    def ifft(self, c):
+        c = np.ascontiguousarray(c, dtype=np.complex128)
+        out = np.empty(self.N)
+        check(self.L.deft_grid_ifft(self.h, c.ctypes.data, out.ctypes.data, 0))
+        return out
+
+    def info(self):
+        dV = ctypes.c_double()
+        vol = ctypes.c_double()
+        sb = ctypes.c_double()
+        check(self.L.deft_grid_info(self.h, None, ctypes.addressof(dV), ctypes.addressof(vol),
+                                    ctypes.addressof(sb)))
+        return dV.value, vol.value, sb.value
+
+    def close(self):
+        self.L.deft_grid_destroy(self.h)
+
+
+class Fmt:
+    def __init__(self, grid, R=1.0, kT=1.0, mu=0.0, terms=7, V=None, mask=None):
+        self.L = grid.L
+        self.grid = grid
+        p = _lib.FmtParams(R, kT, mu, terms)
+        h = ctypes.c_void_p()
+        check(self.L.deft_fmt_create(grid.h, ctypes.byref(p), ctypes.byref(h)))
+        self.h = h
+        if V is not None:
+            V = np.ascontiguousarray(V, dtype=np.float64)
+            check(self.L.deft_fmt_set_vext(h, V.ctypes.data, 0))
+        if mask is not None:
+            m = np.ascontiguousarray(mask, dtype=np.float64)
+            check(self.L.deft_fmt_set_mask(h, m.ctypes.data, 0))
+
+    def energy(self, n):
+        n = np.ascontiguousarray(n, dtype=np.float64)
+        E = ctypes.c_double()
+        t = np.zeros(_lib.NTERMS)
+        check(self.L.deft_fmt_energy(self.h, n.ctypes.data, 0, ctypes.addressof(E), t.ctypes.data))
+        return E.value, t
+
+    def energy_grad(self, n):
+        n = np.ascontiguousarray(n, dtype=np.float64)
+        E = ctypes.c_double()
+        t = np.zeros(_lib.NTERMS)
+        g = np.empty(self.grid.size)
+        check(self.L.deft_fmt_energy_grad(self.h, n.ctypes.data, 0, ctypes.addressof(E),
+                                          g.ctypes.data, t.ctypes.data))
+        return E.value, g, t
+
+    def weighted(self, n):
+        n = np.ascontiguousarray(n, dtype=np.float64)
+        out = np.empty(5 * self.grid.size)
+        check(self.L.deft_fmt_weighted(self.h, n.ctypes.data, 0, out.ctypes.data))
+        return out.reshape(5, -1)
+
+    def close(self):
+        self.L.deft_fmt_destroy(self.h)
+
+
+class CG:
+    def __init__(self, fmt, linesearch=_lib.LS_SECANT, gtol=1e-9, maxiter=0, step=1.0,
+                 precision=0.0):
+        self.L = fmt.L
+        self.size = fmt.grid.size
+        p = _lib.CgParams(linesearch, gtol, maxiter, step, precision)
+        h = ctypes.c_void_p()
+        check(self.L.deft_cg_create(fmt.h, ctypes.byref(p), ctypes.byref(h)))
+        self.h = h
+        self.st = _lib.CgStatus()
+
+    def set_x(self, n):
+        n = np.ascontiguousarray(n, dtype=np.float64)
+        check(self.L.deft_cg_set_x(self.h, n.ctypes.data, 0))
+
+    def get_x(self):
+        out = np.empty(self.size)
+        check(self.L.deft_cg_get_x(self.h, out.ctypes.data, 0))
+        return out
+
+    def step(self):
+        s = self.L.deft_cg_step(self.h, ctypes.byref(self.st))
+        return s, self.st
+
+    def solve(self):
+        s = self.L.deft_cg_solve(self.h, ctypes.byref(self.st))
+        return s, self.st
+
+    def close(self):
+        self.L.deft_cg_destroy(self.h)
