@@ -21,6 +21,7 @@ EXPORTS = (
     "deft_ctx_create", "deft_ctx_destroy", "deft_ctx_sync", "deft_ctx_stream",
     "deft_grid_create", "deft_grid_create_dx", "deft_grid_destroy", "deft_grid_info",
     "deft_grid_fft", "deft_grid_ifft",
+    "deft_grid_profile", "deft_grid_profile_count", "deft_grid_profile_entry",
     "deft_fmt_create", "deft_fmt_destroy", "deft_fmt_set_params", "deft_fmt_set_vext",
     "deft_fmt_set_mask", "deft_fmt_energy", "deft_fmt_energy_grad", "deft_fmt_weighted",
     "deft_find_chemical_potential",
@@ -78,6 +79,10 @@ def load():
         "deft_grid_info": (ctypes.c_int, [_vp, _dp, _dp, _dp, _dp]),
         "deft_grid_fft": (ctypes.c_int, [_vp, _dp, _dp, ctypes.c_int]),
         "deft_grid_ifft": (ctypes.c_int, [_vp, _dp, _dp, ctypes.c_int]),
+        "deft_grid_profile": (ctypes.c_int, [_vp, ctypes.c_int]),
+        "deft_grid_profile_count": (ctypes.c_int, [_vp]),
+        "deft_grid_profile_entry": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_char_p),
+                                                   _dp, _dp]),
         "deft_fmt_create": (ctypes.c_int, [_vp, ctypes.POINTER(FmtParams), _pp]),
         "deft_fmt_destroy": (ctypes.c_int, [_vp]),
         "deft_fmt_set_params": (ctypes.c_int, [_vp, ctypes.POINTER(FmtParams)]),

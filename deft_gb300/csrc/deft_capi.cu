@@ -276,6 +276,23 @@ int deft_grid_ifft(deft_grid *g, const double *in, double *out, int on_device) {
   return sync(g->ctx);
 }
 
+int deft_grid_profile(deft_grid *g, int timing) {
+  if (!g) return set_err(DEFT_ERR_ARG, "grid is NULL");
+  cudaSetDevice(g->ctx->device);
+  g->eng->profile_reset(timing != 0);
+  return DEFT_OK;
+}
+
+int deft_grid_profile_count(deft_grid *g) { return g ? g->eng->profile_kinds() : 0; }
+
+int deft_grid_profile_entry(deft_grid *g, int i, const char **name, long long *launches,
+                            double *total_ms) {
+  if (!g || i < 0 || i >= g->eng->profile_kinds()) return set_err(DEFT_ERR_ARG, "bad index");
+  cudaSetDevice(g->ctx->device);
+  g->eng->profile_get(i, name, launches, total_ms);
+  return DEFT_OK;
+}
+
 int deft_fmt_create(deft_grid *g, const deft_fmt_params *p, deft_fmt **out) {
   if (!g || !p || !out) return set_err(DEFT_ERR_ARG, "NULL argument");
   if (!(p->R > 0) || !(p->kT > 0)) return set_err(DEFT_ERR_ARG, "R and kT must be positive");

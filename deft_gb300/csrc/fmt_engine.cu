@@ -648,8 +648,62 @@ int tile_width(int lines, int L, size_t bytes_per_elem, int nbuf, int cap) {
 
 }  // namespace
 
+enum KernelId {
+  kK_z_r2c, kK_z_c2r, kK_y_fft1, kK_y_fft5, kK_x_fft, kK_x_conv_fwd, kK_x_conv_adj, kK_z_phi_grad,
+  kK_z_phi_energy, kK_z_grad, kK_local_energy, kK_reduce_terms, kK_dots, kK_axpy, kK_scal_add,
+  kK_weight_table, kNumKernels
+};
+const char *const kKernelNames[kNumKernels] = {
+    "z_r2c", "z_c2r", "y_fft_1field", "y_fft_5fields", "x_fft", "x_conv_fwd", "x_conv_adj", "z_phi_grad",
+    "z_phi_energy", "z_grad", "local_energy", "reduce_terms", "dots", "axpy", "scal_add",
+    "weight_table"};
+
 class EngineImpl {
  public:
+  // kernel accounting
+  long long launches[kNumKernels] = {};
+  double total_ms[kNumKernels] = {};
+  bool timing = false;
+  std::vector<cudaEvent_t> pool;
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
+  cudaEvent_t cur_start = nullptr;
+
+  cudaEvent_t take_event() {
+    if (pool.empty()) {
+      cudaEvent_t e;
+      cudaEventCreate(&e);
+      return e;
+    }
+    cudaEvent_t e = pool.back();
+    pool.pop_back();
+    return e;
+  }
+  void pre(int id) {
+    launches[id]++;
+    if (timing) {
+      cur_start = take_event();
+      cudaEventRecord(cur_start, stream);
+    }
+  }
+  void post(int id) {
+    if (timing) {
+      cudaEvent_t stop = take_event();
+      cudaEventRecord(stop, stream);
+      pending.push_back({id, {cur_start, stop}});
+    }
+  }
+  // Call only after the stream has been synchronised.
+  void harvest() {
+    for (auto &p : pending) {
+      float ms = 0;
+      cudaEventElapsedTime(&ms, p.second.first, p.second.second);
+      total_ms[p.first] += ms;
+      pool.push_back(p.second.first);
+      pool.push_back(p.second.second);
+    }
+    pending.clear();
+  }
+
   Geom g{};
   cudaStream_t stream = nullptr;
   FftPlan px{}, py{}, pz{};
@@ -670,6 +724,12 @@ class EngineImpl {
   std::string err;
 
   ~EngineImpl() {
+    if (stream) cudaStreamSynchronize(stream);
+    for (auto &p : pending) {
+      cudaEventDestroy(p.second.first);
+      cudaEventDestroy(p.second.second);
+    }
+    for (cudaEvent_t e : pool) cudaEventDestroy(e);
     cudaFree(tw_x);
     cudaFree(tw_y);
     cudaFree(tw_z);
@@ -829,7 +889,9 @@ class EngineImpl {
   int ensure_table(double R) {
     if (R == table_R) return 0;
     const int blocks = (g.NC + kThreads - 1) / kThreads;
+    pre(kK_weight_table);
     k_weight_table<<<blocks < 4096 ? blocks : 4096, kThreads, 0, stream>>>(g, R, w3, w2, wv);
+    post(kK_weight_table);
     if (check("weight table")) return -1;
     table_R = R;
     return 0;
@@ -839,16 +901,23 @@ class EngineImpl {
 
   void y_fft(double2 *data, int nf, int sign) {
     dim3 grid((g.NzH + By - 1) / By, g.Nx, nf);
+    const int kid = nf == 1 ? kK_y_fft1 : kK_y_fft5;
+    pre(kid);
     if (sign < 0) k_y_fft<double, -1><<<grid, kThreads, smem_y, stream>>>(data, g, py, By);
     else k_y_fft<double, +1><<<grid, kThreads, smem_y, stream>>>(data, g, py, By);
+    post(kid);
   }
   int x_tiles() const { return (g.Ny * g.NzH + Bx - 1) / Bx; }
 
   int forward_weighted(const FmtSpec &f, const double *n) {
     if (ensure_table(f.R)) return -1;
+    pre(kK_z_r2c);
     k_z_r2c<double><<<dim3(pairs_tiles(Pz), 1), kThreads, smem_z, stream>>>(n, S0, g, pz, Pz, 1.0);
+    post(kK_z_r2c);
     y_fft(S0, 1, -1);
+    pre(kK_x_conv_fwd);
     k_x_conv_fwd<double><<<x_tiles(), kThreads, smem_x3, stream>>>(S0, S5, w3, w2, wv, g, px, Bx);
+    post(kK_x_conv_fwd);
     y_fft(S5, 5, +1);
     return check("forward convolution");
   }
@@ -865,10 +934,13 @@ class EngineImpl {
   }
 
   int finish_energy(int nblk, double *E_host, double *terms_host) {
+    pre(kK_reduce_terms);
     k_reduce_terms<<<1, kThreads, 0, stream>>>(partials, nblk, g.dV, results);
+    post(kK_reduce_terms);
     cudaMemcpyAsync(results_host, results, sizeof(double) * 8, cudaMemcpyDeviceToHost, stream);
     cudaError_t e = cudaStreamSynchronize(stream);
     if (e != cudaSuccess) return fail("energy", e);
+    harvest();
     if (E_host) *E_host = results_host[kNumTerms];
     if (terms_host) memcpy(terms_host, results_host, sizeof(double) * kNumTerms);
     return 0;
@@ -881,26 +953,35 @@ class EngineImpl {
     if (f.terms & kTermHS) {
       if (forward_weighted(f, n)) return -1;
       nblk = pairs_tiles(Pphi);
+      pre(grad ? kK_z_phi_grad : kK_z_phi_energy);
       if (grad)
         k_z_phi<double, true><<<nblk, kThreads, smem_phi, stream>>>(S5, n, V, g, pz, Pphi, la,
                                                                     partials);
       else
         k_z_phi<double, false><<<nblk, kThreads, smem_phi, stream>>>(S5, n, V, g, pz, Pphi, la,
                                                                      partials);
+      post(grad ? kK_z_phi_grad : kK_z_phi_energy);
       if (check("phi")) return -1;
       if (grad) {
         y_fft(S5, 5, -1);
+        pre(kK_x_conv_adj);
         k_x_conv_adj<double><<<x_tiles(), kThreads, smem_x3, stream>>>(S5, S0, w3, w2, wv, g, px,
                                                                        Bx);
+        post(kK_x_conv_adj);
         y_fft(S0, 1, +1);
       }
     } else {
       nblk = 4 * 152;
+      pre(kK_local_energy);
       k_local_energy<double><<<nblk, kThreads, 0, stream>>>(n, V, g, la, partials);
+      post(kK_local_energy);
     }
-    if (grad)
+    if (grad) {
+      pre(kK_z_grad);
       k_z_grad<double><<<pairs_tiles(Pz), kThreads, smem_z, stream>>>(S0, n, V, mask, grad, g, pz,
                                                                        Pz, la);
+      post(kK_z_grad);
+    }
     if (check("gradient")) return -1;
     return finish_energy(nblk, E_host, terms_host);
   }
@@ -926,28 +1007,38 @@ const char *Engine::last_error() const { return impl_->err.c_str(); }
 
 int Engine::fft(const double *in, double2 *out) {
   EngineImpl &e = *impl_;
-  k_z_r2c<double><<<dim3(e.pairs_tiles(e.Pz), 1), kThreads, e.smem_z, e.stream>>>(in, out, e.g, e.pz,
+  e.pre(kK_z_r2c);
+    k_z_r2c<double><<<dim3(e.pairs_tiles(e.Pz), 1), kThreads, e.smem_z, e.stream>>>(in, out, e.g, e.pz,
                                                                                  e.Pz, 1.0);
+    e.post(kK_z_r2c);
   e.y_fft(out, 1, -1);
-  k_x_fft<double, -1><<<e.x_tiles(), kThreads, e.smem_x2, e.stream>>>(out, e.g, e.px, e.Bx, e.g.dV);
+  e.pre(kK_x_fft);
+    k_x_fft<double, -1><<<e.x_tiles(), kThreads, e.smem_x2, e.stream>>>(out, e.g, e.px, e.Bx, e.g.dV);
+    e.post(kK_x_fft);
   return e.check("fft");
 }
 
 int Engine::ifft(const double2 *in, double *out) {
   EngineImpl &e = *impl_;
   cudaMemcpyAsync(e.S0, in, sizeof(double2) * e.g.NC, cudaMemcpyDeviceToDevice, e.stream);
-  k_x_fft<double, +1><<<e.x_tiles(), kThreads, e.smem_x2, e.stream>>>(e.S0, e.g, e.px, e.Bx, 1.0);
+  e.pre(kK_x_fft);
+    k_x_fft<double, +1><<<e.x_tiles(), kThreads, e.smem_x2, e.stream>>>(e.S0, e.g, e.px, e.Bx, 1.0);
+    e.post(kK_x_fft);
   e.y_fft(e.S0, 1, +1);
-  k_z_c2r<double><<<dim3(e.pairs_tiles(e.Pz), 1), kThreads, e.smem_z, e.stream>>>(
+  e.pre(kK_z_c2r);
+    k_z_c2r<double><<<dim3(e.pairs_tiles(e.Pz), 1), kThreads, e.smem_z, e.stream>>>(
       e.S0, out, e.g, e.pz, e.Pz, 1.0 / e.g.vol);
+    e.post(kK_z_c2r);
   return e.check("ifft");
 }
 
 int Engine::weighted(const FmtSpec &f, const double *n, double *out5) {
   EngineImpl &e = *impl_;
   if (e.forward_weighted(f, n)) return -1;
-  k_z_c2r<double><<<dim3(e.pairs_tiles(e.Pz), 5), kThreads, e.smem_z, e.stream>>>(e.S5, out5, e.g,
+  e.pre(kK_z_c2r);
+    k_z_c2r<double><<<dim3(e.pairs_tiles(e.Pz), 5), kThreads, e.smem_z, e.stream>>>(e.S5, out5, e.g,
                                                                                  e.pz, e.Pz, 1.0);
+    e.post(kK_z_c2r);
   return e.check("weighted");
 }
 
@@ -963,26 +1054,33 @@ int Engine::energy_grad(const FmtSpec &f, const double *n, const double *V, cons
 
 int Engine::dots(int k, const double *const *a, const double *const *b, double *out_host) {
   EngineImpl &e = *impl_;
-  k_dots<<<e.dot_blocks, kThreads, 0, e.stream>>>(k, a[0], b[0], k > 1 ? a[1] : nullptr,
+  e.pre(kK_dots);
+    k_dots<<<e.dot_blocks, kThreads, 0, e.stream>>>(k, a[0], b[0], k > 1 ? a[1] : nullptr,
                                                   k > 1 ? b[1] : nullptr, k > 2 ? a[2] : nullptr,
                                                   k > 2 ? b[2] : nullptr, e.g.NR, e.dot_partials,
                                                   e.dot_counter, e.results);
+    e.post(kK_dots);
   cudaMemcpyAsync(e.results_host, e.results, sizeof(double) * 3, cudaMemcpyDeviceToHost, e.stream);
   cudaError_t err = cudaStreamSynchronize(e.stream);
   if (err != cudaSuccess) return e.fail("dots", err);
+  e.harvest();
   for (int i = 0; i < k; i++) out_host[i] = e.results_host[i];
   return 0;
 }
 
 int Engine::axpy(double alpha, const double *x, double *y) {
   EngineImpl &e = *impl_;
-  k_axpy<<<e.dot_blocks, kThreads, 0, e.stream>>>(alpha, x, y, e.g.NR);
+  e.pre(kK_axpy);
+    k_axpy<<<e.dot_blocks, kThreads, 0, e.stream>>>(alpha, x, y, e.g.NR);
+    e.post(kK_axpy);
   return e.check("axpy");
 }
 
 int Engine::scal_add(double beta, double *d, double alpha, const double *gv) {
   EngineImpl &e = *impl_;
-  k_scal_add<<<e.dot_blocks, kThreads, 0, e.stream>>>(beta, d, alpha, gv, e.g.NR);
+  e.pre(kK_scal_add);
+    k_scal_add<<<e.dot_blocks, kThreads, 0, e.stream>>>(beta, d, alpha, gv, e.g.NR);
+    e.post(kK_scal_add);
   return e.check("scal_add");
 }
 
@@ -992,6 +1090,29 @@ int Engine::copy(const double *src, double *dst) {
       cudaMemcpyAsync(dst, src, sizeof(double) * e.g.NR, cudaMemcpyDeviceToDevice, e.stream);
   if (err != cudaSuccess) return e.fail("copy", err);
   return 0;
+}
+
+void Engine::profile_reset(bool timing) {
+  EngineImpl &e = *impl_;
+  cudaStreamSynchronize(e.stream);
+  e.harvest();
+  for (int i = 0; i < kNumKernels; i++) {
+    e.launches[i] = 0;
+    e.total_ms[i] = 0;
+  }
+  e.timing = timing;
+}
+
+int Engine::profile_kinds() const { return kNumKernels; }
+
+void Engine::profile_get(int i, const char **name, long long *launches, double *total_ms) {
+  EngineImpl &e = *impl_;
+  cudaStreamSynchronize(e.stream);
+  e.harvest();
+  if (i < 0 || i >= kNumKernels) return;
+  if (name) *name = kKernelNames[i];
+  if (launches) *launches = e.launches[i];
+  if (total_ms) *total_ms = e.total_ms[i];
 }
 
 }  // namespace deft

@@ -75,6 +75,13 @@ class Engine {
   int scal_add(double beta, double *d, double alpha, const double *g);  // d = alpha g + beta d
   int copy(const double *src, double *dst);
 
+  // Kernel accounting: every launch is counted per kernel kind; with timing
+  // on, each launch is also bracketed by CUDA events on the engine's stream.
+  void profile_reset(bool timing);
+  int profile_kinds() const;
+  // Synchronises the stream, then reports kind i.
+  void profile_get(int i, const char **name, long long *launches, double *total_ms);
+
   const char *last_error() const;
 
  private:

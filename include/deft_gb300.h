@@ -107,6 +107,17 @@ int deft_grid_fft(deft_grid *grid, const double *in, double *out, int on_device)
 /* ifft(gd, v): c2r times 1/V (src/ReciprocalGrid.cpp:42-66); input kept. */
 int deft_grid_ifft(deft_grid *grid, const double *in, double *out, int on_device);
 
+/* Kernel accounting for everything queued through this grid (no reference
+ * counterpart).  Every kernel launch is counted per kernel kind; with
+ * timing = 1 each launch is also bracketed by CUDA events on the context's
+ * stream.  deft_grid_profile resets the counters. */
+int deft_grid_profile(deft_grid *grid, int timing);
+/* Number of kernel kinds (entries are 0 .. count-1). */
+int deft_grid_profile_count(deft_grid *grid);
+/* Synchronises, then gives kind i's name, launches and summed event time. */
+int deft_grid_profile_entry(deft_grid *grid, int i, const char **name, long long *launches,
+                            double *total_ms);
+
 /* ---- functional ---- */
 int deft_fmt_create(deft_grid *grid, const deft_fmt_params *p, deft_fmt **out);
 int deft_fmt_destroy(deft_fmt *f);
