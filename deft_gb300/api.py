@@ -87,14 +87,20 @@ class Lattice:
         return np.ascontiguousarray(self.R.reshape(9))
 
 
+def grid_size_from_dx(lat, dx):
+    """N_i = 1 + int(e/100 + |a_i|/dx), the rule of GridDescription(lat, dx)
+    (src/GridDescription.cpp:27-29)."""
+    R = lat.R if isinstance(lat, Lattice) else np.asarray(lat, dtype=np.float64).reshape(3, 3)
+    return [1 + int(math.e / 100 + np.linalg.norm(R[i]) / dx) for i in range(3)]
+
+
 class GridDescription:
     """GridDescription(lat, Nx, Ny, Nz) or GridDescription(lat, dx)."""
 
     def __init__(self, lat, nx, ny=None, nz=None, ctx=None):
         self.Lat = lat
         if ny is None:
-            dx = float(nx)
-            N = [1 + int(math.e / 100 + np.linalg.norm(lat.R[i]) / dx) for i in range(3)]
+            N = grid_size_from_dx(lat, float(nx))
         else:
             N = [int(nx), int(ny), int(nz)]
         self.Nx, self.Ny, self.Nz = N

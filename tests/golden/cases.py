@@ -1,0 +1,54 @@
+"""Seeded inputs of the golden cases (shared by make_golden.py and the tests)."""
+import math
+
+import numpy as np
+
+from oracle import oracle as O
+
+CASES = ("cubic12", "ortho_odd", "fcc12")
+
+
+def make_case(name):
+    if name == "cubic12":
+        rng = np.random.Generator(np.random.PCG64(101))
+        N, lat, R, kT = (12, 12, 12), np.diag([2.4, 2.4, 2.4]), 1.0, 1.0
+        nb = 0.3 / (4 * math.pi / 3)
+        mu = O.find_mu(R, kT, nb)
+        n = nb * (1 + 0.2 * rng.standard_normal(int(np.prod(N))))
+        return O.Problem(lat, N, R=R, kT=kT, mu=mu, terms=O.HS | O.IDEAL | O.MU), n
+    if name == "ortho_odd":
+        rng = np.random.Generator(np.random.PCG64(102))
+        N, lat, R, kT = (10, 12, 15), np.diag([2.0, 2.6, 3.0]), 1.0, 1.0
+        size = int(np.prod(N))
+        nb = 0.25 / (4 * math.pi / 3)
+        mu = O.find_mu(R, kT, nb)
+        mask = (rng.random(size) > 0.3).astype(np.float64)
+        V = 0.3 * rng.standard_normal(size)
+        n = nb * (1 + 0.1 * rng.standard_normal(size))
+        n = np.where(mask > 0, n, 1e-4 * nb)  # floor density in walls, as the drivers do
+        return O.Problem(lat, N, R=R, kT=kT, mu=mu, terms=O.HS | O.IDEAL | O.MU, V=V, mask=mask), n
+    if name == "fcc12":
+        rng = np.random.Generator(np.random.PCG64(103))
+        N = (12, 12, 12)
+        lat = np.array([[0, 2.5, 2.5], [2.5, 0, 2.5], [2.5, 2.5, 0.0]])
+        R, kT = 0.7, 0.8
+        size = int(np.prod(N))
+        mask = (rng.random(size) > 0.2).astype(np.float64)
+        V = 0.1 * rng.standard_normal(size)
+        n = 0.05 * (1 + 0.3 * rng.random(size))
+        return O.Problem(lat, N, R=R, kT=kT, mu=-1.2, terms=O.HS | O.IDEAL | O.MU, V=V,
+                         mask=mask), n
+    raise KeyError(name)
+
+
+def cg_case():
+    N, lat = (12, 12, 16), np.diag([2.4, 2.4, 3.2])
+    nb = 0.3 / (4 * math.pi / 3)
+    mu = O.find_mu(1.0, 1.0, nb)
+    z = np.arange(16) * 0.2
+    mask = np.broadcast_to(((z > 0) & (z < 1.6)).astype(float), N).copy().reshape(-1)
+    rng = np.random.Generator(np.random.PCG64(104))
+    n = nb * (1 + 0.05 * rng.standard_normal(mask.size))
+    n = np.where(mask > 0, n, 1e-4 * nb)
+    P = O.Problem(lat, N, mu=mu, mask=mask)
+    return P, n, 6, 0.1

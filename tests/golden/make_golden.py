@@ -1,0 +1,55 @@
+"""Generates the golden fixtures in this directory from the UNMODIFIED
+reference sources (oracle/_ref/libdeft_ref.so, built by `make -C oracle ref`
+where the reference checkout exists).  Run from the repository root:
+
+    python tests/golden/make_golden.py
+
+Inputs are regenerated from the seeds below by tests/golden/cases.py, so the
+fixtures store only the reference's outputs (plus the small inputs of the CG
+trajectory case, for convenience)."""
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle import oracle as O  # noqa: E402
+from tests.golden.cases import CASES, cg_case, make_case  # noqa: E402
+
+
+def main():
+    O.build(ref=True)
+    assert O.ref_available(), "reference build missing"
+    out = {}
+    arrays = {}
+    for name in CASES:
+        P, n = make_case(name)
+        E, g, t = P.ref_energy_grad(n)
+        w = P.ref_weighted(n)
+        out[name] = {"E": E, "terms": [float(x) for x in t]}
+        arrays[f"{name}_grad"] = g
+        arrays[f"{name}_weighted"] = w
+    # known-answer value of tests/new-hard-spheres.cpp:52-63
+    P = O.Problem(np.diag([2.0, 2.0, 2.0]), (20, 20, 20), R=1.0, kT=1.0, mu=0.0, terms=O.HS)
+    E, _, _ = P.ref_energy_grad(np.full(8000, 0.1), grad=False)
+    out["white_bear_kat"] = {"E": E, "published": 2.72225468848892}
+    # bulk chemical potentials
+    out["find_mu"] = {str(eta): O.ref().ref_find_mu(1.0, 1.0, eta / (4 * np.pi / 3))
+                      for eta in (0.05, 0.1, 0.2, 0.3, 0.4, 0.45)}
+    # reference CG + QuadraticLineMinimizer trajectory
+    P, n, iters, step = cg_case()
+    x, e = P.ref_cg(n, iters, step=step)
+    out["cg_quadratic"] = {"energies": [float(v) for v in e], "iters": iters, "step": step}
+    arrays["cg_quadratic_x"] = x
+    with open(os.path.join(HERE, "reference_values.json"), "w") as f:
+        json.dump(out, f, indent=1, sort_keys=True)
+    np.savez_compressed(os.path.join(HERE, "reference_fields.npz"), **arrays)
+    print("wrote", sorted(out), sorted(arrays))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,157 @@
+"""CPU tests of the oracle: the plain-C restatement against the golden
+fixtures generated from the unmodified reference (tests/golden/), the
+reference's own known-answer value, the weight identities of
+tests/convolve.cpp, and (where the reference build exists) live parity with
+the reference."""
+import json
+import math
+import os
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+@pytest.fixture(scope="module")
+def golden():
+    with open(os.path.join(HERE, "golden", "reference_values.json")) as f:
+        vals = json.load(f)
+    arrs = np.load(os.path.join(HERE, "golden", "reference_fields.npz"))
+    return vals, arrs
+
+
+@pytest.mark.parametrize("shape", [(10, 10, 10), (16, 12, 15), (7, 9, 11), (12, 14, 13), (8, 6, 4)])
+def test_oracle_fft_matches_numpy(oracle_mod, shape):
+    O = oracle_mod
+    rng = np.random.default_rng(1)
+    x = rng.standard_normal(shape)
+    a = O.r2c_3d(x)
+    b = np.fft.rfftn(x)
+    assert np.abs(a - b).max() <= 2e-15 * np.abs(b).max() * math.log2(x.size)
+    back = O.c2r_3d(b, shape[2])
+    ref = np.fft.irfftn(b, s=shape, axes=(0, 1, 2)) * x.size
+    assert np.abs(back - ref).max() <= 2e-15 * np.abs(x).max() * x.size * math.log2(x.size)
+
+
+def test_oracle_fft_round_trip_fcc(oracle_mod):
+    """tests/fftinverse.cpp:30-50: fft then ifft recovers the field to 1e-15."""
+    O = oracle_mod
+    rng = np.random.default_rng(2)
+    x = rng.standard_normal((10, 10, 10))
+    back = O.c2r_3d(O.r2c_3d(x), 10) / x.size
+    assert np.abs(back - x).max() < 1e-15 * 10
+
+
+@pytest.mark.parametrize("name", ["cubic12", "ortho_odd", "fcc12"])
+def test_oracle_matches_reference_golden(oracle_mod, golden, name):
+    from tests.golden.cases import make_case
+    vals, arrs = golden
+    P, n = make_case(name)
+    E, g, t = P.energy_grad(n, terms=True)
+    ref = vals[name]
+    assert abs(E / ref["E"] - 1) < 1e-12
+    tr = np.array(ref["terms"])
+    assert np.abs(t[:len(tr)] - tr).max() <= 1e-12 * np.abs(tr).max()
+    gr = arrs[f"{name}_grad"]
+    assert np.abs(g - gr).max() <= 1e-12 * np.abs(gr).max()
+    w = P.weighted(n)
+    wr = arrs[f"{name}_weighted"]
+    for a in range(5):
+        assert np.abs(w[a] - wr[a]).max() <= 1e-13 * np.abs(wr[a]).max()
+
+
+def test_oracle_white_bear_known_answer(oracle_mod, golden):
+    O = oracle_mod
+    vals, _ = golden
+    P = O.Problem(np.diag([2.0, 2.0, 2.0]), (20, 20, 20), R=1.0, kT=1.0, mu=0.0, terms=O.HS)
+    E = P.energy(np.full(8000, 0.1))
+    assert abs(E / 2.72225468848892 - 1) < 2e-11  # tests/new-hard-spheres.cpp:56,66
+    assert abs(E / vals["white_bear_kat"]["E"] - 1) < 1e-13
+    # homogeneous value F/a^3 (tests/new-hard-spheres.cpp:73-77)
+    hom = _hs_only_homogeneous(O, 0.1)
+    assert abs(hom / (2.72225468848892 / 8) - 1) < 2e-11
+
+
+def _hs_only_homogeneous(O, nb):
+    # HS free-energy density only: total minus ideal gas (mu = 0)
+    x = 18.01528 * 1822.8885 * 1.0 / (2 * math.pi)
+    nQ = x * math.sqrt(x)
+    return O.homogeneous(1.0, 1.0, 0.0, nb) - nb * (math.log(nb / nQ) - 1)
+
+
+def test_oracle_find_mu(oracle_mod, golden):
+    vals, _ = golden
+    for eta, mu in vals["find_mu"].items():
+        nb = float(eta) / (4 * math.pi / 3)
+        assert abs(oracle_mod.find_mu(1.0, 1.0, nb) / mu - 1) < 1e-13
+
+
+def test_oracle_cg_quadratic_trajectory(oracle_mod, golden):
+    from tests.golden.cases import cg_case
+    vals, arrs = golden
+    P, n, iters, step = cg_case()
+    x, e = P.cg_quadratic(n, iters, step=step)
+    er = np.array(vals["cg_quadratic"]["energies"])
+    assert len(e) == len(er)
+    assert np.abs(e / er - 1).max() < 1e-11
+    assert np.abs(x - arrs["cg_quadratic_x"]).max() < 1e-5 * np.abs(x).max()
+
+
+def test_oracle_weight_identities(oracle_mod):
+    """tests/convolve.cpp:79-177 on an FCC cell with a sharp Gaussian:
+    integral of Step(R) * f = 4/3 pi R^3 integral f, Shell = 4 pi R^2, vector
+    shells integrate to 0, |x-shell| <= shell."""
+    O = oracle_mod
+    lat = np.array([[0, 5, 5], [5, 0, 5], [5, 5, 0.0]])
+    N = (40, 40, 40)
+    R = np.array(lat).T
+    ii = np.arange(40) / 40.0
+    rel = np.stack(np.meshgrid(ii, ii, ii, indexing="ij"), -1).reshape(-1, 3)
+    rel = rel - np.round(rel)
+    cart = rel @ R.T
+    f = np.exp(-10.0 * (cart * cart).sum(1))
+    P = O.Problem(lat, N, R=1.0)
+    dV = P.dvolume()
+    w = P.weighted(f)
+    I = f.sum() * dV
+    assert abs(w[0].sum() * dV / I - 4 * math.pi / 3) < 1e-6 * 4 * math.pi / 3
+    assert abs(w[1].sum() * dV / I - 4 * math.pi) < 1e-6 * 4 * math.pi
+    for c in (2, 3, 4):
+        assert abs(w[c].sum() * dV / I) < 1e-10
+        assert np.abs(w[c]).max() <= w[1].max() * (1 + 1e-12)
+
+
+def test_oracle_secant_cg_1d_slit(oracle_mod):
+    O = oracle_mod
+    nb = 0.3 / (4 * math.pi / 3)
+    mu = O.find_mu(1.0, 1.0, nb)
+    z = np.arange(64) * 0.2
+    mask = ((z > 0) & (z < 6.4)).astype(float)
+    P = O.Problem(np.diag([0.2, 0.2, 12.8]), (1, 1, 64), mu=mu, mask=mask)
+    x, info = P.cg_solve(np.where(mask > 0, nb, 0.0), gtol=1e-12, maxiter=5000)
+    assert info["gnorm"] < 1e-12
+    # symmetric slit: the profile is mirror-symmetric about the slit centre
+    inner = x[1:32]
+    assert np.abs(inner - inner[::-1]).max() < 1e-10
+    # far from the walls the density approaches bulk; at contact it is enhanced
+    assert x[1] > 2 * nb
+
+
+@pytest.mark.skipif(not os.path.exists(os.path.join(os.path.dirname(HERE), "oracle", "_ref",
+                                                    "libdeft_ref.so")),
+                    reason="reference build only exists where the reference checkout does")
+def test_oracle_matches_live_reference(oracle_mod):
+    O = oracle_mod
+    rng = np.random.default_rng(9)
+    N = (14, 10, 9)
+    lat = np.array([[2.8, 0.1, 0.0], [0.0, 2.0, -0.1], [0.2, 0.0, 1.8]])
+    size = int(np.prod(N))
+    nb = 0.2 / (4 * math.pi / 3)
+    P = O.Problem(lat, N, R=0.9, kT=1.3, mu=O.find_mu(0.9, 1.3, nb),
+                  V=0.1 * rng.standard_normal(size), mask=(rng.random(size) > 0.1).astype(float))
+    n = nb * (1 + 0.1 * rng.standard_normal(size))
+    E, g = P.energy_grad(n)
+    Er, gr, _ = P.ref_energy_grad(n)
+    assert abs(E / Er - 1) < 1e-13
+    assert np.abs(g - gr).max() <= 1e-13 * np.abs(gr).max()
