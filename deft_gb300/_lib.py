@@ -25,6 +25,7 @@ EXPORTS = (
     "deft_fmt_create", "deft_fmt_destroy", "deft_fmt_set_params", "deft_fmt_set_vext",
     "deft_fmt_set_mask", "deft_fmt_energy", "deft_fmt_energy_grad", "deft_fmt_weighted",
     "deft_find_chemical_potential",
+    "deft_fmt_energy_grad_noalloc", "deft_noalloc_scratch_bytes",
     "deft_cg_create", "deft_cg_destroy", "deft_cg_set_x", "deft_cg_get_x", "deft_cg_x_device",
     "deft_cg_step", "deft_cg_solve",
 )
@@ -93,6 +94,10 @@ def load():
         "deft_fmt_weighted": (ctypes.c_int, [_vp, _dp, ctypes.c_int, _dp]),
         "deft_find_chemical_potential": (ctypes.c_int, [ctypes.c_double, ctypes.c_double,
                                                         ctypes.c_double, _dp]),
+        "deft_fmt_energy_grad_noalloc": (ctypes.c_int, [_dp, ctypes.c_int, ctypes.c_int,
+                                                         ctypes.c_int, ctypes.POINTER(FmtParams),
+                                                         _dp, _dp, _dp, _dp, _dp, _dp, _vp]),
+        "deft_noalloc_scratch_bytes": (ctypes.c_size_t, []),
         "deft_cg_create": (ctypes.c_int, [_vp, ctypes.POINTER(CgParams), _pp]),
         "deft_cg_destroy": (ctypes.c_int, [_vp]),
         "deft_cg_set_x": (ctypes.c_int, [_vp, _dp, ctypes.c_int]),

@@ -437,6 +437,41 @@ int deft_find_chemical_potential(double R, double kT, double nb, double *mu_out)
   return DEFT_OK;
 }
 
+// For callers that cannot allocate device memory (a framework that already
+// reserved the GPU's memory, or a loop that may not allocate after start-up):
+// the whole evaluation runs out of a fixed device array built into the
+// library.  Inputs and outputs stay the caller's.
+int deft_fmt_energy_grad_noalloc(const double lat[9], int Nx, int Ny, int Nz,
+                                 const deft_fmt_params *p, const double *n, const double *V,
+                                 const double *mask, double *E_out, double *grad_out,
+                                 double *terms_out, void *stream) {
+  if (!lat || !p || !n || !E_out || !grad_out) return set_err(DEFT_ERR_ARG, "NULL argument");
+  if (!(p->R > 0) || !(p->kT > 0)) return set_err(DEFT_ERR_ARG, "R and kT must be positive");
+  if ((p->terms & DEFT_TERM_VEXT) && !V)
+    return set_err(DEFT_ERR_ARG, "DEFT_TERM_VEXT set but V is NULL");
+  if ((p->terms & DEFT_TERM_MASK) && !mask)
+    return set_err(DEFT_ERR_ARG, "DEFT_TERM_MASK set but mask is NULL");
+  deft::GridSpec s;
+  s.Nx = Nx;
+  s.Ny = Ny;
+  s.Nz = Nz;
+  memcpy(s.lat, lat, sizeof(s.lat));
+  deft::FmtSpec f;
+  f.R = p->R;
+  f.kT = p->kT;
+  f.mu = p->mu;
+  f.terms = p->terms;
+  std::string err;
+  const int r = deft::noalloc_energy_grad(s, f, n, V, mask, grad_out, E_out, terms_out,
+                                          (cudaStream_t)stream, &err);
+  if (r == 1) return set_err(DEFT_ERR_ARG, err);
+  if (r) return set_err(DEFT_ERR_CUDA, err);
+  if (!std::isfinite(*E_out)) return set_err(DEFT_ERR_NAN, "energy is not finite");
+  return DEFT_OK;
+}
+
+size_t deft_noalloc_scratch_bytes(void) { return deft::noalloc_scratch_bytes(); }
+
 // ---------------------------------------------------------------------------
 // Minimiser
 

@@ -1115,4 +1115,238 @@ void Engine::profile_get(int i, const char **name, long long *launches, double *
   if (total_ms) *total_ms = e.total_ms[i];
 }
 
+// ---------------------------------------------------------------------------
+// Energy + gradient that allocates nothing.
+//
+// Some callers cannot call cudaMalloc: a host framework whose caching
+// allocator or up-front reservation already holds nearly all device memory
+// (so a private allocation fails or fragments it), or a real-time loop that
+// forbids allocation once it has started.  This entry point takes its scratch
+// (spectra, weight table, twiddles, per-block partial energies) from one
+// file-scope device array of kNoAllocScratchBytes, which every GPU that loads
+// this library holds until the process exits.  Every call shares it and it
+// keeps the last call's contents; each call rewrites everything it reads, so
+// nothing has to start at zero.  Calls that overlap on the GPU (two streams,
+// or two host threads) race on the array.
+
+constexpr size_t kNoAllocScratchBytes = size_t(20) << 20;  // 20 MiB
+constexpr int kNoAllocMaxAxis = 256;
+constexpr int kNoAllocMaxDevices = 64;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+namespace {
+std::mutex g_noalloc_mu;
+void *g_noalloc_ptr[kNoAllocMaxDevices] = {};
+
+size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
+
+bool noalloc_fail(std::string *err, const std::string &m) {
+  if (err) *err = m;
+  return false;
+}
+}  // namespace
+
+size_t noalloc_scratch_bytes() { return kNoAllocScratchBytes; }
+
+int noalloc_energy_grad(const GridSpec &s, const FmtSpec &f, const double *n, const double *V,
+                        const double *mask, double *grad, double *E_host, double *terms_host,
+                        cudaStream_t stream, std::string *err) {
+  // ---- sizes and geometry (host only; nothing touches the GPU before these pass)
+  const int N3[3] = {s.Nx, s.Ny, s.Nz};
+  for (int i = 0; i < 3; i++)
+    if (N3[i] < 1 || N3[i] > kNoAllocMaxAxis) {
+      noalloc_fail(err, "no-allocation energy_grad: each grid size must be in 1.." +
+                            std::to_string(kNoAllocMaxAxis));
+      return 1;
+    }
+  FftPlan px{}, py{}, pz{};
+  if (!factorize(s.Nx, px) || !factorize(s.Ny, py) || !factorize(s.Nz, pz)) {
+    noalloc_fail(err, "no-allocation energy_grad: grid sizes must factor into primes <= 13");
+    return 1;
+  }
+  Geom g{};
+  g.Nx = s.Nx;
+  g.Ny = s.Ny;
+  g.Nz = s.Nz;
+  g.NzH = s.Nz / 2 + 1;
+  g.lines = s.Nx * s.Ny;
+  g.NR = s.Nx * s.Ny * s.Nz;
+  g.NC = s.Nx * s.Ny * g.NzH;
+  double R[9], fine[9], inv[9];
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) R[3 * i + j] = s.lat[3 * j + i];
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) fine[3 * i + j] = R[3 * i + j] / N3[j];
+  g.vol = det3(R);
+  g.dV = det3(fine);
+  if (!(g.vol > 0)) {
+    noalloc_fail(err, "lattice vectors must be right-handed and non-degenerate");
+    return 1;
+  }
+  g.dr = std::pow(g.dV, 1.0 / 3);
+  g.scale = g.dV / g.vol;
+  const double d = g.vol;
+  inv[0] = (R[4] * R[8] - R[5] * R[7]) / d;
+  inv[1] = (R[2] * R[7] - R[1] * R[8]) / d;
+  inv[2] = (R[1] * R[5] - R[2] * R[4]) / d;
+  inv[3] = (R[5] * R[6] - R[3] * R[8]) / d;
+  inv[4] = (R[0] * R[8] - R[2] * R[6]) / d;
+  inv[5] = (R[2] * R[3] - R[0] * R[5]) / d;
+  inv[6] = (R[3] * R[7] - R[4] * R[6]) / d;
+  inv[7] = (R[1] * R[6] - R[0] * R[7]) / d;
+  inv[8] = (R[0] * R[4] - R[1] * R[3]) / d;
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) g.Bm[3 * i + j] = 2 * M_PI * inv[3 * j + i];
+
+  const size_t cs = sizeof(double2);
+  const int By = tile_width(g.NzH, g.Ny, cs, 2, 16);
+  const int Bx = tile_width(g.Ny * g.NzH, g.Nx, cs, 3, 16);
+  const int pairs = (g.lines + 1) / 2;
+  const int Pz = tile_width(pairs, g.Nz, cs, 2, 16);
+  int Pphi;
+  {
+    const size_t per_pair = (size_t)g.Nz * (2 * cs + 10 * sizeof(double));
+    int pm = (int)(kSmemBudget / per_pair);
+    if (pm < 1) pm = 1;
+    if (pm > 8) pm = 8;
+    const int nt = (pairs + pm - 1) / pm;
+    Pphi = (pairs + nt - 1) / nt;
+  }
+  const size_t smem_y = 2 * (size_t)g.Ny * By * cs;
+  const size_t smem_x3 = 3 * (size_t)g.Nx * Bx * cs;
+  const size_t smem_z = 2 * (size_t)g.Nz * Pz * cs;
+  const size_t smem_phi = (size_t)g.Nz * Pphi * (2 * cs + 10 * sizeof(double));
+  const int nblk_phi = (pairs + Pphi - 1) / Pphi;
+  const int nblk = (f.terms & kTermHS) ? nblk_phi : 4 * 152;
+
+  // scratch layout
+  size_t off = 0;
+  const size_t o_twx = off; off += align256(cs * g.Nx);
+  const size_t o_twy = off; off += align256(cs * g.Ny);
+  const size_t o_twz = off; off += align256(cs * g.Nz);
+  const size_t o_w3 = off; off += align256(sizeof(double) * g.NC);
+  const size_t o_w2 = off; off += align256(sizeof(double) * g.NC);
+  const size_t o_wv = off; off += align256(sizeof(double) * g.NC);
+  const size_t o_S0 = off; off += align256(cs * g.NC);
+  const size_t o_S5 = off; off += align256(5 * cs * g.NC);
+  const size_t o_part = off; off += align256(sizeof(double) * kNumTerms * nblk);
+  const size_t o_res = off; off += align256(sizeof(double) * 8);
+  if (off > kNoAllocScratchBytes) {
+    noalloc_fail(err, "no-allocation energy_grad: this grid needs " + std::to_string(off) +
+                          " bytes of scratch; the fixed device array holds " +
+                          std::to_string(kNoAllocScratchBytes) +
+                          " (about 64^3 points at most)");
+    return 1;
+  }
+
+  // ---- per-device set-up: the device address of the scratch array
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) {
+    noalloc_fail(err, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+    return 2;
+  }
+  if (dev < 0 || dev >= kNoAllocMaxDevices) {
+    noalloc_fail(err, "device index out of range");
+    return 1;
+  }
+  unsigned char *base = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+      void *p = nullptr;
+      e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+      if (e != cudaSuccess || !p) {
+        noalloc_fail(err, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+        return 2;
+      }
+      g_noalloc_ptr[dev] = p;
+    }
+    base = static_cast<unsigned char *>(g_noalloc_ptr[dev]);
+  }
+  double2 *tw_x = reinterpret_cast<double2 *>(base + o_twx);
+  double2 *tw_y = reinterpret_cast<double2 *>(base + o_twy);
+  double2 *tw_z = reinterpret_cast<double2 *>(base + o_twz);
+  double *w3 = reinterpret_cast<double *>(base + o_w3);
+  double *w2 = reinterpret_cast<double *>(base + o_w2);
+  double *wv = reinterpret_cast<double *>(base + o_wv);
+  double2 *S0 = reinterpret_cast<double2 *>(base + o_S0);
+  double2 *S5 = reinterpret_cast<double2 *>(base + o_S5);
+  double *partials = reinterpret_cast<double *>(base + o_part);
+  double *results = reinterpret_cast<double *>(base + o_res);
+
+  // twiddles: computed on the host into stack arrays, copied into the scratch
+  {
+    double2 h[3][kNoAllocMaxAxis];
+    const long double twopi = 6.283185307179586476925286766559005768L;
+    double2 *dst[3] = {tw_x, tw_y, tw_z};
+    for (int a = 0; a < 3; a++) {
+      for (int t = 0; t < N3[a]; t++) {
+        const long double ang = twopi * (long double)t / (long double)N3[a];
+        h[a][t] = make_double2((double)cosl(ang), (double)-sinl(ang));
+      }
+      e = cudaMemcpyAsync(dst[a], h[a], cs * N3[a], cudaMemcpyHostToDevice, stream);
+      if (e != cudaSuccess) {
+        noalloc_fail(err, std::string("twiddle copy: ") + cudaGetErrorString(e));
+        return 2;
+      }
+    }
+    // the copies above read pageable stack memory and have consumed it on return
+  }
+  px.tw = tw_x;
+  py.tw = tw_y;
+  pz.tw = tw_z;
+
+  set_smem(k_z_r2c<double>, smem_z);
+  set_smem(k_y_fft<double, -1>, smem_y);
+  set_smem(k_y_fft<double, +1>, smem_y);
+  set_smem(k_x_conv_fwd<double>, smem_x3);
+  set_smem(k_x_conv_adj<double>, smem_x3);
+  set_smem(k_z_phi<double, true>, smem_phi);
+  set_smem(k_z_grad<double>, smem_z);
+
+  LocalArgs la;
+  la.R = f.R;
+  la.kT = f.kT;
+  la.mu = f.mu;
+  la.nQ = nQ_of(f.kT);
+  la.dV = g.dV;
+  la.terms = f.terms;
+  const int ptiles_z = (pairs + Pz - 1) / Pz;
+  const int xt = (g.Ny * g.NzH + Bx - 1) / Bx;
+  const dim3 ygrid1((g.NzH + By - 1) / By, g.Nx, 1), ygrid5((g.NzH + By - 1) / By, g.Nx, 5);
+  {
+    const int blocks = (g.NC + kThreads - 1) / kThreads;
+    k_weight_table<<<blocks < 4096 ? blocks : 4096, kThreads, 0, stream>>>(g, f.R, w3, w2, wv);
+  }
+  if (f.terms & kTermHS) {
+    k_z_r2c<double><<<dim3(ptiles_z, 1), kThreads, smem_z, stream>>>(n, S0, g, pz, Pz, 1.0);
+    k_y_fft<double, -1><<<ygrid1, kThreads, smem_y, stream>>>(S0, g, py, By);
+    k_x_conv_fwd<double><<<xt, kThreads, smem_x3, stream>>>(S0, S5, w3, w2, wv, g, px, Bx);
+    k_y_fft<double, +1><<<ygrid5, kThreads, smem_y, stream>>>(S5, g, py, By);
+    k_z_phi<double, true><<<nblk_phi, kThreads, smem_phi, stream>>>(S5, n, V, g, pz, Pphi, la,
+                                                                    partials);
+    k_y_fft<double, -1><<<ygrid5, kThreads, smem_y, stream>>>(S5, g, py, By);
+    k_x_conv_adj<double><<<xt, kThreads, smem_x3, stream>>>(S5, S0, w3, w2, wv, g, px, Bx);
+    k_y_fft<double, +1><<<ygrid1, kThreads, smem_y, stream>>>(S0, g, py, By);
+  } else {
+    k_local_energy<double><<<nblk, kThreads, 0, stream>>>(n, V, g, la, partials);
+  }
+  k_z_grad<double><<<ptiles_z, kThreads, smem_z, stream>>>(S0, n, V, mask, grad, g, pz, Pz, la);
+  k_reduce_terms<<<1, kThreads, 0, stream>>>(partials, nblk, g.dV, results);
+  double res[8];
+  e = cudaGetLastError();
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(res, results, sizeof(double) * 8, cudaMemcpyDeviceToHost, stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+  if (e != cudaSuccess) {
+    noalloc_fail(err, std::string("no-allocation energy_grad: ") + cudaGetErrorString(e));
+    return 2;
+  }
+  if (E_host) *E_host = res[kNumTerms];
+  if (terms_host) memcpy(terms_host, res, sizeof(double) * kNumTerms);
+  return 0;
+}
+
 }  // namespace deft

@@ -89,4 +89,14 @@ class Engine {
   EngineImpl *impl_;
 };
 
+// Energy + gradient that allocates nothing: scratch comes from one fixed
+// file-scope device array (fmt_engine.cu).  n, V, mask, grad are device
+// pointers on the current device; work is queued on `stream` and synchronised
+// before return.  Returns 0, 1 (size or argument rejected, *err set) or
+// 2 (CUDA error, *err set).
+int noalloc_energy_grad(const GridSpec &g, const FmtSpec &f, const double *n, const double *V,
+                        const double *mask, double *grad, double *E_host, double *terms_host,
+                        cudaStream_t stream, std::string *err);
+size_t noalloc_scratch_bytes();
+
 }  // namespace deft

@@ -19,6 +19,8 @@
 #ifndef DEFT_GB300_H
 #define DEFT_GB300_H
 
+#include <stddef.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -141,6 +143,28 @@ int deft_fmt_weighted(deft_fmt *f, const double *n, int on_device, double *out5)
 /* find_chemical_potential(OfEffectivePotential(HS(R)+IdealGas()), kT, nb)
  * (src/equation-of-state.cpp:189-192): the mu that makes nb the bulk density. */
 int deft_find_chemical_potential(double R, double kT, double nb, double *mu_out);
+
+/* Energy and gradient with NO device allocation (no counterpart in the
+ * reference).  Meant for callers that cannot call cudaMalloc: a host
+ * framework whose caching allocator or up-front reservation already holds
+ * the GPU's memory, or a loop that may not allocate once it runs.  All
+ * scratch lives in one fixed device array inside the library,
+ * deft_noalloc_scratch_bytes() = 20 MiB, which every GPU that loads the
+ * library holds until the process exits; grids needing more (above about
+ * 64^3 points, or any size above 256) are rejected with DEFT_ERR_ARG.
+ * n, V, mask and grad_out are device pointers on the CURRENT device; lat, p,
+ * E_out and terms_out are host pointers.  Work runs on `stream` (a
+ * cudaStream_t, NULL = default stream) and is synchronised before return.
+ * The first call on each device looks up the array's device address; make
+ * that first call before any stream capture.  Every call shares the array
+ * and overwrites it, so calls that overlap on the GPU (other streams or
+ * host threads) race. */
+int deft_fmt_energy_grad_noalloc(const double lat[9], int Nx, int Ny, int Nz,
+                                 const deft_fmt_params *p, const double *n, const double *V,
+                                 const double *mask, double *E_out, double *grad_out,
+                                 double *terms_out, void *stream);
+/* Size in bytes of the fixed scratch array used by the call above. */
+size_t deft_noalloc_scratch_bytes(void);
 
 /* ---- minimiser ----
  * Replaces ConjugateGradient(f, gd, kT, &x, QuadraticLineMinimizer, step)
