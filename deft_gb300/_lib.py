@@ -24,6 +24,7 @@ EXPORTS = (
     "deft_grid_profile", "deft_grid_profile_count", "deft_grid_profile_entry",
     "deft_fmt_create", "deft_fmt_destroy", "deft_fmt_set_params", "deft_fmt_set_vext",
     "deft_fmt_set_mask", "deft_fmt_energy", "deft_fmt_energy_grad", "deft_fmt_weighted",
+    "deft_fmt_hessian_vector",
     "deft_find_chemical_potential",
     "deft_fmt_energy_grad_noalloc", "deft_noalloc_scratch_bytes",
     "deft_cg_create", "deft_cg_destroy", "deft_cg_set_x", "deft_cg_get_x", "deft_cg_x_device",
@@ -37,19 +38,24 @@ class DeftError(RuntimeError):
         self.status = status
 
 
+PRECISION_FP64, PRECISION_MIXED = 0, 1
+
+
 class FmtParams(ctypes.Structure):
     _fields_ = [("R", ctypes.c_double), ("kT", ctypes.c_double), ("mu", ctypes.c_double),
-                ("terms", ctypes.c_int)]
+                ("terms", ctypes.c_int), ("precision", ctypes.c_int)]
 
 
 class CgParams(ctypes.Structure):
     _fields_ = [("linesearch", ctypes.c_int), ("gtol", ctypes.c_double), ("maxiter", ctypes.c_int),
-                ("step", ctypes.c_double), ("precision", ctypes.c_double)]
+                ("step", ctypes.c_double), ("precision", ctypes.c_double),
+                ("refine_rel", ctypes.c_double)]
 
 
 class CgStatus(ctypes.Structure):
     _fields_ = [("iter", ctypes.c_int), ("evals", ctypes.c_int), ("energy", ctypes.c_double),
-                ("gnorm", ctypes.c_double), ("converged", ctypes.c_int), ("status", ctypes.c_int)]
+                ("gnorm", ctypes.c_double), ("converged", ctypes.c_int), ("status", ctypes.c_int),
+                ("evals_fp64", ctypes.c_int), ("hvps", ctypes.c_int), ("stage", ctypes.c_int)]
 
 
 _lib = None
@@ -92,6 +98,7 @@ def load():
         "deft_fmt_energy": (ctypes.c_int, [_vp, _dp, ctypes.c_int, _dp, _dp]),
         "deft_fmt_energy_grad": (ctypes.c_int, [_vp, _dp, ctypes.c_int, _dp, _dp, _dp]),
         "deft_fmt_weighted": (ctypes.c_int, [_vp, _dp, ctypes.c_int, _dp]),
+        "deft_fmt_hessian_vector": (ctypes.c_int, [_vp, _dp, _dp, ctypes.c_int, _dp]),
         "deft_find_chemical_potential": (ctypes.c_int, [ctypes.c_double, ctypes.c_double,
                                                         ctypes.c_double, _dp]),
         "deft_fmt_energy_grad_noalloc": (ctypes.c_int, [_dp, ctypes.c_int, ctypes.c_int,

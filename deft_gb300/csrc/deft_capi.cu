@@ -52,6 +52,11 @@ struct deft_cg {
   // Precision modifier state (src/Precision.cpp:23-48)
   double dEdn = 0, log_ratio_avg = 0, deltaE = 0, err_est = 0;
   bool done = false;
+  // mixed form: stage 0 = FP32 CG, 1 = FP64-residual Newton refinement
+  int stage = 0, evals_fp64 = 0, hvps = 0;
+  double g0norm = -1;
+  bool last_eval_mixed = false;          // c->g / c->E came from the FP32 evaluator
+  double *q = nullptr, *dxv = nullptr;  // refinement work vectors
 };
 
 namespace {
@@ -79,8 +84,15 @@ deft::FmtSpec spec_of(const deft_fmt *f) {
   s.kT = f->p.kT;
   s.mu = f->p.mu;
   s.terms = f->p.terms;
+  s.precision = f->p.precision == DEFT_PRECISION_MIXED ? deft::kPrecisionMixed
+                                                       : deft::kPrecisionFP64;
   if (!f->V) s.terms &= ~DEFT_TERM_VEXT;
   if (!f->mask) s.terms &= ~DEFT_TERM_MASK;
+  return s;
+}
+
+deft::FmtSpec fp64_of(deft::FmtSpec s) {
+  s.precision = deft::kPrecisionFP64;
   return s;
 }
 
@@ -296,6 +308,8 @@ int deft_grid_profile_entry(deft_grid *g, int i, const char **name, long long *l
 int deft_fmt_create(deft_grid *g, const deft_fmt_params *p, deft_fmt **out) {
   if (!g || !p || !out) return set_err(DEFT_ERR_ARG, "NULL argument");
   if (!(p->R > 0) || !(p->kT > 0)) return set_err(DEFT_ERR_ARG, "R and kT must be positive");
+  if (p->precision != DEFT_PRECISION_FP64 && p->precision != DEFT_PRECISION_MIXED)
+    return set_err(DEFT_ERR_ARG, "unknown precision");
   cudaSetDevice(g->ctx->device);
   deft_fmt *f = new deft_fmt();
   f->grid = g;
@@ -324,6 +338,8 @@ int deft_fmt_destroy(deft_fmt *f) {
 int deft_fmt_set_params(deft_fmt *f, const deft_fmt_params *p) {
   if (!f || !p) return set_err(DEFT_ERR_ARG, "NULL argument");
   if (!(p->R > 0) || !(p->kT > 0)) return set_err(DEFT_ERR_ARG, "R and kT must be positive");
+  if (p->precision != DEFT_PRECISION_FP64 && p->precision != DEFT_PRECISION_MIXED)
+    return set_err(DEFT_ERR_ARG, "unknown precision");
   f->p = *p;
   return DEFT_OK;
 }
@@ -401,6 +417,26 @@ int deft_fmt_weighted(deft_fmt *f, const double *n, int on_device, double *out5)
   return sync(g->ctx);
 }
 
+int deft_fmt_hessian_vector(deft_fmt *f, const double *n, const double *dx, int on_device,
+                            double *out) {
+  if (!f || !n || !dx || !out) return set_err(DEFT_ERR_ARG, "NULL argument");
+  if (int s = check_terms(f)) return s;
+  deft_grid *g = f->grid;
+  cudaSetDevice(g->ctx->device);
+  const double *ns, *ds;
+  if (int s = stage_in(g, n, on_device, g->in_buf, &ns)) return s;
+  if (int s = stage_in(g, dx, on_device, g->out_buf, &ds)) return s;
+  double *dst = on_device ? out : f->g_buf;
+  const deft::FmtSpec spec = spec_of(f);
+  if (g->eng->hess_setup(spec, ns) || g->eng->hvp(spec, ds, f->mask, dst)) return eng_err(g->eng);
+  if (!on_device) {
+    cudaError_t e = cudaMemcpyAsync(out, dst, sizeof(double) * nr(g), cudaMemcpyDeviceToHost,
+                                    g->ctx->stream);
+    if (e != cudaSuccess) return cuda_err(e, "device-to-host copy");
+  }
+  return sync(g->ctx);
+}
+
 int deft_find_chemical_potential(double R, double kT, double nb, double *mu_out) {
   if (!mu_out || !(R > 0) || !(kT > 0) || !(nb > 0))
     return set_err(DEFT_ERR_ARG, "R, kT and nb must be positive");
@@ -451,6 +487,8 @@ int deft_fmt_energy_grad_noalloc(const double lat[9], int Nx, int Ny, int Nz,
     return set_err(DEFT_ERR_ARG, "DEFT_TERM_VEXT set but V is NULL");
   if ((p->terms & DEFT_TERM_MASK) && !mask)
     return set_err(DEFT_ERR_ARG, "DEFT_TERM_MASK set but mask is NULL");
+  if (p->precision != DEFT_PRECISION_FP64)
+    return set_err(DEFT_ERR_ARG, "the allocation-free entry point evaluates in FP64 only");
   deft::GridSpec s;
   s.Nx = Nx;
   s.Ny = Ny;
@@ -510,6 +548,8 @@ int deft_cg_destroy(deft_cg *c) {
   cudaFree(c->g);
   cudaFree(c->d);
   cudaFree(c->gold);
+  cudaFree(c->q);
+  cudaFree(c->dxv);
   delete c;
   return DEFT_OK;
 }
@@ -529,6 +569,10 @@ static void cg_reset(deft_cg *c) {
   c->log_ratio_avg = 0;
   c->deltaE = 0;
   c->err_est = std::fmax(1.0, 2 * c->p.precision);
+  c->stage = 0;
+  c->evals_fp64 = 0;
+  c->hvps = 0;
+  c->g0norm = -1;
   const size_t bytes = sizeof(double) * nr(c->f->grid);
   cudaMemsetAsync(c->d, 0, bytes, c->f->grid->ctx->stream);
   cudaMemsetAsync(c->gold, 0, bytes, c->f->grid->ctx->stream);
@@ -564,11 +608,13 @@ namespace {
 Engine *eng_of(deft_cg *c) { return c->f->grid->eng; }
 
 // Energy + gradient at x into c->g, c->E.
-int cg_eval(deft_cg *c) {
+int cg_eval(deft_cg *c, const deft::FmtSpec &spec) {
   double E;
-  if (eng_of(c)->energy_grad(spec_of(c->f), c->x, c->f->V, c->f->mask, c->g, &E, nullptr))
+  if (eng_of(c)->energy_grad(spec, c->x, c->f->V, c->f->mask, c->g, &E, nullptr))
     return eng_err(eng_of(c));
   c->evals++;
+  if (spec.precision == deft::kPrecisionFP64) c->evals_fp64++;
+  c->last_eval_mixed = spec.precision != deft::kPrecisionFP64;
   c->E = E;
   c->e_cache = E;
   c->e_valid = true;
@@ -579,9 +625,11 @@ int cg_eval(deft_cg *c) {
 // Minimizer::energy() (src/Minimizer.h:52), cached while x is unchanged.
 int cg_energy(deft_cg *c, double *E) {
   if (!c->e_valid) {
-    if (eng_of(c)->energy(spec_of(c->f), c->x, c->f->V, c->f->mask, &c->e_cache, nullptr))
+    const deft::FmtSpec spec = spec_of(c->f);
+    if (eng_of(c)->energy(spec, c->x, c->f->V, c->f->mask, &c->e_cache, nullptr))
       return eng_err(eng_of(c));
     c->evals++;
+    if (spec.precision == deft::kPrecisionFP64) c->evals_fp64++;
     c->e_valid = true;
   }
   *E = c->e_cache;
@@ -609,14 +657,15 @@ int dots3(deft_cg *c, double *s, double *gg, double *ggold) {
 // Bracketing secant search on s(a) = grad(x + a d).d from s(0) = s0 < 0,
 // accepting |s| <= 0.1 |s0| with no energy rise beyond rounding.  Leaves x,
 // g, E, gg, ggold at the accepted point.
-int secant_search(deft_cg *c, double E0, double s0) {
+int secant_search(deft_cg *c, const deft::FmtSpec &spec, double E0, double s0) {
   double lo = 0, s_lo = s0, hi = -1, s_hi = 0, plo = 0, s_plo = s0;
   double a = c->alpha, at = 0;
-  const double etol = 1e-12 * std::fabs(E0);
+  // energies only guard against rises; FP32 sums carry ~1e-7 relative noise
+  const double etol = (spec.precision == deft::kPrecisionFP64 ? 1e-12 : 1e-6) * std::fabs(E0);
   for (int it = 0; it < 40; it++) {
     if (int st = cg_axpy(c, a - at, c->d)) return st;
     at = a;
-    if (int st = cg_eval(c)) return st;
+    if (int st = cg_eval(c, spec)) return st;
     double s, gg, ggold;
     if (int st = dots3(c, &s, &gg, &ggold)) return st;
     const double E = c->E;
@@ -661,9 +710,9 @@ int secant_search(deft_cg *c, double E0, double s0) {
   return set_err(DEFT_ERR_LINESEARCH, "secant line search did not converge in 40 evaluations");
 }
 
-int step_secant(deft_cg *c, deft_cg_status *st) {
+int step_secant(deft_cg *c, deft_cg_status *st, const deft::FmtSpec &spec, double gtol) {
   if (!c->have_g) {
-    if (int s = cg_eval(c)) return s;
+    if (int s = cg_eval(c, spec)) return s;
     const double *a[2] = {c->g, c->g};
     const double *b[2] = {c->g, c->gold};
     double o[2];
@@ -674,7 +723,8 @@ int step_secant(deft_cg *c, deft_cg_status *st) {
   if (!std::isfinite(c->E) || !std::isfinite(c->gg))
     return set_err(DEFT_ERR_NAN, "energy or gradient is not finite");
   st->gnorm = std::sqrt(c->gg);
-  if (st->gnorm < c->p.gtol) {
+  if (c->g0norm < 0) c->g0norm = st->gnorm;
+  if (st->gnorm < gtol) {
     c->done = true;
     return DEFT_OK;
   }
@@ -701,7 +751,89 @@ int step_secant(deft_cg *c, deft_cg_status *st) {
   if (c->iter > 0 && s0 != 0) c->alpha *= c->s_prev / s0;
   c->s_prev = s0;
   c->iter++;
-  if (int s = secant_search(c, c->E, s0)) return s;
+  if (int s = secant_search(c, spec, c->E, s0)) return s;
+  st->gnorm = std::sqrt(c->gg);
+  if (st->gnorm < gtol) c->done = true;
+  return DEFT_OK;
+}
+
+// One Newton refinement step of the mixed form.  The residual is the FP64
+// gradient g; the step solves H dx = -g by linear CG whose Hessian-vector
+// products run through the FP32 FFTs (Engine::hvp) with FP64 vectors and
+// dot products.  The step is accepted if the FP64 energy does not rise
+// (halved up to five times otherwise).
+int step_newton(deft_cg *c, deft_cg_status *st, const deft::FmtSpec &spec) {
+  Engine *e = eng_of(c);
+  const deft::FmtSpec s64 = fp64_of(spec);
+  const size_t bytes = sizeof(double) * nr(c->f->grid);
+  cudaStream_t stream = c->f->grid->ctx->stream;
+  if (!c->q) {
+    cudaError_t ce = cudaMalloc((void **)&c->q, bytes);
+    if (ce == cudaSuccess) ce = cudaMalloc((void **)&c->dxv, bytes);
+    if (ce != cudaSuccess) return cuda_err(ce, "cudaMalloc");
+  }
+  if (!c->have_g || c->last_eval_mixed) {
+    if (int s = cg_eval(c, s64)) return s;
+    c->last_eval_mixed = false;
+    const double *a[1] = {c->g};
+    const double *b[1] = {c->g};
+    if (e->dots(1, a, b, &c->gg)) return eng_err(e);
+  }
+  if (!std::isfinite(c->E) || !std::isfinite(c->gg))
+    return set_err(DEFT_ERR_NAN, "energy or gradient is not finite");
+  st->gnorm = std::sqrt(c->gg);
+  if (st->gnorm < c->p.gtol) {
+    c->done = true;
+    return DEFT_OK;
+  }
+  c->iter++;
+  if (e->hess_setup(spec, c->x)) return eng_err(e);
+  // r = -g (in gold), p = r (in d), dx = 0
+  double *r = c->gold, *p = c->d, *q = c->q, *dx = c->dxv;
+  if (e->scal_add(0.0, r, -1.0, c->g) || e->copy(r, p)) return eng_err(e);
+  if (cudaMemsetAsync(dx, 0, bytes, stream) != cudaSuccess) return set_err(DEFT_ERR_CUDA, "memset");
+  double rr = c->gg;
+  const double tol = std::fmax(1e-5 * st->gnorm, 0.05 * c->p.gtol);
+  for (int k = 0; k < 400; k++) {
+    if (e->hvp(spec, p, c->f->mask, q)) return eng_err(e);
+    c->hvps++;
+    double pq;
+    {
+      const double *a[1] = {p};
+      const double *b[1] = {q};
+      if (e->dots(1, a, b, &pq)) return eng_err(e);
+    }
+    if (!(pq > 0)) break;  // no positive curvature along p: keep the step so far
+    const double alpha = rr / pq;
+    if (e->axpy(alpha, p, dx) || e->axpy(-alpha, q, r)) return eng_err(e);
+    double rr_new;
+    {
+      const double *a[1] = {r};
+      const double *b[1] = {r};
+      if (e->dots(1, a, b, &rr_new)) return eng_err(e);
+    }
+    if (std::sqrt(rr_new) < tol) break;
+    if (e->scal_add(rr_new / rr, p, 1.0, r)) return eng_err(e);
+    rr = rr_new;
+  }
+  const double E0 = c->E;
+  double scale = 1.0;
+  for (int bt = 0; bt < 6; bt++) {
+    if (int s = cg_axpy(c, scale, dx)) return s;
+    if (int s = cg_eval(c, s64)) return s;
+    if (std::isfinite(c->E) && c->E <= E0 + 1e-12 * std::fabs(E0)) break;
+    if (int s = cg_axpy(c, -scale, dx)) return s;
+    scale *= 0.5;
+    if (bt == 5) {
+      if (int s = cg_eval(c, s64)) return s;
+      return set_err(DEFT_ERR_LINESEARCH, "refinement step did not lower the energy");
+    }
+  }
+  {
+    const double *a[1] = {c->g};
+    const double *b[1] = {c->g};
+    if (e->dots(1, a, b, &c->gg)) return eng_err(e);
+  }
   st->gnorm = std::sqrt(c->gg);
   if (st->gnorm < c->p.gtol) c->done = true;
   return DEFT_OK;
@@ -775,7 +907,7 @@ int step_quadratic(deft_cg *c, bool *more) {
   c->iter++;
   // energy() then grad() at the same x: one fused evaluation gives both
   if (!c->have_g)
-    if (int s = cg_eval(c)) return s;
+    if (int s = cg_eval(c, spec_of(c->f))) return s;
   const double E0 = c->E;
   if (E0 != E0) {
     *more = false;
@@ -830,8 +962,25 @@ int deft_cg_step(deft_cg *c, deft_cg_status *st) {
     if (prec) status = cg_energy(c, &old_energy);
     bool more = true;
     if (!status) {
-      if (c->p.linesearch == DEFT_LS_SECANT) {
-        status = step_secant(c, st);
+      const deft::FmtSpec spec = spec_of(c->f);
+      if (c->p.linesearch == DEFT_LS_SECANT && spec.precision == deft::kPrecisionMixed) {
+        if (c->stage == 0) {
+          // FP32 CG until the gradient has dropped by refine_rel (or the
+          // FP32 line search runs out of resolution), then refine in FP64
+          const double rel = c->p.refine_rel > 0 ? c->p.refine_rel : 1e-4;
+          const double thr = std::fmax(c->g0norm > 0 ? rel * c->g0norm : 0.0, c->p.gtol);
+          status = step_secant(c, st, spec, thr);
+          if (status == DEFT_ERR_LINESEARCH) status = DEFT_OK;
+          if (!status && (c->done || st->gnorm < thr || c->iter > 0 && !c->have_g)) {
+            c->stage = 1;
+            c->done = false;
+          }
+        } else {
+          status = step_newton(c, st, spec);
+        }
+        more = !c->done;
+      } else if (c->p.linesearch == DEFT_LS_SECANT) {
+        status = step_secant(c, st, spec, c->p.gtol);
         more = !c->done;
       } else {
         status = step_quadratic(c, &more);
@@ -867,6 +1016,9 @@ int deft_cg_step(deft_cg *c, deft_cg_status *st) {
   if (st->gnorm == 0 && c->have_g) st->gnorm = std::sqrt(c->gg);
   st->converged = c->done ? 1 : 0;
   st->status = status;
+  st->evals_fp64 = c->evals_fp64;
+  st->hvps = c->hvps;
+  st->stage = c->stage;
   return status;
 }
 

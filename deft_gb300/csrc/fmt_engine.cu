@@ -22,11 +22,13 @@
 // normalisation dV/V folded in.
 #include "fft_smem.cuh"
 #include "fmt_engine.h"
+#include "wb_phi.cuh"
 
 #include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
+#include <type_traits>
 #include <vector>
 
 namespace deft {
@@ -70,57 +72,6 @@ __device__ void weights_at(double k2, double R, double dr, double &w3, double &w
   }
 }
 
-// S(eta) = (eta + (1-eta)^2 ln(1-eta)) / eta^2 and dS/deta; the phi3
-// prefactor of src/HardSpheres.cpp:153 is S / (36 pi (1-eta)^2).  The direct
-// form is 0/0 at eta -> 0, so |eta| < 1e-2 uses its Taylor series
-// S = 3/2 - sum_{j>=1} 2 eta^j / (j (j+1) (j+2)).
-__device__ __forceinline__ void phi3_S(double eta, double &S, double &dS) {
-  if (fabs(eta) < 1e-2) {
-    double s = 1.5, ds = 0, pw = 1;
-#pragma unroll
-    for (int j = 1; j <= 12; j++) {
-      const double c = 2.0 / ((double)j * (j + 1) * (j + 2));
-      ds -= c * j * pw;
-      pw *= eta;
-      s -= c * pw;
-    }
-    S = s;
-    dS = ds;
-  } else {
-    const double l = log(1 - eta);
-    const double gg = eta + (1 - eta) * (1 - eta) * l;
-    const double dg = eta - 2 * (1 - eta) * l;
-    S = gg / (eta * eta);
-    dS = (dg * eta - 2 * gg) / (eta * eta * eta);
-  }
-}
-
-// White Bear (no tensor) phi per kT, split as (phi3, phi1, phi2), and its
-// partials with respect to (n3, n2, n2x, n2y, n2z).
-__device__ __forceinline__ void phi_wb(double R, double n3, double n2, double vx, double vy,
-                                       double vz, double phi[3], double d[5]) {
-  const double v2 = vx * vx + vy * vy + vz * vz;
-  const double omn3 = 1 - n3;
-  const double l = log(omn3);
-  const double four_pi_r = 4 * M_PI * R, four_pi_r2 = 4 * M_PI * R * R;
-  double S, dS;
-  phi3_S(n3, S, dS);
-  const double inv = 1.0 / omn3;
-  const double f3 = S * inv * inv * (1.0 / (36 * M_PI));
-  const double df3 = (dS * omn3 + 2 * S) * inv * inv * inv * (1.0 / (36 * M_PI));
-  const double q = n2 * n2 - v2;
-  const double t3 = n2 * (n2 * n2 - 3 * v2);
-  phi[0] = f3 * t3;
-  phi[1] = -n2 * l / four_pi_r2;
-  phi[2] = q / (four_pi_r * omn3);
-  d[0] = n2 / (four_pi_r2 * omn3) + q / (four_pi_r * omn3 * omn3) + df3 * t3;
-  d[1] = -l / four_pi_r2 + 2 * n2 / (four_pi_r * omn3) + f3 * 3 * q;
-  const double cv = -2 / (four_pi_r * omn3) - 6 * f3 * n2;
-  d[2] = cv * vx;
-  d[3] = cv * vy;
-  d[4] = cv * vz;
-}
-
 // Deterministic block reduction of K doubles; thread 0 gets the sums.
 template <int K>
 __device__ void block_reduce(double (&v)[K], double *smem /* 32*K */) {
@@ -148,7 +99,8 @@ __device__ void block_reduce(double (&v)[K], double *smem /* 32*K */) {
 // ---------------------------------------------------------------------------
 // Kernels
 
-__global__ void k_weight_table(Geom g, double R, double *w3, double *w2, double *wv) {
+template <typename W>
+__global__ void k_weight_table(Geom g, double R, W *w3, W *w2, W *wv) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < g.NC; i += gridDim.x * blockDim.x) {
     const int z = i % g.NzH;
     const int t = i / g.NzH;
@@ -157,9 +109,9 @@ __global__ void k_weight_table(Geom g, double R, double *w3, double *w2, double 
     const double kx = kcomp(g, 0, x, y, z), ky = kcomp(g, 1, x, y, z), kz = kcomp(g, 2, x, y, z);
     double a, b, c;
     weights_at(kx * kx + ky * ky + kz * kz, R, g.dr, a, b, c);
-    w3[i] = a * g.scale;
-    w2[i] = b * g.scale;
-    wv[i] = c * g.scale;
+    w3[i] = W(a * g.scale);
+    w2[i] = W(b * g.scale);
+    wv[i] = W(c * g.scale);
   }
 }
 
@@ -219,7 +171,7 @@ __device__ __forceinline__ void unpack_r2c_store(const typename Cplx<T>::type *r
 
 // Real fields -> half-complex along z.  grid.x = pair tiles, grid.y = field.
 template <typename T>
-__global__ void __launch_bounds__(kThreads) k_z_r2c(const T *__restrict__ in,
+__global__ void __launch_bounds__(kThreads) k_z_r2c(const double *__restrict__ in,
                                                     typename Cplx<T>::type *__restrict__ out,
                                                     Geom g, FftPlan pz, int P, T s) {
   using C = typename Cplx<T>::type;
@@ -232,7 +184,7 @@ __global__ void __launch_bounds__(kThreads) k_z_r2c(const T *__restrict__ in,
   for (int idx = threadIdx.x; idx < 2 * P * g.Nz; idx += blockDim.x) {
     const int z = idx % g.Nz, ll = idx / g.Nz;
     const int line = 2 * p0 + ll;
-    const T v = line < g.lines ? in[(size_t)line * g.Nz + z] : T(0);
+    const T v = line < g.lines ? T(in[(size_t)line * g.Nz + z]) : T(0);
     reinterpret_cast<T *>(&buf0[z * P + (ll >> 1)])[ll & 1] = v;
   }
   C *res = fft_tile<T, -1>(buf0, buf1, P, pz);
@@ -242,8 +194,8 @@ __global__ void __launch_bounds__(kThreads) k_z_r2c(const T *__restrict__ in,
 // Half-complex along z -> real fields.  grid.x = pair tiles, grid.y = field.
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_z_c2r(const typename Cplx<T>::type *__restrict__ in,
-                                                    T *__restrict__ out, Geom g, FftPlan pz, int P,
-                                                    T s) {
+                                                    double *__restrict__ out, Geom g, FftPlan pz,
+                                                    int P, double s) {
   using C = typename Cplx<T>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C *buf0 = reinterpret_cast<C *>(smem_raw);
@@ -258,7 +210,7 @@ __global__ void __launch_bounds__(kThreads) k_z_c2r(const typename Cplx<T>::type
     const int line = 2 * p0 + ll;
     if (line >= g.lines) continue;
     const C v = res[z * P + (ll >> 1)];
-    out[(size_t)line * g.Nz + z] = ((ll & 1) ? v.y : v.x) * s;
+    out[(size_t)line * g.Nz + z] = double((ll & 1) ? v.y : v.x) * s;
   }
 }
 
@@ -310,7 +262,7 @@ __global__ void __launch_bounds__(kThreads) k_x_fft(typename Cplx<T>::type *data
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_x_conv_fwd(
     const typename Cplx<T>::type *__restrict__ in, typename Cplx<T>::type *__restrict__ out5,
-    const double *__restrict__ w3, const double *__restrict__ w2, const double *__restrict__ wv,
+    const T *__restrict__ w3, const T *__restrict__ w2, const T *__restrict__ wv,
     Geom g, FftPlan px, int B) {
   using C = typename Cplx<T>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -334,14 +286,14 @@ __global__ void __launch_bounds__(kThreads) k_x_conv_fwd(
         const size_t i = (size_t)e * J + j;
         const C v = R0[idx];
         if (a == 0) {
-          const T w = T(w3[i]);
+          const T w = w3[i];
           o = C{v.x * w, v.y * w};
         } else if (a == 1) {
-          const T w = T(w2[i]);
+          const T w = w2[i];
           o = C{v.x * w, v.y * w};
         } else {
           const int y = j / g.NzH, z = j % g.NzH;
-          const T w = T(kcomp(g, a - 2, e, y, z) * wv[i]);
+          const T w = T(kcomp(g, a - 2, e, y, z)) * wv[i];
           o = C{-v.y * w, v.x * w};  // times i w
         }
       }
@@ -361,7 +313,7 @@ __global__ void __launch_bounds__(kThreads) k_x_conv_fwd(
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_x_conv_adj(
     const typename Cplx<T>::type *__restrict__ in5, typename Cplx<T>::type *__restrict__ out,
-    const double *__restrict__ w3, const double *__restrict__ w2, const double *__restrict__ wv,
+    const T *__restrict__ w3, const T *__restrict__ w2, const T *__restrict__ wv,
     Geom g, FftPlan px, int B) {
   using C = typename Cplx<T>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -385,16 +337,16 @@ __global__ void __launch_bounds__(kThreads) k_x_conv_adj(
       const C v = res[idx];
       C o = acc[idx];
       if (a == 0) {
-        const T w = T(w3[i]);
+        const T w = w3[i];
         o.x += v.x * w;
         o.y += v.y * w;
       } else if (a == 1) {
-        const T w = T(w2[i]);
+        const T w = w2[i];
         o.x += v.x * w;
         o.y += v.y * w;
       } else {
         const int y = j / g.NzH, z = j % g.NzH;
-        const T w = T(kcomp(g, a - 2, e, y, z) * wv[i]);
+        const T w = T(kcomp(g, a - 2, e, y, z)) * wv[i];
         o.x += v.y * w;  // times -i w
         o.y -= v.x * w;
       }
@@ -410,17 +362,32 @@ __global__ void __launch_bounds__(kThreads) k_x_conv_adj(
 }
 
 struct LocalArgs {
-  double R, kT, mu, nQ, dV;
+  double R, kT, mu, nQ, inv_nQ, dV;
+  WbRadius wr;
   int terms;
 };
+
+// Ideal-gas integrand kT n (ln(n/nQ) - 1) (src/IdealGas.cpp:68-72), 0 at
+// n = 0, and its derivative kT ln(n/nQ), in the arithmetic type T.
+template <typename T>
+__device__ __forceinline__ double ideal_energy(double nv, const LocalArgs &la) {
+  if (nv == 0) return 0.0;
+  const T x = T(nv);
+  return double(T(la.kT) * x * (wb_log<T>(x * T(la.inv_nQ)) - T(1)));
+}
+template <typename T>
+__device__ __forceinline__ double ideal_grad(double nv, const LocalArgs &la) {
+  return double(T(la.kT) * wb_log<T>(T(nv) * T(la.inv_nQ)));
+}
 
 // c2r of the five weighted densities, phi and local terms, per-block
 // energies, and (GRAD) r2c of the five partials dV kT dphi/dn_a in place.
 template <typename T, bool GRAD>
 __global__ void __launch_bounds__(kThreads) k_z_phi(typename Cplx<T>::type *S5,
-                                                    const T *__restrict__ n,
-                                                    const T *__restrict__ V, Geom g, FftPlan pz,
-                                                    int P, LocalArgs la, double *partials) {
+                                                    const double *__restrict__ n,
+                                                    const double *__restrict__ V, Geom g,
+                                                    FftPlan pz, int P, LocalArgs la,
+                                                    double *partials) {
   using C = typename Cplx<T>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C *buf0 = reinterpret_cast<C *>(smem_raw);
@@ -446,26 +413,26 @@ __global__ void __launch_bounds__(kThreads) k_z_phi(typename Cplx<T>::type *S5,
   for (int idx = threadIdx.x; idx < LP; idx += blockDim.x) {
     const int z = idx % Nz, ll = idx / Nz;
     const int line = 2 * p0 + ll;
-    double d[5] = {0, 0, 0, 0, 0};
+    T d[5] = {0, 0, 0, 0, 0};
     if (line < g.lines) {
       const size_t r = (size_t)line * Nz + z;
       if (hs) {
-        double phi[3];
-        phi_wb(la.R, rv[idx], rv[LP + idx], rv[2 * LP + idx], rv[3 * LP + idx], rv[4 * LP + idx],
-               phi, d);
-        acc[0] += la.kT * phi[0];
-        acc[1] += la.kT * phi[1];
-        acc[2] += la.kT * phi[2];
+        T phi[3];
+        wb_phi<T>(la.wr, rv[idx], rv[LP + idx], rv[2 * LP + idx], rv[3 * LP + idx],
+                  rv[4 * LP + idx], phi, d);
+        acc[0] += la.kT * double(phi[0]);
+        acc[1] += la.kT * double(phi[1]);
+        acc[2] += la.kT * double(phi[2]);
       }
       const double nv = n[r];
-      if (la.terms & kTermIdeal) acc[3] += nv == 0 ? 0.0 : la.kT * nv * (log(nv / la.nQ) - 1);
+      if (la.terms & kTermIdeal) acc[3] += ideal_energy<T>(nv, la);
       if (la.terms & kTermMu) acc[4] += la.mu * nv;
-      if (la.terms & kTermVext) acc[5] += (double)V[r] * nv;
+      if (la.terms & kTermVext) acc[5] += V[r] * nv;
     }
     if (GRAD) {
-      const double c = la.dV * la.kT;
+      const T c = T(la.dV * la.kT);
 #pragma unroll
-      for (int a = 0; a < 5; a++) rv[a * LP + idx] = T(c * d[a]);
+      for (int a = 0; a < 5; a++) rv[a * LP + idx] = c * d[a];
     }
   }
   block_reduce<kNumTerms>(acc, red);
@@ -488,10 +455,11 @@ __global__ void __launch_bounds__(kThreads) k_z_phi(typename Cplx<T>::type *S5,
 // c2r of the adjoint sum, + local gradient terms, masked.
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_z_grad(const typename Cplx<T>::type *__restrict__ in,
-                                                     const T *__restrict__ n,
-                                                     const T *__restrict__ V,
-                                                     const T *__restrict__ mask, T *__restrict__ grad,
-                                                     Geom g, FftPlan pz, int P, LocalArgs la) {
+                                                     const double *__restrict__ n,
+                                                     const double *__restrict__ V,
+                                                     const double *__restrict__ mask,
+                                                     double *__restrict__ grad, Geom g, FftPlan pz,
+                                                     int P, LocalArgs la) {
   using C = typename Cplx<T>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C *buf0 = reinterpret_cast<C *>(smem_raw);
@@ -515,30 +483,176 @@ __global__ void __launch_bounds__(kThreads) k_z_grad(const typename Cplx<T>::typ
     }
     double loc = 0;
     const double nv = n[r];
-    if (la.terms & kTermIdeal) loc += la.kT * log(nv / la.nQ);
+    if (la.terms & kTermIdeal) loc += ideal_grad<T>(nv, la);
     if (la.terms & kTermMu) loc += la.mu;
-    if (la.terms & kTermVext) loc += (double)V[r];
+    if (la.terms & kTermVext) loc += V[r];
     double gr = conv + la.dV * loc;
     if (la.terms & kTermMask) {
       const double m = mask[r];
       gr = m == 0 ? 0.0 : m * gr;
     }
-    grad[r] = T(gr);
+    grad[r] = gr;
+  }
+}
+
+// Hessian blocks of kT phi at the weighted densities of n (for the Newton
+// refinement of the mixed form): c2r of the five weighted densities, then
+// per point the packed symmetric 5x5 second derivative of phi (wb_hess) and
+// the ideal-gas curvature kT/n, both stored in FP32.
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_z_hess(const typename Cplx<T>::type *__restrict__ S5,
+                                                     const double *__restrict__ n, Geom g,
+                                                     FftPlan pz, int P, LocalArgs la,
+                                                     float *__restrict__ hess,
+                                                     float *__restrict__ hloc) {
+  using C = typename Cplx<T>::type;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C *buf0 = reinterpret_cast<C *>(smem_raw);
+  C *buf1 = buf0 + g.Nz * P;
+  T *rv = reinterpret_cast<T *>(buf1 + g.Nz * P);  // [5][2P][Nz]
+  const int Nz = g.Nz;
+  const int LP = 2 * P * Nz;
+  const int p0 = blockIdx.x * P;
+  for (int a = 0; a < 5; a++) {
+    pack_c2r<T>(S5 + (size_t)a * g.NC, buf0, g, p0, P);
+    const C *res = fft_tile<T, +1>(buf0, buf1, P, pz);
+    T *dst = rv + a * LP;
+    for (int idx = threadIdx.x; idx < LP; idx += blockDim.x) {
+      const int z = idx % Nz, ll = idx / Nz;
+      const C v = res[z * P + (ll >> 1)];
+      dst[idx] = (ll & 1) ? v.y : v.x;
+    }
+    __syncthreads();
+  }
+  const bool hs = la.terms & kTermHS;
+  for (int idx = threadIdx.x; idx < LP; idx += blockDim.x) {
+    const int z = idx % Nz, ll = idx / Nz;
+    const int line = 2 * p0 + ll;
+    if (line >= g.lines) continue;
+    const size_t r = (size_t)line * Nz + z;
+    T h[kHessPacked];
+    if (hs) {
+      wb_hess<T>(la.wr, rv[idx], rv[LP + idx], rv[2 * LP + idx], rv[3 * LP + idx],
+                 rv[4 * LP + idx], h);
+    } else {
+#pragma unroll
+      for (int k = 0; k < kHessPacked; k++) h[k] = T(0);
+    }
+#pragma unroll
+    for (int k = 0; k < kHessPacked; k++) hess[(size_t)k * g.NR + r] = float(h[k]);
+    const double nv = n[r];
+    hloc[r] = (la.terms & kTermIdeal) && nv > 0 ? float(la.kT / nv) : 0.0f;
+  }
+}
+
+// Hessian-vector product, middle stage: c2r of the five weighted
+// perturbations dw, dP = dV kT J dw with the stored blocks, r2c of dP in place.
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_z_jac(typename Cplx<T>::type *S5, Geom g, FftPlan pz,
+                                                    int P, double c,
+                                                    const float *__restrict__ hess) {
+  using C = typename Cplx<T>::type;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C *buf0 = reinterpret_cast<C *>(smem_raw);
+  C *buf1 = buf0 + g.Nz * P;
+  T *rv = reinterpret_cast<T *>(buf1 + g.Nz * P);  // [5][2P][Nz]
+  const int Nz = g.Nz;
+  const int LP = 2 * P * Nz;
+  const int p0 = blockIdx.x * P;
+  for (int a = 0; a < 5; a++) {
+    pack_c2r<T>(S5 + (size_t)a * g.NC, buf0, g, p0, P);
+    const C *res = fft_tile<T, +1>(buf0, buf1, P, pz);
+    T *dst = rv + a * LP;
+    for (int idx = threadIdx.x; idx < LP; idx += blockDim.x) {
+      const int z = idx % Nz, ll = idx / Nz;
+      const C v = res[z * P + (ll >> 1)];
+      dst[idx] = (ll & 1) ? v.y : v.x;
+    }
+    __syncthreads();
+  }
+  const T cc = T(c);
+  for (int idx = threadIdx.x; idx < LP; idx += blockDim.x) {
+    const int z = idx % Nz, ll = idx / Nz;
+    const int line = 2 * p0 + ll;
+    T o[5] = {0, 0, 0, 0, 0};
+    if (line < g.lines) {
+      const size_t r = (size_t)line * Nz + z;
+      T h[kHessPacked];
+#pragma unroll
+      for (int k = 0; k < kHessPacked; k++) h[k] = T(hess[(size_t)k * g.NR + r]);
+      const T d3 = rv[idx], d2 = rv[LP + idx], dx = rv[2 * LP + idx], dy = rv[3 * LP + idx],
+              dz = rv[4 * LP + idx];
+      o[0] = h[0] * d3 + h[1] * d2 + h[2] * dx + h[3] * dy + h[4] * dz;
+      o[1] = h[1] * d3 + h[5] * d2 + h[6] * dx + h[7] * dy + h[8] * dz;
+      o[2] = h[2] * d3 + h[6] * d2 + h[9] * dx;
+      o[3] = h[3] * d3 + h[7] * d2 + h[9] * dy;
+      o[4] = h[4] * d3 + h[8] * d2 + h[9] * dz;
+    }
+#pragma unroll
+    for (int a = 0; a < 5; a++) rv[a * LP + idx] = cc * o[a];
+  }
+  __syncthreads();
+  for (int a = 0; a < 5; a++) {
+    const T *src = rv + a * LP;
+    for (int idx = threadIdx.x; idx < P * Nz; idx += blockDim.x) {
+      const int pb = idx % P, z = idx / P;
+      buf0[idx] = C{src[(2 * pb) * Nz + z], src[(2 * pb + 1) * Nz + z]};
+    }
+    const C *res = fft_tile<T, -1>(buf0, buf1, P, pz);
+    unpack_r2c_store<T>(res, S5 + (size_t)a * g.NC, g, p0, P, T(1));
+    __syncthreads();
+  }
+}
+
+// Hessian-vector product, last stage: c2r of the adjoint sum plus the
+// ideal-gas curvature dV kT/n * dx, masked (masked points give 0).
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_z_hvp_out(
+    const typename Cplx<T>::type *__restrict__ in, const double *__restrict__ dx,
+    const float *__restrict__ hloc, const double *__restrict__ mask, double *__restrict__ out,
+    Geom g, FftPlan pz, int P, LocalArgs la) {
+  using C = typename Cplx<T>::type;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C *buf0 = reinterpret_cast<C *>(smem_raw);
+  C *buf1 = buf0 + g.Nz * P;
+  const int p0 = blockIdx.x * P;
+  const bool hs = la.terms & kTermHS;
+  const C *res = nullptr;
+  if (hs) {
+    pack_c2r<T>(in, buf0, g, p0, P);
+    res = fft_tile<T, +1>(buf0, buf1, P, pz);
+  }
+  for (int idx = threadIdx.x; idx < 2 * P * g.Nz; idx += blockDim.x) {
+    const int z = idx % g.Nz, ll = idx / g.Nz;
+    const int line = 2 * p0 + ll;
+    if (line >= g.lines) continue;
+    const size_t r = (size_t)line * g.Nz + z;
+    double conv = 0;
+    if (hs) {
+      const C v = res[z * P + (ll >> 1)];
+      conv = (ll & 1) ? v.y : v.x;
+    }
+    double o = conv + la.dV * double(hloc[r]) * dx[r];
+    if (la.terms & kTermMask) {
+      const double m = mask[r];
+      o = m == 0 ? 0.0 : m * o;
+    }
+    out[r] = o;
   }
 }
 
 // Energy partials of the local terms only (no hard spheres).
 template <typename T>
-__global__ void __launch_bounds__(kThreads) k_local_energy(const T *__restrict__ n,
-                                                           const T *__restrict__ V, Geom g,
+__global__ void __launch_bounds__(kThreads) k_local_energy(const double *__restrict__ n,
+                                                           const double *__restrict__ V, Geom g,
                                                            LocalArgs la, double *partials) {
   __shared__ double red[32 * kNumTerms];
   double acc[kNumTerms] = {0, 0, 0, 0, 0, 0};
   for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < g.NR; r += gridDim.x * blockDim.x) {
     const double nv = n[r];
-    if (la.terms & kTermIdeal) acc[3] += nv == 0 ? 0.0 : la.kT * nv * (log(nv / la.nQ) - 1);
+    if (la.terms & kTermIdeal) acc[3] += ideal_energy<T>(nv, la);
     if (la.terms & kTermMu) acc[4] += la.mu * nv;
-    if (la.terms & kTermVext) acc[5] += (double)V[r] * nv;
+    if (la.terms & kTermVext) acc[5] += V[r] * nv;
   }
   block_reduce<kNumTerms>(acc, red);
   if (threadIdx.x == 0)
@@ -651,12 +765,12 @@ int tile_width(int lines, int L, size_t bytes_per_elem, int nbuf, int cap) {
 enum KernelId {
   kK_z_r2c, kK_z_c2r, kK_y_fft1, kK_y_fft5, kK_x_fft, kK_x_conv_fwd, kK_x_conv_adj, kK_z_phi_grad,
   kK_z_phi_energy, kK_z_grad, kK_local_energy, kK_reduce_terms, kK_dots, kK_axpy, kK_scal_add,
-  kK_weight_table, kNumKernels
+  kK_weight_table, kK_z_hess, kK_z_jac, kK_z_hvp_out, kNumKernels
 };
 const char *const kKernelNames[kNumKernels] = {
     "z_r2c", "z_c2r", "y_fft_1field", "y_fft_5fields", "x_fft", "x_conv_fwd", "x_conv_adj", "z_phi_grad",
     "z_phi_energy", "z_grad", "local_energy", "reduce_terms", "dots", "axpy", "scal_add",
-    "weight_table"};
+    "weight_table", "z_hess", "z_jac", "z_hvp_out"};
 
 class EngineImpl {
  public:
@@ -711,6 +825,12 @@ class EngineImpl {
   double2 *S0 = nullptr, *S5 = nullptr;
   double *w3 = nullptr, *w2 = nullptr, *wv = nullptr;
   double table_R = -1;
+  // mixed form: FP32 twiddles and weight table (spectra share S0/S5)
+  FftPlan pxf{}, pyf{}, pzf{};
+  float2 *tw_xf = nullptr, *tw_yf = nullptr, *tw_zf = nullptr;
+  float *w3f = nullptr, *w2f = nullptr, *wvf = nullptr;
+  double table_Rf = -1;
+  float *hess = nullptr, *hloc = nullptr;  // Newton refinement: Hessian blocks
   double *partials = nullptr;
   int max_blocks = 0;
   double *results = nullptr;       // device, 8
@@ -733,6 +853,14 @@ class EngineImpl {
     cudaFree(tw_x);
     cudaFree(tw_y);
     cudaFree(tw_z);
+    cudaFree(tw_xf);
+    cudaFree(tw_yf);
+    cudaFree(tw_zf);
+    cudaFree(w3f);
+    cudaFree(w2f);
+    cudaFree(wvf);
+    cudaFree(hess);
+    cudaFree(hloc);
     cudaFree(S0);
     cudaFree(S5);
     cudaFree(w3);
@@ -763,22 +891,42 @@ class EngineImpl {
     return 0;
   }
 
-  int make_plan(int n, FftPlan &p, double2 **tw) {
+  int make_plan(int n, FftPlan &p, double2 **tw, FftPlan &pf, float2 **twf) {
     if (!factorize(n, p)) {
       err = "grid size " + std::to_string(n) + " has a prime factor above 13";
       return -1;
     }
+    pf = p;
     std::vector<double2> h(n);
+    std::vector<float2> hf(n);
     const long double twopi = 6.283185307179586476925286766559005768L;
     for (int t = 0; t < n; t++) {
       const long double a = twopi * (long double)t / (long double)n;
       h[t] = make_double2((double)cosl(a), (double)-sinl(a));
+      hf[t] = make_float2((float)cosl(a), (float)-sinl(a));
     }
-    if (alloc(tw, sizeof(double2) * n)) return -1;
+    if (alloc(tw, sizeof(double2) * n) || alloc(twf, sizeof(float2) * n)) return -1;
     cudaError_t e = cudaMemcpy(*tw, h.data(), sizeof(double2) * n, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(*twf, hf.data(), sizeof(float2) * n, cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return fail("twiddle upload", e);
     p.tw = *tw;
+    pf.tw = *twf;
     return 0;
+  }
+
+  template <typename T> const FftPlan &plan(int axis) const {
+    if constexpr (std::is_same<T, float>::value) return axis == 0 ? pxf : axis == 1 ? pyf : pzf;
+    else return axis == 0 ? px : axis == 1 ? py : pz;
+  }
+  template <typename T> typename Cplx<T>::type *spec0() {
+    return reinterpret_cast<typename Cplx<T>::type *>(S0);
+  }
+  template <typename T> typename Cplx<T>::type *spec5() {
+    return reinterpret_cast<typename Cplx<T>::type *>(S5);
+  }
+  template <typename T> const T *table(int which) const {
+    if constexpr (std::is_same<T, float>::value) return which == 0 ? w3f : which == 1 ? w2f : wvf;
+    else return which == 0 ? w3 : which == 1 ? w2 : wv;
   }
 
   int init(const GridSpec &s, cudaStream_t st) {
@@ -824,7 +972,8 @@ class EngineImpl {
     for (int i = 0; i < 3; i++)
       for (int j = 0; j < 3; j++) g.Bm[3 * i + j] = 2 * M_PI * inv[3 * j + i];
 
-    if (make_plan(s.Nx, px, &tw_x) || make_plan(s.Ny, py, &tw_y) || make_plan(s.Nz, pz, &tw_z))
+    if (make_plan(s.Nx, px, &tw_x, pxf, &tw_xf) || make_plan(s.Ny, py, &tw_y, pyf, &tw_yf) ||
+        make_plan(s.Nz, pz, &tw_z, pzf, &tw_zf))
       return -1;
 
     // tile widths
@@ -862,6 +1011,18 @@ class EngineImpl {
     set_smem(k_z_phi<double, false>, smem_phi);
     set_smem(k_z_phi<double, true>, smem_phi);
     set_smem(k_z_grad<double>, smem_z);
+    // the FP32 kernels use the same tiles (half the bytes)
+    set_smem(k_z_r2c<float>, smem_z);
+    set_smem(k_y_fft<float, -1>, smem_y);
+    set_smem(k_y_fft<float, +1>, smem_y);
+    set_smem(k_x_conv_fwd<float>, smem_x3);
+    set_smem(k_x_conv_adj<float>, smem_x3);
+    set_smem(k_z_phi<float, false>, smem_phi);
+    set_smem(k_z_phi<float, true>, smem_phi);
+    set_smem(k_z_grad<float>, smem_z);
+    set_smem(k_z_hess<float>, smem_phi);
+    set_smem(k_z_jac<float>, smem_phi);
+    set_smem(k_z_hvp_out<float>, smem_z);
 
     if (alloc(&S0, cs * g.NC) || alloc(&S5, 5 * cs * g.NC) || alloc(&w3, sizeof(double) * g.NC) ||
         alloc(&w2, sizeof(double) * g.NC) || alloc(&wv, sizeof(double) * g.NC))
@@ -886,39 +1047,52 @@ class EngineImpl {
     return check("engine init");
   }
 
-  int ensure_table(double R) {
-    if (R == table_R) return 0;
+  template <typename T> int ensure_table(double R) {
     const int blocks = (g.NC + kThreads - 1) / kThreads;
-    pre(kK_weight_table);
-    k_weight_table<<<blocks < 4096 ? blocks : 4096, kThreads, 0, stream>>>(g, R, w3, w2, wv);
-    post(kK_weight_table);
-    if (check("weight table")) return -1;
-    table_R = R;
-    return 0;
+    const int nb = blocks < 4096 ? blocks : 4096;
+    if constexpr (std::is_same<T, float>::value) {
+      if (R == table_Rf) return 0;
+      if (!w3f && (alloc(&w3f, sizeof(float) * g.NC) || alloc(&w2f, sizeof(float) * g.NC) ||
+                   alloc(&wvf, sizeof(float) * g.NC)))
+        return -1;
+      pre(kK_weight_table);
+      k_weight_table<float><<<nb, kThreads, 0, stream>>>(g, R, w3f, w2f, wvf);
+      post(kK_weight_table);
+      table_Rf = R;
+    } else {
+      if (R == table_R) return 0;
+      pre(kK_weight_table);
+      k_weight_table<double><<<nb, kThreads, 0, stream>>>(g, R, w3, w2, wv);
+      post(kK_weight_table);
+      table_R = R;
+    }
+    return check("weight table");
   }
 
   int pairs_tiles(int P) const { return ((g.lines + 1) / 2 + P - 1) / P; }
 
-  void y_fft(double2 *data, int nf, int sign) {
+  template <typename T> void y_fft(typename Cplx<T>::type *data, int nf, int sign) {
     dim3 grid((g.NzH + By - 1) / By, g.Nx, nf);
     const int kid = nf == 1 ? kK_y_fft1 : kK_y_fft5;
     pre(kid);
-    if (sign < 0) k_y_fft<double, -1><<<grid, kThreads, smem_y, stream>>>(data, g, py, By);
-    else k_y_fft<double, +1><<<grid, kThreads, smem_y, stream>>>(data, g, py, By);
+    if (sign < 0) k_y_fft<T, -1><<<grid, kThreads, smem_y, stream>>>(data, g, plan<T>(1), By);
+    else k_y_fft<T, +1><<<grid, kThreads, smem_y, stream>>>(data, g, plan<T>(1), By);
     post(kid);
   }
   int x_tiles() const { return (g.Ny * g.NzH + Bx - 1) / Bx; }
 
-  int forward_weighted(const FmtSpec &f, const double *n) {
-    if (ensure_table(f.R)) return -1;
+  template <typename T> int forward_weighted(const FmtSpec &f, const double *n) {
+    if (ensure_table<T>(f.R)) return -1;
     pre(kK_z_r2c);
-    k_z_r2c<double><<<dim3(pairs_tiles(Pz), 1), kThreads, smem_z, stream>>>(n, S0, g, pz, Pz, 1.0);
+    k_z_r2c<T><<<dim3(pairs_tiles(Pz), 1), kThreads, smem_z, stream>>>(n, spec0<T>(), g,
+                                                                       plan<T>(2), Pz, T(1));
     post(kK_z_r2c);
-    y_fft(S0, 1, -1);
+    y_fft<T>(spec0<T>(), 1, -1);
     pre(kK_x_conv_fwd);
-    k_x_conv_fwd<double><<<x_tiles(), kThreads, smem_x3, stream>>>(S0, S5, w3, w2, wv, g, px, Bx);
+    k_x_conv_fwd<T><<<x_tiles(), kThreads, smem_x3, stream>>>(
+        spec0<T>(), spec5<T>(), table<T>(0), table<T>(1), table<T>(2), g, plan<T>(0), Bx);
     post(kK_x_conv_fwd);
-    y_fft(S5, 5, +1);
+    y_fft<T>(spec5<T>(), 5, +1);
     return check("forward convolution");
   }
 
@@ -928,7 +1102,10 @@ class EngineImpl {
     la.kT = f.kT;
     la.mu = f.mu;
     la.nQ = nQ_of(f.kT);
+    la.inv_nQ = 1.0 / la.nQ;
     la.dV = g.dV;
+    la.wr.inv_4piR = 1.0 / (4 * M_PI * f.R);
+    la.wr.inv_4piR2 = 1.0 / (4 * M_PI * f.R * f.R);
     la.terms = f.terms;
     return la;
   }
@@ -946,44 +1123,89 @@ class EngineImpl {
     return 0;
   }
 
+  template <typename T>
   int eval(const FmtSpec &f, const double *n, const double *V, const double *mask, double *grad,
            double *E_host, double *terms_host) {
     const LocalArgs la = local_args(f);
     int nblk;
     if (f.terms & kTermHS) {
-      if (forward_weighted(f, n)) return -1;
+      if (forward_weighted<T>(f, n)) return -1;
       nblk = pairs_tiles(Pphi);
       pre(grad ? kK_z_phi_grad : kK_z_phi_energy);
       if (grad)
-        k_z_phi<double, true><<<nblk, kThreads, smem_phi, stream>>>(S5, n, V, g, pz, Pphi, la,
-                                                                    partials);
+        k_z_phi<T, true><<<nblk, kThreads, smem_phi, stream>>>(spec5<T>(), n, V, g, plan<T>(2),
+                                                               Pphi, la, partials);
       else
-        k_z_phi<double, false><<<nblk, kThreads, smem_phi, stream>>>(S5, n, V, g, pz, Pphi, la,
-                                                                     partials);
+        k_z_phi<T, false><<<nblk, kThreads, smem_phi, stream>>>(spec5<T>(), n, V, g, plan<T>(2),
+                                                                Pphi, la, partials);
       post(grad ? kK_z_phi_grad : kK_z_phi_energy);
       if (check("phi")) return -1;
       if (grad) {
-        y_fft(S5, 5, -1);
+        y_fft<T>(spec5<T>(), 5, -1);
         pre(kK_x_conv_adj);
-        k_x_conv_adj<double><<<x_tiles(), kThreads, smem_x3, stream>>>(S5, S0, w3, w2, wv, g, px,
-                                                                       Bx);
+        k_x_conv_adj<T><<<x_tiles(), kThreads, smem_x3, stream>>>(
+            spec5<T>(), spec0<T>(), table<T>(0), table<T>(1), table<T>(2), g, plan<T>(0), Bx);
         post(kK_x_conv_adj);
-        y_fft(S0, 1, +1);
+        y_fft<T>(spec0<T>(), 1, +1);
       }
     } else {
       nblk = 4 * 152;
       pre(kK_local_energy);
-      k_local_energy<double><<<nblk, kThreads, 0, stream>>>(n, V, g, la, partials);
+      k_local_energy<T><<<nblk, kThreads, 0, stream>>>(n, V, g, la, partials);
       post(kK_local_energy);
     }
     if (grad) {
       pre(kK_z_grad);
-      k_z_grad<double><<<pairs_tiles(Pz), kThreads, smem_z, stream>>>(S0, n, V, mask, grad, g, pz,
-                                                                       Pz, la);
+      k_z_grad<T><<<pairs_tiles(Pz), kThreads, smem_z, stream>>>(spec0<T>(), n, V, mask, grad, g,
+                                                                  plan<T>(2), Pz, la);
       post(kK_z_grad);
     }
     if (check("gradient")) return -1;
     return finish_energy(nblk, E_host, terms_host);
+  }
+  int hess_setup(const FmtSpec &f, const double *n) {
+    if (!hess && (alloc(&hess, sizeof(float) * kHessPacked * (size_t)g.NR) ||
+                  alloc(&hloc, sizeof(float) * (size_t)g.NR)))
+      return -1;
+    const LocalArgs la = local_args(f);
+    if (f.terms & kTermHS) {
+      if (forward_weighted<float>(f, n)) return -1;
+    }
+    pre(kK_z_hess);
+    k_z_hess<float><<<pairs_tiles(Pphi), kThreads, smem_phi, stream>>>(
+        spec5<float>(), n, g, plan<float>(2), Pphi, la, hess, hloc);
+    post(kK_z_hess);
+    return check("hessian blocks");
+  }
+
+  int hvp(const FmtSpec &f, const double *dx, const double *mask, double *out) {
+    const LocalArgs la = local_args(f);
+    if (f.terms & kTermHS) {
+      if (forward_weighted<float>(f, dx)) return -1;
+      pre(kK_z_jac);
+      k_z_jac<float><<<pairs_tiles(Pphi), kThreads, smem_phi, stream>>>(
+          spec5<float>(), g, plan<float>(2), Pphi, g.dV * f.kT, hess);
+      post(kK_z_jac);
+      y_fft<float>(spec5<float>(), 5, -1);
+      pre(kK_x_conv_adj);
+      k_x_conv_adj<float><<<x_tiles(), kThreads, smem_x3, stream>>>(
+          spec5<float>(), spec0<float>(), table<float>(0), table<float>(1), table<float>(2), g,
+          plan<float>(0), Bx);
+      post(kK_x_conv_adj);
+      y_fft<float>(spec0<float>(), 1, +1);
+    }
+    pre(kK_z_hvp_out);
+    k_z_hvp_out<float><<<pairs_tiles(Pz), kThreads, smem_z, stream>>>(
+        spec0<float>(), dx, hloc, mask, out, g, plan<float>(2), Pz, la);
+    post(kK_z_hvp_out);
+    return check("hessian-vector product");
+  }
+
+  int eval_any(const FmtSpec &f, const double *n, const double *V, const double *mask,
+               double *grad, double *E_host, double *terms_host) {
+    if (f.precision == kPrecisionMixed)
+      return eval<float>(f, n, V, mask, grad, E_host, terms_host);
+    return eval<double>(f, n, V, mask, grad, E_host, terms_host);
   }
 };
 
@@ -1011,7 +1233,7 @@ int Engine::fft(const double *in, double2 *out) {
     k_z_r2c<double><<<dim3(e.pairs_tiles(e.Pz), 1), kThreads, e.smem_z, e.stream>>>(in, out, e.g, e.pz,
                                                                                  e.Pz, 1.0);
     e.post(kK_z_r2c);
-  e.y_fft(out, 1, -1);
+  e.y_fft<double>(out, 1, -1);
   e.pre(kK_x_fft);
     k_x_fft<double, -1><<<e.x_tiles(), kThreads, e.smem_x2, e.stream>>>(out, e.g, e.px, e.Bx, e.g.dV);
     e.post(kK_x_fft);
@@ -1024,7 +1246,7 @@ int Engine::ifft(const double2 *in, double *out) {
   e.pre(kK_x_fft);
     k_x_fft<double, +1><<<e.x_tiles(), kThreads, e.smem_x2, e.stream>>>(e.S0, e.g, e.px, e.Bx, 1.0);
     e.post(kK_x_fft);
-  e.y_fft(e.S0, 1, +1);
+  e.y_fft<double>(e.S0, 1, +1);
   e.pre(kK_z_c2r);
     k_z_c2r<double><<<dim3(e.pairs_tiles(e.Pz), 1), kThreads, e.smem_z, e.stream>>>(
       e.S0, out, e.g, e.pz, e.Pz, 1.0 / e.g.vol);
@@ -1034,7 +1256,7 @@ int Engine::ifft(const double2 *in, double *out) {
 
 int Engine::weighted(const FmtSpec &f, const double *n, double *out5) {
   EngineImpl &e = *impl_;
-  if (e.forward_weighted(f, n)) return -1;
+  if (e.forward_weighted<double>(f, n)) return -1;
   e.pre(kK_z_c2r);
     k_z_c2r<double><<<dim3(e.pairs_tiles(e.Pz), 5), kThreads, e.smem_z, e.stream>>>(e.S5, out5, e.g,
                                                                                  e.pz, e.Pz, 1.0);
@@ -1044,12 +1266,18 @@ int Engine::weighted(const FmtSpec &f, const double *n, double *out5) {
 
 int Engine::energy(const FmtSpec &f, const double *n, const double *V, const double *mask,
                    double *E_host, double *terms_host) {
-  return impl_->eval(f, n, V, mask, nullptr, E_host, terms_host);
+  return impl_->eval_any(f, n, V, mask, nullptr, E_host, terms_host);
 }
 
 int Engine::energy_grad(const FmtSpec &f, const double *n, const double *V, const double *mask,
                         double *grad, double *E_host, double *terms_host) {
-  return impl_->eval(f, n, V, mask, grad, E_host, terms_host);
+  return impl_->eval_any(f, n, V, mask, grad, E_host, terms_host);
+}
+
+int Engine::hess_setup(const FmtSpec &f, const double *n) { return impl_->hess_setup(f, n); }
+
+int Engine::hvp(const FmtSpec &f, const double *dx, const double *mask, double *out) {
+  return impl_->hvp(f, dx, mask, out);
 }
 
 int Engine::dots(int k, const double *const *a, const double *const *b, double *out_host) {
@@ -1311,14 +1539,18 @@ int noalloc_energy_grad(const GridSpec &s, const FmtSpec &f, const double *n, co
   la.kT = f.kT;
   la.mu = f.mu;
   la.nQ = nQ_of(f.kT);
+  la.inv_nQ = 1.0 / la.nQ;
   la.dV = g.dV;
+  la.wr.inv_4piR = 1.0 / (4 * M_PI * f.R);
+  la.wr.inv_4piR2 = 1.0 / (4 * M_PI * f.R * f.R);
   la.terms = f.terms;
   const int ptiles_z = (pairs + Pz - 1) / Pz;
   const int xt = (g.Ny * g.NzH + Bx - 1) / Bx;
   const dim3 ygrid1((g.NzH + By - 1) / By, g.Nx, 1), ygrid5((g.NzH + By - 1) / By, g.Nx, 5);
   {
     const int blocks = (g.NC + kThreads - 1) / kThreads;
-    k_weight_table<<<blocks < 4096 ? blocks : 4096, kThreads, 0, stream>>>(g, f.R, w3, w2, wv);
+    k_weight_table<double><<<blocks < 4096 ? blocks : 4096, kThreads, 0, stream>>>(g, f.R, w3, w2,
+                                                                                  wv);
   }
   if (f.terms & kTermHS) {
     k_z_r2c<double><<<dim3(ptiles_z, 1), kThreads, smem_z, stream>>>(n, S0, g, pz, Pz, 1.0);

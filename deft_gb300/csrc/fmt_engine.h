@@ -26,9 +26,15 @@ struct GridSpec {
   double lat[9];  // a1 = lat[0..2], a2 = lat[3..5], a3 = lat[6..8]
 };
 
+enum Precision {
+  kPrecisionFP64 = 0,   // everything FP64
+  kPrecisionMixed = 1,  // FFTs, weights and phi in FP32; reductions FP64
+};
+
 struct FmtSpec {
   double R, kT, mu;
   int terms;
+  int precision = kPrecisionFP64;
 };
 
 struct Geom {
@@ -67,6 +73,13 @@ class Engine {
   // Energy and masked gradient (grad: NR reals on device).
   int energy_grad(const FmtSpec &f, const double *n, const double *V, const double *mask,
                   double *grad, double *E_host, double *terms_host);
+
+  // Newton refinement of the mixed form: hess_setup stores, at the point n,
+  // the packed second derivatives of phi (FP32, from FP32 weighted
+  // densities) and the ideal-gas curvature; hvp then gives out = H dx, the
+  // (masked) Hessian of the functional times dx, through FP32 FFTs.
+  int hess_setup(const FmtSpec &f, const double *n);
+  int hvp(const FmtSpec &f, const double *dx, const double *mask, double *out);
 
   // Vector kernels (NR-long device vectors).
   // out_host[i] = a_i . b_i for i < k (k <= 3), one pass, one sync.

@@ -53,11 +53,17 @@ typedef struct deft_grid deft_grid;
 typedef struct deft_fmt deft_fmt;
 typedef struct deft_cg deft_cg;
 
+/* Arithmetic of the evaluator. */
+#define DEFT_PRECISION_FP64 0   /* everything in FP64 (the reference's precision) */
+#define DEFT_PRECISION_MIXED 1  /* FFTs, weights and phi in FP32; energies, dot products,
+                                   line search and the final refinement in FP64 */
+
 typedef struct {
   double R;   /* hard-sphere radius */
   double kT;  /* temperature (the kT argument of Functional::integral, src/Functional.h:131) */
   double mu;  /* ChemicalPotential coefficient (the tree adds mu*n) */
   int terms;  /* DEFT_TERM_* bit set */
+  int precision; /* DEFT_PRECISION_*; the allocation-free entry point is FP64 only */
 } deft_fmt_params;
 
 typedef struct {
@@ -66,15 +72,21 @@ typedef struct {
   int maxiter;      /* CG iteration limit */
   double step;      /* initial step (ConjugateGradient's stepsize, src/LineMinimizer.h:18-19) */
   double precision; /* >0: also stop by Precision(eps) (src/Precision.cpp:53-151) */
+  double refine_rel; /* mixed evaluator only: leave the FP32 CG stage for the FP64-residual
+                        Newton refinement once |grad| < refine_rel * |grad at start|
+                        (0 = default 1e-4) */
 } deft_cg_params;
 
 typedef struct {
-  int iter;          /* CG iterations done */
-  int evals;         /* functional evaluations (energy or energy+gradient) */
+  int iter;          /* CG iterations (plus Newton refinement steps) done */
+  int evals;         /* functional evaluations (energy or energy+gradient, any precision) */
   double energy;     /* current energy */
   double gnorm;      /* |grad|_2 at the current point (secant search; 0 if unknown) */
   int converged;     /* 1 if the stopping rule was met */
   int status;        /* DEFT_OK or the error that ended the run */
+  int evals_fp64;    /* of evals, those done in FP64 */
+  int hvps;          /* Hessian-vector products of the refinement (mixed form) */
+  int stage;         /* mixed form: 0 = FP32 CG, 1 = FP64-residual refinement */
 } deft_cg_status;
 
 /* ---- errors ---- */
@@ -140,6 +152,11 @@ int deft_fmt_energy_grad(deft_fmt *f, const double *n, int on_device, double *E_
 /* The weighted densities n3, n2, n2x, n2y, n2z (5 fields, out5), i.e.
  * StepConvolve/ShellConvolve/x,y,zShellConvolve(R) (src/Gaussian.cpp:82-102). */
 int deft_fmt_weighted(deft_fmt *f, const double *n, int on_device, double *out5);
+/* Second derivative of the functional at n applied to dx (masked like the
+ * gradient): the FP32 Hessian-vector product used by the mixed form's Newton
+ * refinement (no reference counterpart; the reference has no Hessian). */
+int deft_fmt_hessian_vector(deft_fmt *f, const double *n, const double *dx, int on_device,
+                            double *out);
 /* find_chemical_potential(OfEffectivePotential(HS(R)+IdealGas()), kT, nb)
  * (src/equation-of-state.cpp:189-192): the mu that makes nb the bulk density. */
 int deft_find_chemical_potential(double R, double kT, double nb, double *mu_out);

@@ -54,10 +54,10 @@ class Grid:
 
 
 class Fmt:
-    def __init__(self, grid, R=1.0, kT=1.0, mu=0.0, terms=7, V=None, mask=None):
+    def __init__(self, grid, R=1.0, kT=1.0, mu=0.0, terms=7, V=None, mask=None, precision=0):
         self.L = grid.L
         self.grid = grid
-        p = _lib.FmtParams(R, kT, mu, terms)
+        p = _lib.FmtParams(R, kT, mu, terms, precision)
         h = ctypes.c_void_p()
         check(self.L.deft_fmt_create(grid.h, ctypes.byref(p), ctypes.byref(h)))
         self.h = h
@@ -84,6 +84,14 @@ class Fmt:
                                           g.ctypes.data, t.ctypes.data))
         return E.value, g, t
 
+    def hessian_vector(self, n, dx):
+        n = np.ascontiguousarray(n, dtype=np.float64)
+        dx = np.ascontiguousarray(dx, dtype=np.float64)
+        out = np.empty(self.grid.size)
+        check(self.L.deft_fmt_hessian_vector(self.h, n.ctypes.data, dx.ctypes.data, 0,
+                                             out.ctypes.data))
+        return out
+
     def weighted(self, n):
         n = np.ascontiguousarray(n, dtype=np.float64)
         out = np.empty(5 * self.grid.size)
@@ -96,10 +104,10 @@ class Fmt:
 
 class CG:
     def __init__(self, fmt, linesearch=_lib.LS_SECANT, gtol=1e-9, maxiter=0, step=1.0,
-                 precision=0.0):
+                 precision=0.0, refine_rel=0.0):
         self.L = fmt.L
         self.size = fmt.grid.size
-        p = _lib.CgParams(linesearch, gtol, maxiter, step, precision)
+        p = _lib.CgParams(linesearch, gtol, maxiter, step, precision, refine_rel)
         h = ctypes.c_void_p()
         check(self.L.deft_cg_create(fmt.h, ctypes.byref(p), ctypes.byref(h)))
         self.h = h

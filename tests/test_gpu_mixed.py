@@ -1,0 +1,101 @@
+"""GPU tests of the mixed form (FFTs, weights and phi in FP32; energies,
+dot products, line search and the final refinement in FP64) against the FP64
+oracle.  Stated tolerances: single mixed evaluation -- energy 2e-6 relative,
+gradient 2e-5 relative to its max; converged mixed solve -- FP64 gradient
+norm below the FP64 tolerance and profile within 1e-8 of the oracle's."""
+import math
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    from tests.capi import Ctx
+    c = Ctx(0)
+    yield c
+    c.close()
+
+
+def _slit(N=32, Nxy=8):
+    from deft_gb300.workloads import Slit
+    return Slit(N=N, dx=0.2, eta=0.3, Nxy=Nxy, seed=1)
+
+
+@pytest.mark.parametrize("shape", [(8, 8, 32), (16, 12, 15), (48, 20, 10)])
+def test_mixed_energy_grad_vs_oracle(ctx, oracle_mod, shape):
+    from deft_gb300 import _lib
+    from tests.capi import Fmt, Grid
+    O = oracle_mod
+    rng = np.random.default_rng(4)
+    lat = np.diag([0.2 * s for s in shape])
+    nb = 0.3 / (4 * math.pi / 3)
+    mu = O.find_mu(1.0, 1.0, nb)
+    n = nb * (1 + 0.2 * rng.standard_normal(int(np.prod(shape))))
+    P = O.Problem(lat, shape, mu=mu)
+    Er, gr = P.energy_grad(n)
+    g = Grid(ctx, lat, shape)
+    f = Fmt(g, mu=mu, terms=P.terms, precision=_lib.PRECISION_MIXED)
+    E, grad, _ = f.energy_grad(n)
+    assert abs(E / Er - 1) < 2e-6
+    assert np.abs(grad - gr).max() <= 2e-5 * np.abs(gr).max()
+    f.close()
+    g.close()
+
+
+def test_hessian_vector_matches_fp64_gradient_difference(ctx, oracle_mod):
+    """H dx against (g(n + e dx) - g(n - e dx)) / 2e of the FP64 gradient."""
+    from deft_gb300 import _lib
+    from tests.capi import Fmt, Grid
+    O = oracle_mod
+    s = _slit()
+    size = s.size
+    mask = s.mask.reshape(-1)
+    rng = np.random.default_rng(8)
+    n = np.where(mask > 0, s.nb * (1 + 0.1 * rng.standard_normal(size)), 0.0)
+    dx = rng.standard_normal(size) * s.nb * mask
+    g = Grid(ctx, s.lat, s.shape)
+    f64 = Fmt(g, mu=s.mu, terms=O.HS | O.IDEAL | O.MU | O.MASK, mask=mask)
+    fmx = Fmt(g, mu=s.mu, terms=O.HS | O.IDEAL | O.MU | O.MASK, mask=mask,
+              precision=_lib.PRECISION_MIXED)
+    Hd = fmx.hessian_vector(n, dx)
+    eps = 1e-4
+    _, gp, _ = f64.energy_grad(n + eps * dx)
+    _, gm, _ = f64.energy_grad(n - eps * dx)
+    fd = (gp - gm) / (2 * eps)
+    assert np.abs(Hd - fd).max() <= 1e-4 * np.abs(fd).max()
+    assert np.all(Hd[mask == 0] == 0)
+    f64.close()
+    fmx.close()
+    g.close()
+
+
+def test_mixed_solve_reaches_fp64_tolerance_and_profile(ctx, oracle_mod):
+    from deft_gb300 import _lib
+    from tests.capi import CG, Fmt, Grid
+    O = oracle_mod
+    s = _slit()
+    mask = s.mask.reshape(-1)
+    g = Grid(ctx, s.lat, s.shape)
+    f = Fmt(g, mu=s.mu, terms=O.HS | O.IDEAL | O.MU | O.MASK, mask=mask,
+            precision=_lib.PRECISION_MIXED)
+    cg = CG(f, gtol=1e-9, maxiter=2000, step=1.0)
+    cg.set_x(s.n0.reshape(-1))
+    code, st = cg.solve()
+    assert code == 0 and st.converged and st.stage == 1
+    n = cg.get_x()
+    # the convergence test is the FP64 gradient: check it independently
+    f64 = Fmt(g, mu=s.mu, terms=O.HS | O.IDEAL | O.MU | O.MASK, mask=mask)
+    _, g64, _ = f64.energy_grad(n)
+    assert np.linalg.norm(g64) < 1e-9
+    P1 = O.Problem(np.diag([s.dx, s.dx, s.L]), (1, 1, s.shape[2]), mu=s.mu,
+                   terms=O.HS | O.IDEAL | O.MU, mask=s.mask[0, 0].copy())
+    x1, info = P1.cg_solve(np.where(s.mask[0, 0] > 0, s.nb, 0.0), gtol=1e-13, maxiter=20000)
+    assert np.abs(n.reshape(s.shape) - x1[None, None, :]).max() < 1e-8
+    assert st.evals_fp64 < st.evals  # most evaluations ran in FP32
+    cg.close()
+    f.close()
+    f64.close()
+    g.close()
