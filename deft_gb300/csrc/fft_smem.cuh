@@ -16,6 +16,8 @@
 
 #include <cuda_runtime.h>
 
+#include "fastdiv.cuh"
+
 namespace deft {
 
 template <typename T> struct Cplx;
@@ -29,8 +31,18 @@ struct FftPlan {
   int n;
   int npass;
   int radix[kMaxPasses];
-  const void *tw;  // device table, n entries of Cplx<T>
+  FastDiv ns[kMaxPasses];  // product of the radices of the earlier passes
+  const void *tw;          // device table, n entries of Cplx<T>
 };
+
+// Fills ns[] once radix[] and npass are set.
+inline void plan_fill_ns(FftPlan &p) {
+  unsigned int Ns = 1;
+  for (int i = 0; i < p.npass; i++) {
+    p.ns[i] = make_fastdiv(Ns);
+    Ns *= (unsigned)p.radix[i];
+  }
+}
 
 template <typename C> __device__ __forceinline__ C c_add(C a, C b) { return C{a.x + b.x, a.y + b.y}; }
 template <typename C> __device__ __forceinline__ C c_sub(C a, C b) { return C{a.x - b.x, a.y - b.y}; }
@@ -113,16 +125,18 @@ template <int SIGN, typename C> __device__ __forceinline__ C tw_load(const C *tw
 // One radix-R pass over a tile: src -> dst.
 template <typename T, int SIGN, int R>
 __device__ __forceinline__ void fft_pass(const typename Cplx<T>::type *__restrict__ src,
-                                         typename Cplx<T>::type *__restrict__ dst, int B, int L,
-                                         int Ns, const typename Cplx<T>::type *__restrict__ tw) {
+                                         typename Cplx<T>::type *__restrict__ dst,
+                                         const FastDiv &bd, int L, const FastDiv &nsd,
+                                         const typename Cplx<T>::type *__restrict__ tw) {
   using C = typename Cplx<T>::type;
+  const int B = (int)bd.d, Ns = (int)nsd.d;
   const int m = L / R;
   const int twstep = L / (Ns * R);
   const int total = m * B;
   for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
-    const int bl = idx % B;
-    const int j = idx / B;
-    const int k = j % Ns;
+    int j, bl, q, k;
+    fdivmod(idx, bd, j, bl);
+    fdivmod(j, nsd, q, k);
     C v[R];
 #pragma unroll
     for (int s = 0; s < R; ++s) v[s] = src[(j + s * m) * B + bl];
@@ -135,7 +149,7 @@ __device__ __forceinline__ void fft_pass(const typename Cplx<T>::type *__restric
     else if constexpr (R == 8) dft8<SIGN, T>(v);
     else if constexpr (R == 3) dft3<SIGN, T>(v);
     else if constexpr (R == 5) dft5<SIGN, T>(v);
-    const int base = (j - k) * R + k;
+    const int base = q * Ns * R + k;
 #pragma unroll
     for (int s = 0; s < R; ++s) dst[(base + s * Ns) * B + bl] = v[s];
   }
@@ -144,27 +158,34 @@ __device__ __forceinline__ void fft_pass(const typename Cplx<T>::type *__restric
 // Direct-DFT pass for any prime radix r <= kMaxRadix.
 template <typename T, int SIGN>
 __device__ void fft_pass_generic(const typename Cplx<T>::type *__restrict__ src,
-                                 typename Cplx<T>::type *__restrict__ dst, int B, int L, int Ns,
-                                 int r, const typename Cplx<T>::type *__restrict__ tw) {
+                                 typename Cplx<T>::type *__restrict__ dst, const FastDiv &bd,
+                                 int L, const FastDiv &nsd, int r,
+                                 const typename Cplx<T>::type *__restrict__ tw) {
   using C = typename Cplx<T>::type;
+  const int B = (int)bd.d, Ns = (int)nsd.d;
   const int m = L / r;
   const int twstep = L / (Ns * r);
   const int total = m * B;
   for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
-    const int bl = idx % B;
-    const int j = idx / B;
-    const int k = j % Ns;
+    int j, bl, q, k;
+    fdivmod(idx, bd, j, bl);
+    fdivmod(j, nsd, q, k);
     C v[kMaxRadix];
     for (int s = 0; s < r; ++s) {
       C a = src[(j + s * m) * B + bl];
       if (k && s) a = c_mul(a, tw_load<SIGN>(tw, s * k * twstep));
       v[s] = a;
     }
-    const int base = (j - k) * r + k;
-    for (int q = 0; q < r; ++q) {
+    const int base = q * Ns * r + k;
+    for (int o = 0; o < r; ++o) {
       C acc = v[0];
-      for (int s = 1; s < r; ++s) acc = c_add(acc, c_mul(v[s], tw_load<SIGN>(tw, ((s * q) % r) * m)));
-      dst[(base + q * Ns) * B + bl] = acc;
+      int t = 0;  // (s * o) mod r, stepped without a divide
+      for (int s = 1; s < r; ++s) {
+        t += o;
+        if (t >= r) t -= r;
+        acc = c_add(acc, c_mul(v[s], tw_load<SIGN>(tw, t * m)));
+      }
+      dst[(base + o * Ns) * B + bl] = acc;
     }
   }
 }
@@ -173,24 +194,23 @@ __device__ void fft_pass_generic(const typename Cplx<T>::type *__restrict__ src,
 // Returns the buffer that holds the result.  Ends with __syncthreads().
 template <typename T, int SIGN>
 __device__ typename Cplx<T>::type *fft_tile(typename Cplx<T>::type *a, typename Cplx<T>::type *b,
-                                            int B, const FftPlan &p) {
+                                            const FastDiv &bd, const FftPlan &p) {
   using C = typename Cplx<T>::type;
   const C *tw = reinterpret_cast<const C *>(p.tw);
-  int Ns = 1;
   C *src = a, *dst = b;
   __syncthreads();
   for (int ps = 0; ps < p.npass; ++ps) {
     const int r = p.radix[ps];
+    const FastDiv &nsd = p.ns[ps];
     switch (r) {
-      case 2: fft_pass<T, SIGN, 2>(src, dst, B, p.n, Ns, tw); break;
-      case 3: fft_pass<T, SIGN, 3>(src, dst, B, p.n, Ns, tw); break;
-      case 4: fft_pass<T, SIGN, 4>(src, dst, B, p.n, Ns, tw); break;
-      case 5: fft_pass<T, SIGN, 5>(src, dst, B, p.n, Ns, tw); break;
-      case 8: fft_pass<T, SIGN, 8>(src, dst, B, p.n, Ns, tw); break;
-      default: fft_pass_generic<T, SIGN>(src, dst, B, p.n, Ns, r, tw); break;
+      case 2: fft_pass<T, SIGN, 2>(src, dst, bd, p.n, nsd, tw); break;
+      case 3: fft_pass<T, SIGN, 3>(src, dst, bd, p.n, nsd, tw); break;
+      case 4: fft_pass<T, SIGN, 4>(src, dst, bd, p.n, nsd, tw); break;
+      case 5: fft_pass<T, SIGN, 5>(src, dst, bd, p.n, nsd, tw); break;
+      case 8: fft_pass<T, SIGN, 8>(src, dst, bd, p.n, nsd, tw); break;
+      default: fft_pass_generic<T, SIGN>(src, dst, bd, p.n, nsd, r, tw); break;
     }
     __syncthreads();
-    Ns *= r;
     C *t = src;
     src = dst;
     dst = t;

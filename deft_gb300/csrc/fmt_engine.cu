@@ -46,6 +46,15 @@ __device__ __forceinline__ int wrapm(int i, int N) { return i > N / 2 ? i - N : 
 __device__ __forceinline__ double kcomp(const Geom &g, int c, int x, int y, int z) {
   return g.Bm[3 * c] * wrapm(x, g.Nx) + g.Bm[3 * c + 1] * wrapm(y, g.Ny) + g.Bm[3 * c + 2] * z;
 }
+// k-vector component in the arithmetic type of the kernel
+template <typename T>
+__device__ __forceinline__ T kcomp_t(const Geom &g, int c, int x, int y, int z) {
+  if constexpr (sizeof(T) == 4)
+    return g.Bmf[3 * c] * (float)wrapm(x, g.Nx) + g.Bmf[3 * c + 1] * (float)wrapm(y, g.Ny) +
+           g.Bmf[3 * c + 2] * (float)z;
+  else
+    return kcomp(g, c, x, y, z);
+}
 
 // Analytic weights at |k| (src/ReciprocalOperators.h:94-142,162-235):
 // step w3, shell w2, and the radial factor wv of the vector shells, whose
@@ -102,10 +111,9 @@ __device__ void block_reduce(double (&v)[K], double *smem /* 32*K */) {
 template <typename W>
 __global__ void k_weight_table(Geom g, double R, W *w3, W *w2, W *wv) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < g.NC; i += gridDim.x * blockDim.x) {
-    const int z = i % g.NzH;
-    const int t = i / g.NzH;
-    const int y = t % g.Ny;
-    const int x = t / g.Ny;
+    int t, z, x, y;
+    fdivmod(i, g.fNzH, t, z);
+    fdivmod(t, g.fNy, x, y);
     const double kx = kcomp(g, 0, x, y, z), ky = kcomp(g, 1, x, y, z), kz = kcomp(g, 2, x, y, z);
     double a, b, c;
     weights_at(kx * kx + ky * ky + kz * kz, R, g.dr, a, b, c);
@@ -122,10 +130,12 @@ template <typename T>
 __device__ __forceinline__ void pack_c2r(const typename Cplx<T>::type *__restrict__ in,
                                          typename Cplx<T>::type *buf, const Geom &g, int p0,
                                          int P) {
+  // element k of pair pb: idx = pb * Nz + k
   using C = typename Cplx<T>::type;
   const int Nz = g.Nz, NzH = g.NzH;
   for (int idx = threadIdx.x; idx < P * Nz; idx += blockDim.x) {
-    const int k = idx % Nz, pb = idx / Nz;
+    int pb, k;
+    fdivmod(idx, g.fNz, pb, k);
     const int l0 = 2 * (p0 + pb), l1 = l0 + 1;
     C A = C{0, 0}, B = C{0, 0};
     if (k < NzH) {
@@ -155,12 +165,13 @@ __device__ __forceinline__ void unpack_r2c_store(const typename Cplx<T>::type *r
   using C = typename Cplx<T>::type;
   const int Nz = g.Nz, NzH = g.NzH;
   for (int idx = threadIdx.x; idx < 2 * P * NzH; idx += blockDim.x) {
-    const int k = idx % NzH, ll = idx / NzH;
+    int ll, k;
+    fdivmod(idx, g.fNzH, ll, k);
     const int line = 2 * p0 + ll;
     if (line >= g.lines) continue;
     const int pb = ll >> 1;
     const C zk = res[k * P + pb];
-    const C zm = res[((Nz - k) % Nz) * P + pb];
+    const C zm = res[(k == 0 ? 0 : Nz - k) * P + pb];
     const T h = T(0.5) * s;
     C o;
     if ((ll & 1) == 0) o = C{h * (zk.x + zm.x), h * (zk.y - zm.y)};
@@ -173,7 +184,8 @@ __device__ __forceinline__ void unpack_r2c_store(const typename Cplx<T>::type *r
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_z_r2c(const double *__restrict__ in,
                                                     typename Cplx<T>::type *__restrict__ out,
-                                                    Geom g, FftPlan pz, int P, T s) {
+                                                    Geom g, FftPlan pz, FastDiv fP, T s) {
+  const int P = (int)fP.d;
   using C = typename Cplx<T>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C *buf0 = reinterpret_cast<C *>(smem_raw);
@@ -182,12 +194,13 @@ __global__ void __launch_bounds__(kThreads) k_z_r2c(const double *__restrict__ i
   in += (size_t)blockIdx.y * g.NR;
   out += (size_t)blockIdx.y * g.NC;
   for (int idx = threadIdx.x; idx < 2 * P * g.Nz; idx += blockDim.x) {
-    const int z = idx % g.Nz, ll = idx / g.Nz;
+    int ll, z;
+    fdivmod(idx, g.fNz, ll, z);
     const int line = 2 * p0 + ll;
     const T v = line < g.lines ? T(in[(size_t)line * g.Nz + z]) : T(0);
     reinterpret_cast<T *>(&buf0[z * P + (ll >> 1)])[ll & 1] = v;
   }
-  C *res = fft_tile<T, -1>(buf0, buf1, P, pz);
+  C *res = fft_tile<T, -1>(buf0, buf1, fP, pz);
   unpack_r2c_store<T>(res, out, g, p0, P, s);
 }
 
@@ -195,7 +208,8 @@ __global__ void __launch_bounds__(kThreads) k_z_r2c(const double *__restrict__ i
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_z_c2r(const typename Cplx<T>::type *__restrict__ in,
                                                     double *__restrict__ out, Geom g, FftPlan pz,
-                                                    int P, double s) {
+                                                    FastDiv fP, double s) {
+  const int P = (int)fP.d;
   using C = typename Cplx<T>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C *buf0 = reinterpret_cast<C *>(smem_raw);
@@ -204,9 +218,10 @@ __global__ void __launch_bounds__(kThreads) k_z_c2r(const typename Cplx<T>::type
   in += (size_t)blockIdx.y * g.NC;
   out += (size_t)blockIdx.y * g.NR;
   pack_c2r<T>(in, buf0, g, p0, P);
-  C *res = fft_tile<T, +1>(buf0, buf1, P, pz);
+  C *res = fft_tile<T, +1>(buf0, buf1, fP, pz);
   for (int idx = threadIdx.x; idx < 2 * P * g.Nz; idx += blockDim.x) {
-    const int z = idx % g.Nz, ll = idx / g.Nz;
+    int ll, z;
+    fdivmod(idx, g.fNz, ll, z);
     const int line = 2 * p0 + ll;
     if (line >= g.lines) continue;
     const C v = res[z * P + (ll >> 1)];
@@ -217,7 +232,8 @@ __global__ void __launch_bounds__(kThreads) k_z_c2r(const typename Cplx<T>::type
 // FFT along y of complex fields.  grid = (kz tiles, Nx, fields).
 template <typename T, int SIGN>
 __global__ void __launch_bounds__(kThreads) k_y_fft(typename Cplx<T>::type *data, Geom g,
-                                                    FftPlan py, int B) {
+                                                    FftPlan py, FastDiv fB) {
+  const int B = (int)fB.d;
   using C = typename Cplx<T>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C *buf0 = reinterpret_cast<C *>(smem_raw);
@@ -225,13 +241,15 @@ __global__ void __launch_bounds__(kThreads) k_y_fft(typename Cplx<T>::type *data
   const int kz0 = blockIdx.x * B;
   C *base = data + (size_t)blockIdx.z * g.NC + (size_t)blockIdx.y * g.Ny * g.NzH;
   for (int idx = threadIdx.x; idx < g.Ny * B; idx += blockDim.x) {
-    const int e = idx / B, b = idx % B;
+    int e, b;
+    fdivmod(idx, fB, e, b);
     const int kz = kz0 + b;
     buf0[idx] = kz < g.NzH ? base[(size_t)e * g.NzH + kz] : C{0, 0};
   }
-  C *res = fft_tile<T, SIGN>(buf0, buf1, B, py);
+  C *res = fft_tile<T, SIGN>(buf0, buf1, fB, py);
   for (int idx = threadIdx.x; idx < g.Ny * B; idx += blockDim.x) {
-    const int e = idx / B, b = idx % B;
+    int e, b;
+    fdivmod(idx, fB, e, b);
     const int kz = kz0 + b;
     if (kz < g.NzH) base[(size_t)e * g.NzH + kz] = res[idx];
   }
@@ -240,7 +258,8 @@ __global__ void __launch_bounds__(kThreads) k_y_fft(typename Cplx<T>::type *data
 // Plain FFT along x (stride Ny*NzH), optional scale.  grid.x = line tiles.
 template <typename T, int SIGN>
 __global__ void __launch_bounds__(kThreads) k_x_fft(typename Cplx<T>::type *data, Geom g,
-                                                    FftPlan px, int B, T s) {
+                                                    FftPlan px, FastDiv fB, T s) {
+  const int B = (int)fB.d;
   using C = typename Cplx<T>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C *buf0 = reinterpret_cast<C *>(smem_raw);
@@ -248,115 +267,130 @@ __global__ void __launch_bounds__(kThreads) k_x_fft(typename Cplx<T>::type *data
   const int J = g.Ny * g.NzH;
   const int j0 = blockIdx.x * B;
   for (int idx = threadIdx.x; idx < g.Nx * B; idx += blockDim.x) {
-    const int e = idx / B, j = j0 + idx % B;
+    int e, j;
+    fdivmod(idx, fB, e, j);
+    j += j0;
     buf0[idx] = j < J ? data[(size_t)e * J + j] : C{0, 0};
   }
-  C *res = fft_tile<T, SIGN>(buf0, buf1, B, px);
+  C *res = fft_tile<T, SIGN>(buf0, buf1, fB, px);
   for (int idx = threadIdx.x; idx < g.Nx * B; idx += blockDim.x) {
-    const int e = idx / B, j = j0 + idx % B;
+    int e, j;
+    fdivmod(idx, fB, e, j);
+    j += j0;
     if (j < J) data[(size_t)e * J + j] = c_scale(res[idx], s);
   }
 }
 
-// x-FFT of n^, multiplication by the five weights, inverse x-FFT of each.
+// x-FFT of n^, multiplication by the five weights, inverse x-FFT of all
+// five at once: one tile of 5B lines (line a*B + b = field a, column b).
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_x_conv_fwd(
     const typename Cplx<T>::type *__restrict__ in, typename Cplx<T>::type *__restrict__ out5,
-    const T *__restrict__ w3, const T *__restrict__ w2, const T *__restrict__ wv,
-    Geom g, FftPlan px, int B) {
+    const T *__restrict__ w3, const T *__restrict__ w2, const T *__restrict__ wv, Geom g,
+    FftPlan px, FastDiv fB, FastDiv f5B) {
+  const int B = (int)fB.d;
   using C = typename Cplx<T>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  C *bufA = reinterpret_cast<C *>(smem_raw);
-  C *bufB = bufA + g.Nx * B;
-  C *bufC = bufB + g.Nx * B;
+  C *X = reinterpret_cast<C *>(smem_raw);
+  C *Y = X + g.Nx * 5 * B;
   const int J = g.Ny * g.NzH;
   const int j0 = blockIdx.x * B;
   for (int idx = threadIdx.x; idx < g.Nx * B; idx += blockDim.x) {
-    const int e = idx / B, j = j0 + idx % B;
-    bufA[idx] = j < J ? in[(size_t)e * J + j] : C{0, 0};
+    int e, j;
+    fdivmod(idx, fB, e, j);
+    j += j0;
+    X[idx] = j < J ? in[(size_t)e * J + j] : C{0, 0};
   }
-  const C *R0 = fft_tile<T, -1>(bufA, bufB, B, px);
-  C *F1 = (R0 == bufA) ? bufB : bufA;
-  C *F2 = bufC;
-  for (int a = 0; a < 5; a++) {
-    for (int idx = threadIdx.x; idx < g.Nx * B; idx += blockDim.x) {
-      const int e = idx / B, j = j0 + idx % B;
-      C o = C{0, 0};
-      if (j < J) {
-        const size_t i = (size_t)e * J + j;
-        const C v = R0[idx];
-        if (a == 0) {
-          const T w = w3[i];
-          o = C{v.x * w, v.y * w};
-        } else if (a == 1) {
-          const T w = w2[i];
-          o = C{v.x * w, v.y * w};
-        } else {
-          const int y = j / g.NzH, z = j % g.NzH;
-          const T w = T(kcomp(g, a - 2, e, y, z)) * wv[i];
-          o = C{-v.y * w, v.x * w};  // times i w
-        }
+  C *R0 = fft_tile<T, -1>(X, Y, fB, px);  // layout e*B + b
+  C *W = (R0 == X) ? Y : X;               // layout e*5B + a*B + b
+  const int B5 = 5 * B;
+  for (int idx = threadIdx.x; idx < g.Nx * B5; idx += blockDim.x) {
+    int e, bb, a, b;
+    fdivmod(idx, f5B, e, bb);
+    fdivmod(bb, fB, a, b);
+    const int j = j0 + b;
+    C o = C{0, 0};
+    if (j < J) {
+      const size_t i = (size_t)e * J + j;
+      const C v = R0[e * B + b];
+      if (a == 0) {
+        const T w = w3[i];
+        o = C{v.x * w, v.y * w};
+      } else if (a == 1) {
+        const T w = w2[i];
+        o = C{v.x * w, v.y * w};
+      } else {
+        int y, z;
+        fdivmod(j, g.fNzH, y, z);
+        const T w = kcomp_t<T>(g, a - 2, e, y, z) * wv[i];
+        o = C{-v.y * w, v.x * w};  // times i w
       }
-      F1[idx] = o;
     }
-    const C *res = fft_tile<T, +1>(F1, F2, B, px);
-    C *dst = out5 + (size_t)a * g.NC;
-    for (int idx = threadIdx.x; idx < g.Nx * B; idx += blockDim.x) {
-      const int e = idx / B, j = j0 + idx % B;
-      if (j < J) dst[(size_t)e * J + j] = res[idx];
-    }
-    __syncthreads();
+    W[idx] = o;
+  }
+  const C *res = fft_tile<T, +1>(W, R0, f5B, px);
+  for (int idx = threadIdx.x; idx < g.Nx * B5; idx += blockDim.x) {
+    int e, bb, a, b;
+    fdivmod(idx, f5B, e, bb);
+    fdivmod(bb, fB, a, b);
+    const int j = j0 + b;
+    if (j < J) out5[(size_t)a * g.NC + (size_t)e * J + j] = res[idx];
   }
 }
 
-// x-FFT of the five partial spectra, times adjoint weights, summed, inverse x.
+// x-FFT of the five partial spectra at once, times the adjoint weights
+// (odd ones negated), summed over the fields, inverse x-FFT of the sum.
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_x_conv_adj(
     const typename Cplx<T>::type *__restrict__ in5, typename Cplx<T>::type *__restrict__ out,
-    const T *__restrict__ w3, const T *__restrict__ w2, const T *__restrict__ wv,
-    Geom g, FftPlan px, int B) {
+    const T *__restrict__ w3, const T *__restrict__ w2, const T *__restrict__ wv, Geom g,
+    FftPlan px, FastDiv fB, FastDiv f5B) {
+  const int B = (int)fB.d;
   using C = typename Cplx<T>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  C *acc = reinterpret_cast<C *>(smem_raw);
-  C *F1 = acc + g.Nx * B;
-  C *F2 = F1 + g.Nx * B;
+  C *X = reinterpret_cast<C *>(smem_raw);
+  C *Y = X + g.Nx * 5 * B;
   const int J = g.Ny * g.NzH;
   const int j0 = blockIdx.x * B;
-  for (int idx = threadIdx.x; idx < g.Nx * B; idx += blockDim.x) acc[idx] = C{0, 0};
-  for (int a = 0; a < 5; a++) {
-    const C *src = in5 + (size_t)a * g.NC;
-    for (int idx = threadIdx.x; idx < g.Nx * B; idx += blockDim.x) {
-      const int e = idx / B, j = j0 + idx % B;
-      F1[idx] = j < J ? src[(size_t)e * J + j] : C{0, 0};
-    }
-    const C *res = fft_tile<T, -1>(F1, F2, B, px);
-    for (int idx = threadIdx.x; idx < g.Nx * B; idx += blockDim.x) {
-      const int e = idx / B, j = j0 + idx % B;
-      if (j >= J) continue;
-      const size_t i = (size_t)e * J + j;
-      const C v = res[idx];
-      C o = acc[idx];
-      if (a == 0) {
-        const T w = w3[i];
-        o.x += v.x * w;
-        o.y += v.y * w;
-      } else if (a == 1) {
-        const T w = w2[i];
-        o.x += v.x * w;
-        o.y += v.y * w;
-      } else {
-        const int y = j / g.NzH, z = j % g.NzH;
-        const T w = T(kcomp(g, a - 2, e, y, z)) * wv[i];
-        o.x += v.y * w;  // times -i w
-        o.y -= v.x * w;
-      }
-      acc[idx] = o;
-    }
-    __syncthreads();
+  const int B5 = 5 * B;
+  for (int idx = threadIdx.x; idx < g.Nx * B5; idx += blockDim.x) {
+    int e, bb, a, b;
+    fdivmod(idx, f5B, e, bb);
+    fdivmod(bb, fB, a, b);
+    const int j = j0 + b;
+    X[idx] = j < J ? in5[(size_t)a * g.NC + (size_t)e * J + j] : C{0, 0};
   }
-  const C *res = fft_tile<T, +1>(acc, F1, B, px);
+  const C *R = fft_tile<T, -1>(X, Y, f5B, px);
+  C *A = (R == X) ? Y : X;  // layout e*B + b
   for (int idx = threadIdx.x; idx < g.Nx * B; idx += blockDim.x) {
-    const int e = idx / B, j = j0 + idx % B;
+    int e, b;
+    fdivmod(idx, fB, e, b);
+    const int j = j0 + b;
+    C o = C{0, 0};
+    if (j < J) {
+      const size_t i = (size_t)e * J + j;
+      const C *r = R + e * B5 + b;
+      const T a3 = w3[i], a2 = w2[i];
+      o.x = r[0].x * a3 + r[B].x * a2;
+      o.y = r[0].y * a3 + r[B].y * a2;
+      int y, z;
+      fdivmod(j, g.fNzH, y, z);
+      const T v = wv[i];
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        const T w = kcomp_t<T>(g, c, e, y, z) * v;
+        const C q = r[(2 + c) * B];
+        o.x += q.y * w;  // times -i w
+        o.y -= q.x * w;
+      }
+    }
+    A[idx] = o;
+  }
+  const C *res = fft_tile<T, +1>(A, const_cast<C *>(R), fB, px);
+  for (int idx = threadIdx.x; idx < g.Nx * B; idx += blockDim.x) {
+    int e, j;
+    fdivmod(idx, fB, e, j);
+    j += j0;
     if (j < J) out[(size_t)e * J + j] = res[idx];
   }
 }
@@ -379,6 +413,77 @@ template <typename T>
 __device__ __forceinline__ double ideal_grad(double nv, const LocalArgs &la) {
   return double(T(la.kT) * wb_log<T>(T(nv) * T(la.inv_nQ)));
 }
+// The same integrand per kT in T, with no FP64 arithmetic for T = float.
+template <typename T>
+__device__ __forceinline__ T ideal_energy_t(T x, T inv_nQ) {
+  return x == T(0) ? T(0) : x * (wb_log<T>(x * inv_nQ) - T(1));
+}
+
+// Loads the five half-complex fields of the tile's P line pairs as one tile
+// of 5P complex lines (line a*P + pb = field a, pair pb; element k at
+// k*5P + line) and transforms them back along z.  Returns the buffer with
+// the result: entry (z, a*P + pb) holds field a at lines 2(p0+pb) (.x) and
+// 2(p0+pb)+1 (.y).  P odd keeps the z-strided accesses conflict-free.
+template <typename T>
+__device__ typename Cplx<T>::type *z_load5_c2r(const typename Cplx<T>::type *__restrict__ S5,
+                                               typename Cplx<T>::type *A,
+                                               typename Cplx<T>::type *Bf, const Geom &g,
+                                               const FftPlan &pz, const FastDiv &fP,
+                                               const FastDiv &f5P, int p0) {
+  using C = typename Cplx<T>::type;
+  const int P = (int)fP.d, P5 = 5 * P, Nz = g.Nz, NzH = g.NzH;
+  for (int idx = threadIdx.x; idx < P5 * Nz; idx += blockDim.x) {
+    int b, k, a, pb;
+    fdivmod(idx, g.fNz, b, k);
+    fdivmod(b, fP, a, pb);
+    const C *in = S5 + (size_t)a * g.NC;
+    const int l0 = 2 * (p0 + pb), l1 = l0 + 1;
+    C Av = C{0, 0}, Bv = C{0, 0};
+    if (k < NzH) {
+      if (l0 < g.lines) Av = in[(size_t)l0 * NzH + k];
+      if (l1 < g.lines) Bv = in[(size_t)l1 * NzH + k];
+      if (k == 0 || 2 * k == Nz) {
+        Av.y = 0;
+        Bv.y = 0;
+      }
+    } else {
+      const int kk = Nz - k;
+      if (l0 < g.lines) Av = in[(size_t)l0 * NzH + kk];
+      if (l1 < g.lines) Bv = in[(size_t)l1 * NzH + kk];
+      Av.y = -Av.y;
+      Bv.y = -Bv.y;
+    }
+    A[k * P5 + b] = C{Av.x - Bv.y, Av.y + Bv.x};
+  }
+  return fft_tile<T, +1>(A, Bf, f5P, pz);
+}
+
+// Forward z transform of the five real pairs held in `res` (same layout)
+// and the Hermitian split into the five half spectra of S5.
+template <typename T>
+__device__ void z_r2c_store5(typename Cplx<T>::type *res, typename Cplx<T>::type *other,
+                             typename Cplx<T>::type *__restrict__ S5, const Geom &g,
+                             const FftPlan &pz, const FastDiv &fP, const FastDiv &f2P,
+                             const FastDiv &f5P, int p0) {
+  using C = typename Cplx<T>::type;
+  const int P = (int)fP.d, P5 = 5 * P, Nz = g.Nz, NzH = g.NzH;
+  const C *out = fft_tile<T, -1>(res, other, f5P, pz);
+  for (int idx = threadIdx.x; idx < 10 * P * NzH; idx += blockDim.x) {
+    int lb, k, a, ll;
+    fdivmod(idx, g.fNzH, lb, k);
+    fdivmod(lb, f2P, a, ll);
+    const int line = 2 * p0 + ll;
+    if (line >= g.lines) continue;
+    const int b = a * P + (ll >> 1);
+    const C zk = out[k * P5 + b];
+    const C zm = out[(k == 0 ? 0 : Nz - k) * P5 + b];
+    const T h = T(0.5);
+    C o;
+    if ((ll & 1) == 0) o = C{h * (zk.x + zm.x), h * (zk.y - zm.y)};
+    else o = C{h * (zk.y + zm.y), -h * (zk.x - zm.x)};
+    S5[(size_t)a * g.NC + (size_t)line * NzH + k] = o;
+  }
+}
 
 // c2r of the five weighted densities, phi and local terms, per-block
 // energies, and (GRAD) r2c of the five partials dV kT dphi/dn_a in place.
@@ -386,70 +491,58 @@ template <typename T, bool GRAD>
 __global__ void __launch_bounds__(kThreads) k_z_phi(typename Cplx<T>::type *S5,
                                                     const double *__restrict__ n,
                                                     const double *__restrict__ V, Geom g,
-                                                    FftPlan pz, int P, LocalArgs la,
+                                                    FftPlan pz, FastDiv fP, FastDiv f2P,
+                                                    FastDiv f5P, LocalArgs la,
                                                     double *partials) {
+  const int P = (int)fP.d;
   using C = typename Cplx<T>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  C *buf0 = reinterpret_cast<C *>(smem_raw);
-  C *buf1 = buf0 + g.Nz * P;
-  T *rv = reinterpret_cast<T *>(buf1 + g.Nz * P);  // [5][2P][Nz]
+  C *A = reinterpret_cast<C *>(smem_raw);
+  C *Bf = A + g.Nz * 5 * P;
   __shared__ double red[32 * kNumTerms];
-  const int Nz = g.Nz;
-  const int LP = 2 * P * Nz;
+  const int Nz = g.Nz, P5 = 5 * P;
   const int p0 = blockIdx.x * P;
-  for (int a = 0; a < 5; a++) {
-    pack_c2r<T>(S5 + (size_t)a * g.NC, buf0, g, p0, P);
-    const C *res = fft_tile<T, +1>(buf0, buf1, P, pz);
-    T *dst = rv + a * LP;
-    for (int idx = threadIdx.x; idx < LP; idx += blockDim.x) {
-      const int z = idx % Nz, ll = idx / Nz;
-      const C v = res[z * P + (ll >> 1)];
-      dst[idx] = (ll & 1) ? v.y : v.x;
-    }
-    __syncthreads();
-  }
-  double acc[kNumTerms] = {0, 0, 0, 0, 0, 0};
+  C *res = z_load5_c2r<T>(S5, A, Bf, g, pz, fP, f5P, p0);
+  T tacc[kNumTerms] = {0, 0, 0, 0, 0, 0};
   const bool hs = la.terms & kTermHS;
-  for (int idx = threadIdx.x; idx < LP; idx += blockDim.x) {
-    const int z = idx % Nz, ll = idx / Nz;
+  const T inv_nQ = T(la.inv_nQ);
+  const T c = T(la.dV * la.kT);
+  for (int idx = threadIdx.x; idx < 2 * P * Nz; idx += blockDim.x) {
+    int ll, z;
+    fdivmod(idx, g.fNz, ll, z);
     const int line = 2 * p0 + ll;
+    T *cell = reinterpret_cast<T *>(res + z * P5 + (ll >> 1)) + (ll & 1);  // field 0
+    const int fstride = 2 * P;  // T elements between fields
     T d[5] = {0, 0, 0, 0, 0};
     if (line < g.lines) {
       const size_t r = (size_t)line * Nz + z;
       if (hs) {
         T phi[3];
-        wb_phi<T>(la.wr, rv[idx], rv[LP + idx], rv[2 * LP + idx], rv[3 * LP + idx],
-                  rv[4 * LP + idx], phi, d);
-        acc[0] += la.kT * double(phi[0]);
-        acc[1] += la.kT * double(phi[1]);
-        acc[2] += la.kT * double(phi[2]);
+        wb_phi<T>(la.wr, cell[0], cell[fstride], cell[2 * fstride], cell[3 * fstride],
+                  cell[4 * fstride], phi, d);
+        tacc[0] += phi[0];
+        tacc[1] += phi[1];
+        tacc[2] += phi[2];
       }
-      const double nv = n[r];
-      if (la.terms & kTermIdeal) acc[3] += ideal_energy<T>(nv, la);
-      if (la.terms & kTermMu) acc[4] += la.mu * nv;
-      if (la.terms & kTermVext) acc[5] += V[r] * nv;
+      const T nv = T(n[r]);
+      if (la.terms & kTermIdeal) tacc[3] += ideal_energy_t<T>(nv, inv_nQ);
+      if (la.terms & kTermMu) tacc[4] += nv;
+      if (la.terms & kTermVext) tacc[5] += T(V[r]) * nv;
     }
     if (GRAD) {
-      const T c = T(la.dV * la.kT);
 #pragma unroll
-      for (int a = 0; a < 5; a++) rv[a * LP + idx] = c * d[a];
+      for (int a = 0; a < 5; a++) cell[a * fstride] = c * d[a];
     }
   }
+  double acc[kNumTerms] = {la.kT * double(tacc[0]), la.kT * double(tacc[1]),
+                           la.kT * double(tacc[2]), la.kT * double(tacc[3]),
+                           la.mu * double(tacc[4]), double(tacc[5])};
   block_reduce<kNumTerms>(acc, red);
   if (threadIdx.x == 0)
     for (int t = 0; t < kNumTerms; t++) partials[(size_t)blockIdx.x * kNumTerms + t] = acc[t];
   if (!GRAD) return;
   __syncthreads();
-  for (int a = 0; a < 5; a++) {
-    const T *src = rv + a * LP;
-    for (int idx = threadIdx.x; idx < P * Nz; idx += blockDim.x) {
-      const int pb = idx % P, z = idx / P;
-      buf0[idx] = C{src[(2 * pb) * Nz + z], src[(2 * pb + 1) * Nz + z]};
-    }
-    const C *res = fft_tile<T, -1>(buf0, buf1, P, pz);
-    unpack_r2c_store<T>(res, S5 + (size_t)a * g.NC, g, p0, P, T(1));
-    __syncthreads();
-  }
+  z_r2c_store5<T>(res, res == A ? Bf : A, S5, g, pz, fP, f2P, f5P, p0);
 }
 
 // c2r of the adjoint sum, + local gradient terms, masked.
@@ -459,7 +552,8 @@ __global__ void __launch_bounds__(kThreads) k_z_grad(const typename Cplx<T>::typ
                                                      const double *__restrict__ V,
                                                      const double *__restrict__ mask,
                                                      double *__restrict__ grad, Geom g, FftPlan pz,
-                                                     int P, LocalArgs la) {
+                                                     FastDiv fP, LocalArgs la) {
+  const int P = (int)fP.d;
   using C = typename Cplx<T>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C *buf0 = reinterpret_cast<C *>(smem_raw);
@@ -469,29 +563,30 @@ __global__ void __launch_bounds__(kThreads) k_z_grad(const typename Cplx<T>::typ
   const C *res = nullptr;
   if (hs) {
     pack_c2r<T>(in, buf0, g, p0, P);
-    res = fft_tile<T, +1>(buf0, buf1, P, pz);
+    res = fft_tile<T, +1>(buf0, buf1, fP, pz);
   }
   for (int idx = threadIdx.x; idx < 2 * P * g.Nz; idx += blockDim.x) {
-    const int z = idx % g.Nz, ll = idx / g.Nz;
+    int ll, z;
+    fdivmod(idx, g.fNz, ll, z);
     const int line = 2 * p0 + ll;
     if (line >= g.lines) continue;
     const size_t r = (size_t)line * g.Nz + z;
-    double conv = 0;
+    T conv = 0;
     if (hs) {
       const C v = res[z * P + (ll >> 1)];
       conv = (ll & 1) ? v.y : v.x;
     }
-    double loc = 0;
-    const double nv = n[r];
-    if (la.terms & kTermIdeal) loc += ideal_grad<T>(nv, la);
-    if (la.terms & kTermMu) loc += la.mu;
-    if (la.terms & kTermVext) loc += V[r];
-    double gr = conv + la.dV * loc;
+    T loc = 0;
+    const T nv = T(n[r]);
+    if (la.terms & kTermIdeal) loc += T(la.kT) * wb_log<T>(nv * T(la.inv_nQ));
+    if (la.terms & kTermMu) loc += T(la.mu);
+    if (la.terms & kTermVext) loc += T(V[r]);
+    T gr = conv + T(la.dV) * loc;
     if (la.terms & kTermMask) {
-      const double m = mask[r];
-      gr = m == 0 ? 0.0 : m * gr;
+      const T m = T(mask[r]);
+      gr = m == T(0) ? T(0) : m * gr;
     }
-    grad[r] = gr;
+    grad[r] = double(gr);
   }
 }
 
@@ -502,38 +597,29 @@ __global__ void __launch_bounds__(kThreads) k_z_grad(const typename Cplx<T>::typ
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_z_hess(const typename Cplx<T>::type *__restrict__ S5,
                                                      const double *__restrict__ n, Geom g,
-                                                     FftPlan pz, int P, LocalArgs la,
-                                                     float *__restrict__ hess,
+                                                     FftPlan pz, FastDiv fP, FastDiv f5P,
+                                                     LocalArgs la, float *__restrict__ hess,
                                                      float *__restrict__ hloc) {
+  const int P = (int)fP.d;
   using C = typename Cplx<T>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  C *buf0 = reinterpret_cast<C *>(smem_raw);
-  C *buf1 = buf0 + g.Nz * P;
-  T *rv = reinterpret_cast<T *>(buf1 + g.Nz * P);  // [5][2P][Nz]
-  const int Nz = g.Nz;
-  const int LP = 2 * P * Nz;
+  C *A = reinterpret_cast<C *>(smem_raw);
+  C *Bf = A + g.Nz * 5 * P;
+  const int Nz = g.Nz, P5 = 5 * P;
   const int p0 = blockIdx.x * P;
-  for (int a = 0; a < 5; a++) {
-    pack_c2r<T>(S5 + (size_t)a * g.NC, buf0, g, p0, P);
-    const C *res = fft_tile<T, +1>(buf0, buf1, P, pz);
-    T *dst = rv + a * LP;
-    for (int idx = threadIdx.x; idx < LP; idx += blockDim.x) {
-      const int z = idx % Nz, ll = idx / Nz;
-      const C v = res[z * P + (ll >> 1)];
-      dst[idx] = (ll & 1) ? v.y : v.x;
-    }
-    __syncthreads();
-  }
+  C *res = z_load5_c2r<T>(S5, A, Bf, g, pz, fP, f5P, p0);
   const bool hs = la.terms & kTermHS;
-  for (int idx = threadIdx.x; idx < LP; idx += blockDim.x) {
-    const int z = idx % Nz, ll = idx / Nz;
+  for (int idx = threadIdx.x; idx < 2 * P * Nz; idx += blockDim.x) {
+    int ll, z;
+    fdivmod(idx, g.fNz, ll, z);
     const int line = 2 * p0 + ll;
     if (line >= g.lines) continue;
     const size_t r = (size_t)line * Nz + z;
+    const T *cell = reinterpret_cast<const T *>(res + z * P5 + (ll >> 1)) + (ll & 1);
+    const int fs = 2 * P;
     T h[kHessPacked];
     if (hs) {
-      wb_hess<T>(la.wr, rv[idx], rv[LP + idx], rv[2 * LP + idx], rv[3 * LP + idx],
-                 rv[4 * LP + idx], h);
+      wb_hess<T>(la.wr, cell[0], cell[fs], cell[2 * fs], cell[3 * fs], cell[4 * fs], h);
     } else {
 #pragma unroll
       for (int k = 0; k < kHessPacked; k++) h[k] = T(0);
@@ -549,39 +635,31 @@ __global__ void __launch_bounds__(kThreads) k_z_hess(const typename Cplx<T>::typ
 // perturbations dw, dP = dV kT J dw with the stored blocks, r2c of dP in place.
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_z_jac(typename Cplx<T>::type *S5, Geom g, FftPlan pz,
-                                                    int P, double c,
-                                                    const float *__restrict__ hess) {
+                                                    FastDiv fP, FastDiv f2P, FastDiv f5P,
+                                                    double c, const float *__restrict__ hess) {
+  const int P = (int)fP.d;
   using C = typename Cplx<T>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  C *buf0 = reinterpret_cast<C *>(smem_raw);
-  C *buf1 = buf0 + g.Nz * P;
-  T *rv = reinterpret_cast<T *>(buf1 + g.Nz * P);  // [5][2P][Nz]
-  const int Nz = g.Nz;
-  const int LP = 2 * P * Nz;
+  C *A = reinterpret_cast<C *>(smem_raw);
+  C *Bf = A + g.Nz * 5 * P;
+  const int Nz = g.Nz, P5 = 5 * P;
   const int p0 = blockIdx.x * P;
-  for (int a = 0; a < 5; a++) {
-    pack_c2r<T>(S5 + (size_t)a * g.NC, buf0, g, p0, P);
-    const C *res = fft_tile<T, +1>(buf0, buf1, P, pz);
-    T *dst = rv + a * LP;
-    for (int idx = threadIdx.x; idx < LP; idx += blockDim.x) {
-      const int z = idx % Nz, ll = idx / Nz;
-      const C v = res[z * P + (ll >> 1)];
-      dst[idx] = (ll & 1) ? v.y : v.x;
-    }
-    __syncthreads();
-  }
+  C *res = z_load5_c2r<T>(S5, A, Bf, g, pz, fP, f5P, p0);
   const T cc = T(c);
-  for (int idx = threadIdx.x; idx < LP; idx += blockDim.x) {
-    const int z = idx % Nz, ll = idx / Nz;
+  for (int idx = threadIdx.x; idx < 2 * P * Nz; idx += blockDim.x) {
+    int ll, z;
+    fdivmod(idx, g.fNz, ll, z);
     const int line = 2 * p0 + ll;
+    T *cell = reinterpret_cast<T *>(res + z * P5 + (ll >> 1)) + (ll & 1);
+    const int fs = 2 * P;
     T o[5] = {0, 0, 0, 0, 0};
     if (line < g.lines) {
       const size_t r = (size_t)line * Nz + z;
       T h[kHessPacked];
 #pragma unroll
       for (int k = 0; k < kHessPacked; k++) h[k] = T(hess[(size_t)k * g.NR + r]);
-      const T d3 = rv[idx], d2 = rv[LP + idx], dx = rv[2 * LP + idx], dy = rv[3 * LP + idx],
-              dz = rv[4 * LP + idx];
+      const T d3 = cell[0], d2 = cell[fs], dx = cell[2 * fs], dy = cell[3 * fs],
+              dz = cell[4 * fs];
       o[0] = h[0] * d3 + h[1] * d2 + h[2] * dx + h[3] * dy + h[4] * dz;
       o[1] = h[1] * d3 + h[5] * d2 + h[6] * dx + h[7] * dy + h[8] * dz;
       o[2] = h[2] * d3 + h[6] * d2 + h[9] * dx;
@@ -589,19 +667,10 @@ __global__ void __launch_bounds__(kThreads) k_z_jac(typename Cplx<T>::type *S5, 
       o[4] = h[4] * d3 + h[8] * d2 + h[9] * dz;
     }
 #pragma unroll
-    for (int a = 0; a < 5; a++) rv[a * LP + idx] = cc * o[a];
+    for (int a = 0; a < 5; a++) cell[a * fs] = cc * o[a];
   }
   __syncthreads();
-  for (int a = 0; a < 5; a++) {
-    const T *src = rv + a * LP;
-    for (int idx = threadIdx.x; idx < P * Nz; idx += blockDim.x) {
-      const int pb = idx % P, z = idx / P;
-      buf0[idx] = C{src[(2 * pb) * Nz + z], src[(2 * pb + 1) * Nz + z]};
-    }
-    const C *res = fft_tile<T, -1>(buf0, buf1, P, pz);
-    unpack_r2c_store<T>(res, S5 + (size_t)a * g.NC, g, p0, P, T(1));
-    __syncthreads();
-  }
+  z_r2c_store5<T>(res, res == A ? Bf : A, S5, g, pz, fP, f2P, f5P, p0);
 }
 
 // Hessian-vector product, last stage: c2r of the adjoint sum plus the
@@ -610,7 +679,8 @@ template <typename T>
 __global__ void __launch_bounds__(kThreads) k_z_hvp_out(
     const typename Cplx<T>::type *__restrict__ in, const double *__restrict__ dx,
     const float *__restrict__ hloc, const double *__restrict__ mask, double *__restrict__ out,
-    Geom g, FftPlan pz, int P, LocalArgs la) {
+    Geom g, FftPlan pz, FastDiv fP, LocalArgs la) {
+  const int P = (int)fP.d;
   using C = typename Cplx<T>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C *buf0 = reinterpret_cast<C *>(smem_raw);
@@ -620,24 +690,25 @@ __global__ void __launch_bounds__(kThreads) k_z_hvp_out(
   const C *res = nullptr;
   if (hs) {
     pack_c2r<T>(in, buf0, g, p0, P);
-    res = fft_tile<T, +1>(buf0, buf1, P, pz);
+    res = fft_tile<T, +1>(buf0, buf1, fP, pz);
   }
   for (int idx = threadIdx.x; idx < 2 * P * g.Nz; idx += blockDim.x) {
-    const int z = idx % g.Nz, ll = idx / g.Nz;
+    int ll, z;
+    fdivmod(idx, g.fNz, ll, z);
     const int line = 2 * p0 + ll;
     if (line >= g.lines) continue;
     const size_t r = (size_t)line * g.Nz + z;
-    double conv = 0;
+    T conv = 0;
     if (hs) {
       const C v = res[z * P + (ll >> 1)];
       conv = (ll & 1) ? v.y : v.x;
     }
-    double o = conv + la.dV * double(hloc[r]) * dx[r];
+    T o = conv + T(la.dV) * T(hloc[r]) * T(dx[r]);
     if (la.terms & kTermMask) {
-      const double m = mask[r];
-      o = m == 0 ? 0.0 : m * o;
+      const T m = T(mask[r]);
+      o = m == T(0) ? T(0) : m * o;
     }
-    out[r] = o;
+    out[r] = double(o);
   }
 }
 
@@ -762,6 +833,56 @@ int tile_width(int lines, int L, size_t bytes_per_elem, int nbuf, int cap) {
 
 }  // namespace
 
+// Tile widths and shared-memory sizes of every kernel for one precision
+// (cs = bytes of one complex element).
+struct Tiles {
+  int By = 1, Bx = 1, Bxc = 1, Pz = 1, Pphi = 1;
+  FastDiv fBy{}, fBx{}, fBxc{}, f5Bxc{}, fPz{}, fPphi{}, f2Pphi{}, f5Pphi{};
+  size_t smem_y = 0, smem_x2 = 0, smem_xc = 0, smem_z = 0, smem_phi = 0;
+  size_t smem_max() const {
+    size_t m = smem_y;
+    for (size_t v : {smem_x2, smem_xc, smem_z, smem_phi}) m = v > m ? v : m;
+    return m;
+  }
+};
+
+int even_tiles(int lines, int maxb) {
+  if (maxb < 1) maxb = 1;
+  const int nt = (lines + maxb - 1) / maxb;
+  return (lines + nt - 1) / nt;
+}
+
+Tiles make_tiles(const Geom &g, size_t cs, size_t budget) {
+  Tiles t;
+  const int pairs = (g.lines + 1) / 2;
+  auto cap = [](size_t v, int hi) { return (int)(v < (size_t)hi ? v : (size_t)hi); };
+  t.By = even_tiles(g.NzH, cap(budget / (2 * (size_t)g.Ny * cs), 16));
+  t.Bx = even_tiles(g.Ny * g.NzH, cap(budget / (2 * (size_t)g.Nx * cs), 16));
+  t.Bxc = even_tiles(g.Ny * g.NzH, cap(budget / (10 * (size_t)g.Nx * cs), 16));
+  t.Pz = even_tiles(pairs, cap(budget / (2 * (size_t)g.Nz * cs), 16));
+  int pm = cap(budget / (10 * (size_t)g.Nz * cs), 15);
+  if (pm < 1) pm = 1;
+  if (pm > 1 && pm % 2 == 0) pm -= 1;  // odd: conflict-free z-strided shared accesses
+  t.Pphi = pm < pairs ? pm : pairs;
+  t.fBy = make_fastdiv(t.By);
+  t.fBx = make_fastdiv(t.Bx);
+  t.fBxc = make_fastdiv(t.Bxc);
+  t.f5Bxc = make_fastdiv(5 * t.Bxc);
+  t.fPz = make_fastdiv(t.Pz);
+  t.fPphi = make_fastdiv(t.Pphi);
+  t.f2Pphi = make_fastdiv(2 * t.Pphi);
+  t.f5Pphi = make_fastdiv(5 * t.Pphi);
+  t.smem_y = 2 * (size_t)g.Ny * t.By * cs;
+  t.smem_x2 = 2 * (size_t)g.Nx * t.Bx * cs;
+  t.smem_xc = 10 * (size_t)g.Nx * t.Bxc * cs;
+  t.smem_z = 2 * (size_t)g.Nz * t.Pz * cs;
+  t.smem_phi = 10 * (size_t)g.Nz * t.Pphi * cs;
+  return t;
+}
+
+constexpr size_t kBudget64 = 96 * 1024;
+constexpr size_t kBudget32 = 72 * 1024;
+
 enum KernelId {
   kK_z_r2c, kK_z_c2r, kK_y_fft1, kK_y_fft5, kK_x_fft, kK_x_conv_fwd, kK_x_conv_adj, kK_z_phi_grad,
   kK_z_phi_energy, kK_z_grad, kK_local_energy, kK_reduce_terms, kK_dots, kK_axpy, kK_scal_add,
@@ -838,8 +959,8 @@ class EngineImpl {
   double *dot_partials = nullptr;
   unsigned int *dot_counter = nullptr;
   int dot_blocks = 0;
-  int By = 0, Bx = 0, Pz = 0, Pphi = 0;
-  size_t smem_y = 0, smem_x2 = 0, smem_x3 = 0, smem_z = 0, smem_phi = 0;
+  Tiles t64, t32;  // launch shapes of the FP64 and the FP32 kernels
+  template <typename T> const Tiles &tl() const { return sizeof(T) == 4 ? t32 : t64; }
   size_t bytes = 0;
   std::string err;
 
@@ -896,6 +1017,7 @@ class EngineImpl {
       err = "grid size " + std::to_string(n) + " has a prime factor above 13";
       return -1;
     }
+    plan_fill_ns(p);
     pf = p;
     std::vector<double2> h(n);
     std::vector<float2> hf(n);
@@ -971,63 +1093,50 @@ class EngineImpl {
     inv[8] = (R[0] * R[4] - R[1] * R[3]) / d;
     for (int i = 0; i < 3; i++)
       for (int j = 0; j < 3; j++) g.Bm[3 * i + j] = 2 * M_PI * inv[3 * j + i];
+    geom_finish(g);
 
     if (make_plan(s.Nx, px, &tw_x, pxf, &tw_xf) || make_plan(s.Ny, py, &tw_y, pyf, &tw_yf) ||
         make_plan(s.Nz, pz, &tw_z, pzf, &tw_zf))
       return -1;
 
-    // tile widths
     const size_t cs = sizeof(double2);
-    By = tile_width(g.NzH, g.Ny, cs, 2, 16);
-    Bx = tile_width(g.Ny * g.NzH, g.Nx, cs, 3, 16);
+    t64 = make_tiles(g, sizeof(double2), kBudget64);
+    t32 = make_tiles(g, sizeof(float2), kBudget32);
     const int pairs = (g.lines + 1) / 2;
-    Pz = tile_width(pairs, g.Nz, cs, 2, 16);
-    {
-      const size_t per_pair = (size_t)g.Nz * (2 * cs + 10 * sizeof(double));
-      int pm = (int)(kSmemBudget / per_pair);
-      if (pm < 1) pm = 1;
-      if (pm > 8) pm = 8;
-      const int nt = (pairs + pm - 1) / pm;
-      Pphi = (pairs + nt - 1) / nt;
-    }
-    smem_y = 2 * (size_t)g.Ny * By * cs;
-    smem_x2 = 2 * (size_t)g.Nx * Bx * cs;
-    smem_x3 = 3 * (size_t)g.Nx * Bx * cs;
-    smem_z = 2 * (size_t)g.Nz * Pz * cs;
-    smem_phi = (size_t)g.Nz * Pphi * (2 * cs + 10 * sizeof(double));
     const size_t mx = 227 * 1024;
-    if (smem_y > mx || smem_x3 > mx || smem_z > mx || smem_phi > mx) {
+    if (t64.smem_max() > mx || t32.smem_max() > mx) {
       err = "grid line too long for one shared-memory tile";
       return -1;
     }
-    set_smem(k_z_r2c<double>, smem_z);
-    set_smem(k_z_c2r<double>, smem_z);
-    set_smem(k_y_fft<double, -1>, smem_y);
-    set_smem(k_y_fft<double, +1>, smem_y);
-    set_smem(k_x_fft<double, -1>, smem_x2);
-    set_smem(k_x_fft<double, +1>, smem_x2);
-    set_smem(k_x_conv_fwd<double>, smem_x3);
-    set_smem(k_x_conv_adj<double>, smem_x3);
-    set_smem(k_z_phi<double, false>, smem_phi);
-    set_smem(k_z_phi<double, true>, smem_phi);
-    set_smem(k_z_grad<double>, smem_z);
-    // the FP32 kernels use the same tiles (half the bytes)
-    set_smem(k_z_r2c<float>, smem_z);
-    set_smem(k_y_fft<float, -1>, smem_y);
-    set_smem(k_y_fft<float, +1>, smem_y);
-    set_smem(k_x_conv_fwd<float>, smem_x3);
-    set_smem(k_x_conv_adj<float>, smem_x3);
-    set_smem(k_z_phi<float, false>, smem_phi);
-    set_smem(k_z_phi<float, true>, smem_phi);
-    set_smem(k_z_grad<float>, smem_z);
-    set_smem(k_z_hess<float>, smem_phi);
-    set_smem(k_z_jac<float>, smem_phi);
-    set_smem(k_z_hvp_out<float>, smem_z);
+    set_smem(k_z_r2c<double>, t64.smem_z);
+    set_smem(k_z_c2r<double>, t64.smem_z);
+    set_smem(k_y_fft<double, -1>, t64.smem_y);
+    set_smem(k_y_fft<double, +1>, t64.smem_y);
+    set_smem(k_x_fft<double, -1>, t64.smem_x2);
+    set_smem(k_x_fft<double, +1>, t64.smem_x2);
+    set_smem(k_x_conv_fwd<double>, t64.smem_xc);
+    set_smem(k_x_conv_adj<double>, t64.smem_xc);
+    set_smem(k_z_phi<double, false>, t64.smem_phi);
+    set_smem(k_z_phi<double, true>, t64.smem_phi);
+    set_smem(k_z_grad<double>, t64.smem_z);
+    set_smem(k_z_r2c<float>, t32.smem_z);
+    set_smem(k_y_fft<float, -1>, t32.smem_y);
+    set_smem(k_y_fft<float, +1>, t32.smem_y);
+    set_smem(k_x_conv_fwd<float>, t32.smem_xc);
+    set_smem(k_x_conv_adj<float>, t32.smem_xc);
+    set_smem(k_z_phi<float, false>, t32.smem_phi);
+    set_smem(k_z_phi<float, true>, t32.smem_phi);
+    set_smem(k_z_grad<float>, t32.smem_z);
+    set_smem(k_z_hess<float>, t32.smem_phi);
+    set_smem(k_z_jac<float>, t32.smem_phi);
+    set_smem(k_z_hvp_out<float>, t32.smem_z);
 
     if (alloc(&S0, cs * g.NC) || alloc(&S5, 5 * cs * g.NC) || alloc(&w3, sizeof(double) * g.NC) ||
         alloc(&w2, sizeof(double) * g.NC) || alloc(&wv, sizeof(double) * g.NC))
       return -1;
-    max_blocks = (pairs + Pphi - 1) / Pphi;
+    max_blocks = (pairs + t64.Pphi - 1) / t64.Pphi;
+    const int mb32 = (pairs + t32.Pphi - 1) / t32.Pphi;
+    if (max_blocks < mb32) max_blocks = mb32;
     if (max_blocks < 1024) max_blocks = 1024;
     if (alloc(&partials, sizeof(double) * kNumTerms * max_blocks)) return -1;
     if (alloc(&results, sizeof(double) * 8)) return -1;
@@ -1072,25 +1181,30 @@ class EngineImpl {
   int pairs_tiles(int P) const { return ((g.lines + 1) / 2 + P - 1) / P; }
 
   template <typename T> void y_fft(typename Cplx<T>::type *data, int nf, int sign) {
-    dim3 grid((g.NzH + By - 1) / By, g.Nx, nf);
+    const Tiles &t = tl<T>();
+    dim3 grid((g.NzH + t.By - 1) / t.By, g.Nx, nf);
     const int kid = nf == 1 ? kK_y_fft1 : kK_y_fft5;
     pre(kid);
-    if (sign < 0) k_y_fft<T, -1><<<grid, kThreads, smem_y, stream>>>(data, g, plan<T>(1), By);
-    else k_y_fft<T, +1><<<grid, kThreads, smem_y, stream>>>(data, g, plan<T>(1), By);
+    if (sign < 0)
+      k_y_fft<T, -1><<<grid, kThreads, t.smem_y, stream>>>(data, g, plan<T>(1), t.fBy);
+    else
+      k_y_fft<T, +1><<<grid, kThreads, t.smem_y, stream>>>(data, g, plan<T>(1), t.fBy);
     post(kid);
   }
-  int x_tiles() const { return (g.Ny * g.NzH + Bx - 1) / Bx; }
+  int x_tiles(int B) const { return (g.Ny * g.NzH + B - 1) / B; }
 
   template <typename T> int forward_weighted(const FmtSpec &f, const double *n) {
+    const Tiles &t = tl<T>();
     if (ensure_table<T>(f.R)) return -1;
     pre(kK_z_r2c);
-    k_z_r2c<T><<<dim3(pairs_tiles(Pz), 1), kThreads, smem_z, stream>>>(n, spec0<T>(), g,
-                                                                       plan<T>(2), Pz, T(1));
+    k_z_r2c<T><<<dim3(pairs_tiles(t.Pz), 1), kThreads, t.smem_z, stream>>>(
+        n, spec0<T>(), g, plan<T>(2), t.fPz, T(1));
     post(kK_z_r2c);
     y_fft<T>(spec0<T>(), 1, -1);
     pre(kK_x_conv_fwd);
-    k_x_conv_fwd<T><<<x_tiles(), kThreads, smem_x3, stream>>>(
-        spec0<T>(), spec5<T>(), table<T>(0), table<T>(1), table<T>(2), g, plan<T>(0), Bx);
+    k_x_conv_fwd<T><<<x_tiles(t.Bxc), kThreads, t.smem_xc, stream>>>(
+        spec0<T>(), spec5<T>(), table<T>(0), table<T>(1), table<T>(2), g, plan<T>(0), t.fBxc,
+        t.f5Bxc);
     post(kK_x_conv_fwd);
     y_fft<T>(spec5<T>(), 5, +1);
     return check("forward convolution");
@@ -1126,25 +1240,27 @@ class EngineImpl {
   template <typename T>
   int eval(const FmtSpec &f, const double *n, const double *V, const double *mask, double *grad,
            double *E_host, double *terms_host) {
+    const Tiles &t = tl<T>();
     const LocalArgs la = local_args(f);
     int nblk;
     if (f.terms & kTermHS) {
       if (forward_weighted<T>(f, n)) return -1;
-      nblk = pairs_tiles(Pphi);
+      nblk = pairs_tiles(t.Pphi);
       pre(grad ? kK_z_phi_grad : kK_z_phi_energy);
       if (grad)
-        k_z_phi<T, true><<<nblk, kThreads, smem_phi, stream>>>(spec5<T>(), n, V, g, plan<T>(2),
-                                                               Pphi, la, partials);
+        k_z_phi<T, true><<<nblk, kThreads, t.smem_phi, stream>>>(
+            spec5<T>(), n, V, g, plan<T>(2), t.fPphi, t.f2Pphi, t.f5Pphi, la, partials);
       else
-        k_z_phi<T, false><<<nblk, kThreads, smem_phi, stream>>>(spec5<T>(), n, V, g, plan<T>(2),
-                                                                Pphi, la, partials);
+        k_z_phi<T, false><<<nblk, kThreads, t.smem_phi, stream>>>(
+            spec5<T>(), n, V, g, plan<T>(2), t.fPphi, t.f2Pphi, t.f5Pphi, la, partials);
       post(grad ? kK_z_phi_grad : kK_z_phi_energy);
       if (check("phi")) return -1;
       if (grad) {
         y_fft<T>(spec5<T>(), 5, -1);
         pre(kK_x_conv_adj);
-        k_x_conv_adj<T><<<x_tiles(), kThreads, smem_x3, stream>>>(
-            spec5<T>(), spec0<T>(), table<T>(0), table<T>(1), table<T>(2), g, plan<T>(0), Bx);
+        k_x_conv_adj<T><<<x_tiles(t.Bxc), kThreads, t.smem_xc, stream>>>(
+            spec5<T>(), spec0<T>(), table<T>(0), table<T>(1), table<T>(2), g, plan<T>(0),
+            t.fBxc, t.f5Bxc);
         post(kK_x_conv_adj);
         y_fft<T>(spec0<T>(), 1, +1);
       }
@@ -1156,8 +1272,8 @@ class EngineImpl {
     }
     if (grad) {
       pre(kK_z_grad);
-      k_z_grad<T><<<pairs_tiles(Pz), kThreads, smem_z, stream>>>(spec0<T>(), n, V, mask, grad, g,
-                                                                  plan<T>(2), Pz, la);
+      k_z_grad<T><<<pairs_tiles(t.Pz), kThreads, t.smem_z, stream>>>(
+          spec0<T>(), n, V, mask, grad, g, plan<T>(2), t.fPz, la);
       post(kK_z_grad);
     }
     if (check("gradient")) return -1;
@@ -1172,8 +1288,8 @@ class EngineImpl {
       if (forward_weighted<float>(f, n)) return -1;
     }
     pre(kK_z_hess);
-    k_z_hess<float><<<pairs_tiles(Pphi), kThreads, smem_phi, stream>>>(
-        spec5<float>(), n, g, plan<float>(2), Pphi, la, hess, hloc);
+    k_z_hess<float><<<pairs_tiles(t32.Pphi), kThreads, t32.smem_phi, stream>>>(
+        spec5<float>(), n, g, plan<float>(2), t32.fPphi, t32.f5Pphi, la, hess, hloc);
     post(kK_z_hess);
     return check("hessian blocks");
   }
@@ -1183,20 +1299,21 @@ class EngineImpl {
     if (f.terms & kTermHS) {
       if (forward_weighted<float>(f, dx)) return -1;
       pre(kK_z_jac);
-      k_z_jac<float><<<pairs_tiles(Pphi), kThreads, smem_phi, stream>>>(
-          spec5<float>(), g, plan<float>(2), Pphi, g.dV * f.kT, hess);
+      k_z_jac<float><<<pairs_tiles(t32.Pphi), kThreads, t32.smem_phi, stream>>>(
+          spec5<float>(), g, plan<float>(2), t32.fPphi, t32.f2Pphi, t32.f5Pphi, g.dV * f.kT,
+          hess);
       post(kK_z_jac);
       y_fft<float>(spec5<float>(), 5, -1);
       pre(kK_x_conv_adj);
-      k_x_conv_adj<float><<<x_tiles(), kThreads, smem_x3, stream>>>(
+      k_x_conv_adj<float><<<x_tiles(t32.Bxc), kThreads, t32.smem_xc, stream>>>(
           spec5<float>(), spec0<float>(), table<float>(0), table<float>(1), table<float>(2), g,
-          plan<float>(0), Bx);
+          plan<float>(0), t32.fBxc, t32.f5Bxc);
       post(kK_x_conv_adj);
       y_fft<float>(spec0<float>(), 1, +1);
     }
     pre(kK_z_hvp_out);
-    k_z_hvp_out<float><<<pairs_tiles(Pz), kThreads, smem_z, stream>>>(
-        spec0<float>(), dx, hloc, mask, out, g, plan<float>(2), Pz, la);
+    k_z_hvp_out<float><<<pairs_tiles(t32.Pz), kThreads, t32.smem_z, stream>>>(
+        spec0<float>(), dx, hloc, mask, out, g, plan<float>(2), t32.fPz, la);
     post(kK_z_hvp_out);
     return check("hessian-vector product");
   }
@@ -1230,12 +1347,13 @@ const char *Engine::last_error() const { return impl_->err.c_str(); }
 int Engine::fft(const double *in, double2 *out) {
   EngineImpl &e = *impl_;
   e.pre(kK_z_r2c);
-    k_z_r2c<double><<<dim3(e.pairs_tiles(e.Pz), 1), kThreads, e.smem_z, e.stream>>>(in, out, e.g, e.pz,
-                                                                                 e.Pz, 1.0);
+    k_z_r2c<double><<<dim3(e.pairs_tiles(e.t64.Pz), 1), kThreads, e.t64.smem_z, e.stream>>>(
+      in, out, e.g, e.pz, e.t64.fPz, 1.0);
     e.post(kK_z_r2c);
   e.y_fft<double>(out, 1, -1);
   e.pre(kK_x_fft);
-    k_x_fft<double, -1><<<e.x_tiles(), kThreads, e.smem_x2, e.stream>>>(out, e.g, e.px, e.Bx, e.g.dV);
+    k_x_fft<double, -1><<<e.x_tiles(e.t64.Bx), kThreads, e.t64.smem_x2, e.stream>>>(
+      out, e.g, e.px, e.t64.fBx, e.g.dV);
     e.post(kK_x_fft);
   return e.check("fft");
 }
@@ -1244,12 +1362,13 @@ int Engine::ifft(const double2 *in, double *out) {
   EngineImpl &e = *impl_;
   cudaMemcpyAsync(e.S0, in, sizeof(double2) * e.g.NC, cudaMemcpyDeviceToDevice, e.stream);
   e.pre(kK_x_fft);
-    k_x_fft<double, +1><<<e.x_tiles(), kThreads, e.smem_x2, e.stream>>>(e.S0, e.g, e.px, e.Bx, 1.0);
+    k_x_fft<double, +1><<<e.x_tiles(e.t64.Bx), kThreads, e.t64.smem_x2, e.stream>>>(
+      e.S0, e.g, e.px, e.t64.fBx, 1.0);
     e.post(kK_x_fft);
   e.y_fft<double>(e.S0, 1, +1);
   e.pre(kK_z_c2r);
-    k_z_c2r<double><<<dim3(e.pairs_tiles(e.Pz), 1), kThreads, e.smem_z, e.stream>>>(
-      e.S0, out, e.g, e.pz, e.Pz, 1.0 / e.g.vol);
+    k_z_c2r<double><<<dim3(e.pairs_tiles(e.t64.Pz), 1), kThreads, e.t64.smem_z, e.stream>>>(
+      e.S0, out, e.g, e.pz, e.t64.fPz, 1.0 / e.g.vol);
     e.post(kK_z_c2r);
   return e.check("ifft");
 }
@@ -1258,8 +1377,8 @@ int Engine::weighted(const FmtSpec &f, const double *n, double *out5) {
   EngineImpl &e = *impl_;
   if (e.forward_weighted<double>(f, n)) return -1;
   e.pre(kK_z_c2r);
-    k_z_c2r<double><<<dim3(e.pairs_tiles(e.Pz), 5), kThreads, e.smem_z, e.stream>>>(e.S5, out5, e.g,
-                                                                                 e.pz, e.Pz, 1.0);
+    k_z_c2r<double><<<dim3(e.pairs_tiles(e.t64.Pz), 5), kThreads, e.t64.smem_z, e.stream>>>(
+      e.S5, out5, e.g, e.pz, e.t64.fPz, 1.0);
     e.post(kK_z_c2r);
   return e.check("weighted");
 }
@@ -1426,26 +1545,19 @@ int noalloc_energy_grad(const GridSpec &s, const FmtSpec &f, const double *n, co
   inv[8] = (R[0] * R[4] - R[1] * R[3]) / d;
   for (int i = 0; i < 3; i++)
     for (int j = 0; j < 3; j++) g.Bm[3 * i + j] = 2 * M_PI * inv[3 * j + i];
+  geom_finish(g);
+  plan_fill_ns(px);
+  plan_fill_ns(py);
+  plan_fill_ns(pz);
 
   const size_t cs = sizeof(double2);
-  const int By = tile_width(g.NzH, g.Ny, cs, 2, 16);
-  const int Bx = tile_width(g.Ny * g.NzH, g.Nx, cs, 3, 16);
+  const Tiles t = make_tiles(g, cs, kBudget64);
   const int pairs = (g.lines + 1) / 2;
-  const int Pz = tile_width(pairs, g.Nz, cs, 2, 16);
-  int Pphi;
-  {
-    const size_t per_pair = (size_t)g.Nz * (2 * cs + 10 * sizeof(double));
-    int pm = (int)(kSmemBudget / per_pair);
-    if (pm < 1) pm = 1;
-    if (pm > 8) pm = 8;
-    const int nt = (pairs + pm - 1) / pm;
-    Pphi = (pairs + nt - 1) / nt;
+  if (t.smem_max() > 227 * 1024) {
+    noalloc_fail(err, "grid line too long for one shared-memory tile");
+    return 1;
   }
-  const size_t smem_y = 2 * (size_t)g.Ny * By * cs;
-  const size_t smem_x3 = 3 * (size_t)g.Nx * Bx * cs;
-  const size_t smem_z = 2 * (size_t)g.Nz * Pz * cs;
-  const size_t smem_phi = (size_t)g.Nz * Pphi * (2 * cs + 10 * sizeof(double));
-  const int nblk_phi = (pairs + Pphi - 1) / Pphi;
+  const int nblk_phi = (pairs + t.Pphi - 1) / t.Pphi;
   const int nblk = (f.terms & kTermHS) ? nblk_phi : 4 * 152;
 
   // scratch layout
@@ -1526,13 +1638,13 @@ int noalloc_energy_grad(const GridSpec &s, const FmtSpec &f, const double *n, co
   py.tw = tw_y;
   pz.tw = tw_z;
 
-  set_smem(k_z_r2c<double>, smem_z);
-  set_smem(k_y_fft<double, -1>, smem_y);
-  set_smem(k_y_fft<double, +1>, smem_y);
-  set_smem(k_x_conv_fwd<double>, smem_x3);
-  set_smem(k_x_conv_adj<double>, smem_x3);
-  set_smem(k_z_phi<double, true>, smem_phi);
-  set_smem(k_z_grad<double>, smem_z);
+  set_smem(k_z_r2c<double>, t.smem_z);
+  set_smem(k_y_fft<double, -1>, t.smem_y);
+  set_smem(k_y_fft<double, +1>, t.smem_y);
+  set_smem(k_x_conv_fwd<double>, t.smem_xc);
+  set_smem(k_x_conv_adj<double>, t.smem_xc);
+  set_smem(k_z_phi<double, true>, t.smem_phi);
+  set_smem(k_z_grad<double>, t.smem_z);
 
   LocalArgs la;
   la.R = f.R;
@@ -1544,28 +1656,31 @@ int noalloc_energy_grad(const GridSpec &s, const FmtSpec &f, const double *n, co
   la.wr.inv_4piR = 1.0 / (4 * M_PI * f.R);
   la.wr.inv_4piR2 = 1.0 / (4 * M_PI * f.R * f.R);
   la.terms = f.terms;
-  const int ptiles_z = (pairs + Pz - 1) / Pz;
-  const int xt = (g.Ny * g.NzH + Bx - 1) / Bx;
-  const dim3 ygrid1((g.NzH + By - 1) / By, g.Nx, 1), ygrid5((g.NzH + By - 1) / By, g.Nx, 5);
+  const int ptiles_z = (pairs + t.Pz - 1) / t.Pz;
+  const int xt = (g.Ny * g.NzH + t.Bxc - 1) / t.Bxc;
+  const dim3 ygrid1((g.NzH + t.By - 1) / t.By, g.Nx, 1), ygrid5((g.NzH + t.By - 1) / t.By, g.Nx, 5);
   {
     const int blocks = (g.NC + kThreads - 1) / kThreads;
     k_weight_table<double><<<blocks < 4096 ? blocks : 4096, kThreads, 0, stream>>>(g, f.R, w3, w2,
                                                                                   wv);
   }
   if (f.terms & kTermHS) {
-    k_z_r2c<double><<<dim3(ptiles_z, 1), kThreads, smem_z, stream>>>(n, S0, g, pz, Pz, 1.0);
-    k_y_fft<double, -1><<<ygrid1, kThreads, smem_y, stream>>>(S0, g, py, By);
-    k_x_conv_fwd<double><<<xt, kThreads, smem_x3, stream>>>(S0, S5, w3, w2, wv, g, px, Bx);
-    k_y_fft<double, +1><<<ygrid5, kThreads, smem_y, stream>>>(S5, g, py, By);
-    k_z_phi<double, true><<<nblk_phi, kThreads, smem_phi, stream>>>(S5, n, V, g, pz, Pphi, la,
-                                                                    partials);
-    k_y_fft<double, -1><<<ygrid5, kThreads, smem_y, stream>>>(S5, g, py, By);
-    k_x_conv_adj<double><<<xt, kThreads, smem_x3, stream>>>(S5, S0, w3, w2, wv, g, px, Bx);
-    k_y_fft<double, +1><<<ygrid1, kThreads, smem_y, stream>>>(S0, g, py, By);
+    k_z_r2c<double><<<dim3(ptiles_z, 1), kThreads, t.smem_z, stream>>>(n, S0, g, pz, t.fPz, 1.0);
+    k_y_fft<double, -1><<<ygrid1, kThreads, t.smem_y, stream>>>(S0, g, py, t.fBy);
+    k_x_conv_fwd<double><<<xt, kThreads, t.smem_xc, stream>>>(S0, S5, w3, w2, wv, g, px, t.fBxc,
+                                                              t.f5Bxc);
+    k_y_fft<double, +1><<<ygrid5, kThreads, t.smem_y, stream>>>(S5, g, py, t.fBy);
+    k_z_phi<double, true><<<nblk_phi, kThreads, t.smem_phi, stream>>>(
+        S5, n, V, g, pz, t.fPphi, t.f2Pphi, t.f5Pphi, la, partials);
+    k_y_fft<double, -1><<<ygrid5, kThreads, t.smem_y, stream>>>(S5, g, py, t.fBy);
+    k_x_conv_adj<double><<<xt, kThreads, t.smem_xc, stream>>>(S5, S0, w3, w2, wv, g, px, t.fBxc,
+                                                              t.f5Bxc);
+    k_y_fft<double, +1><<<ygrid1, kThreads, t.smem_y, stream>>>(S0, g, py, t.fBy);
   } else {
     k_local_energy<double><<<nblk, kThreads, 0, stream>>>(n, V, g, la, partials);
   }
-  k_z_grad<double><<<ptiles_z, kThreads, smem_z, stream>>>(S0, n, V, mask, grad, g, pz, Pz, la);
+  k_z_grad<double><<<ptiles_z, kThreads, t.smem_z, stream>>>(S0, n, V, mask, grad, g, pz, t.fPz,
+                                                             la);
   k_reduce_terms<<<1, kThreads, 0, stream>>>(partials, nblk, g.dV, results);
   double res[8];
   e = cudaGetLastError();

@@ -7,6 +7,8 @@
 
 #include <cuda_runtime.h>
 
+#include "fastdiv.cuh"
+
 #include <string>
 
 namespace deft {
@@ -43,8 +45,18 @@ struct Geom {
   int NR;     // Nx*Ny*Nz real points
   int NC;     // Nx*Ny*NzH complex points
   double Bm[9];  // k_c = sum_d Bm[3c+d] m_d  (2 pi R^-T)
+  float Bmf[9];  // the same in FP32, for the mixed form
   double dV, vol, dr, scale;  // scale = dV / vol (fft x dV then ifft x 1/V)
+  FastDiv fNz, fNzH, fNy;     // division by Nz, Nz/2+1, Ny
 };
+
+// Fills the derived members (FP32 copy of Bm, fast dividers).
+inline void geom_finish(Geom &g) {
+  for (int i = 0; i < 9; i++) g.Bmf[i] = (float)g.Bm[i];
+  g.fNz = make_fastdiv((unsigned)g.Nz);
+  g.fNzH = make_fastdiv((unsigned)g.NzH);
+  g.fNy = make_fastdiv((unsigned)g.Ny);
+}
 
 class EngineImpl;
 
