@@ -281,60 +281,64 @@ __global__ void __launch_bounds__(kThreads) k_x_fft(typename Cplx<T>::type *data
   }
 }
 
-// x-FFT of n^, multiplication by the five weights, inverse x-FFT of all
-// five at once: one tile of 5B lines (line a*B + b = field a, column b).
+// x-FFT of n^, multiplication by the five weights, and the five inverse
+// x-FFTs one field at a time (three tiles of B lines: the forward result and
+// a ping-pong pair), which keeps B wide for coalesced column runs.
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_x_conv_fwd(
     const typename Cplx<T>::type *__restrict__ in, typename Cplx<T>::type *__restrict__ out5,
     const T *__restrict__ w3, const T *__restrict__ w2, const T *__restrict__ wv, Geom g,
-    FftPlan px, FastDiv fB, FastDiv f5B) {
+    FftPlan px, FastDiv fB) {
   const int B = (int)fB.d;
   using C = typename Cplx<T>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  C *X = reinterpret_cast<C *>(smem_raw);
-  C *Y = X + g.Nx * 5 * B;
+  C *bufA = reinterpret_cast<C *>(smem_raw);
+  C *bufB = bufA + g.Nx * B;
+  C *bufC = bufB + g.Nx * B;
   const int J = g.Ny * g.NzH;
   const int j0 = blockIdx.x * B;
   for (int idx = threadIdx.x; idx < g.Nx * B; idx += blockDim.x) {
     int e, j;
     fdivmod(idx, fB, e, j);
     j += j0;
-    X[idx] = j < J ? in[(size_t)e * J + j] : C{0, 0};
+    bufA[idx] = j < J ? in[(size_t)e * J + j] : C{0, 0};
   }
-  C *R0 = fft_tile<T, -1>(X, Y, fB, px);  // layout e*B + b
-  C *W = (R0 == X) ? Y : X;               // layout e*5B + a*B + b
-  const int B5 = 5 * B;
-  for (int idx = threadIdx.x; idx < g.Nx * B5; idx += blockDim.x) {
-    int e, bb, a, b;
-    fdivmod(idx, f5B, e, bb);
-    fdivmod(bb, fB, a, b);
-    const int j = j0 + b;
-    C o = C{0, 0};
-    if (j < J) {
-      const size_t i = (size_t)e * J + j;
-      const C v = R0[e * B + b];
-      if (a == 0) {
-        const T w = w3[i];
-        o = C{v.x * w, v.y * w};
-      } else if (a == 1) {
-        const T w = w2[i];
-        o = C{v.x * w, v.y * w};
-      } else {
-        int y, z;
-        fdivmod(j, g.fNzH, y, z);
-        const T w = kcomp_t<T>(g, a - 2, e, y, z) * wv[i];
-        o = C{-v.y * w, v.x * w};  // times i w
+  const C *R0 = fft_tile<T, -1>(bufA, bufB, fB, px);
+  C *F1 = (R0 == bufA) ? bufB : bufA;
+  C *F2 = bufC;
+  for (int a = 0; a < 5; a++) {
+    for (int idx = threadIdx.x; idx < g.Nx * B; idx += blockDim.x) {
+      int e, j;
+      fdivmod(idx, fB, e, j);
+      j += j0;
+      C o = C{0, 0};
+      if (j < J) {
+        const size_t i = (size_t)e * J + j;
+        const C v = R0[idx];
+        if (a == 0) {
+          const T w = w3[i];
+          o = C{v.x * w, v.y * w};
+        } else if (a == 1) {
+          const T w = w2[i];
+          o = C{v.x * w, v.y * w};
+        } else {
+          int y, z;
+          fdivmod(j, g.fNzH, y, z);
+          const T w = kcomp_t<T>(g, a - 2, e, y, z) * wv[i];
+          o = C{-v.y * w, v.x * w};  // times i w
+        }
       }
+      F1[idx] = o;
     }
-    W[idx] = o;
-  }
-  const C *res = fft_tile<T, +1>(W, R0, f5B, px);
-  for (int idx = threadIdx.x; idx < g.Nx * B5; idx += blockDim.x) {
-    int e, bb, a, b;
-    fdivmod(idx, f5B, e, bb);
-    fdivmod(bb, fB, a, b);
-    const int j = j0 + b;
-    if (j < J) out5[(size_t)a * g.NC + (size_t)e * J + j] = res[idx];
+    const C *res = fft_tile<T, +1>(F1, F2, fB, px);
+    C *dst = out5 + (size_t)a * g.NC;
+    for (int idx = threadIdx.x; idx < g.Nx * B; idx += blockDim.x) {
+      int e, j;
+      fdivmod(idx, fB, e, j);
+      j += j0;
+      if (j < J) dst[(size_t)e * J + j] = res[idx];
+    }
+    __syncthreads();
   }
 }
 
@@ -755,10 +759,26 @@ __global__ void k_dots(int k, const double *a0, const double *b0, const double *
   __shared__ double red[32 * 3];
   __shared__ bool last;
   double acc[3] = {0, 0, 0};
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    acc[0] += a0[i] * b0[i];
-    if (k > 1) acc[1] += a1[i] * b1[i];
-    if (k > 2) acc[2] += a2[i] * b2[i];
+  const int n2 = n >> 1;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += gridDim.x * blockDim.x) {
+    const double2 x0 = reinterpret_cast<const double2 *>(a0)[i];
+    const double2 y0 = reinterpret_cast<const double2 *>(b0)[i];
+    acc[0] += x0.x * y0.x + x0.y * y0.y;
+    if (k > 1) {
+      const double2 x1 = reinterpret_cast<const double2 *>(a1)[i];
+      const double2 y1 = reinterpret_cast<const double2 *>(b1)[i];
+      acc[1] += x1.x * y1.x + x1.y * y1.y;
+    }
+    if (k > 2) {
+      const double2 x2 = reinterpret_cast<const double2 *>(a2)[i];
+      const double2 y2 = reinterpret_cast<const double2 *>(b2)[i];
+      acc[2] += x2.x * y2.x + x2.y * y2.y;
+    }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0 && (n & 1)) {
+    acc[0] += a0[n - 1] * b0[n - 1];
+    if (k > 1) acc[1] += a1[n - 1] * b1[n - 1];
+    if (k > 2) acc[2] += a2[n - 1] * b2[n - 1];
   }
   block_reduce<3>(acc, red);
   if (threadIdx.x == 0) {
@@ -781,14 +801,34 @@ __global__ void k_dots(int k, const double *a0, const double *b0, const double *
   }
 }
 
+// Vector kernels: two doubles per thread per step (16-byte accesses); the
+// vectors come from cudaMalloc (256-byte aligned), n odd leaves a tail.
 __global__ void k_axpy(double alpha, const double *x, double *y, int n) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-    y[i] += alpha * x[i];
+  const int n2 = n >> 1;
+  const double2 *x2 = reinterpret_cast<const double2 *>(x);
+  double2 *y2 = reinterpret_cast<double2 *>(y);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += gridDim.x * blockDim.x) {
+    const double2 a = x2[i];
+    double2 b = y2[i];
+    b.x += alpha * a.x;
+    b.y += alpha * a.y;
+    y2[i] = b;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0 && (n & 1)) y[n - 1] += alpha * x[n - 1];
 }
 
 __global__ void k_scal_add(double beta, double *d, double alpha, const double *g, int n) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-    d[i] = alpha * g[i] + beta * d[i];
+  const int n2 = n >> 1;
+  const double2 *g2 = reinterpret_cast<const double2 *>(g);
+  double2 *d2 = reinterpret_cast<double2 *>(d);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += gridDim.x * blockDim.x) {
+    const double2 a = g2[i];
+    double2 b = d2[i];
+    b.x = alpha * a.x + beta * b.x;
+    b.y = alpha * a.y + beta * b.y;
+    d2[i] = b;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0 && (n & 1)) d[n - 1] = alpha * g[n - 1] + beta * d[n - 1];
 }
 
 // ---------------------------------------------------------------------------
@@ -836,12 +876,12 @@ int tile_width(int lines, int L, size_t bytes_per_elem, int nbuf, int cap) {
 // Tile widths and shared-memory sizes of every kernel for one precision
 // (cs = bytes of one complex element).
 struct Tiles {
-  int By = 1, Bx = 1, Bxc = 1, Pz = 1, Pphi = 1;
-  FastDiv fBy{}, fBx{}, fBxc{}, f5Bxc{}, fPz{}, fPphi{}, f2Pphi{}, f5Pphi{};
-  size_t smem_y = 0, smem_x2 = 0, smem_xc = 0, smem_z = 0, smem_phi = 0;
+  int By = 1, Bx = 1, Bxf = 1, Bxc = 1, Pz = 1, Pphi = 1;
+  FastDiv fBy{}, fBx{}, fBxf{}, fBxc{}, f5Bxc{}, fPz{}, fPphi{}, f2Pphi{}, f5Pphi{};
+  size_t smem_y = 0, smem_x2 = 0, smem_xf = 0, smem_xc = 0, smem_z = 0, smem_phi = 0;
   size_t smem_max() const {
     size_t m = smem_y;
-    for (size_t v : {smem_x2, smem_xc, smem_z, smem_phi}) m = v > m ? v : m;
+    for (size_t v : {smem_x2, smem_xf, smem_xc, smem_z, smem_phi}) m = v > m ? v : m;
     return m;
   }
 };
@@ -858,6 +898,7 @@ Tiles make_tiles(const Geom &g, size_t cs, size_t budget) {
   auto cap = [](size_t v, int hi) { return (int)(v < (size_t)hi ? v : (size_t)hi); };
   t.By = even_tiles(g.NzH, cap(budget / (2 * (size_t)g.Ny * cs), 16));
   t.Bx = even_tiles(g.Ny * g.NzH, cap(budget / (2 * (size_t)g.Nx * cs), 16));
+  t.Bxf = even_tiles(g.Ny * g.NzH, cap(budget / (3 * (size_t)g.Nx * cs), 16));
   t.Bxc = even_tiles(g.Ny * g.NzH, cap(budget / (10 * (size_t)g.Nx * cs), 16));
   t.Pz = even_tiles(pairs, cap(budget / (2 * (size_t)g.Nz * cs), 16));
   int pm = cap(budget / (10 * (size_t)g.Nz * cs), 15);
@@ -866,6 +907,7 @@ Tiles make_tiles(const Geom &g, size_t cs, size_t budget) {
   t.Pphi = pm < pairs ? pm : pairs;
   t.fBy = make_fastdiv(t.By);
   t.fBx = make_fastdiv(t.Bx);
+  t.fBxf = make_fastdiv(t.Bxf);
   t.fBxc = make_fastdiv(t.Bxc);
   t.f5Bxc = make_fastdiv(5 * t.Bxc);
   t.fPz = make_fastdiv(t.Pz);
@@ -874,6 +916,7 @@ Tiles make_tiles(const Geom &g, size_t cs, size_t budget) {
   t.f5Pphi = make_fastdiv(5 * t.Pphi);
   t.smem_y = 2 * (size_t)g.Ny * t.By * cs;
   t.smem_x2 = 2 * (size_t)g.Nx * t.Bx * cs;
+  t.smem_xf = 3 * (size_t)g.Nx * t.Bxf * cs;
   t.smem_xc = 10 * (size_t)g.Nx * t.Bxc * cs;
   t.smem_z = 2 * (size_t)g.Nz * t.Pz * cs;
   t.smem_phi = 10 * (size_t)g.Nz * t.Pphi * cs;
@@ -1114,7 +1157,7 @@ class EngineImpl {
     set_smem(k_y_fft<double, +1>, t64.smem_y);
     set_smem(k_x_fft<double, -1>, t64.smem_x2);
     set_smem(k_x_fft<double, +1>, t64.smem_x2);
-    set_smem(k_x_conv_fwd<double>, t64.smem_xc);
+    set_smem(k_x_conv_fwd<double>, t64.smem_xf);
     set_smem(k_x_conv_adj<double>, t64.smem_xc);
     set_smem(k_z_phi<double, false>, t64.smem_phi);
     set_smem(k_z_phi<double, true>, t64.smem_phi);
@@ -1122,7 +1165,7 @@ class EngineImpl {
     set_smem(k_z_r2c<float>, t32.smem_z);
     set_smem(k_y_fft<float, -1>, t32.smem_y);
     set_smem(k_y_fft<float, +1>, t32.smem_y);
-    set_smem(k_x_conv_fwd<float>, t32.smem_xc);
+    set_smem(k_x_conv_fwd<float>, t32.smem_xf);
     set_smem(k_x_conv_adj<float>, t32.smem_xc);
     set_smem(k_z_phi<float, false>, t32.smem_phi);
     set_smem(k_z_phi<float, true>, t32.smem_phi);
@@ -1202,9 +1245,8 @@ class EngineImpl {
     post(kK_z_r2c);
     y_fft<T>(spec0<T>(), 1, -1);
     pre(kK_x_conv_fwd);
-    k_x_conv_fwd<T><<<x_tiles(t.Bxc), kThreads, t.smem_xc, stream>>>(
-        spec0<T>(), spec5<T>(), table<T>(0), table<T>(1), table<T>(2), g, plan<T>(0), t.fBxc,
-        t.f5Bxc);
+    k_x_conv_fwd<T><<<x_tiles(t.Bxf), kThreads, t.smem_xf, stream>>>(
+        spec0<T>(), spec5<T>(), table<T>(0), table<T>(1), table<T>(2), g, plan<T>(0), t.fBxf);
     post(kK_x_conv_fwd);
     y_fft<T>(spec5<T>(), 5, +1);
     return check("forward convolution");
@@ -1641,7 +1683,7 @@ int noalloc_energy_grad(const GridSpec &s, const FmtSpec &f, const double *n, co
   set_smem(k_z_r2c<double>, t.smem_z);
   set_smem(k_y_fft<double, -1>, t.smem_y);
   set_smem(k_y_fft<double, +1>, t.smem_y);
-  set_smem(k_x_conv_fwd<double>, t.smem_xc);
+  set_smem(k_x_conv_fwd<double>, t.smem_xf);
   set_smem(k_x_conv_adj<double>, t.smem_xc);
   set_smem(k_z_phi<double, true>, t.smem_phi);
   set_smem(k_z_grad<double>, t.smem_z);
@@ -1667,8 +1709,8 @@ int noalloc_energy_grad(const GridSpec &s, const FmtSpec &f, const double *n, co
   if (f.terms & kTermHS) {
     k_z_r2c<double><<<dim3(ptiles_z, 1), kThreads, t.smem_z, stream>>>(n, S0, g, pz, t.fPz, 1.0);
     k_y_fft<double, -1><<<ygrid1, kThreads, t.smem_y, stream>>>(S0, g, py, t.fBy);
-    k_x_conv_fwd<double><<<xt, kThreads, t.smem_xc, stream>>>(S0, S5, w3, w2, wv, g, px, t.fBxc,
-                                                              t.f5Bxc);
+    k_x_conv_fwd<double><<<(g.Ny * g.NzH + t.Bxf - 1) / t.Bxf, kThreads, t.smem_xf, stream>>>(
+        S0, S5, w3, w2, wv, g, px, t.fBxf);
     k_y_fft<double, +1><<<ygrid5, kThreads, t.smem_y, stream>>>(S5, g, py, t.fBy);
     k_z_phi<double, true><<<nblk_phi, kThreads, t.smem_phi, stream>>>(
         S5, n, V, g, pz, t.fPphi, t.f2Pphi, t.f5Pphi, la, partials);
