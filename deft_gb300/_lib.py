@@ -28,7 +28,7 @@ EXPORTS = (
     "deft_find_chemical_potential",
     "deft_fmt_energy_grad_noalloc", "deft_noalloc_scratch_bytes",
     "deft_cg_create", "deft_cg_destroy", "deft_cg_set_x", "deft_cg_get_x", "deft_cg_x_device",
-    "deft_cg_step", "deft_cg_solve",
+    "deft_cg_step", "deft_cg_solve", "deft_batch_solve",
 )
 
 
@@ -56,6 +56,17 @@ class CgStatus(ctypes.Structure):
     _fields_ = [("iter", ctypes.c_int), ("evals", ctypes.c_int), ("energy", ctypes.c_double),
                 ("gnorm", ctypes.c_double), ("converged", ctypes.c_int), ("status", ctypes.c_int),
                 ("evals_fp64", ctypes.c_int), ("hvps", ctypes.c_int), ("stage", ctypes.c_int)]
+
+
+class BatchProblem(ctypes.Structure):
+    _fields_ = [("lat", ctypes.c_double * 9), ("N", ctypes.c_int * 3), ("R", ctypes.c_double),
+                ("kT", ctypes.c_double), ("mu", ctypes.c_double), ("terms", ctypes.c_int),
+                ("precision", ctypes.c_int), ("mask", ctypes.c_void_p), ("V", ctypes.c_void_p),
+                ("n_init", ctypes.c_void_p), ("n_out", ctypes.c_void_p)]
+
+
+class BatchParams(ctypes.Structure):
+    _fields_ = [("workers", ctypes.c_int), ("cg", CgParams)]
 
 
 _lib = None
@@ -112,6 +123,8 @@ def load():
         "deft_cg_x_device": (_vp, [_vp]),
         "deft_cg_step": (ctypes.c_int, [_vp, ctypes.POINTER(CgStatus)]),
         "deft_cg_solve": (ctypes.c_int, [_vp, ctypes.POINTER(CgStatus)]),
+        "deft_batch_solve": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.POINTER(BatchProblem),
+                                            ctypes.POINTER(BatchParams), ctypes.POINTER(CgStatus)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

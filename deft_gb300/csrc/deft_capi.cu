@@ -136,6 +136,12 @@ int set_field(deft_fmt *f, double **slot, const double *src, int on_device) {
 
 }  // namespace
 
+namespace deft {
+// Sets the calling thread's deft_last_error() message (for batch workers'
+// errors reported on the caller's thread).
+void set_last_error_message(const std::string &m) { g_err = m; }
+}  // namespace deft
+
 extern "C" {
 
 const char *deft_strerror(int s) {

@@ -858,9 +858,21 @@ double nQ_of(double kT) {
   return x * std::sqrt(x);
 }
 
+// Raises the kernel's dynamic shared-memory cap to everything the device
+// allows.  The cap is a per-kernel setting shared by every engine in the
+// process, so it is always set to the same (largest) value: an engine for a
+// small grid must not lower it under a live engine for a larger one.  Each
+// launch still requests only the bytes its tiles need.
 template <typename K>
 void set_smem(K kernel, size_t bytes) {
-  cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  cudaFuncAttributes fa;
+  int dev = 0, optin = 0;
+  cudaFuncGetAttributes(&fa, kernel);
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  int cap = optin - (int)fa.sharedSizeBytes;
+  if (cap < (int)bytes) cap = (int)bytes;  // the launch then reports the shortfall
+  cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
 }
 
 int tile_width(int lines, int L, size_t bytes_per_elem, int nbuf, int cap) {

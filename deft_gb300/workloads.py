@@ -97,3 +97,19 @@ class Solute:
     @property
     def size(self):
         return int(np.prod(self.shape))
+
+
+def batch_sweep(count=64, seed=3, sizes=(32, 48, 64, 96, 128), dx=0.2, eta=(0.05, 0.45),
+                width=(3.0, 10.0), R=1.0, kT=1.0):
+    """The batched sweep: `count` independent hard-wall slits, packing
+    fraction uniform in eta, grid edge drawn from `sizes` (cubic, spacing dx),
+    slit width uniform in `width` but at most 0.7 of the cell edge (so a wall
+    remains on small cells).  Returns a list of Slit problems."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    out = []
+    for i in range(count):
+        N = int(rng.choice(sizes))
+        e = float(rng.uniform(*eta))
+        w = min(float(rng.uniform(*width)), 0.7 * N * dx)
+        out.append(Slit(N=N, dx=dx, eta=e, width=w, R=R, kT=kT, seed=seed * 1000 + i))
+    return out

@@ -200,6 +200,34 @@ int deft_cg_step(deft_cg *cg, deft_cg_status *st);
 /* improve_energy() until converged, an error, or maxiter. */
 int deft_cg_solve(deft_cg *cg, deft_cg_status *st);
 
+/* ---- batched solves ----
+ * Many independent state points and uneven grids on one GPU (no reference
+ * counterpart: the reference solves one problem per process).  Each problem
+ * is minimised exactly as deft_cg_solve would minimise it; problems run
+ * concurrently on `workers` CUDA streams driven by as many host threads,
+ * each reusing one grid (plans, tables, work spectra) per grid shape.
+ * Host pointers throughout. */
+typedef struct {
+  double lat[9];        /* a1, a2, a3 */
+  int N[3];             /* grid */
+  double R, kT, mu;
+  int terms;            /* DEFT_TERM_*; DEFT_TERM_MASK needs mask, DEFT_TERM_VEXT needs V */
+  int precision;        /* DEFT_PRECISION_* */
+  const double *mask;   /* or NULL */
+  const double *V;      /* or NULL */
+  const double *n_init; /* initial density */
+  double *n_out;        /* converged density (may alias n_init) */
+} deft_batch_problem;
+
+typedef struct {
+  int workers;          /* concurrent streams (0 = 8) */
+  deft_cg_params cg;    /* minimiser settings for every problem */
+} deft_batch_params;
+
+/* Returns DEFT_OK or the first error; status_out[i] holds problem i's result. */
+int deft_batch_solve(int device, int count, const deft_batch_problem *problems,
+                     const deft_batch_params *params, deft_cg_status *status_out);
+
 #ifdef __cplusplus
 }
 #endif

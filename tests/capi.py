@@ -132,3 +132,33 @@ class CG:
 
     def close(self):
         self.L.deft_cg_destroy(self.h)
+
+
+def batch_solve(problems, precision=0, workers=4, gtol=1e-9, device=0):
+    """Runs deft_batch_solve on workloads.Slit-like problems (host arrays);
+    returns (status code, list of CgStatus, list of converged profiles)."""
+    keep = []
+    arr = (_lib.BatchProblem * len(problems))()
+    outs = []
+    for k, s in enumerate(problems):
+        mask = np.ascontiguousarray(s.mask.reshape(-1), dtype=np.float64)
+        n0 = np.ascontiguousarray(s.n0.reshape(-1), dtype=np.float64)
+        out = np.empty_like(n0)
+        keep += [mask, n0]
+        outs.append(out)
+        p = arr[k]
+        for i, v in enumerate(np.asarray(s.lat, dtype=np.float64).reshape(9)):
+            p.lat[i] = v
+        for i, v in enumerate(s.shape):
+            p.N[i] = v
+        p.R, p.kT, p.mu = s.R, s.kT, s.mu
+        p.terms = _lib.TERM_HS | _lib.TERM_IDEAL | _lib.TERM_MU | _lib.TERM_MASK
+        p.precision = precision
+        p.mask = mask.ctypes.data
+        p.V = None
+        p.n_init = n0.ctypes.data
+        p.n_out = out.ctypes.data
+    bp = _lib.BatchParams(workers, _lib.CgParams(_lib.LS_SECANT, gtol, 20000, 1.0, 0.0, 0.0))
+    st = (_lib.CgStatus * len(problems))()
+    code = _lib.load().deft_batch_solve(device, len(problems), arr, ctypes.byref(bp), st)
+    return code, list(st), outs
