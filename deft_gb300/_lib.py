@@ -29,6 +29,9 @@ EXPORTS = (
     "deft_fmt_energy_grad_noalloc", "deft_noalloc_scratch_bytes",
     "deft_cg_create", "deft_cg_destroy", "deft_cg_set_x", "deft_cg_get_x", "deft_cg_x_device",
     "deft_cg_step", "deft_cg_solve", "deft_batch_solve",
+    "deft_fno_create", "deft_fno_destroy", "deft_fno_param_count", "deft_fno_get_params",
+    "deft_fno_set_params", "deft_fno_eval", "deft_fno_adam", "deft_fno_train_step",
+    "deft_fno_warm_start", "deft_fno_initial_density",
 )
 
 
@@ -123,6 +126,21 @@ def load():
         "deft_cg_x_device": (_vp, [_vp]),
         "deft_cg_step": (ctypes.c_int, [_vp, ctypes.POINTER(CgStatus)]),
         "deft_cg_solve": (ctypes.c_int, [_vp, ctypes.POINTER(CgStatus)]),
+        "deft_fno_create": (ctypes.c_int, [ctypes.c_int] * 5 + [ctypes.c_ulonglong, _pp]),
+        "deft_fno_destroy": (ctypes.c_int, [_vp]),
+        "deft_fno_param_count": (ctypes.c_size_t, [_vp]),
+        "deft_fno_get_params": (ctypes.c_int, [_vp, _dp]),
+        "deft_fno_set_params": (ctypes.c_int, [_vp, _dp]),
+        "deft_fno_eval": (ctypes.c_int, [_vp, _dp, ctypes.c_float, _dp, ctypes.c_int, _dp, _dp,
+                                         _dp]),
+        "deft_fno_adam": (ctypes.c_int, [_vp, ctypes.c_float]),
+        "deft_fno_train_step": (ctypes.c_int, [_vp, _dp, ctypes.c_float, _dp, ctypes.c_int,
+                                               ctypes.c_float, _dp]),
+        "deft_fno_warm_start": (ctypes.c_int, [_vp, _dp, ctypes.c_double, ctypes.c_double,
+                                               ctypes.c_double, _dp]),
+        "deft_fno_initial_density": (ctypes.c_int, [_vp, _vp, _dp, ctypes.c_double,
+                                                    ctypes.c_double, ctypes.c_double, _dp, _dp,
+                                                    _dp]),
         "deft_batch_solve": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.POINTER(BatchProblem),
                                             ctypes.POINTER(BatchParams), ctypes.POINTER(CgStatus)]),
     }

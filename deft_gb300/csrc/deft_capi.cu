@@ -140,6 +140,13 @@ namespace deft {
 // Sets the calling thread's deft_last_error() message (for batch workers'
 // errors reported on the caller's thread).
 void set_last_error_message(const std::string &m) { g_err = m; }
+// Grid shape of a functional (for entry points in other translation units
+// that must check array sizes against it).
+void fmt_shape(const deft_fmt *f, int N[3]) {
+  N[0] = f->grid->spec.Nx;
+  N[1] = f->grid->spec.Ny;
+  N[2] = f->grid->spec.Nz;
+}
 }  // namespace deft
 
 extern "C" {
@@ -757,7 +764,20 @@ int step_secant(deft_cg *c, deft_cg_status *st, const deft::FmtSpec &spec, doubl
   if (c->iter > 0 && s0 != 0) c->alpha *= c->s_prev / s0;
   c->s_prev = s0;
   c->iter++;
-  if (int s = secant_search(c, spec, c->E, s0)) return s;
+  const double E0 = c->E;
+  int ls = secant_search(c, spec, E0, s0);
+  if (ls == DEFT_ERR_LINESEARCH && beta != 0) {
+    // The search failed along the conjugate direction (x is back at the
+    // start point, whose gradient is in gold): retry once along steepest
+    // descent, which cannot drive a vanishing density negative.
+    if (e->copy(c->gold, c->g)) return eng_err(e);
+    c->E = E0;
+    if (e->scal_add(0.0, c->d, -1.0, c->g)) return eng_err(e);
+    s0 = -c->goldsqr;
+    c->s_prev = s0;
+    ls = secant_search(c, spec, E0, s0);
+  }
+  if (ls) return ls;
   st->gnorm = std::sqrt(c->gg);
   if (st->gnorm < gtol) c->done = true;
   return DEFT_OK;

@@ -113,3 +113,68 @@ def batch_sweep(count=64, seed=3, sizes=(32, 48, 64, 96, 128), dx=0.2, eta=(0.05
         w = min(float(rng.uniform(*width)), 0.7 * N * dx)
         out.append(Slit(N=N, dx=dx, eta=e, width=w, R=R, kT=kT, seed=seed * 1000 + i))
     return out
+
+
+class WallsSolutes:
+    """Hard-wall slit (fluid in 0 < z < width) holding hard-sphere solutes:
+    n = 0 and frozen DOF in the walls and within radius Rs of each solute
+    centre (periodic distances), as sphere.cpp excludes its cavity
+    (papers/contact/figs/sphere.cpp:93-105).  The bulk start is nb on the free
+    points (amp = 0) or nb (1 + amp xi) with the smoothed-noise recipe.  The
+    mask and start are built on each access (a training set holds thousands
+    of these)."""
+
+    def __init__(self, N=128, dx=0.2, eta=0.3, width=6.0, solutes=(), R=1.0, kT=1.0, seed=0,
+                 amp=0.0, sigma=0.4):
+        self.shape = (N, N, N)
+        self.dx = dx
+        self.L = N * dx
+        self.lat = np.diag([self.L] * 3)
+        self.width = width
+        self.solutes = tuple(tuple(float(v) for v in s) for s in solutes)
+        self.R, self.kT, self.eta = R, kT, eta
+        self.nb = bulk_density(eta, R)
+        self.mu = chemical_potential(R, kT, self.nb)
+        self.seed, self.amp, self.sigma = seed, amp, sigma
+
+    @property
+    def mask(self):
+        N, dx = self.shape[0], self.dx
+        c = np.arange(N) * dx
+        inside = (c > 1e-12) & (c < self.width - 1e-12)
+        mask = np.broadcast_to(inside[None, None, :], self.shape).copy()
+        for (x0, y0, z0, rs) in self.solutes:
+            d = [np.minimum(np.abs(c - a), self.L - np.abs(c - a)) for a in (x0, y0, z0)]
+            r2 = d[0][:, None, None] ** 2 + d[1][None, :, None] ** 2 + d[2][None, None, :] ** 2
+            mask &= r2 > rs * rs
+        return mask.astype(np.float64)
+
+    @property
+    def n0(self):
+        if self.amp:
+            xi = smoothed_noise(self.shape, (self.dx,) * 3, self.sigma, self.seed)
+            return self.nb * (1 + self.amp * xi) * self.mask
+        return self.nb * self.mask
+
+    @property
+    def size(self):
+        return int(np.prod(self.shape))
+
+
+def walls_solutes_set(count, seed, N=128, dx=0.2, eta=(0.1, 0.4), width=(3.0, 10.0),
+                      solutes=(1, 4), radius=(1.0, 4.0), R=1.0, kT=1.0):
+    """`count` problems for the learned warm start: slit width uniform in
+    `width` (at most 0.7 of the cell edge), 1-4 solutes with radius uniform in
+    `radius`, centres uniform in x, y and in the slit's z range, packing
+    fraction uniform in `eta`; every problem starts from the bulk density."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    out = []
+    L = N * dx
+    for _ in range(count):
+        e = float(rng.uniform(*eta))
+        w = min(float(rng.uniform(*width)), 0.7 * L)
+        k = int(rng.integers(solutes[0], solutes[1] + 1))
+        sol = [(float(rng.uniform(0, L)), float(rng.uniform(0, L)), float(rng.uniform(0, w)),
+                float(rng.uniform(*radius))) for _ in range(k)]
+        out.append(WallsSolutes(N=N, dx=dx, eta=e, width=w, solutes=sol, R=R, kT=kT))
+    return out

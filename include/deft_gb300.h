@@ -228,6 +228,48 @@ typedef struct {
 int deft_batch_solve(int device, int count, const deft_batch_problem *problems,
                      const deft_batch_params *params, deft_cg_status *status_out);
 
+/* ---- learned warm start ----
+ * A 3-D Fourier neural operator (no reference counterpart) that maps a
+ * problem's constraint mask and bulk packing fraction eta to an initial
+ * relative density y = n / nb, trained on converged solutions; CG from its
+ * output replaces CG from the bulk density.  channels in {4, 8, 16}; modes m
+ * keeps |kx|, |ky| < m (2m values each) and kz < m; N^3 grid.  Weights are
+ * FP32 masters with BF16 copies used by every pass (FP32 accumulation). */
+typedef struct deft_fno deft_fno;
+int deft_fno_create(int device, int N, int channels, int modes, int layers,
+                    unsigned long long seed, deft_fno **out);
+int deft_fno_destroy(deft_fno *f);
+size_t deft_fno_param_count(const deft_fno *f);
+/* FP32 master parameters (deft_fno_param_count floats, host). */
+int deft_fno_get_params(deft_fno *f, float *host);
+int deft_fno_set_params(deft_fno *f, const float *host);
+/* Forward pass on arrays of N^3 floats (host arrays, or device arrays when
+ * on_device != 0): mask (1 free, 0 wall), eta; y_out (may be NULL) gets the
+ * relative density.  With target != NULL, *loss = sum_mask (y - target)^2 /
+ * sum_mask; with grad != NULL as well, the parameter gradient of that loss
+ * is written to grad (a host array of deft_fno_param_count floats). */
+int deft_fno_eval(deft_fno *f, const float *mask, float eta, const float *target, int on_device,
+                  float *y_out, float *loss, float *grad);
+/* One Adam step (beta 0.9 / 0.999) on the gradient of the last deft_fno_eval. */
+int deft_fno_adam(deft_fno *f, float lr);
+/* Loss and gradient on one sample, then one Adam step with rate lr; arrays
+ * as in deft_fno_eval, *loss (may be NULL) gets the loss before the step. */
+int deft_fno_train_step(deft_fno *f, const float *mask, float eta, const float *target,
+                        int on_device, float lr, float *loss);
+/* Warm start on the device: n = nb max(y, floor_rel) on free points and 0
+ * where mask == 0 (eta is the network input, nb the bulk density that scales
+ * its output); mask_dev and n_out_dev are device arrays of N^3 doubles. */
+int deft_fno_warm_start(deft_fno *f, const double *mask_dev, double eta, double nb,
+                        double floor_rel, double *n_out_dev);
+/* Checked warm start for a solve with the functional fmt (same N^3 grid):
+ * writes the network's density to n_out_dev unless it is non-finite or its
+ * energy is above the bulk start's (nb on free points, 0 where mask == 0),
+ * in which case the bulk start.  *used_network (may be NULL) = 1 or 0 says
+ * which; *E_out (may be NULL) gets its energy. */
+int deft_fno_initial_density(deft_fno *f, deft_fmt *fmt, const double *mask_dev, double eta,
+                             double nb, double floor_rel, double *n_out_dev, int *used_network,
+                             double *E_out);
+
 #ifdef __cplusplus
 }
 #endif

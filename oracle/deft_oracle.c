@@ -502,7 +502,8 @@ int oracle_cg_quadratic(const oracle_params *p, const double *V, const double *m
 
 /* Derivative line search along d from x (slope s0 = g.d < 0): bracketing
  * secant on s(a) = grad(x + a d).d until |s| <= 0.1 |s0|.  On return x and
- * m->g hold the accepted point.  Returns the number of evaluations, or -1. */
+ * m->g hold the accepted point.  Returns the number of evaluations, or -1
+ * (x back at the start point) after 40 evaluations. */
 static int secant_linmin(mstate *m, const double *d, double E0, double s0, double *alpha) {
   double lo = 0, s_lo = s0, hi = -1, s_hi = 0;
   double plo = 0, s_plo = s0; /* previous lower point, for extrapolation */
@@ -552,6 +553,7 @@ static int secant_linmin(mstate *m, const double *d, double E0, double s0, doubl
     if (an > hi - 0.01 * w) an = hi - 0.01 * w;
     a = an;
   }
+  m_axpy(m, -at, d); /* back to the start point */
   return -1;
 }
 
@@ -588,7 +590,15 @@ int oracle_cg_solve(const oracle_params *p, const double *V, const double *mask,
     if (it > 0 && s0 != 0) alpha *= s_prev / s0;
     s_prev = s0;
     const double E0 = m.e;
-    const int ne = secant_linmin(&m, d, E0, s0, &alpha);
+    int ne = secant_linmin(&m, d, E0, s0, &alpha);
+    if (ne < 0 && beta != 0) {
+      /* retry once along steepest descent from the same point */
+      evals += 40;
+      for (size_t i = 0; i < m.n; i++) d[i] = -gold[i];
+      s0 = -goldsqr;
+      s_prev = s0;
+      ne = secant_linmin(&m, d, E0, s0, &alpha);
+    }
     if (ne < 0) {
       evals += 40;
       break;
