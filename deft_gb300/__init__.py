@@ -12,9 +12,12 @@ from .api import (  # noqa: F401
     HardSpheresWBnotensor,
     IdealGas,
     Lattice,
+    EffectivePotentialToDensity,
     MaxIter,
     Minimizer,
+    OfEffectivePotential,
     Precision,
+    PreconditionedConjugateGradient,
     QuadraticLineMinimizer,
     SecantLineMinimizer,
     constrain,

@@ -11,7 +11,7 @@ LIB_PATH = os.path.join(HERE, "libdeft_gb300.so")
 
 OK = 0
 ERR_ARG, ERR_CUDA, ERR_NAN, ERR_LINESEARCH, ERR_MAXITER, ERR_NOMEM = 1, 2, 3, 4, 5, 6
-TERM_HS, TERM_IDEAL, TERM_MU, TERM_VEXT, TERM_MASK = 1, 2, 4, 8, 16
+TERM_HS, TERM_IDEAL, TERM_MU, TERM_VEXT, TERM_MASK, TERM_VEFF = 1, 2, 4, 8, 16, 32
 NTERMS = 6
 LS_SECANT, LS_QUADRATIC_REF = 0, 1
 
@@ -23,7 +23,8 @@ EXPORTS = (
     "deft_grid_fft", "deft_grid_ifft",
     "deft_grid_profile", "deft_grid_profile_count", "deft_grid_profile_entry",
     "deft_fmt_create", "deft_fmt_destroy", "deft_fmt_set_params", "deft_fmt_set_vext",
-    "deft_fmt_set_mask", "deft_fmt_energy", "deft_fmt_energy_grad", "deft_fmt_weighted",
+    "deft_fmt_set_mask", "deft_fmt_energy", "deft_fmt_energy_grad", "deft_fmt_energy_grad_pgrad",
+    "deft_fmt_weighted",
     "deft_fmt_hessian_vector",
     "deft_find_chemical_potential",
     "deft_fmt_energy_grad_noalloc", "deft_noalloc_scratch_bytes",
@@ -52,7 +53,7 @@ class FmtParams(ctypes.Structure):
 class CgParams(ctypes.Structure):
     _fields_ = [("linesearch", ctypes.c_int), ("gtol", ctypes.c_double), ("maxiter", ctypes.c_int),
                 ("step", ctypes.c_double), ("precision", ctypes.c_double),
-                ("refine_rel", ctypes.c_double)]
+                ("refine_rel", ctypes.c_double), ("preconditioned", ctypes.c_int)]
 
 
 class CgStatus(ctypes.Structure):
@@ -111,6 +112,7 @@ def load():
         "deft_fmt_set_mask": (ctypes.c_int, [_vp, _dp, ctypes.c_int]),
         "deft_fmt_energy": (ctypes.c_int, [_vp, _dp, ctypes.c_int, _dp, _dp]),
         "deft_fmt_energy_grad": (ctypes.c_int, [_vp, _dp, ctypes.c_int, _dp, _dp, _dp]),
+        "deft_fmt_energy_grad_pgrad": (ctypes.c_int, [_vp, _dp, ctypes.c_int, _dp, _dp, _dp, _dp]),
         "deft_fmt_weighted": (ctypes.c_int, [_vp, _dp, ctypes.c_int, _dp]),
         "deft_fmt_hessian_vector": (ctypes.c_int, [_vp, _dp, _dp, ctypes.c_int, _dp]),
         "deft_find_chemical_potential": (ctypes.c_int, [ctypes.c_double, ctypes.c_double,

@@ -11,6 +11,10 @@ Names, argument meaning and return conventions follow the reference:
   src/IdealGas.cpp, src/ChemicalPotential.cpp, src/ExternalPotential.cpp,
   src/Functional.cpp:834-838, src/Functional.h:88-103)
 * ``f.integral(kT, grid)``, ``f.integralgrad(kT, gd, x, g)``  src/Functional.h:125-149
+* ``OfEffectivePotential(f)``, ``EffectivePotentialToDensity()``
+  src/EffectivePotentialToDensity.cpp:20-91
+* ``PreconditionedConjugateGradient(f, gd, kT, x, lm, step)``
+  src/ConjugateGradient.cpp:115-174
 * ``ConjugateGradient(f, gd, kT, x, QuadraticLineMinimizer, step)``,
   ``Precision(eps, m)``, ``MaxIter(n, m)``, ``m.improve_energy()``,
   ``m.energy()``, ``m.grad()``  src/LineMinimizer.h:18-19, src/Minimizer.h:13-60
@@ -196,12 +200,13 @@ class Grid(np.ndarray):
 class Functional:
     """A sum of the recognised terms, optionally wrapped in constrain(mask, .)."""
 
-    def __init__(self, R=None, ideal=False, mu=None, V=None, mask=None, names=()):
+    def __init__(self, R=None, ideal=False, mu=None, V=None, mask=None, names=(), veff=False):
         self.R = R
         self.ideal = ideal
         self.mu = mu
         self.V = V
         self.mask = mask
+        self.veff = veff  # OfEffectivePotential: the variable is Veff, n = exp(-Veff/kT)
         self.names = tuple(names)
         self._fmt = {}
         self.last_energy = {}
@@ -209,6 +214,8 @@ class Functional:
     def __add__(self, o):
         if self.mask is not None or o.mask is not None:
             raise NotImplementedError("add terms before constrain()")
+        if self.veff or o.veff:
+            raise NotImplementedError("add terms inside OfEffectivePotential()")
         def pick(a, b, what):
             if a is not None and b is not None and a is not b:
                 raise NotImplementedError(f"two {what} terms")
@@ -230,6 +237,8 @@ class Functional:
             t |= _lib.TERM_VEXT
         if self.mask is not None:
             t |= _lib.TERM_MASK
+        if self.veff:
+            t |= _lib.TERM_VEFF
         return t
 
     def fmt(self, gd, kT):
@@ -285,13 +294,20 @@ class Functional:
         h = self.fmt(gd, kT)
         xs = _host_f64(x, gd.NxNyNz)
         out = np.empty(gd.NxNyNz)
+        pout = np.empty(gd.NxNyNz) if pg is not None else None
         E = ctypes.c_double()
-        check(_lib.load().deft_fmt_energy_grad(h, xs.ctypes.data, 0, ctypes.addressof(E),
-                                               out.ctypes.data, None))
+        check(_lib.load().deft_fmt_energy_grad_pgrad(
+            h, xs.ctypes.data, 0, ctypes.addressof(E), out.ctypes.data,
+            pout.ctypes.data if pout is not None else None, None))
         g += out.reshape(g.shape)
         if pg is not None:
-            pg += out.reshape(pg.shape)
+            pg += pout.reshape(pg.shape)
         return E.value
+
+    def integralpgrad(self, kT, gd, x, pg):
+        """Accumulates the preconditioned gradient (src/Functional.h:150-155)."""
+        g = np.zeros(gd.NxNyNz)
+        return self.integralgrad(kT, gd, x, g, pg)
 
     def weighted(self, gd, x):
         h = self.fmt(gd, 1.0)
@@ -323,9 +339,25 @@ def ExternalPotential(V):
 
 
 def constrain(mask, f):
-    c = Functional(R=f.R, ideal=f.ideal, mu=f.mu, V=f.V, names=f.names)
+    c = Functional(R=f.R, ideal=f.ideal, mu=f.mu, V=f.V, names=f.names, veff=f.veff)
     c.mask = np.asarray(mask, dtype=np.float64)
     return c
+
+
+def OfEffectivePotential(f):
+    """f of n = exp(-Veff/kT), as a functional of Veff
+    (src/EffectivePotentialToDensity.cpp:28-91)."""
+    if f.mask is not None:
+        raise NotImplementedError("constrain() outside OfEffectivePotential(), as the drivers do")
+    return Functional(R=f.R, ideal=f.ideal, mu=f.mu, V=f.V, names=f.names, veff=True)
+
+
+def EffectivePotentialToDensity():
+    """The map Veff -> n = exp(-Veff/kT) (src/EffectivePotentialToDensity.cpp:20-23),
+    as a callable (kT, gd, Veff) -> n."""
+    def to_density(kT, gd, V):
+        return np.exp(-np.asarray(V, dtype=np.float64) / kT)
+    return to_density
 
 
 def find_chemical_potential(f, kT, n):
@@ -344,9 +376,10 @@ class Minimizer:
     """ConjugateGradient(...) wrapped in optional Precision / MaxIter."""
 
     def __init__(self, f, gd, kT, x, linmin=QuadraticLineMinimizer, step=0.1, precision=0.0,
-                 maxiter=0, gtol=0.0):
+                 maxiter=0, gtol=0.0, preconditioned=False):
         self.f, self.gd, self.kT, self.x = f, gd, kT, x
         self.linmin, self.step = linmin, step
+        self.preconditioned = preconditioned
         self.precision, self.maxiter, self.gtol = precision, maxiter, gtol
         self.handle = None
         self.status = _lib.CgStatus()
@@ -356,7 +389,8 @@ class Minimizer:
             return
         L = _lib.load()
         p = _lib.CgParams(_lib.LS_SECANT if self.linmin == SecantLineMinimizer else
-                          _lib.LS_QUADRATIC_REF, self.gtol, self.maxiter, self.step, self.precision)
+                          _lib.LS_QUADRATIC_REF, self.gtol, self.maxiter, self.step, self.precision,
+                          0.0, int(bool(self.preconditioned)))
         h = ctypes.c_void_p()
         check(L.deft_cg_create(self.f.fmt(self.gd, self.kT), ctypes.byref(p), ctypes.byref(h)))
         self.handle = h
@@ -404,6 +438,11 @@ class Minimizer:
 
 def ConjugateGradient(f, gd, kT, x, lm=QuadraticLineMinimizer, stepsize=0.1):
     return Minimizer(f, gd, kT, x, linmin=lm, step=stepsize)
+
+
+def PreconditionedConjugateGradient(f, gd, kT, x, lm=QuadraticLineMinimizer, stepsize=0.1):
+    """src/ConjugateGradient.cpp:115-160,171-174."""
+    return Minimizer(f, gd, kT, x, linmin=lm, step=stepsize, preconditioned=True)
 
 
 def Precision(eps, m):

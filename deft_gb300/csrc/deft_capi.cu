@@ -34,12 +34,15 @@ struct deft_fmt {
   double *mask;
   double *g_buf;
   double *w_buf;  // 5*NR, allocated on first deft_fmt_weighted
+  double *n_veff = nullptr, *gn_veff = nullptr;  // NR each, DEFT_TERM_VEFF only
 };
 
 struct deft_cg {
   deft_fmt *f;
   deft_cg_params p;
   double *x, *g, *d, *gold;
+  double *pg = nullptr;  // preconditioned gradient (preconditioned CG only)
+  double pgoldsqr = 0;   // pg.g at the previous point (preconditioned secant CG)
   // shared state
   int iter = 0, evals = 0;
   // secant CG state
@@ -344,6 +347,8 @@ int deft_fmt_destroy(deft_fmt *f) {
   cudaFree(f->mask);
   cudaFree(f->g_buf);
   cudaFree(f->w_buf);
+  cudaFree(f->n_veff);
+  cudaFree(f->gn_veff);
   delete f;
   return DEFT_OK;
 }
@@ -375,6 +380,54 @@ static int check_terms(const deft_fmt *f) {
   return DEFT_OK;
 }
 
+namespace {
+
+int veff_buffers(deft_fmt *f) {
+  if (f->n_veff) return DEFT_OK;
+  const size_t bytes = sizeof(double) * nr(f->grid);
+  cudaError_t e = cudaMalloc((void **)&f->n_veff, bytes);
+  if (e == cudaSuccess) e = cudaMalloc((void **)&f->gn_veff, bytes);
+  if (e != cudaSuccess) {
+    cudaFree(f->n_veff);
+    f->n_veff = nullptr;
+    f->gn_veff = nullptr;
+    return cuda_err(e, "cudaMalloc");
+  }
+  return DEFT_OK;
+}
+
+// The density the functional sees for the variable x (device): x itself, or
+// n = exp(-x/kT) under DEFT_TERM_VEFF (into the functional's buffer).
+int fmt_density(deft_fmt *f, const deft::FmtSpec &spec, const double *x, const double **n) {
+  *n = x;
+  if (!(f->p.terms & DEFT_TERM_VEFF)) return DEFT_OK;
+  if (int s = veff_buffers(f)) return s;
+  Engine *e = f->grid->eng;
+  if (e->veff_density(spec.kT, x, f->n_veff)) return eng_err(e);
+  *n = f->n_veff;
+  return DEFT_OK;
+}
+
+// Energy (grad == NULL) or energy, gradient and, if pgrad != NULL, the
+// preconditioned gradient at the variable x (device arrays).
+int fmt_eval(deft_fmt *f, const deft::FmtSpec &spec, const double *x, double *grad,
+             double *pgrad, double *E, double *terms) {
+  Engine *e = f->grid->eng;
+  const double *n;
+  if (int s = fmt_density(f, spec, x, &n)) return s;
+  if (!grad) return e->energy(spec, n, f->V, f->mask, E, terms) ? eng_err(e) : DEFT_OK;
+  if (f->p.terms & DEFT_TERM_VEFF) {
+    if (e->energy_grad(spec, n, f->V, f->mask, f->gn_veff, E, terms)) return eng_err(e);
+    if (e->veff_grad(spec.kT, x, n, f->gn_veff, grad, pgrad)) return eng_err(e);
+  } else {
+    if (e->energy_grad(spec, n, f->V, f->mask, grad, E, terms)) return eng_err(e);
+    if (pgrad && e->copy(grad, pgrad)) return eng_err(e);
+  }
+  return DEFT_OK;
+}
+
+}  // namespace
+
 int deft_fmt_energy(deft_fmt *f, const double *n, int on_device, double *E, double *terms) {
   if (!f || !n || !E) return set_err(DEFT_ERR_ARG, "NULL argument");
   if (int s = check_terms(f)) return s;
@@ -382,13 +435,13 @@ int deft_fmt_energy(deft_fmt *f, const double *n, int on_device, double *E, doub
   cudaSetDevice(g->ctx->device);
   const double *src;
   if (int s = stage_in(g, n, on_device, g->in_buf, &src)) return s;
-  if (g->eng->energy(spec_of(f), src, f->V, f->mask, E, terms)) return eng_err(g->eng);
+  if (int s = fmt_eval(f, spec_of(f), src, nullptr, nullptr, E, terms)) return s;
   if (!std::isfinite(*E)) return set_err(DEFT_ERR_NAN, "energy is not finite");
   return DEFT_OK;
 }
 
-int deft_fmt_energy_grad(deft_fmt *f, const double *n, int on_device, double *E, double *grad,
-                         double *terms) {
+int deft_fmt_energy_grad_pgrad(deft_fmt *f, const double *n, int on_device, double *E,
+                               double *grad, double *pgrad, double *terms) {
   if (!f || !n || !E || !grad) return set_err(DEFT_ERR_ARG, "NULL argument");
   if (int s = check_terms(f)) return s;
   deft_grid *g = f->grid;
@@ -396,15 +449,31 @@ int deft_fmt_energy_grad(deft_fmt *f, const double *n, int on_device, double *E,
   const double *src;
   if (int s = stage_in(g, n, on_device, g->in_buf, &src)) return s;
   double *dst = on_device ? grad : f->g_buf;
-  if (g->eng->energy_grad(spec_of(f), src, f->V, f->mask, dst, E, terms)) return eng_err(g->eng);
+  double *pdst = pgrad;
+  if (pgrad && !on_device) {
+    if (!f->w_buf) {
+      cudaError_t e = cudaMalloc((void **)&f->w_buf, 5 * sizeof(double) * nr(g));
+      if (e != cudaSuccess) return cuda_err(e, "cudaMalloc");
+    }
+    pdst = f->w_buf;
+  }
+  if (int s = fmt_eval(f, spec_of(f), src, dst, pdst, E, terms)) return s;
   if (!on_device) {
     cudaError_t e = cudaMemcpyAsync(grad, dst, sizeof(double) * nr(g), cudaMemcpyDeviceToHost,
                                     g->ctx->stream);
+    if (e == cudaSuccess && pgrad)
+      e = cudaMemcpyAsync(pgrad, pdst, sizeof(double) * nr(g), cudaMemcpyDeviceToHost,
+                          g->ctx->stream);
     if (e != cudaSuccess) return cuda_err(e, "device-to-host copy");
-    if (int s = sync(g->ctx)) return s;
   }
+  if (int s = sync(g->ctx)) return s;
   if (!std::isfinite(*E)) return set_err(DEFT_ERR_NAN, "energy is not finite");
   return DEFT_OK;
+}
+
+int deft_fmt_energy_grad(deft_fmt *f, const double *n, int on_device, double *E, double *grad,
+                         double *terms) {
+  return deft_fmt_energy_grad_pgrad(f, n, on_device, E, grad, nullptr, terms);
 }
 
 int deft_fmt_weighted(deft_fmt *f, const double *n, int on_device, double *out5) {
@@ -421,7 +490,9 @@ int deft_fmt_weighted(deft_fmt *f, const double *n, int on_device, double *out5)
     }
     dst = f->w_buf;
   }
-  if (g->eng->weighted(spec_of(f), src, dst)) return eng_err(g->eng);
+  const double *dens;
+  if (int s = fmt_density(f, spec_of(f), src, &dens)) return s;
+  if (g->eng->weighted(spec_of(f), dens, dst)) return eng_err(g->eng);
   if (!on_device) {
     cudaError_t e = cudaMemcpyAsync(out5, dst, 5 * sizeof(double) * nr(g), cudaMemcpyDeviceToHost,
                                     g->ctx->stream);
@@ -434,6 +505,8 @@ int deft_fmt_hessian_vector(deft_fmt *f, const double *n, const double *dx, int 
                             double *out) {
   if (!f || !n || !dx || !out) return set_err(DEFT_ERR_ARG, "NULL argument");
   if (int s = check_terms(f)) return s;
+  if (f->p.terms & DEFT_TERM_VEFF)
+    return set_err(DEFT_ERR_ARG, "Hessian-vector products are in the density variable only");
   deft_grid *g = f->grid;
   cudaSetDevice(g->ctx->device);
   const double *ns, *ds;
@@ -542,6 +615,7 @@ int deft_cg_create(deft_fmt *f, const deft_cg_params *p, deft_cg **out) {
   if (e == cudaSuccess) e = cudaMalloc((void **)&c->g, bytes);
   if (e == cudaSuccess) e = cudaMalloc((void **)&c->d, bytes);
   if (e == cudaSuccess) e = cudaMalloc((void **)&c->gold, bytes);
+  if (e == cudaSuccess && p->preconditioned) e = cudaMalloc((void **)&c->pg, bytes);
   if (e == cudaSuccess) e = cudaMemsetAsync(c->d, 0, bytes, f->grid->ctx->stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(c->gold, 0, bytes, f->grid->ctx->stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(c->x, 0, bytes, f->grid->ctx->stream);
@@ -561,6 +635,7 @@ int deft_cg_destroy(deft_cg *c) {
   cudaFree(c->g);
   cudaFree(c->d);
   cudaFree(c->gold);
+  cudaFree(c->pg);
   cudaFree(c->q);
   cudaFree(c->dxv);
   delete c;
@@ -573,6 +648,7 @@ static void cg_reset(deft_cg *c) {
   c->have_g = false;
   c->e_valid = false;
   c->goldsqr = 0;
+  c->pgoldsqr = 0;
   c->oldgradsqr = 0;
   c->s_prev = 0;
   c->alpha = c->p.step;
@@ -623,8 +699,7 @@ Engine *eng_of(deft_cg *c) { return c->f->grid->eng; }
 // Energy + gradient at x into c->g, c->E.
 int cg_eval(deft_cg *c, const deft::FmtSpec &spec) {
   double E;
-  if (eng_of(c)->energy_grad(spec, c->x, c->f->V, c->f->mask, c->g, &E, nullptr))
-    return eng_err(eng_of(c));
+  if (int s = fmt_eval(c->f, spec, c->x, c->g, c->pg, &E, nullptr)) return s;
   c->evals++;
   if (spec.precision == deft::kPrecisionFP64) c->evals_fp64++;
   c->last_eval_mixed = spec.precision != deft::kPrecisionFP64;
@@ -639,8 +714,7 @@ int cg_eval(deft_cg *c, const deft::FmtSpec &spec) {
 int cg_energy(deft_cg *c, double *E) {
   if (!c->e_valid) {
     const deft::FmtSpec spec = spec_of(c->f);
-    if (eng_of(c)->energy(spec, c->x, c->f->V, c->f->mask, &c->e_cache, nullptr))
-      return eng_err(eng_of(c));
+    if (int s = fmt_eval(c->f, spec, c->x, nullptr, nullptr, &c->e_cache, nullptr)) return s;
     c->evals++;
     if (spec.precision == deft::kPrecisionFP64) c->evals_fp64++;
     c->e_valid = true;
@@ -741,24 +815,46 @@ int step_secant(deft_cg *c, deft_cg_status *st, const deft::FmtSpec &spec, doubl
     c->done = true;
     return DEFT_OK;
   }
-  // Polak-Ribiere with reset (src/ConjugateGradient.cpp:77-91)
-  double beta = 0;
-  if (c->goldsqr > 0) {
-    beta = (c->gg - c->ggold) / c->goldsqr;
-    if (beta < 0 || beta != beta) beta = 0;
-  }
   Engine *e = eng_of(c);
-  if (e->scal_add(beta, c->d, -1.0, c->g)) return eng_err(e);
+  double beta = 0, pgg = 0;
+  if (c->pg) {
+    // Preconditioned Polak-Ribiere (src/ConjugateGradient.cpp:115-160):
+    // beta = pg.(g - g_old) / (pg_old.g_old), d = -pg + beta d
+    const double *a[2] = {c->pg, c->pg};
+    const double *b[2] = {c->g, c->gold};
+    double o[2];
+    if (e->dots(2, a, b, o)) return eng_err(e);
+    pgg = o[0];
+    if (c->pgoldsqr != 0) {
+      beta = (o[0] - o[1]) / c->pgoldsqr;
+      if (beta < 0 || beta != beta) beta = 0;
+    }
+    if (e->scal_add(beta, c->d, -1.0, c->pg)) return eng_err(e);
+  } else {
+    // Polak-Ribiere with reset (src/ConjugateGradient.cpp:77-91)
+    if (c->goldsqr > 0) {
+      beta = (c->gg - c->ggold) / c->goldsqr;
+      if (beta < 0 || beta != beta) beta = 0;
+    }
+    if (e->scal_add(beta, c->d, -1.0, c->g)) return eng_err(e);
+  }
   double s0;
   {
     const double *a[1] = {c->g};
     const double *b[1] = {c->d};
     if (e->dots(1, a, b, &s0)) return eng_err(e);
   }
+  if (!(s0 < 0) && c->pg && beta != 0) {
+    // not downhill: the preconditioned steepest direction
+    if (e->scal_add(0.0, c->d, -1.0, c->pg)) return eng_err(e);
+    beta = 0;
+    s0 = -pgg;
+  }
   if (!(s0 < 0)) {
     if (e->scal_add(0.0, c->d, -1.0, c->g)) return eng_err(e);
     s0 = -c->gg;
   }
+  c->pgoldsqr = pgg;
   if (e->copy(c->g, c->gold)) return eng_err(e);
   c->goldsqr = c->gg;
   if (c->iter > 0 && s0 != 0) c->alpha *= c->s_prev / s0;
@@ -971,6 +1067,45 @@ int step_quadratic(deft_cg *c, bool *more) {
   return DEFT_OK;
 }
 
+// PreconditionedConjugateGradientType::improve_energy
+// (src/ConjugateGradient.cpp:115-160) with QuadraticLineMinimizer.
+int step_pquadratic(deft_cg *c, bool *more) {
+  c->iter++;
+  if (!c->have_g)
+    if (int s = cg_eval(c, spec_of(c->f))) return s;
+  const double E0 = c->E;
+  if (E0 != E0) {
+    *more = false;
+    return DEFT_OK;
+  }
+  Engine *e = eng_of(c);
+  // with G = grad and oldgrad (in gold) = -G of the previous point:
+  // beta = -pg.(-G - oldgrad)/oldgradsqr = (pg.G + pg.oldgrad)/oldgradsqr
+  double o[3];
+  {
+    const double *a[3] = {c->pg, c->pg, c->g};
+    const double *b[3] = {c->g, c->gold, c->g};
+    if (e->dots(3, a, b, o)) return eng_err(e);
+  }
+  c->gg = o[2];
+  double beta = (o[0] + o[1]) / c->oldgradsqr;
+  if (e->scal_add(0.0, c->gold, -1.0, c->g)) return eng_err(e);  // oldgrad = -grad
+  if (beta < 0 || beta != beta || c->oldgradsqr == 0) beta = 0;
+  c->oldgradsqr = o[0];                                          // -pgrad.oldgrad
+  if (e->scal_add(beta, c->d, -1.0, c->pg)) return eng_err(e);   // direction
+  double gdotd;
+  {
+    const double *a[1] = {c->gold};
+    const double *b[1] = {c->d};
+    if (e->dots(1, a, b, &gdotd)) return eng_err(e);
+  }
+  if (int s = quad_linmin(c, -gdotd, &c->step)) return s;
+  double E;
+  if (int s = cg_energy(c, &E)) return s;
+  *more = E < E0 || beta != 0;
+  return DEFT_OK;
+}
+
 }  // namespace
 
 int deft_cg_step(deft_cg *c, deft_cg_status *st) {
@@ -1000,7 +1135,16 @@ int deft_cg_step(deft_cg *c, deft_cg_status *st) {
           if (!status && (c->done || st->gnorm < thr || c->iter > 0 && !c->have_g)) {
             c->stage = 1;
             c->done = false;
+            if (c->f->p.terms & DEFT_TERM_VEFF) {
+              // refinement by FP64 CG (the Newton step works in the density
+              // variable): restart the conjugate directions
+              c->have_g = false;
+              c->goldsqr = 0;
+              c->pgoldsqr = 0;
+            }
           }
+        } else if (c->f->p.terms & DEFT_TERM_VEFF) {
+          status = step_secant(c, st, fp64_of(spec), c->p.gtol);
         } else {
           status = step_newton(c, st, spec);
         }
@@ -1009,7 +1153,7 @@ int deft_cg_step(deft_cg *c, deft_cg_status *st) {
         status = step_secant(c, st, spec, c->p.gtol);
         more = !c->done;
       } else {
-        status = step_quadratic(c, &more);
+        status = c->pg ? step_pquadratic(c, &more) : step_quadratic(c, &more);
       }
     }
     if (!status && prec) {

@@ -831,6 +831,27 @@ __global__ void k_scal_add(double beta, double *d, double alpha, const double *g
   if (blockIdx.x == 0 && threadIdx.x == 0 && (n & 1)) d[n - 1] = alpha * g[n - 1] + beta * d[n - 1];
 }
 
+// Effective-potential parametrisation (OfEffectivePotential,
+// src/EffectivePotentialToDensity.cpp:28-91): n = exp(-Veff / kT).
+__global__ void k_veff_density(double inv_kT, const double *__restrict__ x, double *__restrict__ n,
+                               int N) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x)
+    n[i] = exp(-x[i] * inv_kT);
+}
+
+// From the density gradient gn (already masked): grad = gn * n / (-kT), and
+// the reference's preconditioned gradient pgrad = gn / (Veff - kT)
+// (src/EffectivePotentialToDensity.cpp:62-79).
+__global__ void k_veff_grad(double kT, const double *__restrict__ x, const double *__restrict__ n,
+                            const double *gn, double *grad, double *__restrict__ pgrad, int N) {
+  const double m_inv_kT = -1.0 / kT;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+    const double g = gn[i];
+    grad[i] = n[i] * g * m_inv_kT;
+    if (pgrad) pgrad[i] = g / (x[i] - kT);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Host side
 
@@ -941,12 +962,12 @@ constexpr size_t kBudget32 = 72 * 1024;
 enum KernelId {
   kK_z_r2c, kK_z_c2r, kK_y_fft1, kK_y_fft5, kK_x_fft, kK_x_conv_fwd, kK_x_conv_adj, kK_z_phi_grad,
   kK_z_phi_energy, kK_z_grad, kK_local_energy, kK_reduce_terms, kK_dots, kK_axpy, kK_scal_add,
-  kK_weight_table, kK_z_hess, kK_z_jac, kK_z_hvp_out, kNumKernels
+  kK_weight_table, kK_z_hess, kK_z_jac, kK_z_hvp_out, kK_veff_density, kK_veff_grad, kNumKernels
 };
 const char *const kKernelNames[kNumKernels] = {
     "z_r2c", "z_c2r", "y_fft_1field", "y_fft_5fields", "x_fft", "x_conv_fwd", "x_conv_adj", "z_phi_grad",
     "z_phi_energy", "z_grad", "local_energy", "reduce_terms", "dots", "axpy", "scal_add",
-    "weight_table", "z_hess", "z_jac", "z_hvp_out"};
+    "weight_table", "z_hess", "z_jac", "z_hvp_out", "veff_density", "veff_grad"};
 
 class EngineImpl {
  public:
@@ -1483,6 +1504,23 @@ int Engine::scal_add(double beta, double *d, double alpha, const double *gv) {
     k_scal_add<<<e.dot_blocks, kThreads, 0, e.stream>>>(beta, d, alpha, gv, e.g.NR);
     e.post(kK_scal_add);
   return e.check("scal_add");
+}
+
+int Engine::veff_density(double kT, const double *x, double *n) {
+  EngineImpl &e = *impl_;
+  e.pre(kK_veff_density);
+  k_veff_density<<<e.dot_blocks, kThreads, 0, e.stream>>>(1.0 / kT, x, n, e.g.NR);
+  e.post(kK_veff_density);
+  return e.check("veff_density");
+}
+
+int Engine::veff_grad(double kT, const double *x, const double *n, const double *gn, double *grad,
+                      double *pgrad) {
+  EngineImpl &e = *impl_;
+  e.pre(kK_veff_grad);
+  k_veff_grad<<<e.dot_blocks, kThreads, 0, e.stream>>>(kT, x, n, gn, grad, pgrad, e.g.NR);
+  e.post(kK_veff_grad);
+  return e.check("veff_grad");
 }
 
 int Engine::copy(const double *src, double *dst) {

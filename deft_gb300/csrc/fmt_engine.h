@@ -19,6 +19,7 @@ enum TermFlags {
   kTermMu = 4,
   kTermVext = 8,
   kTermMask = 16,
+  kTermVeff = 32,  // the variable is Veff, n = exp(-Veff / kT) (handled by the C ABI)
 };
 
 constexpr int kNumTerms = 6;  // phi3, phi1, phi2, ideal, mu, vext
@@ -99,6 +100,13 @@ class Engine {
   int axpy(double alpha, const double *x, double *y);               // y += alpha x
   int scal_add(double beta, double *d, double alpha, const double *g);  // d = alpha g + beta d
   int copy(const double *src, double *dst);
+
+  // Effective-potential variable (OfEffectivePotential): n = exp(-x / kT);
+  // grad = gn n / (-kT) and, if pgrad != null, pgrad = gn / (x - kT), from
+  // the (masked) density gradient gn.  grad may alias gn.
+  int veff_density(double kT, const double *x, double *n);
+  int veff_grad(double kT, const double *x, const double *n, const double *gn, double *grad,
+                double *pgrad);
 
   // Kernel accounting: every launch is counted per kernel kind; with timing
   // on, each launch is also bracketed by CUDA events on the engine's stream.

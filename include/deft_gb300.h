@@ -39,6 +39,12 @@ extern "C" {
 #define DEFT_TERM_MU 4     /* ChemicalPotential(mu), src/ChemicalPotential.cpp:19-22 */
 #define DEFT_TERM_VEXT 8   /* ExternalPotential(V), src/ExternalPotential.cpp:19-21 */
 #define DEFT_TERM_MASK 16  /* constrain(mask, f), src/Functional.cpp:834-838 */
+/* OfEffectivePotential(f) (src/EffectivePotentialToDensity.cpp:28-91): the
+ * variable x is the effective potential Veff and n = exp(-Veff/kT); energies
+ * are those of n, the gradient is dE/dVeff = (dE/dn) n / (-kT) (masked), and
+ * the preconditioned gradient is (dE/dn) / (Veff - kT).  Not combined with
+ * deft_fmt_hessian_vector. */
+#define DEFT_TERM_VEFF 32
 
 /* Number of per-term energies: phi3, phi1, phi2 (src/HardSpheres.cpp:156),
  * ideal gas, chemical potential, external potential. */
@@ -75,6 +81,8 @@ typedef struct {
   double refine_rel; /* mixed evaluator only: leave the FP32 CG stage for the FP64-residual
                         Newton refinement once |grad| < refine_rel * |grad at start|
                         (0 = default 1e-4) */
+  int preconditioned; /* 1: PreconditionedConjugateGradient (src/ConjugateGradient.cpp:
+                         115-160): directions from the preconditioned gradient */
 } deft_cg_params;
 
 typedef struct {
@@ -149,6 +157,11 @@ int deft_fmt_energy(deft_fmt *f, const double *n, int on_device, double *E_out,
  * accumulates into caller-zeroed buffers. */
 int deft_fmt_energy_grad(deft_fmt *f, const double *n, int on_device, double *E_out,
                          double *grad_out, double *terms_out);
+/* Energy, integralgrad and integralpgrad (src/Functional.h:147-155) in one
+ * evaluation: pgrad_out gets the preconditioned gradient, equal to grad_out
+ * unless DEFT_TERM_VEFF is set.  Both outputs are overwritten. */
+int deft_fmt_energy_grad_pgrad(deft_fmt *f, const double *x, int on_device, double *E_out,
+                               double *grad_out, double *pgrad_out, double *terms_out);
 /* The weighted densities n3, n2, n2x, n2y, n2z (5 fields, out5), i.e.
  * StepConvolve/ShellConvolve/x,y,zShellConvolve(R) (src/Gaussian.cpp:82-102). */
 int deft_fmt_weighted(deft_fmt *f, const double *n, int on_device, double *out5);

@@ -321,14 +321,48 @@ static double eval(const oracle_params *p, const double *n, const double *V, con
   return E;
 }
 
+/* The functional at the variable x: the density, or with ORACLE_VEFF the
+ * effective potential (OfEffectivePotential,
+ * src/EffectivePotentialToDensity.cpp:28-91): n = exp(-x/kT), gradient
+ * g_n n/(-kT) and preconditioned gradient g_n/(x - kT), g_n the masked
+ * density gradient (the mask of constrain() applies after the chain rule,
+ * which is the same pointwise product). */
+static double eval_x(const oracle_params *p, const double *x, const double *V, const double *mask,
+                     double *grad, double *pgrad, double *terms6) {
+  const size_t nr = (size_t)p->Nx * p->Ny * p->Nz;
+  if (!(p->terms & ORACLE_VEFF)) {
+    const double E = eval(p, x, V, mask, grad, terms6);
+    if (grad && pgrad) memcpy(pgrad, grad, sizeof(double) * nr);
+    return E;
+  }
+  double *n = (double *)malloc(sizeof(double) * nr);
+  for (size_t i = 0; i < nr; i++) n[i] = exp(-x[i] / p->kT);
+  const double E = eval(p, n, V, mask, grad, terms6);
+  if (grad) {
+    for (size_t i = 0; i < nr; i++) {
+      const double g = grad[i];
+      grad[i] = n[i] * g / (-p->kT);
+      if (pgrad) pgrad[i] = g / (x[i] - p->kT);
+    }
+  }
+  free(n);
+  return E;
+}
+
 double oracle_energy(const oracle_params *p, const double *n, const double *V, const double *mask,
                      double *terms6) {
-  return eval(p, n, V, mask, NULL, terms6);
+  return eval_x(p, n, V, mask, NULL, NULL, terms6);
 }
 
 double oracle_energy_grad(const oracle_params *p, const double *n, const double *V,
                           const double *mask, double *grad, double *terms6) {
-  return eval(p, n, V, mask, grad, terms6);
+  return eval_x(p, n, V, mask, grad, NULL, terms6);
+}
+
+double oracle_energy_grad_pgrad(const oracle_params *p, const double *x, const double *V,
+                                const double *mask, double *grad, double *pgrad,
+                                double *terms6) {
+  return eval_x(p, x, V, mask, grad, pgrad, terms6);
 }
 
 double oracle_homogeneous(double R, double kT, double mu, double nb) {
@@ -367,18 +401,19 @@ typedef struct {
   double e;
   double *g;
   int g_valid;
+  double *pg; /* preconditioned gradient (preconditioned CG only) */
 } mstate;
 
 static double m_energy(mstate *m) {
   if (!m->e_valid) {
-    m->e = oracle_energy(m->p, m->x, m->V, m->mask, NULL);
+    m->e = eval_x(m->p, m->x, m->V, m->mask, NULL, NULL, NULL);
     m->e_valid = 1;
   }
   return m->e;
 }
 static const double *m_grad(mstate *m) {
   if (!m->g_valid) {
-    m->e = oracle_energy_grad(m->p, m->x, m->V, m->mask, m->g, NULL);
+    m->e = eval_x(m->p, m->x, m->V, m->mask, m->g, m->pg, NULL);
     m->e_valid = 1;
     m->g_valid = 1;
   }
@@ -456,7 +491,7 @@ static void quad_linmin(mstate *m, const double *dir, double slope, double *step
 
 int oracle_cg_quadratic(const oracle_params *p, const double *V, const double *mask,
                         double *n_inout, int iters, double step, double *energies) {
-  mstate m = {p, V, mask, n_inout, (size_t)p->Nx * p->Ny * p->Nz, 0, 0, NULL, 0};
+  mstate m = {p, V, mask, n_inout, (size_t)p->Nx * p->Ny * p->Nz, 0, 0, NULL, 0, NULL};
   m.g = (double *)malloc(sizeof(double) * m.n);
   double *direction = (double *)calloc(m.n, sizeof(double));
   double *oldgrad = (double *)calloc(m.n, sizeof(double));
@@ -497,6 +532,51 @@ int oracle_cg_quadratic(const oracle_params *p, const double *V, const double *m
   free(direction);
   free(oldgrad);
   free(g);
+  return it;
+}
+
+/* PreconditionedConjugateGradientType::improve_energy
+ * (src/ConjugateGradient.cpp:115-160) with the restated
+ * QuadraticLineMinimizer; energies[i] after call i. */
+int oracle_pcg_quadratic(const oracle_params *p, const double *V, const double *mask,
+                         double *x_inout, int iters, double step, double *energies) {
+  mstate m = {p, V, mask, x_inout, (size_t)p->Nx * p->Ny * p->Nz, 0, 0, NULL, 0, NULL};
+  m.g = (double *)malloc(sizeof(double) * m.n);
+  m.pg = (double *)malloc(sizeof(double) * m.n);
+  double *direction = (double *)calloc(m.n, sizeof(double));
+  double *oldgrad = (double *)calloc(m.n, sizeof(double));
+  double oldgradsqr = 0;
+  int it = 0;
+  for (; it < iters; it++) {
+    const double E0 = m_energy(&m);
+    int more;
+    if (E0 != E0) {
+      more = 0;
+    } else {
+      const double *gr = m_grad(&m);
+      const double *pg = m.pg;
+      /* beta = -pgrad.(-grad - oldgrad)/oldgradsqr; oldgrad = -grad */
+      double num = 0;
+      for (size_t i = 0; i < m.n; i++) num += -pg[i] * (-gr[i] - oldgrad[i]);
+      double beta = num / oldgradsqr;
+      for (size_t i = 0; i < m.n; i++) oldgrad[i] = -gr[i];
+      if (beta < 0 || beta != beta || oldgradsqr == 0) beta = 0;
+      oldgradsqr = -dot(pg, oldgrad, m.n);
+      for (size_t i = 0; i < m.n; i++) direction[i] = -pg[i] + beta * direction[i];
+      const double gdotd = dot(oldgrad, direction, m.n);
+      quad_linmin(&m, direction, -gdotd, &step);
+      more = m_energy(&m) < E0 || beta != 0;
+    }
+    energies[it] = m_energy(&m);
+    if (!more) {
+      it++;
+      break;
+    }
+  }
+  free(m.g);
+  free(m.pg);
+  free(direction);
+  free(oldgrad);
   return it;
 }
 
@@ -559,8 +639,16 @@ static int secant_linmin(mstate *m, const double *d, double E0, double s0, doubl
 
 int oracle_cg_solve(const oracle_params *p, const double *V, const double *mask, double *n_inout,
                     double gtol, int maxiter, double step, double *out3) {
-  mstate m = {p, V, mask, n_inout, (size_t)p->Nx * p->Ny * p->Nz, 0, 0, NULL, 0};
+  return oracle_cg_solve_pc(p, V, mask, n_inout, gtol, maxiter, step, 0, out3);
+}
+
+int oracle_cg_solve_pc(const oracle_params *p, const double *V, const double *mask,
+                       double *n_inout, double gtol, int maxiter, double step, int precond,
+                       double *out3) {
+  mstate m = {p, V, mask, n_inout, (size_t)p->Nx * p->Ny * p->Nz, 0, 0, NULL, 0, NULL};
   m.g = (double *)malloc(sizeof(double) * m.n);
+  if (precond) m.pg = (double *)malloc(sizeof(double) * m.n);
+  double pgoldsqr = 0;
   double *d = (double *)calloc(m.n, sizeof(double));
   double *gold = (double *)calloc(m.n, sizeof(double));
   double goldsqr = 0, s_prev = 0, alpha = step;
@@ -571,20 +659,37 @@ int oracle_cg_solve(const oracle_params *p, const double *V, const double *mask,
     const double *g = m.g;
     const double gg = dot(g, g, m.n);
     if (sqrt(gg) < gtol) break;
-    /* Polak-Ribiere with reset, as src/ConjugateGradient.cpp:77-91 */
-    double beta = 0;
-    if (goldsqr > 0) {
-      double num = 0;
-      for (size_t i = 0; i < m.n; i++) num += g[i] * (g[i] - gold[i]);
-      beta = num / goldsqr;
-      if (beta < 0 || beta != beta) beta = 0;
+    double beta = 0, pgg = 0;
+    if (precond) {
+      /* preconditioned Polak-Ribiere (src/ConjugateGradient.cpp:115-160) */
+      const double *pg = m.pg;
+      pgg = dot(pg, g, m.n);
+      if (pgoldsqr != 0) {
+        beta = (pgg - dot(pg, gold, m.n)) / pgoldsqr;
+        if (beta < 0 || beta != beta) beta = 0;
+      }
+      for (size_t i = 0; i < m.n; i++) d[i] = -pg[i] + beta * d[i];
+    } else {
+      /* Polak-Ribiere with reset, as src/ConjugateGradient.cpp:77-91 */
+      if (goldsqr > 0) {
+        double num = 0;
+        for (size_t i = 0; i < m.n; i++) num += g[i] * (g[i] - gold[i]);
+        beta = num / goldsqr;
+        if (beta < 0 || beta != beta) beta = 0;
+      }
+      for (size_t i = 0; i < m.n; i++) d[i] = -g[i] + beta * d[i];
     }
-    for (size_t i = 0; i < m.n; i++) d[i] = -g[i] + beta * d[i];
     double s0 = dot(g, d, m.n);
+    if (!(s0 < 0) && precond && beta != 0) {
+      for (size_t i = 0; i < m.n; i++) d[i] = -m.pg[i];
+      beta = 0;
+      s0 = -pgg;
+    }
     if (!(s0 < 0)) {
       for (size_t i = 0; i < m.n; i++) d[i] = -g[i];
       s0 = -gg;
     }
+    pgoldsqr = pgg;
     memcpy(gold, g, sizeof(double) * m.n);
     goldsqr = gg;
     if (it > 0 && s0 != 0) alpha *= s_prev / s0;
@@ -611,6 +716,7 @@ int oracle_cg_solve(const oracle_params *p, const double *V, const double *mask,
     out3[2] = evals;
   }
   free(m.g);
+  free(m.pg);
   free(d);
   free(gold);
   return it;

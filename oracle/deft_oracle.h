@@ -24,6 +24,7 @@ enum {
   ORACLE_MU = 4,
   ORACLE_VEXT = 8,
   ORACLE_MASK = 16,
+  ORACLE_VEFF = 32, /* OfEffectivePotential: the variable is Veff, n = exp(-Veff/kT) */
 };
 
 typedef struct {
@@ -51,6 +52,12 @@ double oracle_energy(const oracle_params *p, const double *n, const double *V,
 double oracle_energy_grad(const oracle_params *p, const double *n, const double *V,
                           const double *mask, double *grad, double *terms6);
 
+/* Energy, gradient and preconditioned gradient (integralgrad with pgrad,
+ * src/Functional.h:147-149; equal to the gradient unless ORACLE_VEFF). */
+double oracle_energy_grad_pgrad(const oracle_params *p, const double *x, const double *V,
+                                const double *mask, double *grad, double *pgrad,
+                                double *terms6);
+
 /* Bulk chemical potential mu = -d/dn [f_HS + f_ideal](nb)
  * (src/equation-of-state.cpp:189-192 applied to
  *  OfEffectivePotential(HS(R)+IdealGas()), papers/contact/figs/walls.cpp:86-87). */
@@ -64,10 +71,19 @@ double oracle_homogeneous(double R, double kT, double mu, double nb);
 int oracle_cg_quadratic(const oracle_params *p, const double *V, const double *mask,
                         double *n_inout, int iters, double step, double *energies);
 
+/* PreconditionedConjugateGradient with QuadraticLineMinimizer
+ * (src/ConjugateGradient.cpp:115-160): as oracle_cg_quadratic. */
+int oracle_pcg_quadratic(const oracle_params *p, const double *V, const double *mask,
+                         double *x_inout, int iters, double step, double *energies);
+
 /* Derivative line-search CG to |grad|_2 < gtol (or maxiter iterations).
  * Returns the iteration count; out3 = {final energy, final |grad|, evals}. */
 int oracle_cg_solve(const oracle_params *p, const double *V, const double *mask,
                     double *n_inout, double gtol, int maxiter, double step, double *out3);
+/* The same with preconditioned directions when precond != 0. */
+int oracle_cg_solve_pc(const oracle_params *p, const double *V, const double *mask,
+                       double *n_inout, double gtol, int maxiter, double step, int precond,
+                       double *out3);
 
 /* Number of 3-D real FFTs executed by this oracle so far. */
 long long oracle_fft_count(void);

@@ -20,7 +20,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "liboracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libdeft_ref.so")
 
-HS, IDEAL, MU, VEXT, MASK = 1, 2, 4, 8, 16
+HS, IDEAL, MU, VEXT, MASK, VEFF = 1, 2, 4, 8, 16, 32
 NTERMS = 6
 TERM_NAMES = ("phi3", "phi1", "phi2", "ideal_gas", "chemical_potential", "external_potential")
 
@@ -79,6 +79,13 @@ def lib():
         L.oracle_cg_solve.restype = ctypes.c_int
         L.oracle_cg_solve.argtypes = [P, _dp, _dp, _dp, ctypes.c_double, ctypes.c_int,
                                       ctypes.c_double, _dp]
+        L.oracle_cg_solve_pc.restype = ctypes.c_int
+        L.oracle_cg_solve_pc.argtypes = [P, _dp, _dp, _dp, ctypes.c_double, ctypes.c_int,
+                                         ctypes.c_double, ctypes.c_int, _dp]
+        L.oracle_energy_grad_pgrad.restype = ctypes.c_double
+        L.oracle_energy_grad_pgrad.argtypes = [P, _dp, _dp, _dp, _dp, _dp, _dp]
+        L.oracle_pcg_quadratic.restype = ctypes.c_int
+        L.oracle_pcg_quadratic.argtypes = [P, _dp, _dp, _dp, ctypes.c_int, ctypes.c_double, _dp]
         L.oracle_fft_count.restype = ctypes.c_longlong
         L.offt_r2c_3d.argtypes = [ctypes.c_int] * 3 + [_dp, _dp]
         L.offt_c2r_3d.argtypes = [ctypes.c_int] * 3 + [_dp, _dp]
@@ -112,6 +119,13 @@ def ref():
         L.ref_fd_test.restype = ctypes.c_int
         L.ref_fd_test.argtypes = [_dp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                   ctypes.c_double, ctypes.c_double, ctypes.c_int, _dp, _dp]
+        L.ref_eval_veff.argtypes = [_dp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                    ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                    ctypes.c_int, _dp, _dp, _dp, _dp, _dp, _dp]
+        L.ref_pcg.restype = ctypes.c_int
+        L.ref_pcg.argtypes = [_dp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                              ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int, _dp,
+                              _dp, _dp, ctypes.c_int, ctypes.c_double, _dp]
         L.ref_fft_count.restype = ctypes.c_longlong
         _ref = L
     return _ref
@@ -168,6 +182,23 @@ class Problem:
                                      _ptr(self.mask), _ptr(g), _ptr(t))
         return (E, g, t) if terms else (E, g)
 
+    def energy_grad_pgrad(self, x):
+        """Energy, gradient and preconditioned gradient at the variable x
+        (the effective potential when VEFF is in terms)."""
+        x = np.ascontiguousarray(x, dtype=np.float64).reshape(-1)
+        g = np.empty(self.size)
+        pg = np.empty(self.size)
+        E = lib().oracle_energy_grad_pgrad(ctypes.byref(self.params()), _ptr(x), _ptr(self.V),
+                                           _ptr(self.mask), _ptr(g), _ptr(pg), None)
+        return E, g, pg
+
+    def pcg_quadratic(self, x, iters, step=0.1):
+        x = np.array(x, dtype=np.float64).reshape(-1)
+        e = np.zeros(iters)
+        k = lib().oracle_pcg_quadratic(ctypes.byref(self.params()), _ptr(self.V), _ptr(self.mask),
+                                       _ptr(x), iters, step, _ptr(e))
+        return x, e[:k]
+
     def cg_quadratic(self, n, iters, step=0.1):
         x = np.array(n, dtype=np.float64).reshape(-1)
         e = np.zeros(iters)
@@ -175,11 +206,12 @@ class Problem:
                                       _ptr(x), iters, step, _ptr(e))
         return x, e[:k]
 
-    def cg_solve(self, n, gtol=1e-9, maxiter=10000, step=1.0):
+    def cg_solve(self, n, gtol=1e-9, maxiter=10000, step=1.0, preconditioned=False):
         x = np.array(n, dtype=np.float64).reshape(-1)
         out = np.zeros(3)
-        it = lib().oracle_cg_solve(ctypes.byref(self.params()), _ptr(self.V), _ptr(self.mask),
-                                   _ptr(x), gtol, maxiter, step, _ptr(out))
+        it = lib().oracle_cg_solve_pc(ctypes.byref(self.params()), _ptr(self.V), _ptr(self.mask),
+                                      _ptr(x), gtol, maxiter, step, int(bool(preconditioned)),
+                                      _ptr(out))
         return x, {"iters": it, "energy": out[0], "gnorm": out[1], "evals": int(out[2])}
 
     # -- unmodified reference ---------------------------------------------
@@ -197,6 +229,26 @@ class Problem:
         out = np.empty(5 * self.size)
         ref().ref_weighted(_ptr(self.lat), *self.N, self.R, _ptr(n), _ptr(out))
         return out.reshape(5, -1)
+
+    def ref_eval_veff(self, x):
+        """The unmodified reference's constrain(mask, OfEffectivePotential(sum)):
+        energy, integralgrad and pgrad at the effective potential x."""
+        x = np.ascontiguousarray(x, dtype=np.float64).reshape(-1)
+        E = ctypes.c_double(0)
+        g = np.empty(self.size)
+        pg = np.empty(self.size)
+        ref().ref_eval_veff(_ptr(self.lat), *self.N, self.R, self.kT, self.mu, self.terms,
+                            _ptr(x), _ptr(self.V), _ptr(self.mask), ctypes.byref(E), _ptr(g),
+                            _ptr(pg))
+        return E.value, g, pg
+
+    def ref_pcg(self, x, iters, step=0.1):
+        x = np.array(x, dtype=np.float64).reshape(-1)
+        e = np.zeros(iters)
+        k = ref().ref_pcg(_ptr(self.lat), *self.N, self.R, self.kT, self.mu, self.terms,
+                          int(bool(self.terms & VEFF)), _ptr(self.V), _ptr(self.mask), _ptr(x),
+                          iters, step, _ptr(e))
+        return x, e[:k]
 
     def ref_cg(self, n, iters, step=0.1):
         x = np.array(n, dtype=np.float64).reshape(-1)

@@ -147,6 +147,61 @@ int ref_cg(const double *lat, int Nx, int Ny, int Nz, double R, double kT, doubl
   return i;
 }
 
+// constrain(mask, OfEffectivePotential(sum)) as papers/contact/figs/walls.cpp:
+// 86-98 composes it (the mask only with REF_MASK): energy, integralgrad and
+// the preconditioned gradient of the same call (src/Functional.h:144-149,
+// src/EffectivePotentialToDensity.cpp:28-91) at the effective potential x.
+void ref_eval_veff(const double *lat, int Nx, int Ny, int Nz, double R, double kT, double mu,
+                   int terms, const double *x, const double *V, const double *mask,
+                   double *E_out, double *grad, double *pgrad) {
+  GridDescription gd(make_lat(lat), Nx, Ny, Nz);
+  Functional f = OfEffectivePotential(make_sum(gd, R, mu, terms, V));
+  if (terms & REF_MASK) {
+    Grid m(gd);
+    for (int i = 0; i < gd.NxNyNz; i++) m[i] = mask[i];
+    f = constrain(m, f);
+  }
+  Grid xv(gd);
+  for (int i = 0; i < gd.NxNyNz; i++) xv[i] = x[i];
+  *E_out = f.integral(kT, xv);
+  VectorXd g(gd.NxNyNz), pg(gd.NxNyNz);
+  g.setZero();
+  pg.setZero();
+  f.integralgrad(kT, gd, xv, &g, &pg);
+  for (int i = 0; i < gd.NxNyNz; i++) {
+    grad[i] = g[i];
+    pgrad[i] = pg[i];
+  }
+}
+
+// `iters` calls of PreconditionedConjugateGradient(f, gd, kT, &x,
+// QuadraticLineMinimizer, step).improve_energy (src/ConjugateGradient.cpp:
+// 115-160,171-174) on the functional above (veff != 0) or on the plain sum;
+// energies[i] after call i.
+int ref_pcg(const double *lat, int Nx, int Ny, int Nz, double R, double kT, double mu, int terms,
+            int veff, const double *V, const double *mask, double *x_inout, int iters,
+            double step, double *energies) {
+  GridDescription gd(make_lat(lat), Nx, Ny, Nz);
+  Functional f = make_sum(gd, R, mu, terms, V);
+  if (veff) f = OfEffectivePotential(f);
+  if (terms & REF_MASK) {
+    Grid m(gd);
+    for (int i = 0; i < gd.NxNyNz; i++) m[i] = mask[i];
+    f = constrain(m, f);
+  }
+  Grid x(gd);
+  for (int i = 0; i < gd.NxNyNz; i++) x[i] = x_inout[i];
+  Minimizer min = PreconditionedConjugateGradient(f, gd, kT, &x, QuadraticLineMinimizer, step);
+  int i = 0;
+  for (; i < iters; i++) {
+    bool more = min.improve_energy(false);
+    energies[i] = min.energy();
+    if (!more) { i++; break; }
+  }
+  for (int j = 0; j < gd.NxNyNz; j++) x_inout[j] = x[j];
+  return i;
+}
+
 // Functional::run_finite_difference_test (src/Functional.cpp:104-213) on the
 // unconstrained sum; returns its failure count (0 = pass).
 int ref_fd_test(const double *lat, int Nx, int Ny, int Nz, double R, double kT, double mu,

@@ -84,6 +84,15 @@ class Fmt:
                                           g.ctypes.data, t.ctypes.data))
         return E.value, g, t
 
+    def energy_grad_pgrad(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        E = ctypes.c_double()
+        g = np.empty(self.grid.size)
+        pg = np.empty(self.grid.size)
+        check(self.L.deft_fmt_energy_grad_pgrad(self.h, x.ctypes.data, 0, ctypes.addressof(E),
+                                                g.ctypes.data, pg.ctypes.data, None))
+        return E.value, g, pg
+
     def hessian_vector(self, n, dx):
         n = np.ascontiguousarray(n, dtype=np.float64)
         dx = np.ascontiguousarray(dx, dtype=np.float64)
@@ -104,10 +113,10 @@ class Fmt:
 
 class CG:
     def __init__(self, fmt, linesearch=_lib.LS_SECANT, gtol=1e-9, maxiter=0, step=1.0,
-                 precision=0.0, refine_rel=0.0):
+                 precision=0.0, refine_rel=0.0, preconditioned=0):
         self.L = fmt.L
         self.size = fmt.grid.size
-        p = _lib.CgParams(linesearch, gtol, maxiter, step, precision, refine_rel)
+        p = _lib.CgParams(linesearch, gtol, maxiter, step, precision, refine_rel, preconditioned)
         h = ctypes.c_void_p()
         check(self.L.deft_cg_create(fmt.h, ctypes.byref(p), ctypes.byref(h)))
         self.h = h

@@ -52,3 +52,12 @@ def cg_case():
     n = np.where(mask > 0, n, 1e-4 * nb)
     P = O.Problem(lat, N, mu=mu, mask=mask)
     return P, n, 6, 0.1
+
+
+def veff_case():
+    """The cg_case slit in the effective-potential variable, as
+    papers/contact/figs/walls.cpp:86-101 sets it up: x = -kT ln n with the wall
+    density floored at 1e-4 nb, constrain(mask, OfEffectivePotential(...))."""
+    P, n, iters, step = cg_case()
+    P.terms |= O.VEFF
+    return P, -P.kT * np.log(n), iters, step

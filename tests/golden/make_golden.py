@@ -18,7 +18,7 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
 from oracle import oracle as O  # noqa: E402
-from tests.golden.cases import CASES, cg_case, make_case  # noqa: E402
+from tests.golden.cases import CASES, cg_case, make_case, veff_case  # noqa: E402
 
 
 def main():
@@ -45,6 +45,16 @@ def main():
     x, e = P.ref_cg(n, iters, step=step)
     out["cg_quadratic"] = {"energies": [float(v) for v in e], "iters": iters, "step": step}
     arrays["cg_quadratic_x"] = x
+    # OfEffectivePotential: energy, gradient, preconditioned gradient, and a
+    # PreconditionedConjugateGradient + QuadraticLineMinimizer trajectory
+    P, xv, iters, step = veff_case()
+    E, g, pg = P.ref_eval_veff(xv)
+    out["veff"] = {"E": E}
+    arrays["veff_grad"] = g
+    arrays["veff_pgrad"] = pg
+    x, e = P.ref_pcg(xv, iters, step=step)
+    out["pcg_quadratic"] = {"energies": [float(v) for v in e], "iters": iters, "step": step}
+    arrays["pcg_quadratic_x"] = x
     with open(os.path.join(HERE, "reference_values.json"), "w") as f:
         json.dump(out, f, indent=1, sort_keys=True)
     np.savez_compressed(os.path.join(HERE, "reference_fields.npz"), **arrays)

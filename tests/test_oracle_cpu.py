@@ -155,3 +155,58 @@ def test_oracle_matches_live_reference(oracle_mod):
     Er, gr, _ = P.ref_energy_grad(n)
     assert abs(E / Er - 1) < 1e-13
     assert np.abs(g - gr).max() <= 1e-13 * np.abs(gr).max()
+
+
+def test_oracle_effective_potential_matches_reference_golden(oracle_mod, golden):
+    """constrain(mask, OfEffectivePotential(HS + ideal + mu)): energy,
+    gradient and preconditioned gradient (src/EffectivePotentialToDensity.cpp:
+    28-91) against the reference's values."""
+    from tests.golden.cases import veff_case
+    vals, arrs = golden
+    P, x, _, _ = veff_case()
+    E, g, pg = P.energy_grad_pgrad(x)
+    assert abs(E / vals["veff"]["E"] - 1) < 1e-12
+    assert np.abs(g - arrs["veff_grad"]).max() <= 1e-12 * np.abs(arrs["veff_grad"]).max()
+    assert np.abs(pg - arrs["veff_pgrad"]).max() <= 1e-12 * np.abs(arrs["veff_pgrad"]).max()
+    # the energy is that of the density exp(-x/kT)
+    P2 = oracle_mod.Problem(P.lat.reshape(3, 3), P.N, R=P.R, kT=P.kT, mu=P.mu, mask=P.mask)
+    assert abs(P2.energy(np.exp(-x / P.kT)) / E - 1) < 1e-14
+
+
+def test_oracle_effective_potential_gradient_finite_difference(oracle_mod):
+    """Central differences of the energy along a random direction, the
+    check of Functional::run_finite_difference_test (src/Functional.cpp:159-210)."""
+    from tests.golden.cases import veff_case
+    P, x, _, _ = veff_case()
+    _, g, _ = P.energy_grad_pgrad(x)
+    rng = np.random.default_rng(4)
+    d = rng.standard_normal(x.size) * P.mask
+    for h in (1e-4, 1e-5):
+        fd = (P.energy(x + h * d) - P.energy(x - h * d)) / (2 * h)
+        assert abs(fd - g @ d) <= 1e-7 * abs(g @ d)
+
+
+def test_oracle_pcg_quadratic_trajectory(oracle_mod, golden):
+    """PreconditionedConjugateGradient + QuadraticLineMinimizer in the
+    effective-potential variable: the reference's energies step by step."""
+    from tests.golden.cases import veff_case
+    vals, arrs = golden
+    P, x0, iters, step = veff_case()
+    x, e = P.pcg_quadratic(x0, iters, step=step)
+    er = np.array(vals["pcg_quadratic"]["energies"])
+    assert len(e) == len(er)
+    assert np.abs(e / er - 1).max() < 1e-11
+    assert np.abs(x - arrs["pcg_quadratic_x"]).max() < 1e-5 * np.abs(x).max()
+
+
+def test_oracle_preconditioned_secant_cg_converges(oracle_mod):
+    from tests.golden.cases import veff_case
+    P, x0, _, _ = veff_case()
+    # |dF/dVeff| = |n dF/dn| / kT: a tighter tolerance than the density
+    # variable needs for the same profile accuracy
+    x1, i1 = P.cg_solve(x0, gtol=1e-11, maxiter=3000, preconditioned=True)
+    x2, i2 = P.cg_solve(x0, gtol=1e-11, maxiter=3000, preconditioned=False)
+    assert i1["gnorm"] < 1e-11 and i2["gnorm"] < 1e-11
+    n1, n2 = np.exp(-x1 / P.kT), np.exp(-x2 / P.kT)
+    free = P.mask > 0
+    assert np.abs(n1 - n2)[free].max() <= 1e-8 * n1[free].max()
