@@ -22,13 +22,15 @@ EXPORTS = (
     "deft_grid_create", "deft_grid_create_dx", "deft_grid_destroy", "deft_grid_info",
     "deft_grid_fft", "deft_grid_ifft",
     "deft_grid_profile", "deft_grid_profile_count", "deft_grid_profile_entry",
+    "deft_grid_set_tiles", "deft_grid_get_tiles", "deft_grid_graphs", "deft_tuning_set",
+    "deft_tuning_clear",
     "deft_fmt_create", "deft_fmt_destroy", "deft_fmt_set_params", "deft_fmt_set_vext",
     "deft_fmt_set_mask", "deft_fmt_energy", "deft_fmt_energy_grad", "deft_fmt_energy_grad_pgrad",
     "deft_fmt_weighted",
     "deft_fmt_hessian_vector",
     "deft_find_chemical_potential",
     "deft_fmt_energy_grad_noalloc", "deft_noalloc_scratch_bytes",
-    "deft_cg_create", "deft_cg_destroy", "deft_cg_set_x", "deft_cg_get_x", "deft_cg_x_device",
+    "deft_cg_create", "deft_cg_destroy", "deft_cg_set_params", "deft_cg_set_x", "deft_cg_get_x", "deft_cg_x_device",
     "deft_cg_step", "deft_cg_solve", "deft_batch_solve",
     "deft_fno_create", "deft_fno_destroy", "deft_fno_param_count", "deft_fno_get_params",
     "deft_fno_set_params", "deft_fno_eval", "deft_fno_adam", "deft_fno_train_step",
@@ -53,7 +55,8 @@ class FmtParams(ctypes.Structure):
 class CgParams(ctypes.Structure):
     _fields_ = [("linesearch", ctypes.c_int), ("gtol", ctypes.c_double), ("maxiter", ctypes.c_int),
                 ("step", ctypes.c_double), ("precision", ctypes.c_double),
-                ("refine_rel", ctypes.c_double), ("preconditioned", ctypes.c_int)]
+                ("refine_rel", ctypes.c_double), ("preconditioned", ctypes.c_int),
+                ("refine_abs", ctypes.c_double)]
 
 
 class CgStatus(ctypes.Structure):
@@ -105,6 +108,11 @@ def load():
         "deft_grid_profile_count": (ctypes.c_int, [_vp]),
         "deft_grid_profile_entry": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_char_p),
                                                    _dp, _dp]),
+        "deft_grid_set_tiles": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _dp]),
+        "deft_grid_get_tiles": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _dp]),
+        "deft_grid_graphs": (ctypes.c_int, [_vp, ctypes.c_int]),
+        "deft_tuning_set": (ctypes.c_int, [_dp, ctypes.c_int, _dp, _dp]),
+        "deft_tuning_clear": (ctypes.c_int, []),
         "deft_fmt_create": (ctypes.c_int, [_vp, ctypes.POINTER(FmtParams), _pp]),
         "deft_fmt_destroy": (ctypes.c_int, [_vp]),
         "deft_fmt_set_params": (ctypes.c_int, [_vp, ctypes.POINTER(FmtParams)]),
@@ -123,6 +131,7 @@ def load():
         "deft_noalloc_scratch_bytes": (ctypes.c_size_t, []),
         "deft_cg_create": (ctypes.c_int, [_vp, ctypes.POINTER(CgParams), _pp]),
         "deft_cg_destroy": (ctypes.c_int, [_vp]),
+        "deft_cg_set_params": (ctypes.c_int, [_vp, ctypes.POINTER(CgParams)]),
         "deft_cg_set_x": (ctypes.c_int, [_vp, _dp, ctypes.c_int]),
         "deft_cg_get_x": (ctypes.c_int, [_vp, _dp, ctypes.c_int]),
         "deft_cg_x_device": (_vp, [_vp]),
@@ -142,7 +151,7 @@ def load():
                                                ctypes.c_double, _dp]),
         "deft_fno_initial_density": (ctypes.c_int, [_vp, _vp, _dp, ctypes.c_double,
                                                     ctypes.c_double, ctypes.c_double, _dp, _dp,
-                                                    _dp]),
+                                                    _dp, _dp]),
         "deft_batch_solve": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.POINTER(BatchProblem),
                                             ctypes.POINTER(BatchParams), ctypes.POINTER(CgStatus)]),
     }

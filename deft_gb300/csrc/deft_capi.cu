@@ -9,7 +9,9 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
+#include <vector>
 
 using deft::Engine;
 
@@ -119,6 +121,33 @@ int sync(deft_ctx *c) {
   return e == cudaSuccess ? DEFT_OK : cuda_err(e, "stream");
 }
 
+// Tuned launch shapes registered for grid shapes (deft_tuning_set); every
+// grid created afterwards with a matching shape starts from them.
+struct TuningEntry {
+  int N[3];
+  int precision;
+  deft::TileChoice choice;
+};
+std::mutex g_tuning_mu;
+std::vector<TuningEntry> g_tuning;
+
+bool choice_from(const int tiles[6], const int *radix, deft::TileChoice *c) {
+  if (!tiles) return false;
+  c->By = tiles[0];
+  c->Bx = tiles[1];
+  c->Bxf = tiles[2];
+  c->Bxc = tiles[3];
+  c->Pz = tiles[4];
+  c->Pphi = tiles[5];
+  for (int a = 0; a < 3; a++)
+    for (int i = 0; i < 8; i++) c->radix[a][i] = radix ? radix[8 * a + i] : 0;
+  return true;
+}
+
+int engine_precision(int p) {
+  return p == DEFT_PRECISION_MIXED ? deft::kPrecisionMixed : deft::kPrecisionFP64;
+}
+
 int set_field(deft_fmt *f, double **slot, const double *src, int on_device) {
   if (!src) {
     cudaFree(*slot);
@@ -217,6 +246,12 @@ int deft_grid_create(deft_ctx *c, const double lat[9], int Nx, int Ny, int Nz, d
   g->ctx = c;
   g->spec = s;
   g->eng = eng;
+  {
+    std::lock_guard<std::mutex> lock(g_tuning_mu);
+    for (const TuningEntry &t : g_tuning)
+      if (t.N[0] == Nx && t.N[1] == Ny && t.N[2] == Nz)
+        eng->set_tiles(engine_precision(t.precision), t.choice);  // invalid entries are skipped
+  }
   const deft::Geom &ge = eng->geom();
   cudaError_t e = cudaMalloc((void **)&g->in_buf, sizeof(double) * ge.NR);
   if (e == cudaSuccess) e = cudaMalloc((void **)&g->out_buf, sizeof(double) * ge.NR);
@@ -302,6 +337,56 @@ int deft_grid_ifft(deft_grid *g, const double *in, double *out, int on_device) {
     if (e != cudaSuccess) return cuda_err(e, "device-to-host copy");
   }
   return sync(g->ctx);
+}
+
+int deft_grid_set_tiles(deft_grid *g, int precision, const int tiles[6], const int radix[24]) {
+  deft::TileChoice c;
+  if (!g || !choice_from(tiles, radix, &c)) return set_err(DEFT_ERR_ARG, "NULL argument");
+  cudaSetDevice(g->ctx->device);
+  if (g->eng->set_tiles(engine_precision(precision), c)) return set_err(DEFT_ERR_ARG,
+                                                                       g->eng->last_error());
+  return DEFT_OK;
+}
+
+int deft_grid_get_tiles(deft_grid *g, int precision, int tiles[6], int radix[24]) {
+  if (!g || !tiles) return set_err(DEFT_ERR_ARG, "NULL argument");
+  deft::TileChoice c;
+  g->eng->get_tiles(engine_precision(precision), &c);
+  const int v[6] = {c.By, c.Bx, c.Bxf, c.Bxc, c.Pz, c.Pphi};
+  memcpy(tiles, v, sizeof(v));
+  if (radix)
+    for (int a = 0; a < 3; a++)
+      for (int i = 0; i < 8; i++) radix[8 * a + i] = c.radix[a][i];
+  return DEFT_OK;
+}
+
+int deft_grid_graphs(deft_grid *g, int enable) {
+  if (!g) return set_err(DEFT_ERR_ARG, "grid is NULL");
+  cudaSetDevice(g->ctx->device);
+  cudaStreamSynchronize(g->ctx->stream);
+  g->eng->set_graphs(enable != 0);
+  return DEFT_OK;
+}
+
+int deft_tuning_set(const int N[3], int precision, const int tiles[6], const int radix[24]) {
+  TuningEntry t;
+  if (!N || !choice_from(tiles, radix, &t.choice)) return set_err(DEFT_ERR_ARG, "NULL argument");
+  memcpy(t.N, N, sizeof(t.N));
+  t.precision = precision;
+  std::lock_guard<std::mutex> lock(g_tuning_mu);
+  for (TuningEntry &e : g_tuning)
+    if (!memcmp(e.N, t.N, sizeof(t.N)) && e.precision == precision) {
+      e = t;
+      return DEFT_OK;
+    }
+  g_tuning.push_back(t);
+  return DEFT_OK;
+}
+
+int deft_tuning_clear(void) {
+  std::lock_guard<std::mutex> lock(g_tuning_mu);
+  g_tuning.clear();
+  return DEFT_OK;
 }
 
 int deft_grid_profile(deft_grid *g, int timing) {
@@ -625,6 +710,27 @@ int deft_cg_create(deft_fmt *f, const deft_cg_params *p, deft_cg **out) {
   }
   *out = c;
   return sync(f->grid->ctx);
+}
+
+int deft_cg_set_params(deft_cg *c, const deft_cg_params *p) {
+  if (!c || !p) return set_err(DEFT_ERR_ARG, "NULL argument");
+  if (p->linesearch != DEFT_LS_SECANT && p->linesearch != DEFT_LS_QUADRATIC_REF)
+    return set_err(DEFT_ERR_ARG, "unknown line search");
+  cudaSetDevice(c->f->grid->ctx->device);
+  if (p->preconditioned && !c->pg) {
+    cudaError_t e = cudaMalloc((void **)&c->pg, sizeof(double) * nr(c->f->grid));
+    if (e != cudaSuccess) {
+      c->pg = nullptr;
+      return cuda_err(e, "cudaMalloc");
+    }
+  } else if (!p->preconditioned && c->pg) {
+    cudaStreamSynchronize(c->f->grid->ctx->stream);
+    cudaFree(c->pg);
+    c->pg = nullptr;
+  }
+  c->p = *p;
+  c->have_g = false;  // the next step re-evaluates (pg is needed for the new setting)
+  return DEFT_OK;
 }
 
 int deft_cg_destroy(deft_cg *c) {
@@ -1129,7 +1235,9 @@ int deft_cg_step(deft_cg *c, deft_cg_status *st) {
           // FP32 CG until the gradient has dropped by refine_rel (or the
           // FP32 line search runs out of resolution), then refine in FP64
           const double rel = c->p.refine_rel > 0 ? c->p.refine_rel : 1e-4;
-          const double thr = std::fmax(c->g0norm > 0 ? rel * c->g0norm : 0.0, c->p.gtol);
+          const double thr = std::fmax(
+              c->p.refine_abs > 0 ? c->p.refine_abs : (c->g0norm > 0 ? rel * c->g0norm : 0.0),
+              c->p.gtol);
           status = step_secant(c, st, spec, thr);
           if (status == DEFT_ERR_LINESEARCH) status = DEFT_OK;
           if (!status && (c->done || st->gnorm < thr || c->iter > 0 && !c->have_g)) {

@@ -925,19 +925,8 @@ int even_tiles(int lines, int maxb) {
   return (lines + nt - 1) / nt;
 }
 
-Tiles make_tiles(const Geom &g, size_t cs, size_t budget) {
-  Tiles t;
-  const int pairs = (g.lines + 1) / 2;
-  auto cap = [](size_t v, int hi) { return (int)(v < (size_t)hi ? v : (size_t)hi); };
-  t.By = even_tiles(g.NzH, cap(budget / (2 * (size_t)g.Ny * cs), 16));
-  t.Bx = even_tiles(g.Ny * g.NzH, cap(budget / (2 * (size_t)g.Nx * cs), 16));
-  t.Bxf = even_tiles(g.Ny * g.NzH, cap(budget / (3 * (size_t)g.Nx * cs), 16));
-  t.Bxc = even_tiles(g.Ny * g.NzH, cap(budget / (10 * (size_t)g.Nx * cs), 16));
-  t.Pz = even_tiles(pairs, cap(budget / (2 * (size_t)g.Nz * cs), 16));
-  int pm = cap(budget / (10 * (size_t)g.Nz * cs), 15);
-  if (pm < 1) pm = 1;
-  if (pm > 1 && pm % 2 == 0) pm -= 1;  // odd: conflict-free z-strided shared accesses
-  t.Pphi = pm < pairs ? pm : pairs;
+// Fast dividers and shared-memory sizes from the tile widths.
+void finish_tiles(Tiles &t, const Geom &g, size_t cs) {
   t.fBy = make_fastdiv(t.By);
   t.fBx = make_fastdiv(t.Bx);
   t.fBxf = make_fastdiv(t.Bxf);
@@ -953,7 +942,53 @@ Tiles make_tiles(const Geom &g, size_t cs, size_t budget) {
   t.smem_xc = 10 * (size_t)g.Nx * t.Bxc * cs;
   t.smem_z = 2 * (size_t)g.Nz * t.Pz * cs;
   t.smem_phi = 10 * (size_t)g.Nz * t.Pphi * cs;
+}
+
+// Built-in rule: the widest tiles within `budget` bytes of shared memory (at
+// most 16 columns / pairs), evened out over the lines; overrides from `ov`.
+Tiles make_tiles(const Geom &g, size_t cs, size_t budget, const TileChoice *ov = nullptr) {
+  Tiles t;
+  const int pairs = (g.lines + 1) / 2;
+  auto cap = [](size_t v, int hi) { return (int)(v < (size_t)hi ? v : (size_t)hi); };
+  t.By = even_tiles(g.NzH, cap(budget / (2 * (size_t)g.Ny * cs), 16));
+  t.Bx = even_tiles(g.Ny * g.NzH, cap(budget / (2 * (size_t)g.Nx * cs), 16));
+  t.Bxf = even_tiles(g.Ny * g.NzH, cap(budget / (3 * (size_t)g.Nx * cs), 16));
+  t.Bxc = even_tiles(g.Ny * g.NzH, cap(budget / (10 * (size_t)g.Nx * cs), 16));
+  t.Pz = even_tiles(pairs, cap(budget / (2 * (size_t)g.Nz * cs), 16));
+  int pm = cap(budget / (10 * (size_t)g.Nz * cs), 15);
+  if (pm < 1) pm = 1;
+  if (pm > 1 && pm % 2 == 0) pm -= 1;  // odd: conflict-free z-strided shared accesses
+  t.Pphi = pm < pairs ? pm : pairs;
+  if (ov) {
+    if (ov->By > 0) t.By = ov->By < g.NzH ? ov->By : g.NzH;
+    if (ov->Bx > 0) t.Bx = ov->Bx < g.Ny * g.NzH ? ov->Bx : g.Ny * g.NzH;
+    if (ov->Bxf > 0) t.Bxf = ov->Bxf < g.Ny * g.NzH ? ov->Bxf : g.Ny * g.NzH;
+    if (ov->Bxc > 0) t.Bxc = ov->Bxc < g.Ny * g.NzH ? ov->Bxc : g.Ny * g.NzH;
+    if (ov->Pz > 0) t.Pz = ov->Pz < pairs ? ov->Pz : pairs;
+    if (ov->Pphi > 0) t.Pphi = ov->Pphi < pairs ? ov->Pphi : pairs;
+  }
+  finish_tiles(t, g, cs);
   return t;
+}
+
+// Applies a radix order (0-terminated) to a plan; false if it does not
+// factor the length into supported radices.
+bool set_radix_order(FftPlan &p, const int *r) {
+  int k = 0;
+  long long prod = 1;
+  int tmp[kMaxPasses];
+  for (; k < 8 && r[k]; k++) {
+    const int v = r[k];
+    const bool ok = v == 2 || v == 3 || v == 4 || v == 5 || v == 7 || v == 8 || v == 11 || v == 13;
+    if (!ok || k >= kMaxPasses) return false;
+    tmp[k] = v;
+    prod *= v;
+  }
+  if (k == 0 || prod != p.n) return false;
+  p.npass = k;
+  for (int i = 0; i < k; i++) p.radix[i] = tmp[i];
+  plan_fill_ns(p);
+  return true;
 }
 
 constexpr size_t kBudget64 = 96 * 1024;
@@ -1057,6 +1092,7 @@ class EngineImpl {
     cudaFree(w2f);
     cudaFree(wvf);
     cudaFree(hess);
+    clear_graphs();
     cudaFree(hloc);
     cudaFree(S0);
     cudaFree(S5);
@@ -1256,6 +1292,65 @@ class EngineImpl {
 
   int pairs_tiles(int P) const { return ((g.lines + 1) / 2 + P - 1) / P; }
 
+  int set_tiles(int prec, const TileChoice &c) {
+    const bool f32 = prec == kPrecisionMixed;
+    const size_t cs = f32 ? sizeof(float2) : sizeof(double2);
+    Tiles t = make_tiles(g, cs, f32 ? kBudget32 : kBudget64, &c);
+    int optin = 0, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (t.smem_max() + 8 * 1024 > (size_t)optin) {
+      err = "tile choice exceeds shared memory";
+      return -1;
+    }
+    FftPlan np[3] = {f32 ? pxf : px, f32 ? pyf : py, f32 ? pzf : pz};
+    for (int a = 0; a < 3; a++) {
+      if (c.radix[a][0] && !set_radix_order(np[a], c.radix[a])) {
+        err = "radix order does not factor axis " + std::to_string(a);
+        return -1;
+      }
+    }
+    const int need = pairs_tiles(t.Pphi);
+    if (need > max_blocks) {
+      cudaStreamSynchronize(stream);
+      double *np2 = nullptr;
+      if (cudaMalloc((void **)&np2, sizeof(double) * kNumTerms * need) != cudaSuccess) {
+        err = "cudaMalloc (energy partials)";
+        return -1;
+      }
+      cudaFree(partials);
+      partials = np2;
+      max_blocks = need;
+    }
+    clear_graphs();
+    if (f32) {
+      t32 = t;
+      pxf = np[0];
+      pyf = np[1];
+      pzf = np[2];
+    } else {
+      t64 = t;
+      px = np[0];
+      py = np[1];
+      pz = np[2];
+    }
+    return 0;
+  }
+
+  void get_tiles(int prec, TileChoice *c) const {
+    const bool f32 = prec == kPrecisionMixed;
+    const Tiles &t = f32 ? t32 : t64;
+    c->By = t.By;
+    c->Bx = t.Bx;
+    c->Bxf = t.Bxf;
+    c->Bxc = t.Bxc;
+    c->Pz = t.Pz;
+    c->Pphi = t.Pphi;
+    const FftPlan *pl[3] = {f32 ? &pxf : &px, f32 ? &pyf : &py, f32 ? &pzf : &pz};
+    for (int a = 0; a < 3; a++)
+      for (int i = 0; i < 8; i++) c->radix[a][i] = i < pl[a]->npass ? pl[a]->radix[i] : 0;
+  }
+
   template <typename T> void y_fft(typename Cplx<T>::type *data, int nf, int sign) {
     const Tiles &t = tl<T>();
     dim3 grid((g.NzH + t.By - 1) / t.By, g.Nx, nf);
@@ -1269,9 +1364,10 @@ class EngineImpl {
   }
   int x_tiles(int B) const { return (g.Ny * g.NzH + B - 1) / B; }
 
+  // Queues z r2c, y FFT, x convolution and inverse y of n (the weight table
+  // for f.R must be current: ensure_table runs outside any graph capture).
   template <typename T> int forward_weighted(const FmtSpec &f, const double *n) {
     const Tiles &t = tl<T>();
-    if (ensure_table<T>(f.R)) return -1;
     pre(kK_z_r2c);
     k_z_r2c<T><<<dim3(pairs_tiles(t.Pz), 1), kThreads, t.smem_z, stream>>>(
         n, spec0<T>(), g, plan<T>(2), t.fPz, T(1));
@@ -1299,11 +1395,101 @@ class EngineImpl {
     return la;
   }
 
-  int finish_energy(int nblk, double *E_host, double *terms_host) {
+  // ---- CUDA graphs of the evaluation and Hessian-vector launch sequences.
+  // A sequence is captured once per key (everything its launches bake in:
+  // kind, precision, buffers, functional parameters) and replayed with one
+  // cudaGraphLaunch afterwards; with per-kernel event timing on, launches go
+  // out one by one.  Launch counts of a replay are those of its capture.
+  struct GraphKey {
+    int kind, prec, terms, pad;
+    const void *p[4];
+    double R, kT, mu;
+  };
+  struct GraphEntry {
+    GraphKey key;
+    cudaGraphExec_t exec;
+    long long counts[kNumKernels];
+  };
+  std::vector<GraphEntry> graphs;
+  bool use_graphs = true;
+
+  static GraphKey graph_key(int kind, int prec, const FmtSpec &f, const void *a, const void *b,
+                            const void *c, const void *d) {
+    GraphKey k;
+    memset(&k, 0, sizeof(k));
+    k.kind = kind;
+    k.prec = prec;
+    k.terms = f.terms;
+    k.p[0] = a;
+    k.p[1] = b;
+    k.p[2] = c;
+    k.p[3] = d;
+    k.R = f.R;
+    k.kT = f.kT;
+    k.mu = f.mu;
+    return k;
+  }
+
+  void clear_graphs() {
+    for (GraphEntry &e : graphs) cudaGraphExecDestroy(e.exec);
+    graphs.clear();
+  }
+
+  int replay(GraphEntry &e) {
+    cudaError_t r = cudaGraphLaunch(e.exec, stream);
+    if (r != cudaSuccess) return fail("graph launch", r);
+    for (int i = 0; i < kNumKernels; i++) launches[i] += e.counts[i];
+    return 0;
+  }
+
+  template <typename F> int run_graphed(const GraphKey &key, F launch) {
+    if (timing || !use_graphs) return launch();
+    for (GraphEntry &e : graphs)
+      if (!memcmp(&e.key, &key, sizeof(key))) return replay(e);
+    long long before[kNumKernels];
+    memcpy(before, launches, sizeof(before));
+    cudaError_t r = cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal);
+    if (r != cudaSuccess) {
+      cudaGetLastError();
+      use_graphs = false;
+      return launch();
+    }
+    const int rc = launch();
+    cudaGraph_t graph = nullptr;
+    r = cudaStreamEndCapture(stream, &graph);
+    GraphEntry e;
+    e.key = key;
+    for (int i = 0; i < kNumKernels; i++) {
+      e.counts[i] = launches[i] - before[i];
+      launches[i] = before[i];
+    }
+    if (rc || r != cudaSuccess || !graph ||
+        cudaGraphInstantiate(&e.exec, graph, 0) != cudaSuccess) {
+      // capture not possible here: launch directly from now on
+      if (graph) cudaGraphDestroy(graph);
+      cudaGetLastError();
+      use_graphs = false;
+      return launch();
+    }
+    cudaGraphDestroy(graph);
+    if (graphs.size() >= 8) {
+      cudaGraphExecDestroy(graphs.front().exec);
+      graphs.erase(graphs.begin());
+    }
+    graphs.push_back(e);
+    return replay(graphs.back());
+  }
+
+  // Queues the fixed-order reduction of the energy partials and the copy of
+  // the results to the pinned host block.
+  void queue_energy(int nblk) {
     pre(kK_reduce_terms);
     k_reduce_terms<<<1, kThreads, 0, stream>>>(partials, nblk, g.dV, results);
     post(kK_reduce_terms);
     cudaMemcpyAsync(results_host, results, sizeof(double) * 8, cudaMemcpyDeviceToHost, stream);
+  }
+
+  int finish_energy(double *E_host, double *terms_host) {
     cudaError_t e = cudaStreamSynchronize(stream);
     if (e != cudaSuccess) return fail("energy", e);
     harvest();
@@ -1315,6 +1501,15 @@ class EngineImpl {
   template <typename T>
   int eval(const FmtSpec &f, const double *n, const double *V, const double *mask, double *grad,
            double *E_host, double *terms_host) {
+    if ((f.terms & kTermHS) && ensure_table<T>(f.R)) return -1;
+    const GraphKey key = graph_key(grad ? 1 : 0, sizeof(T), f, n, V, mask, grad);
+    if (run_graphed(key, [&] { return eval_launch<T>(f, n, V, mask, grad); })) return -1;
+    return finish_energy(E_host, terms_host);
+  }
+
+  template <typename T>
+  int eval_launch(const FmtSpec &f, const double *n, const double *V, const double *mask,
+                  double *grad) {
     const Tiles &t = tl<T>();
     const LocalArgs la = local_args(f);
     int nblk;
@@ -1352,7 +1547,8 @@ class EngineImpl {
       post(kK_z_grad);
     }
     if (check("gradient")) return -1;
-    return finish_energy(nblk, E_host, terms_host);
+    queue_energy(nblk);
+    return check("energy reduction");
   }
   int hess_setup(const FmtSpec &f, const double *n) {
     if (!hess && (alloc(&hess, sizeof(float) * kHessPacked * (size_t)g.NR) ||
@@ -1360,7 +1556,7 @@ class EngineImpl {
       return -1;
     const LocalArgs la = local_args(f);
     if (f.terms & kTermHS) {
-      if (forward_weighted<float>(f, n)) return -1;
+      if (ensure_table<float>(f.R) || forward_weighted<float>(f, n)) return -1;
     }
     pre(kK_z_hess);
     k_z_hess<float><<<pairs_tiles(t32.Pphi), kThreads, t32.smem_phi, stream>>>(
@@ -1370,6 +1566,12 @@ class EngineImpl {
   }
 
   int hvp(const FmtSpec &f, const double *dx, const double *mask, double *out) {
+    if ((f.terms & kTermHS) && ensure_table<float>(f.R)) return -1;
+    const GraphKey key = graph_key(2, 4, f, dx, mask, out, hess);
+    return run_graphed(key, [&] { return hvp_launch(f, dx, mask, out); });
+  }
+
+  int hvp_launch(const FmtSpec &f, const double *dx, const double *mask, double *out) {
     const LocalArgs la = local_args(f);
     if (f.terms & kTermHS) {
       if (forward_weighted<float>(f, dx)) return -1;
@@ -1450,7 +1652,7 @@ int Engine::ifft(const double2 *in, double *out) {
 
 int Engine::weighted(const FmtSpec &f, const double *n, double *out5) {
   EngineImpl &e = *impl_;
-  if (e.forward_weighted<double>(f, n)) return -1;
+  if (e.ensure_table<double>(f.R) || e.forward_weighted<double>(f, n)) return -1;
   e.pre(kK_z_c2r);
     k_z_c2r<double><<<dim3(e.pairs_tiles(e.t64.Pz), 5), kThreads, e.t64.smem_z, e.stream>>>(
       e.S5, out5, e.g, e.pz, e.t64.fPz, 1.0);
@@ -1505,6 +1707,13 @@ int Engine::scal_add(double beta, double *d, double alpha, const double *gv) {
     e.post(kK_scal_add);
   return e.check("scal_add");
 }
+
+int Engine::set_tiles(int prec, const TileChoice &c) { return impl_->set_tiles(prec, c); }
+void Engine::set_graphs(bool on) {
+  impl_->clear_graphs();
+  impl_->use_graphs = on;
+}
+void Engine::get_tiles(int prec, TileChoice *c) const { impl_->get_tiles(prec, c); }
 
 int Engine::veff_density(double kT, const double *x, double *n) {
   EngineImpl &e = *impl_;

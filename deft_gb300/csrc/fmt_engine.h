@@ -59,6 +59,19 @@ inline void geom_finish(Geom &g) {
   g.fNy = make_fastdiv((unsigned)g.Ny);
 }
 
+// Launch shapes of one precision's kernels and the radix order of each axis's
+// FFT plan (an autotuner's choice).  A zero entry keeps the built-in rule; a
+// radix list ends at the first 0.
+//   By   kz columns per y-FFT tile          Bx   columns per plain x-FFT tile
+//   Bxf  columns per forward-convolution x tile
+//   Bxc  columns per adjoint-convolution x tile (five fields each)
+//   Pz   z-line pairs per r2c / c2r / gradient tile
+//   Pphi z-line pairs per phi / Hessian tile (five fields each)
+struct TileChoice {
+  int By = 0, Bx = 0, Bxf = 0, Bxc = 0, Pz = 0, Pphi = 0;
+  int radix[3][8] = {};  // axes x, y, z
+};
+
 class EngineImpl;
 
 class Engine {
@@ -68,6 +81,17 @@ class Engine {
   ~Engine();
 
   const Geom &geom() const;
+
+  // Replaces the launch shapes and radix orders of precision `prec`
+  // (kPrecisionFP64 / kPrecisionMixed); 0 on success, -1 if the choice is
+  // invalid (a radix order whose product is not the axis length, or a tile
+  // that does not fit in shared memory), leaving the old choice in place.
+  int set_tiles(int prec, const TileChoice &c);
+  // The effective choice (built-in values filled in).
+  void get_tiles(int prec, TileChoice *c) const;
+  // Evaluations and Hessian-vector products are captured as CUDA graphs and
+  // replayed (default on; per-kernel event timing launches directly).
+  void set_graphs(bool on);
   cudaStream_t stream() const;
   size_t scratch_bytes() const;
 

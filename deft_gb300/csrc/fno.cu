@@ -492,6 +492,25 @@ __global__ void k_density(const float *__restrict__ y, const double *__restrict_
   }
 }
 
+constexpr int kNormBlocks = 256;
+
+// Per-block sums of squares (FP64, fixed order) over a strided range.
+__global__ void k_norm2_partial(const double *__restrict__ v, long long n, double *__restrict__ out) {
+  __shared__ double red[kT / 32];
+  double s = 0;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    s += v[i] * v[i];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += red[w];
+    out[blockIdx.x] = t;
+  }
+}
+
 // Bulk start: nb on free points, 0 in the walls.
 __global__ void k_bulk(const double *__restrict__ mask, double nb, double *__restrict__ n,
                        long long NR) {
@@ -540,7 +559,8 @@ struct deft_fno {
   float2 *A = nullptr, *B = nullptr, *S = nullptr, *S2 = nullptr;
   float *hb0 = nullptr, *hb1 = nullptr, *zb = nullptr;
   float *part = nullptr;
-  double *bulk = nullptr;  // N^3 doubles, allocated by the first checked warm start
+  double *bulk = nullptr;    // 2 N^3 doubles (bulk start, its gradient), allocated on first use
+  double *part_d = nullptr;  // kNormBlocks FP64 partial sums
   int nblk = 0;
   std::string err;
 };
@@ -761,6 +781,7 @@ int deft_fno_create(int device, int N, int channels, int modes, int layers, unsi
   dev(&f->zb, act);
   f->nblk = grid_for(f->NR);
   dev(&f->part, sizeof(float) * (size_t)f->nblk * (C * C + 2 * C + 1 + 8));
+  dev(&f->part_d, sizeof(double) * kNormBlocks);
   if (!ok) {
     deft_fno_destroy(f);
     return DEFT_ERR_NOMEM;
@@ -801,7 +822,7 @@ int deft_fno_destroy(deft_fno *f) {
                   (void *)f->Eyi, (void *)f->Exf, (void *)f->Exi, (void *)f->zq, (void *)f->y,
                   (void *)f->mask, (void *)f->target, (void *)f->wt, (void *)f->A, (void *)f->B,
                   (void *)f->S, (void *)f->S2, (void *)f->hb0, (void *)f->hb1, (void *)f->zb,
-                  (void *)f->part, (void *)f->bulk})
+                  (void *)f->part, (void *)f->bulk, (void *)f->part_d})
     cudaFree(q);
   for (float *q : f->h) cudaFree(q);
   for (float *q : f->z) cudaFree(q);
@@ -992,21 +1013,35 @@ int deft_fno_warm_start(deft_fno *f, const double *mask_dev, double eta, double 
 // (nb on free points, 0 in the walls).  *used_network = 1 or 0 says which.
 int deft_fno_initial_density(deft_fno *f, deft_fmt *fmt, const double *mask_dev, double eta,
                              double nb, double floor_rel, double *n_out_dev, int *used_network,
-                             double *E_out) {
+                             double *E_out, double *gnorm_bulk_out) {
   if (!f || !fmt || !mask_dev || !n_out_dev) return DEFT_ERR_ARG;
   int shape[3];
   deft::fmt_shape(fmt, shape);
   if (shape[0] != f->N || shape[1] != f->N || shape[2] != f->N)
     return fno_fail(f, "functional grid does not match the network's N^3", DEFT_ERR_ARG);
   cudaSetDevice(f->device);
-  if (!f->bulk && cudaMalloc((void **)&f->bulk, sizeof(double) * f->NR) != cudaSuccess) {
+  if (!f->bulk && cudaMalloc((void **)&f->bulk, sizeof(double) * 2 * f->NR) != cudaSuccess) {
     f->bulk = nullptr;
     return fno_fail(f, "bulk start buffer", DEFT_ERR_NOMEM);
   }
   k_bulk<<<grid_for(f->NR), kT, 0, f->stream>>>(mask_dev, nb, f->bulk, f->NR);
   if (int s = deft_fno_warm_start(f, mask_dev, eta, nb, floor_rel, n_out_dev)) return s;
   double E0 = 0, E1 = 0;
-  if (int s = deft_fmt_energy(fmt, f->bulk, 1, &E0, nullptr)) return s;
+  if (gnorm_bulk_out) {
+    // energy and gradient of the bulk start (gradient in the buffer's upper half)
+    double *gb = f->bulk + f->NR;
+    if (int s = deft_fmt_energy_grad(fmt, f->bulk, 1, &E0, gb, nullptr)) return s;
+    k_norm2_partial<<<kNormBlocks, kT, 0, f->stream>>>(gb, f->NR, f->part_d);
+    std::vector<double> h(kNormBlocks);
+    cudaMemcpyAsync(h.data(), f->part_d, sizeof(double) * kNormBlocks, cudaMemcpyDeviceToHost,
+                    f->stream);
+    if (cudaStreamSynchronize(f->stream) != cudaSuccess) return check(f, "bulk gradient norm");
+    double ss = 0;
+    for (double v : h) ss += v;
+    *gnorm_bulk_out = std::sqrt(ss);
+  } else if (int s = deft_fmt_energy(fmt, f->bulk, 1, &E0, nullptr)) {
+    return s;
+  }
   const int s1 = deft_fmt_energy(fmt, n_out_dev, 1, &E1, nullptr);
   const bool use = s1 == DEFT_OK && std::isfinite(E1) && E1 <= E0;
   if (!use) {

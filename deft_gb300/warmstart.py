@@ -49,18 +49,27 @@ class FourierOperator:
             raise ValueError(f"expected {self.nparam} parameters, got {p.size}")
         check(self.L.deft_fno_set_params(self.h, p.ctypes.data))
 
-    def header(self):
+    def header(self, dtype="float32"):
         return {"format": "deft_fno", "N": self.N, "channels": self.channels,
                 "modes": self.modes, "layers": self.layers, "nparam": self.nparam,
-                "dtype": "float32 little-endian"}
+                "dtype": dtype + " little-endian"}
 
-    def save(self, path):
-        """Raw little-endian FP32 parameters in `path` and a JSON header in
-        `path + '.json'`."""
+    def save(self, path, dtype="float32"):
+        """Raw little-endian parameters in `path` and a JSON header in
+        `path + '.json'`.  dtype "bfloat16" stores the values every pass
+        uses (round to nearest even), half the size; training from such a
+        file restarts from those values."""
         p = self.get_params()
-        p.astype("<f4").tofile(path)
+        if dtype == "bfloat16":
+            u = p.astype("<f4").view("<u4").astype(np.uint64)
+            u = ((u + 0x7FFF + ((u >> 16) & 1)) >> 16).astype("<u2")
+            u.tofile(path)
+        elif dtype == "float32":
+            p.astype("<f4").tofile(path)
+        else:
+            raise ValueError(dtype)
         with open(path + ".json", "w") as f:
-            json.dump(self.header(), f)
+            json.dump(self.header(dtype), f)
 
     @classmethod
     def load(cls, path, device=0):
@@ -69,7 +78,11 @@ class FourierOperator:
         if h.get("format") != "deft_fno":
             raise ValueError(f"{path}: not a deft_fno weight file")
         net = cls(h["N"], h["channels"], h["modes"], h["layers"], device=device)
-        p = np.fromfile(path, dtype="<f4")
+        if h["dtype"].startswith("bfloat16"):
+            u = np.fromfile(path, dtype="<u2").astype(np.uint32) << 16
+            p = u.view(np.float32)
+        else:
+            p = np.fromfile(path, dtype="<f4")
         net.set_params(p)
         return net
 
@@ -103,14 +116,20 @@ class FourierOperator:
                                    ctypes.addressof(loss), None))
         return loss.value
 
-    def initial_density(self, fmt_handle, mask_ptr, eta, nb, n_out_ptr, floor_rel=1e-3):
+    def initial_density(self, fmt_handle, mask_ptr, eta, nb, n_out_ptr, floor_rel=1e-3,
+                        bulk_gnorm=False):
         """Checked warm start into the device array n_out_ptr (N^3 doubles)
-        for the functional fmt_handle; returns (used_network, energy)."""
+        for the functional fmt_handle; returns (used_network, energy) and,
+        with bulk_gnorm, the bulk start's gradient norm as a third value."""
         used = ctypes.c_int(0)
         E = ctypes.c_double(0)
+        gb = ctypes.c_double(0)
         check(self.L.deft_fno_initial_density(self.h, fmt_handle, mask_ptr, float(eta), float(nb),
                                               float(floor_rel), n_out_ptr,
-                                              ctypes.addressof(used), ctypes.addressof(E)))
+                                              ctypes.addressof(used), ctypes.addressof(E),
+                                              ctypes.addressof(gb) if bulk_gnorm else None))
+        if bulk_gnorm:
+            return bool(used.value), E.value, gb.value
         return bool(used.value), E.value
 
     def close(self):
@@ -212,6 +231,7 @@ class Solver:
 
     def __init__(self, shape, lat, device=0, gtol=1e-9):
         L = self.L = _lib.load()
+        self.gtol = gtol
         self.shape = tuple(int(v) for v in shape)
         self.size = int(np.prod(self.shape))
         h = ctypes.c_void_p()
@@ -240,11 +260,14 @@ class Solver:
             check(self.L.deft_fmt_set_params(f, ctypes.byref(p)))
             check(self.L.deft_fmt_set_mask(f, mask_ptr, 1))
 
-    def solve(self, precision, n0_ptr):
+    def solve(self, precision, n0_ptr, refine_abs=0.0):
         """Solve from the device array n0_ptr; returns (CgStatus, seconds).
+        refine_abs > 0 sets the mixed form's FP32-stage exit |grad| < refine_abs.
         A minimiser that stops without converging (line search, iteration
         limit, non-finite values) is reported in CgStatus.status, not raised."""
         t0 = time.perf_counter()
+        cp = _lib.CgParams(_lib.LS_SECANT, self.gtol, 20000, 1.0, 0.0, 0.0, 0, float(refine_abs))
+        check(self.L.deft_cg_set_params(self.cg[precision], ctypes.byref(cp)))
         check(self.L.deft_cg_set_x(self.cg[precision], n0_ptr, 1))
         st = _lib.CgStatus()
         code = self.L.deft_cg_solve(self.cg[precision], ctypes.byref(st))
@@ -265,47 +288,58 @@ class Solver:
         self.L.deft_ctx_destroy(self.ctx)
 
 
-def compare_starts(net, problems, device=0, fp64=True, floor_rel=1e-3):
+def compare_starts(net, problems, device=0, fp64=True, floor_rel=1e-3, switch=(None,)):
     """Solves each problem to |grad F| < 1e-9 from the bulk start and from
     the checked warm start, in the mixed form (and in FP64 if asked); the
-    warm-start time includes the network's forward pass and the two energy
-    evaluations of the check.  Returns one record per problem."""
+    warm-start time includes the network's forward pass and the energy
+    checks.  `switch` lists the mixed warm-start variants: None leaves the
+    FP32 stage at 1e-4 of the start's gradient norm (the default rule), a
+    number c at c times the bulk start's gradient norm.  Returns one record
+    per problem."""
     import torch
     dev = f"cuda:{device}"
     sv = Solver(problems[0].shape, problems[0].lat, device=device)
     recs = []
+
+    def rec(st, t, extra=None):
+        r = {"s": t, "iter": st.iter, "evals": st.evals, "evals_fp64": st.evals_fp64,
+             "hvps": st.hvps, "gnorm": st.gnorm, "status": st.status,
+             "converged": bool(st.converged) and st.status == 0}
+        if extra:
+            r.update(extra)
+        return r
+
     try:
         for s in problems:
             mask = torch.tensor(s.mask.reshape(-1), dtype=torch.float64, device=dev)
             bulk = torch.tensor(s.n0.reshape(-1), dtype=torch.float64, device=dev)
             n_ws = torch.empty_like(mask)
+            x = torch.empty_like(mask)
             sv.set_problem(s, mask.data_ptr())
             r = {"eta": s.eta, "solutes": len(getattr(s, "solutes", ())),
                  "width": getattr(s, "width", None)}
-            runs = [(_lib.PRECISION_MIXED, "mixed")]
-            if fp64:
-                runs.insert(0, (_lib.PRECISION_FP64, "fp64"))
+            runs = [(_lib.PRECISION_FP64, "fp64")] if fp64 else []
+            runs.append((_lib.PRECISION_MIXED, "mixed"))
             ref_x = None
             for prec, name in runs:
                 st, t = sv.solve(prec, bulk.data_ptr())
-                r[f"{name}_bulk"] = {"s": t, "iter": st.iter, "evals": st.evals,
-                                     "gnorm": st.gnorm, "status": st.status,
-                                     "converged": bool(st.converged) and st.status == 0}
+                r[f"{name}_bulk"] = rec(st, t)
                 if ref_x is None:
                     ref_x = torch.empty_like(mask)
                     check(sv.L.deft_cg_get_x(sv.cg[prec], ref_x.data_ptr(), 1))
-                t0 = time.perf_counter()
-                used, _ = net.initial_density(sv.fmt[prec], mask.data_ptr(), s.eta, s.nb,
-                                              n_ws.data_ptr(), floor_rel=floor_rel)
-                t_ws = time.perf_counter() - t0
-                st, t = sv.solve(prec, n_ws.data_ptr())
-                x = torch.empty_like(mask)
-                check(sv.L.deft_cg_get_x(sv.cg[prec], x.data_ptr(), 1))
-                dmax = float((x - ref_x).abs().max() / ref_x.abs().max())
-                r[f"{name}_warm"] = {"s": t + t_ws, "s_network": t_ws, "iter": st.iter,
-                                     "evals": st.evals, "gnorm": st.gnorm, "status": st.status,
-                                     "converged": bool(st.converged) and st.status == 0,
-                                     "used_network": used, "profile_rel_diff": dmax}
+                variants = switch if prec == _lib.PRECISION_MIXED else (None,)
+                for c in variants:
+                    t0 = time.perf_counter()
+                    used, _, gb = net.initial_density(sv.fmt[prec], mask.data_ptr(), s.eta, s.nb,
+                                                      n_ws.data_ptr(), floor_rel=floor_rel,
+                                                      bulk_gnorm=True)
+                    t_ws = time.perf_counter() - t0
+                    st, t = sv.solve(prec, n_ws.data_ptr(), refine_abs=c * gb if c else 0.0)
+                    check(sv.L.deft_cg_get_x(sv.cg[prec], x.data_ptr(), 1))
+                    dmax = float((x - ref_x).abs().max() / ref_x.abs().max())
+                    key = f"{name}_warm" if c is None else f"{name}_warm_abs{c:g}"
+                    r[key] = rec(st, t + t_ws, {"s_network": t_ws, "used_network": used,
+                                                "profile_rel_diff": dmax})
             recs.append(r)
     finally:
         sv.close()
@@ -315,7 +349,7 @@ def compare_starts(net, problems, device=0, fp64=True, floor_rel=1e-3):
 def summarize(recs):
     """Means over the problems every run converged on (failures counted
     separately, with their status codes)."""
-    keys = [k for k in ("fp64_bulk", "fp64_warm", "mixed_bulk", "mixed_warm") if k in recs[0]]
+    keys = [k for k in recs[0] if k.endswith("_bulk") or "_warm" in k]
     ok = [r for r in recs if all(r[k]["converged"] for k in keys)]
     out = {"problems": len(recs), "all_converged": len(ok)}
     for key in keys:
@@ -326,19 +360,20 @@ def summarize(recs):
                     "converged": int(sum(r[key]["converged"] for r in recs)),
                     "failures": [(i, r[key]["status"]) for i, r in enumerate(recs)
                                  if not r[key]["converged"]]}
-        if key.endswith("warm"):
+        if "_warm" in key:
             out[key]["used_network"] = int(sum(col("used_network")))
             out[key]["max_profile_rel_diff"] = float(np.max(col("profile_rel_diff")))
             out[key]["mean_network_s"] = float(np.mean(col("s_network")))
     if "fp64_bulk" in out:
-        out["speedup_warm_mixed_vs_fp64_bulk"] = (out["fp64_bulk"]["mean_s"]
-                                                  / out["mixed_warm"]["mean_s"])
         out["speedup_mixed_bulk_vs_fp64_bulk"] = (out["fp64_bulk"]["mean_s"]
                                                   / out["mixed_bulk"]["mean_s"])
-        out["speedup_warm_vs_bulk_fp64"] = out["fp64_bulk"]["mean_s"] / out["fp64_warm"]["mean_s"]
-    out["speedup_warm_vs_bulk_mixed"] = out["mixed_bulk"]["mean_s"] / out["mixed_warm"]["mean_s"]
-    out["iter_ratio_warm_vs_bulk_mixed"] = (out["mixed_warm"]["mean_iter"]
-                                            / out["mixed_bulk"]["mean_iter"])
+        out["speedup_fp64_warm_vs_fp64_bulk"] = (out["fp64_bulk"]["mean_s"]
+                                                 / out["fp64_warm"]["mean_s"])
+    for key in keys:
+        if key.startswith("mixed_warm"):
+            out[f"speedup_{key}_vs_fp64_bulk"] = (out["fp64_bulk"]["mean_s"] / out[key]["mean_s"]
+                                                  if "fp64_bulk" in out else None)
+            out[f"speedup_{key}_vs_mixed_bulk"] = out["mixed_bulk"]["mean_s"] / out[key]["mean_s"]
     return out
 
 
@@ -361,6 +396,12 @@ def main(argv=None):
     ap.add_argument("--fp64-held", type=int, default=None,
                     help="held-out problems also solved in FP64 (default: all)")
     ap.add_argument("--save", default=None, help="weight file to write")
+    ap.add_argument("--save-dtype", default="bfloat16", choices=["bfloat16", "float32"])
+    ap.add_argument("--load", default=None, help="weight file to start from (skips training "
+                                                  "unless --count > 0 is given as well)")
+    ap.add_argument("--switch", default="",
+                    help="comma-separated c values: mixed warm-start variants leaving the "
+                         "FP32 stage at c x the bulk start's gradient norm")
     ap.add_argument("--json", default=None, help="summary file to write")
     ap.add_argument("--device", type=int, default=0)
     a = ap.parse_args(argv)
@@ -370,33 +411,39 @@ def main(argv=None):
     def log(m):
         print(m, file=sys.stderr, flush=True)
 
-    t0 = time.perf_counter()
-    ds = make_dataset(walls_solutes_set(a.count, a.seed, N=a.N), device=a.device, log=log)
-    t_data = time.perf_counter() - t0
-    net = FourierOperator(a.N, a.channels, a.modes, a.layers, seed=a.seed, device=a.device)
-    t0 = time.perf_counter()
-    losses = train(net, ds, epochs=a.epochs, lr=a.lr, lr_final=a.lr_final, seed=a.seed, log=log,
-                   log_every=max(1, len(ds) // 4))
-    t_train = time.perf_counter() - t0
+    res = {}
+    if a.load:
+        net = FourierOperator.load(a.load, device=a.device)
+        res["network"] = dict(net.header(), loaded_from=a.load)
+    else:
+        net = FourierOperator(a.N, a.channels, a.modes, a.layers, seed=a.seed, device=a.device)
+        res["network"] = net.header()
+    if not a.load or a.count > 0:
+        t0 = time.perf_counter()
+        ds = make_dataset(walls_solutes_set(a.count, a.seed, N=net.N), device=a.device, log=log)
+        t_data = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        losses = train(net, ds, epochs=a.epochs, lr=a.lr, lr_final=a.lr_final, seed=a.seed,
+                       log=log, log_every=max(1, len(ds) // 4))
+        t_train = time.perf_counter() - t0
+        res["data"] = {"problems": a.count, "kept": len(ds), "seed": a.seed, "seconds": t_data,
+                       "mean_iter": float(np.mean([x[0] for x in ds.stats])),
+                       "form": "mixed solves refined on the FP64 gradient to |grad F| < 1e-9"}
+        res["training"] = {"steps": len(losses), "epochs": a.epochs, "seconds": t_train,
+                           "ms_per_step": t_train / max(1, len(losses)) * 1e3,
+                           "loss_first_epoch": float(np.mean(losses[:len(ds)])),
+                           "loss_last_epoch": float(np.mean(losses[-len(ds):]))}
+        del ds
     if a.save:
-        net.save(a.save)
-    held = walls_solutes_set(a.held, a.held_seed, N=a.N)
+        net.save(a.save, dtype=a.save_dtype)
+    switch = (None,) + tuple(float(c) for c in a.switch.split(",") if c)
+    held = walls_solutes_set(a.held, a.held_seed, N=net.N)
     nf = a.held if a.fp64_held is None else a.fp64_held
-    recs = compare_starts(net, held[:nf], device=a.device, fp64=True)
+    recs = compare_starts(net, held[:nf], device=a.device, fp64=True, switch=switch)
     if nf < len(held):
-        recs += compare_starts(net, held[nf:], device=a.device, fp64=False)
-    res = {
-        "network": net.header(),
-        "data": {"problems": a.count, "kept": len(ds), "seed": a.seed, "seconds": t_data,
-                 "mean_iter": float(np.mean([x[0] for x in ds.stats])),
-                 "form": "mixed solves refined on the FP64 gradient to |grad F| < 1e-9"},
-        "training": {"steps": len(losses), "epochs": a.epochs, "seconds": t_train,
-                     "ms_per_step": t_train / max(1, len(losses)) * 1e3,
-                     "loss_first_epoch": float(np.mean(losses[:len(ds)])),
-                     "loss_last_epoch": float(np.mean(losses[-len(ds):]))},
-        "held_out": {"seed": a.held_seed, **summarize(recs[:nf])},
-        "held_out_mixed_only": summarize(recs) if nf < len(recs) else None,
-    }
+        recs += compare_starts(net, held[nf:], device=a.device, fp64=False, switch=switch)
+    res["held_out"] = {"seed": a.held_seed, **summarize(recs[:nf])}
+    res["held_out_mixed_only"] = summarize(recs) if nf < len(recs) else None
     net.close()
     txt = json.dumps(res, indent=1)
     if a.json:

@@ -83,6 +83,9 @@ typedef struct {
                         (0 = default 1e-4) */
   int preconditioned; /* 1: PreconditionedConjugateGradient (src/ConjugateGradient.cpp:
                          115-160): directions from the preconditioned gradient */
+  double refine_abs; /* mixed evaluator only: if > 0, leave the FP32 stage once
+                        |grad| < refine_abs instead (e.g. a fraction of the bulk start's
+                        gradient norm when starting from a warm start) */
 } deft_cg_params;
 
 typedef struct {
@@ -139,6 +142,28 @@ int deft_grid_profile_count(deft_grid *grid);
 /* Synchronises, then gives kind i's name, launches and summed event time. */
 int deft_grid_profile_entry(deft_grid *grid, int i, const char **name, long long *launches,
                             double *total_ms);
+
+/* Launch shapes and FFT radix orders (no reference counterpart; chosen by
+ * the autotuner in deft_gb300/autotune.py).  tiles[6] = By, Bx, Bxf, Bxc,
+ * Pz, Pphi: columns per y-FFT tile, per plain x-FFT tile, per forward and
+ * adjoint convolution x tile, z-line pairs per r2c/c2r/gradient tile and per
+ * phi/Hessian tile; 0 keeps the built-in rule.  radix[24] (may be NULL) =
+ * three 8-entry radix orders for the x, y, z axes, each ending at its first 0
+ * (all 0 = built-in).  Results change only by rounding. */
+int deft_grid_set_tiles(deft_grid *grid, int precision, const int tiles[6], const int radix[24]);
+/* The effective choice (built-in values filled in). */
+int deft_grid_get_tiles(deft_grid *grid, int precision, int tiles[6], int radix[24]);
+/* CUDA graphs (no reference counterpart): with enable = 1 (the default) each
+ * evaluation's and Hessian-vector product's launch sequence is captured once
+ * per set of buffers and parameters and replayed as one graph launch; 0
+ * launches kernel by kernel.  Per-kernel timing (deft_grid_profile with
+ * timing = 1) always launches kernel by kernel. */
+int deft_grid_graphs(deft_grid *grid, int enable);
+/* Registers a choice for grids of shape N[3] in `precision`: every grid
+ * created afterwards with that shape (deft_grid_create, deft_batch_solve's
+ * grids) starts from it.  deft_tuning_clear forgets all entries. */
+int deft_tuning_set(const int N[3], int precision, const int tiles[6], const int radix[24]);
+int deft_tuning_clear(void);
 
 /* ---- functional ---- */
 int deft_fmt_create(deft_grid *grid, const deft_fmt_params *p, deft_fmt **out);
@@ -203,6 +228,9 @@ size_t deft_noalloc_scratch_bytes(void);
  * its own device copy of x; get/set move it. */
 int deft_cg_create(deft_fmt *f, const deft_cg_params *p, deft_cg **out);
 int deft_cg_destroy(deft_cg *cg);
+/* New parameters for an existing minimiser (no reference counterpart); they
+ * take effect from the next step, and deft_cg_set_x restarts as before. */
+int deft_cg_set_params(deft_cg *cg, const deft_cg_params *p);
 int deft_cg_set_x(deft_cg *cg, const double *n, int on_device);
 int deft_cg_get_x(deft_cg *cg, double *n, int on_device);
 /* Device pointer of the minimiser's x (valid until deft_cg_destroy). */
@@ -278,10 +306,11 @@ int deft_fno_warm_start(deft_fno *f, const double *mask_dev, double eta, double 
  * writes the network's density to n_out_dev unless it is non-finite or its
  * energy is above the bulk start's (nb on free points, 0 where mask == 0),
  * in which case the bulk start.  *used_network (may be NULL) = 1 or 0 says
- * which; *E_out (may be NULL) gets its energy. */
+ * which; *E_out (may be NULL) gets its energy, *gnorm_bulk_out (may be NULL)
+ * the norm of the bulk start's gradient (a scale for deft_cg_params.refine_abs). */
 int deft_fno_initial_density(deft_fno *f, deft_fmt *fmt, const double *mask_dev, double eta,
                              double nb, double floor_rel, double *n_out_dev, int *used_network,
-                             double *E_out);
+                             double *E_out, double *gnorm_bulk_out);
 
 #ifdef __cplusplus
 }

@@ -81,6 +81,7 @@ def test_eval_is_deterministic_and_device_inputs_agree():
 
 def test_training_reduces_loss_and_weights_round_trip(tmp_path):
     import torch
+    from deft_gb300.warmstart import FourierOperator
     N, C, m, L = 16, 8, 4, 2
     net = _net(N, C, m, L, seed=1)
     try:
@@ -93,9 +94,18 @@ def test_training_reduces_loss_and_weights_round_trip(tmp_path):
             net.train_step(a.data_ptr(), 0.3, b.data_ptr(), 3e-3)
         last = [net.loss_device(a.data_ptr(), 0.3, b.data_ptr()) for a, b in dev]
         assert np.mean(last) < 0.5 * np.mean(first), (first, last)
+        path16 = os.path.join(tmp_path, "w16.bin")
+        net.save(path16, dtype="bfloat16")
+        net16 = FourierOperator.load(path16)
+        try:
+            # the BF16 file holds exactly the values every pass uses
+            y_a, _, _ = net.eval(samples[1][0], 0.3)
+            y_b, _, _ = net16.eval(samples[1][0], 0.3)
+            assert np.array_equal(y_a, y_b)
+        finally:
+            net16.close()
         path = os.path.join(tmp_path, "w.bin")
         net.save(path)
-        from deft_gb300.warmstart import FourierOperator
         net2 = FourierOperator.load(path)
         try:
             assert np.array_equal(net2.get_params(), net.get_params())
@@ -149,7 +159,7 @@ def test_warm_start_falls_back_to_bulk():
         net2 = _net(12, 4, 3, 2)
         try:
             code = net2.L.deft_fno_initial_density(net2.h, f.h, mask.data_ptr(), 0.3, s.nb, 1e-3,
-                                                   out.data_ptr(), None, None)
+                                                   out.data_ptr(), None, None, None)
             assert code == _lib.ERR_ARG
         finally:
             net2.close()
@@ -160,9 +170,10 @@ def test_warm_start_falls_back_to_bulk():
         ctx.close()
 
 
-def _solve_from(f, n0_dev, precision):
+def _solve_from(f, n0_dev, precision, refine_abs=0.0):
     from .capi import CG
-    cg = CG(f, linesearch=_lib.LS_SECANT, gtol=1e-9, maxiter=20000, step=1.0)
+    cg = CG(f, linesearch=_lib.LS_SECANT, gtol=1e-9, maxiter=20000, step=1.0,
+            refine_abs=refine_abs)
     try:
         _lib.check(cg.L.deft_cg_set_x(cg.h, n0_dev.data_ptr(), 1))
         st = _lib.CgStatus()
@@ -196,11 +207,14 @@ def test_trained_warm_start_beats_bulk_start_on_held_out_problems():
             try:
                 mask = torch.tensor(s.mask.reshape(-1), device="cuda:0")
                 n_ws = torch.empty_like(mask)
-                used, _ = net.initial_density(f.h, mask.data_ptr(), s.eta, s.nb, n_ws.data_ptr())
+                used, _, g_bulk = net.initial_density(f.h, mask.data_ptr(), s.eta, s.nb,
+                                                      n_ws.data_ptr(), bulk_gnorm=True)
                 used_all.append(used)
                 n_b = torch.tensor(s.n0.reshape(-1), device="cuda:0")
                 ib, eb, gb, cb, xb = _solve_from(f, n_b, _lib.PRECISION_MIXED)
-                iw, ew, gw, cw, xw = _solve_from(f, n_ws, _lib.PRECISION_MIXED)
+                # leave the FP32 stage where the bulk start would (1e-4 of its gradient)
+                iw, ew, gw, cw, xw = _solve_from(f, n_ws, _lib.PRECISION_MIXED,
+                                                 refine_abs=1e-4 * g_bulk)
                 assert cb and cw and gb < 1e-9 and gw < 1e-9
                 assert np.max(np.abs(xb - xw)) <= 1e-8 * np.max(np.abs(xb)) + 1e-12
                 it_bulk.append(ib)
