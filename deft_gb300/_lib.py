@@ -34,7 +34,7 @@ EXPORTS = (
     "deft_cg_step", "deft_cg_solve", "deft_batch_solve",
     "deft_fno_create", "deft_fno_destroy", "deft_fno_param_count", "deft_fno_get_params",
     "deft_fno_set_params", "deft_fno_eval", "deft_fno_adam", "deft_fno_train_step",
-    "deft_fno_warm_start", "deft_fno_initial_density",
+    "deft_fno_warm_start", "deft_fno_initial_density", "deft_fno_launches",
 )
 
 
@@ -145,6 +145,7 @@ def load():
         "deft_fno_eval": (ctypes.c_int, [_vp, _dp, ctypes.c_float, _dp, ctypes.c_int, _dp, _dp,
                                          _dp]),
         "deft_fno_adam": (ctypes.c_int, [_vp, ctypes.c_float]),
+        "deft_fno_launches": (ctypes.c_longlong, [_vp]),
         "deft_fno_train_step": (ctypes.c_int, [_vp, _dp, ctypes.c_float, _dp, ctypes.c_int,
                                                ctypes.c_float, _dp]),
         "deft_fno_warm_start": (ctypes.c_int, [_vp, _dp, ctypes.c_double, ctypes.c_double,

@@ -561,6 +561,7 @@ struct deft_fno {
   float *part = nullptr;
   double *bulk = nullptr;    // 2 N^3 doubles (bulk start, its gradient), allocated on first use
   double *part_d = nullptr;  // kNormBlocks FP64 partial sums
+  long long launches = 0;    // kernel launches queued so far
   int nblk = 0;
   std::string err;
 };
@@ -640,6 +641,7 @@ void launch_project(deft_fno *f, float *zq, const float *target, const float *w,
 }
 
 void project(deft_fno *f, float *zq, const float *target, const float *w, float *part) {
+  f->launches++;
   if (f->C == 16) launch_project<16>(f, zq, target, w, part);
   else if (f->C == 8) launch_project<8>(f, zq, target, w, part);
   else launch_project<4>(f, zq, target, w, part);
@@ -647,6 +649,7 @@ void project(deft_fno *f, float *zq, const float *target, const float *w, float 
 
 int forward(deft_fno *f, float eta) {
   const int C = f->C;
+  f->launches += 1 + 8 * f->L;  // lift; per layer 7 spectral launches and the pointwise one
   k_lift<<<grid_for(f->NR), kT, 0, f->stream>>>(f->mask, eta, f->pb + f->oP, f->pb + f->op, f->h[0],
                                                C, f->NR);
   for (int l = 0; l < f->L; l++) {
@@ -890,6 +893,7 @@ int eval_impl(deft_fno *f, const float *mask, float eta, const float *target, cu
   }
   if (y_out) cudaMemcpyAsync(y_out, f->y, rb, kout, f->stream);
   if (want_grad && target) {
+    f->launches += 4 + 9 * f->L;  // projection, lift and layer backward passes with their sums
     cudaMemsetAsync(f->g, 0, sizeof(float) * f->nparam, f->stream);
     const float invW = (float)(1.0 / (W > 0 ? W : 1));
     // projection
@@ -943,6 +947,7 @@ int eval_impl(deft_fno *f, const float *mask, float eta, const float *target, cu
 
 int adam_impl(deft_fno *f, float lr) {
   f->adam_t++;
+  f->launches++;
   const float b1 = 0.9f, b2 = 0.999f;
   const float c1 = 1.f / (1.f - std::pow(b1, (float)f->adam_t));
   const float c2 = 1.f / (1.f - std::pow(b2, (float)f->adam_t));
@@ -1000,6 +1005,7 @@ int deft_fno_warm_start(deft_fno *f, const double *mask_dev, double eta, double 
   cudaSetDevice(f->device);
   const int C = f->C;
   k_d2f<<<grid_for(f->NR), kT, 0, f->stream>>>(mask_dev, f->mask, f->NR, 1.f);
+  f->launches += 2;  // this and the density below
   if (int s = forward(f, (float)eta)) return s;
   project(f, nullptr, nullptr, nullptr, nullptr);
   k_density<<<grid_for(f->NR), kT, 0, f->stream>>>(f->y, mask_dev, nb, floor_rel, n_out_dev,
@@ -1025,6 +1031,7 @@ int deft_fno_initial_density(deft_fno *f, deft_fmt *fmt, const double *mask_dev,
     return fno_fail(f, "bulk start buffer", DEFT_ERR_NOMEM);
   }
   k_bulk<<<grid_for(f->NR), kT, 0, f->stream>>>(mask_dev, nb, f->bulk, f->NR);
+  f->launches++;
   if (int s = deft_fno_warm_start(f, mask_dev, eta, nb, floor_rel, n_out_dev)) return s;
   double E0 = 0, E1 = 0;
   if (gnorm_bulk_out) {
@@ -1032,6 +1039,7 @@ int deft_fno_initial_density(deft_fno *f, deft_fmt *fmt, const double *mask_dev,
     double *gb = f->bulk + f->NR;
     if (int s = deft_fmt_energy_grad(fmt, f->bulk, 1, &E0, gb, nullptr)) return s;
     k_norm2_partial<<<kNormBlocks, kT, 0, f->stream>>>(gb, f->NR, f->part_d);
+    f->launches++;
     std::vector<double> h(kNormBlocks);
     cudaMemcpyAsync(h.data(), f->part_d, sizeof(double) * kNormBlocks, cudaMemcpyDeviceToHost,
                     f->stream);
@@ -1054,5 +1062,9 @@ int deft_fno_initial_density(deft_fno *f, deft_fmt *fmt, const double *mask_dev,
   if (E_out) *E_out = use ? E1 : E0;
   return DEFT_OK;
 }
+
+// Kernel launches this network has queued (forward, backward, Adam and warm
+// start kernels; the functional's own evaluations are counted by its grid).
+long long deft_fno_launches(const deft_fno *f) { return f ? f->launches : 0; }
 
 }  // extern "C"

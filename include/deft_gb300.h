@@ -308,6 +308,8 @@ int deft_fno_warm_start(deft_fno *f, const double *mask_dev, double eta, double 
  * in which case the bulk start.  *used_network (may be NULL) = 1 or 0 says
  * which; *E_out (may be NULL) gets its energy, *gnorm_bulk_out (may be NULL)
  * the norm of the bulk start's gradient (a scale for deft_cg_params.refine_abs). */
+/* Kernel launches the network has queued so far (its own kernels only). */
+long long deft_fno_launches(const deft_fno *f);
 int deft_fno_initial_density(deft_fno *f, deft_fmt *fmt, const double *mask_dev, double eta,
                              double nb, double floor_rel, double *n_out_dev, int *used_network,
                              double *E_out, double *gnorm_bulk_out);

