@@ -551,6 +551,46 @@ def run_reference(args, rank, world):
     }
 
 
+def kernel_case(precision, N, evals=3):
+    """A small fixed case for kernel profiling: `evals` energy+gradient
+    evaluations (and, in the mixed form, one Hessian-vector product) of the
+    N^3 hard-wall slit (dx = 0.2, eta = 0.3), about 0.5 GB on the device at
+    128^3."""
+    import torch
+    from deft_gb300 import _lib
+    from deft_gb300.workloads import Slit
+    L = _lib.load()
+    s = Slit(N=N, dx=0.2, eta=0.3, seed=1)
+    h = ctypes.c_void_p()
+    _lib.check(L.deft_ctx_create(0, ctypes.byref(h)))
+    ctx = h
+    lat = np.ascontiguousarray(s.lat.reshape(9))
+    h = ctypes.c_void_p()
+    _lib.check(L.deft_grid_create(ctx, lat.ctypes.data, *s.shape, ctypes.byref(h)))
+    grid = h
+    p = _lib.FmtParams(1.0, 1.0, s.mu, _lib.TERM_HS | _lib.TERM_IDEAL | _lib.TERM_MU |
+                       _lib.TERM_MASK, precision)
+    h = ctypes.c_void_p()
+    _lib.check(L.deft_fmt_create(grid, ctypes.byref(p), ctypes.byref(h)))
+    f = h
+    mask = torch.tensor(s.mask.reshape(-1), device="cuda:0")
+    _lib.check(L.deft_fmt_set_mask(f, mask.data_ptr(), 1))
+    n = torch.tensor(s.n0.reshape(-1), device="cuda:0")
+    g = torch.empty_like(n)
+    E = ctypes.c_double()
+    for _ in range(evals):
+        _lib.check(L.deft_fmt_energy_grad(f, n.data_ptr(), 1, ctypes.addressof(E), g.data_ptr(),
+                                          None))
+    if precision == _lib.PRECISION_MIXED:
+        _lib.check(L.deft_fmt_hessian_vector(f, n.data_ptr(), g.data_ptr(), 1, g.data_ptr()))
+    torch.cuda.synchronize()
+    L.deft_fmt_destroy(f)
+    L.deft_grid_destroy(grid)
+    L.deft_ctx_destroy(ctx)
+    return {"kernel_case": "mixed" if precision else "fp64", "N": N, "evals": evals,
+            "energy": E.value}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -565,7 +605,12 @@ def main():
     ap.add_argument("--no-extra", action="store_true", help="skip cuFFT and batched sweep")
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--verbose", action="store_true")
+    ap.add_argument("--kernel-case", default=None, choices=["mixed", "fp64"],
+                    help="only run the small kernel-profiling case and exit")
     args = ap.parse_args()
+    if args.kernel_case:
+        print(json.dumps(kernel_case(1 if args.kernel_case == "mixed" else 0, args.N)))
+        return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if world > 1 and args.impl == "ours":

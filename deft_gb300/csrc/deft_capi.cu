@@ -1310,3 +1310,155 @@ int deft_cg_solve(deft_cg *c, deft_cg_status *st) {
 }
 
 }  // extern "C"
+
+namespace {
+
+// Checkpoint layout: `path` holds the minimiser's device vectors as raw
+// little-endian FP64 (x, d, g_old, g, then pgrad if preconditioned), and
+// `path.json` a header with the grid shape, the vector list and every scalar
+// of the minimiser state, written with 17 significant digits so that the
+// state round-trips exactly.
+struct CgScalar {
+  const char *name;
+  double *d;
+  int *i;
+  bool *b;
+};
+
+std::vector<CgScalar> cg_scalars(deft_cg *c) {
+  return {{"iter", nullptr, &c->iter, nullptr},
+          {"evals", nullptr, &c->evals, nullptr},
+          {"have_g", nullptr, nullptr, &c->have_g},
+          {"E", &c->E, nullptr, nullptr},
+          {"gg", &c->gg, nullptr, nullptr},
+          {"ggold", &c->ggold, nullptr, nullptr},
+          {"goldsqr", &c->goldsqr, nullptr, nullptr},
+          {"pgoldsqr", &c->pgoldsqr, nullptr, nullptr},
+          {"s_prev", &c->s_prev, nullptr, nullptr},
+          {"alpha", &c->alpha, nullptr, nullptr},
+          {"step", &c->step, nullptr, nullptr},
+          {"oldgradsqr", &c->oldgradsqr, nullptr, nullptr},
+          {"e_valid", nullptr, nullptr, &c->e_valid},
+          {"e_cache", &c->e_cache, nullptr, nullptr},
+          {"dEdn", &c->dEdn, nullptr, nullptr},
+          {"log_ratio_avg", &c->log_ratio_avg, nullptr, nullptr},
+          {"deltaE", &c->deltaE, nullptr, nullptr},
+          {"err_est", &c->err_est, nullptr, nullptr},
+          {"done", nullptr, nullptr, &c->done},
+          {"stage", nullptr, &c->stage, nullptr},
+          {"evals_fp64", nullptr, &c->evals_fp64, nullptr},
+          {"hvps", nullptr, &c->hvps, nullptr},
+          {"g0norm", &c->g0norm, nullptr, nullptr},
+          {"last_eval_mixed", nullptr, nullptr, &c->last_eval_mixed}};
+}
+
+std::vector<double *> cg_vectors(deft_cg *c) {
+  std::vector<double *> v = {c->x, c->d, c->gold, c->g};
+  if (c->pg) v.push_back(c->pg);
+  return v;
+}
+
+// Reads `"key": value` from a flat JSON object.
+bool json_number(const std::string &js, const char *key, double *out) {
+  const std::string k = std::string("\"") + key + "\"";
+  size_t p = js.find(k);
+  if (p == std::string::npos) return false;
+  p = js.find(':', p + k.size());
+  if (p == std::string::npos) return false;
+  char *end = nullptr;
+  *out = std::strtod(js.c_str() + p + 1, &end);
+  return end != js.c_str() + p + 1;
+}
+
+}  // namespace
+
+extern "C" {
+
+int deft_cg_checkpoint(deft_cg *c, const char *path) {
+  if (!c || !path) return set_err(DEFT_ERR_ARG, "NULL argument");
+  deft_grid *g = c->f->grid;
+  cudaSetDevice(g->ctx->device);
+  if (int s = sync(g->ctx)) return s;
+  const size_t n = nr(g);
+  std::vector<double> host(n);
+  FILE *fb = std::fopen(path, "wb");
+  if (!fb) return set_err(DEFT_ERR_ARG, std::string("cannot write ") + path);
+  const std::vector<double *> vecs = cg_vectors(c);
+  for (double *v : vecs) {
+    cudaError_t e = cudaMemcpy(host.data(), v, sizeof(double) * n, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess || std::fwrite(host.data(), sizeof(double), n, fb) != n) {
+      std::fclose(fb);
+      return e != cudaSuccess ? cuda_err(e, "checkpoint copy")
+                              : set_err(DEFT_ERR_ARG, "checkpoint write failed");
+    }
+  }
+  std::fclose(fb);
+  const std::string hp = std::string(path) + ".json";
+  FILE *fh = std::fopen(hp.c_str(), "w");
+  if (!fh) return set_err(DEFT_ERR_ARG, "cannot write " + hp);
+  std::fprintf(fh, "{\"format\": \"deft_gb300 cg checkpoint\", \"dtype\": \"float64 "
+                   "little-endian\", \"vectors\": \"x d g_old g%s\", \"Nx\": %d, "
+                   "\"Ny\": %d, \"Nz\": %d, \"preconditioned\": %d",
+               c->pg ? " pgrad" : "", g->spec.Nx, g->spec.Ny, g->spec.Nz, c->pg ? 1 : 0);
+  for (const CgScalar &sc : cg_scalars(c)) {
+    if (sc.d) std::fprintf(fh, ", \"%s\": %.17g", sc.name, *sc.d);
+    else if (sc.i) std::fprintf(fh, ", \"%s\": %d", sc.name, *sc.i);
+    else std::fprintf(fh, ", \"%s\": %d", sc.name, *sc.b ? 1 : 0);
+  }
+  std::fprintf(fh, "}\n");
+  std::fclose(fh);
+  return DEFT_OK;
+}
+
+int deft_cg_restore(deft_cg *c, const char *path) {
+  if (!c || !path) return set_err(DEFT_ERR_ARG, "NULL argument");
+  deft_grid *g = c->f->grid;
+  cudaSetDevice(g->ctx->device);
+  const std::string hp = std::string(path) + ".json";
+  FILE *fh = std::fopen(hp.c_str(), "r");
+  if (!fh) return set_err(DEFT_ERR_ARG, "cannot read " + hp);
+  std::string js;
+  char buf[4096];
+  size_t k;
+  while ((k = std::fread(buf, 1, sizeof(buf), fh)) > 0) js.append(buf, k);
+  std::fclose(fh);
+  double v;
+  const int shape[3] = {g->spec.Nx, g->spec.Ny, g->spec.Nz};
+  const char *axes[3] = {"Nx", "Ny", "Nz"};
+  for (int a = 0; a < 3; a++)
+    if (!json_number(js, axes[a], &v) || (int)v != shape[a])
+      return set_err(DEFT_ERR_ARG, "checkpoint grid does not match the minimiser's");
+  if (!json_number(js, "preconditioned", &v) || (v != 0) != (c->pg != nullptr))
+    return set_err(DEFT_ERR_ARG, "checkpoint preconditioning does not match the minimiser's");
+  for (const CgScalar &sc : cg_scalars(c))
+    if (!json_number(js, sc.name, &v)) return set_err(DEFT_ERR_ARG, "checkpoint header incomplete");
+  const size_t n = nr(g);
+  std::vector<double> host(n);
+  FILE *fb = std::fopen(path, "rb");
+  if (!fb) return set_err(DEFT_ERR_ARG, std::string("cannot read ") + path);
+  if (int s = sync(g->ctx)) {
+    std::fclose(fb);
+    return s;
+  }
+  for (double *dv : cg_vectors(c)) {
+    if (std::fread(host.data(), sizeof(double), n, fb) != n) {
+      std::fclose(fb);
+      return set_err(DEFT_ERR_ARG, "checkpoint data truncated");
+    }
+    cudaError_t e = cudaMemcpy(dv, host.data(), sizeof(double) * n, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+      std::fclose(fb);
+      return cuda_err(e, "checkpoint copy");
+    }
+  }
+  std::fclose(fb);
+  for (const CgScalar &sc : cg_scalars(c)) {
+    json_number(js, sc.name, &v);
+    if (sc.d) *sc.d = v;
+    else if (sc.i) *sc.i = (int)v;
+    else *sc.b = v != 0;
+  }
+  return DEFT_OK;
+}
+
+}  // extern "C"

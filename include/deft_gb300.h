@@ -240,6 +240,13 @@ double *deft_cg_x_device(deft_cg *cg);
 int deft_cg_step(deft_cg *cg, deft_cg_status *st);
 /* improve_energy() until converged, an error, or maxiter. */
 int deft_cg_solve(deft_cg *cg, deft_cg_status *st);
+/* Checkpoint / resume (no reference counterpart): `path` gets the
+ * minimiser's vectors (x, direction, previous gradient, gradient[, pgrad]) as
+ * raw little-endian FP64 and `path`.json a header with the grid shape and
+ * every scalar of its state; restoring into a minimiser of the same grid and
+ * settings continues the run bit-identically. */
+int deft_cg_checkpoint(deft_cg *cg, const char *path);
+int deft_cg_restore(deft_cg *cg, const char *path);
 
 /* ---- batched solves ----
  * Many independent state points and uneven grids on one GPU (no reference
