@@ -1016,13 +1016,23 @@ int step_newton(deft_cg *c, deft_cg_status *st, const deft::FmtSpec &spec) {
   }
   c->iter++;
   if (e->hess_setup(spec, c->x)) return eng_err(e);
-  // r = -g (in gold), p = r (in d), dx = 0
+  // Preconditioned linear CG on H dx = -g with M^-1 = n / (kT dV) (the
+  // inverse ideal-gas curvature, which spans orders of magnitude between
+  // walls, contacts and bulk): r = -g (in gold), z (in pg or g), p = z (in d)
   double *r = c->gold, *p = c->d, *q = c->q, *dx = c->dxv;
-  if (e->scal_add(0.0, r, -1.0, c->g) || e->copy(r, p)) return eng_err(e);
+  double *z = c->g;  // the FP64 gradient is re-evaluated after the step
+  if (e->scal_add(0.0, r, -1.0, c->g)) return eng_err(e);
+  if (e->diag_precond(spec, c->x, r, c->f->mask, z) || e->copy(z, p)) return eng_err(e);
+  c->have_g = false;
   if (cudaMemsetAsync(dx, 0, bytes, stream) != cudaSuccess) return set_err(DEFT_ERR_CUDA, "memset");
-  double rr = c->gg;
+  double rz;
+  {
+    const double *a[1] = {r};
+    const double *b[1] = {z};
+    if (e->dots(1, a, b, &rz)) return eng_err(e);
+  }
   const double tol = std::fmax(1e-5 * st->gnorm, 0.05 * c->p.gtol);
-  for (int k = 0; k < 400; k++) {
+  for (int k = 0; k < 400 && rz > 0; k++) {
     if (e->hvp(spec, p, c->f->mask, q)) return eng_err(e);
     c->hvps++;
     double pq;
@@ -1032,17 +1042,18 @@ int step_newton(deft_cg *c, deft_cg_status *st, const deft::FmtSpec &spec) {
       if (e->dots(1, a, b, &pq)) return eng_err(e);
     }
     if (!(pq > 0)) break;  // no positive curvature along p: keep the step so far
-    const double alpha = rr / pq;
+    const double alpha = rz / pq;
     if (e->axpy(alpha, p, dx) || e->axpy(-alpha, q, r)) return eng_err(e);
-    double rr_new;
+    if (e->diag_precond(spec, c->x, r, c->f->mask, z)) return eng_err(e);
+    double o[2];
     {
-      const double *a[1] = {r};
-      const double *b[1] = {r};
-      if (e->dots(1, a, b, &rr_new)) return eng_err(e);
+      const double *a[2] = {r, r};
+      const double *b[2] = {r, z};
+      if (e->dots(2, a, b, o)) return eng_err(e);
     }
-    if (std::sqrt(rr_new) < tol) break;
-    if (e->scal_add(rr_new / rr, p, 1.0, r)) return eng_err(e);
-    rr = rr_new;
+    if (std::sqrt(o[0]) < tol) break;
+    if (e->scal_add(o[1] / rz, p, 1.0, z)) return eng_err(e);
+    rz = o[1];
   }
   const double E0 = c->E;
   double scale = 1.0;

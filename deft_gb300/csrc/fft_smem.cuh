@@ -33,6 +33,7 @@ struct FftPlan {
   int radix[kMaxPasses];
   FastDiv ns[kMaxPasses];  // product of the radices of the earlier passes
   const void *tw;          // device table, n entries of Cplx<T>
+  int reg;                 // 1: register-resident two-stage transform (radix order 16, n/16)
 };
 
 // Fills ns[] once radix[] and npass are set.
@@ -188,6 +189,159 @@ __device__ void fft_pass_generic(const typename Cplx<T>::type *__restrict__ src,
       dst[(base + o * Ns) * B + bl] = acc;
     }
   }
+}
+
+// (x + iy) (cr + i ci)
+template <typename C, typename T> __device__ __forceinline__ C c_mulc(C a, T cr, T ci) {
+  return C{a.x * cr - a.y * ci, a.x * ci + a.y * cr};
+}
+
+// 16-point DFT in registers, natural order in and out: 4 x 4 with the
+// inner factors exp(SIGN 2 pi i m / 16).
+template <int SIGN, typename T, typename C> __device__ __forceinline__ void dft16(C *v) {
+  const T c1 = T(0.92387953251128675613), s1 = T(0.38268343236508977173);
+  const T h = T(0.70710678118654752440), sg = T(SIGN);
+#pragma unroll
+  for (int j1 = 0; j1 < 4; j1++) dft4<SIGN>(v[j1], v[j1 + 4], v[j1 + 8], v[j1 + 12]);
+  // v[j1 + 4 k2] now holds a[j1][k2]; times exp(SIGN 2 pi i j1 k2 / 16)
+  v[5] = c_mulc(v[5], c1, sg * s1);     // m = 1
+  v[9] = c_mulc(v[9], h, sg * h);       // m = 2
+  v[13] = c_mulc(v[13], s1, sg * c1);   // m = 3
+  v[6] = c_mulc(v[6], h, sg * h);       // m = 2
+  v[10] = c_mul_si<SIGN>(v[10]);        // m = 4
+  v[14] = c_mulc(v[14], -h, sg * h);    // m = 6
+  v[7] = c_mulc(v[7], s1, sg * c1);     // m = 3
+  v[11] = c_mulc(v[11], -h, sg * h);    // m = 6
+  v[15] = c_mulc(v[15], -c1, -sg * s1); // m = 9
+  C o[16];
+#pragma unroll
+  for (int k2 = 0; k2 < 4; k2++) {
+    // element j1 of row k2 sits at v[j1 + 4 k2] after the first stage
+    C w0 = v[4 * k2], w1 = v[4 * k2 + 1], w2 = v[4 * k2 + 2], w3 = v[4 * k2 + 3];
+    dft4<SIGN>(w0, w1, w2, w3);
+    o[k2] = w0;
+    o[k2 + 4] = w1;
+    o[k2 + 8] = w2;
+    o[k2 + 12] = w3;
+  }
+#pragma unroll
+  for (int k = 0; k < 16; k++) v[k] = o[k];
+}
+
+template <int SIGN, typename T, typename C, int M> __device__ __forceinline__ void dft_m(C *v) {
+  if constexpr (M == 2) dft2<SIGN>(v[0], v[1]);
+  else if constexpr (M == 3) dft3<SIGN, T>(v);
+  else if constexpr (M == 4) dft4<SIGN>(v[0], v[1], v[2], v[3]);
+  else if constexpr (M == 5) dft5<SIGN, T>(v);
+  else if constexpr (M == 8) dft8<SIGN, T>(v);
+  else dft16<SIGN, T>(v);
+}
+
+// Register-resident transform of the B lines of an element-major tile
+// s[e*B + b] of length N = 16 M, in place.  M consecutive threads own a
+// line: thread t loads x[t + M j] (j < 16), does a 16-point DFT in
+// registers, applies exp(SIGN 2 pi i t k1 / N), exchanges through the tile
+// (rows k1 M + t) and does M-point DFTs for its 16/M values of k1, writing
+// X[k1 + 16 k2].  When M divides 32 a line's threads share a warp and the
+// exchanges need only __syncwarp (otherwise __syncthreads; every thread runs
+// the same number of sweeps); 256 threads per block.  Ends with
+// __syncthreads().
+template <typename T, int SIGN, int N>
+__device__ void fft_tile_reg(typename Cplx<T>::type *s, int B,
+                             const typename Cplx<T>::type *__restrict__ tw) {
+  using C = typename Cplx<T>::type;
+  constexpr int M = N / 16, KP = 16 / M > 0 ? 16 / M : 1;
+  static_assert(16 % M == 0 || M == 3 || M == 5, "unsupported length");
+  constexpr int LPB = 256 / M;  // lines per sweep of the block
+  const int t = threadIdx.x % M, grp = threadIdx.x / M;
+  const int sweeps = (B + LPB - 1) / LPB;
+  auto line_sync = []() {
+    if constexpr (32 % M == 0) __syncwarp();
+    else __syncthreads();
+  };
+  __syncthreads();
+  for (int sw = 0; sw < sweeps; sw++) {
+    const int b = sw * LPB + grp;
+    const bool act = b < B && grp < LPB;
+    C v[16];
+#pragma unroll
+    for (int j = 0; j < 16; j++) v[j] = act ? s[(t + M * j) * B + b] : C{0, 0};
+    dft16<SIGN, T>(v);
+    if (t) {
+#pragma unroll
+      for (int k1 = 1; k1 < 16; k1++) v[k1] = c_mul(v[k1], tw_load<SIGN>(tw, t * k1));
+    }
+    line_sync();
+    if (act) {
+#pragma unroll
+      for (int k1 = 0; k1 < 16; k1++) s[(k1 * M + t) * B + b] = v[k1];
+    }
+    line_sync();
+    if constexpr (M == 3 || M == 5) {
+      // 16 values of k1 over M threads: thread t takes k1 = t, t + M, ...
+      C w[6 * M];
+#pragma unroll
+      for (int i = 0; i < (16 + M - 1) / M; i++) {
+        const int k1 = t + M * i;
+#pragma unroll
+        for (int t2 = 0; t2 < M; t2++)
+          w[i * M + t2] = (act && k1 < 16) ? s[(k1 * M + t2) * B + b] : C{0, 0};
+        dft_m<SIGN, T, C, M>(&w[i * M]);
+      }
+      line_sync();
+      if (act) {
+#pragma unroll
+        for (int i = 0; i < (16 + M - 1) / M; i++) {
+          const int k1 = t + M * i;
+          if (k1 < 16) {
+#pragma unroll
+            for (int k2 = 0; k2 < M; k2++) s[(k1 + 16 * k2) * B + b] = w[i * M + k2];
+          }
+        }
+      }
+    } else {
+      C w[16];
+#pragma unroll
+      for (int i = 0; i < KP; i++) {
+#pragma unroll
+        for (int t2 = 0; t2 < M; t2++)
+          w[i * M + t2] = act ? s[((t * KP + i) * M + t2) * B + b] : C{0, 0};
+        dft_m<SIGN, T, C, M>(&w[i * M]);
+      }
+      line_sync();
+      if (act) {
+#pragma unroll
+        for (int i = 0; i < KP; i++) {
+#pragma unroll
+          for (int k2 = 0; k2 < M; k2++) s[((t * KP + i) + 16 * k2) * B + b] = w[i * M + k2];
+        }
+      }
+    }
+    line_sync();
+  }
+  __syncthreads();
+}
+
+template <typename T, int SIGN>
+__device__ bool fft_tile_reg_dispatch(typename Cplx<T>::type *a, const FastDiv &bd,
+                                      const FftPlan &p) {
+  using C = typename Cplx<T>::type;
+  const C *tw = reinterpret_cast<const C *>(p.tw);
+  const int B = (int)bd.d;
+  switch (p.n) {
+    case 32: fft_tile_reg<T, SIGN, 32>(a, B, tw); return true;
+    case 48: fft_tile_reg<T, SIGN, 48>(a, B, tw); return true;
+    case 64: fft_tile_reg<T, SIGN, 64>(a, B, tw); return true;
+    case 80: fft_tile_reg<T, SIGN, 80>(a, B, tw); return true;
+    case 128: fft_tile_reg<T, SIGN, 128>(a, B, tw); return true;
+    case 256: fft_tile_reg<T, SIGN, 256>(a, B, tw); return true;
+    default: return false;
+  }
+}
+
+// Lengths the register-resident transform handles (n = 16 M).
+inline bool reg_fft_length(int n) {
+  return n == 32 || n == 48 || n == 64 || n == 80 || n == 128 || n == 256;
 }
 
 // Transforms a tile of B lines held in `a`; `b` is scratch of the same size.

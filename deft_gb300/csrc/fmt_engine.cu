@@ -105,6 +105,32 @@ __device__ void block_reduce(double (&v)[K], double *smem /* 32*K */) {
   }
 }
 
+// Per-block energy partials of the six terms: warp sums in the kernel's
+// arithmetic type T (no FP64 work per thread in the FP32 kernels), then the
+// warps' sums in FP64 in a fixed order, scaled by kT (phi, ideal gas), mu, 1.
+template <typename T, typename LA>
+__device__ void block_reduce_terms(T (&t)[6], const LA &la, double *red /* 32*6 */,
+                                   double *partials) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < 6; k++) {
+    T x = t[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if (lane == 0) red[warp * 6 + k] = double(x);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const double scale[6] = {la.kT, la.kT, la.kT, la.kT, la.mu, 1.0};
+    const int nw = (blockDim.x + 31) >> 5;
+    for (int k = 0; k < 6; k++) {
+      double sum = 0;
+      for (int w = 0; w < nw; w++) sum += red[w * 6 + k];
+      partials[(size_t)blockIdx.x * 6 + k] = scale[k] * sum;
+    }
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Kernels
 
@@ -133,6 +159,7 @@ __device__ __forceinline__ void pack_c2r(const typename Cplx<T>::type *__restric
   // element k of pair pb: idx = pb * Nz + k
   using C = typename Cplx<T>::type;
   const int Nz = g.Nz, NzH = g.NzH;
+  #pragma unroll 4
   for (int idx = threadIdx.x; idx < P * Nz; idx += blockDim.x) {
     int pb, k;
     fdivmod(idx, g.fNz, pb, k);
@@ -164,6 +191,7 @@ __device__ __forceinline__ void unpack_r2c_store(const typename Cplx<T>::type *r
                                                  const Geom &g, int p0, int P, T s) {
   using C = typename Cplx<T>::type;
   const int Nz = g.Nz, NzH = g.NzH;
+  #pragma unroll 4
   for (int idx = threadIdx.x; idx < 2 * P * NzH; idx += blockDim.x) {
     int ll, k;
     fdivmod(idx, g.fNzH, ll, k);
@@ -193,6 +221,7 @@ __global__ void __launch_bounds__(kThreads) k_z_r2c(const double *__restrict__ i
   const int p0 = blockIdx.x * P;
   in += (size_t)blockIdx.y * g.NR;
   out += (size_t)blockIdx.y * g.NC;
+  #pragma unroll 4
   for (int idx = threadIdx.x; idx < 2 * P * g.Nz; idx += blockDim.x) {
     int ll, z;
     fdivmod(idx, g.fNz, ll, z);
@@ -219,6 +248,7 @@ __global__ void __launch_bounds__(kThreads) k_z_c2r(const typename Cplx<T>::type
   out += (size_t)blockIdx.y * g.NR;
   pack_c2r<T>(in, buf0, g, p0, P);
   C *res = fft_tile<T, +1>(buf0, buf1, fP, pz);
+  #pragma unroll 4
   for (int idx = threadIdx.x; idx < 2 * P * g.Nz; idx += blockDim.x) {
     int ll, z;
     fdivmod(idx, g.fNz, ll, z);
@@ -240,6 +270,7 @@ __global__ void __launch_bounds__(kThreads) k_y_fft(typename Cplx<T>::type *data
   C *buf1 = buf0 + g.Ny * B;
   const int kz0 = blockIdx.x * B;
   C *base = data + (size_t)blockIdx.z * g.NC + (size_t)blockIdx.y * g.Ny * g.NzH;
+  #pragma unroll 4
   for (int idx = threadIdx.x; idx < g.Ny * B; idx += blockDim.x) {
     int e, b;
     fdivmod(idx, fB, e, b);
@@ -247,6 +278,7 @@ __global__ void __launch_bounds__(kThreads) k_y_fft(typename Cplx<T>::type *data
     buf0[idx] = kz < g.NzH ? base[(size_t)e * g.NzH + kz] : C{0, 0};
   }
   C *res = fft_tile<T, SIGN>(buf0, buf1, fB, py);
+  #pragma unroll 4
   for (int idx = threadIdx.x; idx < g.Ny * B; idx += blockDim.x) {
     int e, b;
     fdivmod(idx, fB, e, b);
@@ -266,6 +298,7 @@ __global__ void __launch_bounds__(kThreads) k_x_fft(typename Cplx<T>::type *data
   C *buf1 = buf0 + g.Nx * B;
   const int J = g.Ny * g.NzH;
   const int j0 = blockIdx.x * B;
+  #pragma unroll 4
   for (int idx = threadIdx.x; idx < g.Nx * B; idx += blockDim.x) {
     int e, j;
     fdivmod(idx, fB, e, j);
@@ -273,6 +306,7 @@ __global__ void __launch_bounds__(kThreads) k_x_fft(typename Cplx<T>::type *data
     buf0[idx] = j < J ? data[(size_t)e * J + j] : C{0, 0};
   }
   C *res = fft_tile<T, SIGN>(buf0, buf1, fB, px);
+  #pragma unroll 4
   for (int idx = threadIdx.x; idx < g.Nx * B; idx += blockDim.x) {
     int e, j;
     fdivmod(idx, fB, e, j);
@@ -297,6 +331,7 @@ __global__ void __launch_bounds__(kThreads) k_x_conv_fwd(
   C *bufC = bufB + g.Nx * B;
   const int J = g.Ny * g.NzH;
   const int j0 = blockIdx.x * B;
+  #pragma unroll 4
   for (int idx = threadIdx.x; idx < g.Nx * B; idx += blockDim.x) {
     int e, j;
     fdivmod(idx, fB, e, j);
@@ -307,6 +342,7 @@ __global__ void __launch_bounds__(kThreads) k_x_conv_fwd(
   C *F1 = (R0 == bufA) ? bufB : bufA;
   C *F2 = bufC;
   for (int a = 0; a < 5; a++) {
+    #pragma unroll 4
     for (int idx = threadIdx.x; idx < g.Nx * B; idx += blockDim.x) {
       int e, j;
       fdivmod(idx, fB, e, j);
@@ -332,6 +368,7 @@ __global__ void __launch_bounds__(kThreads) k_x_conv_fwd(
     }
     const C *res = fft_tile<T, +1>(F1, F2, fB, px);
     C *dst = out5 + (size_t)a * g.NC;
+    #pragma unroll 4
     for (int idx = threadIdx.x; idx < g.Nx * B; idx += blockDim.x) {
       int e, j;
       fdivmod(idx, fB, e, j);
@@ -357,6 +394,7 @@ __global__ void __launch_bounds__(kThreads) k_x_conv_adj(
   const int J = g.Ny * g.NzH;
   const int j0 = blockIdx.x * B;
   const int B5 = 5 * B;
+  #pragma unroll 4
   for (int idx = threadIdx.x; idx < g.Nx * B5; idx += blockDim.x) {
     int e, bb, a, b;
     fdivmod(idx, f5B, e, bb);
@@ -366,6 +404,7 @@ __global__ void __launch_bounds__(kThreads) k_x_conv_adj(
   }
   const C *R = fft_tile<T, -1>(X, Y, f5B, px);
   C *A = (R == X) ? Y : X;  // layout e*B + b
+  #pragma unroll 4
   for (int idx = threadIdx.x; idx < g.Nx * B; idx += blockDim.x) {
     int e, b;
     fdivmod(idx, fB, e, b);
@@ -391,6 +430,7 @@ __global__ void __launch_bounds__(kThreads) k_x_conv_adj(
     A[idx] = o;
   }
   const C *res = fft_tile<T, +1>(A, const_cast<C *>(R), fB, px);
+  #pragma unroll 4
   for (int idx = threadIdx.x; idx < g.Nx * B; idx += blockDim.x) {
     int e, j;
     fdivmod(idx, fB, e, j);
@@ -436,6 +476,7 @@ __device__ typename Cplx<T>::type *z_load5_c2r(const typename Cplx<T>::type *__r
                                                const FastDiv &f5P, int p0) {
   using C = typename Cplx<T>::type;
   const int P = (int)fP.d, P5 = 5 * P, Nz = g.Nz, NzH = g.NzH;
+  #pragma unroll 4
   for (int idx = threadIdx.x; idx < P5 * Nz; idx += blockDim.x) {
     int b, k, a, pb;
     fdivmod(idx, g.fNz, b, k);
@@ -472,6 +513,7 @@ __device__ void z_r2c_store5(typename Cplx<T>::type *res, typename Cplx<T>::type
   using C = typename Cplx<T>::type;
   const int P = (int)fP.d, P5 = 5 * P, Nz = g.Nz, NzH = g.NzH;
   const C *out = fft_tile<T, -1>(res, other, f5P, pz);
+  #pragma unroll 4
   for (int idx = threadIdx.x; idx < 10 * P * NzH; idx += blockDim.x) {
     int lb, k, a, ll;
     fdivmod(idx, g.fNzH, lb, k);
@@ -511,6 +553,7 @@ __global__ void __launch_bounds__(kThreads) k_z_phi(typename Cplx<T>::type *S5,
   const bool hs = la.terms & kTermHS;
   const T inv_nQ = T(la.inv_nQ);
   const T c = T(la.dV * la.kT);
+  #pragma unroll 4
   for (int idx = threadIdx.x; idx < 2 * P * Nz; idx += blockDim.x) {
     int ll, z;
     fdivmod(idx, g.fNz, ll, z);
@@ -538,12 +581,7 @@ __global__ void __launch_bounds__(kThreads) k_z_phi(typename Cplx<T>::type *S5,
       for (int a = 0; a < 5; a++) cell[a * fstride] = c * d[a];
     }
   }
-  double acc[kNumTerms] = {la.kT * double(tacc[0]), la.kT * double(tacc[1]),
-                           la.kT * double(tacc[2]), la.kT * double(tacc[3]),
-                           la.mu * double(tacc[4]), double(tacc[5])};
-  block_reduce<kNumTerms>(acc, red);
-  if (threadIdx.x == 0)
-    for (int t = 0; t < kNumTerms; t++) partials[(size_t)blockIdx.x * kNumTerms + t] = acc[t];
+  block_reduce_terms<T>(tacc, la, red, partials);
   if (!GRAD) return;
   __syncthreads();
   z_r2c_store5<T>(res, res == A ? Bf : A, S5, g, pz, fP, f2P, f5P, p0);
@@ -569,6 +607,7 @@ __global__ void __launch_bounds__(kThreads) k_z_grad(const typename Cplx<T>::typ
     pack_c2r<T>(in, buf0, g, p0, P);
     res = fft_tile<T, +1>(buf0, buf1, fP, pz);
   }
+  #pragma unroll 4
   for (int idx = threadIdx.x; idx < 2 * P * g.Nz; idx += blockDim.x) {
     int ll, z;
     fdivmod(idx, g.fNz, ll, z);
@@ -613,6 +652,7 @@ __global__ void __launch_bounds__(kThreads) k_z_hess(const typename Cplx<T>::typ
   const int p0 = blockIdx.x * P;
   C *res = z_load5_c2r<T>(S5, A, Bf, g, pz, fP, f5P, p0);
   const bool hs = la.terms & kTermHS;
+  #pragma unroll 4
   for (int idx = threadIdx.x; idx < 2 * P * Nz; idx += blockDim.x) {
     int ll, z;
     fdivmod(idx, g.fNz, ll, z);
@@ -650,6 +690,7 @@ __global__ void __launch_bounds__(kThreads) k_z_jac(typename Cplx<T>::type *S5, 
   const int p0 = blockIdx.x * P;
   C *res = z_load5_c2r<T>(S5, A, Bf, g, pz, fP, f5P, p0);
   const T cc = T(c);
+  #pragma unroll 4
   for (int idx = threadIdx.x; idx < 2 * P * Nz; idx += blockDim.x) {
     int ll, z;
     fdivmod(idx, g.fNz, ll, z);
@@ -696,6 +737,7 @@ __global__ void __launch_bounds__(kThreads) k_z_hvp_out(
     pack_c2r<T>(in, buf0, g, p0, P);
     res = fft_tile<T, +1>(buf0, buf1, fP, pz);
   }
+  #pragma unroll 4
   for (int idx = threadIdx.x; idx < 2 * P * g.Nz; idx += blockDim.x) {
     int ll, z;
     fdivmod(idx, g.fNz, ll, z);
@@ -831,6 +873,18 @@ __global__ void k_scal_add(double beta, double *d, double alpha, const double *g
   if (blockIdx.x == 0 && threadIdx.x == 0 && (n & 1)) d[n - 1] = alpha * g[n - 1] + beta * d[n - 1];
 }
 
+// Jacobi preconditioner of the Newton step's linear CG: z = r n / (kT dV),
+// the inverse of the ideal-gas curvature kT dV / n (0 where masked or n <= 0).
+__global__ void k_diag_precond(const double *__restrict__ n, const double *__restrict__ r,
+                               const double *__restrict__ mask, double inv_c,
+                               double *__restrict__ z, int N) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+    const double m = mask ? mask[i] : 1.0;
+    const double nv = n[i];
+    z[i] = (m == 0 || !(nv > 0)) ? 0.0 : r[i] * nv * inv_c;
+  }
+}
+
 // Effective-potential parametrisation (OfEffectivePotential,
 // src/EffectivePotentialToDensity.cpp:28-91): n = exp(-Veff / kT).
 __global__ void k_veff_density(double inv_kT, const double *__restrict__ x, double *__restrict__ n,
@@ -858,6 +912,7 @@ __global__ void k_veff_grad(double kT, const double *__restrict__ x, const doubl
 bool factorize(int n, FftPlan &p) {
   int k = 0;
   p.n = n;
+  p.reg = 0;
   while (n % 8 == 0 && k < kMaxPasses) { p.radix[k++] = 8; n /= 8; }
   while (n % 4 == 0 && k < kMaxPasses) { p.radix[k++] = 4; n /= 4; }
   while (n % 2 == 0 && k < kMaxPasses) { p.radix[k++] = 2; n /= 2; }
@@ -988,6 +1043,19 @@ bool set_radix_order(FftPlan &p, const int *r) {
   p.npass = k;
   for (int i = 0; i < k; i++) p.radix[i] = tmp[i];
   plan_fill_ns(p);
+  p.reg = 0;
+  return true;
+}
+
+// The register-resident transform is selected with the radix order
+// {16, n/16} (n = 32, 48, 64, 80, 128, 256).
+bool set_reg_order(FftPlan &p, const int *r) {
+  if (!(r[0] == 16 && r[1] > 0 && r[2] == 0 && 16 * r[1] == p.n && reg_fft_length(p.n)))
+    return false;
+  p.reg = 1;
+  p.npass = 2;
+  p.radix[0] = 16;
+  p.radix[1] = r[1];
   return true;
 }
 
@@ -997,12 +1065,14 @@ constexpr size_t kBudget32 = 72 * 1024;
 enum KernelId {
   kK_z_r2c, kK_z_c2r, kK_y_fft1, kK_y_fft5, kK_x_fft, kK_x_conv_fwd, kK_x_conv_adj, kK_z_phi_grad,
   kK_z_phi_energy, kK_z_grad, kK_local_energy, kK_reduce_terms, kK_dots, kK_axpy, kK_scal_add,
-  kK_weight_table, kK_z_hess, kK_z_jac, kK_z_hvp_out, kK_veff_density, kK_veff_grad, kNumKernels
+  kK_weight_table, kK_z_hess, kK_z_jac, kK_z_hvp_out, kK_veff_density, kK_veff_grad,
+  kK_diag_precond, kNumKernels
 };
 const char *const kKernelNames[kNumKernels] = {
     "z_r2c", "z_c2r", "y_fft_1field", "y_fft_5fields", "x_fft", "x_conv_fwd", "x_conv_adj", "z_phi_grad",
     "z_phi_energy", "z_grad", "local_energy", "reduce_terms", "dots", "axpy", "scal_add",
-    "weight_table", "z_hess", "z_jac", "z_hvp_out", "veff_density", "veff_grad"};
+    "weight_table", "z_hess", "z_jac", "z_hvp_out", "veff_density", "veff_grad",
+    "diag_precond"};
 
 class EngineImpl {
  public:
@@ -1714,6 +1784,16 @@ void Engine::set_graphs(bool on) {
   impl_->use_graphs = on;
 }
 void Engine::get_tiles(int prec, TileChoice *c) const { impl_->get_tiles(prec, c); }
+
+int Engine::diag_precond(const FmtSpec &f, const double *n, const double *r, const double *mask,
+                         double *z) {
+  EngineImpl &e = *impl_;
+  e.pre(kK_diag_precond);
+  k_diag_precond<<<e.dot_blocks, kThreads, 0, e.stream>>>(n, r, mask, 1.0 / (f.kT * e.g.dV), z,
+                                                          e.g.NR);
+  e.post(kK_diag_precond);
+  return e.check("diag_precond");
+}
 
 int Engine::veff_density(double kT, const double *x, double *n) {
   EngineImpl &e = *impl_;

@@ -118,6 +118,11 @@ class Engine {
   int hess_setup(const FmtSpec &f, const double *n);
   int hvp(const FmtSpec &f, const double *dx, const double *mask, double *out);
 
+  // z = r n / (kT dV): the inverse ideal-gas curvature applied to r (0 where
+  // masked), the preconditioner of the Newton step's linear CG.
+  int diag_precond(const FmtSpec &f, const double *n, const double *r, const double *mask,
+                   double *z);
+
   // Vector kernels (NR-long device vectors).
   // out_host[i] = a_i . b_i for i < k (k <= 3), one pass, one sync.
   int dots(int k, const double *const *a, const double *const *b, double *out_host);
