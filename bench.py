@@ -48,11 +48,12 @@ UNIT = "s"
 GTOL = 1e-9
 HELD_SEED = 6
 TRAIN_SEED = 5
-# Mean energy+gradient evaluations of the plain FP64 solve from the bulk
-# density over 200 held-out problems of this family at 128^3 (169.1,
-# measured on GB300; the CPU port runs the same algorithm).  The reference
-# arm scales its per-evaluation time by it.
-FP64_EVALS = {128: 169.1}
+# Energy+gradient evaluations of the plain FP64 solve from the bulk density
+# of held-out problems 0..15 at 128^3 (measured on GB300; the CPU port runs
+# the same CG), and the mean over 200 held-out problems for later ones.  The
+# reference arm scales each step's per-evaluation time by its problem's count.
+FP64_EVALS_128 = [149, 100, 104, 83, 40, 50, 157, 322, 360, 142, 101, 439, 38, 368, 65, 66]
+FP64_EVALS_MEAN_128 = 169.1
 HBM_FALLBACK_GBS = 6800.0
 
 
@@ -104,7 +105,7 @@ class Clocks:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "100"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -387,7 +388,7 @@ def run_ours(args, rank, world):
     mask_host = [torch.tensor(s.mask.reshape(-1)).pin_memory() for s in probs]
     out_host = torch.empty(probs[0].size, dtype=torch.float64).pin_memory()
     mask_dev = torch.empty_like(masks[0])
-    K2 = max(1, min(args.steps, 3))
+    K2 = args.steps  # the timed steps' problems
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for k in range(K2):
@@ -516,15 +517,22 @@ def run_reference(args, rank, world):
     if rank != 0:
         return None
     N = args.N
-    evals = FP64_EVALS.get(N, 169.1)
     probs = held_out(N, args.steps + args.warmup)
+
+    def evals_of(i):
+        if N == 128 and i < len(FP64_EVALS_128):
+            return FP64_EVALS_128[i]
+        return FP64_EVALS_MEAN_128
+
     for i in range(args.warmup):
         cpu_eval_seconds(probs[i], budget_s=0.0, max_evals=1)
     samples = []
     t0 = time.perf_counter()
     for k in range(args.steps):
-        sec, _k = cpu_eval_seconds(probs[args.warmup + k], budget_s=0.0, max_evals=1)
-        samples.append(sec * evals)
+        i = args.warmup + k
+        sec, _k = cpu_eval_seconds(probs[i], budget_s=0.0, max_evals=1)
+        samples.append(sec * evals_of(i))
+    evals = sum(evals_of(args.warmup + k) for k in range(args.steps)) / args.steps
     wall = time.perf_counter() - t0
     v = sum(samples) / len(samples)
     return {
@@ -545,22 +553,24 @@ def run_reference(args, rank, world):
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
                          "sample": f"per step: one energy+gradient evaluation of the step's "
                                    f"held-out {N}^3 problem by the oracle port (plain-C "
-                                   f"restatement of the reference path), scaled by the {evals} "
-                                   f"evaluations of a converged FP64 solve"},
+                                   f"restatement of the reference path), scaled by that "
+                                   f"problem's evaluation count for a converged FP64 solve "
+                                   f"(mean {evals:.1f})"},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 
 
-def kernel_case(precision, N, evals=3):
+def kernel_case(precision, N, problem="slit", evals=3):
     """A small fixed case for kernel profiling: `evals` energy+gradient
     evaluations (and, in the mixed form, one Hessian-vector product) of the
-    N^3 hard-wall slit (dx = 0.2, eta = 0.3), about 0.5 GB on the device at
-    128^3."""
+    N^3 hard-wall slit (dx = 0.2, eta = 0.3) or of the first timed held-out
+    wall + solute problem, about 0.5 GB on the device at 128^3; per-kernel
+    event times of the evaluations are returned."""
     import torch
     from deft_gb300 import _lib
     from deft_gb300.workloads import Slit
     L = _lib.load()
-    s = Slit(N=N, dx=0.2, eta=0.3, seed=1)
+    s = Slit(N=N, dx=0.2, eta=0.3, seed=1) if problem == "slit" else held_out(N, 4)[3]
     h = ctypes.c_void_p()
     _lib.check(L.deft_ctx_create(0, ctypes.byref(h)))
     ctx = h
@@ -583,18 +593,24 @@ def kernel_case(precision, N, evals=3):
                                           None))
     if precision == _lib.PRECISION_MIXED:
         _lib.check(L.deft_fmt_hessian_vector(f, n.data_ptr(), g.data_ptr(), 1, g.data_ptr()))
+    _lib.check(L.deft_grid_profile(grid, 1))
+    for _ in range(evals):
+        _lib.check(L.deft_fmt_energy_grad(f, n.data_ptr(), 1, ctypes.addressof(E), g.data_ptr(),
+                                          None))
+    prof = kernel_profile(L, grid)
     torch.cuda.synchronize()
     L.deft_fmt_destroy(f)
     L.deft_grid_destroy(grid)
     L.deft_ctx_destroy(ctx)
-    return {"kernel_case": "mixed" if precision else "fp64", "N": N, "evals": evals,
-            "energy": E.value}
+    return {"kernel_case": "mixed" if precision else "fp64", "problem": problem, "N": N,
+            "evals": evals, "energy": E.value,
+            "us_per_launch": {k: round(1e3 * v[1] / v[0], 2) for k, v in prof.items()}}
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--N", type=int, default=128)
@@ -607,9 +623,11 @@ def main():
     ap.add_argument("--verbose", action="store_true")
     ap.add_argument("--kernel-case", default=None, choices=["mixed", "fp64"],
                     help="only run the small kernel-profiling case and exit")
+    ap.add_argument("--case-problem", default="slit", choices=["slit", "solutes"])
     args = ap.parse_args()
     if args.kernel_case:
-        print(json.dumps(kernel_case(1 if args.kernel_case == "mixed" else 0, args.N)))
+        print(json.dumps(kernel_case(1 if args.kernel_case == "mixed" else 0, args.N,
+                                     args.case_problem)))
         return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
