@@ -197,7 +197,18 @@ def kernel_table(prof):
             for k, v in sorted(prof.items(), key=lambda kv: -kv[1][1])}
 
 
+def by_precision(prof, fp32):
+    """The profile entries of one arithmetic type, under their kernel names
+    (FP32 launches carry a "_f32" suffix in the engine's accounting)."""
+    out = {}
+    for k, v in prof.items():
+        if k.endswith("_f32") == fp32:
+            out[k[:-4] if fp32 else k] = v
+    return out
+
+
 def roofline(prof, N, fp32, peak, peak_kind):
+    prof = by_precision(prof, fp32)
     ab = alg_bytes(N, fp32)
     dom = max((k for k in prof if k in ab), key=lambda k: prof[k][1])
     dom_ms = prof[dom][1] / prof[dom][0]

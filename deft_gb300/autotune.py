@@ -135,8 +135,10 @@ class _Bench:
         for i in range(L.deft_grid_profile_count(self.grid)):
             check(L.deft_grid_profile_entry(self.grid, i, ctypes.byref(name),
                                             ctypes.addressof(launches), ctypes.addressof(tot)))
-            if launches.value:
-                out[name.value.decode()] = tot.value
+            nm = name.value.decode()
+            # FP32 launches carry "_f32" in the engine's accounting
+            if launches.value and nm.endswith("_f32") == (self.precision == _lib.PRECISION_MIXED):
+                out[nm[:-4] if nm.endswith("_f32") else nm] = tot.value
         check(L.deft_grid_profile(self.grid, 0))
         return out
 

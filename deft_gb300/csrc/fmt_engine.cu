@@ -1074,11 +1074,17 @@ const char *const kKernelNames[kNumKernels] = {
     "weight_table", "z_hess", "z_jac", "z_hvp_out", "veff_density", "veff_grad",
     "diag_precond"};
 
+// Accounting slot of kernel kind `id` in the arithmetic type T: FP32
+// launches are counted apart from FP64 ones (slots kNumKernels and up), so a
+// mixed solve's FP64 refinement does not blend into the FP32 kernels' times.
+template <typename T> constexpr int kslot(int id) { return sizeof(T) == 4 ? id + kNumKernels : id; }
+constexpr int kNumSlots = 2 * kNumKernels;
+
 class EngineImpl {
  public:
   // kernel accounting
-  long long launches[kNumKernels] = {};
-  double total_ms[kNumKernels] = {};
+  long long launches[kNumSlots] = {};
+  double total_ms[kNumSlots] = {};
   bool timing = false;
   std::vector<cudaEvent_t> pool;
   std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
@@ -1346,9 +1352,9 @@ class EngineImpl {
       if (!w3f && (alloc(&w3f, sizeof(float) * g.NC) || alloc(&w2f, sizeof(float) * g.NC) ||
                    alloc(&wvf, sizeof(float) * g.NC)))
         return -1;
-      pre(kK_weight_table);
+      pre(kslot<float>(kK_weight_table));
       k_weight_table<float><<<nb, kThreads, 0, stream>>>(g, R, w3f, w2f, wvf);
-      post(kK_weight_table);
+      post(kslot<float>(kK_weight_table));
       table_Rf = R;
     } else {
       if (R == table_R) return 0;
@@ -1424,7 +1430,7 @@ class EngineImpl {
   template <typename T> void y_fft(typename Cplx<T>::type *data, int nf, int sign) {
     const Tiles &t = tl<T>();
     dim3 grid((g.NzH + t.By - 1) / t.By, g.Nx, nf);
-    const int kid = nf == 1 ? kK_y_fft1 : kK_y_fft5;
+    const int kid = kslot<T>(nf == 1 ? kK_y_fft1 : kK_y_fft5);
     pre(kid);
     if (sign < 0)
       k_y_fft<T, -1><<<grid, kThreads, t.smem_y, stream>>>(data, g, plan<T>(1), t.fBy);
@@ -1438,15 +1444,15 @@ class EngineImpl {
   // for f.R must be current: ensure_table runs outside any graph capture).
   template <typename T> int forward_weighted(const FmtSpec &f, const double *n) {
     const Tiles &t = tl<T>();
-    pre(kK_z_r2c);
+    pre(kslot<T>(kK_z_r2c));
     k_z_r2c<T><<<dim3(pairs_tiles(t.Pz), 1), kThreads, t.smem_z, stream>>>(
         n, spec0<T>(), g, plan<T>(2), t.fPz, T(1));
-    post(kK_z_r2c);
+    post(kslot<T>(kK_z_r2c));
     y_fft<T>(spec0<T>(), 1, -1);
-    pre(kK_x_conv_fwd);
+    pre(kslot<T>(kK_x_conv_fwd));
     k_x_conv_fwd<T><<<x_tiles(t.Bxf), kThreads, t.smem_xf, stream>>>(
         spec0<T>(), spec5<T>(), table<T>(0), table<T>(1), table<T>(2), g, plan<T>(0), t.fBxf);
-    post(kK_x_conv_fwd);
+    post(kslot<T>(kK_x_conv_fwd));
     y_fft<T>(spec5<T>(), 5, +1);
     return check("forward convolution");
   }
@@ -1478,7 +1484,7 @@ class EngineImpl {
   struct GraphEntry {
     GraphKey key;
     cudaGraphExec_t exec;
-    long long counts[kNumKernels];
+    long long counts[kNumSlots];
   };
   std::vector<GraphEntry> graphs;
   bool use_graphs = true;
@@ -1508,7 +1514,7 @@ class EngineImpl {
   int replay(GraphEntry &e) {
     cudaError_t r = cudaGraphLaunch(e.exec, stream);
     if (r != cudaSuccess) return fail("graph launch", r);
-    for (int i = 0; i < kNumKernels; i++) launches[i] += e.counts[i];
+    for (int i = 0; i < kNumSlots; i++) launches[i] += e.counts[i];
     return 0;
   }
 
@@ -1516,7 +1522,7 @@ class EngineImpl {
     if (timing || !use_graphs) return launch();
     for (GraphEntry &e : graphs)
       if (!memcmp(&e.key, &key, sizeof(key))) return replay(e);
-    long long before[kNumKernels];
+    long long before[kNumSlots];
     memcpy(before, launches, sizeof(before));
     cudaError_t r = cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal);
     if (r != cudaSuccess) {
@@ -1529,7 +1535,7 @@ class EngineImpl {
     r = cudaStreamEndCapture(stream, &graph);
     GraphEntry e;
     e.key = key;
-    for (int i = 0; i < kNumKernels; i++) {
+    for (int i = 0; i < kNumSlots; i++) {
       e.counts[i] = launches[i] - before[i];
       launches[i] = before[i];
     }
@@ -1586,35 +1592,35 @@ class EngineImpl {
     if (f.terms & kTermHS) {
       if (forward_weighted<T>(f, n)) return -1;
       nblk = pairs_tiles(t.Pphi);
-      pre(grad ? kK_z_phi_grad : kK_z_phi_energy);
+      pre(kslot<T>(grad ? kK_z_phi_grad : kK_z_phi_energy));
       if (grad)
         k_z_phi<T, true><<<nblk, kThreads, t.smem_phi, stream>>>(
             spec5<T>(), n, V, g, plan<T>(2), t.fPphi, t.f2Pphi, t.f5Pphi, la, partials);
       else
         k_z_phi<T, false><<<nblk, kThreads, t.smem_phi, stream>>>(
             spec5<T>(), n, V, g, plan<T>(2), t.fPphi, t.f2Pphi, t.f5Pphi, la, partials);
-      post(grad ? kK_z_phi_grad : kK_z_phi_energy);
+      post(kslot<T>(grad ? kK_z_phi_grad : kK_z_phi_energy));
       if (check("phi")) return -1;
       if (grad) {
         y_fft<T>(spec5<T>(), 5, -1);
-        pre(kK_x_conv_adj);
+        pre(kslot<T>(kK_x_conv_adj));
         k_x_conv_adj<T><<<x_tiles(t.Bxc), kThreads, t.smem_xc, stream>>>(
             spec5<T>(), spec0<T>(), table<T>(0), table<T>(1), table<T>(2), g, plan<T>(0),
             t.fBxc, t.f5Bxc);
-        post(kK_x_conv_adj);
+        post(kslot<T>(kK_x_conv_adj));
         y_fft<T>(spec0<T>(), 1, +1);
       }
     } else {
       nblk = 4 * 152;
-      pre(kK_local_energy);
+      pre(kslot<T>(kK_local_energy));
       k_local_energy<T><<<nblk, kThreads, 0, stream>>>(n, V, g, la, partials);
-      post(kK_local_energy);
+      post(kslot<T>(kK_local_energy));
     }
     if (grad) {
-      pre(kK_z_grad);
+      pre(kslot<T>(kK_z_grad));
       k_z_grad<T><<<pairs_tiles(t.Pz), kThreads, t.smem_z, stream>>>(
           spec0<T>(), n, V, mask, grad, g, plan<T>(2), t.fPz, la);
-      post(kK_z_grad);
+      post(kslot<T>(kK_z_grad));
     }
     if (check("gradient")) return -1;
     queue_energy(nblk);
@@ -1628,10 +1634,10 @@ class EngineImpl {
     if (f.terms & kTermHS) {
       if (ensure_table<float>(f.R) || forward_weighted<float>(f, n)) return -1;
     }
-    pre(kK_z_hess);
+    pre(kslot<float>(kK_z_hess));
     k_z_hess<float><<<pairs_tiles(t32.Pphi), kThreads, t32.smem_phi, stream>>>(
         spec5<float>(), n, g, plan<float>(2), t32.fPphi, t32.f5Pphi, la, hess, hloc);
-    post(kK_z_hess);
+    post(kslot<float>(kK_z_hess));
     return check("hessian blocks");
   }
 
@@ -1645,23 +1651,23 @@ class EngineImpl {
     const LocalArgs la = local_args(f);
     if (f.terms & kTermHS) {
       if (forward_weighted<float>(f, dx)) return -1;
-      pre(kK_z_jac);
+      pre(kslot<float>(kK_z_jac));
       k_z_jac<float><<<pairs_tiles(t32.Pphi), kThreads, t32.smem_phi, stream>>>(
           spec5<float>(), g, plan<float>(2), t32.fPphi, t32.f2Pphi, t32.f5Pphi, g.dV * f.kT,
           hess);
-      post(kK_z_jac);
+      post(kslot<float>(kK_z_jac));
       y_fft<float>(spec5<float>(), 5, -1);
-      pre(kK_x_conv_adj);
+      pre(kslot<float>(kK_x_conv_adj));
       k_x_conv_adj<float><<<x_tiles(t32.Bxc), kThreads, t32.smem_xc, stream>>>(
           spec5<float>(), spec0<float>(), table<float>(0), table<float>(1), table<float>(2), g,
           plan<float>(0), t32.fBxc, t32.f5Bxc);
-      post(kK_x_conv_adj);
+      post(kslot<float>(kK_x_conv_adj));
       y_fft<float>(spec0<float>(), 1, +1);
     }
-    pre(kK_z_hvp_out);
+    pre(kslot<float>(kK_z_hvp_out));
     k_z_hvp_out<float><<<pairs_tiles(t32.Pz), kThreads, t32.smem_z, stream>>>(
         spec0<float>(), dx, hloc, mask, out, g, plan<float>(2), t32.fPz, la);
-    post(kK_z_hvp_out);
+    post(kslot<float>(kK_z_hvp_out));
     return check("hessian-vector product");
   }
 
@@ -1824,21 +1830,35 @@ void Engine::profile_reset(bool timing) {
   EngineImpl &e = *impl_;
   cudaStreamSynchronize(e.stream);
   e.harvest();
-  for (int i = 0; i < kNumKernels; i++) {
+  for (int i = 0; i < kNumSlots; i++) {
     e.launches[i] = 0;
     e.total_ms[i] = 0;
   }
   e.timing = timing;
 }
 
-int Engine::profile_kinds() const { return kNumKernels; }
+int Engine::profile_kinds() const { return kNumSlots; }
+
+// Names of the accounting slots: the kernel kind, with "_f32" for the FP32
+// launches of kernels that exist in both arithmetic types.
+const char *slot_name(int i) {
+  static std::string names[kNumSlots];
+  static std::once_flag once;
+  std::call_once(once, [] {
+    for (int k = 0; k < kNumKernels; k++) {
+      names[k] = kKernelNames[k];
+      names[k + kNumKernels] = std::string(kKernelNames[k]) + "_f32";
+    }
+  });
+  return names[i].c_str();
+}
 
 void Engine::profile_get(int i, const char **name, long long *launches, double *total_ms) {
   EngineImpl &e = *impl_;
   cudaStreamSynchronize(e.stream);
   e.harvest();
-  if (i < 0 || i >= kNumKernels) return;
-  if (name) *name = kKernelNames[i];
+  if (i < 0 || i >= kNumSlots) return;
+  if (name) *name = slot_name(i);
   if (launches) *launches = e.launches[i];
   if (total_ms) *total_ms = e.total_ms[i];
 }
