@@ -243,7 +243,8 @@ def get_network(args, N, dev, log):
         net = FourierOperator.load(args.weights, device=dev)
         return net, {"source": args.weights}
     t0 = time.perf_counter()
-    ds = make_dataset(walls_solutes_set(args.train_count, TRAIN_SEED, N=N), device=dev)
+    ds = make_dataset(walls_solutes_set(args.train_count, TRAIN_SEED, N=N), device=dev,
+                      workers=args.train_workers)
     t_data = time.perf_counter() - t0
     net = FourierOperator(N, 16, 12, 4, seed=TRAIN_SEED, device=dev)
     t0 = time.perf_counter()
@@ -628,6 +629,8 @@ def main():
     ap.add_argument("--weights", default=None, help="warm-start network weight file")
     ap.add_argument("--train-count", type=int, default=256)
     ap.add_argument("--train-epochs", type=int, default=2)
+    ap.add_argument("--train-workers", type=int, default=8,
+                    help="concurrent streams generating the training solves")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extra", action="store_true", help="skip cuFFT and batched sweep")
     ap.add_argument("--cpu-budget", type=float, default=20.0)

@@ -40,6 +40,9 @@ AXIS_KERNELS = (
     ("y_fft_1field", "y_fft_5fields"),
     ("z_r2c", "z_phi_grad", "z_phi_energy", "z_grad", "z_hess", "z_jac", "z_hvp_out"),
 )
+# tile widths tried per parameter (those that do not fit in shared memory are
+# refused by deft_grid_set_tiles and skipped)
+CANDIDATES = tuple(range(1, 17)) + (20, 24, 28, 32, 40, 48, 64)
 BUNDLED = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tuning_gb300.json")
 
 
@@ -170,7 +173,7 @@ def tune(shape, precision=_lib.PRECISION_MIXED, device=0, repeats=4, trials=2, l
                 continue  # plain x FFTs only serve deft_grid_fft / ifft
             kern = KERNELS[p]
             best_v, best_c = int(tiles[pi]), cost(kern)
-            for v in range(1, 17):
+            for v in CANDIDATES:
                 if v == best_v:
                     continue
                 cand = tiles.copy()
@@ -187,6 +190,8 @@ def tune(shape, precision=_lib.PRECISION_MIXED, device=0, repeats=4, trials=2, l
         N = shape
         for a in range(3):
             orders = radix_orders(N[a])
+            if precision == _lib.PRECISION_MIXED and N[a] in (32, 64, 128, 256):
+                orders = [[16, N[a] // 16]] + orders  # register-resident transform
             if len(orders) < 2:
                 continue
             cur = [int(v) for v in radix[8 * a:8 * a + 8] if v]

@@ -322,34 +322,22 @@ __device__ void fft_tile_reg(typename Cplx<T>::type *s, int B,
   __syncthreads();
 }
 
-template <typename T, int SIGN>
-__device__ bool fft_tile_reg_dispatch(typename Cplx<T>::type *a, const FastDiv &bd,
-                                      const FftPlan &p) {
-  using C = typename Cplx<T>::type;
-  const C *tw = reinterpret_cast<const C *>(p.tw);
-  const int B = (int)bd.d;
-  switch (p.n) {
-    case 32: fft_tile_reg<T, SIGN, 32>(a, B, tw); return true;
-    case 48: fft_tile_reg<T, SIGN, 48>(a, B, tw); return true;
-    case 64: fft_tile_reg<T, SIGN, 64>(a, B, tw); return true;
-    case 80: fft_tile_reg<T, SIGN, 80>(a, B, tw); return true;
-    case 128: fft_tile_reg<T, SIGN, 128>(a, B, tw); return true;
-    case 256: fft_tile_reg<T, SIGN, 256>(a, B, tw); return true;
-    default: return false;
-  }
-}
-
-// Lengths the register-resident transform handles (n = 16 M).
-inline bool reg_fft_length(int n) {
-  return n == 32 || n == 48 || n == 64 || n == 80 || n == 128 || n == 256;
-}
+// Lengths the register-resident transform is instantiated for (n = 16 M).
+inline bool reg_fft_length(int n) { return n == 32 || n == 64 || n == 128 || n == 256; }
 
 // Transforms a tile of B lines held in `a`; `b` is scratch of the same size.
-// Returns the buffer that holds the result.  Ends with __syncthreads().
-template <typename T, int SIGN>
+// Returns the buffer that holds the result.  Ends with __syncthreads().  RN > 0
+// selects the register-resident transform of length RN (in place in `a`);
+// kernels are instantiated per RN so that the register cost of that path
+// never lands on the shared-memory one.
+template <typename T, int SIGN, int RN = 0>
 __device__ typename Cplx<T>::type *fft_tile(typename Cplx<T>::type *a, typename Cplx<T>::type *b,
                                             const FastDiv &bd, const FftPlan &p) {
   using C = typename Cplx<T>::type;
+  if constexpr (RN > 0) {
+    fft_tile_reg<T, SIGN, RN>(a, (int)bd.d, reinterpret_cast<const C *>(p.tw));
+    return a;
+  }
   const C *tw = reinterpret_cast<const C *>(p.tw);
   C *src = a, *dst = b;
   __syncthreads();

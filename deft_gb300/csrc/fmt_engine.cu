@@ -209,8 +209,8 @@ __device__ __forceinline__ void unpack_r2c_store(const typename Cplx<T>::type *r
 }
 
 // Real fields -> half-complex along z.  grid.x = pair tiles, grid.y = field.
-template <typename T>
-__global__ void __launch_bounds__(kThreads) k_z_r2c(const double *__restrict__ in,
+template <typename T, int RN = 0>
+__global__ void __launch_bounds__(kThreads, RN > 0 ? 2 : 1) k_z_r2c(const double *__restrict__ in,
                                                     typename Cplx<T>::type *__restrict__ out,
                                                     Geom g, FftPlan pz, FastDiv fP, T s) {
   const int P = (int)fP.d;
@@ -229,7 +229,7 @@ __global__ void __launch_bounds__(kThreads) k_z_r2c(const double *__restrict__ i
     const T v = line < g.lines ? T(in[(size_t)line * g.Nz + z]) : T(0);
     reinterpret_cast<T *>(&buf0[z * P + (ll >> 1)])[ll & 1] = v;
   }
-  C *res = fft_tile<T, -1>(buf0, buf1, fP, pz);
+  C *res = fft_tile<T, -1, RN>(buf0, buf1, fP, pz);
   unpack_r2c_store<T>(res, out, g, p0, P, s);
 }
 
@@ -260,8 +260,8 @@ __global__ void __launch_bounds__(kThreads) k_z_c2r(const typename Cplx<T>::type
 }
 
 // FFT along y of complex fields.  grid = (kz tiles, Nx, fields).
-template <typename T, int SIGN>
-__global__ void __launch_bounds__(kThreads) k_y_fft(typename Cplx<T>::type *data, Geom g,
+template <typename T, int SIGN, int RN = 0>
+__global__ void __launch_bounds__(kThreads, RN > 0 ? 2 : 1) k_y_fft(typename Cplx<T>::type *data, Geom g,
                                                     FftPlan py, FastDiv fB) {
   const int B = (int)fB.d;
   using C = typename Cplx<T>::type;
@@ -277,7 +277,7 @@ __global__ void __launch_bounds__(kThreads) k_y_fft(typename Cplx<T>::type *data
     const int kz = kz0 + b;
     buf0[idx] = kz < g.NzH ? base[(size_t)e * g.NzH + kz] : C{0, 0};
   }
-  C *res = fft_tile<T, SIGN>(buf0, buf1, fB, py);
+  C *res = fft_tile<T, SIGN, RN>(buf0, buf1, fB, py);
   #pragma unroll 4
   for (int idx = threadIdx.x; idx < g.Ny * B; idx += blockDim.x) {
     int e, b;
@@ -318,8 +318,8 @@ __global__ void __launch_bounds__(kThreads) k_x_fft(typename Cplx<T>::type *data
 // x-FFT of n^, multiplication by the five weights, and the five inverse
 // x-FFTs one field at a time (three tiles of B lines: the forward result and
 // a ping-pong pair), which keeps B wide for coalesced column runs.
-template <typename T>
-__global__ void __launch_bounds__(kThreads) k_x_conv_fwd(
+template <typename T, int RN = 0>
+__global__ void __launch_bounds__(kThreads, RN > 0 ? 2 : 1) k_x_conv_fwd(
     const typename Cplx<T>::type *__restrict__ in, typename Cplx<T>::type *__restrict__ out5,
     const T *__restrict__ w3, const T *__restrict__ w2, const T *__restrict__ wv, Geom g,
     FftPlan px, FastDiv fB) {
@@ -338,7 +338,7 @@ __global__ void __launch_bounds__(kThreads) k_x_conv_fwd(
     j += j0;
     bufA[idx] = j < J ? in[(size_t)e * J + j] : C{0, 0};
   }
-  const C *R0 = fft_tile<T, -1>(bufA, bufB, fB, px);
+  const C *R0 = fft_tile<T, -1, RN>(bufA, bufB, fB, px);
   C *F1 = (R0 == bufA) ? bufB : bufA;
   C *F2 = bufC;
   for (int a = 0; a < 5; a++) {
@@ -366,7 +366,7 @@ __global__ void __launch_bounds__(kThreads) k_x_conv_fwd(
       }
       F1[idx] = o;
     }
-    const C *res = fft_tile<T, +1>(F1, F2, fB, px);
+    const C *res = fft_tile<T, +1, RN>(F1, F2, fB, px);
     C *dst = out5 + (size_t)a * g.NC;
     #pragma unroll 4
     for (int idx = threadIdx.x; idx < g.Nx * B; idx += blockDim.x) {
@@ -381,8 +381,8 @@ __global__ void __launch_bounds__(kThreads) k_x_conv_fwd(
 
 // x-FFT of the five partial spectra at once, times the adjoint weights
 // (odd ones negated), summed over the fields, inverse x-FFT of the sum.
-template <typename T>
-__global__ void __launch_bounds__(kThreads) k_x_conv_adj(
+template <typename T, int RN = 0>
+__global__ void __launch_bounds__(kThreads, RN > 0 ? 2 : 1) k_x_conv_adj(
     const typename Cplx<T>::type *__restrict__ in5, typename Cplx<T>::type *__restrict__ out,
     const T *__restrict__ w3, const T *__restrict__ w2, const T *__restrict__ wv, Geom g,
     FftPlan px, FastDiv fB, FastDiv f5B) {
@@ -402,7 +402,7 @@ __global__ void __launch_bounds__(kThreads) k_x_conv_adj(
     const int j = j0 + b;
     X[idx] = j < J ? in5[(size_t)a * g.NC + (size_t)e * J + j] : C{0, 0};
   }
-  const C *R = fft_tile<T, -1>(X, Y, f5B, px);
+  const C *R = fft_tile<T, -1, RN>(X, Y, f5B, px);
   C *A = (R == X) ? Y : X;  // layout e*B + b
   #pragma unroll 4
   for (int idx = threadIdx.x; idx < g.Nx * B; idx += blockDim.x) {
@@ -429,7 +429,7 @@ __global__ void __launch_bounds__(kThreads) k_x_conv_adj(
     }
     A[idx] = o;
   }
-  const C *res = fft_tile<T, +1>(A, const_cast<C *>(R), fB, px);
+  const C *res = fft_tile<T, +1, RN>(A, const_cast<C *>(R), fB, px);
   #pragma unroll 4
   for (int idx = threadIdx.x; idx < g.Nx * B; idx += blockDim.x) {
     int e, j;
@@ -468,7 +468,7 @@ __device__ __forceinline__ T ideal_energy_t(T x, T inv_nQ) {
 // k*5P + line) and transforms them back along z.  Returns the buffer with
 // the result: entry (z, a*P + pb) holds field a at lines 2(p0+pb) (.x) and
 // 2(p0+pb)+1 (.y).  P odd keeps the z-strided accesses conflict-free.
-template <typename T>
+template <typename T, int RN = 0>
 __device__ typename Cplx<T>::type *z_load5_c2r(const typename Cplx<T>::type *__restrict__ S5,
                                                typename Cplx<T>::type *A,
                                                typename Cplx<T>::type *Bf, const Geom &g,
@@ -500,19 +500,19 @@ __device__ typename Cplx<T>::type *z_load5_c2r(const typename Cplx<T>::type *__r
     }
     A[k * P5 + b] = C{Av.x - Bv.y, Av.y + Bv.x};
   }
-  return fft_tile<T, +1>(A, Bf, f5P, pz);
+  return fft_tile<T, +1, RN>(A, Bf, f5P, pz);
 }
 
 // Forward z transform of the five real pairs held in `res` (same layout)
 // and the Hermitian split into the five half spectra of S5.
-template <typename T>
+template <typename T, int RN = 0>
 __device__ void z_r2c_store5(typename Cplx<T>::type *res, typename Cplx<T>::type *other,
                              typename Cplx<T>::type *__restrict__ S5, const Geom &g,
                              const FftPlan &pz, const FastDiv &fP, const FastDiv &f2P,
                              const FastDiv &f5P, int p0) {
   using C = typename Cplx<T>::type;
   const int P = (int)fP.d, P5 = 5 * P, Nz = g.Nz, NzH = g.NzH;
-  const C *out = fft_tile<T, -1>(res, other, f5P, pz);
+  const C *out = fft_tile<T, -1, RN>(res, other, f5P, pz);
   #pragma unroll 4
   for (int idx = threadIdx.x; idx < 10 * P * NzH; idx += blockDim.x) {
     int lb, k, a, ll;
@@ -533,8 +533,8 @@ __device__ void z_r2c_store5(typename Cplx<T>::type *res, typename Cplx<T>::type
 
 // c2r of the five weighted densities, phi and local terms, per-block
 // energies, and (GRAD) r2c of the five partials dV kT dphi/dn_a in place.
-template <typename T, bool GRAD>
-__global__ void __launch_bounds__(kThreads) k_z_phi(typename Cplx<T>::type *S5,
+template <typename T, bool GRAD, int RN = 0>
+__global__ void __launch_bounds__(kThreads, RN > 0 ? 2 : 1) k_z_phi(typename Cplx<T>::type *S5,
                                                     const double *__restrict__ n,
                                                     const double *__restrict__ V, Geom g,
                                                     FftPlan pz, FastDiv fP, FastDiv f2P,
@@ -548,7 +548,7 @@ __global__ void __launch_bounds__(kThreads) k_z_phi(typename Cplx<T>::type *S5,
   __shared__ double red[32 * kNumTerms];
   const int Nz = g.Nz, P5 = 5 * P;
   const int p0 = blockIdx.x * P;
-  C *res = z_load5_c2r<T>(S5, A, Bf, g, pz, fP, f5P, p0);
+  C *res = z_load5_c2r<T, RN>(S5, A, Bf, g, pz, fP, f5P, p0);
   T tacc[kNumTerms] = {0, 0, 0, 0, 0, 0};
   const bool hs = la.terms & kTermHS;
   const T inv_nQ = T(la.inv_nQ);
@@ -584,12 +584,12 @@ __global__ void __launch_bounds__(kThreads) k_z_phi(typename Cplx<T>::type *S5,
   block_reduce_terms<T>(tacc, la, red, partials);
   if (!GRAD) return;
   __syncthreads();
-  z_r2c_store5<T>(res, res == A ? Bf : A, S5, g, pz, fP, f2P, f5P, p0);
+  z_r2c_store5<T, RN>(res, res == A ? Bf : A, S5, g, pz, fP, f2P, f5P, p0);
 }
 
 // c2r of the adjoint sum, + local gradient terms, masked.
-template <typename T>
-__global__ void __launch_bounds__(kThreads) k_z_grad(const typename Cplx<T>::type *__restrict__ in,
+template <typename T, int RN = 0>
+__global__ void __launch_bounds__(kThreads, RN > 0 ? 2 : 1) k_z_grad(const typename Cplx<T>::type *__restrict__ in,
                                                      const double *__restrict__ n,
                                                      const double *__restrict__ V,
                                                      const double *__restrict__ mask,
@@ -605,7 +605,7 @@ __global__ void __launch_bounds__(kThreads) k_z_grad(const typename Cplx<T>::typ
   const C *res = nullptr;
   if (hs) {
     pack_c2r<T>(in, buf0, g, p0, P);
-    res = fft_tile<T, +1>(buf0, buf1, fP, pz);
+    res = fft_tile<T, +1, RN>(buf0, buf1, fP, pz);
   }
   #pragma unroll 4
   for (int idx = threadIdx.x; idx < 2 * P * g.Nz; idx += blockDim.x) {
@@ -637,8 +637,8 @@ __global__ void __launch_bounds__(kThreads) k_z_grad(const typename Cplx<T>::typ
 // refinement of the mixed form): c2r of the five weighted densities, then
 // per point the packed symmetric 5x5 second derivative of phi (wb_hess) and
 // the ideal-gas curvature kT/n, both stored in FP32.
-template <typename T>
-__global__ void __launch_bounds__(kThreads) k_z_hess(const typename Cplx<T>::type *__restrict__ S5,
+template <typename T, int RN = 0>
+__global__ void __launch_bounds__(kThreads, RN > 0 ? 2 : 1) k_z_hess(const typename Cplx<T>::type *__restrict__ S5,
                                                      const double *__restrict__ n, Geom g,
                                                      FftPlan pz, FastDiv fP, FastDiv f5P,
                                                      LocalArgs la, float *__restrict__ hess,
@@ -650,7 +650,7 @@ __global__ void __launch_bounds__(kThreads) k_z_hess(const typename Cplx<T>::typ
   C *Bf = A + g.Nz * 5 * P;
   const int Nz = g.Nz, P5 = 5 * P;
   const int p0 = blockIdx.x * P;
-  C *res = z_load5_c2r<T>(S5, A, Bf, g, pz, fP, f5P, p0);
+  C *res = z_load5_c2r<T, RN>(S5, A, Bf, g, pz, fP, f5P, p0);
   const bool hs = la.terms & kTermHS;
   #pragma unroll 4
   for (int idx = threadIdx.x; idx < 2 * P * Nz; idx += blockDim.x) {
@@ -677,8 +677,8 @@ __global__ void __launch_bounds__(kThreads) k_z_hess(const typename Cplx<T>::typ
 
 // Hessian-vector product, middle stage: c2r of the five weighted
 // perturbations dw, dP = dV kT J dw with the stored blocks, r2c of dP in place.
-template <typename T>
-__global__ void __launch_bounds__(kThreads) k_z_jac(typename Cplx<T>::type *S5, Geom g, FftPlan pz,
+template <typename T, int RN = 0>
+__global__ void __launch_bounds__(kThreads, RN > 0 ? 2 : 1) k_z_jac(typename Cplx<T>::type *S5, Geom g, FftPlan pz,
                                                     FastDiv fP, FastDiv f2P, FastDiv f5P,
                                                     double c, const float *__restrict__ hess) {
   const int P = (int)fP.d;
@@ -688,7 +688,7 @@ __global__ void __launch_bounds__(kThreads) k_z_jac(typename Cplx<T>::type *S5, 
   C *Bf = A + g.Nz * 5 * P;
   const int Nz = g.Nz, P5 = 5 * P;
   const int p0 = blockIdx.x * P;
-  C *res = z_load5_c2r<T>(S5, A, Bf, g, pz, fP, f5P, p0);
+  C *res = z_load5_c2r<T, RN>(S5, A, Bf, g, pz, fP, f5P, p0);
   const T cc = T(c);
   #pragma unroll 4
   for (int idx = threadIdx.x; idx < 2 * P * Nz; idx += blockDim.x) {
@@ -715,13 +715,13 @@ __global__ void __launch_bounds__(kThreads) k_z_jac(typename Cplx<T>::type *S5, 
     for (int a = 0; a < 5; a++) cell[a * fs] = cc * o[a];
   }
   __syncthreads();
-  z_r2c_store5<T>(res, res == A ? Bf : A, S5, g, pz, fP, f2P, f5P, p0);
+  z_r2c_store5<T, RN>(res, res == A ? Bf : A, S5, g, pz, fP, f2P, f5P, p0);
 }
 
 // Hessian-vector product, last stage: c2r of the adjoint sum plus the
 // ideal-gas curvature dV kT/n * dx, masked (masked points give 0).
-template <typename T>
-__global__ void __launch_bounds__(kThreads) k_z_hvp_out(
+template <typename T, int RN = 0>
+__global__ void __launch_bounds__(kThreads, RN > 0 ? 2 : 1) k_z_hvp_out(
     const typename Cplx<T>::type *__restrict__ in, const double *__restrict__ dx,
     const float *__restrict__ hloc, const double *__restrict__ mask, double *__restrict__ out,
     Geom g, FftPlan pz, FastDiv fP, LocalArgs la) {
@@ -735,7 +735,7 @@ __global__ void __launch_bounds__(kThreads) k_z_hvp_out(
   const C *res = nullptr;
   if (hs) {
     pack_c2r<T>(in, buf0, g, p0, P);
-    res = fft_tile<T, +1>(buf0, buf1, fP, pz);
+    res = fft_tile<T, +1, RN>(buf0, buf1, fP, pz);
   }
   #pragma unroll 4
   for (int idx = threadIdx.x; idx < 2 * P * g.Nz; idx += blockDim.x) {
@@ -1074,6 +1074,24 @@ const char *const kKernelNames[kNumKernels] = {
     "weight_table", "z_hess", "z_jac", "z_hvp_out", "veff_density", "veff_grad",
     "diag_precond"};
 
+// Calls f(std::integral_constant<int, RN>()) with RN = the plan's length
+// when it is an FP32 plan marked for the register-resident transform, else
+// RN = 0 (shared-memory passes): picks the kernel instantiation to launch.
+template <typename T, typename F> void with_rn(const FftPlan &p, F &&f) {
+  if constexpr (sizeof(T) == 4) {
+    if (p.reg) {
+      switch (p.n) {
+        case 32: f(std::integral_constant<int, 32>()); return;
+        case 64: f(std::integral_constant<int, 64>()); return;
+        case 128: f(std::integral_constant<int, 128>()); return;
+        case 256: f(std::integral_constant<int, 256>()); return;
+        default: break;
+      }
+    }
+  }
+  f(std::integral_constant<int, 0>());
+}
+
 // Accounting slot of kernel kind `id` in the arithmetic type T: FP32
 // launches are counted apart from FP64 ones (slots kNumKernels and up), so a
 // mixed solve's FP64 refinement does not blend into the FP32 kernels' times.
@@ -1307,17 +1325,26 @@ class EngineImpl {
     set_smem(k_z_phi<double, false>, t64.smem_phi);
     set_smem(k_z_phi<double, true>, t64.smem_phi);
     set_smem(k_z_grad<double>, t64.smem_z);
-    set_smem(k_z_r2c<float>, t32.smem_z);
-    set_smem(k_y_fft<float, -1>, t32.smem_y);
-    set_smem(k_y_fft<float, +1>, t32.smem_y);
-    set_smem(k_x_conv_fwd<float>, t32.smem_xf);
-    set_smem(k_x_conv_adj<float>, t32.smem_xc);
-    set_smem(k_z_phi<float, false>, t32.smem_phi);
-    set_smem(k_z_phi<float, true>, t32.smem_phi);
-    set_smem(k_z_grad<float>, t32.smem_z);
-    set_smem(k_z_hess<float>, t32.smem_phi);
-    set_smem(k_z_jac<float>, t32.smem_phi);
-    set_smem(k_z_hvp_out<float>, t32.smem_z);
+    // every FP32 instantiation (shared-memory passes and register lengths)
+    auto smem32 = [&](auto rn) {
+      constexpr int RN = decltype(rn)::value;
+      set_smem(k_z_r2c<float, RN>, t32.smem_z);
+      set_smem(k_y_fft<float, -1, RN>, t32.smem_y);
+      set_smem(k_y_fft<float, +1, RN>, t32.smem_y);
+      set_smem(k_x_conv_fwd<float, RN>, t32.smem_xf);
+      set_smem(k_x_conv_adj<float, RN>, t32.smem_xc);
+      set_smem(k_z_phi<float, false, RN>, t32.smem_phi);
+      set_smem(k_z_phi<float, true, RN>, t32.smem_phi);
+      set_smem(k_z_grad<float, RN>, t32.smem_z);
+      set_smem(k_z_hess<float, RN>, t32.smem_phi);
+      set_smem(k_z_jac<float, RN>, t32.smem_phi);
+      set_smem(k_z_hvp_out<float, RN>, t32.smem_z);
+    };
+    smem32(std::integral_constant<int, 0>());
+    smem32(std::integral_constant<int, 32>());
+    smem32(std::integral_constant<int, 64>());
+    smem32(std::integral_constant<int, 128>());
+    smem32(std::integral_constant<int, 256>());
 
     if (alloc(&S0, cs * g.NC) || alloc(&S5, 5 * cs * g.NC) || alloc(&w3, sizeof(double) * g.NC) ||
         alloc(&w2, sizeof(double) * g.NC) || alloc(&wv, sizeof(double) * g.NC))
@@ -1381,7 +1408,8 @@ class EngineImpl {
     }
     FftPlan np[3] = {f32 ? pxf : px, f32 ? pyf : py, f32 ? pzf : pz};
     for (int a = 0; a < 3; a++) {
-      if (c.radix[a][0] && !set_radix_order(np[a], c.radix[a])) {
+      if (c.radix[a][0] && !(f32 && set_reg_order(np[a], c.radix[a])) &&
+          !set_radix_order(np[a], c.radix[a])) {
         err = "radix order does not factor axis " + std::to_string(a);
         return -1;
       }
@@ -1432,10 +1460,13 @@ class EngineImpl {
     dim3 grid((g.NzH + t.By - 1) / t.By, g.Nx, nf);
     const int kid = kslot<T>(nf == 1 ? kK_y_fft1 : kK_y_fft5);
     pre(kid);
-    if (sign < 0)
-      k_y_fft<T, -1><<<grid, kThreads, t.smem_y, stream>>>(data, g, plan<T>(1), t.fBy);
-    else
-      k_y_fft<T, +1><<<grid, kThreads, t.smem_y, stream>>>(data, g, plan<T>(1), t.fBy);
+    with_rn<T>(plan<T>(1), [&](auto rn) {
+      constexpr int RN = decltype(rn)::value;
+      if (sign < 0)
+        k_y_fft<T, -1, RN><<<grid, kThreads, t.smem_y, stream>>>(data, g, plan<T>(1), t.fBy);
+      else
+        k_y_fft<T, +1, RN><<<grid, kThreads, t.smem_y, stream>>>(data, g, plan<T>(1), t.fBy);
+    });
     post(kid);
   }
   int x_tiles(int B) const { return (g.Ny * g.NzH + B - 1) / B; }
@@ -1445,13 +1476,17 @@ class EngineImpl {
   template <typename T> int forward_weighted(const FmtSpec &f, const double *n) {
     const Tiles &t = tl<T>();
     pre(kslot<T>(kK_z_r2c));
-    k_z_r2c<T><<<dim3(pairs_tiles(t.Pz), 1), kThreads, t.smem_z, stream>>>(
-        n, spec0<T>(), g, plan<T>(2), t.fPz, T(1));
+    with_rn<T>(plan<T>(2), [&](auto rn) {
+      k_z_r2c<T, decltype(rn)::value><<<dim3(pairs_tiles(t.Pz), 1), kThreads, t.smem_z, stream>>>(
+          n, spec0<T>(), g, plan<T>(2), t.fPz, T(1));
+    });
     post(kslot<T>(kK_z_r2c));
     y_fft<T>(spec0<T>(), 1, -1);
     pre(kslot<T>(kK_x_conv_fwd));
-    k_x_conv_fwd<T><<<x_tiles(t.Bxf), kThreads, t.smem_xf, stream>>>(
-        spec0<T>(), spec5<T>(), table<T>(0), table<T>(1), table<T>(2), g, plan<T>(0), t.fBxf);
+    with_rn<T>(plan<T>(0), [&](auto rn) {
+      k_x_conv_fwd<T, decltype(rn)::value><<<x_tiles(t.Bxf), kThreads, t.smem_xf, stream>>>(
+          spec0<T>(), spec5<T>(), table<T>(0), table<T>(1), table<T>(2), g, plan<T>(0), t.fBxf);
+    });
     post(kslot<T>(kK_x_conv_fwd));
     y_fft<T>(spec5<T>(), 5, +1);
     return check("forward convolution");
@@ -1593,20 +1628,25 @@ class EngineImpl {
       if (forward_weighted<T>(f, n)) return -1;
       nblk = pairs_tiles(t.Pphi);
       pre(kslot<T>(grad ? kK_z_phi_grad : kK_z_phi_energy));
-      if (grad)
-        k_z_phi<T, true><<<nblk, kThreads, t.smem_phi, stream>>>(
-            spec5<T>(), n, V, g, plan<T>(2), t.fPphi, t.f2Pphi, t.f5Pphi, la, partials);
-      else
-        k_z_phi<T, false><<<nblk, kThreads, t.smem_phi, stream>>>(
-            spec5<T>(), n, V, g, plan<T>(2), t.fPphi, t.f2Pphi, t.f5Pphi, la, partials);
+      with_rn<T>(plan<T>(2), [&](auto rn) {
+        constexpr int RN = decltype(rn)::value;
+        if (grad)
+          k_z_phi<T, true, RN><<<nblk, kThreads, t.smem_phi, stream>>>(
+              spec5<T>(), n, V, g, plan<T>(2), t.fPphi, t.f2Pphi, t.f5Pphi, la, partials);
+        else
+          k_z_phi<T, false, RN><<<nblk, kThreads, t.smem_phi, stream>>>(
+              spec5<T>(), n, V, g, plan<T>(2), t.fPphi, t.f2Pphi, t.f5Pphi, la, partials);
+      });
       post(kslot<T>(grad ? kK_z_phi_grad : kK_z_phi_energy));
       if (check("phi")) return -1;
       if (grad) {
         y_fft<T>(spec5<T>(), 5, -1);
         pre(kslot<T>(kK_x_conv_adj));
-        k_x_conv_adj<T><<<x_tiles(t.Bxc), kThreads, t.smem_xc, stream>>>(
-            spec5<T>(), spec0<T>(), table<T>(0), table<T>(1), table<T>(2), g, plan<T>(0),
-            t.fBxc, t.f5Bxc);
+        with_rn<T>(plan<T>(0), [&](auto rn) {
+          k_x_conv_adj<T, decltype(rn)::value><<<x_tiles(t.Bxc), kThreads, t.smem_xc, stream>>>(
+              spec5<T>(), spec0<T>(), table<T>(0), table<T>(1), table<T>(2), g, plan<T>(0),
+              t.fBxc, t.f5Bxc);
+        });
         post(kslot<T>(kK_x_conv_adj));
         y_fft<T>(spec0<T>(), 1, +1);
       }
@@ -1618,8 +1658,10 @@ class EngineImpl {
     }
     if (grad) {
       pre(kslot<T>(kK_z_grad));
-      k_z_grad<T><<<pairs_tiles(t.Pz), kThreads, t.smem_z, stream>>>(
-          spec0<T>(), n, V, mask, grad, g, plan<T>(2), t.fPz, la);
+      with_rn<T>(plan<T>(2), [&](auto rn) {
+        k_z_grad<T, decltype(rn)::value><<<pairs_tiles(t.Pz), kThreads, t.smem_z, stream>>>(
+            spec0<T>(), n, V, mask, grad, g, plan<T>(2), t.fPz, la);
+      });
       post(kslot<T>(kK_z_grad));
     }
     if (check("gradient")) return -1;
@@ -1635,8 +1677,11 @@ class EngineImpl {
       if (ensure_table<float>(f.R) || forward_weighted<float>(f, n)) return -1;
     }
     pre(kslot<float>(kK_z_hess));
-    k_z_hess<float><<<pairs_tiles(t32.Pphi), kThreads, t32.smem_phi, stream>>>(
-        spec5<float>(), n, g, plan<float>(2), t32.fPphi, t32.f5Pphi, la, hess, hloc);
+    with_rn<float>(plan<float>(2), [&](auto rn) {
+      k_z_hess<float, decltype(rn)::value><<<pairs_tiles(t32.Pphi), kThreads, t32.smem_phi,
+                                             stream>>>(spec5<float>(), n, g, plan<float>(2),
+                                                       t32.fPphi, t32.f5Pphi, la, hess, hloc);
+    });
     post(kslot<float>(kK_z_hess));
     return check("hessian blocks");
   }
@@ -1652,21 +1697,30 @@ class EngineImpl {
     if (f.terms & kTermHS) {
       if (forward_weighted<float>(f, dx)) return -1;
       pre(kslot<float>(kK_z_jac));
-      k_z_jac<float><<<pairs_tiles(t32.Pphi), kThreads, t32.smem_phi, stream>>>(
-          spec5<float>(), g, plan<float>(2), t32.fPphi, t32.f2Pphi, t32.f5Pphi, g.dV * f.kT,
-          hess);
+      with_rn<float>(plan<float>(2), [&](auto rn) {
+        k_z_jac<float, decltype(rn)::value><<<pairs_tiles(t32.Pphi), kThreads, t32.smem_phi,
+                                              stream>>>(spec5<float>(), g, plan<float>(2),
+                                                        t32.fPphi, t32.f2Pphi, t32.f5Pphi,
+                                                        g.dV * f.kT, hess);
+      });
       post(kslot<float>(kK_z_jac));
       y_fft<float>(spec5<float>(), 5, -1);
       pre(kslot<float>(kK_x_conv_adj));
-      k_x_conv_adj<float><<<x_tiles(t32.Bxc), kThreads, t32.smem_xc, stream>>>(
-          spec5<float>(), spec0<float>(), table<float>(0), table<float>(1), table<float>(2), g,
-          plan<float>(0), t32.fBxc, t32.f5Bxc);
+      with_rn<float>(plan<float>(0), [&](auto rn) {
+        k_x_conv_adj<float, decltype(rn)::value><<<x_tiles(t32.Bxc), kThreads, t32.smem_xc,
+                                                   stream>>>(
+            spec5<float>(), spec0<float>(), table<float>(0), table<float>(1), table<float>(2), g,
+            plan<float>(0), t32.fBxc, t32.f5Bxc);
+      });
       post(kslot<float>(kK_x_conv_adj));
       y_fft<float>(spec0<float>(), 1, +1);
     }
     pre(kslot<float>(kK_z_hvp_out));
-    k_z_hvp_out<float><<<pairs_tiles(t32.Pz), kThreads, t32.smem_z, stream>>>(
-        spec0<float>(), dx, hloc, mask, out, g, plan<float>(2), t32.fPz, la);
+    with_rn<float>(plan<float>(2), [&](auto rn) {
+      k_z_hvp_out<float, decltype(rn)::value><<<pairs_tiles(t32.Pz), kThreads, t32.smem_z,
+                                                stream>>>(spec0<float>(), dx, hloc, mask, out, g,
+                                                          plan<float>(2), t32.fPz, la);
+    });
     post(kslot<float>(kK_z_hvp_out));
     return check("hessian-vector product");
   }

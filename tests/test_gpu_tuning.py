@@ -181,3 +181,34 @@ def test_graph_replay_is_bitwise_identical_to_direct_launches(precision):
         f.close()
         g.close()
         ctx.close()
+
+
+def test_register_resident_transform_matches_shared_memory_passes():
+    """The register-resident FFT (radix order [16, N/16], FP32 kernels only)
+    gives the mixed evaluator's energy, gradient and Hessian-vector product
+    to FP32 rounding; the FP64 kernels refuse it."""
+    s, ctx, g, f = _setup((32, 32, 64), 1)
+    try:
+        n = s.n0.reshape(-1)
+        E0, g0, _ = f.energy_grad(n)
+        dx = 0.01 * s.nb * s.mask.reshape(-1)
+        h0 = f.hessian_vector(n, dx)
+        t, r = _tiles(g, 1)
+        rr = np.zeros(24, dtype=np.int32)  # axes x, y, z
+        rr[0:2] = [16, 2]
+        rr[8:10] = [16, 2]
+        rr[16:18] = [16, 4]
+        for tt in ([4, 16, 8, 4, 8, 4], [32, 16, 32, 8, 32, 8]):
+            assert _set(g, 1, tt, rr) == 0
+            t2, r2 = _tiles(g, 1)
+            assert list(r2[16:18]) == [16, 4] and r2[18] == 0
+            E, gr, _ = f.energy_grad(n)
+            h = f.hessian_vector(n, dx)
+            assert abs(E / E0 - 1) < 2e-6
+            assert np.abs(gr - g0).max() <= 2e-5 * np.abs(g0).max()
+            assert np.abs(h - h0).max() <= 2e-5 * np.abs(h0).max()
+        assert _set(g, 0, t, rr) == _lib.ERR_ARG
+    finally:
+        f.close()
+        g.close()
+        ctx.close()
