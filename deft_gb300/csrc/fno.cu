@@ -191,11 +191,16 @@ __global__ void k_lift(const float *__restrict__ mask, float eta, const __nv_bfl
 }
 
 // Layer output: z[o][r] = spec[o][r] + sum_i Wp[o][i] h[i][r] + b[o];
-// hn = act(z).  spec is already in z (from the inverse transform).
+// hn = act(z).  spec is already in z (from the inverse transform); z is
+// written back only when a backward pass will need it (store_z).  The
+// output-channel loop is not unrolled, so the weights stay in shared memory
+// instead of C*C registers.
 template <int C>
-__global__ void k_layer_pw(const float *__restrict__ h, float *__restrict__ z,
-                           float *__restrict__ hn, const __nv_bfloat16 *__restrict__ Wp,
-                           const __nv_bfloat16 *__restrict__ b, long long NR, int act) {
+__global__ void __launch_bounds__(256) k_layer_pw(const float *__restrict__ h,
+                                                  float *__restrict__ z, float *__restrict__ hn,
+                                                  const __nv_bfloat16 *__restrict__ Wp,
+                                                  const __nv_bfloat16 *__restrict__ b,
+                                                  long long NR, int act, int store_z) {
   __shared__ float Ws[C * C], bs[C];
   for (int i = threadIdx.x; i < C * C; i += blockDim.x) Ws[i] = bf(Wp, i);
   for (int i = threadIdx.x; i < C; i += blockDim.x) bs[i] = bf(b, i);
@@ -205,12 +210,12 @@ __global__ void k_layer_pw(const float *__restrict__ h, float *__restrict__ z,
     float hv[C];
 #pragma unroll
     for (int i = 0; i < C; i++) hv[i] = h[(size_t)i * NR + r];
-#pragma unroll
+#pragma unroll 1
     for (int o = 0; o < C; o++) {
       float acc = z[(size_t)o * NR + r] + bs[o];
 #pragma unroll
       for (int i = 0; i < C; i++) acc += Ws[o * C + i] * hv[i];
-      z[(size_t)o * NR + r] = acc;
+      if (store_z) z[(size_t)o * NR + r] = acc;
       hn[(size_t)o * NR + r] = act ? gelu(acc) : acc;
     }
   }
@@ -258,7 +263,7 @@ __global__ void k_project(const float *__restrict__ h, const __nv_bfloat16 *__re
 #pragma unroll
     for (int i = 0; i < C; i++) hv[i] = h[(size_t)i * NR + r];
     float out = q2v;
-#pragma unroll
+#pragma unroll 1
     for (int c = 0; c < C; c++) {
       float a = q1s[c];
 #pragma unroll
@@ -311,7 +316,7 @@ __global__ void __launch_bounds__(256) k_project_bwd(
           hs[i][p] = h[(size_t)i * NR + r];
           hb[i] = 0.f;
         }
-#pragma unroll
+#pragma unroll 1
         for (int c = 0; c < C; c++) {
           const float a = zq[(size_t)c * NR + r];
           gs[c][p] = gelu(a);
@@ -381,7 +386,7 @@ __global__ void __launch_bounds__(256) k_layer_pw_bwd(
           hs[i][p] = hprev[(size_t)i * NR + r];
           hb[i] = 0.f;
         }
-#pragma unroll
+#pragma unroll 1
         for (int o = 0; o < C; o++) {
           const float hbo = hbar[(size_t)o * NR + r];
           const float zb = act ? hbo * gelu_d(z[(size_t)o * NR + r]) : hbo;
@@ -627,10 +632,10 @@ void spectral_bwd(deft_fno *f, int l, const float *zbar, float *hin_bar) {
 }
 
 template <int C>
-void launch_layer_pw(deft_fno *f, int l) {
+void launch_layer_pw(deft_fno *f, int l, int store_z) {
   k_layer_pw<C><<<grid_for(f->NR), kT, 0, f->stream>>>(f->h[l], f->z[l], f->h[l + 1],
                                                        f->pb + f->oWp[l], f->pb + f->ob[l], f->NR,
-                                                       l < f->L - 1 ? 1 : 0);
+                                                       l < f->L - 1 ? 1 : 0, store_z);
 }
 
 template <int C>
@@ -647,16 +652,19 @@ void project(deft_fno *f, float *zq, const float *target, const float *w, float 
   else launch_project<4>(f, zq, target, w, part);
 }
 
-int forward(deft_fno *f, float eta) {
+// Forward through the Fourier layers; `train` keeps the pre-activations the
+// backward pass reads.
+int forward(deft_fno *f, float eta, bool train) {
   const int C = f->C;
   f->launches += 1 + 8 * f->L;  // lift; per layer 7 spectral launches and the pointwise one
   k_lift<<<grid_for(f->NR), kT, 0, f->stream>>>(f->mask, eta, f->pb + f->oP, f->pb + f->op, f->h[0],
                                                C, f->NR);
   for (int l = 0; l < f->L; l++) {
     spectral_fwd(f, l, f->h[l], f->z[l]);
-    if (C == 16) launch_layer_pw<16>(f, l);
-    else if (C == 8) launch_layer_pw<8>(f, l);
-    else launch_layer_pw<4>(f, l);
+    const int sz = train ? 1 : 0;
+    if (C == 16) launch_layer_pw<16>(f, l, sz);
+    else if (C == 8) launch_layer_pw<8>(f, l, sz);
+    else launch_layer_pw<4>(f, l, sz);
   }
   return check(f, "fno forward");
 }
@@ -877,7 +885,7 @@ int eval_impl(deft_fno *f, const float *mask, float eta, const float *target, cu
     cudaMemcpyAsync(f->target, target, rb, kin, f->stream);
     cudaMemcpyAsync(f->wt, mask, rb, kin, f->stream);
   }
-  if (int s = forward(f, eta)) return s;
+  if (int s = forward(f, eta, want_grad)) return s;
   project(f, f->zq, target ? f->target : nullptr, f->wt, target ? f->part : nullptr);
   double W = 0, Ls = 0;
   if (target) {
@@ -1006,7 +1014,7 @@ int deft_fno_warm_start(deft_fno *f, const double *mask_dev, double eta, double 
   const int C = f->C;
   k_d2f<<<grid_for(f->NR), kT, 0, f->stream>>>(mask_dev, f->mask, f->NR, 1.f);
   f->launches += 2;  // this and the density below
-  if (int s = forward(f, (float)eta)) return s;
+  if (int s = forward(f, (float)eta, false)) return s;
   project(f, nullptr, nullptr, nullptr, nullptr);
   k_density<<<grid_for(f->NR), kT, 0, f->stream>>>(f->y, mask_dev, nb, floor_rel, n_out_dev,
                                                    f->NR);
