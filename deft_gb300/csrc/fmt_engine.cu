@@ -81,6 +81,35 @@ __device__ void weights_at(double k2, double R, double dr, double &w3, double &w
   }
 }
 
+// The same weights in FP32, evaluated on the fly in the convolution kernels
+// (scale = dV/V folded in).  Below kR = 0.5 the closed forms lose digits to
+// cancellation in FP32, so the Taylor series of the reference's small-kR
+// branch is used there, times the smear factor (which is not 1 to FP32
+// precision at that threshold; at kR <= 1e-3, where the FP64 branch omits it,
+// the two differ by at most 6 (k dr)^2 < 3e-7).
+__device__ __forceinline__ void weights_at_f(float k2, float R, float dr, float scale, float &w3,
+                                             float &w2, float &wv) {
+  const float kk = sqrtf(k2);
+  const float kR = kk * R;
+  const float kdr = kk * dr;
+  const float smear = expf(-6.0f * kdr * kdr) * scale;
+  const float fpi = 12.566370614359172954f;
+  if (kR > 0.5f) {
+    float sn, cs;
+    sincosf(kR, &sn, &cs);
+    const float ik = 1.0f / kk;
+    w3 = smear * fpi * (sn - kR * cs) * ik * ik * ik;
+    w2 = smear * fpi * R * sn * ik;
+    wv = smear * fpi * ik * ik * (R * cs - sn * ik);
+  } else {
+    const float x = kR * kR, R3 = R * R * R;
+    w3 = smear * (fpi / 3) * R3 * (((-1.0f / 15120) * x + 1.0f / 280) * x - 0.1f) * x + smear * (fpi / 3) * R3;
+    w2 = smear * fpi * R * R * ((((-1.0f / 5040) * x + 1.0f / 120) * x - 1.0f / 6) * x + 1.0f);
+    wv = smear * fpi * R3 * (((1.0f / 5040 - 1.0f / 720) * x + (1.0f / 24 - 1.0f / 120)) * x -
+                             1.0f / 3);
+  }
+}
+
 // Deterministic block reduction of K doubles; thread 0 gets the sums.
 template <int K>
 __device__ void block_reduce(double (&v)[K], double *smem /* 32*K */) {
@@ -322,13 +351,15 @@ template <typename T, int RN = 0>
 __global__ void __launch_bounds__(kThreads, RN > 0 ? 2 : 1) k_x_conv_fwd(
     const typename Cplx<T>::type *__restrict__ in, typename Cplx<T>::type *__restrict__ out5,
     const T *__restrict__ w3, const T *__restrict__ w2, const T *__restrict__ wv, Geom g,
-    FftPlan px, FastDiv fB) {
+    FftPlan px, FastDiv fB, float Rw) {
   const int B = (int)fB.d;
   using C = typename Cplx<T>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C *bufA = reinterpret_cast<C *>(smem_raw);
   C *bufB = bufA + g.Nx * B;
   C *bufC = bufB + g.Nx * B;
+  // FP32: the three weights of the tile's k-points, evaluated here once
+  float *Wt = reinterpret_cast<float *>(bufC + g.Nx * B);
   const int J = g.Ny * g.NzH;
   const int j0 = blockIdx.x * B;
   #pragma unroll 4
@@ -337,6 +368,17 @@ __global__ void __launch_bounds__(kThreads, RN > 0 ? 2 : 1) k_x_conv_fwd(
     fdivmod(idx, fB, e, j);
     j += j0;
     bufA[idx] = j < J ? in[(size_t)e * J + j] : C{0, 0};
+    if constexpr (sizeof(T) == 4) {
+      int y, z;
+      fdivmod(j < J ? j : 0, g.fNzH, y, z);
+      const float kx = kcomp_t<float>(g, 0, e, y, z), ky = kcomp_t<float>(g, 1, e, y, z),
+                  kz = kcomp_t<float>(g, 2, e, y, z);
+      float a3, a2, av;
+      weights_at_f(kx * kx + ky * ky + kz * kz, Rw, (float)g.dr, (float)g.scale, a3, a2, av);
+      Wt[idx] = a3;
+      Wt[g.Nx * B + idx] = a2;
+      Wt[2 * g.Nx * B + idx] = av;
+    }
   }
   const C *R0 = fft_tile<T, -1, RN>(bufA, bufB, fB, px);
   C *F1 = (R0 == bufA) ? bufB : bufA;
@@ -351,17 +393,17 @@ __global__ void __launch_bounds__(kThreads, RN > 0 ? 2 : 1) k_x_conv_fwd(
       if (j < J) {
         const size_t i = (size_t)e * J + j;
         const C v = R0[idx];
-        if (a == 0) {
-          const T w = w3[i];
-          o = C{v.x * w, v.y * w};
-        } else if (a == 1) {
-          const T w = w2[i];
+        const int slot = a < 2 ? a : 2;
+        T w;
+        if constexpr (sizeof(T) == 4) w = Wt[slot * g.Nx * B + idx];
+        else w = slot == 0 ? w3[i] : slot == 1 ? w2[i] : wv[i];
+        if (a < 2) {
           o = C{v.x * w, v.y * w};
         } else {
           int y, z;
           fdivmod(j, g.fNzH, y, z);
-          const T w = kcomp_t<T>(g, a - 2, e, y, z) * wv[i];
-          o = C{-v.y * w, v.x * w};  // times i w
+          const T wk = kcomp_t<T>(g, a - 2, e, y, z) * w;
+          o = C{-v.y * wk, v.x * wk};  // times i w
         }
       }
       F1[idx] = o;
@@ -385,7 +427,7 @@ template <typename T, int RN = 0>
 __global__ void __launch_bounds__(kThreads, RN > 0 ? 2 : 1) k_x_conv_adj(
     const typename Cplx<T>::type *__restrict__ in5, typename Cplx<T>::type *__restrict__ out,
     const T *__restrict__ w3, const T *__restrict__ w2, const T *__restrict__ wv, Geom g,
-    FftPlan px, FastDiv fB, FastDiv f5B) {
+    FftPlan px, FastDiv fB, FastDiv f5B, float Rw) {
   const int B = (int)fB.d;
   using C = typename Cplx<T>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -413,12 +455,20 @@ __global__ void __launch_bounds__(kThreads, RN > 0 ? 2 : 1) k_x_conv_adj(
     if (j < J) {
       const size_t i = (size_t)e * J + j;
       const C *r = R + e * B5 + b;
-      const T a3 = w3[i], a2 = w2[i];
-      o.x = r[0].x * a3 + r[B].x * a2;
-      o.y = r[0].y * a3 + r[B].y * a2;
       int y, z;
       fdivmod(j, g.fNzH, y, z);
-      const T v = wv[i];
+      T a3, a2, v;
+      if constexpr (sizeof(T) == 4) {
+        const float kx = kcomp_t<float>(g, 0, e, y, z), ky = kcomp_t<float>(g, 1, e, y, z),
+                    kz = kcomp_t<float>(g, 2, e, y, z);
+        weights_at_f(kx * kx + ky * ky + kz * kz, Rw, (float)g.dr, (float)g.scale, a3, a2, v);
+      } else {
+        a3 = w3[i];
+        a2 = w2[i];
+        v = wv[i];
+      }
+      o.x = r[0].x * a3 + r[B].x * a2;
+      o.y = r[0].y * a3 + r[B].y * a2;
 #pragma unroll
       for (int c = 0; c < 3; c++) {
         const T w = kcomp_t<T>(g, c, e, y, z) * v;
@@ -993,7 +1043,7 @@ void finish_tiles(Tiles &t, const Geom &g, size_t cs) {
   t.f5Pphi = make_fastdiv(5 * t.Pphi);
   t.smem_y = 2 * (size_t)g.Ny * t.By * cs;
   t.smem_x2 = 2 * (size_t)g.Nx * t.Bx * cs;
-  t.smem_xf = 3 * (size_t)g.Nx * t.Bxf * cs;
+  t.smem_xf = 3 * (size_t)g.Nx * t.Bxf * cs + (cs == 8 ? 3 * (size_t)g.Nx * t.Bxf * 4 : 0);
   t.smem_xc = 10 * (size_t)g.Nx * t.Bxc * cs;
   t.smem_z = 2 * (size_t)g.Nz * t.Pz * cs;
   t.smem_phi = 10 * (size_t)g.Nz * t.Pphi * cs;
@@ -1485,7 +1535,8 @@ class EngineImpl {
     pre(kslot<T>(kK_x_conv_fwd));
     with_rn<T>(plan<T>(0), [&](auto rn) {
       k_x_conv_fwd<T, decltype(rn)::value><<<x_tiles(t.Bxf), kThreads, t.smem_xf, stream>>>(
-          spec0<T>(), spec5<T>(), table<T>(0), table<T>(1), table<T>(2), g, plan<T>(0), t.fBxf);
+          spec0<T>(), spec5<T>(), table<T>(0), table<T>(1), table<T>(2), g, plan<T>(0), t.fBxf,
+          (float)f.R);
     });
     post(kslot<T>(kK_x_conv_fwd));
     y_fft<T>(spec5<T>(), 5, +1);
@@ -1645,7 +1696,7 @@ class EngineImpl {
         with_rn<T>(plan<T>(0), [&](auto rn) {
           k_x_conv_adj<T, decltype(rn)::value><<<x_tiles(t.Bxc), kThreads, t.smem_xc, stream>>>(
               spec5<T>(), spec0<T>(), table<T>(0), table<T>(1), table<T>(2), g, plan<T>(0),
-              t.fBxc, t.f5Bxc);
+              t.fBxc, t.f5Bxc, (float)f.R);
         });
         post(kslot<T>(kK_x_conv_adj));
         y_fft<T>(spec0<T>(), 1, +1);
@@ -1710,7 +1761,7 @@ class EngineImpl {
         k_x_conv_adj<float, decltype(rn)::value><<<x_tiles(t32.Bxc), kThreads, t32.smem_xc,
                                                    stream>>>(
             spec5<float>(), spec0<float>(), table<float>(0), table<float>(1), table<float>(2), g,
-            plan<float>(0), t32.fBxc, t32.f5Bxc);
+            plan<float>(0), t32.fBxc, t32.f5Bxc, (float)f.R);
       });
       post(kslot<float>(kK_x_conv_adj));
       y_fft<float>(spec0<float>(), 1, +1);
@@ -2123,13 +2174,13 @@ int noalloc_energy_grad(const GridSpec &s, const FmtSpec &f, const double *n, co
     k_z_r2c<double><<<dim3(ptiles_z, 1), kThreads, t.smem_z, stream>>>(n, S0, g, pz, t.fPz, 1.0);
     k_y_fft<double, -1><<<ygrid1, kThreads, t.smem_y, stream>>>(S0, g, py, t.fBy);
     k_x_conv_fwd<double><<<(g.Ny * g.NzH + t.Bxf - 1) / t.Bxf, kThreads, t.smem_xf, stream>>>(
-        S0, S5, w3, w2, wv, g, px, t.fBxf);
+        S0, S5, w3, w2, wv, g, px, t.fBxf, (float)f.R);
     k_y_fft<double, +1><<<ygrid5, kThreads, t.smem_y, stream>>>(S5, g, py, t.fBy);
     k_z_phi<double, true><<<nblk_phi, kThreads, t.smem_phi, stream>>>(
         S5, n, V, g, pz, t.fPphi, t.f2Pphi, t.f5Pphi, la, partials);
     k_y_fft<double, -1><<<ygrid5, kThreads, t.smem_y, stream>>>(S5, g, py, t.fBy);
     k_x_conv_adj<double><<<xt, kThreads, t.smem_xc, stream>>>(S5, S0, w3, w2, wv, g, px, t.fBxc,
-                                                              t.f5Bxc);
+                                                              t.f5Bxc, (float)f.R);
     k_y_fft<double, +1><<<ygrid1, kThreads, t.smem_y, stream>>>(S0, g, py, t.fBy);
   } else {
     k_local_energy<double><<<nblk, kThreads, 0, stream>>>(n, V, g, la, partials);
