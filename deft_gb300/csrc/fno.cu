@@ -51,63 +51,104 @@ __device__ __forceinline__ float bf(const __nv_bfloat16 *w, size_t i) {
 
 // ---------------------------------------------------------------------------
 // Truncated DFT along z (contiguous lines of length N).
-// fwd: out[l][k] = s_k sum_z in[l][z] e^{-2 pi i k z / N}   (k < Kz)
-// E[z*Kz + k] = s_k (cos, -sin) precomputed.
-__global__ void k_dft_z_fwd(const float *__restrict__ in, float2 *__restrict__ out,
-                            const float2 *__restrict__ E, int L, int N, int Kz) {
+// fwd: out[l][k] = s_k sum_z in[l][z] e^{-2 pi i k z / N}   (k < Kz <= kMaxKz)
+// E[z*Kz + k] = s_k (cos, -sin) precomputed.  A block stages LB lines (row
+// stride N + 4: the four threads of a line and the eight lines of a warp hit
+// distinct banks); four consecutive threads share a line, each summing every
+// fourth z for all k in registers, then a shuffle reduction.
+constexpr int kMaxKz = 16;
+
+__global__ void __launch_bounds__(256) k_dft_z_fwd(const float *__restrict__ in,
+                                                   float2 *__restrict__ out,
+                                                   const float2 *__restrict__ E, int L, int N,
+                                                   int Kz) {
   extern __shared__ float sm[];
-  const int LB = 64;
-  float *tile = sm;                                        // [LB][N+1]
-  float2 *Es = reinterpret_cast<float2 *>(tile + LB * (N + 1));  // [N][Kz]
+  const int LB = 64, S = N + 4;
+  float *tile = sm;                                             // [LB][N+4]
+  float2 *Es = reinterpret_cast<float2 *>(tile + LB * S);      // [N][Kz]
   const int l0 = blockIdx.x * LB;
   for (int i = threadIdx.x; i < N * Kz; i += blockDim.x) Es[i] = E[i];
   for (int i = threadIdx.x; i < LB * N; i += blockDim.x) {
     const int ll = i / N, z = i - ll * N;
     const int l = l0 + ll;
-    tile[ll * (N + 1) + z] = l < L ? in[(size_t)l * N + z] : 0.f;
+    tile[ll * S + z] = l < L ? in[(size_t)l * N + z] : 0.f;
   }
   __syncthreads();
-  const int groups = blockDim.x / LB;  // threads per line
-  const int ll = threadIdx.x % LB, grp = threadIdx.x / LB;
+  const int ll = threadIdx.x >> 2, q = threadIdx.x & 3;
   const int l = l0 + ll;
-  for (int k = grp; k < Kz; k += groups) {
-    float re = 0.f, im = 0.f;
-    const float *row = tile + ll * (N + 1);
-    for (int z = 0; z < N; z++) {
-      const float v = row[z];
-      const float2 e = Es[z * Kz + k];
-      re += v * e.x;
-      im += v * e.y;
+  float2 acc[kMaxKz];
+#pragma unroll
+  for (int k = 0; k < kMaxKz; k++) acc[k] = make_float2(0.f, 0.f);
+  const float *row = tile + ll * S;
+  for (int z = q; z < N; z += 4) {
+    const float v = row[z];
+    const float2 *e = Es + z * Kz;
+#pragma unroll
+    for (int k = 0; k < kMaxKz; k++) {
+      if (k < Kz) {
+        const float2 w = e[k];
+        acc[k].x += v * w.x;
+        acc[k].y += v * w.y;
+      }
     }
-    if (l < L) out[(size_t)l * Kz + k] = make_float2(re, im);
+  }
+#pragma unroll
+  for (int k = 0; k < kMaxKz; k++) {
+    if (k < Kz) {
+      acc[k].x += __shfl_xor_sync(0xffffffffu, acc[k].x, 1);
+      acc[k].y += __shfl_xor_sync(0xffffffffu, acc[k].y, 1);
+      acc[k].x += __shfl_xor_sync(0xffffffffu, acc[k].x, 2);
+      acc[k].y += __shfl_xor_sync(0xffffffffu, acc[k].y, 2);
+    }
+  }
+  if (l < L) {
+#pragma unroll
+    for (int k = 0; k < kMaxKz; k++)
+      if (k < Kz && (k & 3) == q) out[(size_t)l * Kz + k] = acc[k];
   }
 }
 
-// inv: out[l][z] (+)= sum_k Re[in[l][k] G[k][z]],  G = c_k s (cos, sin)
-__global__ void k_dft_z_inv(const float2 *__restrict__ in, float *__restrict__ out,
-                            const float2 *__restrict__ G, int L, int N, int Kz, int accumulate) {
+// inv: out[l][z] (+)= sum_k Re[in[l][k] G[z][k]],  G = c_k s (cos, sin), z-major.
+// Four threads per line hold the line's Kz coefficients in registers and
+// produce every fourth z into a staged tile, written back coalesced.
+__global__ void __launch_bounds__(256) k_dft_z_inv(const float2 *__restrict__ in,
+                                                   float *__restrict__ out,
+                                                   const float2 *__restrict__ G, int L, int N,
+                                                   int Kz, int accumulate) {
   extern __shared__ float sm[];
-  const int LB = 16;
-  float2 *ins = reinterpret_cast<float2 *>(sm);  // [LB][Kz]
-  float2 *Gs = ins + LB * Kz;                    // [Kz][N]
+  const int LB = 64, S = N + 4;
+  float *tile = sm;                                        // [LB][N+4]
+  float2 *Gs = reinterpret_cast<float2 *>(tile + LB * S);  // [N][Kz]
   const int l0 = blockIdx.x * LB;
   for (int i = threadIdx.x; i < Kz * N; i += blockDim.x) Gs[i] = G[i];
-  for (int i = threadIdx.x; i < LB * Kz; i += blockDim.x) {
-    const int l = l0 + i / Kz;
-    ins[i] = l < L ? in[(size_t)l * Kz + (i % Kz)] : make_float2(0.f, 0.f);
+  __syncthreads();
+  const int ll = threadIdx.x >> 2, q = threadIdx.x & 3;
+  const int l = l0 + ll;
+  float2 c[kMaxKz];
+#pragma unroll
+  for (int k = 0; k < kMaxKz; k++)
+    c[k] = (k < Kz && l < L) ? in[(size_t)l * Kz + k] : make_float2(0.f, 0.f);
+  float *row = tile + ll * S;
+  for (int z = q; z < N; z += 4) {
+    const float2 *gz = Gs + z * Kz;
+    float acc = 0.f;
+#pragma unroll
+    for (int k = 0; k < kMaxKz; k++) {
+      if (k < Kz) {
+        const float2 gk = gz[k];
+        acc += c[k].x * gk.x - c[k].y * gk.y;
+      }
+    }
+    row[z] = acc;
   }
   __syncthreads();
   for (int i = threadIdx.x; i < LB * N; i += blockDim.x) {
-    const int ll = i / N, z = i - ll * N;
-    const int l = l0 + ll;
-    if (l >= L) continue;
-    float acc = 0.f;
-    for (int k = 0; k < Kz; k++) {
-      const float2 a = ins[ll * Kz + k], gk = Gs[k * N + z];
-      acc += a.x * gk.x - a.y * gk.y;
-    }
-    float *o = out + (size_t)l * N + z;
-    *o = accumulate ? *o + acc : acc;
+    const int lr = i / N, z = i - lr * N;
+    const int lo = l0 + lr;
+    if (lo >= L) continue;
+    float *o = out + (size_t)lo * N + z;
+    const float v = tile[lr * S + z];
+    *o = accumulate ? *o + v : v;
   }
 }
 
@@ -554,8 +595,8 @@ struct deft_fno {
   // DFT tables
   float2 *Ezf = nullptr;  // [N][Kz] forward z, scale 1
   float2 *Ezb = nullptr;  // [N][Kz] forward z with the synthesis scale c_k / N^3 (adjoint use)
-  float2 *Gzi = nullptr;  // [Kz][N] synthesis c_k / N^3
-  float2 *Gza = nullptr;  // [Kz][N] adjoint of the forward z transform (c = 1, s = 1)
+  float2 *Gzi = nullptr;  // [N][Kz] synthesis c_k / N^3
+  float2 *Gza = nullptr;  // [N][Kz] adjoint of the forward z transform (c = 1, s = 1)
   float2 *Eyf = nullptr, *Eyi = nullptr, *Exf = nullptr, *Exi = nullptr;
   // activations
   std::vector<float *> h, z;  // h[0..L], z[0..L-1]
@@ -585,8 +626,8 @@ int check(deft_fno *f, const char *what) {
   return DEFT_OK;
 }
 
-size_t smem_z_fwd(int N, int Kz) { return sizeof(float) * 64 * (N + 1) + sizeof(float2) * N * Kz; }
-size_t smem_z_inv(int N, int Kz) { return sizeof(float2) * (16 * Kz + Kz * N); }
+size_t smem_z_fwd(int N, int Kz) { return sizeof(float) * 64 * (N + 4) + sizeof(float2) * N * Kz; }
+size_t smem_z_inv(int N, int Kz) { return sizeof(float) * 64 * (N + 4) + sizeof(float2) * Kz * N; }
 
 void launch_z_fwd(deft_fno *f, const float *in, float2 *out, const float2 *E) {
   const int L = f->C * f->N * f->N;
@@ -594,7 +635,7 @@ void launch_z_fwd(deft_fno *f, const float *in, float2 *out, const float2 *E) {
 }
 void launch_z_inv(deft_fno *f, const float2 *in, float *out, const float2 *G, int acc) {
   const int L = f->C * f->N * f->N;
-  k_dft_z_inv<<<(L + 15) / 16, kT, smem_z_inv(f->N, f->Kz), f->stream>>>(in, out, G, L, f->N, f->Kz,
+  k_dft_z_inv<<<(L + 63) / 64, kT, smem_z_inv(f->N, f->Kz), f->stream>>>(in, out, G, L, f->N, f->Kz,
                                                                         acc);
 }
 void launch_axis(deft_fno *f, const float2 *in, float2 *out, const float2 *E, int outer, int Nin,
@@ -675,8 +716,8 @@ extern "C" {
 
 int deft_fno_create(int device, int N, int channels, int modes, int layers, unsigned long long seed,
                     deft_fno **out) {
-  if (!out || N < 4 || channels != 16 && channels != 4 && channels != 8 || modes < 1 ||
-      2 * modes > N || modes > N / 2 + 1 || layers < 1 || layers > 8)
+  if (!out || N < 4 || (channels != 16 && channels != 4 && channels != 8) || modes < 1 ||
+      modes > kMaxKz || 2 * modes > N || layers < 1 || layers > 8)
     return DEFT_ERR_ARG;
   deft_fno *f = new deft_fno();
   f->device = device;
@@ -739,8 +780,8 @@ int deft_fno_create(int device, int N, int channels, int modes, int layers, unsi
       const float2 e = cexp(-a);
       ezb[z * f->Kz + k] = make_float2((float)(e.x * ck / N3), (float)(e.y * ck / N3));
       const float2 gg = cexp(a);
-      gzi[k * N + z] = make_float2((float)(gg.x * ck / N3), (float)(gg.y * ck / N3));
-      gza[k * N + z] = gg;
+      gzi[z * f->Kz + k] = make_float2((float)(gg.x * ck / N3), (float)(gg.y * ck / N3));
+      gza[z * f->Kz + k] = gg;
     }
   std::vector<float2> eyf(f->Ky * N), eyi(N * f->Ky), exf(f->Kx * N), exi(N * f->Kx);
   for (int k = 0; k < f->Ky; k++)
