@@ -344,6 +344,15 @@ __global__ void __launch_bounds__(kThreads) k_x_fft(typename Cplx<T>::type *data
   }
 }
 
+// Functional parameters the kernels read from a device copy (uploaded before
+// each launch sequence when they change, so captured graphs stay valid
+// across problems).
+struct LocalArgs {
+  double R, kT, mu, nQ, inv_nQ, dV;
+  WbRadius wr;
+  int terms;
+};
+
 // x-FFT of n^, multiplication by the five weights, and the five inverse
 // x-FFTs one field at a time (three tiles of B lines: the forward result and
 // a ping-pong pair), which keeps B wide for coalesced column runs.
@@ -351,7 +360,8 @@ template <typename T, int RN = 0>
 __global__ void __launch_bounds__(kThreads, RN > 0 ? 2 : 1) k_x_conv_fwd(
     const typename Cplx<T>::type *__restrict__ in, typename Cplx<T>::type *__restrict__ out5,
     const T *__restrict__ w3, const T *__restrict__ w2, const T *__restrict__ wv, Geom g,
-    FftPlan px, FastDiv fB, float Rw) {
+    FftPlan px, FastDiv fB, const LocalArgs *__restrict__ lap) {
+  const float Rw = (float)lap->R;
   const int B = (int)fB.d;
   using C = typename Cplx<T>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -427,7 +437,8 @@ template <typename T, int RN = 0>
 __global__ void __launch_bounds__(kThreads, RN > 0 ? 2 : 1) k_x_conv_adj(
     const typename Cplx<T>::type *__restrict__ in5, typename Cplx<T>::type *__restrict__ out,
     const T *__restrict__ w3, const T *__restrict__ w2, const T *__restrict__ wv, Geom g,
-    FftPlan px, FastDiv fB, FastDiv f5B, float Rw) {
+    FftPlan px, FastDiv fB, FastDiv f5B, const LocalArgs *__restrict__ lap) {
+  const float Rw = (float)lap->R;
   const int B = (int)fB.d;
   using C = typename Cplx<T>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -488,12 +499,6 @@ __global__ void __launch_bounds__(kThreads, RN > 0 ? 2 : 1) k_x_conv_adj(
     if (j < J) out[(size_t)e * J + j] = res[idx];
   }
 }
-
-struct LocalArgs {
-  double R, kT, mu, nQ, inv_nQ, dV;
-  WbRadius wr;
-  int terms;
-};
 
 // Ideal-gas integrand kT n (ln(n/nQ) - 1) (src/IdealGas.cpp:68-72), 0 at
 // n = 0, and its derivative kT ln(n/nQ), in the arithmetic type T.
@@ -588,8 +593,9 @@ __global__ void __launch_bounds__(kThreads, RN > 0 ? 2 : 1) k_z_phi(typename Cpl
                                                     const double *__restrict__ n,
                                                     const double *__restrict__ V, Geom g,
                                                     FftPlan pz, FastDiv fP, FastDiv f2P,
-                                                    FastDiv f5P, LocalArgs la,
+                                                    FastDiv f5P, const LocalArgs *__restrict__ lap,
                                                     double *partials) {
+  const LocalArgs la = *lap;
   const int P = (int)fP.d;
   using C = typename Cplx<T>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -644,7 +650,8 @@ __global__ void __launch_bounds__(kThreads, RN > 0 ? 2 : 1) k_z_grad(const typen
                                                      const double *__restrict__ V,
                                                      const double *__restrict__ mask,
                                                      double *__restrict__ grad, Geom g, FftPlan pz,
-                                                     FastDiv fP, LocalArgs la) {
+                                                     FastDiv fP, const LocalArgs *__restrict__ lap) {
+  const LocalArgs la = *lap;
   const int P = (int)fP.d;
   using C = typename Cplx<T>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -691,8 +698,10 @@ template <typename T, int RN = 0>
 __global__ void __launch_bounds__(kThreads, RN > 0 ? 2 : 1) k_z_hess(const typename Cplx<T>::type *__restrict__ S5,
                                                      const double *__restrict__ n, Geom g,
                                                      FftPlan pz, FastDiv fP, FastDiv f5P,
-                                                     LocalArgs la, float *__restrict__ hess,
+                                                     const LocalArgs *__restrict__ lap,
+                                                     float *__restrict__ hess,
                                                      float *__restrict__ hloc) {
+  const LocalArgs la = *lap;
   const int P = (int)fP.d;
   using C = typename Cplx<T>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -730,7 +739,9 @@ __global__ void __launch_bounds__(kThreads, RN > 0 ? 2 : 1) k_z_hess(const typen
 template <typename T, int RN = 0>
 __global__ void __launch_bounds__(kThreads, RN > 0 ? 2 : 1) k_z_jac(typename Cplx<T>::type *S5, Geom g, FftPlan pz,
                                                     FastDiv fP, FastDiv f2P, FastDiv f5P,
-                                                    double c, const float *__restrict__ hess) {
+                                                    const LocalArgs *__restrict__ lap,
+                                                    const float *__restrict__ hess) {
+  const double c = lap->dV * lap->kT;
   const int P = (int)fP.d;
   using C = typename Cplx<T>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -774,7 +785,8 @@ template <typename T, int RN = 0>
 __global__ void __launch_bounds__(kThreads, RN > 0 ? 2 : 1) k_z_hvp_out(
     const typename Cplx<T>::type *__restrict__ in, const double *__restrict__ dx,
     const float *__restrict__ hloc, const double *__restrict__ mask, double *__restrict__ out,
-    Geom g, FftPlan pz, FastDiv fP, LocalArgs la) {
+    Geom g, FftPlan pz, FastDiv fP, const LocalArgs *__restrict__ lap) {
+  const LocalArgs la = *lap;
   const int P = (int)fP.d;
   using C = typename Cplx<T>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -812,7 +824,9 @@ __global__ void __launch_bounds__(kThreads, RN > 0 ? 2 : 1) k_z_hvp_out(
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_local_energy(const double *__restrict__ n,
                                                            const double *__restrict__ V, Geom g,
-                                                           LocalArgs la, double *partials) {
+                                                           const LocalArgs *__restrict__ lap,
+                                                           double *partials) {
+  const LocalArgs la = *lap;
   __shared__ double red[32 * kNumTerms];
   double acc[kNumTerms] = {0, 0, 0, 0, 0, 0};
   for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < g.NR; r += gridDim.x * blockDim.x) {
@@ -1237,6 +1251,7 @@ class EngineImpl {
     cudaFree(wvf);
     cudaFree(hess);
     clear_graphs();
+    cudaFree(la_dev);
     cudaFree(hloc);
     cudaFree(S0);
     cudaFree(S5);
@@ -1404,7 +1419,7 @@ class EngineImpl {
     if (max_blocks < mb32) max_blocks = mb32;
     if (max_blocks < 1024) max_blocks = 1024;
     if (alloc(&partials, sizeof(double) * kNumTerms * max_blocks)) return -1;
-    if (alloc(&results, sizeof(double) * 8)) return -1;
+    if (alloc(&results, sizeof(double) * 8) || alloc(&la_dev, sizeof(LocalArgs))) return -1;
     cudaError_t e = cudaMallocHost((void **)&results_host, sizeof(double) * 8);
     if (e != cudaSuccess) return fail("cudaMallocHost", e);
     int dev = 0, sms = 0;
@@ -1536,7 +1551,7 @@ class EngineImpl {
     with_rn<T>(plan<T>(0), [&](auto rn) {
       k_x_conv_fwd<T, decltype(rn)::value><<<x_tiles(t.Bxf), kThreads, t.smem_xf, stream>>>(
           spec0<T>(), spec5<T>(), table<T>(0), table<T>(1), table<T>(2), g, plan<T>(0), t.fBxf,
-          (float)f.R);
+          la_dev);
     });
     post(kslot<T>(kK_x_conv_fwd));
     y_fft<T>(spec5<T>(), 5, +1);
@@ -1545,6 +1560,7 @@ class EngineImpl {
 
   LocalArgs local_args(const FmtSpec &f) const {
     LocalArgs la;
+    memset(&la, 0, sizeof(la));  // padding too: copies are compared bytewise
     la.R = f.R;
     la.kT = f.kT;
     la.mu = f.mu;
@@ -1557,9 +1573,24 @@ class EngineImpl {
     return la;
   }
 
+  // Device copy of the functional parameters the kernels read; uploaded on
+  // the stream (before any graph launch that reads it) when they change.
+  LocalArgs *la_dev = nullptr;
+  LocalArgs la_last{};
+  bool la_valid = false;
+  int upload_args(const FmtSpec &f) {
+    const LocalArgs la = local_args(f);
+    if (la_valid && !memcmp(&la, &la_last, sizeof(la))) return 0;
+    cudaError_t e = cudaMemcpyAsync(la_dev, &la, sizeof(la), cudaMemcpyHostToDevice, stream);
+    if (e != cudaSuccess) return fail("parameter upload", e);
+    la_last = la;
+    la_valid = true;
+    return 0;
+  }
+
   // ---- CUDA graphs of the evaluation and Hessian-vector launch sequences.
   // A sequence is captured once per key (everything its launches bake in:
-  // kind, precision, buffers, functional parameters) and replayed with one
+  // kind, precision, buffers, which terms are on) and replayed with one
   // cudaGraphLaunch afterwards; with per-kernel event timing on, launches go
   // out one by one.  Launch counts of a replay are those of its capture.
   struct GraphKey {
@@ -1586,10 +1617,7 @@ class EngineImpl {
     k.p[1] = b;
     k.p[2] = c;
     k.p[3] = d;
-    k.R = f.R;
-    k.kT = f.kT;
-    k.mu = f.mu;
-    return k;
+    return k;  // R, kT and mu reach the kernels through la_dev, not the graph
   }
 
   void clear_graphs() {
@@ -1664,6 +1692,7 @@ class EngineImpl {
   int eval(const FmtSpec &f, const double *n, const double *V, const double *mask, double *grad,
            double *E_host, double *terms_host) {
     if ((f.terms & kTermHS) && ensure_table<T>(f.R)) return -1;
+    if (upload_args(f)) return -1;
     const GraphKey key = graph_key(grad ? 1 : 0, sizeof(T), f, n, V, mask, grad);
     if (run_graphed(key, [&] { return eval_launch<T>(f, n, V, mask, grad); })) return -1;
     return finish_energy(E_host, terms_host);
@@ -1673,7 +1702,6 @@ class EngineImpl {
   int eval_launch(const FmtSpec &f, const double *n, const double *V, const double *mask,
                   double *grad) {
     const Tiles &t = tl<T>();
-    const LocalArgs la = local_args(f);
     int nblk;
     if (f.terms & kTermHS) {
       if (forward_weighted<T>(f, n)) return -1;
@@ -1683,10 +1711,10 @@ class EngineImpl {
         constexpr int RN = decltype(rn)::value;
         if (grad)
           k_z_phi<T, true, RN><<<nblk, kThreads, t.smem_phi, stream>>>(
-              spec5<T>(), n, V, g, plan<T>(2), t.fPphi, t.f2Pphi, t.f5Pphi, la, partials);
+              spec5<T>(), n, V, g, plan<T>(2), t.fPphi, t.f2Pphi, t.f5Pphi, la_dev, partials);
         else
           k_z_phi<T, false, RN><<<nblk, kThreads, t.smem_phi, stream>>>(
-              spec5<T>(), n, V, g, plan<T>(2), t.fPphi, t.f2Pphi, t.f5Pphi, la, partials);
+              spec5<T>(), n, V, g, plan<T>(2), t.fPphi, t.f2Pphi, t.f5Pphi, la_dev, partials);
       });
       post(kslot<T>(grad ? kK_z_phi_grad : kK_z_phi_energy));
       if (check("phi")) return -1;
@@ -1696,7 +1724,7 @@ class EngineImpl {
         with_rn<T>(plan<T>(0), [&](auto rn) {
           k_x_conv_adj<T, decltype(rn)::value><<<x_tiles(t.Bxc), kThreads, t.smem_xc, stream>>>(
               spec5<T>(), spec0<T>(), table<T>(0), table<T>(1), table<T>(2), g, plan<T>(0),
-              t.fBxc, t.f5Bxc, (float)f.R);
+              t.fBxc, t.f5Bxc, la_dev);
         });
         post(kslot<T>(kK_x_conv_adj));
         y_fft<T>(spec0<T>(), 1, +1);
@@ -1704,14 +1732,14 @@ class EngineImpl {
     } else {
       nblk = 4 * 152;
       pre(kslot<T>(kK_local_energy));
-      k_local_energy<T><<<nblk, kThreads, 0, stream>>>(n, V, g, la, partials);
+      k_local_energy<T><<<nblk, kThreads, 0, stream>>>(n, V, g, la_dev, partials);
       post(kslot<T>(kK_local_energy));
     }
     if (grad) {
       pre(kslot<T>(kK_z_grad));
       with_rn<T>(plan<T>(2), [&](auto rn) {
         k_z_grad<T, decltype(rn)::value><<<pairs_tiles(t.Pz), kThreads, t.smem_z, stream>>>(
-            spec0<T>(), n, V, mask, grad, g, plan<T>(2), t.fPz, la);
+            spec0<T>(), n, V, mask, grad, g, plan<T>(2), t.fPz, la_dev);
       });
       post(kslot<T>(kK_z_grad));
     }
@@ -1723,7 +1751,7 @@ class EngineImpl {
     if (!hess && (alloc(&hess, sizeof(float) * kHessPacked * (size_t)g.NR) ||
                   alloc(&hloc, sizeof(float) * (size_t)g.NR)))
       return -1;
-    const LocalArgs la = local_args(f);
+    if (upload_args(f)) return -1;
     if (f.terms & kTermHS) {
       if (ensure_table<float>(f.R) || forward_weighted<float>(f, n)) return -1;
     }
@@ -1731,7 +1759,8 @@ class EngineImpl {
     with_rn<float>(plan<float>(2), [&](auto rn) {
       k_z_hess<float, decltype(rn)::value><<<pairs_tiles(t32.Pphi), kThreads, t32.smem_phi,
                                              stream>>>(spec5<float>(), n, g, plan<float>(2),
-                                                       t32.fPphi, t32.f5Pphi, la, hess, hloc);
+                                                       t32.fPphi, t32.f5Pphi, la_dev, hess,
+                                                       hloc);
     });
     post(kslot<float>(kK_z_hess));
     return check("hessian blocks");
@@ -1739,12 +1768,12 @@ class EngineImpl {
 
   int hvp(const FmtSpec &f, const double *dx, const double *mask, double *out) {
     if ((f.terms & kTermHS) && ensure_table<float>(f.R)) return -1;
+    if (upload_args(f)) return -1;
     const GraphKey key = graph_key(2, 4, f, dx, mask, out, hess);
     return run_graphed(key, [&] { return hvp_launch(f, dx, mask, out); });
   }
 
   int hvp_launch(const FmtSpec &f, const double *dx, const double *mask, double *out) {
-    const LocalArgs la = local_args(f);
     if (f.terms & kTermHS) {
       if (forward_weighted<float>(f, dx)) return -1;
       pre(kslot<float>(kK_z_jac));
@@ -1752,7 +1781,7 @@ class EngineImpl {
         k_z_jac<float, decltype(rn)::value><<<pairs_tiles(t32.Pphi), kThreads, t32.smem_phi,
                                               stream>>>(spec5<float>(), g, plan<float>(2),
                                                         t32.fPphi, t32.f2Pphi, t32.f5Pphi,
-                                                        g.dV * f.kT, hess);
+                                                        la_dev, hess);
       });
       post(kslot<float>(kK_z_jac));
       y_fft<float>(spec5<float>(), 5, -1);
@@ -1761,7 +1790,7 @@ class EngineImpl {
         k_x_conv_adj<float, decltype(rn)::value><<<x_tiles(t32.Bxc), kThreads, t32.smem_xc,
                                                    stream>>>(
             spec5<float>(), spec0<float>(), table<float>(0), table<float>(1), table<float>(2), g,
-            plan<float>(0), t32.fBxc, t32.f5Bxc, (float)f.R);
+            plan<float>(0), t32.fBxc, t32.f5Bxc, la_dev);
       });
       post(kslot<float>(kK_x_conv_adj));
       y_fft<float>(spec0<float>(), 1, +1);
@@ -1770,7 +1799,7 @@ class EngineImpl {
     with_rn<float>(plan<float>(2), [&](auto rn) {
       k_z_hvp_out<float, decltype(rn)::value><<<pairs_tiles(t32.Pz), kThreads, t32.smem_z,
                                                 stream>>>(spec0<float>(), dx, hloc, mask, out, g,
-                                                          plan<float>(2), t32.fPz, la);
+                                                          plan<float>(2), t32.fPz, la_dev);
     });
     post(kslot<float>(kK_z_hvp_out));
     return check("hessian-vector product");
@@ -2078,6 +2107,7 @@ int noalloc_energy_grad(const GridSpec &s, const FmtSpec &f, const double *n, co
   const size_t o_S5 = off; off += align256(5 * cs * g.NC);
   const size_t o_part = off; off += align256(sizeof(double) * kNumTerms * nblk);
   const size_t o_res = off; off += align256(sizeof(double) * 8);
+  const size_t o_la = off; off += align256(sizeof(LocalArgs));
   if (off > kNoAllocScratchBytes) {
     noalloc_fail(err, "no-allocation energy_grad: this grid needs " + std::to_string(off) +
                           " bytes of scratch; the fixed device array holds " +
@@ -2121,6 +2151,7 @@ int noalloc_energy_grad(const GridSpec &s, const FmtSpec &f, const double *n, co
   double2 *S5 = reinterpret_cast<double2 *>(base + o_S5);
   double *partials = reinterpret_cast<double *>(base + o_part);
   double *results = reinterpret_cast<double *>(base + o_res);
+  LocalArgs *la_dev = reinterpret_cast<LocalArgs *>(base + o_la);
 
   // twiddles: computed on the host into stack arrays, copied into the scratch
   {
@@ -2153,6 +2184,7 @@ int noalloc_energy_grad(const GridSpec &s, const FmtSpec &f, const double *n, co
   set_smem(k_z_grad<double>, t.smem_z);
 
   LocalArgs la;
+  memset(&la, 0, sizeof(la));
   la.R = f.R;
   la.kT = f.kT;
   la.mu = f.mu;
@@ -2162,6 +2194,12 @@ int noalloc_energy_grad(const GridSpec &s, const FmtSpec &f, const double *n, co
   la.wr.inv_4piR = 1.0 / (4 * M_PI * f.R);
   la.wr.inv_4piR2 = 1.0 / (4 * M_PI * f.R * f.R);
   la.terms = f.terms;
+  // the kernels read it from the scratch array (pageable source, consumed on return)
+  e = cudaMemcpyAsync(la_dev, &la, sizeof(la), cudaMemcpyHostToDevice, stream);
+  if (e != cudaSuccess) {
+    noalloc_fail(err, std::string("parameter copy: ") + cudaGetErrorString(e));
+    return 2;
+  }
   const int ptiles_z = (pairs + t.Pz - 1) / t.Pz;
   const int xt = (g.Ny * g.NzH + t.Bxc - 1) / t.Bxc;
   const dim3 ygrid1((g.NzH + t.By - 1) / t.By, g.Nx, 1), ygrid5((g.NzH + t.By - 1) / t.By, g.Nx, 5);
@@ -2174,19 +2212,19 @@ int noalloc_energy_grad(const GridSpec &s, const FmtSpec &f, const double *n, co
     k_z_r2c<double><<<dim3(ptiles_z, 1), kThreads, t.smem_z, stream>>>(n, S0, g, pz, t.fPz, 1.0);
     k_y_fft<double, -1><<<ygrid1, kThreads, t.smem_y, stream>>>(S0, g, py, t.fBy);
     k_x_conv_fwd<double><<<(g.Ny * g.NzH + t.Bxf - 1) / t.Bxf, kThreads, t.smem_xf, stream>>>(
-        S0, S5, w3, w2, wv, g, px, t.fBxf, (float)f.R);
+        S0, S5, w3, w2, wv, g, px, t.fBxf, la_dev);
     k_y_fft<double, +1><<<ygrid5, kThreads, t.smem_y, stream>>>(S5, g, py, t.fBy);
     k_z_phi<double, true><<<nblk_phi, kThreads, t.smem_phi, stream>>>(
-        S5, n, V, g, pz, t.fPphi, t.f2Pphi, t.f5Pphi, la, partials);
+        S5, n, V, g, pz, t.fPphi, t.f2Pphi, t.f5Pphi, la_dev, partials);
     k_y_fft<double, -1><<<ygrid5, kThreads, t.smem_y, stream>>>(S5, g, py, t.fBy);
     k_x_conv_adj<double><<<xt, kThreads, t.smem_xc, stream>>>(S5, S0, w3, w2, wv, g, px, t.fBxc,
-                                                              t.f5Bxc, (float)f.R);
+                                                              t.f5Bxc, la_dev);
     k_y_fft<double, +1><<<ygrid1, kThreads, t.smem_y, stream>>>(S0, g, py, t.fBy);
   } else {
-    k_local_energy<double><<<nblk, kThreads, 0, stream>>>(n, V, g, la, partials);
+    k_local_energy<double><<<nblk, kThreads, 0, stream>>>(n, V, g, la_dev, partials);
   }
   k_z_grad<double><<<ptiles_z, kThreads, t.smem_z, stream>>>(S0, n, V, mask, grad, g, pz, t.fPz,
-                                                             la);
+                                                             la_dev);
   k_reduce_terms<<<1, kThreads, 0, stream>>>(partials, nblk, g.dV, results);
   double res[8];
   e = cudaGetLastError();
