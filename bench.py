@@ -316,7 +316,7 @@ def run_ours(args, rank, world):
     N = args.N
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(dev)
-    tuned = autotune.load(device=dev)
+    tuned = autotune.load(args.tuning, device=dev) if args.tuning else autotune.load(device=dev)
     peak, peak_kind = measured_peaks()
 
     def barrier():
@@ -335,12 +335,18 @@ def run_ours(args, rank, world):
     n_ws = torch.empty_like(masks[0])
     MIXED, FP64 = _lib.PRECISION_MIXED, _lib.PRECISION_FP64
 
+    phases = {"network_s": [], "cg_s": []}
+
     def warm_step(i):
         s = probs[i]
         sv.set_problem(s, masks[i].data_ptr())
+        t0 = time.perf_counter()
         used, _, gb = net.initial_density(sv.fmt[MIXED], masks[i].data_ptr(), s.eta, s.nb,
                                           n_ws.data_ptr(), bulk_gnorm=True)
+        t1 = time.perf_counter()
         st, _ = sv.solve(MIXED, n_ws.data_ptr(), refine_abs=1e-4 * gb)
+        phases["network_s"].append(t1 - t0)
+        phases["cg_s"].append(time.perf_counter() - t1)
         return st, used
 
     def fp64_step(i):
@@ -383,6 +389,7 @@ def run_ours(args, rank, world):
 
     _lib.check(L.deft_grid_profile(sv.grid, 0))
     ms_w, st_w, ck_w, nl_w = timed(warm_step, "warm start + mixed")
+    phase_means = {k: float(np.mean(v[-args.steps:])) for k, v in phases.items()}
     ms_64, st_64, ck_64, nl_64 = timed(fp64_step, "plain FP64")
     avg = lambda sts, k: sum(getattr(x[0], k) for x in sts) / len(sts)  # noqa: E731
 
@@ -442,7 +449,11 @@ def run_ours(args, rank, world):
             "warm_mixed": {"solve_s": ms_w / 1e3, "iters": avg(st_w, "iter"),
                            "evals": avg(st_w, "evals"), "evals_fp64": avg(st_w, "evals_fp64"),
                            "hvps": avg(st_w, "hvps"), "network_used": used_net,
-                           "final_gnorm_fp64": st_w[-1][0].gnorm},
+                           "final_gnorm_fp64": st_w[-1][0].gnorm,
+                           "host_wall_split_s": dict(phase_means,
+                                                     note="host wall time per timed step: "
+                                                          "checked warm start (network "
+                                                          "forward + energy checks) and CG")},
             "fp64_bulk": {"solve_s": ms_64 / 1e3, "iters": avg(st_64, "iter"),
                           "evals": avg(st_64, "evals"), "final_gnorm": st_64[-1][0].gnorm,
                           "gpu_launches": nl_64},
@@ -572,7 +583,7 @@ def run_reference(args, rank, world):
     }
 
 
-def kernel_case(precision, N, problem="slit", evals=3):
+def kernel_case(precision, N, problem="slit", evals=3, tuning=None):
     """A small fixed case for kernel profiling: `evals` energy+gradient
     evaluations (and, in the mixed form, one Hessian-vector product) of the
     N^3 hard-wall slit (dx = 0.2, eta = 0.3) or of the first timed held-out
@@ -581,7 +592,9 @@ def kernel_case(precision, N, problem="slit", evals=3):
     import torch
     from deft_gb300 import _lib
     from deft_gb300.workloads import Slit
+    from deft_gb300 import autotune
     L = _lib.load()
+    autotune.load(tuning) if tuning else autotune.load()
     s = Slit(N=N, dx=0.2, eta=0.3, seed=1) if problem == "slit" else held_out(N, 4)[3]
     h = ctypes.c_void_p()
     _lib.check(L.deft_ctx_create(0, ctypes.byref(h)))
@@ -631,6 +644,8 @@ def main():
     ap.add_argument("--train-epochs", type=int, default=2)
     ap.add_argument("--train-workers", type=int, default=8,
                     help="concurrent streams generating the training solves")
+    ap.add_argument("--tuning", default=None,
+                    help="tuning file to register instead of the bundled one")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extra", action="store_true", help="skip cuFFT and batched sweep")
     ap.add_argument("--cpu-budget", type=float, default=20.0)
@@ -641,7 +656,7 @@ def main():
     args = ap.parse_args()
     if args.kernel_case:
         print(json.dumps(kernel_case(1 if args.kernel_case == "mixed" else 0, args.N,
-                                     args.case_problem)))
+                                     args.case_problem, tuning=args.tuning)))
         return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

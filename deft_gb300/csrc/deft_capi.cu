@@ -816,6 +816,30 @@ int cg_eval(deft_cg *c, const deft::FmtSpec &spec) {
   return DEFT_OK;
 }
 
+// cg_eval followed by the dot products a_i . b_i (k <= 3); without the
+// effective-potential change of variable the products are queued behind the
+// evaluation, in its graph, and come back with the energy in one sync.
+int cg_eval_dots(deft_cg *c, const deft::FmtSpec &spec, int k, const double *const *a,
+                 const double *const *b, double *out) {
+  Engine *e = eng_of(c);
+  if (c->f->p.terms & DEFT_TERM_VEFF) {
+    if (int s = cg_eval(c, spec)) return s;
+    return e->dots(k, a, b, out) ? eng_err(e) : DEFT_OK;
+  }
+  double E;
+  if (e->energy_grad_dots(spec, c->x, c->f->V, c->f->mask, c->g, &E, k, a, b, out))
+    return eng_err(e);
+  if (c->pg && e->copy(c->g, c->pg)) return eng_err(e);
+  c->evals++;
+  if (spec.precision == deft::kPrecisionFP64) c->evals_fp64++;
+  c->last_eval_mixed = spec.precision != deft::kPrecisionFP64;
+  c->E = E;
+  c->e_cache = E;
+  c->e_valid = true;
+  c->have_g = true;
+  return DEFT_OK;
+}
+
 // Minimizer::energy() (src/Minimizer.h:52), cached while x is unchanged.
 int cg_energy(deft_cg *c, double *E) {
   if (!c->e_valid) {
@@ -836,17 +860,6 @@ int cg_axpy(deft_cg *c, double a, const double *v) {
   return DEFT_OK;
 }
 
-int dots3(deft_cg *c, double *s, double *gg, double *ggold) {
-  const double *a[3] = {c->g, c->g, c->g};
-  const double *b[3] = {c->d, c->g, c->gold};
-  double o[3];
-  if (eng_of(c)->dots(3, a, b, o)) return eng_err(eng_of(c));
-  *s = o[0];
-  *gg = o[1];
-  *ggold = o[2];
-  return DEFT_OK;
-}
-
 // Bracketing secant search on s(a) = grad(x + a d).d from s(0) = s0 < 0,
 // accepting |s| <= 0.1 |s0| with no energy rise beyond rounding.  Leaves x,
 // g, E, gg, ggold at the accepted point.
@@ -858,9 +871,13 @@ int secant_search(deft_cg *c, const deft::FmtSpec &spec, double E0, double s0) {
   for (int it = 0; it < 40; it++) {
     if (int st = cg_axpy(c, a - at, c->d)) return st;
     at = a;
-    if (int st = cg_eval(c, spec)) return st;
-    double s, gg, ggold;
-    if (int st = dots3(c, &s, &gg, &ggold)) return st;
+    double o[3];
+    {
+      const double *da[3] = {c->g, c->g, c->g};
+      const double *db[3] = {c->d, c->g, c->gold};
+      if (int st = cg_eval_dots(c, spec, 3, da, db, o)) return st;
+    }
+    const double s = o[0], gg = o[1], ggold = o[2];
     const double E = c->E;
     if (!std::isfinite(E) || !std::isfinite(s)) {
       hi = a;
@@ -905,11 +922,10 @@ int secant_search(deft_cg *c, const deft::FmtSpec &spec, double E0, double s0) {
 
 int step_secant(deft_cg *c, deft_cg_status *st, const deft::FmtSpec &spec, double gtol) {
   if (!c->have_g) {
-    if (int s = cg_eval(c, spec)) return s;
     const double *a[2] = {c->g, c->g};
     const double *b[2] = {c->g, c->gold};
     double o[2];
-    if (eng_of(c)->dots(2, a, b, o)) return eng_err(eng_of(c));
+    if (int s = cg_eval_dots(c, spec, 2, a, b, o)) return s;
     c->gg = o[0];
     c->ggold = o[1];
   }

@@ -237,9 +237,16 @@ __device__ __forceinline__ void unpack_r2c_store(const typename Cplx<T>::type *r
   }
 }
 
+// Launch bounds of the FP32/FP64 transform kernels.  Register-resident
+// instantiations (RN > 0) ask for two resident blocks, i.e. at most 128
+// registers a thread.  The shared-memory ones set no minimum, which leaves
+// ptxas its own occupancy heuristic (40-64 registers); a minimum of one block
+// let it double their registers and cost a third of their speed.
+#define DEFT_FFT_BOUNDS(RN) __launch_bounds__(kThreads, (RN) > 0 ? 2 : 0)
+
 // Real fields -> half-complex along z.  grid.x = pair tiles, grid.y = field.
 template <typename T, int RN = 0>
-__global__ void __launch_bounds__(kThreads, RN > 0 ? 2 : 1) k_z_r2c(const double *__restrict__ in,
+__global__ void DEFT_FFT_BOUNDS(RN) k_z_r2c(const double *__restrict__ in,
                                                     typename Cplx<T>::type *__restrict__ out,
                                                     Geom g, FftPlan pz, FastDiv fP, T s) {
   const int P = (int)fP.d;
@@ -290,7 +297,7 @@ __global__ void __launch_bounds__(kThreads) k_z_c2r(const typename Cplx<T>::type
 
 // FFT along y of complex fields.  grid = (kz tiles, Nx, fields).
 template <typename T, int SIGN, int RN = 0>
-__global__ void __launch_bounds__(kThreads, RN > 0 ? 2 : 1) k_y_fft(typename Cplx<T>::type *data, Geom g,
+__global__ void DEFT_FFT_BOUNDS(RN) k_y_fft(typename Cplx<T>::type *data, Geom g,
                                                     FftPlan py, FastDiv fB) {
   const int B = (int)fB.d;
   using C = typename Cplx<T>::type;
@@ -357,7 +364,7 @@ struct LocalArgs {
 // x-FFTs one field at a time (three tiles of B lines: the forward result and
 // a ping-pong pair), which keeps B wide for coalesced column runs.
 template <typename T, int RN = 0>
-__global__ void __launch_bounds__(kThreads, RN > 0 ? 2 : 1) k_x_conv_fwd(
+__global__ void DEFT_FFT_BOUNDS(RN) k_x_conv_fwd(
     const typename Cplx<T>::type *__restrict__ in, typename Cplx<T>::type *__restrict__ out5,
     const T *__restrict__ w3, const T *__restrict__ w2, const T *__restrict__ wv, Geom g,
     FftPlan px, FastDiv fB, const LocalArgs *__restrict__ lap) {
@@ -434,7 +441,7 @@ __global__ void __launch_bounds__(kThreads, RN > 0 ? 2 : 1) k_x_conv_fwd(
 // x-FFT of the five partial spectra at once, times the adjoint weights
 // (odd ones negated), summed over the fields, inverse x-FFT of the sum.
 template <typename T, int RN = 0>
-__global__ void __launch_bounds__(kThreads, RN > 0 ? 2 : 1) k_x_conv_adj(
+__global__ void DEFT_FFT_BOUNDS(RN) k_x_conv_adj(
     const typename Cplx<T>::type *__restrict__ in5, typename Cplx<T>::type *__restrict__ out,
     const T *__restrict__ w3, const T *__restrict__ w2, const T *__restrict__ wv, Geom g,
     FftPlan px, FastDiv fB, FastDiv f5B, const LocalArgs *__restrict__ lap) {
@@ -589,7 +596,7 @@ __device__ void z_r2c_store5(typename Cplx<T>::type *res, typename Cplx<T>::type
 // c2r of the five weighted densities, phi and local terms, per-block
 // energies, and (GRAD) r2c of the five partials dV kT dphi/dn_a in place.
 template <typename T, bool GRAD, int RN = 0>
-__global__ void __launch_bounds__(kThreads, RN > 0 ? 2 : 1) k_z_phi(typename Cplx<T>::type *S5,
+__global__ void DEFT_FFT_BOUNDS(RN) k_z_phi(typename Cplx<T>::type *S5,
                                                     const double *__restrict__ n,
                                                     const double *__restrict__ V, Geom g,
                                                     FftPlan pz, FastDiv fP, FastDiv f2P,
@@ -645,7 +652,7 @@ __global__ void __launch_bounds__(kThreads, RN > 0 ? 2 : 1) k_z_phi(typename Cpl
 
 // c2r of the adjoint sum, + local gradient terms, masked.
 template <typename T, int RN = 0>
-__global__ void __launch_bounds__(kThreads, RN > 0 ? 2 : 1) k_z_grad(const typename Cplx<T>::type *__restrict__ in,
+__global__ void DEFT_FFT_BOUNDS(RN) k_z_grad(const typename Cplx<T>::type *__restrict__ in,
                                                      const double *__restrict__ n,
                                                      const double *__restrict__ V,
                                                      const double *__restrict__ mask,
@@ -695,7 +702,7 @@ __global__ void __launch_bounds__(kThreads, RN > 0 ? 2 : 1) k_z_grad(const typen
 // per point the packed symmetric 5x5 second derivative of phi (wb_hess) and
 // the ideal-gas curvature kT/n, both stored in FP32.
 template <typename T, int RN = 0>
-__global__ void __launch_bounds__(kThreads, RN > 0 ? 2 : 1) k_z_hess(const typename Cplx<T>::type *__restrict__ S5,
+__global__ void DEFT_FFT_BOUNDS(RN) k_z_hess(const typename Cplx<T>::type *__restrict__ S5,
                                                      const double *__restrict__ n, Geom g,
                                                      FftPlan pz, FastDiv fP, FastDiv f5P,
                                                      const LocalArgs *__restrict__ lap,
@@ -737,7 +744,7 @@ __global__ void __launch_bounds__(kThreads, RN > 0 ? 2 : 1) k_z_hess(const typen
 // Hessian-vector product, middle stage: c2r of the five weighted
 // perturbations dw, dP = dV kT J dw with the stored blocks, r2c of dP in place.
 template <typename T, int RN = 0>
-__global__ void __launch_bounds__(kThreads, RN > 0 ? 2 : 1) k_z_jac(typename Cplx<T>::type *S5, Geom g, FftPlan pz,
+__global__ void DEFT_FFT_BOUNDS(RN) k_z_jac(typename Cplx<T>::type *S5, Geom g, FftPlan pz,
                                                     FastDiv fP, FastDiv f2P, FastDiv f5P,
                                                     const LocalArgs *__restrict__ lap,
                                                     const float *__restrict__ hess) {
@@ -782,7 +789,7 @@ __global__ void __launch_bounds__(kThreads, RN > 0 ? 2 : 1) k_z_jac(typename Cpl
 // Hessian-vector product, last stage: c2r of the adjoint sum plus the
 // ideal-gas curvature dV kT/n * dx, masked (masked points give 0).
 template <typename T, int RN = 0>
-__global__ void __launch_bounds__(kThreads, RN > 0 ? 2 : 1) k_z_hvp_out(
+__global__ void DEFT_FFT_BOUNDS(RN) k_z_hvp_out(
     const typename Cplx<T>::type *__restrict__ in, const double *__restrict__ dx,
     const float *__restrict__ hloc, const double *__restrict__ mask, double *__restrict__ out,
     Geom g, FftPlan pz, FastDiv fP, const LocalArgs *__restrict__ lap) {
@@ -1013,14 +1020,6 @@ void set_smem(K kernel, size_t bytes) {
   int cap = optin - (int)fa.sharedSizeBytes;
   if (cap < (int)bytes) cap = (int)bytes;  // the launch then reports the shortfall
   cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
-}
-
-int tile_width(int lines, int L, size_t bytes_per_elem, int nbuf, int cap) {
-  int maxb = (int)(kSmemBudget / ((size_t)L * bytes_per_elem * nbuf));
-  if (maxb < 1) maxb = 1;
-  if (maxb > cap) maxb = cap;
-  const int ntiles = (lines + maxb - 1) / maxb;
-  return (lines + ntiles - 1) / ntiles;
 }
 
 }  // namespace
@@ -1419,8 +1418,8 @@ class EngineImpl {
     if (max_blocks < mb32) max_blocks = mb32;
     if (max_blocks < 1024) max_blocks = 1024;
     if (alloc(&partials, sizeof(double) * kNumTerms * max_blocks)) return -1;
-    if (alloc(&results, sizeof(double) * 8) || alloc(&la_dev, sizeof(LocalArgs))) return -1;
-    cudaError_t e = cudaMallocHost((void **)&results_host, sizeof(double) * 8);
+    if (alloc(&results, sizeof(double) * 16) || alloc(&la_dev, sizeof(LocalArgs))) return -1;
+    cudaError_t e = cudaMallocHost((void **)&results_host, sizeof(double) * 16);
     if (e != cudaSuccess) return fail("cudaMallocHost", e);
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
@@ -1594,9 +1593,8 @@ class EngineImpl {
   // cudaGraphLaunch afterwards; with per-kernel event timing on, launches go
   // out one by one.  Launch counts of a replay are those of its capture.
   struct GraphKey {
-    int kind, prec, terms, pad;
-    const void *p[4];
-    double R, kT, mu;
+    int kind, prec, terms, ndots;
+    const void *p[10];
   };
   struct GraphEntry {
     GraphKey key;
@@ -1607,16 +1605,22 @@ class EngineImpl {
   bool use_graphs = true;
 
   static GraphKey graph_key(int kind, int prec, const FmtSpec &f, const void *a, const void *b,
-                            const void *c, const void *d) {
+                            const void *c, const void *d, int kd = 0,
+                            const double *const *da = nullptr, const double *const *db = nullptr) {
     GraphKey k;
     memset(&k, 0, sizeof(k));
     k.kind = kind;
     k.prec = prec;
     k.terms = f.terms;
+    k.ndots = kd;
     k.p[0] = a;
     k.p[1] = b;
     k.p[2] = c;
     k.p[3] = d;
+    for (int i = 0; i < kd; i++) {
+      k.p[4 + 2 * i] = da[i];
+      k.p[5 + 2 * i] = db[i];
+    }
     return k;  // R, kT and mu reach the kernels through la_dev, not the graph
   }
 
@@ -1679,23 +1683,46 @@ class EngineImpl {
     cudaMemcpyAsync(results_host, results, sizeof(double) * 8, cudaMemcpyDeviceToHost, stream);
   }
 
-  int finish_energy(double *E_host, double *terms_host) {
+  int finish_energy(double *E_host, double *terms_host, int kd = 0, double *dots_host = nullptr) {
     cudaError_t e = cudaStreamSynchronize(stream);
     if (e != cudaSuccess) return fail("energy", e);
     harvest();
     if (E_host) *E_host = results_host[kNumTerms];
     if (terms_host) memcpy(terms_host, results_host, sizeof(double) * kNumTerms);
+    for (int i = 0; i < kd; i++) dots_host[i] = results_host[8 + i];
     return 0;
   }
 
+  // Energy (+ gradient) and, with kd > 0, the dot products da[i].db[i] of
+  // vectors that may include the new gradient, all in one launch sequence
+  // and one synchronisation.
   template <typename T>
   int eval(const FmtSpec &f, const double *n, const double *V, const double *mask, double *grad,
-           double *E_host, double *terms_host) {
+           double *E_host, double *terms_host, int kd = 0, const double *const *da = nullptr,
+           const double *const *db = nullptr, double *dots_host = nullptr) {
     if ((f.terms & kTermHS) && ensure_table<T>(f.R)) return -1;
     if (upload_args(f)) return -1;
-    const GraphKey key = graph_key(grad ? 1 : 0, sizeof(T), f, n, V, mask, grad);
-    if (run_graphed(key, [&] { return eval_launch<T>(f, n, V, mask, grad); })) return -1;
-    return finish_energy(E_host, terms_host);
+    const GraphKey key = graph_key(grad ? 1 : 0, sizeof(T), f, n, V, mask, grad, kd, da, db);
+    if (run_graphed(key, [&] {
+          if (eval_launch<T>(f, n, V, mask, grad)) return -1;
+          if (kd > 0) queue_dots(kd, da, db, 8);
+          return check("dots");
+        }))
+      return -1;
+    return finish_energy(E_host, terms_host, kd, dots_host);
+  }
+
+  // Queues k_dots for kd <= 3 pairs into results[slot..] and its copy to the
+  // pinned host block.
+  void queue_dots(int kd, const double *const *a, const double *const *b, int slot) {
+    pre(kK_dots);
+    k_dots<<<dot_blocks, kThreads, 0, stream>>>(kd, a[0], b[0], kd > 1 ? a[1] : nullptr,
+                                                kd > 1 ? b[1] : nullptr, kd > 2 ? a[2] : nullptr,
+                                                kd > 2 ? b[2] : nullptr, g.NR, dot_partials,
+                                                dot_counter, results + slot);
+    post(kK_dots);
+    cudaMemcpyAsync(results_host + slot, results + slot, sizeof(double) * 3,
+                    cudaMemcpyDeviceToHost, stream);
   }
 
   template <typename T>
@@ -1806,10 +1833,12 @@ class EngineImpl {
   }
 
   int eval_any(const FmtSpec &f, const double *n, const double *V, const double *mask,
-               double *grad, double *E_host, double *terms_host) {
+               double *grad, double *E_host, double *terms_host, int kd = 0,
+               const double *const *da = nullptr, const double *const *db = nullptr,
+               double *dots_host = nullptr) {
     if (f.precision == kPrecisionMixed)
-      return eval<float>(f, n, V, mask, grad, E_host, terms_host);
-    return eval<double>(f, n, V, mask, grad, E_host, terms_host);
+      return eval<float>(f, n, V, mask, grad, E_host, terms_host, kd, da, db, dots_host);
+    return eval<double>(f, n, V, mask, grad, E_host, terms_host, kd, da, db, dots_host);
   }
 };
 
@@ -1873,6 +1902,13 @@ int Engine::weighted(const FmtSpec &f, const double *n, double *out5) {
 int Engine::energy(const FmtSpec &f, const double *n, const double *V, const double *mask,
                    double *E_host, double *terms_host) {
   return impl_->eval_any(f, n, V, mask, nullptr, E_host, terms_host);
+}
+
+int Engine::energy_grad_dots(const FmtSpec &f, const double *n, const double *V,
+                             const double *mask, double *grad, double *E_host, int k,
+                             const double *const *a, const double *const *b, double *dots_host) {
+  if (k < 1 || k > 3) return impl_->eval_any(f, n, V, mask, grad, E_host, nullptr);
+  return impl_->eval_any(f, n, V, mask, grad, E_host, nullptr, k, a, b, dots_host);
 }
 
 int Engine::energy_grad(const FmtSpec &f, const double *n, const double *V, const double *mask,

@@ -111,6 +111,13 @@ class Engine {
   int energy_grad(const FmtSpec &f, const double *n, const double *V, const double *mask,
                   double *grad, double *E_host, double *terms_host);
 
+  // energy_grad, then the dot products out_host[i] = a_i . b_i (k <= 3) of
+  // vectors that may include the new gradient, in the same launch sequence
+  // and a single synchronisation.
+  int energy_grad_dots(const FmtSpec &f, const double *n, const double *V, const double *mask,
+                       double *grad, double *E_host, int k, const double *const *a,
+                       const double *const *b, double *dots_host);
+
   // Newton refinement of the mixed form: hess_setup stores, at the point n,
   // the packed second derivatives of phi (FP32, from FP32 weighted
   // densities) and the ideal-gas curvature; hvp then gives out = H dx, the
