@@ -334,6 +334,7 @@ def run_ours(args, rank, world):
     bulks = [torch.tensor(s.n0.reshape(-1), device=dd) for s in probs]
     n_ws = torch.empty_like(masks[0])
     MIXED, FP64 = _lib.PRECISION_MIXED, _lib.PRECISION_FP64
+    PC = _lib.PC_NONE if args.no_precond else _lib.PC_DENSITY
 
     phases = {"network_s": [], "cg_s": []}
 
@@ -344,7 +345,7 @@ def run_ours(args, rank, world):
         used, _, gb = net.initial_density(sv.fmt[MIXED], masks[i].data_ptr(), s.eta, s.nb,
                                           n_ws.data_ptr(), bulk_gnorm=True)
         t1 = time.perf_counter()
-        st, _ = sv.solve(MIXED, n_ws.data_ptr(), refine_abs=1e-4 * gb)
+        st, _ = sv.solve(MIXED, n_ws.data_ptr(), refine_abs=1e-4 * gb, preconditioned=PC)
         phases["network_s"].append(t1 - t0)
         phases["cg_s"].append(time.perf_counter() - t1)
         return st, used
@@ -394,8 +395,12 @@ def run_ours(args, rank, world):
     avg = lambda sts, k: sum(getattr(x[0], k) for x in sts) / len(sts)  # noqa: E731
 
     # one profiled headline step (per-kernel CUDA events; launches go out one by one)
+    # (NVTX range "warm_mixed_step": an ncu launch list of this one solve is
+    # `ncu --nvtx --nvtx-include "warm_mixed_step/" --metrics gpu__time_duration.sum`)
     _lib.check(L.deft_grid_profile(sv.grid, 1))
+    torch.cuda.nvtx.range_push("warm_mixed_step")
     warm_step(args.warmup)
+    torch.cuda.nvtx.range_pop()
     prof_w = kernel_profile(L, sv.grid)
     _lib.check(L.deft_grid_profile(sv.grid, 1))
     fp64_step(args.warmup)
@@ -418,7 +423,7 @@ def run_ours(args, rank, world):
         sv.set_problem(s, mask_dev.data_ptr())
         used, _, gb = net.initial_density(sv.fmt[MIXED], mask_dev.data_ptr(), s.eta, s.nb,
                                           n_ws.data_ptr(), bulk_gnorm=True)
-        st, _ = sv.solve(MIXED, n_ws.data_ptr(), refine_abs=1e-4 * gb)
+        st, _ = sv.solve(MIXED, n_ws.data_ptr(), refine_abs=1e-4 * gb, preconditioned=PC)
         _lib.check(L.deft_cg_get_x(sv.cg[MIXED], out_host.data_ptr(), 0))
     e2e_s = (time.perf_counter() - t0) / K2
     e2e = {"value": e2e_s, "unit": UNIT, "h2d_bytes_per_step": 8 * probs[0].size,
@@ -444,8 +449,10 @@ def run_ours(args, rank, world):
         "data": "synthetic (seeded wall + solute problems, see config)",
         "config": config(N, {
             "parallelism": "replicas only" if world > 1 else "single GPU",
-            "form": "checked learned warm start, FP32 CG stage, Newton refinement on the FP64 "
-                    "gradient (FP32 stage left at 1e-4 of the bulk start's gradient norm)",
+            "form": "checked learned warm start, FP32 CG stage" +
+                    ("" if args.no_precond else " (density-variable diagonal preconditioner "
+                     "n/(kT dV))") + ", Newton refinement on the FP64 gradient (FP32 stage "
+                    "left at 1e-4 of the bulk start's gradient norm)",
             "warm_mixed": {"solve_s": ms_w / 1e3, "iters": avg(st_w, "iter"),
                            "evals": avg(st_w, "evals"), "evals_fp64": avg(st_w, "evals_fp64"),
                            "hvps": avg(st_w, "hvps"), "network_used": used_net,
@@ -646,6 +653,8 @@ def main():
                     help="concurrent streams generating the training solves")
     ap.add_argument("--tuning", default=None,
                     help="tuning file to register instead of the bundled one")
+    ap.add_argument("--no-precond", action="store_true",
+                    help="mixed solve without the density-variable preconditioner")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extra", action="store_true", help="skip cuFFT and batched sweep")
     ap.add_argument("--cpu-budget", type=float, default=20.0)

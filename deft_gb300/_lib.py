@@ -14,6 +14,8 @@ ERR_ARG, ERR_CUDA, ERR_NAN, ERR_LINESEARCH, ERR_MAXITER, ERR_NOMEM = 1, 2, 3, 4,
 TERM_HS, TERM_IDEAL, TERM_MU, TERM_VEXT, TERM_MASK, TERM_VEFF = 1, 2, 4, 8, 16, 32
 NTERMS = 6
 LS_SECANT, LS_QUADRATIC_REF = 0, 1
+PC_NONE, PC_FUNCTIONAL, PC_DENSITY = 0, 1, 2
+HS_WB_NOTENSOR, HS_RF, HS_WB_MARK2 = 0, 1, 2
 
 # Every symbol include/deft_gb300.h declares.
 EXPORTS = (
@@ -49,7 +51,7 @@ PRECISION_FP64, PRECISION_MIXED = 0, 1
 
 class FmtParams(ctypes.Structure):
     _fields_ = [("R", ctypes.c_double), ("kT", ctypes.c_double), ("mu", ctypes.c_double),
-                ("terms", ctypes.c_int), ("precision", ctypes.c_int)]
+                ("terms", ctypes.c_int), ("precision", ctypes.c_int), ("functional", ctypes.c_int)]
 
 
 class CgParams(ctypes.Structure):

@@ -91,6 +91,7 @@ deft::FmtSpec spec_of(const deft_fmt *f) {
   s.terms = f->p.terms;
   s.precision = f->p.precision == DEFT_PRECISION_MIXED ? deft::kPrecisionMixed
                                                        : deft::kPrecisionFP64;
+  s.hs = f->p.functional;
   if (!f->V) s.terms &= ~DEFT_TERM_VEXT;
   if (!f->mask) s.terms &= ~DEFT_TERM_MASK;
   return s;
@@ -406,11 +407,18 @@ int deft_grid_profile_entry(deft_grid *g, int i, const char **name, long long *l
   return DEFT_OK;
 }
 
-int deft_fmt_create(deft_grid *g, const deft_fmt_params *p, deft_fmt **out) {
-  if (!g || !p || !out) return set_err(DEFT_ERR_ARG, "NULL argument");
+static int check_fmt_params(const deft_fmt_params *p) {
   if (!(p->R > 0) || !(p->kT > 0)) return set_err(DEFT_ERR_ARG, "R and kT must be positive");
   if (p->precision != DEFT_PRECISION_FP64 && p->precision != DEFT_PRECISION_MIXED)
     return set_err(DEFT_ERR_ARG, "unknown precision");
+  if (p->functional < DEFT_HS_WB_NOTENSOR || p->functional > DEFT_HS_WB_MARK2)
+    return set_err(DEFT_ERR_ARG, "unknown hard-sphere functional");
+  return DEFT_OK;
+}
+
+int deft_fmt_create(deft_grid *g, const deft_fmt_params *p, deft_fmt **out) {
+  if (!g || !p || !out) return set_err(DEFT_ERR_ARG, "NULL argument");
+  if (int s = check_fmt_params(p)) return s;
   cudaSetDevice(g->ctx->device);
   deft_fmt *f = new deft_fmt();
   f->grid = g;
@@ -440,9 +448,7 @@ int deft_fmt_destroy(deft_fmt *f) {
 
 int deft_fmt_set_params(deft_fmt *f, const deft_fmt_params *p) {
   if (!f || !p) return set_err(DEFT_ERR_ARG, "NULL argument");
-  if (!(p->R > 0) || !(p->kT > 0)) return set_err(DEFT_ERR_ARG, "R and kT must be positive");
-  if (p->precision != DEFT_PRECISION_FP64 && p->precision != DEFT_PRECISION_MIXED)
-    return set_err(DEFT_ERR_ARG, "unknown precision");
+  if (int s = check_fmt_params(p)) return s;
   f->p = *p;
   return DEFT_OK;
 }
@@ -653,7 +659,7 @@ int deft_fmt_energy_grad_noalloc(const double lat[9], int Nx, int Ny, int Nz,
                                  const double *mask, double *E_out, double *grad_out,
                                  double *terms_out, void *stream) {
   if (!lat || !p || !n || !E_out || !grad_out) return set_err(DEFT_ERR_ARG, "NULL argument");
-  if (!(p->R > 0) || !(p->kT > 0)) return set_err(DEFT_ERR_ARG, "R and kT must be positive");
+  if (int s = check_fmt_params(p)) return s;
   if ((p->terms & DEFT_TERM_VEXT) && !V)
     return set_err(DEFT_ERR_ARG, "DEFT_TERM_VEXT set but V is NULL");
   if ((p->terms & DEFT_TERM_MASK) && !mask)
@@ -670,6 +676,7 @@ int deft_fmt_energy_grad_noalloc(const double lat[9], int Nx, int Ny, int Nz,
   f.kT = p->kT;
   f.mu = p->mu;
   f.terms = p->terms;
+  f.hs = p->functional;
   std::string err;
   const int r = deft::noalloc_energy_grad(s, f, n, V, mask, grad_out, E_out, terms_out,
                                           (cudaStream_t)stream, &err);
@@ -684,10 +691,21 @@ size_t deft_noalloc_scratch_bytes(void) { return deft::noalloc_scratch_bytes(); 
 // ---------------------------------------------------------------------------
 // Minimiser
 
-int deft_cg_create(deft_fmt *f, const deft_cg_params *p, deft_cg **out) {
-  if (!f || !p || !out) return set_err(DEFT_ERR_ARG, "NULL argument");
+static int check_cg_params(const deft_fmt *f, const deft_cg_params *p) {
   if (p->linesearch != DEFT_LS_SECANT && p->linesearch != DEFT_LS_QUADRATIC_REF)
     return set_err(DEFT_ERR_ARG, "unknown line search");
+  if (p->preconditioned < DEFT_PC_NONE || p->preconditioned > DEFT_PC_DENSITY)
+    return set_err(DEFT_ERR_ARG, "unknown preconditioner");
+  if (p->preconditioned == DEFT_PC_DENSITY &&
+      (p->linesearch != DEFT_LS_SECANT || (f->p.terms & DEFT_TERM_VEFF)))
+    return set_err(DEFT_ERR_ARG,
+                   "the density preconditioner needs the secant search and the density variable");
+  return DEFT_OK;
+}
+
+int deft_cg_create(deft_fmt *f, const deft_cg_params *p, deft_cg **out) {
+  if (!f || !p || !out) return set_err(DEFT_ERR_ARG, "NULL argument");
+  if (int s = check_cg_params(f, p)) return s;
   cudaSetDevice(f->grid->ctx->device);
   deft_cg *c = new deft_cg();
   c->f = f;
@@ -714,8 +732,7 @@ int deft_cg_create(deft_fmt *f, const deft_cg_params *p, deft_cg **out) {
 
 int deft_cg_set_params(deft_cg *c, const deft_cg_params *p) {
   if (!c || !p) return set_err(DEFT_ERR_ARG, "NULL argument");
-  if (p->linesearch != DEFT_LS_SECANT && p->linesearch != DEFT_LS_QUADRATIC_REF)
-    return set_err(DEFT_ERR_ARG, "unknown line search");
+  if (int s = check_cg_params(c->f, p)) return s;
   cudaSetDevice(c->f->grid->ctx->device);
   if (p->preconditioned && !c->pg) {
     cudaError_t e = cudaMalloc((void **)&c->pg, sizeof(double) * nr(c->f->grid));
@@ -803,9 +820,23 @@ namespace {
 Engine *eng_of(deft_cg *c) { return c->f->grid->eng; }
 
 // Energy + gradient at x into c->g, c->E.
+// The constraint mask when the functional applies one, else NULL.
+const double *active_mask(const deft_fmt *f) {
+  return (f->p.terms & DEFT_TERM_MASK) ? f->mask : nullptr;
+}
+
+// pg = M^-1 g for the density preconditioner (DEFT_PC_DENSITY).
+int density_precond(deft_cg *c, const deft::FmtSpec &spec) {
+  Engine *e = eng_of(c);
+  return e->diag_precond(spec, c->x, c->g, active_mask(c->f), c->pg) ? eng_err(e) : DEFT_OK;
+}
+
 int cg_eval(deft_cg *c, const deft::FmtSpec &spec) {
   double E;
-  if (int s = fmt_eval(c->f, spec, c->x, c->g, c->pg, &E, nullptr)) return s;
+  const bool pcd = c->pg && c->p.preconditioned == DEFT_PC_DENSITY;
+  if (int s = fmt_eval(c->f, spec, c->x, c->g, pcd ? nullptr : c->pg, &E, nullptr)) return s;
+  if (pcd)
+    if (int s = density_precond(c, spec)) return s;
   c->evals++;
   if (spec.precision == deft::kPrecisionFP64) c->evals_fp64++;
   c->last_eval_mixed = spec.precision != deft::kPrecisionFP64;
@@ -829,7 +860,11 @@ int cg_eval_dots(deft_cg *c, const deft::FmtSpec &spec, int k, const double *con
   double E;
   if (e->energy_grad_dots(spec, c->x, c->f->V, c->f->mask, c->g, &E, k, a, b, out))
     return eng_err(e);
-  if (c->pg && e->copy(c->g, c->pg)) return eng_err(e);
+  if (c->pg && c->p.preconditioned == DEFT_PC_DENSITY) {
+    if (int s = density_precond(c, spec)) return s;
+  } else if (c->pg && e->copy(c->g, c->pg)) {
+    return eng_err(e);
+  }
   c->evals++;
   if (spec.precision == deft::kPrecisionFP64) c->evals_fp64++;
   c->last_eval_mixed = spec.precision != deft::kPrecisionFP64;
@@ -1038,7 +1073,7 @@ int step_newton(deft_cg *c, deft_cg_status *st, const deft::FmtSpec &spec) {
   double *r = c->gold, *p = c->d, *q = c->q, *dx = c->dxv;
   double *z = c->g;  // the FP64 gradient is re-evaluated after the step
   if (e->scal_add(0.0, r, -1.0, c->g)) return eng_err(e);
-  if (e->diag_precond(spec, c->x, r, c->f->mask, z) || e->copy(z, p)) return eng_err(e);
+  if (e->diag_precond(spec, c->x, r, active_mask(c->f), z) || e->copy(z, p)) return eng_err(e);
   c->have_g = false;
   if (cudaMemsetAsync(dx, 0, bytes, stream) != cudaSuccess) return set_err(DEFT_ERR_CUDA, "memset");
   double rz;
@@ -1060,7 +1095,7 @@ int step_newton(deft_cg *c, deft_cg_status *st, const deft::FmtSpec &spec) {
     if (!(pq > 0)) break;  // no positive curvature along p: keep the step so far
     const double alpha = rz / pq;
     if (e->axpy(alpha, p, dx) || e->axpy(-alpha, q, r)) return eng_err(e);
-    if (e->diag_precond(spec, c->x, r, c->f->mask, z)) return eng_err(e);
+    if (e->diag_precond(spec, c->x, r, active_mask(c->f), z)) return eng_err(e);
     double o[2];
     {
       const double *a[2] = {r, r};

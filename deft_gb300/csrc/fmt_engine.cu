@@ -1568,6 +1568,7 @@ class EngineImpl {
     la.dV = g.dV;
     la.wr.inv_4piR = 1.0 / (4 * M_PI * f.R);
     la.wr.inv_4piR2 = 1.0 / (4 * M_PI * f.R * f.R);
+    la.wr.kind = f.hs;
     la.terms = f.terms;
     return la;
   }
@@ -2229,6 +2230,7 @@ int noalloc_energy_grad(const GridSpec &s, const FmtSpec &f, const double *n, co
   la.dV = g.dV;
   la.wr.inv_4piR = 1.0 / (4 * M_PI * f.R);
   la.wr.inv_4piR2 = 1.0 / (4 * M_PI * f.R * f.R);
+  la.wr.kind = f.hs;
   la.terms = f.terms;
   // the kernels read it from the scratch array (pageable source, consumed on return)
   e = cudaMemcpyAsync(la_dev, &la, sizeof(la), cudaMemcpyHostToDevice, stream);

@@ -38,6 +38,7 @@ struct FmtSpec {
   double R, kT, mu;
   int terms;
   int precision = kPrecisionFP64;
+  int hs = 0;  // hard-sphere functional kind (kHs* of wb_phi.cuh)
 };
 
 struct Geom {

@@ -54,6 +54,13 @@ extern "C" {
 #define DEFT_LS_SECANT 0         /* derivative (secant) search on grad.d, reuses the gradient */
 #define DEFT_LS_QUADRATIC_REF 1  /* QuadraticLineMinimizer, src/QuadraticLineMinimizer.cpp:27-198 */
 
+/* deft_cg_params.preconditioned */
+#define DEFT_PC_NONE 0
+#define DEFT_PC_FUNCTIONAL 1 /* the functional's preconditioned gradient (PreconditionedConjugateGradient) */
+#define DEFT_PC_DENSITY 2    /* diagonal M^-1 = n / (kT dV) in the density variable: the inverse of
+                                the ideal-gas curvature, zero on masked points (secant search,
+                                density variable only; an extension, not in the reference) */
+
 typedef struct deft_ctx deft_ctx;
 typedef struct deft_grid deft_grid;
 typedef struct deft_fmt deft_fmt;
@@ -64,12 +71,20 @@ typedef struct deft_cg deft_cg;
 #define DEFT_PRECISION_MIXED 1  /* FFTs, weights and phi in FP32; energies, dot products,
                                    line search and the final refinement in FP64 */
 
+/* Hard-sphere functional (deft_fmt_params.functional); all three share the
+ * weighted densities n3, n2, n2v and differ in their phi2, phi3 prefactors. */
+#define DEFT_HS_WB_NOTENSOR 0 /* HardSpheresWBnotensor, src/HardSpheres.cpp:137-159 */
+#define DEFT_HS_RF 1          /* HardSpheresRF (Rosenfeld), src/HardSpheres.cpp:69-88 */
+#define DEFT_HS_WB_MARK2 2    /* WhiteBearMarkII (whitebear_m2, src/haskell/WhiteBear.hs:140-159),
+                                 vector third term */
+
 typedef struct {
   double R;   /* hard-sphere radius */
   double kT;  /* temperature (the kT argument of Functional::integral, src/Functional.h:131) */
   double mu;  /* ChemicalPotential coefficient (the tree adds mu*n) */
   int terms;  /* DEFT_TERM_* bit set */
   int precision; /* DEFT_PRECISION_*; the allocation-free entry point is FP64 only */
+  int functional; /* DEFT_HS_* (0, the White Bear functional, when left zeroed) */
 } deft_fmt_params;
 
 typedef struct {
@@ -81,8 +96,10 @@ typedef struct {
   double refine_rel; /* mixed evaluator only: leave the FP32 CG stage for the FP64-residual
                         Newton refinement once |grad| < refine_rel * |grad at start|
                         (0 = default 1e-4) */
-  int preconditioned; /* 1: PreconditionedConjugateGradient (src/ConjugateGradient.cpp:
-                         115-160): directions from the preconditioned gradient */
+  int preconditioned; /* DEFT_PC_*.  1: PreconditionedConjugateGradient
+                         (src/ConjugateGradient.cpp:115-160): directions from the
+                         preconditioned gradient.  2: the same Polak-Ribiere formulas with
+                         the density-variable diagonal preconditioner */
   double refine_abs; /* mixed evaluator only: if > 0, leave the FP32 stage once
                         |grad| < refine_abs instead (e.g. a fraction of the bulk start's
                         gradient norm when starting from a warm start) */

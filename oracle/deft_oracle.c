@@ -239,6 +239,75 @@ static void phi_wb(double R, double n3, double n2, double vx, double vy, double 
   d[4] = cv * vz;
 }
 
+/* The Rosenfeld and mark II functionals share phi1 and the n2/v structure
+ * of phi2 and phi3 with the White Bear one:
+ *   phi2 = (n2^2 - |v|^2) / (4 pi R) * f2(n3),  phi3 = n2 (n2^2 - 3|v|^2) * f3(n3).
+ * Rosenfeld (src/HardSpheres.cpp:69-88): f2 = 1/(1-e), f3 = 1/(24 pi (1-e)^2).
+ * Mark II (src/haskell/WhiteBear.hs:140-159): f2 = P2/(1-e), f3 = P3/(24 pi (1-e)^2),
+ *   P2 = 1 + (6 - 3e + 6 (1-e) ln(1-e)/e) / 9,
+ *   P3 = 1 - (6 - 9e + 6e^2 + 6 (1-e)^2 ln(1-e)/e) / (9e),
+ * with the Taylor series of P2 and P3 below |e| = 0.1 (20 terms):
+ *   P2 = 1 + (2/3) sum_{k>=2} e^k/(k(k+1)),
+ *   P3 = 1 - (4/9) e + (4/3) sum_{k>=3} e^(k-1)/((k-1)k(k+1)). */
+static void m2_P(double e, double *P2, double *dP2, double *P3, double *dP3) {
+  if (fabs(e) < 0.1) {
+    double p2 = 0, dp2 = 0, p3 = 0, dp3 = 0;
+    for (int k = 2; k <= 20; k++) {
+      const double a = 1.0 / ((double)k * (k + 1));
+      p2 += a * pow(e, k);
+      dp2 += k * a * pow(e, k - 1);
+      if (k >= 3) {
+        p3 += a / (k - 1) * pow(e, k - 1);
+        dp3 += a * pow(e, k - 2);
+      }
+    }
+    *P2 = 1 + 2.0 / 3 * p2;
+    *dP2 = 2.0 / 3 * dp2;
+    *P3 = 1 - 4.0 / 9 * e + 4.0 / 3 * p3;
+    *dP3 = -4.0 / 9 + 4.0 / 3 * dp3;
+  } else {
+    const double l = log(1 - e);
+    const double B = (1 - e) * l / e, dB = -(e + l) / (e * e);
+    *P2 = 1 + (6 - 3 * e + 6 * B) / 9;
+    *dP2 = (6 * dB - 3) / 9;
+    const double g = (1 - e) * (1 - e) * l, dg = -2 * (1 - e) * l - (1 - e);
+    const double C = g / e, dC = dg / e - g / (e * e);
+    const double N = 6 - 9 * e + 6 * e * e + 6 * C, dN = 12 * e - 9 + 6 * dC;
+    *P3 = 1 - N / e / 9;
+    *dP3 = -(dN / e - N / (e * e)) / 9;
+  }
+}
+
+static void phi_hs(int kind, double R, double n3, double n2, double vx, double vy, double vz,
+                   double phi[3], double d[5]) {
+  if (kind == ORACLE_HS_WB) {
+    phi_wb(R, n3, n2, vx, vy, vz, phi, d);
+    return;
+  }
+  const double v2 = vx * vx + vy * vy + vz * vz;
+  const double u = 1 / (1 - n3), l = log(1 - n3);
+  const double a1 = 1 / (4 * M_PI * R * R), a2 = 1 / (4 * M_PI * R);
+  double f2 = u, df2 = u * u, P3 = 1, dP3 = 0;
+  if (kind == ORACLE_HS_M2) {
+    double P2, dP2;
+    m2_P(n3, &P2, &dP2, &P3, &dP3);
+    f2 = P2 * u;
+    df2 = dP2 * u + P2 * u * u;
+  }
+  const double f3 = P3 * u * u / (24 * M_PI);
+  const double df3 = (dP3 + 2 * P3 * u) * u * u / (24 * M_PI);
+  const double q = n2 * n2 - v2, t3 = n2 * (n2 * n2 - 3 * v2);
+  phi[0] = f3 * t3;
+  phi[1] = -a1 * n2 * l;
+  phi[2] = a2 * q * f2;
+  d[0] = a1 * n2 * u + a2 * q * df2 + df3 * t3;
+  d[1] = -a1 * l + 2 * a2 * n2 * f2 + 3 * f3 * q;
+  const double cv = -2 * a2 * f2 - 6 * f3 * n2;
+  d[2] = cv * vx;
+  d[3] = cv * vy;
+  d[4] = cv * vz;
+}
+
 static double nQ_of(double kT) {
   /* find_nQ, src/IdealGas.cpp:54-59: (m kT / 2 pi)^(3/2), m = water mass */
   const double x = 18.01528 * 1822.8885 * kT / (2 * M_PI);
@@ -260,7 +329,8 @@ static double eval(const oracle_params *p, const double *n, const double *V, con
     if (grad) part = (double *)malloc(sizeof(double) * 5 * nr);
     for (size_t i = 0; i < nr; i++) {
       double phi[3], d[5];
-      phi_wb(p->R, wd[i], wd[nr + i], wd[2 * nr + i], wd[3 * nr + i], wd[4 * nr + i], phi, d);
+      phi_hs(p->hs, p->R, wd[i], wd[nr + i], wd[2 * nr + i], wd[3 * nr + i], wd[4 * nr + i], phi,
+             d);
       t[0] += kT * phi[0];
       t[1] += kT * phi[1];
       t[2] += kT * phi[2];
@@ -402,6 +472,7 @@ typedef struct {
   double *g;
   int g_valid;
   double *pg; /* preconditioned gradient (preconditioned CG only) */
+  int pc;     /* 2: pg = M^-1 g with M^-1 = n / (kT dV) on unmasked points */
 } mstate;
 
 static double m_energy(mstate *m) {
@@ -414,6 +485,14 @@ static double m_energy(mstate *m) {
 static const double *m_grad(mstate *m) {
   if (!m->g_valid) {
     m->e = eval_x(m->p, m->x, m->V, m->mask, m->g, m->pg, NULL);
+    if (m->pc == 2 && m->pg) {
+      /* inverse ideal-gas curvature kT dV / n as a diagonal preconditioner */
+      const double inv_c = 1.0 / (m->p->kT * oracle_dvolume(m->p));
+      for (size_t i = 0; i < m->n; i++) {
+        const double mk = m->mask ? m->mask[i] : 1.0, nv = m->x[i];
+        m->pg[i] = (mk == 0 || !(nv > 0)) ? 0.0 : m->g[i] * nv * inv_c;
+      }
+    }
     m->e_valid = 1;
     m->g_valid = 1;
   }
@@ -645,7 +724,7 @@ int oracle_cg_solve(const oracle_params *p, const double *V, const double *mask,
 int oracle_cg_solve_pc(const oracle_params *p, const double *V, const double *mask,
                        double *n_inout, double gtol, int maxiter, double step, int precond,
                        double *out3) {
-  mstate m = {p, V, mask, n_inout, (size_t)p->Nx * p->Ny * p->Nz, 0, 0, NULL, 0, NULL};
+  mstate m = {p, V, mask, n_inout, (size_t)p->Nx * p->Ny * p->Nz, 0, 0, NULL, 0, NULL, precond};
   m.g = (double *)malloc(sizeof(double) * m.n);
   if (precond) m.pg = (double *)malloc(sizeof(double) * m.n);
   double pgoldsqr = 0;

@@ -27,11 +27,19 @@ enum {
   ORACLE_VEFF = 32, /* OfEffectivePotential: the variable is Veff, n = exp(-Veff/kT) */
 };
 
+/* Hard-sphere functional kinds (oracle_params.hs). */
+enum {
+  ORACLE_HS_WB = 0, /* HardSpheresWBnotensor, src/HardSpheres.cpp:137-159 */
+  ORACLE_HS_RF = 1, /* HardSpheresRF (Rosenfeld), src/HardSpheres.cpp:69-88 */
+  ORACLE_HS_M2 = 2, /* White Bear mark II, src/haskell/WhiteBear.hs:140-159 */
+};
+
 typedef struct {
   int Nx, Ny, Nz;
   double lat[9]; /* a1 = lat[0..2], a2 = lat[3..5], a3 = lat[6..8] (Cartesian) */
   double R, kT, mu;
   int terms;
+  int hs; /* ORACLE_HS_* */
 } oracle_params;
 
 /* Per-term energies, in the reference's sum order: phi3, phi1, phi2 (the
@@ -80,7 +88,9 @@ int oracle_pcg_quadratic(const oracle_params *p, const double *V, const double *
  * Returns the iteration count; out3 = {final energy, final |grad|, evals}. */
 int oracle_cg_solve(const oracle_params *p, const double *V, const double *mask,
                     double *n_inout, double gtol, int maxiter, double step, double *out3);
-/* The same with preconditioned directions when precond != 0. */
+/* The same with preconditioned directions: precond 1 uses the functional's
+ * preconditioned gradient (PreconditionedConjugateGradient), precond 2 the
+ * diagonal M^-1 = n / (kT dV) in the density variable (unmasked points). */
 int oracle_cg_solve_pc(const oracle_params *p, const double *V, const double *mask,
                        double *n_inout, double gtol, int maxiter, double step, int precond,
                        double *out3);

@@ -21,6 +21,7 @@ ORACLE_SO = os.path.join(HERE, "liboracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libdeft_ref.so")
 
 HS, IDEAL, MU, VEXT, MASK, VEFF = 1, 2, 4, 8, 16, 32
+HS_WB, HS_RF, HS_M2 = 0, 1, 2  # hard-sphere functional kinds (oracle_params.hs)
 NTERMS = 6
 TERM_NAMES = ("phi3", "phi1", "phi2", "ideal_gas", "chemical_potential", "external_potential")
 
@@ -39,7 +40,7 @@ class _Params(ctypes.Structure):
         ("Nx", ctypes.c_int), ("Ny", ctypes.c_int), ("Nz", ctypes.c_int),
         ("lat", ctypes.c_double * 9),
         ("R", ctypes.c_double), ("kT", ctypes.c_double), ("mu", ctypes.c_double),
-        ("terms", ctypes.c_int),
+        ("terms", ctypes.c_int), ("hs", ctypes.c_int),
     ]
 
 
@@ -127,6 +128,7 @@ def ref():
                               ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int, _dp,
                               _dp, _dp, ctypes.c_int, ctypes.c_double, _dp]
         L.ref_fft_count.restype = ctypes.c_longlong
+        L.ref_set_hs.argtypes = [ctypes.c_int]
         _ref = L
     return _ref
 
@@ -134,7 +136,9 @@ def ref():
 class Problem:
     """One evaluation setting: lattice (rows a1, a2, a3), grid, R, kT, mu, terms."""
 
-    def __init__(self, lat, N, R=1.0, kT=1.0, mu=0.0, terms=HS | IDEAL | MU, V=None, mask=None):
+    def __init__(self, lat, N, R=1.0, kT=1.0, mu=0.0, terms=HS | IDEAL | MU, V=None, mask=None,
+                 hs=0):
+        self.hs = int(hs)  # HS_WB, HS_RF or HS_M2
         self.lat = np.ascontiguousarray(np.asarray(lat, dtype=np.float64).reshape(9))
         self.N = tuple(int(v) for v in N)
         self.R, self.kT, self.mu, self.terms = float(R), float(kT), float(mu), int(terms)
@@ -154,7 +158,7 @@ class Problem:
         p.Nx, p.Ny, p.Nz = self.N
         for i in range(9):
             p.lat[i] = self.lat[i]
-        p.R, p.kT, p.mu, p.terms = self.R, self.kT, self.mu, self.terms
+        p.R, p.kT, p.mu, p.terms, p.hs = self.R, self.kT, self.mu, self.terms, self.hs
         return p
 
     # -- restatement -------------------------------------------------------
@@ -210,24 +214,30 @@ class Problem:
         x = np.array(n, dtype=np.float64).reshape(-1)
         out = np.zeros(3)
         it = lib().oracle_cg_solve_pc(ctypes.byref(self.params()), _ptr(self.V), _ptr(self.mask),
-                                      _ptr(x), gtol, maxiter, step, int(bool(preconditioned)),
+                                      _ptr(x), gtol, maxiter, step, int(preconditioned),
                                       _ptr(out))
         return x, {"iters": it, "energy": out[0], "gnorm": out[1], "evals": int(out[2])}
 
     # -- unmodified reference ---------------------------------------------
+    def _ref(self):
+        """The reference build, set to this problem's hard-sphere functional."""
+        L = ref()
+        L.ref_set_hs(self.hs)
+        return L
+
     def ref_energy_grad(self, n, grad=True):
         n = np.ascontiguousarray(n, dtype=np.float64).reshape(-1)
         E = ctypes.c_double(0)
         t = np.zeros(8)
         g = np.empty(self.size) if grad else None
-        nt = ref().ref_eval(_ptr(self.lat), *self.N, self.R, self.kT, self.mu, self.terms,
+        nt = self._ref().ref_eval(_ptr(self.lat), *self.N, self.R, self.kT, self.mu, self.terms,
                             _ptr(n), _ptr(self.V), _ptr(self.mask), ctypes.byref(E), _ptr(t), _ptr(g))
         return E.value, g, t[:nt]
 
     def ref_weighted(self, n):
         n = np.ascontiguousarray(n, dtype=np.float64).reshape(-1)
         out = np.empty(5 * self.size)
-        ref().ref_weighted(_ptr(self.lat), *self.N, self.R, _ptr(n), _ptr(out))
+        self._ref().ref_weighted(_ptr(self.lat), *self.N, self.R, _ptr(n), _ptr(out))
         return out.reshape(5, -1)
 
     def ref_eval_veff(self, x):
@@ -237,7 +247,7 @@ class Problem:
         E = ctypes.c_double(0)
         g = np.empty(self.size)
         pg = np.empty(self.size)
-        ref().ref_eval_veff(_ptr(self.lat), *self.N, self.R, self.kT, self.mu, self.terms,
+        self._ref().ref_eval_veff(_ptr(self.lat), *self.N, self.R, self.kT, self.mu, self.terms,
                             _ptr(x), _ptr(self.V), _ptr(self.mask), ctypes.byref(E), _ptr(g),
                             _ptr(pg))
         return E.value, g, pg
@@ -245,7 +255,7 @@ class Problem:
     def ref_pcg(self, x, iters, step=0.1):
         x = np.array(x, dtype=np.float64).reshape(-1)
         e = np.zeros(iters)
-        k = ref().ref_pcg(_ptr(self.lat), *self.N, self.R, self.kT, self.mu, self.terms,
+        k = self._ref().ref_pcg(_ptr(self.lat), *self.N, self.R, self.kT, self.mu, self.terms,
                           int(bool(self.terms & VEFF)), _ptr(self.V), _ptr(self.mask), _ptr(x),
                           iters, step, _ptr(e))
         return x, e[:k]
@@ -253,7 +263,7 @@ class Problem:
     def ref_cg(self, n, iters, step=0.1):
         x = np.array(n, dtype=np.float64).reshape(-1)
         e = np.zeros(iters)
-        k = ref().ref_cg(_ptr(self.lat), *self.N, self.R, self.kT, self.mu, self.terms,
+        k = self._ref().ref_cg(_ptr(self.lat), *self.N, self.R, self.kT, self.mu, self.terms,
                          _ptr(self.V), _ptr(self.mask), _ptr(x), iters, step, _ptr(e))
         return x, e[:k]
 

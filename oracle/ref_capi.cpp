@@ -36,10 +36,50 @@ static Lattice make_lat(const double *lat) {
                  Cartesian(lat[6], lat[7], lat[8]));
 }
 
+// White Bear mark II as src/haskell/WhiteBear.hs:140-159 defines it (the
+// generated WhiteBearMarkII of papers/contact/figs/walls.cpp:48-49 needs ghc,
+// which is absent), composed here from the reference's own weighted
+// densities and Functional algebra, with n1 = n2/(4 pi R), n1v = n2v/(4 pi R),
+// n0 = n2/(4 pi R^2):
+//   Phi2 = (1 + n3^2 phi2II / 9) (n2 n1 - n1v.n2v) / (1 - n3)
+//   Phi3 = (1 - 4 n3 phi3II / 9) (n2^3 - 3 n2 |n2v|^2) / (24 pi (1 - n3)^2)
+// The compiled HardSpheresWBm2slow (src/HardSpheres.cpp:161-183) has the
+// same Phi1 and Phi2 but 1/(36 pi) where WhiteBear.hs has 1/(24 pi) in Phi3.
+static Functional mark_ii(double radius) {
+  Functional n3 = StepConvolve(radius), n2 = ShellConvolve(radius);
+  Functional vx = xShellConvolve(radius), vy = yShellConvolve(radius),
+             vz = zShellConvolve(radius);
+  const double c1 = 1 / (4 * M_PI * radius), c0 = 1 / (4 * M_PI * radius * radius);
+  Functional lg = log(1 - n3);
+  Functional v2 = sqr(vx) + sqr(vy) + sqr(vz);
+  Functional phi1 = (-c0) * n2 * lg;
+  Functional phi2II = (6 * n3 - 3 * sqr(n3) + 6 * (1 - n3) * lg) / (n3 * sqr(n3));
+  Functional phi2 = (Functional(1.0) + (1 / 9.0) * sqr(n3) * phi2II) * (c1 * (sqr(n2) - v2)) /
+                    (1 - n3);
+  Functional phi3II = (6 * n3 - 9 * sqr(n3) + 6 * n3 * sqr(n3) + 6 * sqr(1 - n3) * lg) /
+                      (4 * n3 * sqr(n3));
+  Functional phi3 = (1 - (4 / 9.0) * n3 * phi3II) * (n2 * (sqr(n2) - 3 * v2)) /
+                    (24 * M_PI * sqr(1 - n3));
+  return (kT() * phi3) + (kT() * phi1) + (kT() * phi2);
+}
+
+// Hard-sphere functional of the composed sums: 0 HardSpheresWBnotensor,
+// 1 HardSpheresRF, 2 mark II (above), 3 HardSpheresWBm2slow as compiled.
+static int g_hs_kind = 0;
+
+static Functional hard_spheres(double R) {
+  switch (g_hs_kind) {
+    case 1: return HardSpheresRF(R);
+    case 2: return mark_ii(R);
+    case 3: return HardSpheresWBm2slow(R);
+    default: return HardSpheresWBnotensor(R);
+  }
+}
+
 static Functional make_sum(const GridDescription &gd, double R, double mu, int terms,
                            const double *V) {
   Functional f(0.0);
-  if (terms & REF_HS) f = HardSpheresWBnotensor(R);
+  if (terms & REF_HS) f = hard_spheres(R);
   if (terms & REF_IDEAL) f = f + IdealGas();
   if (terms & REF_MU) f = f + ChemicalPotential(mu);
   if (terms & REF_VEXT) {
@@ -53,6 +93,10 @@ static Functional make_sum(const GridDescription &gd, double R, double mu, int t
 extern "C" {
 
 long long ref_fft_count(void) { return deft_shim_fft_count(); }
+
+// Selects the hard-sphere functional of every later ref_* call (see
+// hard_spheres above).
+void ref_set_hs(int kind) { g_hs_kind = kind; }
 
 // Energy (Functional::integral, src/Functional.h:131-143), per-term energies
 // in sum order (phi3, phi1, phi2 for the hard spheres, then ideal gas, mu,

@@ -54,10 +54,11 @@ class Grid:
 
 
 class Fmt:
-    def __init__(self, grid, R=1.0, kT=1.0, mu=0.0, terms=7, V=None, mask=None, precision=0):
+    def __init__(self, grid, R=1.0, kT=1.0, mu=0.0, terms=7, V=None, mask=None, precision=0,
+                 functional=0):
         self.L = grid.L
         self.grid = grid
-        p = _lib.FmtParams(R, kT, mu, terms, precision)
+        p = _lib.FmtParams(R, kT, mu, terms, precision, functional)
         h = ctypes.c_void_p()
         check(self.L.deft_fmt_create(grid.h, ctypes.byref(p), ctypes.byref(h)))
         self.h = h

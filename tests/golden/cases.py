@@ -6,9 +6,18 @@ import numpy as np
 from oracle import oracle as O
 
 CASES = ("cubic12", "ortho_odd", "fcc12")
+# (case, hard-sphere functional) pairs of the Rosenfeld and mark II fixtures
+HS_CASES = (("cubic12", O.HS_RF), ("ortho_odd", O.HS_RF), ("cubic12", O.HS_M2),
+            ("ortho_odd", O.HS_M2))
 
 
-def make_case(name):
+def make_case(name, hs=O.HS_WB):
+    P, n = _make_case(name)
+    P.hs = hs
+    return P, n
+
+
+def _make_case(name):
     if name == "cubic12":
         rng = np.random.Generator(np.random.PCG64(101))
         N, lat, R, kT = (12, 12, 12), np.diag([2.4, 2.4, 2.4]), 1.0, 1.0

@@ -18,7 +18,7 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
 from oracle import oracle as O  # noqa: E402
-from tests.golden.cases import CASES, cg_case, make_case, veff_case  # noqa: E402
+from tests.golden.cases import CASES, HS_CASES, cg_case, make_case, veff_case  # noqa: E402
 
 
 def main():
@@ -33,6 +33,13 @@ def main():
         out[name] = {"E": E, "terms": [float(x) for x in t]}
         arrays[f"{name}_grad"] = g
         arrays[f"{name}_weighted"] = w
+    # the Rosenfeld functional (HardSpheresRF) and White Bear mark II (the
+    # WhiteBear.hs definition through the reference's Functional algebra)
+    for name, hs in HS_CASES:
+        P, n = make_case(name, hs)
+        E, g, t = P.ref_energy_grad(n)
+        out[f"{name}_hs{hs}"] = {"E": E, "terms": [float(x) for x in t]}
+        arrays[f"{name}_hs{hs}_grad"] = g
     # known-answer value of tests/new-hard-spheres.cpp:52-63
     P = O.Problem(np.diag([2.0, 2.0, 2.0]), (20, 20, 20), R=1.0, kT=1.0, mu=0.0, terms=O.HS)
     E, _, _ = P.ref_energy_grad(np.full(8000, 0.1), grad=False)

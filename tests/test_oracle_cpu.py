@@ -61,6 +61,70 @@ def test_oracle_matches_reference_golden(oracle_mod, golden, name):
         assert np.abs(w[a] - wr[a]).max() <= 1e-13 * np.abs(wr[a]).max()
 
 
+@pytest.mark.parametrize("name,hs", [("cubic12", 1), ("ortho_odd", 1), ("cubic12", 2),
+                                     ("ortho_odd", 2)])
+def test_oracle_rosenfeld_and_mark2_match_reference_golden(oracle_mod, golden, name, hs):
+    """HardSpheresRF as compiled, and White Bear mark II as WhiteBear.hs
+    defines it, evaluated by the reference's Functional machinery."""
+    from tests.golden.cases import make_case
+    vals, arrs = golden
+    P, n = make_case(name, hs)
+    E, g, t = P.energy_grad(n, terms=True)
+    ref = vals[f"{name}_hs{hs}"]
+    assert abs(E / ref["E"] - 1) < 1e-12
+    tr = np.array(ref["terms"])
+    assert np.abs(t[:len(tr)] - tr).max() <= 1e-12 * np.abs(tr).max()
+    gr = arrs[f"{name}_hs{hs}_grad"]
+    assert np.abs(g - gr).max() <= 1e-12 * np.abs(gr).max()
+
+
+@pytest.mark.parametrize("hs", [0, 1, 2])
+def test_oracle_bulk_equations_of_state(oracle_mod, hs):
+    """Uniform density: White Bear and mark II give the Carnahan-Starling
+    excess free energy eta (4 - 3 eta) / (1 - eta)^2 per particle, Rosenfeld
+    the Percus-Yevick (compressibility) one -ln(1-eta) + 3 eta (2 - eta) / (2 (1-eta)^2)."""
+    O = oracle_mod
+    for eta in (0.05, 0.2, 0.4):
+        nu = eta / (4 * math.pi / 3)
+        P = O.Problem(np.diag([3.2] * 3), (16, 16, 16), terms=O.HS, hs=hs)
+        E = P.energy(np.full(16 ** 3, nu))
+        if hs == O.HS_RF:
+            fex = -math.log(1 - eta) + 3 * eta * (2 - eta) / (2 * (1 - eta) ** 2)
+        else:
+            fex = eta * (4 - 3 * eta) / (1 - eta) ** 2
+        assert abs(E / (3.2 ** 3 * nu * fex) - 1) < 1e-12
+
+
+def test_oracle_mark2_small_packing_series(oracle_mod):
+    """Near n3 = 0 the mark II prefactors switch to their Taylor series: the
+    energy and gradient stay continuous across the switch (|n3| = 0.1)."""
+    O = oracle_mod
+    vals = []
+    for eta in (0.1 - 1e-9, 0.1 + 1e-9):
+        nu = eta / (4 * math.pi / 3)
+        P = O.Problem(np.diag([3.2] * 3), (16, 16, 16), terms=O.HS, hs=O.HS_M2)
+        E, g = P.energy_grad(np.full(16 ** 3, nu))
+        vals.append((E / nu, g.mean() / nu))
+    assert abs(vals[0][0] / vals[1][0] - 1) < 1e-7 and abs(vals[0][1] / vals[1][1] - 1) < 1e-7
+
+
+@pytest.mark.skipif(not os.path.exists(os.path.join(os.path.dirname(HERE), "oracle", "_ref",
+                                                    "libdeft_ref.so")),
+                    reason="reference build only exists where the reference checkout does")
+def test_mark2_vs_compiled_wbm2slow(oracle_mod):
+    """The compiled HardSpheresWBm2slow has the mark II Phi1 and Phi2 but
+    1/(36 pi) where WhiteBear.hs has 1/(24 pi) in Phi3: its Phi3 term is 2/3
+    of the oracle's."""
+    from tests.golden.cases import make_case
+    P, n = make_case("cubic12", 2)
+    P.terms = oracle_mod.HS
+    _, t = P.energy(n, terms=True)
+    P.hs = 3  # the reference bindings' HardSpheresWBm2slow
+    _, _, tr = P.ref_energy_grad(n, grad=False)
+    assert abs(tr[0] / t[0] - 2 / 3) < 1e-12
+    assert abs(tr[1] / t[1] - 1) < 1e-12 and abs(tr[2] / t[2] - 1) < 1e-12
+
+
 def test_oracle_white_bear_known_answer(oracle_mod, golden):
     O = oracle_mod
     vals, _ = golden
@@ -210,3 +274,21 @@ def test_oracle_preconditioned_secant_cg_converges(oracle_mod):
     n1, n2 = np.exp(-x1 / P.kT), np.exp(-x2 / P.kT)
     free = P.mask > 0
     assert np.abs(n1 - n2)[free].max() <= 1e-8 * n1[free].max()
+
+
+def test_oracle_density_preconditioner_same_profile_fewer_evaluations(oracle_mod):
+    """Polak-Ribiere with the diagonal M^-1 = n / (kT dV) (the inverse
+    ideal-gas curvature) reaches the same slit profile as the plain secant CG
+    with fewer evaluations."""
+    O = oracle_mod
+    nb = 0.3 / (4 * math.pi / 3)
+    mu = O.find_mu(1.0, 1.0, nb)
+    z = np.arange(64) * 0.2
+    mask = ((z > 0) & (z < 6.4)).astype(float)
+    P = O.Problem(np.diag([0.2, 0.2, 12.8]), (1, 1, 64), mu=mu, mask=mask)
+    x0 = np.where(mask > 0, nb, 0.0)
+    x1, i1 = P.cg_solve(x0, gtol=1e-12, maxiter=5000, preconditioned=2)
+    x2, i2 = P.cg_solve(x0, gtol=1e-12, maxiter=5000, preconditioned=0)
+    assert i1["gnorm"] < 1e-12 and i2["gnorm"] < 1e-12
+    assert np.abs(x1 - x2).max() <= 1e-9 * x2.max()
+    assert i1["evals"] < i2["evals"]
