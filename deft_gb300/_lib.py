@@ -71,7 +71,8 @@ class BatchProblem(ctypes.Structure):
     _fields_ = [("lat", ctypes.c_double * 9), ("N", ctypes.c_int * 3), ("R", ctypes.c_double),
                 ("kT", ctypes.c_double), ("mu", ctypes.c_double), ("terms", ctypes.c_int),
                 ("precision", ctypes.c_int), ("mask", ctypes.c_void_p), ("V", ctypes.c_void_p),
-                ("n_init", ctypes.c_void_p), ("n_out", ctypes.c_void_p)]
+                ("n_init", ctypes.c_void_p), ("n_out", ctypes.c_void_p),
+                ("functional", ctypes.c_int)]
 
 
 class BatchParams(ctypes.Structure):

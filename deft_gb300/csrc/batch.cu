@@ -56,7 +56,8 @@ int solve_one(Worker &w, const deft_batch_problem &p, const deft_cg_params &cgp,
   int s = DEFT_OK;
   deft_grid *g = w.grid_for(p, &s);
   if (!g) return s;
-  deft_fmt_params fp;
+  deft_fmt_params fp{};
+  fp.functional = p.functional;
   fp.R = p.R;
   fp.kT = p.kT;
   fp.mu = p.mu;

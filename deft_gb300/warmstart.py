@@ -183,7 +183,9 @@ class Dataset:
 def make_dataset(problems, chunk=16, workers=8, gtol=1e-9, device=0, log=None):
     """Solves `problems` (mixed form: FP32 CG stage, then the FP64-gradient
     refinement to |grad F| < gtol) and keeps the converged relative
-    densities on the device.  Problems whose solve fails are skipped."""
+    densities on the device.  Problems whose minimiser stops without
+    converging are skipped; an error of the batch call itself (bad
+    arguments, CUDA) raises, and so does a chunk that keeps no problem."""
     import torch
     dev = f"cuda:{device}"
     ds = Dataset()
@@ -191,6 +193,9 @@ def make_dataset(problems, chunk=16, workers=8, gtol=1e-9, device=0, log=None):
     for c0 in range(0, len(problems), chunk):
         part = problems[c0:c0 + chunk]
         code, st, outs = solve_batch(part, workers=workers, gtol=gtol, device=device)
+        if code not in (_lib.OK, _lib.ERR_LINESEARCH, _lib.ERR_MAXITER, _lib.ERR_NAN):
+            _lib.check(code)
+        kept = len(ds)
         for s, r, n in zip(part, st, outs):
             if r.status or not r.converged:
                 continue
@@ -198,6 +203,8 @@ def make_dataset(problems, chunk=16, workers=8, gtol=1e-9, device=0, log=None):
             ds.target.append(torch.tensor(n / s.nb, dtype=torch.float32, device=dev))
             ds.eta.append(float(s.eta))
             ds.stats.append((r.iter, r.evals, r.gnorm))
+        if len(ds) == kept:
+            raise RuntimeError(f"no problem of {len(part)} converged (batch status {code})")
         if log:
             log(f"solved {min(c0 + chunk, len(problems))}/{len(problems)} "
                 f"({time.perf_counter() - t0:.1f} s, kept {len(ds)})")

@@ -282,6 +282,7 @@ typedef struct {
   const double *V;      /* or NULL */
   const double *n_init; /* initial density */
   double *n_out;        /* converged density (may alias n_init) */
+  int functional;       /* DEFT_HS_* (0 when left zeroed) */
 } deft_batch_problem;
 
 typedef struct {
