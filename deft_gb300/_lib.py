@@ -16,6 +16,7 @@ NTERMS = 6
 LS_SECANT, LS_QUADRATIC_REF = 0, 1
 PC_NONE, PC_FUNCTIONAL, PC_DENSITY = 0, 1, 2
 HS_WB_NOTENSOR, HS_RF, HS_WB_MARK2 = 0, 1, 2
+CONTACT_GSIGMA_S, CONTACT_GSIGMA_A, CONTACT_GROSS, CONTACT_YUWU, CONTACT_YUWU_S = 0, 1, 2, 3, 4
 
 # Every symbol include/deft_gb300.h declares.
 EXPORTS = (
@@ -28,7 +29,7 @@ EXPORTS = (
     "deft_tuning_clear",
     "deft_fmt_create", "deft_fmt_destroy", "deft_fmt_set_params", "deft_fmt_set_vext",
     "deft_fmt_set_mask", "deft_fmt_energy", "deft_fmt_energy_grad", "deft_fmt_energy_grad_pgrad",
-    "deft_fmt_weighted",
+    "deft_fmt_weighted", "deft_fmt_contact",
     "deft_fmt_hessian_vector",
     "deft_find_chemical_potential",
     "deft_fmt_energy_grad_noalloc", "deft_noalloc_scratch_bytes",
@@ -125,6 +126,7 @@ def load():
         "deft_fmt_energy_grad": (ctypes.c_int, [_vp, _dp, ctypes.c_int, _dp, _dp, _dp]),
         "deft_fmt_energy_grad_pgrad": (ctypes.c_int, [_vp, _dp, ctypes.c_int, _dp, _dp, _dp, _dp]),
         "deft_fmt_weighted": (ctypes.c_int, [_vp, _dp, ctypes.c_int, _dp]),
+        "deft_fmt_contact": (ctypes.c_int, [_vp, _dp, ctypes.c_int, ctypes.c_int, _dp]),
         "deft_fmt_hessian_vector": (ctypes.c_int, [_vp, _dp, _dp, ctypes.c_int, _dp]),
         "deft_find_chemical_potential": (ctypes.c_int, [ctypes.c_double, ctypes.c_double,
                                                         ctypes.c_double, _dp]),

@@ -19,6 +19,12 @@ Names, argument meaning and return conventions follow the reference:
   ``Precision(eps, m)``, ``MaxIter(n, m)``, ``m.improve_energy()``,
   ``m.energy()``, ``m.grad()``  src/LineMinimizer.h:18-19, src/Minimizer.h:13-60
 * ``find_chemical_potential(f, kT, n)``          src/equation-of-state.cpp:189-192
+* ``HardSpheresRF(R)`` src/HardSpheres.cpp:69-88; ``WhiteBearMarkII(R)``
+  src/haskell/WhiteBear.hs:140-159
+* ``gSigmaS(R)``, ``gSigmaA(R)``, ``gSigmaSm2(R)``, ``gSigmaAm2(R)``,
+  ``CorrelationGrossCorrect(R)``, ``YuWuCorrelation(R)``,
+  ``YuWuCorrelation_S(R)``, each called as ``f(kT, gd, density)``
+  (src/ContactDensity.h, papers/contact/figs/walls.cpp:118-129)
 
 Everything is evaluated by the sm_103a kernels; there is no CPU path.  The
 functional composition is recognised (White Bear + ideal gas + mu + V_ext,
@@ -200,8 +206,10 @@ class Grid(np.ndarray):
 class Functional:
     """A sum of the recognised terms, optionally wrapped in constrain(mask, .)."""
 
-    def __init__(self, R=None, ideal=False, mu=None, V=None, mask=None, names=(), veff=False):
+    def __init__(self, R=None, ideal=False, mu=None, V=None, mask=None, names=(), veff=False,
+                 hs=_lib.HS_WB_NOTENSOR):
         self.R = R
+        self.hs = hs  # hard-sphere kind (White Bear, Rosenfeld, mark II)
         self.ideal = ideal
         self.mu = mu
         self.V = V
@@ -223,7 +231,8 @@ class Functional:
         return Functional(R=pick(self.R, o.R, "hard-sphere"), ideal=self.ideal or o.ideal,
                           mu=pick(self.mu, o.mu, "chemical-potential"),
                           V=pick(self.V, o.V, "external-potential"),
-                          names=self.names + o.names)
+                          names=self.names + o.names,
+                          hs=self.hs if self.R is not None else o.hs)
 
     def terms(self):
         t = 0
@@ -246,7 +255,7 @@ class Functional:
         key = id(gd)
         L = _lib.load()
         p = _lib.FmtParams(self.R if self.R is not None else 1.0, kT,
-                           self.mu if self.mu is not None else 0.0, self.terms())
+                           self.mu if self.mu is not None else 0.0, self.terms(), 0, self.hs)
         if key not in self._fmt:
             h = ctypes.c_void_p()
             check(L.deft_fmt_create(gd.handle, ctypes.byref(p), ctypes.byref(h)))
@@ -324,6 +333,67 @@ class Functional:
 
 def HardSpheresWBnotensor(R):
     return Functional(R=float(R), names=("phi3", "phi1", "phi2"))
+
+
+def HardSpheresRF(R):
+    """Rosenfeld's functional (src/HardSpheres.cpp:69-88)."""
+    return Functional(R=float(R), names=("phi3", "phi1", "phi2"), hs=_lib.HS_RF)
+
+
+def WhiteBearMarkII(R):
+    """White Bear mark II (src/haskell/WhiteBear.hs:140-159)."""
+    return Functional(R=float(R), names=("phi3", "phi1", "phi2"), hs=_lib.HS_WB_MARK2)
+
+
+class _ContactField:
+    """A transformation of the density into a contact field, called as the
+    reference's Functional transformations are: f(kT, gd, density) -> Grid
+    (papers/contact/figs/walls.cpp:120-129)."""
+
+    def __init__(self, R, which, hs):
+        self.f = Functional(R=float(R), hs=hs)
+        self.which = which
+
+    def __call__(self, kT, gd, x):
+        h = self.f.fmt(gd, kT)
+        xs = _host_f64(x, gd.NxNyNz)
+        out = Grid(gd)
+        check(_lib.load().deft_fmt_contact(h, xs.ctypes.data, 0, self.which, out.ctypes.data))
+        return out
+
+    def close(self):
+        self.f.close()
+
+
+def gSigmaS(R):
+    return _ContactField(R, _lib.CONTACT_GSIGMA_S, _lib.HS_WB_NOTENSOR)
+
+
+def gSigmaA(R):
+    return _ContactField(R, _lib.CONTACT_GSIGMA_A, _lib.HS_WB_NOTENSOR)
+
+
+def gSigmaSm2(R):
+    return _ContactField(R, _lib.CONTACT_GSIGMA_S, _lib.HS_WB_MARK2)
+
+
+def gSigmaAm2(R):
+    return _ContactField(R, _lib.CONTACT_GSIGMA_A, _lib.HS_WB_MARK2)
+
+
+def GrossCorrelation(R):
+    return _ContactField(R, _lib.CONTACT_GROSS, _lib.HS_WB_NOTENSOR)
+
+
+CorrelationGrossCorrect = GrossCorrelation
+
+
+def YuWuCorrelation(R):
+    return _ContactField(R, _lib.CONTACT_YUWU, _lib.HS_WB_NOTENSOR)
+
+
+def YuWuCorrelation_S(R):
+    return _ContactField(R, _lib.CONTACT_YUWU_S, _lib.HS_WB_NOTENSOR)
 
 
 def IdealGas():

@@ -4,6 +4,7 @@
 // the host; every vector operation and reduction runs on the GPU, and only
 // scalars (energies and dot products) come back.
 #include "../../include/deft_gb300.h"
+#include "contact.h"
 #include "fmt_engine.h"
 
 #include <cmath>
@@ -590,6 +591,33 @@ int deft_fmt_weighted(deft_fmt *f, const double *n, int on_device, double *out5)
     if (e != cudaSuccess) return cuda_err(e, "device-to-host copy");
   }
   return sync(g->ctx);
+}
+
+int deft_fmt_contact(deft_fmt *f, const double *n, int on_device, int which, double *out) {
+  if (!f || !n || !out) return set_err(DEFT_ERR_ARG, "NULL argument");
+  if (which < DEFT_CONTACT_GSIGMA_S || which > DEFT_CONTACT_YUWU_S)
+    return set_err(DEFT_ERR_ARG, "unknown contact field");
+  deft_grid *g = f->grid;
+  cudaSetDevice(g->ctx->device);
+  const double *src;
+  if (int s = stage_in(g, n, on_device, g->in_buf, &src)) return s;
+  const deft::FmtSpec spec = spec_of(f);
+  const double *dens;
+  if (int s = fmt_density(f, spec, src, &dens)) return s;
+  const size_t ns = deft::contact_scratch_doubles(g->eng->geom(), which);
+  double *scratch = nullptr;
+  cudaError_t ce = cudaMalloc((void **)&scratch, sizeof(double) * (ns + (on_device ? 0 : nr(g))));
+  if (ce != cudaSuccess) return cuda_err(ce, "cudaMalloc");
+  double *dst = on_device ? out : scratch + ns;
+  std::string err;
+  const int r = deft::contact_values(g->eng, spec, which, dens, scratch, dst, &err);
+  if (!r && !on_device)
+    ce = cudaMemcpyAsync(out, dst, sizeof(double) * nr(g), cudaMemcpyDeviceToHost, g->ctx->stream);
+  const int sr = sync(g->ctx);
+  cudaFree(scratch);
+  if (r) return set_err(DEFT_ERR_CUDA, err);
+  if (ce != cudaSuccess) return cuda_err(ce, "device-to-host copy");
+  return sr;
 }
 
 int deft_fmt_hessian_vector(deft_fmt *f, const double *n, const double *dx, int on_device,

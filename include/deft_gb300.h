@@ -265,6 +265,20 @@ int deft_cg_solve(deft_cg *cg, deft_cg_status *st);
 int deft_cg_checkpoint(deft_cg *cg, const char *path);
 int deft_cg_restore(deft_cg *cg, const char *path);
 
+/* ---- contact values (src/ContactDensity.cpp, src/haskell/WhiteBear.hs:68-137) ----
+ * The step after the solve in the reference's papers
+ * (papers/contact/figs/walls.cpp:118-132): fields of the pair distribution
+ * at contact and its estimates, from a density n, for the functional's
+ * radius and hard-sphere kind (White Bear or mark II; Rosenfeld through the
+ * same formulas).  Host or device n and out (NR reals). */
+#define DEFT_CONTACT_GSIGMA_S 0 /* gSigmaS (gSigmaSm2 for mark II), WhiteBear.hs:79-96 */
+#define DEFT_CONTACT_GSIGMA_A 1 /* gSigmaA (gSigmaAm2), src/ContactDensity.cpp:208-276 */
+#define DEFT_CONTACT_GROSS 2    /* GrossCorrelation / CorrelationGrossCorrect,
+                                   src/ContactDensity.cpp:360-370 */
+#define DEFT_CONTACT_YUWU 3     /* YuWuCorrelation, src/ContactDensity.cpp:382-413 */
+#define DEFT_CONTACT_YUWU_S 4   /* YuWuCorrelation_S, src/ContactDensity.cpp:372-380 */
+int deft_fmt_contact(deft_fmt *f, const double *n, int on_device, int which, double *out);
+
 /* ---- batched solves ----
  * Many independent state points and uneven grids on one GPU (no reference
  * counterpart: the reference solves one problem per process).  Each problem

@@ -435,6 +435,166 @@ double oracle_energy_grad_pgrad(const oracle_params *p, const double *x, const d
   return eval_x(p, x, V, mask, grad, pgrad, terms6);
 }
 
+/* ---- contact values (src/ContactDensity.cpp, src/haskell/WhiteBear.hs:68-137) ---- */
+
+/* f2, f3 of the kind and their first derivatives at e = n3 (see phi_hs). */
+static void hs_f(int kind, double e, double f2[2], double f3[2]) {
+  const double u = 1 / (1 - e);
+  if (kind == ORACLE_HS_WB) {
+    double S, dS;
+    phi3_S(e, &S, &dS);
+    f2[0] = u;
+    f2[1] = u * u;
+    f3[0] = S * u * u / (36 * M_PI);
+    f3[1] = (dS + 2 * S * u) * u * u / (36 * M_PI);
+    return;
+  }
+  double P2 = 1, dP2 = 0, P3 = 1, dP3 = 0;
+  if (kind == ORACLE_HS_M2) m2_P(e, &P2, &dP2, &P3, &dP3);
+  f2[0] = P2 * u;
+  f2[1] = dP2 * u + P2 * u * u;
+  f3[0] = P3 * u * u / (24 * M_PI);
+  f3[1] = (dP3 + 2 * P3 * u) * u * u / (24 * M_PI);
+}
+
+/* Partial derivatives of phi in the six-variable form of WhiteBear.hs
+ * (n0 = n2/(4 pi R^2), n1 = n2/(4 pi R), n1v = n2v/(4 pi R)): d[0..3] by
+ * n0..n3, d[4] and d[5] the coefficients of n2v in dphi/dn1v and dphi/dn2v
+ * (src/ContactDensity.cpp:90-206 for the White Bear and mark II cases). */
+static void contact_partials(int kind, double R, double n3, double n2, double v2, double d[6]) {
+  double f2[2], f3[2];
+  hs_f(kind, n3, f2, f3);
+  const double c1 = 1 / (4 * M_PI * R), c0 = c1 / R;
+  const double q = n2 * n2 - v2, t3 = n2 * (n2 * n2 - 3 * v2);
+  d[0] = -log(1 - n3);
+  d[1] = n2 * f2[0];
+  d[2] = c1 * n2 * f2[0] + 3 * q * f3[0];
+  d[3] = c0 * n2 / (1 - n3) + c1 * q * f2[1] + t3 * f3[1];
+  d[4] = -f2[0];
+  d[5] = -c1 * f2[0] - 6 * n2 * f3[0];
+}
+
+/* Weight a at k: 0 shell(R), 1 -shellPrime(R), 2-4 x/y/zshell(R),
+ * 5-7 x/y/zshellprime(R), 8 shell(2R), 9 step(2R)
+ * (src/ReciprocalOperators.h:94-291); W = wr + i wi. */
+static void contact_weight(int a, const double k[3], double R, double dr, double *wr,
+                           double *wi) {
+  const double k2 = k[0] * k[0] + k[1] * k[1] + k[2] * k[2], kk = sqrt(k2);
+  const double smear = exp(-kSpreading * k2 * dr * dr);
+  const double Ra = a >= 8 ? 2 * R : R, kR = kk * Ra;
+  *wr = 0;
+  *wi = 0;
+  if (a == 0 || a == 8) {
+    const double x = kR * kR;
+    *wr = kR > 1e-3 ? smear * (4 * M_PI) * Ra * sin(kR) / kk
+                    : (4 * M_PI) * Ra * Ra *
+                          (-x * x * x * (1.0 / 120 / 6 / 7) + x * x * (1.0 / 120) - x / 6 + 1);
+  } else if (a == 1) {
+    *wr = kR > 1e-5 ? -smear * (4 * M_PI) * (-sin(kR) / kk - Ra * cos(kR)) : 8 * M_PI * Ra;
+  } else if (a < 5) {
+    const double x = kR * kR, kc = k[a - 2];
+    *wi = kR > 1e-3 ? smear * (4 * M_PI) * kc / k2 * (Ra * cos(kR) - sin(kR) / kk)
+                    : (4 * M_PI) * Ra * Ra * Ra * kc *
+                          (x * x * (1.0 / 5040 - 1.0 / 720) + x * (1.0 / 24 - 1.0 / 120) - 1.0 / 3);
+  } else if (a < 8) {
+    const double kc = k[a - 5], thr = a == 5 ? 1e-5 : 1e-3;
+    *wi = kR > thr ? smear * (4 * M_PI) * Ra * kc / kk * sin(kR) : (4 * M_PI) * Ra * Ra * kc;
+  } else {
+    const double x = kR * kR;
+    *wr = kR > 1e-3 ? smear * (4 * M_PI) * (sin(kR) - kR * cos(kR)) / (k2 * kk)
+                    : (4 * M_PI / 3) * Ra * Ra * Ra *
+                          (x * x * x * (-1.0 / 15120) + x * x * (1.0 / 280) - x / 10 + 1);
+  }
+}
+
+/* acc (+)= W_a * fft(src) with the convolution's dV/V scale. */
+static void contact_accum(const oracle_params *p, const kspace *ks, int a, const double *src,
+                          double *fk, double *acc, int first) {
+  r2c(p, src, fk);
+  for (size_t i = 0; i < ks->nc; i++) {
+    double wr, wi;
+    contact_weight(a, ks->kv + 3 * i, p->R, ks->dr, &wr, &wi);
+    const double re = fk[2 * i] * ks->scale, im = fk[2 * i + 1] * ks->scale;
+    const double tr = wr * re - wi * im, ti = wr * im + wi * re;
+    if (first) {
+      acc[2 * i] = tr;
+      acc[2 * i + 1] = ti;
+    } else {
+      acc[2 * i] += tr;
+      acc[2 * i + 1] += ti;
+    }
+  }
+}
+
+void oracle_contact(const oracle_params *p, const double *n, int which, double *out) {
+  kspace ks;
+  kspace_init(p, &ks);
+  const size_t nr = ks.nr;
+  const double R = p->R, c1 = 1 / (4 * M_PI * R), c0 = c1 / R;
+  double *fk = (double *)malloc(sizeof(double) * 2 * ks.nc);
+  double *acc = (double *)malloc(sizeof(double) * 2 * ks.nc);
+  if (which == ORACLE_CONTACT_GROSS) {
+    /* src/ContactDensity.cpp:360-370 */
+    contact_accum(p, &ks, 9, n, fk, acc, 1);
+    c2r(p, acc, out);
+    for (size_t i = 0; i < nr; i++) {
+      const double eta = out[i] / 8, d = 1 - eta;
+      out[i] = (1 - 0.5 * eta) / (d * d * d);
+    }
+  } else {
+    double *w = (double *)malloc(sizeof(double) * 5 * nr);
+    weighted(p, &ks, n, w);
+    if (which == ORACLE_CONTACT_GSIGMA_A) {
+      /* src/ContactDensity.cpp:208-233,271-276 */
+      double *src = (double *)malloc(sizeof(double) * nr);
+      double *num = (double *)malloc(sizeof(double) * nr);
+      for (int a = 0; a < 8; a++) {
+        for (size_t i = 0; i < nr; i++) {
+          const double v[3] = {w[2 * nr + i], w[3 * nr + i], w[4 * nr + i]};
+          double d[6];
+          contact_partials(p->hs, R, w[i], w[nr + i], v[0] * v[0] + v[1] * v[1] + v[2] * v[2], d);
+          if (a == 0) src[i] = d[3] - 2 * c0 / R * d[0] - c0 * d[1];
+          else if (a == 1) src[i] = d[2] + c1 * d[1] + c0 * d[0];
+          else if (a < 5) src[i] = v[a - 2] * c0 * d[4];
+          else src[i] = v[a - 5] * (c1 * d[4] + d[5]);
+        }
+        contact_accum(p, &ks, a, src, fk, acc, a == 0);
+      }
+      c2r(p, acc, num);
+      contact_accum(p, &ks, 8, n, fk, acc, 1);
+      c2r(p, acc, out);
+      for (size_t i = 0; i < nr; i++) out[i] = num[i] / out[i];
+      free(src);
+      free(num);
+    } else {
+      for (size_t i = 0; i < nr; i++) {
+        const double n3 = w[i], n2 = w[nr + i];
+        const double v2 = w[2 * nr + i] * w[2 * nr + i] + w[3 * nr + i] * w[3 * nr + i] +
+                          w[4 * nr + i] * w[4 * nr + i];
+        if (which == ORACLE_CONTACT_GSIGMA_S) {
+          /* WhiteBear.hs:86-96 */
+          double d[6];
+          contact_partials(p->hs, R, n3, n2, v2, d);
+          const double n0 = c0 * n2, n2p = -2 * n2 / R;
+          const double dAdR = d[3] * n2 - d[2] * n2p - d[1] * (c1 * n2p + n0) -
+                              d[0] * (c0 * n2p + 2 * n0 / R) -
+                              (d[5] * (-2 / R) * v2 + c1 * d[4] * (-3 / R) * v2);
+          out[i] = dAdR / (n0 * n0 * 4 * M_PI * (2 * R) * (2 * R));
+        } else {
+          /* src/ContactDensity.cpp:372-413 */
+          const double zeta2 = R / 3 * n2, invdiff = 1 / (1 - n3), zeta = 1 - v2 / (n2 * n2);
+          const double ghs = invdiff * (1 + 0.5 * (invdiff * zeta2) * zeta * (3 + invdiff * zeta2));
+          out[i] = which == ORACLE_CONTACT_YUWU_S ? ghs * zeta * zeta : ghs;
+        }
+      }
+    }
+    free(w);
+  }
+  free(fk);
+  free(acc);
+  kspace_free(&ks);
+}
+
 double oracle_homogeneous(double R, double kT, double mu, double nb) {
   const double n3 = nb * (4 * M_PI / 3) * R * R * R, n2 = nb * 4 * M_PI * R * R;
   double phi[3], d[5];

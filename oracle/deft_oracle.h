@@ -95,6 +95,18 @@ int oracle_cg_solve_pc(const oracle_params *p, const double *V, const double *ma
                        double *n_inout, double gtol, int maxiter, double step, int precond,
                        double *out3);
 
+/* Contact values and pair-correlation estimates at the density n
+ * (src/ContactDensity.cpp, src/haskell/WhiteBear.hs:68-137), for p->R and
+ * the hard-sphere kind p->hs. */
+enum {
+  ORACLE_CONTACT_GSIGMA_S = 0,
+  ORACLE_CONTACT_GSIGMA_A = 1,
+  ORACLE_CONTACT_GROSS = 2,
+  ORACLE_CONTACT_YUWU = 3,
+  ORACLE_CONTACT_YUWU_S = 4,
+};
+void oracle_contact(const oracle_params *p, const double *n, int which, double *out);
+
 /* Number of 3-D real FFTs executed by this oracle so far. */
 long long oracle_fft_count(void);
 

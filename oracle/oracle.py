@@ -22,6 +22,8 @@ REF_SO = os.path.join(HERE, "_ref", "libdeft_ref.so")
 
 HS, IDEAL, MU, VEXT, MASK, VEFF = 1, 2, 4, 8, 16, 32
 HS_WB, HS_RF, HS_M2 = 0, 1, 2  # hard-sphere functional kinds (oracle_params.hs)
+# contact fields (oracle_contact)
+CONTACT_GSIGMA_S, CONTACT_GSIGMA_A, CONTACT_GROSS, CONTACT_YUWU, CONTACT_YUWU_S = 0, 1, 2, 3, 4
 NTERMS = 6
 TERM_NAMES = ("phi3", "phi1", "phi2", "ideal_gas", "chemical_potential", "external_potential")
 
@@ -88,6 +90,7 @@ def lib():
         L.oracle_pcg_quadratic.restype = ctypes.c_int
         L.oracle_pcg_quadratic.argtypes = [P, _dp, _dp, _dp, ctypes.c_int, ctypes.c_double, _dp]
         L.oracle_fft_count.restype = ctypes.c_longlong
+        L.oracle_contact.argtypes = [P, _dp, ctypes.c_int, _dp]
         L.offt_r2c_3d.argtypes = [ctypes.c_int] * 3 + [_dp, _dp]
         L.offt_c2r_3d.argtypes = [ctypes.c_int] * 3 + [_dp, _dp]
         _lib = L
@@ -129,6 +132,8 @@ def ref():
                               _dp, _dp, ctypes.c_int, ctypes.c_double, _dp]
         L.ref_fft_count.restype = ctypes.c_longlong
         L.ref_set_hs.argtypes = [ctypes.c_int]
+        L.ref_contact.argtypes = [_dp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                  ctypes.c_int, _dp, _dp]
         _ref = L
     return _ref
 
@@ -218,6 +223,13 @@ class Problem:
                                       _ptr(out))
         return x, {"iters": it, "energy": out[0], "gnorm": out[1], "evals": int(out[2])}
 
+    def contact(self, n, which):
+        """Contact field `which` (CONTACT_*) at the density n."""
+        n = np.ascontiguousarray(n, dtype=np.float64).reshape(-1)
+        out = np.empty(self.size)
+        lib().oracle_contact(ctypes.byref(self.params()), _ptr(n), int(which), _ptr(out))
+        return out
+
     # -- unmodified reference ---------------------------------------------
     def _ref(self):
         """The reference build, set to this problem's hard-sphere functional."""
@@ -233,6 +245,12 @@ class Problem:
         nt = self._ref().ref_eval(_ptr(self.lat), *self.N, self.R, self.kT, self.mu, self.terms,
                             _ptr(n), _ptr(self.V), _ptr(self.mask), ctypes.byref(E), _ptr(t), _ptr(g))
         return E.value, g, t[:nt]
+
+    def ref_contact(self, n, which):
+        n = np.ascontiguousarray(n, dtype=np.float64).reshape(-1)
+        out = np.empty(self.size)
+        self._ref().ref_contact(_ptr(self.lat), *self.N, self.R, int(which), _ptr(n), _ptr(out))
+        return out
 
     def ref_weighted(self, n):
         n = np.ascontiguousarray(n, dtype=np.float64).reshape(-1)

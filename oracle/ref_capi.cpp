@@ -13,6 +13,7 @@
 // src/IdealGas.cpp:68-72, ChemicalPotential at src/ChemicalPotential.cpp:19-22,
 // ExternalPotential at src/ExternalPotential.cpp:19-21, constrain at
 // src/Functional.cpp:834-838.
+#include "ContactDensity.h"
 #include "Functionals.h"
 #include "Grid.h"
 #include "LineMinimizer.h"
@@ -97,6 +98,55 @@ long long ref_fft_count(void) { return deft_shim_fft_count(); }
 // Selects the hard-sphere functional of every later ref_* call (see
 // hard_spheres above).
 void ref_set_hs(int kind) { g_hs_kind = kind; }
+
+}  // extern "C"
+
+// Defined in src/ContactDensity.cpp, declarations commented out in its header.
+Functional gSigmaAcpp(double radius);
+Functional gSigmaAm2cpp(double radius);
+
+// gSigmaS as src/haskell/WhiteBear.hs:79-96 defines it (the generated gSigmaS
+// and gSigmaSm2 need ghc), composed from the reference's partial derivatives
+// of phi (src/ContactDensity.cpp:90-206) and weighted densities:
+//   dA/dR = d3 n2 - d2 n2' - d1 (n2'/(4 pi R) + n0) - d0 (n2'/(4 pi R^2) + 2 n0/R)
+//           - (dphi/dn2v . n2v' + dphi/dn1v . (n2v' - n2v/R) / (4 pi R)),
+//   n2' = -2 n2 / R, n2v' = -2 n2v / R,   gSigmaS = dA/dR / (n0^2 4 pi (2R)^2).
+// (The compiled dAdR_S of src/ContactDensity.cpp:235-269 multiplies each
+// n2v component by -2 n2 / R instead of -2 n2v_c / R.)
+static Functional gsigma_s_hs(double R, bool m2) {
+  Functional n2 = ShellConvolve(R);
+  Functional vx = xShellConvolve(R), vy = yShellConvolve(R), vz = zShellConvolve(R);
+  Functional v2 = sqr(vx) + sqr(vy) + sqr(vz);
+  Functional d0 = m2 ? dWBm2_dn0(R) : dWB_dn0(R), d1 = m2 ? dWBm2_dn1(R) : dWB_dn1(R);
+  Functional d2 = m2 ? dWBm2_dn2(R) : dWB_dn2(R), d3 = m2 ? dWBm2_dn3(R) : dWB_dn3(R);
+  Functional d1v = m2 ? dWBm2_dn1v_over_n2v(R) : dWB_dn1v_over_n2v(R);
+  Functional d2v = m2 ? dWBm2_dn2v_over_n2v(R) : dWB_dn2v_over_n2v(R);
+  const double c1 = 1 / (4 * M_PI * R), c0 = c1 / R;
+  Functional n0 = c0 * n2, n2p = (-2 / R) * n2;
+  Functional dAdR = d3 * n2 - d2 * n2p - d1 * (c1 * n2p + n0) - d0 * (c0 * n2p + (2 / R) * n0) -
+                    ((-2 / R) * d2v * v2 + (-3 * c1 / R) * d1v * v2);
+  return (1 / (16 * M_PI * R * R)) * dAdR / sqr(n0);
+}
+
+extern "C" {
+
+// Contact fields at the density n for the kind set by ref_set_hs (0 White
+// Bear, 2 mark II): 0 gSigmaS (above), 1 gSigmaAcpp / gSigmaAm2cpp,
+// 2 GrossCorrelation, 3 YuWuCorrelation, 4 YuWuCorrelation_S.
+void ref_contact(const double *lat, int Nx, int Ny, int Nz, double R, int which,
+                 const double *n, double *out) {
+  GridDescription gd(make_lat(lat), Nx, Ny, Nz);
+  Grid x(gd);
+  for (int i = 0; i < gd.NxNyNz; i++) x[i] = n[i];
+  const bool m2 = g_hs_kind == 2;
+  Functional f = which == 0   ? gsigma_s_hs(R, m2)
+                 : which == 1 ? (m2 ? gSigmaAm2cpp(R) : gSigmaAcpp(R))
+                 : which == 2 ? GrossCorrelation(R)
+                 : which == 3 ? YuWuCorrelation(R)
+                              : YuWuCorrelation_S(R);
+  VectorXd v = f(gd, 1.0, x);
+  for (int i = 0; i < gd.NxNyNz; i++) out[i] = v[i];
+}
 
 // Energy (Functional::integral, src/Functional.h:131-143), per-term energies
 // in sum order (phi3, phi1, phi2 for the hard spheres, then ideal gas, mu,

@@ -40,6 +40,15 @@ def main():
         E, g, t = P.ref_energy_grad(n)
         out[f"{name}_hs{hs}"] = {"E": E, "terms": [float(x) for x in t]}
         arrays[f"{name}_hs{hs}_grad"] = g
+    # contact values (src/ContactDensity.cpp; gSigmaS as WhiteBear.hs defines
+    # it) on the slit of the CG case, converged by the oracle's secant CG
+    P, n, _, _ = cg_case()
+    x, _ = P.cg_solve(n, gtol=1e-9, maxiter=3000)
+    arrays["contact_slit_x"] = x
+    for hs in (O.HS_WB, O.HS_M2):
+        P.hs = hs
+        for which in range(5):
+            arrays[f"contact_slit_hs{hs}_{which}"] = P.ref_contact(x, which)
     # known-answer value of tests/new-hard-spheres.cpp:52-63
     P = O.Problem(np.diag([2.0, 2.0, 2.0]), (20, 20, 20), R=1.0, kT=1.0, mu=0.0, terms=O.HS)
     E, _, _ = P.ref_energy_grad(np.full(8000, 0.1), grad=False)

@@ -292,3 +292,20 @@ def test_oracle_density_preconditioner_same_profile_fewer_evaluations(oracle_mod
     assert i1["gnorm"] < 1e-12 and i2["gnorm"] < 1e-12
     assert np.abs(x1 - x2).max() <= 1e-9 * x2.max()
     assert i1["evals"] < i2["evals"]
+
+
+@pytest.mark.parametrize("hs", [0, 2])
+@pytest.mark.parametrize("which", [0, 1, 2, 3, 4])
+def test_oracle_contact_values_match_reference_golden(oracle_mod, golden, hs, which):
+    """gSigmaS (WhiteBear.hs, through the reference's partial derivatives),
+    gSigmaA (gSigmaAcpp / gSigmaAm2cpp), GrossCorrelation, YuWuCorrelation
+    and YuWuCorrelation_S on a converged slit profile."""
+    from tests.golden.cases import cg_case
+    _, arrs = golden
+    P, _, _, _ = cg_case()
+    P.hs = hs
+    x = arrs["contact_slit_x"]
+    got = P.contact(x, which)
+    ref = arrs[f"contact_slit_hs{hs}_{which}"]
+    assert np.all(np.isfinite(ref))
+    assert np.abs(got - ref).max() <= 1e-12 * np.abs(ref).max()
