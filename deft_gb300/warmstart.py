@@ -298,14 +298,17 @@ class Solver:
         self.L.deft_ctx_destroy(self.ctx)
 
 
-def compare_starts(net, problems, device=0, fp64=True, floor_rel=1e-3, switch=(None,)):
+def compare_starts(net, problems, device=0, fp64=True, floor_rel=1e-3, switch=(None,),
+                   preconditioned=_lib.PC_DENSITY):
     """Solves each problem to |grad F| < 1e-9 from the bulk start and from
     the checked warm start, in the mixed form (and in FP64 if asked); the
     warm-start time includes the network's forward pass and the energy
     checks.  `switch` lists the mixed warm-start variants: None leaves the
     FP32 stage at 1e-4 of the start's gradient norm (the default rule), a
-    number c at c times the bulk start's gradient norm.  Returns one record
-    per problem."""
+    number c at c times the bulk start's gradient norm.  Mixed solves use
+    the `preconditioned` setting (the density preconditioner by default);
+    FP64 solves are the plain reference CG.  Returns one record per
+    problem."""
     import torch
     dev = f"cuda:{device}"
     sv = Solver(problems[0].shape, problems[0].lat, device=device)
@@ -332,7 +335,8 @@ def compare_starts(net, problems, device=0, fp64=True, floor_rel=1e-3, switch=(N
             runs.append((_lib.PRECISION_MIXED, "mixed"))
             ref_x = None
             for prec, name in runs:
-                st, t = sv.solve(prec, bulk.data_ptr())
+                pc = preconditioned if prec == _lib.PRECISION_MIXED else _lib.PC_NONE
+                st, t = sv.solve(prec, bulk.data_ptr(), preconditioned=pc)
                 r[f"{name}_bulk"] = rec(st, t)
                 if ref_x is None:
                     ref_x = torch.empty_like(mask)
@@ -344,7 +348,8 @@ def compare_starts(net, problems, device=0, fp64=True, floor_rel=1e-3, switch=(N
                                                       n_ws.data_ptr(), floor_rel=floor_rel,
                                                       bulk_gnorm=True)
                     t_ws = time.perf_counter() - t0
-                    st, t = sv.solve(prec, n_ws.data_ptr(), refine_abs=c * gb if c else 0.0)
+                    st, t = sv.solve(prec, n_ws.data_ptr(), refine_abs=c * gb if c else 0.0,
+                                     preconditioned=pc)
                     check(sv.L.deft_cg_get_x(sv.cg[prec], x.data_ptr(), 1))
                     dmax = float((x - ref_x).abs().max() / ref_x.abs().max())
                     key = f"{name}_warm" if c is None else f"{name}_warm_abs{c:g}"
@@ -367,6 +372,8 @@ def summarize(recs):
         out[key] = {"mean_s": float(np.mean(col("s"))), "median_s": float(np.median(col("s"))),
                     "mean_iter": float(np.mean(col("iter"))),
                     "mean_evals": float(np.mean(col("evals"))),
+                    "mean_evals_fp64": float(np.mean(col("evals_fp64"))),
+                    "mean_hvps": float(np.mean(col("hvps"))),
                     "converged": int(sum(r[key]["converged"] for r in recs)),
                     "failures": [(i, r[key]["status"]) for i, r in enumerate(recs)
                                  if not r[key]["converged"]]}
@@ -413,6 +420,8 @@ def main(argv=None):
                     help="comma-separated c values: mixed warm-start variants leaving the "
                          "FP32 stage at c x the bulk start's gradient norm")
     ap.add_argument("--json", default=None, help="summary file to write")
+    ap.add_argument("--no-precond", action="store_true",
+                    help="mixed solves without the density preconditioner")
     ap.add_argument("--device", type=int, default=0)
     a = ap.parse_args(argv)
     import sys
@@ -449,10 +458,13 @@ def main(argv=None):
     switch = (None,) + tuple(float(c) for c in a.switch.split(",") if c)
     held = walls_solutes_set(a.held, a.held_seed, N=net.N)
     nf = a.held if a.fp64_held is None else a.fp64_held
-    recs = compare_starts(net, held[:nf], device=a.device, fp64=True, switch=switch)
+    pc = _lib.PC_NONE if a.no_precond else _lib.PC_DENSITY
+    recs = compare_starts(net, held[:nf], device=a.device, fp64=True, switch=switch,
+                          preconditioned=pc) if nf else []
     if nf < len(held):
-        recs += compare_starts(net, held[nf:], device=a.device, fp64=False, switch=switch)
-    res["held_out"] = {"seed": a.held_seed, **summarize(recs[:nf])}
+        recs += compare_starts(net, held[nf:], device=a.device, fp64=False, switch=switch,
+                               preconditioned=pc)
+    res["held_out"] = {"seed": a.held_seed, **summarize(recs[:nf])} if nf else None
     res["held_out_mixed_only"] = summarize(recs) if nf < len(recs) else None
     net.close()
     txt = json.dumps(res, indent=1)
