@@ -853,18 +853,12 @@ const double *active_mask(const deft_fmt *f) {
   return (f->p.terms & DEFT_TERM_MASK) ? f->mask : nullptr;
 }
 
-// pg = M^-1 g for the density preconditioner (DEFT_PC_DENSITY).
-int density_precond(deft_cg *c, const deft::FmtSpec &spec) {
-  Engine *e = eng_of(c);
-  return e->diag_precond(spec, c->x, c->g, active_mask(c->f), c->pg) ? eng_err(e) : DEFT_OK;
-}
-
+// (With DEFT_PC_DENSITY, pg is formed where the step uses it, together with
+// its dot products: step_secant.)
 int cg_eval(deft_cg *c, const deft::FmtSpec &spec) {
   double E;
   const bool pcd = c->pg && c->p.preconditioned == DEFT_PC_DENSITY;
   if (int s = fmt_eval(c->f, spec, c->x, c->g, pcd ? nullptr : c->pg, &E, nullptr)) return s;
-  if (pcd)
-    if (int s = density_precond(c, spec)) return s;
   c->evals++;
   if (spec.precision == deft::kPrecisionFP64) c->evals_fp64++;
   c->last_eval_mixed = spec.precision != deft::kPrecisionFP64;
@@ -888,11 +882,7 @@ int cg_eval_dots(deft_cg *c, const deft::FmtSpec &spec, int k, const double *con
   double E;
   if (e->energy_grad_dots(spec, c->x, c->f->V, c->f->mask, c->g, &E, k, a, b, out))
     return eng_err(e);
-  if (c->pg && c->p.preconditioned == DEFT_PC_DENSITY) {
-    if (int s = density_precond(c, spec)) return s;
-  } else if (c->pg && e->copy(c->g, c->pg)) {
-    return eng_err(e);
-  }
+  if (c->pg && c->p.preconditioned != DEFT_PC_DENSITY && e->copy(c->g, c->pg)) return eng_err(e);
   c->evals++;
   if (spec.precision == deft::kPrecisionFP64) c->evals_fp64++;
   c->last_eval_mixed = spec.precision != deft::kPrecisionFP64;
@@ -1005,10 +995,16 @@ int step_secant(deft_cg *c, deft_cg_status *st, const deft::FmtSpec &spec, doubl
   if (c->pg) {
     // Preconditioned Polak-Ribiere (src/ConjugateGradient.cpp:115-160):
     // beta = pg.(g - g_old) / (pg_old.g_old), d = -pg + beta d
-    const double *a[2] = {c->pg, c->pg};
-    const double *b[2] = {c->g, c->gold};
     double o[2];
-    if (e->dots(2, a, b, o)) return eng_err(e);
+    if (c->p.preconditioned == DEFT_PC_DENSITY) {
+      // pg = M^-1 g, M^-1 = n / (kT dV), formed with its two dot products
+      if (e->precond_dots(spec, c->x, c->g, active_mask(c->f), c->pg, c->gold, o))
+        return eng_err(e);
+    } else {
+      const double *a[2] = {c->pg, c->pg};
+      const double *b[2] = {c->g, c->gold};
+      if (e->dots(2, a, b, o)) return eng_err(e);
+    }
     pgg = o[0];
     if (c->pgoldsqr != 0) {
       beta = (o[0] - o[1]) / c->pgoldsqr;
@@ -1122,14 +1118,10 @@ int step_newton(deft_cg *c, deft_cg_status *st, const deft::FmtSpec &spec) {
     }
     if (!(pq > 0)) break;  // no positive curvature along p: keep the step so far
     const double alpha = rz / pq;
-    if (e->axpy(alpha, p, dx) || e->axpy(-alpha, q, r)) return eng_err(e);
-    if (e->diag_precond(spec, c->x, r, active_mask(c->f), z)) return eng_err(e);
+    // dx += alpha p, r -= alpha q, z = M^-1 r, (r.r, r.z) in one pass
     double o[2];
-    {
-      const double *a[2] = {r, r};
-      const double *b[2] = {r, z};
-      if (e->dots(2, a, b, o)) return eng_err(e);
-    }
+    if (e->newton_update(spec, c->x, alpha, p, q, dx, r, active_mask(c->f), z, o))
+      return eng_err(e);
     if (std::sqrt(o[0]) < tol) break;
     if (e->scal_add(o[1] / rz, p, 1.0, z)) return eng_err(e);
     rz = o[1];

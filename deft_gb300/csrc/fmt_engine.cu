@@ -295,7 +295,10 @@ __global__ void __launch_bounds__(kThreads) k_z_c2r(const typename Cplx<T>::type
   }
 }
 
-// FFT along y of complex fields.  grid = (kz tiles, Nx, fields).
+// FFT along y of complex fields.  The (x, kz) lines of a field are tiled B at
+// a time in their flattened order l = x*NzH + kz, so every tile but the last
+// is full whatever B is (NzH = N/2+1 is odd for even N).  grid = (line
+// tiles, fields).
 template <typename T, int SIGN, int RN = 0>
 __global__ void DEFT_FFT_BOUNDS(RN) k_y_fft(typename Cplx<T>::type *data, Geom g,
                                                     FftPlan py, FastDiv fB) {
@@ -304,22 +307,24 @@ __global__ void DEFT_FFT_BOUNDS(RN) k_y_fft(typename Cplx<T>::type *data, Geom g
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C *buf0 = reinterpret_cast<C *>(smem_raw);
   C *buf1 = buf0 + g.Ny * B;
-  const int kz0 = blockIdx.x * B;
-  C *base = data + (size_t)blockIdx.z * g.NC + (size_t)blockIdx.y * g.Ny * g.NzH;
+  const int l0 = blockIdx.x * B, lines = g.Nx * g.NzH;
+  C *base = data + (size_t)blockIdx.y * g.NC;
   #pragma unroll 4
   for (int idx = threadIdx.x; idx < g.Ny * B; idx += blockDim.x) {
-    int e, b;
+    int e, b, x, kz;
     fdivmod(idx, fB, e, b);
-    const int kz = kz0 + b;
-    buf0[idx] = kz < g.NzH ? base[(size_t)e * g.NzH + kz] : C{0, 0};
+    const int l = l0 + b;
+    fdivmod(l, g.fNzH, x, kz);
+    buf0[idx] = l < lines ? base[((size_t)x * g.Ny + e) * g.NzH + kz] : C{0, 0};
   }
   C *res = fft_tile<T, SIGN, RN>(buf0, buf1, fB, py);
   #pragma unroll 4
   for (int idx = threadIdx.x; idx < g.Ny * B; idx += blockDim.x) {
-    int e, b;
+    int e, b, x, kz;
     fdivmod(idx, fB, e, b);
-    const int kz = kz0 + b;
-    if (kz < g.NzH) base[(size_t)e * g.NzH + kz] = res[idx];
+    const int l = l0 + b;
+    fdivmod(l, g.fNzH, x, kz);
+    if (l < lines) base[((size_t)x * g.Ny + e) * g.NzH + kz] = res[idx];
   }
 }
 
@@ -914,6 +919,80 @@ __global__ void k_dots(int k, const double *a0, const double *b0, const double *
   }
 }
 
+// Last-block reduction of per-thread sums acc[0..K) (fixed order, so the
+// result is bit-reproducible): every block writes its block sum to
+// partials, the last block to arrive sums them into out[0..K) and resets
+// the counter.
+template <int K>
+__device__ void finish_dots(double (&acc)[K], double *red, double *partials,
+                            unsigned int *counter, double *out) {
+  __shared__ bool last;
+  block_reduce<K>(acc, red);
+  if (threadIdx.x == 0) {
+    for (int t = 0; t < K; t++) partials[(size_t)blockIdx.x * K + t] = acc[t];
+    __threadfence();
+    const unsigned int done = atomicAdd(counter, 1u);
+    last = (done == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  double s[K];
+  for (int t = 0; t < K; t++) s[t] = 0;
+  for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
+    for (int t = 0; t < K; t++) s[t] += ((volatile double *)partials)[(size_t)b * K + t];
+  __syncthreads();
+  block_reduce<K>(s, red);
+  if (threadIdx.x == 0) {
+    for (int t = 0; t < K; t++) out[t] = s[t];
+    *counter = 0;
+  }
+}
+
+// The density preconditioner of the secant CG with its two dot products in
+// one pass: z = g n / (kT dV) (0 where masked or n <= 0), out = (z.g, z.h).
+__global__ void k_precond_dots(const double *__restrict__ n, const double *__restrict__ g,
+                               const double *__restrict__ mask, const double *__restrict__ h,
+                               double inv_c, double *__restrict__ z, int N, double *partials,
+                               unsigned int *counter, double *out) {
+  __shared__ double red[32 * 2];
+  double acc[2] = {0, 0};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+    const double m = mask ? mask[i] : 1.0;
+    const double nv = n[i], gv = g[i];
+    const double zv = (m == 0 || !(nv > 0)) ? 0.0 : gv * nv * inv_c;
+    z[i] = zv;
+    acc[0] += zv * gv;
+    acc[1] += zv * h[i];
+  }
+  finish_dots<2>(acc, red, partials, counter, out);
+}
+
+// One update of the Newton step's preconditioned linear CG in one pass:
+// dx += alpha p, r -= alpha q, z = r n / (kT dV) (0 where masked or
+// n <= 0), out = (r.r, r.z).
+__global__ void k_newton_update(double alpha, const double *__restrict__ p,
+                                const double *__restrict__ q, double *__restrict__ dx,
+                                double *__restrict__ r, const double *__restrict__ n,
+                                const double *__restrict__ mask, double inv_c,
+                                double *__restrict__ z, int N, double *partials,
+                                unsigned int *counter, double *out) {
+  __shared__ double red[32 * 2];
+  double acc[2] = {0, 0};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+    dx[i] += alpha * p[i];
+    const double rv = r[i] + (-alpha) * q[i];
+    r[i] = rv;
+    const double m = mask ? mask[i] : 1.0;
+    const double nv = n[i];
+    const double zv = (m == 0 || !(nv > 0)) ? 0.0 : rv * nv * inv_c;
+    z[i] = zv;
+    acc[0] += rv * rv;
+    acc[1] += rv * zv;
+  }
+  finish_dots<2>(acc, red, partials, counter, out);
+}
+
 // Vector kernels: two doubles per thread per step (16-byte accesses); the
 // vectors come from cudaMalloc (256-byte aligned), n odd leaves a tail.
 __global__ void k_axpy(double alpha, const double *x, double *y, int n) {
@@ -1068,7 +1147,7 @@ Tiles make_tiles(const Geom &g, size_t cs, size_t budget, const TileChoice *ov =
   Tiles t;
   const int pairs = (g.lines + 1) / 2;
   auto cap = [](size_t v, int hi) { return (int)(v < (size_t)hi ? v : (size_t)hi); };
-  t.By = even_tiles(g.NzH, cap(budget / (2 * (size_t)g.Ny * cs), 16));
+  t.By = even_tiles(g.Nx * g.NzH, cap(budget / (2 * (size_t)g.Ny * cs), 16));
   t.Bx = even_tiles(g.Ny * g.NzH, cap(budget / (2 * (size_t)g.Nx * cs), 16));
   t.Bxf = even_tiles(g.Ny * g.NzH, cap(budget / (3 * (size_t)g.Nx * cs), 16));
   t.Bxc = even_tiles(g.Ny * g.NzH, cap(budget / (10 * (size_t)g.Nx * cs), 16));
@@ -1078,7 +1157,7 @@ Tiles make_tiles(const Geom &g, size_t cs, size_t budget, const TileChoice *ov =
   if (pm > 1 && pm % 2 == 0) pm -= 1;  // odd: conflict-free z-strided shared accesses
   t.Pphi = pm < pairs ? pm : pairs;
   if (ov) {
-    if (ov->By > 0) t.By = ov->By < g.NzH ? ov->By : g.NzH;
+    if (ov->By > 0) t.By = ov->By < g.Nx * g.NzH ? ov->By : g.Nx * g.NzH;
     if (ov->Bx > 0) t.Bx = ov->Bx < g.Ny * g.NzH ? ov->Bx : g.Ny * g.NzH;
     if (ov->Bxf > 0) t.Bxf = ov->Bxf < g.Ny * g.NzH ? ov->Bxf : g.Ny * g.NzH;
     if (ov->Bxc > 0) t.Bxc = ov->Bxc < g.Ny * g.NzH ? ov->Bxc : g.Ny * g.NzH;
@@ -1129,13 +1208,13 @@ enum KernelId {
   kK_z_r2c, kK_z_c2r, kK_y_fft1, kK_y_fft5, kK_x_fft, kK_x_conv_fwd, kK_x_conv_adj, kK_z_phi_grad,
   kK_z_phi_energy, kK_z_grad, kK_local_energy, kK_reduce_terms, kK_dots, kK_axpy, kK_scal_add,
   kK_weight_table, kK_z_hess, kK_z_jac, kK_z_hvp_out, kK_veff_density, kK_veff_grad,
-  kK_diag_precond, kNumKernels
+  kK_diag_precond, kK_precond_dots, kK_newton_update, kNumKernels
 };
 const char *const kKernelNames[kNumKernels] = {
     "z_r2c", "z_c2r", "y_fft_1field", "y_fft_5fields", "x_fft", "x_conv_fwd", "x_conv_adj", "z_phi_grad",
     "z_phi_energy", "z_grad", "local_energy", "reduce_terms", "dots", "axpy", "scal_add",
     "weight_table", "z_hess", "z_jac", "z_hvp_out", "veff_density", "veff_grad",
-    "diag_precond"};
+    "diag_precond", "precond_dots", "newton_update"};
 
 // Calls f(std::integral_constant<int, RN>()) with RN = the plan's length
 // when it is an FP32 plan marked for the register-resident transform, else
@@ -1521,7 +1600,7 @@ class EngineImpl {
 
   template <typename T> void y_fft(typename Cplx<T>::type *data, int nf, int sign) {
     const Tiles &t = tl<T>();
-    dim3 grid((g.NzH + t.By - 1) / t.By, g.Nx, nf);
+    dim3 grid((g.Nx * g.NzH + t.By - 1) / t.By, nf);
     const int kid = kslot<T>(nf == 1 ? kK_y_fft1 : kK_y_fft5);
     pre(kid);
     with_rn<T>(plan<T>(1), [&](auto rn) {
@@ -1691,6 +1770,16 @@ class EngineImpl {
     if (E_host) *E_host = results_host[kNumTerms];
     if (terms_host) memcpy(terms_host, results_host, sizeof(double) * kNumTerms);
     for (int i = 0; i < kd; i++) dots_host[i] = results_host[8 + i];
+    return 0;
+  }
+
+  // Copies results[0..k) to out_host after the stream's queued work.
+  int read_results(int k, double *out_host, const char *what) {
+    cudaMemcpyAsync(results_host, results, sizeof(double) * 3, cudaMemcpyDeviceToHost, stream);
+    cudaError_t err = cudaStreamSynchronize(stream);
+    if (err != cudaSuccess) return fail(what, err);
+    harvest();
+    for (int i = 0; i < k; i++) out_host[i] = results_host[i];
     return 0;
   }
 
@@ -1931,12 +2020,7 @@ int Engine::dots(int k, const double *const *a, const double *const *b, double *
                                                   k > 2 ? b[2] : nullptr, e.g.NR, e.dot_partials,
                                                   e.dot_counter, e.results);
     e.post(kK_dots);
-  cudaMemcpyAsync(e.results_host, e.results, sizeof(double) * 3, cudaMemcpyDeviceToHost, e.stream);
-  cudaError_t err = cudaStreamSynchronize(e.stream);
-  if (err != cudaSuccess) return e.fail("dots", err);
-  e.harvest();
-  for (int i = 0; i < k; i++) out_host[i] = e.results_host[i];
-  return 0;
+  return e.read_results(k, out_host, "dots");
 }
 
 int Engine::axpy(double alpha, const double *x, double *y) {
@@ -1970,6 +2054,30 @@ int Engine::diag_precond(const FmtSpec &f, const double *n, const double *r, con
                                                           e.g.NR);
   e.post(kK_diag_precond);
   return e.check("diag_precond");
+}
+
+int Engine::precond_dots(const FmtSpec &f, const double *n, const double *g, const double *mask,
+                         double *z, const double *h, double *out_host) {
+  EngineImpl &e = *impl_;
+  e.pre(kK_precond_dots);
+  k_precond_dots<<<e.dot_blocks, kThreads, 0, e.stream>>>(n, g, mask, h, 1.0 / (f.kT * e.g.dV), z,
+                                                          e.g.NR, e.dot_partials, e.dot_counter,
+                                                          e.results);
+  e.post(kK_precond_dots);
+  return e.read_results(2, out_host, "precond_dots");
+}
+
+int Engine::newton_update(const FmtSpec &f, const double *n, double alpha, const double *p,
+                          const double *q, double *dx, double *r, const double *mask, double *z,
+                          double *out_host) {
+  EngineImpl &e = *impl_;
+  e.pre(kK_newton_update);
+  k_newton_update<<<e.dot_blocks, kThreads, 0, e.stream>>>(alpha, p, q, dx, r, n, mask,
+                                                           1.0 / (f.kT * e.g.dV), z, e.g.NR,
+                                                           e.dot_partials, e.dot_counter,
+                                                           e.results);
+  e.post(kK_newton_update);
+  return e.read_results(2, out_host, "newton_update");
 }
 
 int Engine::veff_density(double kT, const double *x, double *n) {
@@ -2240,7 +2348,8 @@ int noalloc_energy_grad(const GridSpec &s, const FmtSpec &f, const double *n, co
   }
   const int ptiles_z = (pairs + t.Pz - 1) / t.Pz;
   const int xt = (g.Ny * g.NzH + t.Bxc - 1) / t.Bxc;
-  const dim3 ygrid1((g.NzH + t.By - 1) / t.By, g.Nx, 1), ygrid5((g.NzH + t.By - 1) / t.By, g.Nx, 5);
+  const dim3 ygrid1((g.Nx * g.NzH + t.By - 1) / t.By, 1),
+      ygrid5((g.Nx * g.NzH + t.By - 1) / t.By, 5);
   {
     const int blocks = (g.NC + kThreads - 1) / kThreads;
     k_weight_table<double><<<blocks < 4096 ? blocks : 4096, kThreads, 0, stream>>>(g, f.R, w3, w2,

@@ -63,7 +63,7 @@ inline void geom_finish(Geom &g) {
 // Launch shapes of one precision's kernels and the radix order of each axis's
 // FFT plan (an autotuner's choice).  A zero entry keeps the built-in rule; a
 // radix list ends at the first 0.
-//   By   kz columns per y-FFT tile          Bx   columns per plain x-FFT tile
+//   By   (x, kz) lines per y-FFT tile       Bx   columns per plain x-FFT tile
 //   Bxf  columns per forward-convolution x tile
 //   Bxc  columns per adjoint-convolution x tile (five fields each)
 //   Pz   z-line pairs per r2c / c2r / gradient tile
@@ -130,6 +130,16 @@ class Engine {
   // masked), the preconditioner of the Newton step's linear CG.
   int diag_precond(const FmtSpec &f, const double *n, const double *r, const double *mask,
                    double *z);
+
+  // The density preconditioner of the secant CG, z = g n / (kT dV) (0 where
+  // masked or n <= 0), and out_host = (z.g, z.h) in the same pass; one sync.
+  int precond_dots(const FmtSpec &f, const double *n, const double *g, const double *mask,
+                   double *z, const double *h, double *out_host);
+  // One update of the Newton step's linear CG in one pass: dx += alpha p,
+  // r -= alpha q, z = r n / (kT dV), out_host = (r.r, r.z); one sync.
+  int newton_update(const FmtSpec &f, const double *n, double alpha, const double *p,
+                    const double *q, double *dx, double *r, const double *mask, double *z,
+                    double *out_host);
 
   // Vector kernels (NR-long device vectors).
   // out_host[i] = a_i . b_i for i < k (k <= 3), one pass, one sync.
