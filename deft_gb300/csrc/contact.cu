@@ -49,13 +49,13 @@ struct Partials {
 };
 
 __device__ Partials partials(int kind, double R, double n3, double n2, double v2) {
-  const double u = 1.0 / (1.0 - n3);
+  const double u = 1.0 / (1.0 - n3), l = log(1.0 - n3);
   double f2[3], f3[3];
-  hs_coeffs<double>(kind, n3, u, f2, f3);
+  hs_coeffs<double>(kind, n3, u, l, f2, f3);
   const double c1 = 1.0 / (4 * kPi * R), c0 = c1 / R;
   const double q = n2 * n2 - v2, t3 = n2 * (n2 * n2 - 3 * v2);
   Partials p;
-  p.d0 = -log(1.0 - n3);
+  p.d0 = -l;
   p.d1 = n2 * f2[0];
   p.d2 = c1 * n2 * f2[0] + 3 * q * f3[0];
   p.d3 = c0 * n2 * u + c1 * q * f2[1] + t3 * f3[1];

@@ -51,9 +51,9 @@ template <typename T> __device__ __forceinline__ T wb_log(T x);
 template <> __device__ __forceinline__ double wb_log<double>(double x) { return log(x); }
 template <> __device__ __forceinline__ float wb_log<float>(float x) { return logf(x); }
 
-// S, S', S'' at e.
+// S, S', S'' at e; l = ln(1 - e) (computed once by the caller).
 template <typename T>
-__device__ __forceinline__ void wb_S(T e, T &S, T &dS, T &d2S) {
+__device__ __forceinline__ void wb_S(T e, T l, T &S, T &dS, T &d2S) {
   if (fabs(e) < WbConst<T>::series_below) {
     T s = T(1.5), ds = T(0), d2s = T(0);
     T pm2 = T(1), pm1 = T(1);  // e^(j-2) (from j = 2), e^(j-1)
@@ -73,7 +73,6 @@ __device__ __forceinline__ void wb_S(T e, T &S, T &dS, T &d2S) {
     d2S = d2s;
   } else {
     const T one_m = T(1) - e;
-    const T l = wb_log<T>(one_m);
     const T g = e + one_m * one_m * l;
     const T dg = e - T(2) * one_m * l;
     const T d2g = T(3) + T(2) * l;
@@ -85,9 +84,10 @@ __device__ __forceinline__ void wb_S(T e, T &S, T &dS, T &d2S) {
   }
 }
 
-// P2, P3 of the mark II functional and their first two derivatives.
+// P2, P3 of the mark II functional and their first two derivatives;
+// l = ln(1 - e).
 template <typename T>
-__device__ __forceinline__ void m2_P(T e, T P2[3], T P3[3]) {
+__device__ __forceinline__ void m2_P(T e, T l, T P2[3], T P3[3]) {
   if (fabs(e) < WbConst<T>::m2_below) {
     T p2 = T(0), dp2 = T(0), d2p2 = T(0), p3 = T(0), dp3 = T(0), d2p3 = T(0);
     T ekm3 = T(0);  // e^(k-3): read from k = 3 on, after the first shift
@@ -117,7 +117,6 @@ __device__ __forceinline__ void m2_P(T e, T P2[3], T P3[3]) {
     P3[2] = T(4.0 / 3) * d2p3;
   } else {
     const T one_m = T(1) - e;
-    const T l = wb_log<T>(one_m);
     const T ie = T(1) / e, ie2 = ie * ie, ie3 = ie2 * ie;
     // P2 = 1 + (6 - 3e + 6B) / 9, B = (1-e) ln(1-e) / e
     const T B = one_m * l * ie;
@@ -138,13 +137,14 @@ __device__ __forceinline__ void m2_P(T e, T P2[3], T P3[3]) {
   }
 }
 
-// f2, f3 of the kind and their first two derivatives at e = n3 (u = 1/(1-e)).
+// f2, f3 of the kind and their first two derivatives at e = n3
+// (u = 1/(1-e), l = ln(1-e)).
 template <typename T>
-__device__ __forceinline__ void hs_coeffs(int kind, T e, T u, T f2[3], T f3[3]) {
+__device__ __forceinline__ void hs_coeffs(int kind, T e, T u, T l, T f2[3], T f3[3]) {
   const T u2 = u * u;
   if (kind == kHsMarkII) {
     T P2[3], P3[3];
-    m2_P<T>(e, P2, P3);
+    m2_P<T>(e, l, P2, P3);
     const T k24 = T(1.0 / (24 * 3.14159265358979323846));
     f2[0] = P2[0] * u;
     f2[1] = P2[1] * u + P2[0] * u2;
@@ -165,7 +165,7 @@ __device__ __forceinline__ void hs_coeffs(int kind, T e, T u, T f2[3], T f3[3]) 
     return;
   }
   T S, dS, d2S;
-  wb_S<T>(e, S, dS, d2S);
+  wb_S<T>(e, l, S, dS, d2S);
   const T k36 = T(1.0 / (36 * 3.14159265358979323846));
   f3[0] = S * u2 * k36;
   f3[1] = (dS + T(2) * S * u) * u2 * k36;
@@ -187,7 +187,7 @@ __device__ __forceinline__ void wb_phi(const WbRadius &r, T n3, T n2, T vx, T vy
   const T u = T(1) / (T(1) - n3);
   const T l = wb_log<T>(T(1) - n3);
   T f2[3], f3[3];
-  hs_coeffs<T>(r.kind, n3, u, f2, f3);
+  hs_coeffs<T>(r.kind, n3, u, l, f2, f3);
   const T q = n2 * n2 - v2;
   const T t3 = n2 * (n2 * n2 - T(3) * v2);
   phi[0] = f3[0] * t3;
@@ -211,7 +211,7 @@ __device__ __forceinline__ void wb_hess(const WbRadius &r, T n3, T n2, T vx, T v
   const T v2 = vx * vx + vy * vy + vz * vz;
   const T u = T(1) / (T(1) - n3);
   T f2[3], f3[3];
-  hs_coeffs<T>(r.kind, n3, u, f2, f3);
+  hs_coeffs<T>(r.kind, n3, u, wb_log<T>(T(1) - n3), f2, f3);
   const T u2 = u * u;
   const T q = n2 * n2 - v2;
   const T t3 = n2 * (n2 * n2 - T(3) * v2);
