@@ -12,6 +12,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <utility>
 #include <vector>
 
 using deft::Engine;
@@ -1010,21 +1011,16 @@ int step_secant(deft_cg *c, deft_cg_status *st, const deft::FmtSpec &spec, doubl
       beta = (o[0] - o[1]) / c->pgoldsqr;
       if (beta < 0 || beta != beta) beta = 0;
     }
-    if (e->scal_add(beta, c->d, -1.0, c->pg)) return eng_err(e);
   } else {
     // Polak-Ribiere with reset (src/ConjugateGradient.cpp:77-91)
     if (c->goldsqr > 0) {
       beta = (c->gg - c->ggold) / c->goldsqr;
       if (beta < 0 || beta != beta) beta = 0;
     }
-    if (e->scal_add(beta, c->d, -1.0, c->g)) return eng_err(e);
   }
+  // d = -(p)g + beta d and its slope s0 = g.d, one pass
   double s0;
-  {
-    const double *a[1] = {c->g};
-    const double *b[1] = {c->d};
-    if (e->dots(1, a, b, &s0)) return eng_err(e);
-  }
+  if (e->scal_add_dot(beta, c->d, -1.0, c->pg ? c->pg : c->g, c->g, &s0)) return eng_err(e);
   if (!(s0 < 0) && c->pg && beta != 0) {
     // not downhill: the preconditioned steepest direction
     if (e->scal_add(0.0, c->d, -1.0, c->pg)) return eng_err(e);
@@ -1036,7 +1032,8 @@ int step_secant(deft_cg *c, deft_cg_status *st, const deft::FmtSpec &spec, doubl
     s0 = -c->gg;
   }
   c->pgoldsqr = pgg;
-  if (e->copy(c->g, c->gold)) return eng_err(e);
+  // g_old = g by exchanging the buffers: the next evaluation writes g
+  std::swap(c->g, c->gold);
   c->goldsqr = c->gg;
   if (c->iter > 0 && s0 != 0) c->alpha *= c->s_prev / s0;
   c->s_prev = s0;

@@ -63,7 +63,7 @@ inline void geom_finish(Geom &g) {
 // Launch shapes of one precision's kernels and the radix order of each axis's
 // FFT plan (an autotuner's choice).  A zero entry keeps the built-in rule; a
 // radix list ends at the first 0.
-//   By   (x, kz) lines per y-FFT tile       Bx   columns per plain x-FFT tile
+//   By   kz columns per y-FFT tile          Bx   columns per plain x-FFT tile
 //   Bxf  columns per forward-convolution x tile
 //   Bxc  columns per adjoint-convolution x tile (five fields each)
 //   Pz   z-line pairs per r2c / c2r / gradient tile
@@ -140,6 +140,10 @@ class Engine {
   int newton_update(const FmtSpec &f, const double *n, double alpha, const double *p,
                     const double *q, double *dx, double *r, const double *mask, double *z,
                     double *out_host);
+
+  // d = alpha g + beta d and out_host = h.d in one pass; one sync.
+  int scal_add_dot(double beta, double *d, double alpha, const double *g, const double *h,
+                   double *out_host);
 
   // Vector kernels (NR-long device vectors).
   // out_host[i] = a_i . b_i for i < k (k <= 3), one pass, one sync.
