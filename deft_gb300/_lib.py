@@ -15,7 +15,7 @@ TERM_HS, TERM_IDEAL, TERM_MU, TERM_VEXT, TERM_MASK, TERM_VEFF = 1, 2, 4, 8, 16, 
 NTERMS = 6
 LS_SECANT, LS_QUADRATIC_REF = 0, 1
 PC_NONE, PC_FUNCTIONAL, PC_DENSITY = 0, 1, 2
-HS_WB_NOTENSOR, HS_RF, HS_WB_MARK2 = 0, 1, 2
+HS_WB_NOTENSOR, HS_RF, HS_WB_MARK2, HS_WB_TENSOR, HS_TARAZONA = 0, 1, 2, 3, 4
 CONTACT_GSIGMA_S, CONTACT_GSIGMA_A, CONTACT_GROSS, CONTACT_YUWU, CONTACT_YUWU_S = 0, 1, 2, 3, 4
 
 # Every symbol include/deft_gb300.h declares.

@@ -20,7 +20,8 @@ Names, argument meaning and return conventions follow the reference:
   ``m.energy()``, ``m.grad()``  src/LineMinimizer.h:18-19, src/Minimizer.h:13-60
 * ``find_chemical_potential(f, kT, n)``          src/equation-of-state.cpp:189-192
 * ``HardSpheresRF(R)`` src/HardSpheres.cpp:69-88; ``WhiteBearMarkII(R)``
-  src/haskell/WhiteBear.hs:140-159
+  src/haskell/WhiteBear.hs:140-159; ``HardSpheresWB(R)`` (tensor, also
+  ``HardSpheres``) and ``HardSpheresTarazona(R)`` src/HardSpheres.cpp:90-135
 * ``gSigmaS(R)``, ``gSigmaA(R)``, ``gSigmaSm2(R)``, ``gSigmaAm2(R)``,
   ``CorrelationGrossCorrect(R)``, ``YuWuCorrelation(R)``,
   ``YuWuCorrelation_S(R)``, each called as ``f(kT, gd, density)``
@@ -338,6 +339,19 @@ def HardSpheresWBnotensor(R):
 def HardSpheresRF(R):
     """Rosenfeld's functional (src/HardSpheres.cpp:69-88)."""
     return Functional(R=float(R), names=("phi3", "phi1", "phi2"), hs=_lib.HS_RF)
+
+
+def HardSpheresWB(R):
+    """White Bear with the tensor third term (src/HardSpheres.cpp:113-135)."""
+    return Functional(R=float(R), names=("phi3", "phi1", "phi2"), hs=_lib.HS_WB_TENSOR)
+
+
+def HardSpheresTarazona(R):
+    """Tarazona's tensor functional (src/HardSpheres.cpp:90-111)."""
+    return Functional(R=float(R), names=("phi3", "phi1", "phi2"), hs=_lib.HS_TARAZONA)
+
+
+HardSpheres = HardSpheresWB  # src/HardSpheres.cpp:185-187
 
 
 def WhiteBearMarkII(R):

@@ -6,6 +6,7 @@
 #include "../../include/deft_gb300.h"
 #include "contact.h"
 #include "fmt_engine.h"
+#include "tensor.h"
 
 #include <cmath>
 #include <cstdio>
@@ -39,6 +40,7 @@ struct deft_fmt {
   double *g_buf;
   double *w_buf;  // 5*NR, allocated on first deft_fmt_weighted
   double *n_veff = nullptr, *gn_veff = nullptr;  // NR each, DEFT_TERM_VEFF only
+  double *t_buf = nullptr, *t_grad = nullptr;     // tensor functionals only
 };
 
 struct deft_cg {
@@ -413,8 +415,10 @@ static int check_fmt_params(const deft_fmt_params *p) {
   if (!(p->R > 0) || !(p->kT > 0)) return set_err(DEFT_ERR_ARG, "R and kT must be positive");
   if (p->precision != DEFT_PRECISION_FP64 && p->precision != DEFT_PRECISION_MIXED)
     return set_err(DEFT_ERR_ARG, "unknown precision");
-  if (p->functional < DEFT_HS_WB_NOTENSOR || p->functional > DEFT_HS_WB_MARK2)
+  if (p->functional < DEFT_HS_WB_NOTENSOR || p->functional > DEFT_HS_TARAZONA)
     return set_err(DEFT_ERR_ARG, "unknown hard-sphere functional");
+  if (p->functional >= DEFT_HS_WB_TENSOR && p->precision != DEFT_PRECISION_FP64)
+    return set_err(DEFT_ERR_ARG, "the tensor functionals evaluate in FP64 only");
   return DEFT_OK;
 }
 
@@ -442,6 +446,7 @@ int deft_fmt_destroy(deft_fmt *f) {
   cudaFree(f->mask);
   cudaFree(f->g_buf);
   cudaFree(f->w_buf);
+  cudaFree(f->t_buf);
   cudaFree(f->n_veff);
   cudaFree(f->gn_veff);
   delete f;
@@ -501,6 +506,50 @@ int fmt_density(deft_fmt *f, const deft::FmtSpec &spec, const double *x, const d
   return DEFT_OK;
 }
 
+bool is_tensor(const deft_fmt *f) {
+  return f->p.functional >= DEFT_HS_WB_TENSOR && (f->p.terms & DEFT_TERM_HS);
+}
+
+// Energy (grad == NULL) or energy and masked gradient at the density n.
+// The tensor functionals' hard-sphere part comes from tensor.cu and the
+// local terms (ideal gas, mu, V_ext, mask) from the fused evaluator.
+int density_eval(deft_fmt *f, const deft::FmtSpec &spec, const double *n, double *grad,
+                 double *E, double *terms) {
+  Engine *e = f->grid->eng;
+  if (!is_tensor(f)) {
+    if (!grad) return e->energy(spec, n, f->V, f->mask, E, terms) ? eng_err(e) : DEFT_OK;
+    return e->energy_grad(spec, n, f->V, f->mask, grad, E, terms) ? eng_err(e) : DEFT_OK;
+  }
+  deft_grid *g = f->grid;
+  if (!f->t_buf) {
+    const size_t nd = deft::tensor_scratch_doubles(e->geom()) + nr(g);
+    cudaError_t ce = cudaMalloc((void **)&f->t_buf, sizeof(double) * nd);
+    if (ce != cudaSuccess) {
+      f->t_buf = nullptr;
+      return cuda_err(ce, "cudaMalloc");
+    }
+    f->t_grad = f->t_buf + deft::tensor_scratch_doubles(e->geom());
+  }
+  double t3[3];
+  std::string err;
+  if (deft::tensor_hs(e, spec, n, f->t_buf, grad ? f->t_grad : nullptr, t3, &err))
+    return set_err(DEFT_ERR_CUDA, err);
+  deft::FmtSpec loc = spec;
+  loc.terms &= ~DEFT_TERM_HS;
+  double El, tl[deft::kNumTerms];
+  if (grad ? e->energy_grad(loc, n, f->V, f->mask, grad, &El, tl)
+           : e->energy(loc, n, f->V, f->mask, &El, tl))
+    return eng_err(e);
+  if (grad && deft::add_masked(e, f->t_grad, (loc.terms & DEFT_TERM_MASK) ? f->mask : nullptr, grad))
+    return set_err(DEFT_ERR_CUDA, "tensor functional: gradient sum");
+  *E = El + t3[0] + t3[1] + t3[2];
+  if (terms) {
+    memcpy(terms, tl, sizeof(tl));
+    for (int i = 0; i < 3; i++) terms[i] = t3[i];
+  }
+  return DEFT_OK;
+}
+
 // Energy (grad == NULL) or energy, gradient and, if pgrad != NULL, the
 // preconditioned gradient at the variable x (device arrays).
 int fmt_eval(deft_fmt *f, const deft::FmtSpec &spec, const double *x, double *grad,
@@ -508,12 +557,12 @@ int fmt_eval(deft_fmt *f, const deft::FmtSpec &spec, const double *x, double *gr
   Engine *e = f->grid->eng;
   const double *n;
   if (int s = fmt_density(f, spec, x, &n)) return s;
-  if (!grad) return e->energy(spec, n, f->V, f->mask, E, terms) ? eng_err(e) : DEFT_OK;
+  if (!grad) return density_eval(f, spec, n, nullptr, E, terms);
   if (f->p.terms & DEFT_TERM_VEFF) {
-    if (e->energy_grad(spec, n, f->V, f->mask, f->gn_veff, E, terms)) return eng_err(e);
+    if (int s = density_eval(f, spec, n, f->gn_veff, E, terms)) return s;
     if (e->veff_grad(spec.kT, x, n, f->gn_veff, grad, pgrad)) return eng_err(e);
   } else {
-    if (e->energy_grad(spec, n, f->V, f->mask, grad, E, terms)) return eng_err(e);
+    if (int s = density_eval(f, spec, n, grad, E, terms)) return s;
     if (pgrad && e->copy(grad, pgrad)) return eng_err(e);
   }
   return DEFT_OK;
@@ -598,6 +647,9 @@ int deft_fmt_contact(deft_fmt *f, const double *n, int on_device, int which, dou
   if (!f || !n || !out) return set_err(DEFT_ERR_ARG, "NULL argument");
   if (which < DEFT_CONTACT_GSIGMA_S || which > DEFT_CONTACT_YUWU_S)
     return set_err(DEFT_ERR_ARG, "unknown contact field");
+  if (f->p.functional >= DEFT_HS_WB_TENSOR)
+    return set_err(DEFT_ERR_ARG,
+                   "contact values are built for the White Bear, Rosenfeld and mark II functionals");
   deft_grid *g = f->grid;
   cudaSetDevice(g->ctx->device);
   const double *src;
@@ -627,6 +679,8 @@ int deft_fmt_hessian_vector(deft_fmt *f, const double *n, const double *dx, int 
   if (int s = check_terms(f)) return s;
   if (f->p.terms & DEFT_TERM_VEFF)
     return set_err(DEFT_ERR_ARG, "Hessian-vector products are in the density variable only");
+  if (is_tensor(f))
+    return set_err(DEFT_ERR_ARG, "Hessian-vector products are not built for the tensor functionals");
   deft_grid *g = f->grid;
   cudaSetDevice(g->ctx->device);
   const double *ns, *ds;
@@ -695,6 +749,8 @@ int deft_fmt_energy_grad_noalloc(const double lat[9], int Nx, int Ny, int Nz,
     return set_err(DEFT_ERR_ARG, "DEFT_TERM_MASK set but mask is NULL");
   if (p->precision != DEFT_PRECISION_FP64)
     return set_err(DEFT_ERR_ARG, "the allocation-free entry point evaluates in FP64 only");
+  if (p->functional >= DEFT_HS_WB_TENSOR && (p->terms & DEFT_TERM_HS))
+    return set_err(DEFT_ERR_ARG, "the allocation-free entry point has no tensor functionals");
   deft::GridSpec s;
   s.Nx = Nx;
   s.Ny = Ny;
@@ -876,7 +932,7 @@ int cg_eval(deft_cg *c, const deft::FmtSpec &spec) {
 int cg_eval_dots(deft_cg *c, const deft::FmtSpec &spec, int k, const double *const *a,
                  const double *const *b, double *out) {
   Engine *e = eng_of(c);
-  if (c->f->p.terms & DEFT_TERM_VEFF) {
+  if ((c->f->p.terms & DEFT_TERM_VEFF) || is_tensor(c->f)) {
     if (int s = cg_eval(c, spec)) return s;
     return e->dots(k, a, b, out) ? eng_err(e) : DEFT_OK;
   }

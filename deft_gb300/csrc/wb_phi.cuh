@@ -46,6 +46,9 @@ template <> struct WbConst<float> {
 constexpr int kHsWhiteBear = 0;
 constexpr int kHsRosenfeld = 1;
 constexpr int kHsMarkII = 2;
+// Tensor third term (tensor.cu): HardSpheresWB and HardSpheresTarazona.
+constexpr int kHsWhiteBearTensor = 3;
+constexpr int kHsTarazona = 4;
 
 template <typename T> __device__ __forceinline__ T wb_log(T x);
 template <> __device__ __forceinline__ double wb_log<double>(double x) { return log(x); }

@@ -119,6 +119,25 @@ static void weights_at(const double k[3], double R, double dr, double *w3, doubl
   }
 }
 
+/* Tensor shell weights xx, yy, zz, xy, yz, zx at k
+ * (src/ReciprocalOperators.h:292-404; 0 at k = 0). */
+static void tensor_weights(const double k[3], double R, double dr, double w[6]) {
+  const double k2 = k[0] * k[0] + k[1] * k[1] + k[2] * k[2], kk = sqrt(k2), kR = kk * R;
+  for (int i = 0; i < 6; i++) w[i] = 0;
+  if (!(kR > 0)) return;
+  const double smear = exp(-kSpreading * k2 * dr * dr);
+  const double s = sin(kR), c = cos(kR);
+  for (int a = 0; a < 3; a++) {
+    const double c2 = k[a] * k[a] / k2;
+    w[a] = smear * (4 * M_PI * R * R) *
+           (s / kR * (-1.0 / 3 + c2 - 3 * c2 / (kR * kR) + 1 / (kR * kR)) + c / (kR * kR) * (-1 + 3 * c2));
+  }
+  const int pa[3] = {0, 1, 2}, pb[3] = {1, 2, 0};
+  for (int o = 0; o < 3; o++)
+    w[3 + o] = -smear * (4 * M_PI) * k[pa[o]] * k[pb[o]] / (k2 * k2) *
+               ((3 - kR * kR) * s / kR - 3 * c);
+}
+
 typedef struct {
   size_t nr, nc;     /* real points, complex points */
   double dV, V, dr, scale;
@@ -180,6 +199,25 @@ static void weighted(const oracle_params *p, const kspace *ks, const double *n, 
       }
     }
     c2r(p, tk, out5 + (size_t)a * ks->nr);
+  }
+  free(nk);
+  free(tk);
+}
+
+/* out6 = the tensor weighted densities Txx, Tyy, Tzz, Txy, Tyz, Tzx. */
+static void tensor_weighted(const oracle_params *p, const kspace *ks, const double *n,
+                            double *out6) {
+  double *nk = (double *)malloc(sizeof(double) * 2 * ks->nc);
+  double *tk = (double *)malloc(sizeof(double) * 2 * ks->nc);
+  r2c(p, n, nk);
+  for (int a = 0; a < 6; a++) {
+    for (size_t i = 0; i < ks->nc; i++) {
+      double tw[6];
+      tensor_weights(ks->kv + 3 * i, p->R, ks->dr, tw);
+      tk[2 * i] = nk[2 * i] * ks->scale * tw[a];
+      tk[2 * i + 1] = nk[2 * i + 1] * ks->scale * tw[a];
+    }
+    c2r(p, tk, out6 + (size_t)a * ks->nr);
   }
   free(nk);
   free(tk);
@@ -308,6 +346,53 @@ static void phi_hs(int kind, double R, double n3, double n2, double vx, double v
   d[4] = cv * vz;
 }
 
+/* Tensor White Bear / Tarazona: phi1 and phi2 of the vector form, phi3 =
+ * f3(n3) [n2^3 - 3 n2 |v|^2 + 9 (v.T.v - tr(T^3)/2)] (TensorThirdTerm,
+ * src/HardSpheres.cpp:30-61) with f3 of White Bear (WBT) or Rosenfeld (TZ);
+ * d[0..10] = d phi / d(n3, n2, vx, vy, vz, Txx, Tyy, Tzz, Txy, Tyz, Tzx),
+ * the off-diagonal ones for the single variable T_ab = T_ba. */
+static void phi_tensor(int kind, double R, const double w[11], double phi[3], double d[11]) {
+  const double n3 = w[0], n2 = w[1], v[3] = {w[2], w[3], w[4]};
+  const double xx = w[5], yy = w[6], zz = w[7], xy = w[8], yz = w[9], zx = w[10];
+  const double v2 = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+  const double u = 1 / (1 - n3), l = log(1 - n3);
+  const double a1 = 1 / (4 * M_PI * R * R), a2 = 1 / (4 * M_PI * R);
+  double f3, df3;
+  if (kind == ORACLE_HS_WBT) {
+    double S, dS;
+    phi3_S(n3, &S, &dS);
+    f3 = S * u * u / (36 * M_PI);
+    df3 = (dS + 2 * S * u) * u * u / (36 * M_PI);
+  } else {
+    f3 = u * u / (24 * M_PI);
+    df3 = 2 * u * u * u / (24 * M_PI);
+  }
+  const double Tv[3] = {xx * v[0] + xy * v[1] + zx * v[2], xy * v[0] + yy * v[1] + yz * v[2],
+                        zx * v[0] + yz * v[1] + zz * v[2]};
+  const double T2xx = xx * xx + xy * xy + zx * zx, T2yy = xy * xy + yy * yy + yz * yz,
+               T2zz = zx * zx + yz * yz + zz * zz;
+  const double T2xy = xx * xy + xy * yy + zx * yz, T2yz = xy * zx + yy * yz + yz * zz,
+               T2zx = xx * zx + xy * yz + zx * zz;
+  const double vTv = v[0] * Tv[0] + v[1] * Tv[1] + v[2] * Tv[2];
+  const double tr3 = xx * T2xx + yy * T2yy + zz * T2zz + 2 * (xy * T2xy + yz * T2yz + zx * T2zx);
+  const double t = n2 * n2 * n2 - 3 * n2 * v2 + 9 * (vTv - 0.5 * tr3);
+  const double q = n2 * n2 - v2;
+  phi[0] = f3 * t;
+  phi[1] = -a1 * n2 * l;
+  phi[2] = a2 * q * u;
+  d[0] = a1 * n2 * u + a2 * q * u * u + df3 * t;
+  d[1] = -a1 * l + 2 * a2 * n2 * u + f3 * 3 * q;
+  for (int c = 0; c < 3; c++) d[2 + c] = -2 * a2 * u * v[c] + f3 * (-6 * n2 * v[c] + 18 * Tv[c]);
+  d[5] = f3 * 9 * (v[0] * v[0] - 1.5 * T2xx);
+  d[6] = f3 * 9 * (v[1] * v[1] - 1.5 * T2yy);
+  d[7] = f3 * 9 * (v[2] * v[2] - 1.5 * T2zz);
+  d[8] = f3 * 9 * (2 * v[0] * v[1] - 3 * T2xy);
+  d[9] = f3 * 9 * (2 * v[1] * v[2] - 3 * T2yz);
+  d[10] = f3 * 9 * (2 * v[2] * v[0] - 3 * T2zx);
+}
+
+static int is_tensor(int kind) { return kind == ORACLE_HS_WBT || kind == ORACLE_HS_TZ; }
+
 static double nQ_of(double kT) {
   /* find_nQ, src/IdealGas.cpp:54-59: (m kT / 2 pi)^(3/2), m = water mass */
   const double x = 18.01528 * 1822.8885 * kT / (2 * M_PI);
@@ -323,19 +408,27 @@ static double eval(const oracle_params *p, const double *n, const double *V, con
   const double kT = p->kT, dV = ks.dV;
   double t[ORACLE_NTERMS] = {0, 0, 0, 0, 0, 0};
   double *wd = NULL, *part = NULL;
+  const int nw = is_tensor(p->hs) ? 11 : 5; /* weighted densities */
   if (p->terms & ORACLE_HS) {
-    wd = (double *)malloc(sizeof(double) * 5 * nr);
+    wd = (double *)malloc(sizeof(double) * nw * nr);
     weighted(p, &ks, n, wd);
-    if (grad) part = (double *)malloc(sizeof(double) * 5 * nr);
+    if (nw == 11) tensor_weighted(p, &ks, n, wd + 5 * nr);
+    if (grad) part = (double *)malloc(sizeof(double) * nw * nr);
     for (size_t i = 0; i < nr; i++) {
-      double phi[3], d[5];
-      phi_hs(p->hs, p->R, wd[i], wd[nr + i], wd[2 * nr + i], wd[3 * nr + i], wd[4 * nr + i], phi,
-             d);
+      double phi[3], d[11];
+      if (nw == 11) {
+        double w[11];
+        for (int a = 0; a < 11; a++) w[a] = wd[a * nr + i];
+        phi_tensor(p->hs, p->R, w, phi, d);
+      } else {
+        phi_hs(p->hs, p->R, wd[i], wd[nr + i], wd[2 * nr + i], wd[3 * nr + i], wd[4 * nr + i],
+               phi, d);
+      }
       t[0] += kT * phi[0];
       t[1] += kT * phi[1];
       t[2] += kT * phi[2];
       if (part)
-        for (int a = 0; a < 5; a++) part[a * nr + i] = dV * kT * d[a];
+        for (int a = 0; a < nw; a++) part[a * nr + i] = dV * kT * d[a];
     }
   }
   const double nQ = nQ_of(kT);
@@ -355,11 +448,17 @@ static double eval(const oracle_params *p, const double *n, const double *V, con
     if (part) {
       double *pk = (double *)malloc(sizeof(double) * 2 * nc);
       double *gk = (double *)calloc(2 * nc, sizeof(double));
-      for (int a = 0; a < 5; a++) {
+      for (int a = 0; a < nw; a++) {
         r2c(p, part + a * nr, pk);
         for (size_t i = 0; i < nc; i++) {
           const double re = pk[2 * i] * ks.scale, im = pk[2 * i + 1] * ks.scale;
-          if (a < 2) {
+          if (a >= 5) {
+            /* tensor weights: real and even, their own adjoints */
+            double tw[6];
+            tensor_weights(ks.kv + 3 * i, p->R, ks.dr, tw);
+            gk[2 * i] += re * tw[a - 5];
+            gk[2 * i + 1] += im * tw[a - 5];
+          } else if (a < 2) {
             const double w = a == 0 ? ks.w3[i] : ks.w2[i];
             gk[2 * i] += re * w;
             gk[2 * i + 1] += im * w;

@@ -32,6 +32,8 @@ enum {
   ORACLE_HS_WB = 0, /* HardSpheresWBnotensor, src/HardSpheres.cpp:137-159 */
   ORACLE_HS_RF = 1, /* HardSpheresRF (Rosenfeld), src/HardSpheres.cpp:69-88 */
   ORACLE_HS_M2 = 2, /* White Bear mark II, src/haskell/WhiteBear.hs:140-159 */
+  ORACLE_HS_WBT = 3, /* HardSpheresWB (tensor third term), src/HardSpheres.cpp:30-61,113-135 */
+  ORACLE_HS_TZ = 4,  /* HardSpheresTarazona, src/HardSpheres.cpp:90-111 */
 };
 
 typedef struct {

@@ -21,7 +21,7 @@ ORACLE_SO = os.path.join(HERE, "liboracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libdeft_ref.so")
 
 HS, IDEAL, MU, VEXT, MASK, VEFF = 1, 2, 4, 8, 16, 32
-HS_WB, HS_RF, HS_M2 = 0, 1, 2  # hard-sphere functional kinds (oracle_params.hs)
+HS_WB, HS_RF, HS_M2, HS_WBT, HS_TZ = 0, 1, 2, 3, 4  # hard-sphere kinds (oracle_params.hs)
 # contact fields (oracle_contact)
 CONTACT_GSIGMA_S, CONTACT_GSIGMA_A, CONTACT_GROSS, CONTACT_YUWU, CONTACT_YUWU_S = 0, 1, 2, 3, 4
 NTERMS = 6

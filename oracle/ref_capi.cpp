@@ -64,15 +64,19 @@ static Functional mark_ii(double radius) {
   return (kT() * phi3) + (kT() * phi1) + (kT() * phi2);
 }
 
-// Hard-sphere functional of the composed sums: 0 HardSpheresWBnotensor,
-// 1 HardSpheresRF, 2 mark II (above), 3 HardSpheresWBm2slow as compiled.
+// Hard-sphere functional of the composed sums (the oracle's numbering):
+// 0 HardSpheresWBnotensor, 1 HardSpheresRF, 2 mark II (above),
+// 3 HardSpheresWB (tensor), 4 HardSpheresTarazona, 5 HardSpheresWBm2slow as
+// compiled.
 static int g_hs_kind = 0;
 
 static Functional hard_spheres(double R) {
   switch (g_hs_kind) {
     case 1: return HardSpheresRF(R);
     case 2: return mark_ii(R);
-    case 3: return HardSpheresWBm2slow(R);
+    case 3: return HardSpheresWB(R);  // tensor third term
+    case 4: return HardSpheresTarazona(R);
+    case 5: return HardSpheresWBm2slow(R);
     default: return HardSpheresWBnotensor(R);
   }
 }

@@ -6,9 +6,11 @@ import numpy as np
 from oracle import oracle as O
 
 CASES = ("cubic12", "ortho_odd", "fcc12")
-# (case, hard-sphere functional) pairs of the Rosenfeld and mark II fixtures
+# (case, hard-sphere functional) pairs of the Rosenfeld, mark II, tensor
+# White Bear and Tarazona fixtures
 HS_CASES = (("cubic12", O.HS_RF), ("ortho_odd", O.HS_RF), ("cubic12", O.HS_M2),
-            ("ortho_odd", O.HS_M2))
+            ("ortho_odd", O.HS_M2), ("cubic12", O.HS_WBT), ("ortho_odd", O.HS_WBT),
+            ("fcc12", O.HS_WBT), ("cubic12", O.HS_TZ), ("fcc12", O.HS_TZ))
 
 
 def make_case(name, hs=O.HS_WB):

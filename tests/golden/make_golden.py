@@ -33,8 +33,9 @@ def main():
         out[name] = {"E": E, "terms": [float(x) for x in t]}
         arrays[f"{name}_grad"] = g
         arrays[f"{name}_weighted"] = w
-    # the Rosenfeld functional (HardSpheresRF) and White Bear mark II (the
-    # WhiteBear.hs definition through the reference's Functional algebra)
+    # the Rosenfeld functional (HardSpheresRF), White Bear mark II (the
+    # WhiteBear.hs definition through the reference's Functional algebra),
+    # the tensor White Bear (HardSpheresWB) and Tarazona functionals
     for name, hs in HS_CASES:
         P, n = make_case(name, hs)
         E, g, t = P.ref_energy_grad(n)

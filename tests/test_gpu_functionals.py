@@ -1,6 +1,6 @@
-"""GPU tests of the Rosenfeld (HardSpheresRF) and White Bear mark II
-functionals: FP64 energies and gradients against the reference's outputs
-(tests/golden/) and the oracle, the mixed form within its FP32 tolerances
+"""GPU tests of the Rosenfeld (HardSpheresRF), White Bear mark II, tensor
+White Bear (HardSpheresWB) and Tarazona functionals: FP64 energies and
+gradients against the reference's outputs (tests/golden/) and the oracle, the mixed form within its FP32 tolerances
 (energy 2e-6, gradient 2e-5 relative), the Hessian-vector product of the
 Newton refinement against a difference of FP64 gradients, and a converged
 mixed solve at the oracle's profile.  Stated FP64 tolerances: energy 1e-10,
@@ -138,8 +138,66 @@ def test_mixed_solve_reaches_fp64_tolerance_at_oracle_profile(ctx, oracle_mod, h
 def test_unknown_functional_is_refused(ctx):
     from tests.capi import Grid
     g = Grid(ctx, np.diag([2.4, 2.4, 2.4]), (12, 12, 12))
-    p = _lib.FmtParams(1.0, 1.0, 0.0, 7, 0, 7)
+    p = _lib.FmtParams(1.0, 1.0, 0.0, 7, 0, 9)
     import ctypes
+    h = ctypes.c_void_p()
+    assert g.L.deft_fmt_create(g.h, ctypes.byref(p), ctypes.byref(h)) == _lib.ERR_ARG
+    g.close()
+
+
+@pytest.mark.parametrize("name,hs", [("cubic12", 3), ("ortho_odd", 3), ("fcc12", 3),
+                                     ("cubic12", 4), ("fcc12", 4)])
+def test_tensor_fp64_matches_reference_golden(ctx, oracle_mod, golden, name, hs):
+    from tests.capi import Fmt, Grid
+    from tests.golden.cases import make_case
+    vals, arrs = golden
+    P, n = make_case(name, hs)
+    g = Grid(ctx, P.lat.reshape(3, 3), P.N)
+    f = Fmt(g, R=P.R, kT=P.kT, mu=P.mu, terms=P.terms, V=P.V, mask=P.mask, functional=hs)
+    E, grad, terms = f.energy_grad(n)
+    ref = vals[f"{name}_hs{hs}"]
+    assert abs(E / ref["E"] - 1) < 1e-10
+    tr = np.array(ref["terms"])
+    assert np.abs(terms[:len(tr)] - tr).max() <= 1e-10 * np.abs(tr).max()
+    gr = arrs[f"{name}_hs{hs}_grad"]
+    assert np.abs(grad - gr).max() <= 1e-9 * np.abs(gr).max()
+    E2, _ = f.energy(n)
+    assert abs(E2 / E - 1) < 1e-14
+    f.close()
+    g.close()
+
+
+@pytest.mark.parametrize("hs", [_lib.HS_WB_TENSOR, _lib.HS_TARAZONA])
+def test_tensor_secant_solve_matches_oracle_profile(ctx, oracle_mod, hs):
+    """FP64 CG with the tensor functional on the slit, to |grad| < 1e-10:
+    the profile equals the oracle's 1-D solve of the same functional."""
+    from tests.capi import CG, Fmt, Grid
+    O = oracle_mod
+    s = _slit()
+    mask = s.mask.reshape(-1)
+    terms = O.HS | O.IDEAL | O.MU | O.MASK
+    g = Grid(ctx, s.lat, s.shape)
+    f = Fmt(g, mu=s.mu, terms=terms, mask=mask, functional=hs)
+    cg = CG(f, gtol=1e-10, maxiter=5000, step=1.0, preconditioned=_lib.PC_DENSITY)
+    cg.set_x(s.n0.reshape(-1))
+    code, st = cg.solve()
+    assert code == 0 and st.converged
+    n = cg.get_x()
+    P1 = O.Problem(np.diag([s.dx, s.dx, s.L]), (1, 1, s.shape[2]), mu=s.mu,
+                   terms=O.HS | O.IDEAL | O.MU, mask=s.mask[0, 0].copy(), hs=hs)
+    x1, info = P1.cg_solve(np.where(s.mask[0, 0] > 0, s.nb, 0.0), gtol=1e-13, maxiter=20000)
+    assert info["gnorm"] < 1e-13
+    assert np.abs(n.reshape(s.shape) - x1[None, None, :]).max() < 1e-8
+    cg.close()
+    f.close()
+    g.close()
+
+
+def test_tensor_functionals_refuse_the_mixed_form(ctx):
+    import ctypes
+    from tests.capi import Grid
+    g = Grid(ctx, np.diag([2.4, 2.4, 2.4]), (12, 12, 12))
+    p = _lib.FmtParams(1.0, 1.0, 0.0, 7, _lib.PRECISION_MIXED, _lib.HS_WB_TENSOR)
     h = ctypes.c_void_p()
     assert g.L.deft_fmt_create(g.h, ctypes.byref(p), ctypes.byref(h)) == _lib.ERR_ARG
     g.close()

@@ -62,10 +62,12 @@ def test_oracle_matches_reference_golden(oracle_mod, golden, name):
 
 
 @pytest.mark.parametrize("name,hs", [("cubic12", 1), ("ortho_odd", 1), ("cubic12", 2),
-                                     ("ortho_odd", 2)])
-def test_oracle_rosenfeld_and_mark2_match_reference_golden(oracle_mod, golden, name, hs):
-    """HardSpheresRF as compiled, and White Bear mark II as WhiteBear.hs
-    defines it, evaluated by the reference's Functional machinery."""
+                                     ("ortho_odd", 2), ("cubic12", 3), ("ortho_odd", 3),
+                                     ("fcc12", 3), ("cubic12", 4), ("fcc12", 4)])
+def test_oracle_rosenfeld_mark2_tensor_match_reference_golden(oracle_mod, golden, name, hs):
+    """HardSpheresRF, HardSpheresWB (tensor) and HardSpheresTarazona as
+    compiled, and White Bear mark II as WhiteBear.hs defines it, evaluated
+    by the reference's Functional machinery."""
     from tests.golden.cases import make_case
     vals, arrs = golden
     P, n = make_case(name, hs)
@@ -78,17 +80,18 @@ def test_oracle_rosenfeld_and_mark2_match_reference_golden(oracle_mod, golden, n
     assert np.abs(g - gr).max() <= 1e-12 * np.abs(gr).max()
 
 
-@pytest.mark.parametrize("hs", [0, 1, 2])
+@pytest.mark.parametrize("hs", [0, 1, 2, 3, 4])
 def test_oracle_bulk_equations_of_state(oracle_mod, hs):
-    """Uniform density: White Bear and mark II give the Carnahan-Starling
-    excess free energy eta (4 - 3 eta) / (1 - eta)^2 per particle, Rosenfeld
-    the Percus-Yevick (compressibility) one -ln(1-eta) + 3 eta (2 - eta) / (2 (1-eta)^2)."""
+    """Uniform density: White Bear (vector or tensor) and mark II give the
+    Carnahan-Starling excess free energy eta (4 - 3 eta) / (1 - eta)^2 per
+    particle, Rosenfeld and Tarazona the Percus-Yevick (compressibility) one
+    -ln(1-eta) + 3 eta (2 - eta) / (2 (1-eta)^2)."""
     O = oracle_mod
     for eta in (0.05, 0.2, 0.4):
         nu = eta / (4 * math.pi / 3)
         P = O.Problem(np.diag([3.2] * 3), (16, 16, 16), terms=O.HS, hs=hs)
         E = P.energy(np.full(16 ** 3, nu))
-        if hs == O.HS_RF:
+        if hs in (O.HS_RF, O.HS_TZ):
             fex = -math.log(1 - eta) + 3 * eta * (2 - eta) / (2 * (1 - eta) ** 2)
         else:
             fex = eta * (4 - 3 * eta) / (1 - eta) ** 2
@@ -119,7 +122,7 @@ def test_mark2_vs_compiled_wbm2slow(oracle_mod):
     P, n = make_case("cubic12", 2)
     P.terms = oracle_mod.HS
     _, t = P.energy(n, terms=True)
-    P.hs = 3  # the reference bindings' HardSpheresWBm2slow
+    P.hs = 5  # the reference bindings' HardSpheresWBm2slow
     _, _, tr = P.ref_energy_grad(n, grad=False)
     assert abs(tr[0] / t[0] - 2 / 3) < 1e-12
     assert abs(tr[1] / t[1] - 1) < 1e-12 and abs(tr[2] / t[2] - 1) < 1e-12
