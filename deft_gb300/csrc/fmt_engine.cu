@@ -851,9 +851,14 @@ __global__ void __launch_bounds__(kThreads) k_local_energy(const double *__restr
 }
 
 // Sums per-block energy partials in a fixed order: out[t] = dV sum, out[6] = E.
-__global__ void k_reduce_terms(const double *partials, int nblk, double dV, double *out) {
+// One block of kReduceThreads: the per-block partials of an evaluation (a
+// few thousand rows) are read with many loads in flight.
+constexpr int kReduceThreads = 1024;
+__global__ void __launch_bounds__(kReduceThreads) k_reduce_terms(const double *partials, int nblk,
+                                                                 double dV, double *out) {
   __shared__ double red[32 * kNumTerms];
   double acc[kNumTerms] = {0, 0, 0, 0, 0, 0};
+  #pragma unroll 4
   for (int b = threadIdx.x; b < nblk; b += blockDim.x)
     for (int t = 0; t < kNumTerms; t++) acc[t] += partials[(size_t)b * kNumTerms + t];
   block_reduce<kNumTerms>(acc, red);
@@ -1777,7 +1782,7 @@ class EngineImpl {
   // the results to the pinned host block.
   void queue_energy(int nblk) {
     pre(kK_reduce_terms);
-    k_reduce_terms<<<1, kThreads, 0, stream>>>(partials, nblk, g.dV, results);
+    k_reduce_terms<<<1, kReduceThreads, 0, stream>>>(partials, nblk, g.dV, results);
     post(kK_reduce_terms);
     cudaMemcpyAsync(results_host, results, sizeof(double) * 8, cudaMemcpyDeviceToHost, stream);
   }
@@ -2400,7 +2405,7 @@ int noalloc_energy_grad(const GridSpec &s, const FmtSpec &f, const double *n, co
   }
   k_z_grad<double><<<ptiles_z, kThreads, t.smem_z, stream>>>(S0, n, V, mask, grad, g, pz, t.fPz,
                                                              la_dev);
-  k_reduce_terms<<<1, kThreads, 0, stream>>>(partials, nblk, g.dV, results);
+  k_reduce_terms<<<1, kReduceThreads, 0, stream>>>(partials, nblk, g.dV, results);
   double res[8];
   e = cudaGetLastError();
   if (e == cudaSuccess)
