@@ -443,6 +443,11 @@ static double eval(const oracle_params *p, const double *n, const double *V, con
     E += t[a];
   }
   if (terms6) memcpy(terms6, t, sizeof(t));
+  double *gs = NULL; /* SAFT association + dispersion gradient */
+  if (p->saft_on) {
+    if (grad) gs = (double *)malloc(sizeof(double) * nr);
+    E += oracle_saft(p, p->saft, n, gs, NULL);
+  }
   if (grad) {
     memset(grad, 0, sizeof(double) * nr);
     if (part) {
@@ -479,11 +484,12 @@ static double eval(const oracle_params *p, const double *n, const double *V, con
       if (p->terms & ORACLE_IDEAL) loc += kT * log(n[i] / nQ);
       if (p->terms & ORACLE_MU) loc += p->mu;
       if (p->terms & ORACLE_VEXT) loc += V[i];
-      double g = grad[i] + dV * loc;
+      double g = grad[i] + dV * loc + (gs ? gs[i] : 0.0);
       if (p->terms & ORACLE_MASK) g = mask[i] == 0 ? 0.0 : mask[i] * g;
       grad[i] = g;
     }
   }
+  free(gs);
   free(wd);
   free(part);
   kspace_free(&ks);
@@ -692,6 +698,253 @@ void oracle_contact(const oracle_params *p, const double *n, int which, double *
   free(fk);
   free(acc);
   kspace_free(&ks);
+}
+
+/* ---- water SAFT association + dispersion (src/haskell/WaterSaft.hs:35-104) ----
+ * F_disp = int n a1 + int n a2 / kT,
+ *   eta_d = (4 pi R^3 / 3) ifft(exp(-k^2 (2 ls lambda R)^2 / 2) fft n),
+ *   eta_eff = (c1 + c2 eta_d + c3 eta_d^2) eta_d (Gil-Villegas 1997 eq. 36),
+ *   a1 = -4 (lambda^3 - 1) eps_d eta_d g(eta_eff), g(x) = (1 - x/2) / (1 - x)^3,
+ *   a2 = K_HS eps_d eta_d (d a1 / d eta_d) / 2, K_HS = (1 - eta_d)^4 / (1 + 4 (eta_d + eta_d^2));
+ * F_assoc = int 4 kT n (ln X - X/2 + 1/2), X = (sqrt(1 + 8 nA D) - 1) / (4 nA D),
+ *   nA = shell_2R(n) / (4 pi (2R)^2), D = gSW kappa_a (exp(eps_a / kT) - 1),
+ *   gSW = gSigmaA + (d a1/d eta_d - lambda / (3 eta_d) d a1/d lambda) / (4 kT).
+ * The gradient is the exact chain rule through every convolution: the
+ * adjoint of gSigmaA's eight convolutions times the Jacobian of its source
+ * fields in the weighted densities (second derivatives of phi), then the
+ * adjoint weighted-density convolutions. */
+
+/* S'' as well (phi3_S gives S, S'). */
+static double phi3_S2(double eta) {
+  if (fabs(eta) < 1e-2) {
+    double d2 = 0, pw = 1; /* eta^(j-2) from j = 2 */
+    for (int j = 2; j <= 14; j++) {
+      d2 -= 2.0 / ((double)j * (j + 1) * (j + 2)) * j * (j - 1) * pw;
+      pw *= eta;
+    }
+    return d2;
+  }
+  const double l = log(1 - eta), om = 1 - eta;
+  const double g = eta + om * om * l, dg = eta - 2 * om * l, d2g = 3 + 2 * l;
+  const double ie = 1 / eta;
+  return (d2g - 4 * dg * ie + 6 * g * ie * ie) * ie * ie;
+}
+
+/* White Bear f2, f3 and their first two derivatives. */
+static void wb_f(double e, double f2[3], double f3[3]) {
+  const double u = 1 / (1 - e), k36 = 1 / (36 * M_PI);
+  double S, dS;
+  phi3_S(e, &S, &dS);
+  const double d2S = phi3_S2(e);
+  f2[0] = u;
+  f2[1] = u * u;
+  f2[2] = 2 * u * u * u;
+  f3[0] = S * u * u * k36;
+  f3[1] = (dS + 2 * S * u) * u * u * k36;
+  f3[2] = (d2S + 4 * dS * u + 6 * S * u * u) * u * u * k36;
+}
+
+/* a1 and its derivatives in eta and lambda (eps = eps_d). */
+static void saft_a1(double eta, double lam, double eps, double o[5]) {
+  const double c[3] = {2.25855 - 1.50349 * lam + 0.249434 * lam * lam,
+                       -0.669270 + 1.40049 * lam - 0.827739 * lam * lam,
+                       10.1576 - 15.0427 * lam + 5.30827 * lam * lam};
+  const double cl[3] = {-1.50349 + 2 * 0.249434 * lam, 1.40049 - 2 * 0.827739 * lam,
+                        -15.0427 + 2 * 5.30827 * lam};
+  const double x = (c[0] + c[1] * eta + c[2] * eta * eta) * eta;
+  const double xe = c[0] + 2 * c[1] * eta + 3 * c[2] * eta * eta, xee = 2 * c[1] + 6 * c[2] * eta;
+  const double xl = (cl[0] + cl[1] * eta + cl[2] * eta * eta) * eta;
+  const double xel = cl[0] + 2 * cl[1] * eta + 3 * cl[2] * eta * eta;
+  const double om = 1 - x;
+  const double g = (1 - x / 2) / (om * om * om), g1 = (2.5 - x) / (om * om * om * om),
+               g2 = (9 - 3 * x) / (om * om * om * om * om);
+  const double L3 = lam * lam * lam - 1, pre = -4 * eps;
+  o[0] = pre * L3 * eta * g;                                              /* a1 */
+  o[1] = pre * L3 * (g + eta * g1 * xe);                                  /* a1_eta */
+  o[2] = pre * eta * (3 * lam * lam * g + L3 * g1 * xl);                  /* a1_lambda */
+  o[3] = pre * L3 * (2 * g1 * xe + eta * (g2 * xe * xe + g1 * xee));      /* a1_eta_eta */
+  o[4] = pre * (3 * lam * lam * (g + eta * g1 * xe) +
+                L3 * (g1 * xl + eta * (g2 * xl * xe + g1 * xel)));        /* a1_eta_lambda */
+}
+
+/* out = W_b^(adj) conv of src (b as contact_weight; adjoint negates the odd
+ * ones), accumulated into the spectrum acc. */
+static void saft_conv_acc(const oracle_params *p, const kspace *ks, double R, int kind_w,
+                          int adjoint, const double *src, double *fk, double *acc, int first,
+                          double gauss_s) {
+  r2c(p, src, fk);
+  for (size_t i = 0; i < ks->nc; i++) {
+    const double *k = ks->kv + 3 * i;
+    double wr = 0, wi = 0;
+    if (kind_w < 10) {
+      contact_weight(kind_w, k, R, ks->dr, &wr, &wi);
+    } else if (kind_w == 10) { /* Gaussian of eta_d (no smear) */
+      const double k2 = k[0] * k[0] + k[1] * k[1] + k[2] * k[2];
+      wr = exp(-0.5 * k2 * gauss_s * gauss_s);
+    } else { /* 11 step, 12 shell, 13-15 vector shell: the weighted densities */
+      if (kind_w == 11) wr = ks->w3[i];
+      else if (kind_w == 12) wr = ks->w2[i];
+      else wi = k[kind_w - 13] * ks->wv[i];
+    }
+    if (adjoint) wi = -wi;
+    const double re = fk[2 * i] * ks->scale, im = fk[2 * i + 1] * ks->scale;
+    const double tr = wr * re - wi * im, ti = wr * im + wi * re;
+    if (first) {
+      acc[2 * i] = tr;
+      acc[2 * i + 1] = ti;
+    } else {
+      acc[2 * i] += tr;
+      acc[2 * i + 1] += ti;
+    }
+  }
+}
+
+double oracle_saft(const oracle_params *p, const double saft[5], const double *n, double *grad,
+                   double out2[2]) {
+  const double eps_a = saft[0], kap_a = saft[1], eps_d = saft[2], lam = saft[3], ls = saft[4];
+  const double R = p->R, kT = p->kT;
+  kspace ks;
+  kspace_init(p, &ks);
+  const size_t nr = ks.nr, nc = ks.nc;
+  const double dV = ks.dV, c1 = 1 / (4 * M_PI * R), c0 = c1 / R;
+  const double gauss_s = 2 * ls * lam * R, Kf = kap_a * (exp(eps_a / kT) - 1);
+  double *w = (double *)malloc(sizeof(double) * 5 * nr);
+  double *A = (double *)malloc(sizeof(double) * nr), *D2 = (double *)malloc(sizeof(double) * nr);
+  double *Eg = (double *)malloc(sizeof(double) * nr), *src = (double *)malloc(sizeof(double) * nr);
+  double *fk = (double *)malloc(sizeof(double) * 2 * nc), *acc = (double *)malloc(sizeof(double) * 2 * nc);
+  weighted(p, &ks, n, w);
+  /* A = dAdR_A_over_n: sum over the eight source fields (as oracle_contact) */
+  for (int a = 0; a < 8; a++) {
+    for (size_t i = 0; i < nr; i++) {
+      const double v[3] = {w[2 * nr + i], w[3 * nr + i], w[4 * nr + i]};
+      double d[6];
+      contact_partials(ORACLE_HS_WB, R, w[i], w[nr + i], v[0] * v[0] + v[1] * v[1] + v[2] * v[2], d);
+      if (a == 0) src[i] = d[3] - 2 * c0 / R * d[0] - c0 * d[1];
+      else if (a == 1) src[i] = d[2] + c1 * d[1] + c0 * d[0];
+      else if (a < 5) src[i] = v[a - 2] * c0 * d[4];
+      else src[i] = v[a - 5] * (c1 * d[4] + d[5]);
+    }
+    saft_conv_acc(p, &ks, R, a, 0, src, fk, acc, a == 0, 0);
+  }
+  c2r(p, acc, A);
+  saft_conv_acc(p, &ks, R, 8, 0, n, fk, acc, 1, 0); /* shell_2R */
+  c2r(p, acc, D2);
+  saft_conv_acc(p, &ks, R, 10, 0, n, fk, acc, 1, gauss_s);
+  c2r(p, acc, Eg);
+  double Fa = 0, Fd = 0;
+  double *lA = NULL, *lD = NULL, *lE = NULL, *expl = NULL;
+  if (grad) {
+    lA = (double *)malloc(sizeof(double) * nr);
+    lD = (double *)malloc(sizeof(double) * nr);
+    lE = (double *)malloc(sizeof(double) * nr);
+    expl = (double *)malloc(sizeof(double) * nr);
+  }
+  const double v43 = 4 * M_PI * R * R * R / 3;
+  for (size_t i = 0; i < nr; i++) {
+    const double ni = n[i], eta = v43 * Eg[i];
+    double a1[5];
+    saft_a1(eta, lam, eps_d, a1);
+    const double om = 1 - eta, q = 1 + 2 * eta;
+    const double KHS = om * om * om * om / (q * q);
+    const double KHS1 = -4 * om * om * om * (2 + eta) / (q * q * q);
+    const double a2 = 0.5 * eps_d * KHS * eta * a1[1];
+    const double gsig = A[i] / D2[i], nA = D2[i] / (16 * M_PI * R * R);
+    const double gSW = gsig + (a1[1] - lam / (3 * eta) * a1[2]) / (4 * kT);
+    const double Dl = gSW * Kf, y = nA * Dl;
+    const double X = (sqrt(1 + 8 * y) - 1) / (4 * y);
+    Fa += 4 * kT * ni * (log(X) - X / 2 + 0.5);
+    Fd += ni * a1[0] + ni * a2 / kT;
+    if (grad) {
+      const double lX = 4 * kT * ni * (1 / X - 0.5);
+      const double ly = lX * (-2 * X * X / (1 + 4 * y * X));
+      const double lnA = ly * Dl, lgSW = ly * nA * Kf;
+      lA[i] = lgSW / D2[i];
+      lD[i] = -lgSW * A[i] / (D2[i] * D2[i]) + lnA / (16 * M_PI * R * R);
+      double leta = lgSW / (4 * kT) *
+                    (a1[3] - lam * (a1[4] / (3 * eta) - a1[2] / (3 * eta * eta)));
+      leta += ni * a1[1] + ni / kT * 0.5 * eps_d * (KHS1 * eta * a1[1] + KHS * a1[1] + KHS * eta * a1[3]);
+      lE[i] = v43 * leta;
+      expl[i] = 4 * kT * (log(X) - X / 2 + 0.5) + a1[0] + a2 / kT;
+    }
+  }
+  if (out2) {
+    out2[0] = Fa * dV;
+    out2[1] = Fd * dV;
+  }
+  if (grad) {
+    /* lambda of the weighted densities: sum_a (W_a^adj lA) dS_a/dw_b */
+    double *lw = (double *)calloc(5 * nr, sizeof(double));
+    double *t = (double *)malloc(sizeof(double) * nr);
+    for (int a = 0; a < 8; a++) {
+      saft_conv_acc(p, &ks, R, a, 1, lA, fk, acc, 1, 0);
+      c2r(p, acc, t);
+      for (size_t i = 0; i < nr; i++) {
+        const double n3 = w[i], n2 = w[nr + i];
+        const double v[3] = {w[2 * nr + i], w[3 * nr + i], w[4 * nr + i]};
+        const double v2 = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+        double f2[3], f3[3];
+        wb_f(n3, f2, f3);
+        const double u = 1 / (1 - n3), q = n2 * n2 - v2, t3 = n2 * (n2 * n2 - 3 * v2);
+        /* d's and their derivatives in (n3, n2, v2) */
+        const double d1v = -f2[0], d2v = -c1 * f2[0] - 6 * n2 * f3[0];
+        const double D0[3] = {u, 0, 0};
+        const double D1[3] = {n2 * f2[1], f2[0], 0};
+        const double D2d[3] = {c1 * n2 * f2[1] + 3 * q * f3[1], c1 * f2[0] + 6 * n2 * f3[0], -3 * f3[0]};
+        const double D3[3] = {c0 * n2 * u * u + c1 * q * f2[2] + t3 * f3[2],
+                              c0 * u + 2 * c1 * n2 * f2[1] + (3 * n2 * n2 - 3 * v2) * f3[1],
+                              -c1 * f2[1] - 3 * n2 * f3[1]};
+        const double D1v[3] = {-f2[1], 0, 0};
+        const double D2v[3] = {-c1 * f2[1] - 6 * n2 * f3[1], -6 * f3[0], 0};
+        double J[5]; /* dS_a / d(n3, n2, vx, vy, vz) */
+        if (a < 2) {
+          double g3[3];
+          for (int m = 0; m < 3; m++)
+            g3[m] = a == 0 ? D3[m] - 2 * c0 / R * D0[m] - c0 * D1[m] : D2d[m] + c1 * D1[m] + c0 * D0[m];
+          J[0] = g3[0];
+          J[1] = g3[1];
+          for (int e = 0; e < 3; e++) J[2 + e] = 2 * v[e] * g3[2];
+        } else if (a < 5) {
+          const int cc = a - 2;
+          J[0] = v[cc] * c0 * D1v[0];
+          J[1] = 0;
+          for (int e = 0; e < 3; e++) J[2 + e] = e == cc ? c0 * d1v : 0;
+        } else {
+          const int cc = a - 5;
+          J[0] = v[cc] * (c1 * D1v[0] + D2v[0]);
+          J[1] = v[cc] * D2v[1];
+          for (int e = 0; e < 3; e++) J[2 + e] = e == cc ? c1 * d1v + d2v : 0;
+        }
+        for (int b = 0; b < 5; b++) lw[b * nr + i] += t[i] * J[b];
+      }
+    }
+    /* gradient spectrum: weighted-density adjoints + shell_2R + Gaussian */
+    for (int b = 0; b < 5; b++) saft_conv_acc(p, &ks, R, 11 + b, 1, lw + b * nr, fk, acc, b == 0, 0);
+    {
+      double *acc2 = (double *)malloc(sizeof(double) * 2 * nc);
+      saft_conv_acc(p, &ks, R, 8, 1, lD, fk, acc2, 1, 0);
+      for (size_t i = 0; i < 2 * nc; i++) acc[i] += acc2[i];
+      saft_conv_acc(p, &ks, R, 10, 1, lE, fk, acc2, 1, gauss_s);
+      for (size_t i = 0; i < 2 * nc; i++) acc[i] += acc2[i];
+      free(acc2);
+    }
+    c2r(p, acc, t);
+    for (size_t i = 0; i < nr; i++) grad[i] = dV * (expl[i] + t[i]);
+    free(lw);
+    free(t);
+    free(lA);
+    free(lD);
+    free(lE);
+    free(expl);
+  }
+  free(w);
+  free(A);
+  free(D2);
+  free(Eg);
+  free(src);
+  free(fk);
+  free(acc);
+  kspace_free(&ks);
+  return (Fa + Fd) * dV;
 }
 
 double oracle_homogeneous(double R, double kT, double mu, double nb) {

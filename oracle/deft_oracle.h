@@ -42,6 +42,9 @@ typedef struct {
   double R, kT, mu;
   int terms;
   int hs; /* ORACLE_HS_* */
+  int saft_on;    /* add the water SAFT association + dispersion terms (oracle_saft) */
+  double saft[5]; /* eps_association, kappa_association, eps_dispersion,
+                     lambda_dispersion, length_scaling */
 } oracle_params;
 
 /* Per-term energies, in the reference's sum order: phi3, phi1, phi2 (the
@@ -108,6 +111,15 @@ enum {
   ORACLE_CONTACT_YUWU_S = 4,
 };
 void oracle_contact(const oracle_params *p, const double *n, int which, double *out);
+
+/* Water SAFT association + dispersion terms (src/haskell/WaterSaft.hs:35-104;
+ * the White Bear, ideal-gas and mu parts are those of oracle_energy_grad) at
+ * the density n, for p->R, p->kT and saft = {eps_association,
+ * kappa_association, eps_dispersion, lambda_dispersion, length_scaling}.
+ * Returns their energy (out2 = {F_assoc, F_disp} if non-NULL); if grad is
+ * non-NULL it gets their unmasked gradient (dV included). */
+double oracle_saft(const oracle_params *p, const double saft[5], const double *n, double *grad,
+                   double out2[2]);
 
 /* Number of 3-D real FFTs executed by this oracle so far. */
 long long oracle_fft_count(void);

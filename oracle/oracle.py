@@ -43,6 +43,7 @@ class _Params(ctypes.Structure):
         ("lat", ctypes.c_double * 9),
         ("R", ctypes.c_double), ("kT", ctypes.c_double), ("mu", ctypes.c_double),
         ("terms", ctypes.c_int), ("hs", ctypes.c_int),
+        ("saft_on", ctypes.c_int), ("saft", ctypes.c_double * 5),
     ]
 
 
@@ -91,6 +92,8 @@ def lib():
         L.oracle_pcg_quadratic.argtypes = [P, _dp, _dp, _dp, ctypes.c_int, ctypes.c_double, _dp]
         L.oracle_fft_count.restype = ctypes.c_longlong
         L.oracle_contact.argtypes = [P, _dp, ctypes.c_int, _dp]
+        L.oracle_saft.restype = ctypes.c_double
+        L.oracle_saft.argtypes = [P, _dp, _dp, _dp, _dp]
         L.offt_r2c_3d.argtypes = [ctypes.c_int] * 3 + [_dp, _dp]
         L.offt_c2r_3d.argtypes = [ctypes.c_int] * 3 + [_dp, _dp]
         _lib = L
@@ -132,6 +135,8 @@ def ref():
                               _dp, _dp, ctypes.c_int, ctypes.c_double, _dp]
         L.ref_fft_count.restype = ctypes.c_longlong
         L.ref_set_hs.argtypes = [ctypes.c_int]
+        L.ref_saft.restype = ctypes.c_double
+        L.ref_saft.argtypes = [_dp] + [ctypes.c_int] * 3 + [ctypes.c_double] * 8 + [_dp, _dp, _dp]
         L.ref_contact.argtypes = [_dp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                   ctypes.c_int, _dp, _dp]
         _ref = L
@@ -142,8 +147,10 @@ class Problem:
     """One evaluation setting: lattice (rows a1, a2, a3), grid, R, kT, mu, terms."""
 
     def __init__(self, lat, N, R=1.0, kT=1.0, mu=0.0, terms=HS | IDEAL | MU, V=None, mask=None,
-                 hs=0):
-        self.hs = int(hs)  # HS_WB, HS_RF or HS_M2
+                 hs=0, saft=None):
+        self.hs = int(hs)  # HS_WB, HS_RF, HS_M2, HS_WBT or HS_TZ
+        # water SAFT terms: (eps_a, kappa_a, eps_d, lambda_d, length_scaling) or None
+        self.saft_params = None if saft is None else tuple(float(v) for v in saft)
         self.lat = np.ascontiguousarray(np.asarray(lat, dtype=np.float64).reshape(9))
         self.N = tuple(int(v) for v in N)
         self.R, self.kT, self.mu, self.terms = float(R), float(kT), float(mu), int(terms)
@@ -164,6 +171,10 @@ class Problem:
         for i in range(9):
             p.lat[i] = self.lat[i]
         p.R, p.kT, p.mu, p.terms, p.hs = self.R, self.kT, self.mu, self.terms, self.hs
+        if self.saft_params is not None:
+            p.saft_on = 1
+            for i, v in enumerate(self.saft_params):
+                p.saft[i] = v
         return p
 
     # -- restatement -------------------------------------------------------
@@ -223,6 +234,16 @@ class Problem:
                                       _ptr(out))
         return x, {"iters": it, "energy": out[0], "gnorm": out[1], "evals": int(out[2])}
 
+    def saft(self, n, saft_params, grad=True):
+        """Water SAFT association + dispersion energy and (unmasked) gradient
+        at n; saft_params = (eps_a, kappa_a, eps_d, lambda_d, length_scaling)."""
+        n = np.ascontiguousarray(n, dtype=np.float64).reshape(-1)
+        sp = np.ascontiguousarray(saft_params, dtype=np.float64)
+        g = np.empty(self.size) if grad else None
+        out2 = np.zeros(2)
+        E = lib().oracle_saft(ctypes.byref(self.params()), _ptr(sp), _ptr(n), _ptr(g), _ptr(out2))
+        return E, g, out2
+
     def contact(self, n, which):
         """Contact field `which` (CONTACT_*) at the density n."""
         n = np.ascontiguousarray(n, dtype=np.float64).reshape(-1)
@@ -245,6 +266,15 @@ class Problem:
         nt = self._ref().ref_eval(_ptr(self.lat), *self.N, self.R, self.kT, self.mu, self.terms,
                             _ptr(n), _ptr(self.V), _ptr(self.mask), ctypes.byref(E), _ptr(t), _ptr(g))
         return E.value, g, t[:nt]
+
+    def ref_saft(self, n, saft_params, grad=True):
+        """The reference's WaterSaft (all terms, mu included) energy and
+        integralgrad (constrained by this problem's mask)."""
+        n = np.ascontiguousarray(n, dtype=np.float64).reshape(-1)
+        g = np.empty(self.size) if grad else None
+        E = ref().ref_saft(_ptr(self.lat), *self.N, self.R, *[float(v) for v in saft_params],
+                           self.mu, self.kT, _ptr(n), _ptr(self.mask), _ptr(g))
+        return E, g
 
     def ref_contact(self, n, which):
         n = np.ascontiguousarray(n, dtype=np.float64).reshape(-1)

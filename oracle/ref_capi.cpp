@@ -15,6 +15,7 @@
 // src/Functional.cpp:834-838.
 #include "ContactDensity.h"
 #include "Functionals.h"
+#include "OptimizedFunctionals.h"
 #include "Grid.h"
 #include "LineMinimizer.h"
 #include "Minimizer.h"
@@ -133,6 +134,34 @@ static Functional gsigma_s_hs(double R, bool m2) {
 }
 
 extern "C" {
+
+// The water SAFT functional (src/WaterSaftFast.cpp, generated from
+// src/haskell/WaterSaft.hs): ideal gas + White Bear + association +
+// dispersion + mu N, with the parameters of a LiquidProperties record
+// (src/water-constants.cpp:22-40).  Energy, and if grad != NULL its
+// integralgrad (constrained by mask when given).
+double ref_saft(const double *lat, int Nx, int Ny, int Nz, double R, double eps_a,
+                double kappa_a, double eps_d, double lambda_d, double lscale, double mu,
+                double kT, const double *n, const double *mask, double *grad) {
+  GridDescription gd(make_lat(lat), Nx, Ny, Nz);
+  Grid x(gd);
+  for (int i = 0; i < gd.NxNyNz; i++) x[i] = n[i];
+  Functional f = WaterSaft(R, eps_a, kappa_a, eps_d, lambda_d, lscale, mu);
+  const double E = f.integral(kT, x);
+  if (grad) {
+    Functional fc = f;
+    if (mask) {
+      Grid m(gd);
+      for (int i = 0; i < gd.NxNyNz; i++) m[i] = mask[i];
+      fc = constrain(m, f);
+    }
+    VectorXd g(gd.NxNyNz);
+    g.setZero();
+    fc.integralgrad(kT, gd, x, &g);
+    for (int i = 0; i < gd.NxNyNz; i++) grad[i] = g[i];
+  }
+  return E;
+}
 
 // Contact fields at the density n for the kind set by ref_set_hs (0 White
 // Bear, 2 mark II): 0 gSigmaS (above), 1 gSigmaAcpp / gSigmaAm2cpp,
