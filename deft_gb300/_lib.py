@@ -11,7 +11,7 @@ LIB_PATH = os.path.join(HERE, "libdeft_gb300.so")
 
 OK = 0
 ERR_ARG, ERR_CUDA, ERR_NAN, ERR_LINESEARCH, ERR_MAXITER, ERR_NOMEM = 1, 2, 3, 4, 5, 6
-TERM_HS, TERM_IDEAL, TERM_MU, TERM_VEXT, TERM_MASK, TERM_VEFF = 1, 2, 4, 8, 16, 32
+TERM_HS, TERM_IDEAL, TERM_MU, TERM_VEXT, TERM_MASK, TERM_VEFF, TERM_SAFT = 1, 2, 4, 8, 16, 32, 64
 NTERMS = 6
 LS_SECANT, LS_QUADRATIC_REF = 0, 1
 PC_NONE, PC_FUNCTIONAL, PC_DENSITY = 0, 1, 2
@@ -29,7 +29,7 @@ EXPORTS = (
     "deft_tuning_clear",
     "deft_fmt_create", "deft_fmt_destroy", "deft_fmt_set_params", "deft_fmt_set_vext",
     "deft_fmt_set_mask", "deft_fmt_energy", "deft_fmt_energy_grad", "deft_fmt_energy_grad_pgrad",
-    "deft_fmt_weighted", "deft_fmt_contact",
+    "deft_fmt_weighted", "deft_fmt_contact", "deft_fmt_set_saft",
     "deft_fmt_hessian_vector",
     "deft_find_chemical_potential",
     "deft_fmt_energy_grad_noalloc", "deft_noalloc_scratch_bytes",
@@ -127,6 +127,7 @@ def load():
         "deft_fmt_energy_grad_pgrad": (ctypes.c_int, [_vp, _dp, ctypes.c_int, _dp, _dp, _dp, _dp]),
         "deft_fmt_weighted": (ctypes.c_int, [_vp, _dp, ctypes.c_int, _dp]),
         "deft_fmt_contact": (ctypes.c_int, [_vp, _dp, ctypes.c_int, ctypes.c_int, _dp]),
+        "deft_fmt_set_saft": (ctypes.c_int, [_vp, _dp]),
         "deft_fmt_hessian_vector": (ctypes.c_int, [_vp, _dp, _dp, ctypes.c_int, _dp]),
         "deft_find_chemical_potential": (ctypes.c_int, [ctypes.c_double, ctypes.c_double,
                                                         ctypes.c_double, _dp]),

@@ -23,46 +23,14 @@
 #include <string>
 
 #include "contact.h"
-#include "wb_phi.cuh"
+#include "contact_math.cuh"
 
 namespace deft {
 namespace {
 
 constexpr int kThreads = 256;
-constexpr double kPi = 3.14159265358979323846;
-
-__device__ __forceinline__ int wrap_index(int i, int N) { return i > N / 2 ? i - N : i; }
-
-// k-vector of half-complex entry i (layout x*Ny*NzH + y*NzH + kz).
-__device__ __forceinline__ void k_of(const Geom &g, int i, double k[3]) {
-  int t, z, x, y;
-  fdivmod(i, g.fNzH, t, z);
-  fdivmod(t, g.fNy, x, y);
-  const int m[3] = {wrap_index(x, g.Nx), wrap_index(y, g.Ny), z};
-  for (int c = 0; c < 3; c++) k[c] = g.Bm[3 * c] * m[0] + g.Bm[3 * c + 1] * m[1] + g.Bm[3 * c + 2] * m[2];
-}
-
-// Partial derivatives of phi in the six-variable form: d0..d3 by n0..n3;
-// dPhi/dn1v = d1v n2v and dPhi/dn2v = d2v n2v.
-struct Partials {
-  double d0, d1, d2, d3, d1v, d2v;
-};
-
-__device__ Partials partials(int kind, double R, double n3, double n2, double v2) {
-  const double u = 1.0 / (1.0 - n3), l = log(1.0 - n3);
-  double f2[3], f3[3];
-  hs_coeffs<double>(kind, n3, u, l, f2, f3);
-  const double c1 = 1.0 / (4 * kPi * R), c0 = c1 / R;
-  const double q = n2 * n2 - v2, t3 = n2 * (n2 * n2 - 3 * v2);
-  Partials p;
-  p.d0 = -l;
-  p.d1 = n2 * f2[0];
-  p.d2 = c1 * n2 * f2[0] + 3 * q * f3[0];
-  p.d3 = c0 * n2 * u + c1 * q * f2[1] + t3 * f3[1];
-  p.d1v = -f2[0];
-  p.d2v = -c1 * f2[0] - 6 * n2 * f3[0];
-  return p;
-}
+using cm::kPi;
+using cm::Partials;
 
 // gSigmaS, YuWu, YuWu_S at each point from the weighted densities.
 __global__ void k_contact_point(int which, int kind, double R, const double *__restrict__ w,
@@ -73,7 +41,7 @@ __global__ void k_contact_point(int which, int kind, double R, const double *__r
     const double v2 = vx * vx + vy * vy + vz * vz;
     if (which == DEFT_CONTACT_GSIGMA_S) {
       // WhiteBear.hs:86-96: dA/dR with n2' = -2 n2 / R, n2v' = -2 n2v / R
-      const Partials p = partials(kind, R, n3, n2, v2);
+      const Partials p = cm::partials(kind, R, n3, n2, v2);
       const double c1 = 1.0 / (4 * kPi * R), c0 = c1 / R, n0 = c0 * n2;
       const double n2p = -2 * n2 / R;
       const double dAdR = p.d3 * n2 - p.d2 * n2p - p.d1 * (c1 * n2p + n0) -
@@ -91,83 +59,14 @@ __global__ void k_contact_point(int which, int kind, double R, const double *__r
   }
 }
 
-// Source field a of gSigmaA's numerator (src/ContactDensity.cpp:219-232):
-// 0 shell(.)      d3 - 2 d0/(4 pi R^3) - d1/(4 pi R^2)
-// 1 shellPrime(.) d2 + d1/(4 pi R) + d0/(4 pi R^2)        (subtracted)
-// 2-4 vshell_c(.) n2v_c d1v / (4 pi R^2)
-// 5-7 vshellPrime_c(.) n2v_c (d1v/(4 pi R) + d2v)
+// Source field a of gSigmaA's numerator (cm::gsa_source).
 __global__ void k_contact_source(int a, int kind, double R, const double *__restrict__ w, int NR,
                                  double *__restrict__ src) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < NR; i += gridDim.x * blockDim.x) {
     const double n3 = w[i], n2 = w[NR + i];
     const double v[3] = {w[2 * NR + i], w[3 * NR + i], w[4 * NR + i]};
-    const double v2 = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
-    const Partials p = partials(kind, R, n3, n2, v2);
-    const double c1 = 1.0 / (4 * kPi * R), c0 = c1 / R;
-    double s;
-    if (a == 0) s = p.d3 - 2 * c0 / R * p.d0 - c0 * p.d1;
-    else if (a == 1) s = p.d2 + c1 * p.d1 + c0 * p.d0;
-    else if (a < 5) s = v[a - 2] * c0 * p.d1v;
-    else s = v[a - 5] * (c1 * p.d1v + p.d2v);
-    src[i] = s;
-  }
-}
-
-// Weight `a` at k (src/ReciprocalOperators.h:94-291), as acc += W F
-// (W real, or i times real for the odd vector weights):
-// 0 shell(R), 1 -shellPrime(R), 2-4 x/y/zshell(R), 5-7 x/y/zshellprime(R),
-// 8 shell(2R), 9 step(2R).
-__global__ void k_contact_accum(int a, Geom g, double R, const double2 *__restrict__ F,
-                                double2 *__restrict__ acc, int first) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < g.NC; i += gridDim.x * blockDim.x) {
-    double kv[3];
-    k_of(g, i, kv);
-    const double k2 = kv[0] * kv[0] + kv[1] * kv[1] + kv[2] * kv[2];
-    const double k = sqrt(k2);
-    const double smear = exp(-6.0 * k2 * g.dr * g.dr);
-    double wr = 0, wi = 0;  // W = wr + i wi
-    const double Ra = (a >= 8) ? 2 * R : R;
-    const double kR = k * Ra;
-    if (a == 0 || a == 8) {
-      if (kR > 1e-3) {
-        wr = smear * (4 * kPi) * Ra * sin(kR) / k;
-      } else {
-        const double x = kR * kR;
-        wr = (4 * kPi) * (Ra * Ra) * (-x * x * x * (1.0 / 120 / 6 / 7) + x * x * (1.0 / 120) -
-                                      x * (1.0 / 6) + 1);
-      }
-    } else if (a == 1) {
-      wr = kR > 1e-5 ? -smear * (4 * kPi) * (-sin(kR) / k - Ra * cos(kR)) : 2 * (4 * kPi) * Ra;
-    } else if (a < 5) {
-      const int c = a - 2;
-      if (kR > 1e-3) {
-        wi = smear * (4 * kPi) * kv[c] / k2 * (Ra * cos(kR) - sin(kR) / k);
-      } else {
-        const double x = kR * kR;
-        wi = (4 * kPi) * Ra * Ra * Ra * kv[c] *
-             (x * x * (1.0 / 5040 - 1.0 / 720) + x * (1.0 / 24 - 1.0 / 120) - 1.0 / 3);
-      }
-    } else if (a < 8) {
-      const int c = a - 5;
-      const double thr = c == 0 ? 1e-5 : 1e-3;  // the reference's x vs y, z thresholds
-      wi = kR > thr ? smear * (4 * kPi) * Ra * kv[c] / k * sin(kR) : (4 * kPi) * Ra * Ra * kv[c];
-    } else {
-      if (kR > 1e-3) {
-        wr = smear * (4 * kPi) * (sin(kR) - kR * cos(kR)) / (k2 * k);
-      } else {
-        const double x = kR * kR;
-        wr = (4 * kPi / 3) * Ra * Ra * Ra *
-             (x * x * x * (-1.0 / 15120) + x * x * (1.0 / 280) + x * (-1.0 / 10) + 1);
-      }
-    }
-    const double2 f = F[i];
-    const double2 t = {wr * f.x - wi * f.y, wr * f.y + wi * f.x};
-    if (first) {
-      acc[i] = t;
-    } else {
-      const double2 o = acc[i];
-      acc[i] = double2{o.x + t.x, o.y + t.y};
-    }
+    const Partials p = cm::partials(kind, R, n3, n2, v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    src[i] = cm::gsa_source(a, p, v, R);
   }
 }
 
@@ -213,7 +112,7 @@ int contact_values(Engine *e, const FmtSpec &f, int which, const double *n, doub
     double2 *acc = spec + NC;
     double *num = reinterpret_cast<double *>(acc + NC);
     if (e->fft(n, spec)) return fail("fft");
-    k_contact_accum<<<blocks_for(NC), kThreads, 0, s>>>(9, g, f.R, spec, acc, 1);
+    cm::k_weight_apply<<<blocks_for(NC), kThreads, 0, s>>>(9, g, f.R, 0.0, spec, acc, 0, 1);
     if (e->ifft(acc, num)) return fail("ifft");
     k_contact_finish<<<blocks_for(NR), kThreads, 0, s>>>(which, num, nullptr, NR, out);
   } else {
@@ -228,11 +127,11 @@ int contact_values(Engine *e, const FmtSpec &f, int which, const double *n, doub
       for (int a = 0; a < 8; a++) {
         k_contact_source<<<blocks_for(NR), kThreads, 0, s>>>(a, f.hs, f.R, w, NR, src);
         if (e->fft(src, spec)) return fail("fft");
-        k_contact_accum<<<blocks_for(NC), kThreads, 0, s>>>(a, g, f.R, spec, acc, a == 0);
+        cm::k_weight_apply<<<blocks_for(NC), kThreads, 0, s>>>(a, g, f.R, 0.0, spec, acc, 0, a == 0);
       }
       if (e->ifft(acc, num)) return fail("ifft");
       if (e->fft(n, spec)) return fail("fft");
-      k_contact_accum<<<blocks_for(NC), kThreads, 0, s>>>(8, g, f.R, spec, acc, 1);
+      cm::k_weight_apply<<<blocks_for(NC), kThreads, 0, s>>>(8, g, f.R, 0.0, spec, acc, 0, 1);
       if (e->ifft(acc, den)) return fail("ifft");
       k_contact_finish<<<blocks_for(NR), kThreads, 0, s>>>(which, num, den, NR, out);
     }
@@ -245,5 +144,25 @@ int contact_values(Engine *e, const FmtSpec &f, int which, const double *n, doub
   }
   return 0;
 }
+
+namespace cm {
+__global__ void k_weight_apply(int a, Geom g, double R, double s, const double2 *__restrict__ F,
+                               double2 *__restrict__ acc, int adjoint, int first) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < g.NC; i += gridDim.x * blockDim.x) {
+    double k[3], wr, wi;
+    k_of(g, i, k);
+    weight(a, k, R, g.dr, s, wr, wi);
+    if (adjoint) wi = -wi;
+    const double2 f = F[i];
+    const double2 t = {wr * f.x - wi * f.y, wr * f.y + wi * f.x};
+    if (first) {
+      acc[i] = t;
+    } else {
+      const double2 o = acc[i];
+      acc[i] = double2{o.x + t.x, o.y + t.y};
+    }
+  }
+}
+}  // namespace cm
 
 }  // namespace deft

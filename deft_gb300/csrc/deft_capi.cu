@@ -6,6 +6,7 @@
 #include "../../include/deft_gb300.h"
 #include "contact.h"
 #include "fmt_engine.h"
+#include "saft.h"
 #include "tensor.h"
 
 #include <cmath>
@@ -41,6 +42,9 @@ struct deft_fmt {
   double *w_buf;  // 5*NR, allocated on first deft_fmt_weighted
   double *n_veff = nullptr, *gn_veff = nullptr;  // NR each, DEFT_TERM_VEFF only
   double *t_buf = nullptr, *t_grad = nullptr;     // tensor functionals only
+  double *s_buf = nullptr, *s_grad = nullptr;     // DEFT_TERM_SAFT only
+  deft::SaftParams saft{};
+  bool saft_set = false;
 };
 
 struct deft_cg {
@@ -419,6 +423,9 @@ static int check_fmt_params(const deft_fmt_params *p) {
     return set_err(DEFT_ERR_ARG, "unknown hard-sphere functional");
   if (p->functional >= DEFT_HS_WB_TENSOR && p->precision != DEFT_PRECISION_FP64)
     return set_err(DEFT_ERR_ARG, "the tensor functionals evaluate in FP64 only");
+  if ((p->terms & DEFT_TERM_SAFT) &&
+      (p->precision != DEFT_PRECISION_FP64 || p->functional != DEFT_HS_WB_NOTENSOR))
+    return set_err(DEFT_ERR_ARG, "the SAFT terms go with the FP64 White Bear functional");
   return DEFT_OK;
 }
 
@@ -447,6 +454,7 @@ int deft_fmt_destroy(deft_fmt *f) {
   cudaFree(f->g_buf);
   cudaFree(f->w_buf);
   cudaFree(f->t_buf);
+  cudaFree(f->s_buf);
   cudaFree(f->n_veff);
   cudaFree(f->gn_veff);
   delete f;
@@ -475,6 +483,17 @@ static int check_terms(const deft_fmt *f) {
     return set_err(DEFT_ERR_ARG, "DEFT_TERM_VEXT set but no external potential given");
   if ((f->p.terms & DEFT_TERM_MASK) && !f->mask)
     return set_err(DEFT_ERR_ARG, "DEFT_TERM_MASK set but no mask given");
+  if ((f->p.terms & DEFT_TERM_SAFT) && !f->saft_set)
+    return set_err(DEFT_ERR_ARG, "DEFT_TERM_SAFT set but no SAFT parameters given");
+  return DEFT_OK;
+}
+
+int deft_fmt_set_saft(deft_fmt *f, const double params[5]) {
+  if (!f || !params) return set_err(DEFT_ERR_ARG, "NULL argument");
+  for (int i = 0; i < 5; i++)
+    if (!std::isfinite(params[i])) return set_err(DEFT_ERR_ARG, "SAFT parameters must be finite");
+  f->saft = deft::SaftParams{params[0], params[1], params[2], params[3], params[4]};
+  f->saft_set = true;
   return DEFT_OK;
 }
 
@@ -509,12 +528,44 @@ int fmt_density(deft_fmt *f, const deft::FmtSpec &spec, const double *x, const d
 bool is_tensor(const deft_fmt *f) {
   return f->p.functional >= DEFT_HS_WB_TENSOR && (f->p.terms & DEFT_TERM_HS);
 }
+bool has_saft(const deft_fmt *f) { return f->p.terms & DEFT_TERM_SAFT; }
 
-// Energy (grad == NULL) or energy and masked gradient at the density n.
-// The tensor functionals' hard-sphere part comes from tensor.cu and the
-// local terms (ideal gas, mu, V_ext, mask) from the fused evaluator.
-int density_eval(deft_fmt *f, const deft::FmtSpec &spec, const double *n, double *grad,
+int density_eval_fmt(deft_fmt *f, const deft::FmtSpec &spec, const double *n, double *grad,
+                     double *E, double *terms);
+
+// Energy (grad == NULL) or energy and masked gradient at the density n:
+// the fused evaluator's terms (and the tensor hard-sphere part), plus the
+// water SAFT terms when they are on.
+int density_eval(deft_fmt *f, const deft::FmtSpec &spec_in, const double *n, double *grad,
                  double *E, double *terms) {
+  deft::FmtSpec spec = spec_in;
+  spec.terms &= ~DEFT_TERM_SAFT;
+  if (int s = density_eval_fmt(f, spec, n, grad, E, terms)) return s;
+  if (!has_saft(f)) return DEFT_OK;
+  Engine *e = f->grid->eng;
+  if (!f->s_buf) {
+    const size_t ns = deft::saft_scratch_doubles(e->geom());
+    cudaError_t ce = cudaMalloc((void **)&f->s_buf, sizeof(double) * (ns + nr(f->grid)));
+    if (ce != cudaSuccess) {
+      f->s_buf = nullptr;
+      return cuda_err(ce, "cudaMalloc");
+    }
+    f->s_grad = f->s_buf + ns;
+  }
+  double t2[2];
+  std::string err;
+  if (deft::saft_terms(e, spec, f->saft, n, f->s_buf, grad ? f->s_grad : nullptr, t2, &err))
+    return set_err(DEFT_ERR_CUDA, err);
+  if (grad && deft::add_masked(e, f->s_grad, (spec.terms & DEFT_TERM_MASK) ? f->mask : nullptr, grad))
+    return set_err(DEFT_ERR_CUDA, "SAFT: gradient sum");
+  *E += t2[0] + t2[1];
+  return DEFT_OK;
+}
+
+// The fused evaluator's terms; the tensor functionals' hard-sphere part
+// comes from tensor.cu and their local terms from the fused evaluator.
+int density_eval_fmt(deft_fmt *f, const deft::FmtSpec &spec, const double *n, double *grad,
+                     double *E, double *terms) {
   Engine *e = f->grid->eng;
   if (!is_tensor(f)) {
     if (!grad) return e->energy(spec, n, f->V, f->mask, E, terms) ? eng_err(e) : DEFT_OK;
@@ -679,8 +730,9 @@ int deft_fmt_hessian_vector(deft_fmt *f, const double *n, const double *dx, int 
   if (int s = check_terms(f)) return s;
   if (f->p.terms & DEFT_TERM_VEFF)
     return set_err(DEFT_ERR_ARG, "Hessian-vector products are in the density variable only");
-  if (is_tensor(f))
-    return set_err(DEFT_ERR_ARG, "Hessian-vector products are not built for the tensor functionals");
+  if (is_tensor(f) || has_saft(f))
+    return set_err(DEFT_ERR_ARG,
+                   "Hessian-vector products are not built for the tensor or SAFT functionals");
   deft_grid *g = f->grid;
   cudaSetDevice(g->ctx->device);
   const double *ns, *ds;
@@ -749,8 +801,10 @@ int deft_fmt_energy_grad_noalloc(const double lat[9], int Nx, int Ny, int Nz,
     return set_err(DEFT_ERR_ARG, "DEFT_TERM_MASK set but mask is NULL");
   if (p->precision != DEFT_PRECISION_FP64)
     return set_err(DEFT_ERR_ARG, "the allocation-free entry point evaluates in FP64 only");
-  if (p->functional >= DEFT_HS_WB_TENSOR && (p->terms & DEFT_TERM_HS))
-    return set_err(DEFT_ERR_ARG, "the allocation-free entry point has no tensor functionals");
+  if ((p->functional >= DEFT_HS_WB_TENSOR && (p->terms & DEFT_TERM_HS)) ||
+      (p->terms & DEFT_TERM_SAFT))
+    return set_err(DEFT_ERR_ARG,
+                   "the allocation-free entry point has no tensor functionals or SAFT terms");
   deft::GridSpec s;
   s.Nx = Nx;
   s.Ny = Ny;
@@ -932,7 +986,7 @@ int cg_eval(deft_cg *c, const deft::FmtSpec &spec) {
 int cg_eval_dots(deft_cg *c, const deft::FmtSpec &spec, int k, const double *const *a,
                  const double *const *b, double *out) {
   Engine *e = eng_of(c);
-  if ((c->f->p.terms & DEFT_TERM_VEFF) || is_tensor(c->f)) {
+  if ((c->f->p.terms & DEFT_TERM_VEFF) || is_tensor(c->f) || has_saft(c->f)) {
     if (int s = cg_eval(c, spec)) return s;
     return e->dots(k, a, b, out) ? eng_err(e) : DEFT_OK;
   }

@@ -45,6 +45,10 @@ extern "C" {
  * the preconditioned gradient is (dE/dn) / (Veff - kT).  Not combined with
  * deft_fmt_hessian_vector. */
 #define DEFT_TERM_VEFF 32
+#define DEFT_TERM_SAFT 64 /* water SAFT association + dispersion terms (src/haskell/WaterSaft.hs:
+                             35-104; src/WaterSaftFast.cpp), parameters from deft_fmt_set_saft;
+                             with DEFT_TERM_HS (White Bear), IDEAL and MU this is WaterSaft(...).
+                             FP64 only */
 
 /* Number of per-term energies: phi3, phi1, phi2 (src/HardSpheres.cpp:156),
  * ideal gas, chemical potential, external potential. */
@@ -282,6 +286,14 @@ int deft_cg_restore(deft_cg *cg, const char *path);
 #define DEFT_CONTACT_YUWU 3     /* YuWuCorrelation, src/ContactDensity.cpp:382-413 */
 #define DEFT_CONTACT_YUWU_S 4   /* YuWuCorrelation_S, src/ContactDensity.cpp:372-380 */
 int deft_fmt_contact(deft_fmt *f, const double *n, int on_device, int which, double *out);
+
+/* Parameters of the DEFT_TERM_SAFT terms, in the order of a LiquidProperties
+ * record (src/water-constants.cpp:22-40): {epsilon_association,
+ * kappa_association, epsilon_dispersion, lambda_dispersion, length_scaling};
+ * the hard-sphere radius and kT are the functional's R and kT
+ * (WaterSaft(R, epsAB, kappaAB, epsilon_dispersion, lambda_dispersion,
+ * length_scaling, mu), src/OptimizedFunctionals.h:13-15). */
+int deft_fmt_set_saft(deft_fmt *f, const double params[5]);
 
 /* ---- batched solves ----
  * Many independent state points and uneven grids on one GPU (no reference

@@ -72,3 +72,33 @@ def veff_case():
     P, n, iters, step = cg_case()
     P.terms |= O.VEFF
     return P, -P.kT * np.log(n), iters, step
+
+
+# Water SAFT (src/water-constants.cpp:22-40, hughes_water_prop) in atomic units
+KB_HARTREE = 3.16681539628059e-6
+ANGSTROM = 1.8897261
+WATER_R = 3.03420 * ANGSTROM / 2
+WATER_KT = 298.15 * KB_HARTREE
+WATER_N = 4.9388942e-3
+# (epsilon_association, kappa_association, epsilon_dispersion, lambda_dispersion, length_scaling)
+WATER_SAFT = (1400.0 * KB_HARTREE, 0.0381876 * (3.03420 * ANGSTROM) ** 3, 250.0 * KB_HARTREE,
+              1.78890, 0.353)
+SAFT_CASES = ("saft_cubic12", "saft_ortho_mask")
+
+
+def saft_case(name):
+    if name == "saft_cubic12":
+        rng = np.random.Generator(np.random.PCG64(201))
+        N, lat = (12, 12, 12), np.diag([6.0, 6.0, 6.0])
+        n = np.abs(WATER_N * (1 + 0.1 * rng.standard_normal(int(np.prod(N)))))
+        return O.Problem(lat, N, R=WATER_R, kT=WATER_KT, mu=-0.01, terms=O.HS | O.IDEAL | O.MU,
+                         saft=WATER_SAFT), n
+    if name == "saft_ortho_mask":
+        rng = np.random.Generator(np.random.PCG64(202))
+        N, lat = (10, 14, 9), np.diag([5.8, 8.2, 5.3])
+        size = int(np.prod(N))
+        n = np.abs(WATER_N * (1 + 0.3 * rng.standard_normal(size)))
+        mask = (rng.random(size) > 0.2).astype(np.float64)
+        return O.Problem(lat, N, R=WATER_R, kT=WATER_KT, mu=0.02, terms=O.HS | O.IDEAL | O.MU,
+                         mask=mask, saft=WATER_SAFT), n
+    raise KeyError(name)

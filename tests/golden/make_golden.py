@@ -18,7 +18,8 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
 from oracle import oracle as O  # noqa: E402
-from tests.golden.cases import CASES, HS_CASES, cg_case, make_case, veff_case  # noqa: E402
+from tests.golden.cases import (CASES, HS_CASES, SAFT_CASES, WATER_SAFT, cg_case,  # noqa: E402
+                                make_case, saft_case, veff_case)
 
 
 def main():
@@ -50,6 +51,13 @@ def main():
         P.hs = hs
         for which in range(5):
             arrays[f"contact_slit_hs{hs}_{which}"] = P.ref_contact(x, which)
+    # the water SAFT functional (WaterSaft, src/WaterSaftFast.cpp): total
+    # energy and (masked) gradient
+    for name in SAFT_CASES:
+        P, n = saft_case(name)
+        E, g = P.ref_saft(n, WATER_SAFT)
+        out[name] = {"E": E}
+        arrays[f"{name}_grad"] = g
     # known-answer value of tests/new-hard-spheres.cpp:52-63
     P = O.Problem(np.diag([2.0, 2.0, 2.0]), (20, 20, 20), R=1.0, kT=1.0, mu=0.0, terms=O.HS)
     E, _, _ = P.ref_energy_grad(np.full(8000, 0.1), grad=False)

@@ -312,3 +312,32 @@ def test_oracle_contact_values_match_reference_golden(oracle_mod, golden, hs, wh
     ref = arrs[f"contact_slit_hs{hs}_{which}"]
     assert np.all(np.isfinite(ref))
     assert np.abs(got - ref).max() <= 1e-12 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("name", ["saft_cubic12", "saft_ortho_mask"])
+def test_oracle_water_saft_matches_reference_golden(oracle_mod, golden, name):
+    """Water SAFT (ideal gas + White Bear + association + dispersion + mu N,
+    constrained by the mask when given): energy and gradient against the
+    compiled WaterSaft (src/WaterSaftFast.cpp)."""
+    from tests.golden.cases import saft_case
+    vals, arrs = golden
+    P, n = saft_case(name)
+    E, g = P.energy_grad(n)
+    assert abs(E / vals[name]["E"] - 1) < 1e-12
+    gr = arrs[f"{name}_grad"]
+    assert np.abs(g - gr).max() <= 1e-12 * np.abs(gr).max()
+
+
+def test_oracle_water_saft_gradient_is_the_energy_derivative(oracle_mod):
+    """Directional finite difference of the SAFT association + dispersion
+    energy against the chain-rule gradient (central, two step sizes)."""
+    from tests.golden.cases import WATER_SAFT, saft_case
+    P, n = saft_case("saft_cubic12")
+    _, g, _ = P.saft(n, WATER_SAFT)
+    rng = np.random.default_rng(3)
+    d = rng.standard_normal(n.size) * n * 0.01
+    gd = g @ d
+    for h in (1e-3, 5e-4):
+        Ep, _, _ = P.saft(n + h * d, WATER_SAFT, grad=False)
+        Em, _, _ = P.saft(n - h * d, WATER_SAFT, grad=False)
+        assert abs((Ep - Em) / (2 * h) / gd - 1) < 1e-6
