@@ -644,6 +644,98 @@ def kernel_case(precision, N, problem="slit", evals=3, tuning=None):
             "us_per_launch": {k: round(1e3 * v[1] / v[0], 2) for k, v in prof.items()}}
 
 
+def saft_case(N=128, dx=0.2, evals=10, gtol=1e-11):
+    """The water SAFT workload (WaterSaft with hughes_water_prop,
+    src/water-constants.cpp:22-40; atomic units): N^3 grid of spacing dx bohr,
+    liquid density 4.9388942e-3 bohr^-3 around a hard-sphere solute whose
+    centre-exclusion radius is 3 Angstrom = 5.669 bohr (the density inside it
+    floored at 1e-5 of the liquid's), mu of the homogeneous liquid.  Times
+    FP64 energy+gradient evaluations with CUDA events and one converged solve
+    (density-preconditioned CG to |grad F| < gtol)."""
+    import torch
+    from deft_gb300 import _lib
+    L = _lib.load()
+    kB, ang = 3.16681539628059e-6, 1.8897261
+    R, kT, nl = 3.03420 * ang / 2, 298.15 * kB, 4.9388942e-3
+    sp = np.array([1400.0 * kB, 0.0381876 * (3.03420 * ang) ** 3, 250.0 * kB, 1.78890, 0.353])
+    terms = _lib.TERM_HS | _lib.TERM_IDEAL | _lib.TERM_MU | _lib.TERM_SAFT
+
+    def fmt(grid, mu, mask=None):
+        h = ctypes.c_void_p()
+        p = _lib.FmtParams(R, kT, mu, terms | (_lib.TERM_MASK if mask is not None else 0), 0, 0)
+        _lib.check(L.deft_fmt_create(grid, ctypes.byref(p), ctypes.byref(h)))
+        _lib.check(L.deft_fmt_set_saft(h, sp.ctypes.data))
+        if mask is not None:
+            _lib.check(L.deft_fmt_set_mask(h, mask.data_ptr(), 1))
+        return h
+
+    h = ctypes.c_void_p()
+    _lib.check(L.deft_ctx_create(0, ctypes.byref(h)))
+    ctx = h
+    # chemical potential of the homogeneous liquid: -dF/dN on a small cell
+    cell = 8 * dx
+    lat8 = np.ascontiguousarray(np.diag([cell] * 3).reshape(9))
+    h = ctypes.c_void_p()
+    _lib.check(L.deft_grid_create(ctx, lat8.ctypes.data, 8, 8, 8, ctypes.byref(h)))
+    g8 = h
+    f8 = fmt(g8, 0.0)
+    E = ctypes.c_double()
+    dn = 1e-7 * nl
+    Es = []
+    for v in (nl + dn, nl - dn):
+        u = np.full(512, v)
+        _lib.check(L.deft_fmt_energy(f8, u.ctypes.data, 0, ctypes.addressof(E), None))
+        Es.append(E.value)
+    mu = -(Es[0] - Es[1]) / (2 * dn * cell ** 3)
+    L.deft_fmt_destroy(f8)
+    L.deft_grid_destroy(g8)
+    lat = np.ascontiguousarray(np.diag([N * dx] * 3).reshape(9))
+    h = ctypes.c_void_p()
+    _lib.check(L.deft_grid_create(ctx, lat.ctypes.data, N, N, N, ctypes.byref(h)))
+    grid = h
+    x = (np.arange(N) - N / 2) * dx
+    r = np.sqrt(x[:, None, None] ** 2 + x[None, :, None] ** 2 + x[None, None, :] ** 2)
+    mask_h = (r > 3 * ang).astype(np.float64).reshape(-1)
+    mask = torch.tensor(mask_h, device="cuda:0")
+    n0 = torch.tensor(np.where(mask_h > 0, nl, 1e-5 * nl), device="cuda:0")
+    f = fmt(grid, mu, mask)
+    gbuf = torch.empty_like(n0)
+    for _ in range(3):
+        _lib.check(L.deft_fmt_energy_grad(f, n0.data_ptr(), 1, ctypes.addressof(E), gbuf.data_ptr(),
+                                          None))
+    stream = torch.cuda.ExternalStream(L.deft_ctx_stream(ctx))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(evals):
+        _lib.check(L.deft_fmt_energy_grad(f, n0.data_ptr(), 1, ctypes.addressof(E), gbuf.data_ptr(),
+                                          None))
+    e1.record(stream)
+    e1.synchronize()
+    ms_eval = e0.elapsed_time(e1) / evals
+    cp = _lib.CgParams(_lib.LS_SECANT, gtol, 20000, 1.0, 0.0, 0.0, _lib.PC_DENSITY, 0.0)
+    h = ctypes.c_void_p()
+    _lib.check(L.deft_cg_create(f, ctypes.byref(cp), ctypes.byref(h)))
+    cg = h
+    _lib.check(L.deft_cg_set_x(cg, n0.data_ptr(), 1))
+    st = _lib.CgStatus()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    code = L.deft_cg_solve(cg, ctypes.byref(st))
+    torch.cuda.synchronize()
+    t_solve = time.perf_counter() - t0
+    L.deft_cg_destroy(cg)
+    L.deft_fmt_destroy(f)
+    L.deft_grid_destroy(grid)
+    L.deft_ctx_destroy(ctx)
+    return {"saft_case": "water SAFT (WaterSaft, hughes_water_prop) FP64, hard-sphere solute "
+                          "of exclusion radius 3 Angstrom in liquid water",
+            "N": N, "dx_bohr": dx, "mu_hartree": mu, "ms_per_energy_grad": ms_eval,
+            "solve": {"status": code, "converged": bool(st.converged), "seconds": t_solve,
+                      "iters": st.iter, "evals": st.evals, "gnorm": st.gnorm, "gtol": gtol,
+                      "energy_hartree": st.energy, "form": "FP64 secant CG with the density "
+                                                          "preconditioner"}}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -667,7 +759,12 @@ def main():
     ap.add_argument("--kernel-case", default=None, choices=["mixed", "fp64"],
                     help="only run the small kernel-profiling case and exit")
     ap.add_argument("--case-problem", default="slit", choices=["slit", "solutes"])
+    ap.add_argument("--saft-case", action="store_true",
+                    help="only time the water SAFT workload (FP64) and exit")
     args = ap.parse_args()
+    if args.saft_case:
+        print(json.dumps(saft_case(args.N)))
+        return
     if args.kernel_case:
         print(json.dumps(kernel_case(1 if args.kernel_case == "mixed" else 0, args.N,
                                      args.case_problem, tuning=args.tuning)))

@@ -19,6 +19,8 @@ Names, argument meaning and return conventions follow the reference:
   ``Precision(eps, m)``, ``MaxIter(n, m)``, ``m.improve_energy()``,
   ``m.energy()``, ``m.grad()``  src/LineMinimizer.h:18-19, src/Minimizer.h:13-60
 * ``find_chemical_potential(f, kT, n)``          src/equation-of-state.cpp:189-192
+* ``WaterSaft(R, epsAB, kappaAB, eps_d, lambda_d, length_scaling, mu)``
+  src/OptimizedFunctionals.h:13-15 (src/haskell/WaterSaft.hs)
 * ``HardSpheresRF(R)`` src/HardSpheres.cpp:69-88; ``WhiteBearMarkII(R)``
   src/haskell/WhiteBear.hs:140-159; ``HardSpheresWB(R)`` (tensor, also
   ``HardSpheres``) and ``HardSpheresTarazona(R)`` src/HardSpheres.cpp:90-135
@@ -208,9 +210,10 @@ class Functional:
     """A sum of the recognised terms, optionally wrapped in constrain(mask, .)."""
 
     def __init__(self, R=None, ideal=False, mu=None, V=None, mask=None, names=(), veff=False,
-                 hs=_lib.HS_WB_NOTENSOR):
+                 hs=_lib.HS_WB_NOTENSOR, saft=None):
         self.R = R
-        self.hs = hs  # hard-sphere kind (White Bear, Rosenfeld, mark II)
+        self.hs = hs  # hard-sphere kind (White Bear, Rosenfeld, mark II, tensor kinds)
+        self.saft = saft  # water SAFT parameters (5 values) or None
         self.ideal = ideal
         self.mu = mu
         self.V = V
@@ -233,7 +236,8 @@ class Functional:
                           mu=pick(self.mu, o.mu, "chemical-potential"),
                           V=pick(self.V, o.V, "external-potential"),
                           names=self.names + o.names,
-                          hs=self.hs if self.R is not None else o.hs)
+                          hs=self.hs if self.R is not None else o.hs,
+                          saft=pick(self.saft, o.saft, "SAFT"))
 
     def terms(self):
         t = 0
@@ -249,6 +253,8 @@ class Functional:
             t |= _lib.TERM_MASK
         if self.veff:
             t |= _lib.TERM_VEFF
+        if self.saft is not None:
+            t |= _lib.TERM_SAFT
         return t
 
     def fmt(self, gd, kT):
@@ -266,6 +272,9 @@ class Functional:
             if self.mask is not None:
                 m = _host_f64(self.mask, gd.NxNyNz)
                 check(L.deft_fmt_set_mask(h, m.ctypes.data, 0))
+            if self.saft is not None:
+                sp = np.ascontiguousarray(self.saft, dtype=np.float64)
+                check(L.deft_fmt_set_saft(h, sp.ctypes.data))
             self._fmt[key] = (gd, h)
         else:
             check(L.deft_fmt_set_params(self._fmt[key][1], ctypes.byref(p)))
@@ -352,6 +361,18 @@ def HardSpheresTarazona(R):
 
 
 HardSpheres = HardSpheresWB  # src/HardSpheres.cpp:185-187
+
+
+def WaterSaft(R, epsilon_association, kappa_association, epsilon_dispersion, lambda_dispersion,
+              length_scaling, mu):
+    """The water SAFT functional (src/OptimizedFunctionals.h:13-15,
+    src/WaterSaftFast.cpp): ideal gas + White Bear + association +
+    dispersion + mu N, in the reference's units (kT is the caller's)."""
+    return Functional(R=float(R), ideal=True, mu=float(mu),
+                      names=("phi3", "phi1", "phi2", "ideal_gas", "chemical_potential"),
+                      saft=(float(epsilon_association), float(kappa_association),
+                            float(epsilon_dispersion), float(lambda_dispersion),
+                            float(length_scaling)))
 
 
 def WhiteBearMarkII(R):
