@@ -13,7 +13,7 @@ OK = 0
 ERR_ARG, ERR_CUDA, ERR_NAN, ERR_LINESEARCH, ERR_MAXITER, ERR_NOMEM = 1, 2, 3, 4, 5, 6
 TERM_HS, TERM_IDEAL, TERM_MU, TERM_VEXT, TERM_MASK, TERM_VEFF, TERM_SAFT = 1, 2, 4, 8, 16, 32, 64
 NTERMS = 6
-LS_SECANT, LS_QUADRATIC_REF = 0, 1
+LS_SECANT, LS_QUADRATIC_REF, LS_NEW_API = 0, 1, 2
 PC_NONE, PC_FUNCTIONAL, PC_DENSITY = 0, 1, 2
 HS_WB_NOTENSOR, HS_RF, HS_WB_MARK2, HS_WB_TENSOR, HS_TARAZONA = 0, 1, 2, 3, 4
 CONTACT_GSIGMA_S, CONTACT_GSIGMA_A, CONTACT_GROSS, CONTACT_YUWU, CONTACT_YUWU_S = 0, 1, 2, 3, 4
@@ -59,7 +59,8 @@ class CgParams(ctypes.Structure):
     _fields_ = [("linesearch", ctypes.c_int), ("gtol", ctypes.c_double), ("maxiter", ctypes.c_int),
                 ("step", ctypes.c_double), ("precision", ctypes.c_double),
                 ("refine_rel", ctypes.c_double), ("preconditioned", ctypes.c_int),
-                ("refine_abs", ctypes.c_double)]
+                ("refine_abs", ctypes.c_double), ("relative_precision", ctypes.c_double),
+                ("miniter", ctypes.c_int)]
 
 
 class CgStatus(ctypes.Structure):

@@ -19,6 +19,9 @@ Names, argument meaning and return conventions follow the reference:
   ``Precision(eps, m)``, ``MaxIter(n, m)``, ``m.improve_energy()``,
   ``m.energy()``, ``m.grad()``  src/LineMinimizer.h:18-19, src/Minimizer.h:13-60
 * ``find_chemical_potential(f, kT, n)``          src/equation-of-state.cpp:189-192
+* the "new" API: ``NewFunctional(f, gd, kT, x)``, ``Minimize(newf)`` with
+  ``set_precision``, ``set_relative_precision``, ``set_maxiter``,
+  ``set_miniter``, ``precondition``, ``improve_energy``  src/new/Minimize.h
 * ``WaterSaft(R, epsAB, kappaAB, eps_d, lambda_d, length_scaling, mu)``
   src/OptimizedFunctionals.h:13-15 (src/haskell/WaterSaft.hs)
 * ``HardSpheresRF(R)`` src/HardSpheres.cpp:69-88; ``WhiteBearMarkII(R)``
@@ -361,6 +364,96 @@ def HardSpheresTarazona(R):
 
 
 HardSpheres = HardSpheresWB  # src/HardSpheres.cpp:185-187
+
+
+# ---------------------------------------------------------------------------
+# The "new" API (src/new/NewFunctional.h, src/new/Minimize.h)
+
+class NewFunctional:
+    """A functional bound to its input, as the new API's NewFunctional holds
+    its data: (f, gd, kT, x); ``data`` is the current x (host array)."""
+
+    def __init__(self, f, gd, kT, x):
+        self.f, self.gd, self.kT = f, gd, float(kT)
+        self.data = np.array(_host_f64(x, gd.NxNyNz))
+
+    def energy(self):
+        return self.f.integral(self.kT, self.gd, self.data)
+
+    def grad(self):
+        g = np.zeros(self.gd.NxNyNz)
+        self.f.integralgrad(self.kT, self.gd, self.data, g)
+        return g
+
+
+class Minimize:
+    """The new API's minimiser (src/new/Minimize.cpp:9-304), run by the C ABI
+    (DEFT_LS_NEW_API): set_precision, set_relative_precision, set_maxiter,
+    set_miniter, precondition, improve_energy, energy, get_iteration_count.
+    The minimiser keeps its own copy of x and writes it back into
+    ``newf.data`` after every improve_energy call."""
+
+    def __init__(self, newf):
+        self.nf = newf
+        self.precision, self.relative_precision = 0.0, 1e-15
+        self.maxiter, self.miniter = 10000000, 6
+        self.use_preconditioning = False
+        self._cg = None
+        self._st = _lib.CgStatus()
+
+    def set_precision(self, p):
+        self.precision = float(p)
+        self._cg = None
+
+    def set_relative_precision(self, p):
+        self.relative_precision = float(p)
+        self._cg = None
+
+    def set_maxiter(self, n):
+        self.maxiter = int(n)
+        self._cg = None
+
+    def set_miniter(self, n):
+        self.miniter = int(n)
+        self._cg = None
+
+    def precondition(self, u):
+        self.use_preconditioning = bool(u)
+        self._cg = None
+
+    def _make(self):
+        L = _lib.load()
+        h = self.nf.f.fmt(self.nf.gd, self.nf.kT)
+        pc = _lib.PC_FUNCTIONAL if (self.use_preconditioning and self.nf.f.veff) else _lib.PC_NONE
+        p = _lib.CgParams(_lib.LS_NEW_API, 0.0, self.maxiter, 0.1, self.precision, 0.0, pc, 0.0,
+                          self.relative_precision, self.miniter)
+        c = ctypes.c_void_p()
+        check(L.deft_cg_create(h, ctypes.byref(p), ctypes.byref(c)))
+        check(L.deft_cg_set_x(c, self.nf.data.ctypes.data, 0))
+        self._cg = c
+
+    def improve_energy(self, verbose=False):
+        if self._cg is None:
+            self._make()
+        L = _lib.load()
+        check(L.deft_cg_step(self._cg, ctypes.byref(self._st)))
+        check(L.deft_cg_get_x(self._cg, self.nf.data.ctypes.data, 0))
+        if verbose:
+            print(f"==== Iteration {self._st.iter} ====  total energy = {self._st.energy:.15g}")
+        return not self._st.converged
+
+    def energy(self):
+        if self._cg is None:
+            return self.nf.energy()
+        return self._st.energy
+
+    def get_iteration_count(self):
+        return self._st.iter
+
+    def close(self):
+        if self._cg is not None:
+            _lib.load().deft_cg_destroy(self._cg)
+            self._cg = None
 
 
 def WaterSaft(R, epsilon_association, kappa_association, epsilon_dispersion, lambda_dispersion,

@@ -9,6 +9,7 @@
 #include "saft.h"
 #include "tensor.h"
 
+#include <cfloat>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -64,6 +65,9 @@ struct deft_cg {
   double e_cache = 0;
   // Precision modifier state (src/Precision.cpp:23-48)
   double dEdn = 0, log_ratio_avg = 0, deltaE = 0, err_est = 0;
+  // "new" API Minimize state (src/new/Minimize.h:17-45)
+  double nm_step = 0.1, nm_oldgradsqr = 1.0, nm_deltaE = 0, nm_dEdn = 0, nm_log_avg = 0,
+         nm_err = 0;
   bool done = false;
   // mixed form: stage 0 = FP32 CG, 1 = FP64-residual Newton refinement
   int stage = 0, evals_fp64 = 0, hvps = 0;
@@ -831,7 +835,8 @@ size_t deft_noalloc_scratch_bytes(void) { return deft::noalloc_scratch_bytes(); 
 // Minimiser
 
 static int check_cg_params(const deft_fmt *f, const deft_cg_params *p) {
-  if (p->linesearch != DEFT_LS_SECANT && p->linesearch != DEFT_LS_QUADRATIC_REF)
+  if (p->linesearch != DEFT_LS_SECANT && p->linesearch != DEFT_LS_QUADRATIC_REF &&
+      p->linesearch != DEFT_LS_NEW_API)
     return set_err(DEFT_ERR_ARG, "unknown line search");
   if (p->preconditioned < DEFT_PC_NONE || p->preconditioned > DEFT_PC_DENSITY)
     return set_err(DEFT_ERR_ARG, "unknown preconditioner");
@@ -924,6 +929,9 @@ static void cg_reset(deft_cg *c) {
   c->evals_fp64 = 0;
   c->hvps = 0;
   c->g0norm = -1;
+  c->nm_step = 0.1;  // the new API's Minimize() constructor state
+  c->nm_oldgradsqr = 1.0;
+  c->nm_deltaE = c->nm_dEdn = c->nm_log_avg = c->nm_err = 0;
   const size_t bytes = sizeof(double) * nr(c->f->grid);
   cudaMemsetAsync(c->d, 0, bytes, c->f->grid->ctx->stream);
   cudaMemsetAsync(c->gold, 0, bytes, c->f->grid->ctx->stream);
@@ -1401,6 +1409,121 @@ int step_pquadratic(deft_cg *c, bool *more) {
   return DEFT_OK;
 }
 
+// Minimize::improve_energy of the "new" API (src/new/Minimize.cpp:9-304):
+// Polak-Ribiere with reset on its (preconditioned) gradient, a quadratic
+// line search that starts from 0.001 |E0| / slope, halves until the energy
+// drops, fits a parabola (doubling when the curvature is negative, pushing
+// out while the energy does not change, falling back to the first try),
+// then its own energy-error estimate against precision and
+// relative_precision |E|, never stopping before miniter calls.
+int step_newapi(deft_cg *c, bool *more) {
+  *more = false;
+  c->iter++;
+  const int maxiter = c->p.maxiter > 0 ? c->p.maxiter : 10000000;
+  const int miniter = c->p.miniter > 0 ? c->p.miniter : 6;
+  const double relp = c->p.relative_precision > 0 ? c->p.relative_precision : 1e-15;
+  if (c->iter >= maxiter) return DEFT_OK;
+  double E0;
+  if (int s = cg_energy(c, &E0)) return s;
+  const double old_deltaE = c->nm_deltaE;
+  if (E0 != E0) return DEFT_OK;
+  if (!c->have_g)
+    if (int s = cg_eval(c, spec_of(c->f))) return s;
+  Engine *e = eng_of(c);
+  const double *pg = (c->pg && c->p.preconditioned == DEFT_PC_FUNCTIONAL) ? c->pg : c->g;
+  double o[2];
+  {
+    const double *a[2] = {pg, pg};
+    const double *b[2] = {c->g, c->gold};
+    if (e->dots(2, a, b, o)) return eng_err(e);
+  }
+  double beta = (o[0] - o[1]) / c->nm_oldgradsqr;  // pg.(g - oldgrad) / oldgradsqr
+  if (e->copy(c->g, c->gold)) return eng_err(e);   // oldgrad = g
+  if (beta < 0 || beta != beta || c->nm_oldgradsqr == 0) beta = 0;
+  c->nm_oldgradsqr = o[0];
+  double gdotd;
+  if (e->scal_add_dot(beta, c->d, -1.0, pg, c->g, &gdotd)) return eng_err(e);
+  if (gdotd > 0) {  // uphill: reset to the gradient
+    if (e->scal_add_dot(0.0, c->d, -1.0, c->g, c->g, &gdotd)) return eng_err(e);
+  }
+  const double slope = -gdotd;
+  if (E0 >= DBL_MAX || E0 <= -DBL_MAX || slope != slope || slope == 0) return DEFT_OK;
+  if (c->nm_step == 0.1 && std::fabs(E0) > 1e-200 && std::fabs(slope) > 1e-100)
+    c->nm_step = 0.001 * std::fabs(E0) / slope;
+  if (slope * c->nm_step < 0) c->nm_step *= -1;
+  double step1 = c->nm_step, E;
+  if (int s = cg_axpy(c, step1, c->d)) return s;
+  double Etried = -137;
+  for (;;) {
+    step1 *= 0.5;
+    if (int s = cg_axpy(c, -step1, c->d)) return s;
+    if (int s = cg_energy(c, &E)) return s;
+    if (E == Etried) break;
+    Etried = E;
+    if (!better(E0, E)) break;
+  }
+  const double E1 = E;
+  const double curvature = 2.0 * (E1 - E0 + step1 * slope) / (step1 * step1);
+  const double step2 = slope / curvature;
+  if (curvature <= 0.0) {
+    if (better(E0, E1)) return cg_axpy(c, -step1, c->d);
+    double Ebest = E0;
+    for (;;) {
+      if (int s = cg_energy(c, &E)) return s;
+      if (!(E <= Ebest)) break;
+      Ebest = E;
+      if (int s = cg_axpy(c, step1, c->d)) return s;
+      step1 *= 2;
+    }
+    step1 *= 0.5;
+    if (int s = cg_axpy(c, -step1, c->d)) return s;
+    c->nm_step = step1;
+  } else if (E1 == E0) {
+    do {
+      if (int s = cg_axpy(c, -step1, c->d)) return s;
+      step1 *= 2;
+      if (int s = cg_axpy(c, step1, c->d)) return s;
+      if (int s = cg_energy(c, &E)) return s;
+    } while (E == E0);
+    if (E > E0 || E != E) {
+      if (int s = cg_axpy(c, -step1, c->d)) return s;
+      step1 = 0;
+    }
+  } else {
+    c->nm_step = step2;
+    if (int s = cg_axpy(c, step2 - step1, c->d)) return s;
+    if (int s = cg_energy(c, &E)) return s;
+    if (better(E1, E) && better(E1, E0)) {
+      if (int s = cg_axpy(c, -(step2 - step1), c->d)) return s;
+      c->nm_step = step1;
+    } else if (E > E0) {
+      return cg_axpy(c, -step2, c->d);
+    }
+  }
+  double newE;
+  if (int s = cg_energy(c, &newE)) return s;
+  c->nm_deltaE = newE - E0;
+  const double w = 0.01;
+  c->nm_dEdn = (1 - w) * c->nm_dEdn + w * c->nm_deltaE;
+  c->nm_dEdn = std::fmax(c->nm_deltaE, old_deltaE);
+  const double nl =
+      (c->nm_deltaE && old_deltaE) ? std::log(std::fabs(c->nm_deltaE / old_deltaE)) : 0;
+  c->nm_log_avg = (1 - w) * c->nm_log_avg + w * nl;
+  const double ratio = std::exp(c->nm_log_avg);
+  double guess = std::fabs(std::fmax(c->nm_dEdn, c->nm_deltaE) / c->nm_log_avg);
+  if (ratio >= 1) guess = c->p.precision + std::fabs(newE);
+  c->nm_err = 2 * guess;
+  if (c->nm_deltaE == 0 && old_deltaE == 0) {
+    *more = c->iter < miniter;
+    return DEFT_OK;
+  }
+  if (!(c->nm_err < c->p.precision) && !(c->nm_err < relp * std::fabs(newE)))
+    *more = true;
+  else
+    *more = c->iter < miniter;
+  return DEFT_OK;
+}
+
 }  // namespace
 
 int deft_cg_step(deft_cg *c, deft_cg_status *st) {
@@ -1414,7 +1537,8 @@ int deft_cg_step(deft_cg *c, deft_cg_status *st) {
   if (!c->done) {
     // Precision modifier bookkeeping (src/Precision.cpp:53-151)
     double old_energy = 0;
-    const bool prec = c->p.precision > 0;
+    // (the new API's minimiser keeps its own precision estimate)
+    const bool prec = c->p.precision > 0 && c->p.linesearch != DEFT_LS_NEW_API;
     if (prec) status = cg_energy(c, &old_energy);
     bool more = true;
     if (!status) {
@@ -1449,6 +1573,8 @@ int deft_cg_step(deft_cg *c, deft_cg_status *st) {
       } else if (c->p.linesearch == DEFT_LS_SECANT) {
         status = step_secant(c, st, spec, c->p.gtol);
         more = !c->done;
+      } else if (c->p.linesearch == DEFT_LS_NEW_API) {
+        status = step_newapi(c, &more);
       } else {
         status = c->pg ? step_pquadratic(c, &more) : step_quadratic(c, &more);
       }
@@ -1538,7 +1664,13 @@ std::vector<CgScalar> cg_scalars(deft_cg *c) {
           {"evals_fp64", nullptr, &c->evals_fp64, nullptr},
           {"hvps", nullptr, &c->hvps, nullptr},
           {"g0norm", &c->g0norm, nullptr, nullptr},
-          {"last_eval_mixed", nullptr, nullptr, &c->last_eval_mixed}};
+          {"last_eval_mixed", nullptr, nullptr, &c->last_eval_mixed},
+          {"nm_step", &c->nm_step, nullptr, nullptr},
+          {"nm_oldgradsqr", &c->nm_oldgradsqr, nullptr, nullptr},
+          {"nm_deltaE", &c->nm_deltaE, nullptr, nullptr},
+          {"nm_dEdn", &c->nm_dEdn, nullptr, nullptr},
+          {"nm_log_avg", &c->nm_log_avg, nullptr, nullptr},
+          {"nm_err", &c->nm_err, nullptr, nullptr}};
 }
 
 std::vector<double *> cg_vectors(deft_cg *c) {

@@ -57,6 +57,9 @@ extern "C" {
 /* Line searches for the CG minimiser. */
 #define DEFT_LS_SECANT 0         /* derivative (secant) search on grad.d, reuses the gradient */
 #define DEFT_LS_QUADRATIC_REF 1  /* QuadraticLineMinimizer, src/QuadraticLineMinimizer.cpp:27-198 */
+#define DEFT_LS_NEW_API 2        /* the "new" API's Minimize::improve_energy (src/new/Minimize.cpp:
+                                    9-304): PR CG with its own quadratic search and precision
+                                    estimate (precision, relative_precision, miniter) */
 
 /* deft_cg_params.preconditioned */
 #define DEFT_PC_NONE 0
@@ -111,6 +114,9 @@ typedef struct {
   double refine_abs; /* mixed evaluator only: if > 0, leave the FP32 stage once
                         |grad| < refine_abs instead (e.g. a fraction of the bulk start's
                         gradient norm when starting from a warm start) */
+  double relative_precision; /* DEFT_LS_NEW_API: Minimize::set_relative_precision
+                                (0 = the constructor's 1e-15) */
+  int miniter;               /* DEFT_LS_NEW_API: Minimize::set_miniter (0 = the constructor's 6) */
 } deft_cg_params;
 
 typedef struct {

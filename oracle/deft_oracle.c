@@ -31,6 +31,7 @@
 #include "deft_oracle.h"
 #include "offt.h"
 
+#include <float.h>
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
@@ -1078,6 +1079,138 @@ static void quad_linmin(mstate *m, const double *dir, double slope, double *step
       return;
     }
   }
+}
+
+/* The "new" API minimiser, Minimize::improve_energy (src/new/Minimize.cpp:9-304),
+ * on the same functional: Polak-Ribiere CG (pgrad = grad here), its own
+ * quadratic line search (first step 0.001 |E0| / slope, halving until the
+ * energy drops, parabola, doubling when the curvature is negative, pushing
+ * out while the energy does not change, falling back to the first try) and
+ * the precision estimate with precision, relative_precision and miniter = 6.
+ * Returns the number of calls made; energies[k] = energy after call k. */
+typedef struct {
+  int iter, maxiter, miniter;
+  double step, orig_step, oldgradsqr, precision, relative_precision;
+  double deltaE, dEdn, log_avg, error_estimate;
+  double *direction, *oldgrad;
+} newmin;
+
+static int newmin_improve(mstate *m, newmin *q) {
+  q->iter++;
+  if (q->iter >= q->maxiter) return 0;
+  const double E0 = m_energy(m);
+  const double old_deltaE = q->deltaE;
+  if (E0 != E0) return 0;
+  const size_t n = m->n;
+  double gdotd;
+  {
+    const double *g = m_grad(m);
+    double num = 0, pgg = 0;
+    for (size_t i = 0; i < n; i++) num += g[i] * (g[i] - q->oldgrad[i]);
+    double beta = num / q->oldgradsqr;
+    memcpy(q->oldgrad, g, sizeof(double) * n);
+    if (beta < 0 || beta != beta || q->oldgradsqr == 0) beta = 0;
+    for (size_t i = 0; i < n; i++) pgg += g[i] * g[i];
+    q->oldgradsqr = pgg;
+    for (size_t i = 0; i < n; i++) q->direction[i] = -g[i] + beta * q->direction[i];
+    gdotd = dot(g, q->direction, n);
+    if (gdotd > 0) {
+      for (size_t i = 0; i < n; i++) q->direction[i] = -g[i];
+      gdotd = dot(g, q->direction, n);
+    }
+  }
+  const double *d = q->direction;
+  const double slope = -gdotd;
+  if (E0 >= DBL_MAX || E0 <= -DBL_MAX || slope != slope || slope == 0) return 0;
+  if (q->step == q->orig_step && fabs(E0) > 1e-200 && fabs(slope) > 1e-100)
+    q->step = 0.001 * fabs(E0) / slope;
+  if (slope * q->step < 0) q->step *= -1;
+  double step1 = q->step;
+  m_axpy(m, step1, d);
+  double Etried = -137;
+  do {
+    step1 *= 0.5;
+    m_axpy(m, -step1, d);
+    if (m_energy(m) == Etried) break;
+    Etried = m_energy(m);
+  } while (better(E0, m_energy(m)));
+  const double E1 = m_energy(m);
+  const double curvature = 2.0 * (E1 - E0 + step1 * slope) / (step1 * step1);
+  const double step2 = slope / curvature;
+  if (curvature <= 0.0) {
+    if (better(E0, E1)) {
+      m_axpy(m, -step1, d);
+      return 0;
+    }
+    double Ebest = E0;
+    while (m_energy(m) <= Ebest) {
+      Ebest = m_energy(m);
+      m_axpy(m, step1, d);
+      step1 *= 2;
+    }
+    step1 *= 0.5;
+    m_axpy(m, -step1, d);
+    q->step = step1;
+  } else if (E1 == E0) {
+    do {
+      m_axpy(m, -step1, d);
+      step1 *= 2;
+      m_axpy(m, step1, d);
+    } while (m_energy(m) == E0);
+    if (m_energy(m) > E0) {
+      m_axpy(m, -step1, d);
+      step1 = 0;
+    } else if (m_energy(m) != m_energy(m)) {
+      m_axpy(m, -step1, d);
+      step1 = 0;
+    }
+  } else {
+    q->step = step2;
+    m_axpy(m, step2 - step1, d);
+    if (better(E1, m_energy(m)) && better(E1, E0)) {
+      m_axpy(m, -(step2 - step1), d);
+      q->step = step1;
+    } else if (m_energy(m) > E0) {
+      m_axpy(m, -step2, d);
+      return 0;
+    }
+  }
+  const double newE = m_energy(m);
+  q->deltaE = newE - E0;
+  const double w = 0.01;
+  q->dEdn = (1 - w) * q->dEdn + w * q->deltaE;
+  q->dEdn = q->deltaE > old_deltaE ? q->deltaE : old_deltaE;
+  const double nl = (q->deltaE && old_deltaE) ? log(fabs(q->deltaE / old_deltaE)) : 0;
+  q->log_avg = (1 - w) * q->log_avg + w * nl;
+  const double ratio = exp(q->log_avg);
+  double guess = fabs((q->dEdn > q->deltaE ? q->dEdn : q->deltaE) / q->log_avg);
+  if (ratio >= 1) guess = q->precision + fabs(newE);
+  q->error_estimate = 2 * guess;
+  if (q->deltaE == 0 && old_deltaE == 0) return q->iter < q->miniter;
+  if (!(q->error_estimate < q->precision) &&
+      !(q->error_estimate < q->relative_precision * fabs(newE)))
+    return 1;
+  return q->iter < q->miniter;
+}
+
+int oracle_new_minimize(const oracle_params *p, const double *V, const double *mask,
+                        double *x_inout, int iters, double precision, double relative_precision,
+                        double *energies) {
+  mstate m = {p, V, mask, x_inout, (size_t)p->Nx * p->Ny * p->Nz, 0, 0, NULL, 0, NULL};
+  m.g = (double *)malloc(sizeof(double) * m.n);
+  newmin q = {0, 10000000, 6, 0.1, 0.1, 1.0, precision, relative_precision, 0, 0, 0, 0, NULL, NULL};
+  q.direction = (double *)calloc(m.n, sizeof(double));
+  q.oldgrad = (double *)calloc(m.n, sizeof(double));
+  int k = 0;
+  while (k < iters) {
+    const int more = newmin_improve(&m, &q);
+    energies[k++] = m_energy(&m);
+    if (!more) break;
+  }
+  free(m.g);
+  free(q.direction);
+  free(q.oldgrad);
+  return k;
 }
 
 int oracle_cg_quadratic(const oracle_params *p, const double *V, const double *mask,

@@ -89,6 +89,13 @@ int oracle_cg_quadratic(const oracle_params *p, const double *V, const double *m
 int oracle_pcg_quadratic(const oracle_params *p, const double *V, const double *mask,
                          double *x_inout, int iters, double step, double *energies);
 
+/* The "new" API minimiser (src/new/Minimize.cpp): up to `iters`
+ * improve_energy calls from x_inout; energies[k] = energy after call k;
+ * returns the number of calls made. */
+int oracle_new_minimize(const oracle_params *p, const double *V, const double *mask,
+                        double *x_inout, int iters, double precision, double relative_precision,
+                        double *energies);
+
 /* Derivative line-search CG to |grad|_2 < gtol (or maxiter iterations).
  * Returns the iteration count; out3 = {final energy, final |grad|, evals}. */
 int oracle_cg_solve(const oracle_params *p, const double *V, const double *mask,

@@ -92,6 +92,9 @@ def lib():
         L.oracle_pcg_quadratic.argtypes = [P, _dp, _dp, _dp, ctypes.c_int, ctypes.c_double, _dp]
         L.oracle_fft_count.restype = ctypes.c_longlong
         L.oracle_contact.argtypes = [P, _dp, ctypes.c_int, _dp]
+        L.oracle_new_minimize.restype = ctypes.c_int
+        L.oracle_new_minimize.argtypes = [P, _dp, _dp, _dp, ctypes.c_int, ctypes.c_double,
+                                          ctypes.c_double, _dp]
         L.oracle_saft.restype = ctypes.c_double
         L.oracle_saft.argtypes = [P, _dp, _dp, _dp, _dp]
         L.offt_r2c_3d.argtypes = [ctypes.c_int] * 3 + [_dp, _dp]
@@ -135,6 +138,10 @@ def ref():
                               _dp, _dp, ctypes.c_int, ctypes.c_double, _dp]
         L.ref_fft_count.restype = ctypes.c_longlong
         L.ref_set_hs.argtypes = [ctypes.c_int]
+        L.ref_new_minimize.restype = ctypes.c_int
+        L.ref_new_minimize.argtypes = ([_dp] + [ctypes.c_int] * 3 + [ctypes.c_double] * 3 +
+                                       [ctypes.c_int, _dp, _dp, _dp, ctypes.c_int, ctypes.c_double,
+                                        ctypes.c_double, _dp])
         L.ref_saft.restype = ctypes.c_double
         L.ref_saft.argtypes = [_dp] + [ctypes.c_int] * 3 + [ctypes.c_double] * 8 + [_dp, _dp, _dp]
         L.ref_contact.argtypes = [_dp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
@@ -234,6 +241,14 @@ class Problem:
                                       _ptr(out))
         return x, {"iters": it, "energy": out[0], "gnorm": out[1], "evals": int(out[2])}
 
+    def new_minimize(self, x, iters, precision=0.0, relative_precision=1e-15):
+        """The restated "new" API Minimize from x: (x after, energies)."""
+        x = np.array(x, dtype=np.float64).reshape(-1)
+        e = np.zeros(iters)
+        k = lib().oracle_new_minimize(ctypes.byref(self.params()), _ptr(self.V), _ptr(self.mask),
+                                      _ptr(x), iters, precision, relative_precision, _ptr(e))
+        return x, e[:k]
+
     def saft(self, n, saft_params, grad=True):
         """Water SAFT association + dispersion energy and (unmasked) gradient
         at n; saft_params = (eps_a, kappa_a, eps_d, lambda_d, length_scaling)."""
@@ -275,6 +290,16 @@ class Problem:
         E = ref().ref_saft(_ptr(self.lat), *self.N, self.R, *[float(v) for v in saft_params],
                            self.mu, self.kT, _ptr(n), _ptr(self.mask), _ptr(g))
         return E, g
+
+    def ref_new_minimize(self, x, iters, precision=0.0, relative_precision=1e-15):
+        """The reference's "new" API Minimize (src/new/Minimize.cpp) from x:
+        (x after, energies after each improve_energy call)."""
+        x = np.array(x, dtype=np.float64).reshape(-1)
+        e = np.zeros(iters)
+        k = self._ref().ref_new_minimize(_ptr(self.lat), *self.N, self.R, self.kT, self.mu,
+                                         self.terms, _ptr(self.V), _ptr(self.mask), _ptr(x), iters,
+                                         precision, relative_precision, _ptr(e))
+        return x, e[:k]
 
     def ref_contact(self, n, which):
         n = np.ascontiguousarray(n, dtype=np.float64).reshape(-1)

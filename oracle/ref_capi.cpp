@@ -16,6 +16,7 @@
 #include "ContactDensity.h"
 #include "Functionals.h"
 #include "OptimizedFunctionals.h"
+#include "new/Minimize.h"
 #include "Grid.h"
 #include "LineMinimizer.h"
 #include "Minimizer.h"
@@ -161,6 +162,73 @@ double ref_saft(const double *lat, int Nx, int Ny, int Nz, double R, double eps_
     for (int i = 0; i < gd.NxNyNz; i++) grad[i] = g[i];
   }
   return E;
+}
+
+}  // extern "C"
+
+// The composed functional seen through the "new" API (src/new/NewFunctional.h):
+// data is x, energy() is integral, grad() the (constrained) integralgrad.
+class ComposedAsNew : public NewFunctional {
+ public:
+  ComposedAsNew(const Functional &f, const Functional &fg, const GridDescription &gd, double kT,
+                const double *x0)
+      : f_(f), fg_(fg), gd_(gd), kT_(kT) {
+    data = Vector(gd.NxNyNz);
+    for (int i = 0; i < gd.NxNyNz; i++) data[i] = x0[i];
+  }
+  double energy() const {
+    Grid x(gd_);
+    for (int i = 0; i < gd_.NxNyNz; i++) x[i] = data[i];
+    return f_.integral(kT_, x);
+  }
+  Vector grad() const {
+    Grid x(gd_);
+    for (int i = 0; i < gd_.NxNyNz; i++) x[i] = data[i];
+    VectorXd g(gd_.NxNyNz);
+    g.setZero();
+    fg_.integralgrad(kT_, gd_, x, &g);
+    Vector out(gd_.NxNyNz);
+    for (int i = 0; i < gd_.NxNyNz; i++) out[i] = g[i];
+    return out;
+  }
+  void printme(const char *) const {}
+  double at(int i) const { return data[i]; }
+
+ private:
+  Functional f_, fg_;
+  GridDescription gd_;
+  double kT_;
+};
+
+extern "C" {
+
+// The "new" API minimiser (src/new/Minimize.cpp) on the composed functional
+// from x (overwritten): up to `iters` improve_energy() calls with the given
+// precision and relative precision (miniter and step as constructed);
+// energies[k] = energy after call k.  Returns the number of calls made.
+int ref_new_minimize(const double *lat, int Nx, int Ny, int Nz, double R, double kT, double mu,
+                     int terms, const double *V, const double *mask, double *x, int iters,
+                     double precision, double relative_precision, double *energies) {
+  GridDescription gd(make_lat(lat), Nx, Ny, Nz);
+  Functional f = make_sum(gd, R, mu, terms, V);
+  Functional fg = f;
+  if (terms & REF_MASK) {
+    Grid m(gd);
+    for (int i = 0; i < gd.NxNyNz; i++) m[i] = mask[i];
+    fg = constrain(m, f);
+  }
+  ComposedAsNew nf(f, fg, gd, kT, x);
+  Minimize min(&nf);
+  min.set_precision(precision);
+  min.set_relative_precision(relative_precision);
+  int k = 0;
+  while (k < iters) {
+    const bool more = min.improve_energy(silent);
+    energies[k++] = min.energy();
+    if (!more) break;
+  }
+  for (int i = 0; i < gd.NxNyNz; i++) x[i] = nf.at(i);
+  return k;
 }
 
 // Contact fields at the density n for the kind set by ref_set_hs (0 White

@@ -114,11 +114,12 @@ class Fmt:
 
 class CG:
     def __init__(self, fmt, linesearch=_lib.LS_SECANT, gtol=1e-9, maxiter=0, step=1.0,
-                 precision=0.0, refine_rel=0.0, preconditioned=0, refine_abs=0.0):
+                 precision=0.0, refine_rel=0.0, preconditioned=0, refine_abs=0.0,
+                 relative_precision=0.0, miniter=0):
         self.L = fmt.L
         self.size = fmt.grid.size
         p = _lib.CgParams(linesearch, gtol, maxiter, step, precision, refine_rel, preconditioned,
-                          refine_abs)
+                          refine_abs, relative_precision, miniter)
         h = ctypes.c_void_p()
         check(self.L.deft_cg_create(fmt.h, ctypes.byref(p), ctypes.byref(h)))
         self.h = h

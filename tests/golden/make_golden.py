@@ -58,6 +58,15 @@ def main():
         E, g = P.ref_saft(n, WATER_SAFT)
         out[name] = {"E": E}
         arrays[f"{name}_grad"] = g
+    # the "new" API minimiser (src/new/Minimize.cpp) on the random cubic case
+    # (8 calls) and on the CG case's slit (to its own stopping rule)
+    P, n = make_case("cubic12")
+    x, e = P.ref_new_minimize(n, 8)
+    out["new_minimize_cubic12"] = {"energies": [float(v) for v in e]}
+    P, n, _, _ = cg_case()
+    x, e = P.ref_new_minimize(n, 60)
+    out["new_minimize_slit"] = {"energies": [float(v) for v in e]}
+    arrays["new_minimize_slit_x"] = x
     # known-answer value of tests/new-hard-spheres.cpp:52-63
     P = O.Problem(np.diag([2.0, 2.0, 2.0]), (20, 20, 20), R=1.0, kT=1.0, mu=0.0, terms=O.HS)
     E, _, _ = P.ref_energy_grad(np.full(8000, 0.1), grad=False)
