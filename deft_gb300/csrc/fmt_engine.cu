@@ -299,8 +299,13 @@ __global__ void __launch_bounds__(kThreads) k_z_c2r(const typename Cplx<T>::type
 // the flattened (x, kz) lines instead, which fills every tile at any width,
 // measured 10 % slower at 128^3: the extra index division per element and
 // tiles that straddle two x planes cost more than the idle lanes it saves.)
+#ifndef DEFT_Y_FFT_MIN_BLOCKS
+#define DEFT_Y_FFT_MIN_BLOCKS 0
+#endif
 template <typename T, int SIGN, int RN = 0>
-__global__ void DEFT_FFT_BOUNDS(RN) k_y_fft(typename Cplx<T>::type *data, Geom g,
+__global__ void __launch_bounds__(kThreads,
+                                  RN > 0 ? 2 : (sizeof(T) == 4 ? DEFT_Y_FFT_MIN_BLOCKS : 0))
+    k_y_fft(typename Cplx<T>::type *data, Geom g,
                                                     FftPlan py, FastDiv fB) {
   const int B = (int)fB.d;
   using C = typename Cplx<T>::type;
@@ -598,8 +603,13 @@ __device__ void z_r2c_store5(typename Cplx<T>::type *res, typename Cplx<T>::type
 
 // c2r of the five weighted densities, phi and local terms, per-block
 // energies, and (GRAD) r2c of the five partials dV kT dphi/dn_a in place.
+#ifndef DEFT_Z_PHI_MIN_BLOCKS
+#define DEFT_Z_PHI_MIN_BLOCKS 0
+#endif
 template <typename T, bool GRAD, int RN = 0>
-__global__ void DEFT_FFT_BOUNDS(RN) k_z_phi(typename Cplx<T>::type *S5,
+__global__ void __launch_bounds__(kThreads,
+                                  RN > 0 ? 2 : (sizeof(T) == 4 ? DEFT_Z_PHI_MIN_BLOCKS : 0))
+    k_z_phi(typename Cplx<T>::type *S5,
                                                     const double *__restrict__ n,
                                                     const double *__restrict__ V, Geom g,
                                                     FftPlan pz, FastDiv fP, FastDiv f2P,
