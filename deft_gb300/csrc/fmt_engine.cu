@@ -298,14 +298,11 @@ __global__ void __launch_bounds__(kThreads) k_z_c2r(const typename Cplx<T>::type
 // FFT along y of complex fields.  grid = (kz tiles, Nx, fields).  (Tiling
 // the flattened (x, kz) lines instead, which fills every tile at any width,
 // measured 10 % slower at 128^3: the extra index division per element and
-// tiles that straddle two x planes cost more than the idle lanes it saves.)
-#ifndef DEFT_Y_FFT_MIN_BLOCKS
-#define DEFT_Y_FFT_MIN_BLOCKS 0
-#endif
+// tiles that straddle two x planes cost more than the idle lanes it saves.
+// A register cap for the FP32 form, 8 blocks per SM, gave no gain: 32
+// registers and spills.)
 template <typename T, int SIGN, int RN = 0>
-__global__ void __launch_bounds__(kThreads,
-                                  RN > 0 ? 2 : (sizeof(T) == 4 ? DEFT_Y_FFT_MIN_BLOCKS : 0))
-    k_y_fft(typename Cplx<T>::type *data, Geom g,
+__global__ void DEFT_FFT_BOUNDS(RN) k_y_fft(typename Cplx<T>::type *data, Geom g,
                                                     FftPlan py, FastDiv fB) {
   const int B = (int)fB.d;
   using C = typename Cplx<T>::type;
@@ -603,8 +600,11 @@ __device__ void z_r2c_store5(typename Cplx<T>::type *res, typename Cplx<T>::type
 
 // c2r of the five weighted densities, phi and local terms, per-block
 // energies, and (GRAD) r2c of the five partials dV kT dphi/dn_a in place.
+// The shared-memory FP32 form asks for 5 blocks per SM (48 registers, 20 B
+// of spills): 88 us at 128^3 against 92 us with ptxas's own choice (64
+// registers).  A 6-block cap spills 76 B.
 #ifndef DEFT_Z_PHI_MIN_BLOCKS
-#define DEFT_Z_PHI_MIN_BLOCKS 0
+#define DEFT_Z_PHI_MIN_BLOCKS 5
 #endif
 template <typename T, bool GRAD, int RN = 0>
 __global__ void __launch_bounds__(kThreads,
