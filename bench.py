@@ -630,6 +630,14 @@ def kernel_case(precision, N, problem="slit", evals=3, tuning=None):
                                           None))
     if precision == _lib.PRECISION_MIXED:
         _lib.check(L.deft_fmt_hessian_vector(f, n.data_ptr(), g.data_ptr(), 1, g.data_ptr()))
+    # host wall time of one synchronous call (graph replay, energy read back)
+    reps = 20
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        _lib.check(L.deft_fmt_energy_grad(f, n.data_ptr(), 1, ctypes.addressof(E), g.data_ptr(),
+                                          None))
+    wall_eval = (time.perf_counter() - t0) / reps
     _lib.check(L.deft_grid_profile(grid, 1))
     for _ in range(evals):
         _lib.check(L.deft_fmt_energy_grad(f, n.data_ptr(), 1, ctypes.addressof(E), g.data_ptr(),
@@ -641,6 +649,8 @@ def kernel_case(precision, N, problem="slit", evals=3, tuning=None):
     L.deft_ctx_destroy(ctx)
     return {"kernel_case": "mixed" if precision else "fp64", "problem": problem, "N": N,
             "evals": evals, "energy": E.value,
+            "wall_us_per_eval_call": round(1e6 * wall_eval, 1),
+            "kernel_us_per_eval": round(1e3 * sum(v[1] for v in prof.values()) / evals, 1),
             "us_per_launch": {k: round(1e3 * v[1] / v[0], 2) for k, v in prof.items()}}
 
 

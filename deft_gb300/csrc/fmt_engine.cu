@@ -178,37 +178,39 @@ __global__ void k_weight_table(Geom g, double R, W *w3, W *w2, W *wv) {
   }
 }
 
-// Packs two half-complex z-lines A (line l0) and B (line l0+1) into one
-// complex line Z = A + iB of full length (Hermitian extension); only the real
-// parts of the kz = 0 and Nyquist entries enter, as in a c2r of Hermitian data.
+// Writes element k of two half-complex z-lines A (line l0) and B (line
+// l0+1) into the packed complex line Z = A + iB of full length: Z[k] at
+// col[k * ld] and, for 0 < k < Nz/2, the Hermitian mirror Z[Nz - k] =
+// conj(A[k]) + i conj(B[k]).  Only the real parts of the kz = 0 and Nyquist
+// entries enter, as in a c2r of Hermitian data.  Each stored half-spectrum
+// element is read from global memory once.
+template <typename C>
+__device__ __forceinline__ void pack_pair_elem(C A, C B, int k, int Nz, C *col, int ld) {
+  if (k == 0 || 2 * k == Nz) {
+    A.y = 0;
+    B.y = 0;
+  }
+  col[k * ld] = C{A.x - B.y, A.y + B.x};
+  if (k > 0 && 2 * k < Nz) col[(Nz - k) * ld] = C{A.x + B.y, B.x - A.y};
+}
+
+// Packs the half-complex z-lines of P line pairs into P full-length complex
+// lines (pair pb at buf[k * P + pb]) for one complex c2r transform.
 template <typename T>
 __device__ __forceinline__ void pack_c2r(const typename Cplx<T>::type *__restrict__ in,
                                          typename Cplx<T>::type *buf, const Geom &g, int p0,
                                          int P) {
-  // element k of pair pb: idx = pb * Nz + k
   using C = typename Cplx<T>::type;
-  const int Nz = g.Nz, NzH = g.NzH;
+  const int NzH = g.NzH;
   #pragma unroll 4
-  for (int idx = threadIdx.x; idx < P * Nz; idx += blockDim.x) {
+  for (int idx = threadIdx.x; idx < P * NzH; idx += blockDim.x) {
     int pb, k;
-    fdivmod(idx, g.fNz, pb, k);
+    fdivmod(idx, g.fNzH, pb, k);
     const int l0 = 2 * (p0 + pb), l1 = l0 + 1;
     C A = C{0, 0}, B = C{0, 0};
-    if (k < NzH) {
-      if (l0 < g.lines) A = in[(size_t)l0 * NzH + k];
-      if (l1 < g.lines) B = in[(size_t)l1 * NzH + k];
-      if (k == 0 || 2 * k == Nz) {
-        A.y = 0;
-        B.y = 0;
-      }
-    } else {
-      const int kk = Nz - k;
-      if (l0 < g.lines) A = in[(size_t)l0 * NzH + kk];
-      if (l1 < g.lines) B = in[(size_t)l1 * NzH + kk];
-      A.y = -A.y;
-      B.y = -B.y;
-    }
-    buf[k * P + pb] = C{A.x - B.y, A.y + B.x};
+    if (l0 < g.lines) A = in[(size_t)l0 * NzH + k];
+    if (l1 < g.lines) B = in[(size_t)l1 * NzH + k];
+    pack_pair_elem(A, B, k, g.Nz, buf + pb, P);
   }
 }
 
@@ -542,30 +544,18 @@ __device__ typename Cplx<T>::type *z_load5_c2r(const typename Cplx<T>::type *__r
                                                const FftPlan &pz, const FastDiv &fP,
                                                const FastDiv &f5P, int p0) {
   using C = typename Cplx<T>::type;
-  const int P = (int)fP.d, P5 = 5 * P, Nz = g.Nz, NzH = g.NzH;
+  const int P = (int)fP.d, P5 = 5 * P, NzH = g.NzH;
   #pragma unroll 4
-  for (int idx = threadIdx.x; idx < P5 * Nz; idx += blockDim.x) {
+  for (int idx = threadIdx.x; idx < P5 * NzH; idx += blockDim.x) {
     int b, k, a, pb;
-    fdivmod(idx, g.fNz, b, k);
+    fdivmod(idx, g.fNzH, b, k);
     fdivmod(b, fP, a, pb);
     const C *in = S5 + (size_t)a * g.NC;
     const int l0 = 2 * (p0 + pb), l1 = l0 + 1;
     C Av = C{0, 0}, Bv = C{0, 0};
-    if (k < NzH) {
-      if (l0 < g.lines) Av = in[(size_t)l0 * NzH + k];
-      if (l1 < g.lines) Bv = in[(size_t)l1 * NzH + k];
-      if (k == 0 || 2 * k == Nz) {
-        Av.y = 0;
-        Bv.y = 0;
-      }
-    } else {
-      const int kk = Nz - k;
-      if (l0 < g.lines) Av = in[(size_t)l0 * NzH + kk];
-      if (l1 < g.lines) Bv = in[(size_t)l1 * NzH + kk];
-      Av.y = -Av.y;
-      Bv.y = -Bv.y;
-    }
-    A[k * P5 + b] = C{Av.x - Bv.y, Av.y + Bv.x};
+    if (l0 < g.lines) Av = in[(size_t)l0 * NzH + k];
+    if (l1 < g.lines) Bv = in[(size_t)l1 * NzH + k];
+    pack_pair_elem(Av, Bv, k, g.Nz, A + b, P5);
   }
   return fft_tile<T, +1, RN>(A, Bf, f5P, pz);
 }
