@@ -367,6 +367,21 @@ struct LocalArgs {
   int terms;
 };
 
+// Dot products of the new gradient with up to k <= 3 vectors, taken by the
+// kernel that writes the gradient (b[i] == nullptr: the gradient itself);
+// per-block sums go to partials[3 * block + i] and k_reduce_terms adds them
+// up in block order.
+struct GradDots {
+  const double *b[3];
+  int k;
+  double *partials;
+};
+
+// Last-block reduction of per-block dot products (defined with k_dots).
+template <int K>
+__device__ void finish_dots(double (&acc)[K], double *red, double *partials,
+                            unsigned int *counter, double *out);
+
 // x-FFT of n^, multiplication by the five weights, and the five inverse
 // x-FFTs one field at a time (three tiles of B lines: the forward result and
 // a ping-pong pair), which keeps B wide for coalesced column runs.
@@ -660,7 +675,8 @@ __global__ void DEFT_FFT_BOUNDS(RN) k_z_grad(const typename Cplx<T>::type *__res
                                                      const double *__restrict__ V,
                                                      const double *__restrict__ mask,
                                                      double *__restrict__ grad, Geom g, FftPlan pz,
-                                                     FastDiv fP, const LocalArgs *__restrict__ lap) {
+                                                     FastDiv fP, const LocalArgs *__restrict__ lap,
+                                                     GradDots gd) {
   const LocalArgs la = *lap;
   const int P = (int)fP.d;
   using C = typename Cplx<T>::type;
@@ -670,6 +686,7 @@ __global__ void DEFT_FFT_BOUNDS(RN) k_z_grad(const typename Cplx<T>::type *__res
   const int p0 = blockIdx.x * P;
   const bool hs = la.terms & kTermHS;
   const C *res = nullptr;
+  T dacc[3] = {0, 0, 0};
   if (hs) {
     pack_c2r<T>(in, buf0, g, p0, P);
     res = fft_tile<T, +1, RN>(buf0, buf1, fP, pz);
@@ -697,6 +714,18 @@ __global__ void DEFT_FFT_BOUNDS(RN) k_z_grad(const typename Cplx<T>::type *__res
       gr = m == T(0) ? T(0) : m * gr;
     }
     grad[r] = double(gr);
+    // per-thread sums in T (a dozen terms; FP32 products of the FP32
+    // gradient), the block and grid sums in FP64
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+      if (i < gd.k) dacc[i] += gr * (gd.b[i] ? T(gd.b[i][r]) : gr);
+  }
+  if (gd.k > 0) {
+    __shared__ double dred[32 * 3];
+    double dsum[3] = {double(dacc[0]), double(dacc[1]), double(dacc[2])};
+    block_reduce<3>(dsum, dred);
+    if (threadIdx.x == 0)
+      for (int i = 0; i < 3; i++) gd.partials[(size_t)blockIdx.x * 3 + i] = dsum[i];
   }
 }
 
@@ -795,8 +824,10 @@ template <typename T, int RN = 0>
 __global__ void DEFT_FFT_BOUNDS(RN) k_z_hvp_out(
     const typename Cplx<T>::type *__restrict__ in, const double *__restrict__ dx,
     const float *__restrict__ hloc, const double *__restrict__ mask, double *__restrict__ out,
-    Geom g, FftPlan pz, FastDiv fP, const LocalArgs *__restrict__ lap) {
+    Geom g, FftPlan pz, FastDiv fP, const LocalArgs *__restrict__ lap, double *dpart,
+    unsigned int *counter, double *dout) {
   const LocalArgs la = *lap;
+  double pq[1] = {0};
   const int P = (int)fP.d;
   using C = typename Cplx<T>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -821,12 +852,19 @@ __global__ void DEFT_FFT_BOUNDS(RN) k_z_hvp_out(
       const C v = res[z * P + (ll >> 1)];
       conv = (ll & 1) ? v.y : v.x;
     }
-    T o = conv + T(la.dV) * T(hloc[r]) * T(dx[r]);
+    const double dxv = dx[r];
+    T o = conv + T(la.dV) * T(hloc[r]) * T(dxv);
     if (la.terms & kTermMask) {
       const T m = T(mask[r]);
       o = m == T(0) ? T(0) : m * o;
     }
     out[r] = double(o);
+    pq[0] += dxv * double(o);
+  }
+  // dout: dx.out by the last block to finish, in block order
+  if (dout) {
+    __shared__ double red[32];
+    finish_dots<1>(pq, red, dpart, counter, dout);
   }
 }
 
@@ -853,7 +891,10 @@ __global__ void __launch_bounds__(kThreads) k_local_energy(const double *__restr
 // Sums per-block energy partials in a fixed order: out[t] = dV sum, out[6] = E.
 // One block (a 1024-thread block measured slower: 27 vs 18 us at 128^3).
 constexpr int kReduceThreads = kThreads;
-__global__ void k_reduce_terms(const double *partials, int nblk, double dV, double *out) {
+// Energy terms (out[0..6), total in out[6]) and, with dk > 0, the gradient
+// dot products of k_z_grad (out[8..8+dk)), both summed in block order.
+__global__ void k_reduce_terms(const double *partials, int nblk, double dV, double *out,
+                               const double *dpart = nullptr, int dk = 0, int dblk = 0) {
   __shared__ double red[32 * kNumTerms];
   double acc[kNumTerms] = {0, 0, 0, 0, 0, 0};
   for (int b = threadIdx.x; b < nblk; b += blockDim.x)
@@ -866,6 +907,15 @@ __global__ void k_reduce_terms(const double *partials, int nblk, double dV, doub
       E += out[t];
     }
     out[kNumTerms] = E;
+  }
+  if (dk > 0) {
+    __syncthreads();
+    double d[3] = {0, 0, 0};
+    for (int b = threadIdx.x; b < dblk; b += blockDim.x)
+      for (int t = 0; t < 3; t++) d[t] += dpart[(size_t)b * 3 + t];
+    block_reduce<3>(d, red);
+    if (threadIdx.x == 0)
+      for (int t = 0; t < dk; t++) out[8 + t] = d[t];
   }
 }
 
@@ -1325,6 +1375,7 @@ class EngineImpl {
   double *results = nullptr;       // device, 8
   double *results_host = nullptr;  // pinned, 8
   double *dot_partials = nullptr;
+  double *grad_partials = nullptr;  // k_z_grad's dot-product block sums
   unsigned int *dot_counter = nullptr;
   int dot_blocks = 0;
   Tiles t64, t32;  // launch shapes of the FP64 and the FP32 kernels
@@ -1360,6 +1411,7 @@ class EngineImpl {
     cudaFree(partials);
     cudaFree(results);
     cudaFree(dot_partials);
+    cudaFree(grad_partials);
     cudaFree(dot_counter);
     cudaFreeHost(results_host);
   }
@@ -1530,6 +1582,8 @@ class EngineImpl {
     if (dot_blocks < 1) dot_blocks = 1;
     if (alloc(&dot_partials, sizeof(double) * 3 * dot_blocks) || alloc(&dot_counter, sizeof(unsigned)))
       return -1;
+    // one slot triple per gradient block at any pair-tile width
+    if (alloc(&grad_partials, sizeof(double) * 3 * (size_t)(pairs > 0 ? pairs : 1))) return -1;
     e = cudaMemset(dot_counter, 0, sizeof(unsigned));
     if (e != cudaSuccess) return fail("cudaMemset", e);
     return check("engine init");
@@ -1777,11 +1831,15 @@ class EngineImpl {
 
   // Queues the fixed-order reduction of the energy partials and the copy of
   // the results to the pinned host block.
-  void queue_energy(int nblk) {
+  // With gd, also the gradient dot products k_z_grad took (results[8..11)).
+  void queue_energy(int nblk, const GradDots *gd = nullptr, int gblk = 0) {
     pre(kK_reduce_terms);
-    k_reduce_terms<<<1, kReduceThreads, 0, stream>>>(partials, nblk, g.dV, results);
+    k_reduce_terms<<<1, kReduceThreads, 0, stream>>>(partials, nblk, g.dV, results,
+                                                      gd ? gd->partials : nullptr,
+                                                      gd ? gd->k : 0, gblk);
     post(kK_reduce_terms);
-    cudaMemcpyAsync(results_host, results, sizeof(double) * 8, cudaMemcpyDeviceToHost, stream);
+    cudaMemcpyAsync(results_host, results, sizeof(double) * (gd ? 11 : 8), cudaMemcpyDeviceToHost,
+                    stream);
   }
 
   int finish_energy(double *E_host, double *terms_host, int kd = 0, double *dots_host = nullptr) {
@@ -1814,9 +1872,18 @@ class EngineImpl {
     if ((f.terms & kTermHS) && ensure_table<T>(f.R)) return -1;
     if (upload_args(f)) return -1;
     const GraphKey key = graph_key(grad ? 1 : 0, sizeof(T), f, n, V, mask, grad, kd, da, db);
+    // dot products of the new gradient ride on the kernel that writes it
+    bool fused = grad && kd > 0;
+    GradDots gd{};
+    for (int i = 0; i < kd && fused; i++) {
+      fused = da[i] == grad;
+      gd.b[i] = db[i] == grad ? nullptr : db[i];
+    }
+    gd.k = kd;
+    gd.partials = grad_partials;
     if (run_graphed(key, [&] {
-          if (eval_launch<T>(f, n, V, mask, grad)) return -1;
-          if (kd > 0) queue_dots(kd, da, db, 8);
+          if (eval_launch<T>(f, n, V, mask, grad, fused ? &gd : nullptr)) return -1;
+          if (kd > 0 && !fused) queue_dots(kd, da, db, 8);
           return check("dots");
         }))
       return -1;
@@ -1838,7 +1905,7 @@ class EngineImpl {
 
   template <typename T>
   int eval_launch(const FmtSpec &f, const double *n, const double *V, const double *mask,
-                  double *grad) {
+                  double *grad, const GradDots *gd = nullptr) {
     const Tiles &t = tl<T>();
     int nblk;
     if (f.terms & kTermHS) {
@@ -1877,12 +1944,12 @@ class EngineImpl {
       pre(kslot<T>(kK_z_grad));
       with_rn<T>(plan<T>(2), [&](auto rn) {
         k_z_grad<T, decltype(rn)::value><<<pairs_tiles(t.Pz), kThreads, t.smem_z, stream>>>(
-            spec0<T>(), n, V, mask, grad, g, plan<T>(2), t.fPz, la_dev);
+            spec0<T>(), n, V, mask, grad, g, plan<T>(2), t.fPz, la_dev, gd ? *gd : GradDots{});
       });
       post(kslot<T>(kK_z_grad));
     }
     if (check("gradient")) return -1;
-    queue_energy(nblk);
+    queue_energy(nblk, grad ? gd : nullptr, pairs_tiles(t.Pz));
     return check("energy reduction");
   }
   int hess_setup(const FmtSpec &f, const double *n) {
@@ -1904,14 +1971,19 @@ class EngineImpl {
     return check("hessian blocks");
   }
 
-  int hvp(const FmtSpec &f, const double *dx, const double *mask, double *out) {
+  // With pq_host, also dx.out (taken by the output kernel) read back.
+  int hvp(const FmtSpec &f, const double *dx, const double *mask, double *out,
+          double *pq_host = nullptr) {
     if ((f.terms & kTermHS) && ensure_table<float>(f.R)) return -1;
     if (upload_args(f)) return -1;
-    const GraphKey key = graph_key(2, 4, f, dx, mask, out, hess);
-    return run_graphed(key, [&] { return hvp_launch(f, dx, mask, out); });
+    const GraphKey key = graph_key(pq_host ? 3 : 2, 4, f, dx, mask, out, hess);
+    if (run_graphed(key, [&] { return hvp_launch(f, dx, mask, out, pq_host != nullptr); }))
+      return -1;
+    return pq_host ? read_results(1, pq_host, "hessian-vector product") : 0;
   }
 
-  int hvp_launch(const FmtSpec &f, const double *dx, const double *mask, double *out) {
+  int hvp_launch(const FmtSpec &f, const double *dx, const double *mask, double *out,
+                 bool with_dot = false) {
     if (f.terms & kTermHS) {
       if (forward_weighted<float>(f, dx)) return -1;
       pre(kslot<float>(kK_z_jac));
@@ -1937,7 +2009,9 @@ class EngineImpl {
     with_rn<float>(plan<float>(2), [&](auto rn) {
       k_z_hvp_out<float, decltype(rn)::value><<<pairs_tiles(t32.Pz), kThreads, t32.smem_z,
                                                 stream>>>(spec0<float>(), dx, hloc, mask, out, g,
-                                                          plan<float>(2), t32.fPz, la_dev);
+                                                          plan<float>(2), t32.fPz, la_dev,
+                                                          grad_partials, dot_counter,
+                                                          with_dot ? results : nullptr);
     });
     post(kslot<float>(kK_z_hvp_out));
     return check("hessian-vector product");
@@ -2029,8 +2103,9 @@ int Engine::energy_grad(const FmtSpec &f, const double *n, const double *V, cons
 
 int Engine::hess_setup(const FmtSpec &f, const double *n) { return impl_->hess_setup(f, n); }
 
-int Engine::hvp(const FmtSpec &f, const double *dx, const double *mask, double *out) {
-  return impl_->hvp(f, dx, mask, out);
+int Engine::hvp(const FmtSpec &f, const double *dx, const double *mask, double *out,
+                double *pq_host) {
+  return impl_->hvp(f, dx, mask, out, pq_host);
 }
 
 int Engine::dots(int k, const double *const *a, const double *const *b, double *out_host) {
@@ -2401,7 +2476,7 @@ int noalloc_energy_grad(const GridSpec &s, const FmtSpec &f, const double *n, co
     k_local_energy<double><<<nblk, kThreads, 0, stream>>>(n, V, g, la_dev, partials);
   }
   k_z_grad<double><<<ptiles_z, kThreads, t.smem_z, stream>>>(S0, n, V, mask, grad, g, pz, t.fPz,
-                                                             la_dev);
+                                                             la_dev, GradDots{});
   k_reduce_terms<<<1, kReduceThreads, 0, stream>>>(partials, nblk, g.dV, results);
   double res[8];
   e = cudaGetLastError();

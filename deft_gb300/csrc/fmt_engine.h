@@ -122,9 +122,11 @@ class Engine {
   // Newton refinement of the mixed form: hess_setup stores, at the point n,
   // the packed second derivatives of phi (FP32, from FP32 weighted
   // densities) and the ideal-gas curvature; hvp then gives out = H dx, the
-  // (masked) Hessian of the functional times dx, through FP32 FFTs.
+  // (masked) Hessian of the functional times dx, through FP32 FFTs; with
+  // pq_host also the FP64 dot product dx.out.
   int hess_setup(const FmtSpec &f, const double *n);
-  int hvp(const FmtSpec &f, const double *dx, const double *mask, double *out);
+  int hvp(const FmtSpec &f, const double *dx, const double *mask, double *out,
+          double *pq_host = nullptr);
 
   // z = r n / (kT dV): the inverse ideal-gas curvature applied to r (0 where
   // masked), the preconditioner of the Newton step's linear CG.
