@@ -654,6 +654,38 @@ def kernel_case(precision, N, problem="slit", evals=3, tuning=None):
             "us_per_launch": {k: round(1e3 * v[1] / v[0], 2) for k, v in prof.items()}}
 
 
+def fno_case(N=128, reps=5):
+    """The warm-start network's forward pass at the timed configuration
+    (N^3 grid, 16 channels, 12 modes, 4 Fourier layers; seeded random
+    weights): `reps` passes of deft_fno_warm_start on a slit mask, each
+    timed on the host around a device synchronisation."""
+    import torch
+    from deft_gb300 import _lib
+    from deft_gb300.warmstart import FourierOperator
+    L = _lib.load()
+    net = FourierOperator(N, 16, 12, 4, seed=TRAIN_SEED, device=0)
+    z = np.arange(N) * 0.2
+    mask1 = ((z > 0) & (z < 0.35 * N * 0.2)).astype(np.float64)
+    mask = torch.tensor(np.broadcast_to(mask1, (N, N, N)).reshape(-1).copy(), device="cuda:0")
+    n = torch.empty_like(mask)
+    nb = 0.3 / (4 * math.pi / 3)
+    times = []
+    try:
+        for k in range(reps + 2):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            _lib.check(L.deft_fno_warm_start(net.h, mask.data_ptr(), 0.3, nb, 1e-3, n.data_ptr()))
+            torch.cuda.synchronize()
+            if k >= 2:
+                times.append(time.perf_counter() - t0)
+        launches = int(L.deft_fno_launches(net.h))
+    finally:
+        net.close()
+    return {"fno_case": {"N": N, "channels": 16, "modes": 12, "layers": 4},
+            "ms_per_forward": round(1e3 * statistics.median(times), 3),
+            "launches_per_forward": launches // (reps + 2)}
+
+
 def saft_case(N=128, dx=0.2, evals=10, gtol=1e-11):
     """The water SAFT workload (WaterSaft with hughes_water_prop,
     src/water-constants.cpp:22-40; atomic units): N^3 grid of spacing dx bohr,
@@ -771,9 +803,14 @@ def main():
     ap.add_argument("--case-problem", default="slit", choices=["slit", "solutes"])
     ap.add_argument("--saft-case", action="store_true",
                     help="only time the water SAFT workload (FP64) and exit")
+    ap.add_argument("--fno-case", action="store_true",
+                    help="only time the warm-start network's forward pass and exit")
     args = ap.parse_args()
     if args.saft_case:
         print(json.dumps(saft_case(args.N)))
+        return
+    if args.fno_case:
+        print(json.dumps(fno_case(args.N)))
         return
     if args.kernel_case:
         print(json.dumps(kernel_case(1 if args.kernel_case == "mixed" else 0, args.N,

@@ -50,105 +50,123 @@ __device__ __forceinline__ float bf(const __nv_bfloat16 *w, size_t i) {
 }
 
 // ---------------------------------------------------------------------------
-// Truncated DFT along z (contiguous lines of length N).
+// Truncated DFT along z (contiguous lines of length N), as two small dense
+// contractions per block in registers.
 // fwd: out[l][k] = s_k sum_z in[l][z] e^{-2 pi i k z / N}   (k < Kz <= kMaxKz)
-// E[z*Kz + k] = s_k (cos, -sin) precomputed.  A block stages LB lines (row
-// stride N + 4: the four threads of a line and the eight lines of a warp hit
-// distinct banks); four consecutive threads share a line, each summing every
-// fourth z for all k in registers, then a shuffle reduction.
+// with E[z*Kz + k] = s_k (cos, -sin) precomputed.  A block of 128 threads
+// stages 128 lines (16-byte loads, eight in flight per thread) with row
+// stride N + 4 floats (16-byte rows; the eight rows one load instruction
+// touches fall in distinct banks).  Lane (lg = lane / 4,
+// mg = lane % 4) of warp w accumulates lines 32 w + lg + 8 r (r < 4) and
+// modes mg + 4 j (j < KB / 4): per z, four row values and KB / 4 table
+// entries feed 2 KB multiply-adds.  KB is Kz rounded up to a multiple of 4.
 constexpr int kMaxKz = 16;
+constexpr int kZfLines = 128;
 
-__global__ void __launch_bounds__(256) k_dft_z_fwd(const float *__restrict__ in,
+template <int KB>
+__global__ void __launch_bounds__(128) k_dft_z_fwd(const float *__restrict__ in,
                                                    float2 *__restrict__ out,
                                                    const float2 *__restrict__ E, int L, int N,
                                                    int Kz) {
-  extern __shared__ float sm[];
-  const int LB = 64, S = N + 4;
-  float *tile = sm;                                             // [LB][N+4]
-  float2 *Es = reinterpret_cast<float2 *>(tile + LB * S);      // [N][Kz]
-  const int l0 = blockIdx.x * LB;
+  constexpr int J = KB / 4;
+  extern __shared__ __align__(16) float sm[];
+  const int S = N + 4;
+  float *tile = sm;                                                   // [128][N+4]
+  float2 *Es = reinterpret_cast<float2 *>(tile + kZfLines * S);      // [N][Kz]
+  const int l0 = blockIdx.x * kZfLines;
   for (int i = threadIdx.x; i < N * Kz; i += blockDim.x) Es[i] = E[i];
-  for (int i = threadIdx.x; i < LB * N; i += blockDim.x) {
-    const int ll = i / N, z = i - ll * N;
-    const int l = l0 + ll;
-    tile[ll * S + z] = l < L ? in[(size_t)l * N + z] : 0.f;
+  // N is a multiple of 4 (the network's grids are): float4 rows
+  const int N4 = N >> 2;
+  const int nl = L - l0 < kZfLines ? L - l0 : kZfLines;
+  const float4 *src = reinterpret_cast<const float4 *>(in + (size_t)l0 * N);
+#pragma unroll 8
+  for (int i = threadIdx.x; i < kZfLines * N4; i += blockDim.x) {
+    const int ll = i / N4, q = i - ll * N4;
+    const float4 v = ll < nl ? src[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    *reinterpret_cast<float4 *>(tile + ll * S + 4 * q) = v;
   }
   __syncthreads();
-  const int ll = threadIdx.x >> 2, q = threadIdx.x & 3;
-  const int l = l0 + ll;
-  float2 acc[kMaxKz];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int lg = lane >> 2, mg = lane & 3;
+  float2 acc[4][J];
 #pragma unroll
-  for (int k = 0; k < kMaxKz; k++) acc[k] = make_float2(0.f, 0.f);
-  const float *row = tile + ll * S;
-  for (int z = q; z < N; z += 4) {
-    const float v = row[z];
-    const float2 *e = Es + z * Kz;
+  for (int r = 0; r < 4; r++)
 #pragma unroll
-    for (int k = 0; k < kMaxKz; k++) {
-      if (k < Kz) {
-        const float2 w = e[k];
-        acc[k].x += v * w.x;
-        acc[k].y += v * w.y;
+    for (int j = 0; j < J; j++) acc[r][j] = make_float2(0.f, 0.f);
+  const float *rows = tile + (32 * w + lg) * S;
+#pragma unroll 2
+  for (int z = 0; z < N; z++) {
+    float a[4];
+#pragma unroll
+    for (int r = 0; r < 4; r++) a[r] = rows[8 * r * S + z];
+    float2 e[J];
+#pragma unroll
+    for (int j = 0; j < J; j++) {
+      const int k = mg + 4 * j;
+      e[j] = k < Kz ? Es[z * Kz + k] : make_float2(0.f, 0.f);
+    }
+#pragma unroll
+    for (int r = 0; r < 4; r++)
+#pragma unroll
+      for (int j = 0; j < J; j++) {
+        acc[r][j].x += a[r] * e[j].x;
+        acc[r][j].y += a[r] * e[j].y;
       }
-    }
   }
 #pragma unroll
-  for (int k = 0; k < kMaxKz; k++) {
-    if (k < Kz) {
-      acc[k].x += __shfl_xor_sync(0xffffffffu, acc[k].x, 1);
-      acc[k].y += __shfl_xor_sync(0xffffffffu, acc[k].y, 1);
-      acc[k].x += __shfl_xor_sync(0xffffffffu, acc[k].x, 2);
-      acc[k].y += __shfl_xor_sync(0xffffffffu, acc[k].y, 2);
-    }
-  }
-  if (l < L) {
+  for (int r = 0; r < 4; r++) {
+    const int l = l0 + 32 * w + lg + 8 * r;
+    if (l >= L) continue;
 #pragma unroll
-    for (int k = 0; k < kMaxKz; k++)
-      if (k < Kz && (k & 3) == q) out[(size_t)l * Kz + k] = acc[k];
+    for (int j = 0; j < J; j++) {
+      const int k = mg + 4 * j;
+      if (k < Kz) out[(size_t)l * Kz + k] = acc[r][j];
+    }
   }
 }
 
 // inv: out[l][z] (+)= sum_k Re[in[l][k] G[z][k]],  G = c_k s (cos, sin), z-major.
-// Four threads per line hold the line's Kz coefficients in registers and
-// produce every fourth z into a staged tile, written back coalesced.
-__global__ void __launch_bounds__(256) k_dft_z_inv(const float2 *__restrict__ in,
+// A block of 128 threads takes 64 lines: thread t keeps the table rows of
+// z = t mod 64 and z + 64 (per chunk of 128 z) in registers and walks every
+// second line (t / 64 picks the parity), so the line's Kz coefficients are
+// read by a whole warp at once (broadcast) and each feeds 4 multiply-adds.
+constexpr int kZiLines = 64;
+
+template <int KB>
+__global__ void __launch_bounds__(128) k_dft_z_inv(const float2 *__restrict__ in,
                                                    float *__restrict__ out,
                                                    const float2 *__restrict__ G, int L, int N,
                                                    int Kz, int accumulate) {
-  extern __shared__ float sm[];
-  const int LB = 64, S = N + 4;
-  float *tile = sm;                                        // [LB][N+4]
-  float2 *Gs = reinterpret_cast<float2 *>(tile + LB * S);  // [N][Kz]
-  const int l0 = blockIdx.x * LB;
-  for (int i = threadIdx.x; i < Kz * N; i += blockDim.x) Gs[i] = G[i];
+  __shared__ float2 cs[kZiLines * kMaxKz];
+  const int l0 = blockIdx.x * kZiLines;
+  const int nl = L - l0 < kZiLines ? L - l0 : kZiLines;
+  for (int i = threadIdx.x; i < kZiLines * Kz; i += blockDim.x)
+    cs[i] = i < nl * Kz ? in[(size_t)l0 * Kz + i] : make_float2(0.f, 0.f);
   __syncthreads();
-  const int ll = threadIdx.x >> 2, q = threadIdx.x & 3;
-  const int l = l0 + ll;
-  float2 c[kMaxKz];
+  const int zs = threadIdx.x & 63, par = threadIdx.x >> 6;
+  for (int zc = 0; zc < N; zc += 128) {
+    const int z0 = zc + zs, z1 = z0 + 64;
+    float2 g0[KB], g1[KB];
 #pragma unroll
-  for (int k = 0; k < kMaxKz; k++)
-    c[k] = (k < Kz && l < L) ? in[(size_t)l * Kz + k] : make_float2(0.f, 0.f);
-  float *row = tile + ll * S;
-  for (int z = q; z < N; z += 4) {
-    const float2 *gz = Gs + z * Kz;
-    float acc = 0.f;
-#pragma unroll
-    for (int k = 0; k < kMaxKz; k++) {
-      if (k < Kz) {
-        const float2 gk = gz[k];
-        acc += c[k].x * gk.x - c[k].y * gk.y;
-      }
+    for (int k = 0; k < KB; k++) {
+      g0[k] = (k < Kz && z0 < N) ? G[(size_t)z0 * Kz + k] : make_float2(0.f, 0.f);
+      g1[k] = (k < Kz && z1 < N) ? G[(size_t)z1 * Kz + k] : make_float2(0.f, 0.f);
     }
-    row[z] = acc;
-  }
-  __syncthreads();
-  for (int i = threadIdx.x; i < LB * N; i += blockDim.x) {
-    const int lr = i / N, z = i - lr * N;
-    const int lo = l0 + lr;
-    if (lo >= L) continue;
-    float *o = out + (size_t)lo * N + z;
-    const float v = tile[lr * S + z];
-    *o = accumulate ? *o + v : v;
+    for (int ll = par; ll < nl; ll += 2) {
+      const float2 *c = cs + ll * Kz;
+      float v0 = 0.f, v1 = 0.f;
+#pragma unroll
+      for (int k = 0; k < KB; k++) {
+        if (k < Kz) {
+          const float2 a = c[k];
+          v0 += a.x * g0[k].x - a.y * g0[k].y;
+          v1 += a.x * g1[k].x - a.y * g1[k].y;
+        }
+      }
+      float *o = out + (size_t)(l0 + ll) * N;
+      if (z0 < N) o[z0] = accumulate ? o[z0] + v0 : v0;
+      if (z1 < N) o[z1] = accumulate ? o[z1] + v1 : v1;
+    }
   }
 }
 
@@ -171,7 +189,20 @@ __global__ void k_dft_axis(const float2 *__restrict__ in, float2 *__restrict__ o
     const float2 *src = in + (size_t)o * Nin * inner + i;
     const float2 *e = Es + m * Nin;
     float re = 0.f, im = 0.f;
-    for (int n = 0; n < Nin; n++) {
+    int n = 0;
+    // eight strided loads in flight before their multiply-adds (same order)
+    for (; n + 8 <= Nin; n += 8) {
+      float2 a[8];
+#pragma unroll
+      for (int u = 0; u < 8; u++) a[u] = src[(size_t)(n + u) * inner];
+#pragma unroll
+      for (int u = 0; u < 8; u++) {
+        const float2 b = e[n + u];
+        re += a[u].x * b.x - a[u].y * b.y;
+        im += a[u].x * b.y + a[u].y * b.x;
+      }
+    }
+    for (; n < Nin; n++) {
       const float2 a = src[(size_t)n * inner], b = e[n];
       re += a.x * b.x - a.y * b.y;
       im += a.x * b.y + a.y * b.x;
@@ -233,9 +264,15 @@ __global__ void k_lift(const float *__restrict__ mask, float eta, const __nv_bfl
 
 // Layer output: z[o][r] = spec[o][r] + sum_i Wp[o][i] h[i][r] + b[o];
 // hn = act(z).  spec is already in z (from the inverse transform); z is
-// written back only when a backward pass will need it (store_z).  The
-// output-channel loop is not unrolled, so the weights stay in shared memory
-// instead of C*C registers.
+// written back only when a backward pass will need it (store_z).  A thread
+// takes four consecutive points (16-byte loads and stores; N^3 is a
+// multiple of 4), so each weight read from shared memory feeds four
+// multiply-adds.  The output-channel loop is not unrolled, so the weights
+// stay in shared memory instead of C*C registers.
+__device__ __forceinline__ float4 gelu4(float4 a) {
+  return make_float4(gelu(a.x), gelu(a.y), gelu(a.z), gelu(a.w));
+}
+
 template <int C>
 __global__ void __launch_bounds__(256) k_layer_pw(const float *__restrict__ h,
                                                   float *__restrict__ z, float *__restrict__ hn,
@@ -246,18 +283,33 @@ __global__ void __launch_bounds__(256) k_layer_pw(const float *__restrict__ h,
   for (int i = threadIdx.x; i < C * C; i += blockDim.x) Ws[i] = bf(Wp, i);
   for (int i = threadIdx.x; i < C; i += blockDim.x) bs[i] = bf(b, i);
   __syncthreads();
-  for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < NR;
-       r += (long long)gridDim.x * blockDim.x) {
-    float hv[C];
+  const long long NR4 = NR >> 2;
+  const float4 *h4 = reinterpret_cast<const float4 *>(h);
+  float4 *z4 = reinterpret_cast<float4 *>(z);
+  float4 *hn4 = reinterpret_cast<float4 *>(hn);
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < NR4;
+       q += (long long)gridDim.x * blockDim.x) {
+    float4 hv[C];
 #pragma unroll
-    for (int i = 0; i < C; i++) hv[i] = h[(size_t)i * NR + r];
+    for (int i = 0; i < C; i++) hv[i] = h4[(size_t)i * NR4 + q];
 #pragma unroll 1
     for (int o = 0; o < C; o++) {
-      float acc = z[(size_t)o * NR + r] + bs[o];
+      float4 acc = z4[(size_t)o * NR4 + q];
+      const float bo = bs[o];
+      acc.x += bo;
+      acc.y += bo;
+      acc.z += bo;
+      acc.w += bo;
 #pragma unroll
-      for (int i = 0; i < C; i++) acc += Ws[o * C + i] * hv[i];
-      if (store_z) z[(size_t)o * NR + r] = acc;
-      hn[(size_t)o * NR + r] = act ? gelu(acc) : acc;
+      for (int i = 0; i < C; i++) {
+        const float w = Ws[o * C + i];
+        acc.x += w * hv[i].x;
+        acc.y += w * hv[i].y;
+        acc.z += w * hv[i].z;
+        acc.w += w * hv[i].w;
+      }
+      if (store_z) z4[(size_t)o * NR4 + q] = acc;
+      hn4[(size_t)o * NR4 + q] = act ? gelu4(acc) : acc;
     }
   }
 }
@@ -298,25 +350,41 @@ __global__ void k_project(const float *__restrict__ h, const __nv_bfloat16 *__re
   __syncthreads();
   const float q2v = bf(q2, 0);
   float acc[2] = {0.f, 0.f};
-  for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < NR;
-       r += (long long)gridDim.x * blockDim.x) {
-    float hv[C];
+  // four consecutive points per thread (16-byte accesses; N^3 is a multiple of 4)
+  const long long NR4 = NR >> 2;
+  const float4 *h4 = reinterpret_cast<const float4 *>(h);
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < NR4;
+       q += (long long)gridDim.x * blockDim.x) {
+    float4 hv[C];
 #pragma unroll
-    for (int i = 0; i < C; i++) hv[i] = h[(size_t)i * NR + r];
-    float out = q2v;
+    for (int i = 0; i < C; i++) hv[i] = h4[(size_t)i * NR4 + q];
+    float4 out = make_float4(q2v, q2v, q2v, q2v);
 #pragma unroll 1
     for (int c = 0; c < C; c++) {
-      float a = q1s[c];
+      const float qc = q1s[c];
+      float4 a = make_float4(qc, qc, qc, qc);
 #pragma unroll
-      for (int i = 0; i < C; i++) a += Q1s[c * C + i] * hv[i];
-      if (zq) zq[(size_t)c * NR + r] = a;
-      out += Q2s[c] * gelu(a);
+      for (int i = 0; i < C; i++) {
+        const float w = Q1s[c * C + i];
+        a.x += w * hv[i].x;
+        a.y += w * hv[i].y;
+        a.z += w * hv[i].z;
+        a.w += w * hv[i].w;
+      }
+      if (zq) reinterpret_cast<float4 *>(zq)[(size_t)c * NR4 + q] = a;
+      const float q2c = Q2s[c];
+      out.x += q2c * gelu(a.x);
+      out.y += q2c * gelu(a.y);
+      out.z += q2c * gelu(a.z);
+      out.w += q2c * gelu(a.w);
     }
-    y[r] = out;
+    reinterpret_cast<float4 *>(y)[q] = out;
     if (target) {
-      const float d = out - target[r], wr = w ? w[r] : 1.f;
-      acc[0] += wr * d * d;
-      acc[1] += wr;
+      const float4 t = reinterpret_cast<const float4 *>(target)[q];
+      const float4 wv = w ? reinterpret_cast<const float4 *>(w)[q] : make_float4(1.f, 1.f, 1.f, 1.f);
+      const float d0 = out.x - t.x, d1 = out.y - t.y, d2 = out.z - t.z, d3 = out.w - t.w;
+      acc[0] += wv.x * d0 * d0 + wv.y * d1 * d1 + wv.z * d2 * d2 + wv.w * d3 * d3;
+      acc[1] += wv.x + wv.y + wv.z + wv.w;
     }
   }
   if (part) block_sum_store<2>(acc, part);
@@ -626,17 +694,33 @@ int check(deft_fno *f, const char *what) {
   return DEFT_OK;
 }
 
-size_t smem_z_fwd(int N, int Kz) { return sizeof(float) * 64 * (N + 4) + sizeof(float2) * N * Kz; }
-size_t smem_z_inv(int N, int Kz) { return sizeof(float) * 64 * (N + 4) + sizeof(float2) * Kz * N; }
+size_t smem_z_fwd(int N, int Kz) {
+  return sizeof(float) * kZfLines * (N + 4) + sizeof(float2) * N * Kz;
+}
+
+// Kz rounded up to the register tile of the z transforms (4, 8, 12, 16).
+int kz_block(int Kz) { return (Kz + 3) / 4 * 4; }
 
 void launch_z_fwd(deft_fno *f, const float *in, float2 *out, const float2 *E) {
   const int L = f->C * f->N * f->N;
-  k_dft_z_fwd<<<(L + 63) / 64, kT, smem_z_fwd(f->N, f->Kz), f->stream>>>(in, out, E, L, f->N, f->Kz);
+  const dim3 grid((L + kZfLines - 1) / kZfLines);
+  const size_t sm = smem_z_fwd(f->N, f->Kz);
+  switch (kz_block(f->Kz)) {
+    case 4: k_dft_z_fwd<4><<<grid, 128, sm, f->stream>>>(in, out, E, L, f->N, f->Kz); break;
+    case 8: k_dft_z_fwd<8><<<grid, 128, sm, f->stream>>>(in, out, E, L, f->N, f->Kz); break;
+    case 12: k_dft_z_fwd<12><<<grid, 128, sm, f->stream>>>(in, out, E, L, f->N, f->Kz); break;
+    default: k_dft_z_fwd<16><<<grid, 128, sm, f->stream>>>(in, out, E, L, f->N, f->Kz); break;
+  }
 }
 void launch_z_inv(deft_fno *f, const float2 *in, float *out, const float2 *G, int acc) {
   const int L = f->C * f->N * f->N;
-  k_dft_z_inv<<<(L + 63) / 64, kT, smem_z_inv(f->N, f->Kz), f->stream>>>(in, out, G, L, f->N, f->Kz,
-                                                                        acc);
+  const dim3 grid((L + kZiLines - 1) / kZiLines);
+  switch (kz_block(f->Kz)) {
+    case 4: k_dft_z_inv<4><<<grid, 128, 0, f->stream>>>(in, out, G, L, f->N, f->Kz, acc); break;
+    case 8: k_dft_z_inv<8><<<grid, 128, 0, f->stream>>>(in, out, G, L, f->N, f->Kz, acc); break;
+    case 12: k_dft_z_inv<12><<<grid, 128, 0, f->stream>>>(in, out, G, L, f->N, f->Kz, acc); break;
+    default: k_dft_z_inv<16><<<grid, 128, 0, f->stream>>>(in, out, G, L, f->N, f->Kz, acc); break;
+  }
 }
 void launch_axis(deft_fno *f, const float2 *in, float2 *out, const float2 *E, int outer, int Nin,
                  int Mout, int inner) {
@@ -674,7 +758,7 @@ void spectral_bwd(deft_fno *f, int l, const float *zbar, float *hin_bar) {
 
 template <int C>
 void launch_layer_pw(deft_fno *f, int l, int store_z) {
-  k_layer_pw<C><<<grid_for(f->NR), kT, 0, f->stream>>>(f->h[l], f->z[l], f->h[l + 1],
+  k_layer_pw<C><<<grid_for(f->NR / 4), kT, 0, f->stream>>>(f->h[l], f->z[l], f->h[l + 1],
                                                        f->pb + f->oWp[l], f->pb + f->ob[l], f->NR,
                                                        l < f->L - 1 ? 1 : 0, store_z);
 }
@@ -716,7 +800,7 @@ extern "C" {
 
 int deft_fno_create(int device, int N, int channels, int modes, int layers, unsigned long long seed,
                     deft_fno **out) {
-  if (!out || N < 4 || (channels != 16 && channels != 4 && channels != 8) || modes < 1 ||
+  if (!out || N < 4 || N % 4 != 0 || (channels != 16 && channels != 4 && channels != 8) || modes < 1 ||
       modes > kMaxKz || 2 * modes > N || layers < 1 || layers > 8)
     return DEFT_ERR_ARG;
   deft_fno *f = new deft_fno();
@@ -850,9 +934,11 @@ int deft_fno_create(int device, int N, int channels, int modes, int layers, unsi
   cudaMemcpy(f->Eyi, eyi.data(), sizeof(float2) * eyi.size(), cudaMemcpyHostToDevice);
   cudaMemcpy(f->Exf, exf.data(), sizeof(float2) * exf.size(), cudaMemcpyHostToDevice);
   cudaMemcpy(f->Exi, exi.data(), sizeof(float2) * exi.size(), cudaMemcpyHostToDevice);
-  const size_t zf = smem_z_fwd(N, f->Kz), zi = smem_z_inv(N, f->Kz);
-  cudaFuncSetAttribute(k_dft_z_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)zf);
-  cudaFuncSetAttribute(k_dft_z_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)zi);
+  const size_t zf = smem_z_fwd(N, f->Kz);
+  cudaFuncSetAttribute(k_dft_z_fwd<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)zf);
+  cudaFuncSetAttribute(k_dft_z_fwd<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)zf);
+  cudaFuncSetAttribute(k_dft_z_fwd<12>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)zf);
+  cudaFuncSetAttribute(k_dft_z_fwd<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)zf);
   cudaFuncSetAttribute(k_dft_axis, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)(sizeof(float2) * 2 * modes * N));
   k_to_bf16<<<grid_for((long long)off), kT, 0, f->stream>>>(f->p, f->pb, (long long)off);

@@ -334,7 +334,8 @@ int deft_batch_solve(int device, int count, const deft_batch_problem *problems,
  * A 3-D Fourier neural operator (no reference counterpart) that maps a
  * problem's constraint mask and bulk packing fraction eta to an initial
  * relative density y = n / nb, trained on converged solutions; CG from its
- * output replaces CG from the bulk density.  channels in {4, 8, 16}; modes m
+ * output replaces CG from the bulk density.  channels in {4, 8, 16}; N a
+ * multiple of 4; modes m
  * keeps |kx|, |ky| < m (2m values each) and kz < m; N^3 grid.  Weights are
  * FP32 masters with BF16 copies used by every pass (FP32 accumulation). */
 typedef struct deft_fno deft_fno;
