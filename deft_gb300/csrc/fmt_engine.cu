@@ -888,18 +888,53 @@ __global__ void __launch_bounds__(kThreads) k_local_energy(const double *__restr
     for (int t = 0; t < kNumTerms; t++) partials[(size_t)blockIdx.x * kNumTerms + t] = acc[t];
 }
 
-// Sums per-block energy partials in a fixed order: out[t] = dV sum, out[6] = E.
-// One block (a 1024-thread block measured slower: 27 vs 18 us at 128^3).
+// Sums per-block energy partials in a fixed order: out[t] = dV sum, out[6] =
+// E, and with dk > 0 the gradient dot products of k_z_grad (out[8..8+dk)).
+// With one block, that block sums everything (256 threads; 1024 measured
+// slower: 27 vs 18 us at 128^3).  With several, block b sums the b-th slice
+// of each partial array into stage[9 b..], and the last block to finish adds
+// the slices in order (deterministic): the slices' reads overlap.
 constexpr int kReduceThreads = kThreads;
-// Energy terms (out[0..6), total in out[6]) and, with dk > 0, the gradient
-// dot products of k_z_grad (out[8..8+dk)), both summed in block order.
+constexpr int kReduceBlocks = 16;
 __global__ void k_reduce_terms(const double *partials, int nblk, double dV, double *out,
-                               const double *dpart = nullptr, int dk = 0, int dblk = 0) {
+                               const double *dpart = nullptr, int dk = 0, int dblk = 0,
+                               double *stage = nullptr, unsigned int *counter = nullptr) {
   __shared__ double red[32 * kNumTerms];
+  __shared__ bool last;
+  const int G = gridDim.x;
+  const int per = (nblk + G - 1) / G, b0 = blockIdx.x * per;
+  const int b1 = b0 + per < nblk ? b0 + per : nblk;
   double acc[kNumTerms] = {0, 0, 0, 0, 0, 0};
-  for (int b = threadIdx.x; b < nblk; b += blockDim.x)
+  for (int b = b0 + threadIdx.x; b < b1; b += blockDim.x)
     for (int t = 0; t < kNumTerms; t++) acc[t] += partials[(size_t)b * kNumTerms + t];
   block_reduce<kNumTerms>(acc, red);
+  double d[3] = {0, 0, 0};
+  if (dk > 0) {
+    __syncthreads();
+    const int dper = (dblk + G - 1) / G, d0 = blockIdx.x * dper;
+    const int d1 = d0 + dper < dblk ? d0 + dper : dblk;
+    for (int b = d0 + threadIdx.x; b < d1; b += blockDim.x)
+      for (int t = 0; t < 3; t++) d[t] += dpart[(size_t)b * 3 + t];
+    block_reduce<3>(d, red);
+  }
+  if (G > 1) {
+    if (threadIdx.x == 0) {
+      for (int t = 0; t < kNumTerms; t++) stage[blockIdx.x * 9 + t] = acc[t];
+      for (int t = 0; t < 3; t++) stage[blockIdx.x * 9 + kNumTerms + t] = d[t];
+      __threadfence();
+      last = atomicAdd(counter, 1u) == (unsigned)G - 1;
+    }
+    __syncthreads();
+    if (!last || threadIdx.x != 0) return;
+    __threadfence();
+    for (int t = 0; t < kNumTerms; t++) acc[t] = 0;
+    for (int t = 0; t < 3; t++) d[t] = 0;
+    for (int b = 0; b < G; b++) {
+      for (int t = 0; t < kNumTerms; t++) acc[t] += ((volatile double *)stage)[b * 9 + t];
+      for (int t = 0; t < 3; t++) d[t] += ((volatile double *)stage)[b * 9 + kNumTerms + t];
+    }
+    *counter = 0;
+  }
   if (threadIdx.x == 0) {
     double E = 0;
     for (int t = 0; t < kNumTerms; t++) {
@@ -907,15 +942,7 @@ __global__ void k_reduce_terms(const double *partials, int nblk, double dV, doub
       E += out[t];
     }
     out[kNumTerms] = E;
-  }
-  if (dk > 0) {
-    __syncthreads();
-    double d[3] = {0, 0, 0};
-    for (int b = threadIdx.x; b < dblk; b += blockDim.x)
-      for (int t = 0; t < 3; t++) d[t] += dpart[(size_t)b * 3 + t];
-    block_reduce<3>(d, red);
-    if (threadIdx.x == 0)
-      for (int t = 0; t < dk; t++) out[8 + t] = d[t];
+    for (int t = 0; t < dk; t++) out[8 + t] = d[t];
   }
 }
 
@@ -1376,6 +1403,8 @@ class EngineImpl {
   double *results_host = nullptr;  // pinned, 8
   double *dot_partials = nullptr;
   double *grad_partials = nullptr;  // k_z_grad's dot-product block sums
+  double *reduce_stage = nullptr;   // k_reduce_terms' per-block slices
+  unsigned int *reduce_counter = nullptr;
   unsigned int *dot_counter = nullptr;
   int dot_blocks = 0;
   Tiles t64, t32;  // launch shapes of the FP64 and the FP32 kernels
@@ -1412,6 +1441,8 @@ class EngineImpl {
     cudaFree(results);
     cudaFree(dot_partials);
     cudaFree(grad_partials);
+    cudaFree(reduce_stage);
+    cudaFree(reduce_counter);
     cudaFree(dot_counter);
     cudaFreeHost(results_host);
   }
@@ -1584,6 +1615,11 @@ class EngineImpl {
       return -1;
     // one slot triple per gradient block at any pair-tile width
     if (alloc(&grad_partials, sizeof(double) * 3 * (size_t)(pairs > 0 ? pairs : 1))) return -1;
+    if (alloc(&reduce_stage, sizeof(double) * 9 * kReduceBlocks) ||
+        alloc(&reduce_counter, sizeof(unsigned)))
+      return -1;
+    e = cudaMemset(reduce_counter, 0, sizeof(unsigned));
+    if (e != cudaSuccess) return fail("cudaMemset", e);
     e = cudaMemset(dot_counter, 0, sizeof(unsigned));
     if (e != cudaSuccess) return fail("cudaMemset", e);
     return check("engine init");
@@ -1834,9 +1870,9 @@ class EngineImpl {
   // With gd, also the gradient dot products k_z_grad took (results[8..11)).
   void queue_energy(int nblk, const GradDots *gd = nullptr, int gblk = 0) {
     pre(kK_reduce_terms);
-    k_reduce_terms<<<1, kReduceThreads, 0, stream>>>(partials, nblk, g.dV, results,
-                                                      gd ? gd->partials : nullptr,
-                                                      gd ? gd->k : 0, gblk);
+    k_reduce_terms<<<kReduceBlocks, kReduceThreads, 0, stream>>>(
+        partials, nblk, g.dV, results, gd ? gd->partials : nullptr, gd ? gd->k : 0, gblk,
+        reduce_stage, reduce_counter);
     post(kK_reduce_terms);
     cudaMemcpyAsync(results_host, results, sizeof(double) * (gd ? 11 : 8), cudaMemcpyDeviceToHost,
                     stream);
