@@ -110,6 +110,16 @@ __device__ __forceinline__ void weights_at_f(float k2, float R, float dr, float 
   }
 }
 
+// (m != 0 && n > 0) for the diagonal preconditioner, on the bit patterns
+// (integer pipe, not GB300's narrow FP64 pipe): m is +-0 iff its bits
+// shifted past the sign are 0; n > 0 (+inf included, NaN excluded) iff its
+// bits lie in [1, 0x7FF0000000000000].
+__device__ __forceinline__ bool precond_active(double m, double nv) {
+  const unsigned long long mb = (unsigned long long)__double_as_longlong(m);
+  const unsigned long long nb = (unsigned long long)__double_as_longlong(nv);
+  return (mb << 1) != 0 && nb - 1ull < 0x7FF0000000000000ull;
+}
+
 // Deterministic block reduction of K doubles; thread 0 gets the sums.
 template <int K>
 __device__ void block_reduce(double (&v)[K], double *smem /* 32*K */) {
@@ -827,7 +837,7 @@ __global__ void DEFT_FFT_BOUNDS(RN) k_z_hvp_out(
     Geom g, FftPlan pz, FastDiv fP, const LocalArgs *__restrict__ lap, double *dpart,
     unsigned int *counter, double *dout) {
   const LocalArgs la = *lap;
-  double pq[1] = {0};
+  T pq[1] = {0};  // per-thread sum in T (a dozen terms), block and grid sums in FP64
   const int P = (int)fP.d;
   using C = typename Cplx<T>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -853,18 +863,20 @@ __global__ void DEFT_FFT_BOUNDS(RN) k_z_hvp_out(
       conv = (ll & 1) ? v.y : v.x;
     }
     const double dxv = dx[r];
-    T o = conv + T(la.dV) * T(hloc[r]) * T(dxv);
+    const T dxt = T(dxv);
+    T o = conv + T(la.dV) * T(hloc[r]) * dxt;
     if (la.terms & kTermMask) {
       const T m = T(mask[r]);
       o = m == T(0) ? T(0) : m * o;
     }
     out[r] = double(o);
-    pq[0] += dxv * double(o);
+    pq[0] += dxt * o;
   }
   // dout: dx.out by the last block to finish, in block order
   if (dout) {
     __shared__ double red[32];
-    finish_dots<1>(pq, red, dpart, counter, dout);
+    double pqd[1] = {double(pq[0])};
+    finish_dots<1>(pqd, red, dpart, counter, dout);
   }
 }
 
@@ -888,53 +900,18 @@ __global__ void __launch_bounds__(kThreads) k_local_energy(const double *__restr
     for (int t = 0; t < kNumTerms; t++) partials[(size_t)blockIdx.x * kNumTerms + t] = acc[t];
 }
 
-// Sums per-block energy partials in a fixed order: out[t] = dV sum, out[6] =
-// E, and with dk > 0 the gradient dot products of k_z_grad (out[8..8+dk)).
-// With one block, that block sums everything (256 threads; 1024 measured
-// slower: 27 vs 18 us at 128^3).  With several, block b sums the b-th slice
-// of each partial array into stage[9 b..], and the last block to finish adds
-// the slices in order (deterministic): the slices' reads overlap.
+// Sums per-block energy partials in a fixed order: out[t] = dV sum, out[6] = E.
+// One block (a 1024-thread block measured slower: 27 vs 18 us at 128^3).
 constexpr int kReduceThreads = kThreads;
-constexpr int kReduceBlocks = 16;
+// Energy terms (out[0..6), total in out[6]) and, with dk > 0, the gradient
+// dot products of k_z_grad (out[8..8+dk)), both summed in block order.
 __global__ void k_reduce_terms(const double *partials, int nblk, double dV, double *out,
-                               const double *dpart = nullptr, int dk = 0, int dblk = 0,
-                               double *stage = nullptr, unsigned int *counter = nullptr) {
+                               const double *dpart = nullptr, int dk = 0, int dblk = 0) {
   __shared__ double red[32 * kNumTerms];
-  __shared__ bool last;
-  const int G = gridDim.x;
-  const int per = (nblk + G - 1) / G, b0 = blockIdx.x * per;
-  const int b1 = b0 + per < nblk ? b0 + per : nblk;
   double acc[kNumTerms] = {0, 0, 0, 0, 0, 0};
-  for (int b = b0 + threadIdx.x; b < b1; b += blockDim.x)
+  for (int b = threadIdx.x; b < nblk; b += blockDim.x)
     for (int t = 0; t < kNumTerms; t++) acc[t] += partials[(size_t)b * kNumTerms + t];
   block_reduce<kNumTerms>(acc, red);
-  double d[3] = {0, 0, 0};
-  if (dk > 0) {
-    __syncthreads();
-    const int dper = (dblk + G - 1) / G, d0 = blockIdx.x * dper;
-    const int d1 = d0 + dper < dblk ? d0 + dper : dblk;
-    for (int b = d0 + threadIdx.x; b < d1; b += blockDim.x)
-      for (int t = 0; t < 3; t++) d[t] += dpart[(size_t)b * 3 + t];
-    block_reduce<3>(d, red);
-  }
-  if (G > 1) {
-    if (threadIdx.x == 0) {
-      for (int t = 0; t < kNumTerms; t++) stage[blockIdx.x * 9 + t] = acc[t];
-      for (int t = 0; t < 3; t++) stage[blockIdx.x * 9 + kNumTerms + t] = d[t];
-      __threadfence();
-      last = atomicAdd(counter, 1u) == (unsigned)G - 1;
-    }
-    __syncthreads();
-    if (!last || threadIdx.x != 0) return;
-    __threadfence();
-    for (int t = 0; t < kNumTerms; t++) acc[t] = 0;
-    for (int t = 0; t < 3; t++) d[t] = 0;
-    for (int b = 0; b < G; b++) {
-      for (int t = 0; t < kNumTerms; t++) acc[t] += ((volatile double *)stage)[b * 9 + t];
-      for (int t = 0; t < 3; t++) d[t] += ((volatile double *)stage)[b * 9 + kNumTerms + t];
-    }
-    *counter = 0;
-  }
   if (threadIdx.x == 0) {
     double E = 0;
     for (int t = 0; t < kNumTerms; t++) {
@@ -942,7 +919,15 @@ __global__ void k_reduce_terms(const double *partials, int nblk, double dV, doub
       E += out[t];
     }
     out[kNumTerms] = E;
-    for (int t = 0; t < dk; t++) out[8 + t] = d[t];
+  }
+  if (dk > 0) {
+    __syncthreads();
+    double d[3] = {0, 0, 0};
+    for (int b = threadIdx.x; b < dblk; b += blockDim.x)
+      for (int t = 0; t < 3; t++) d[t] += dpart[(size_t)b * 3 + t];
+    block_reduce<3>(d, red);
+    if (threadIdx.x == 0)
+      for (int t = 0; t < dk; t++) out[8 + t] = d[t];
   }
 }
 
@@ -1039,7 +1024,7 @@ __global__ void k_precond_dots(const double *__restrict__ n, const double *__res
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
     const double m = mask ? mask[i] : 1.0;
     const double nv = n[i], gv = g[i];
-    const double zv = (m == 0 || !(nv > 0)) ? 0.0 : gv * nv * inv_c;
+    const double zv = precond_active(m, nv) ? gv * nv * inv_c : 0.0;
     z[i] = zv;
     acc[0] += zv * gv;
     acc[1] += zv * h[i];
@@ -1065,7 +1050,7 @@ __global__ void k_newton_update(double alpha, const double *__restrict__ p,
     r[i] = rv;
     const double m = mask ? mask[i] : 1.0;
     const double nv = n[i];
-    const double zv = (m == 0 || !(nv > 0)) ? 0.0 : rv * nv * inv_c;
+    const double zv = precond_active(m, nv) ? rv * nv * inv_c : 0.0;
     z[i] = zv;
     acc[0] += rv * rv;
     acc[1] += rv * zv;
@@ -1129,7 +1114,7 @@ __global__ void k_diag_precond(const double *__restrict__ n, const double *__res
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
     const double m = mask ? mask[i] : 1.0;
     const double nv = n[i];
-    z[i] = (m == 0 || !(nv > 0)) ? 0.0 : r[i] * nv * inv_c;
+    z[i] = precond_active(m, nv) ? r[i] * nv * inv_c : 0.0;
   }
 }
 
@@ -1403,8 +1388,6 @@ class EngineImpl {
   double *results_host = nullptr;  // pinned, 8
   double *dot_partials = nullptr;
   double *grad_partials = nullptr;  // k_z_grad's dot-product block sums
-  double *reduce_stage = nullptr;   // k_reduce_terms' per-block slices
-  unsigned int *reduce_counter = nullptr;
   unsigned int *dot_counter = nullptr;
   int dot_blocks = 0;
   Tiles t64, t32;  // launch shapes of the FP64 and the FP32 kernels
@@ -1441,8 +1424,6 @@ class EngineImpl {
     cudaFree(results);
     cudaFree(dot_partials);
     cudaFree(grad_partials);
-    cudaFree(reduce_stage);
-    cudaFree(reduce_counter);
     cudaFree(dot_counter);
     cudaFreeHost(results_host);
   }
@@ -1615,11 +1596,7 @@ class EngineImpl {
       return -1;
     // one slot triple per gradient block at any pair-tile width
     if (alloc(&grad_partials, sizeof(double) * 3 * (size_t)(pairs > 0 ? pairs : 1))) return -1;
-    if (alloc(&reduce_stage, sizeof(double) * 9 * kReduceBlocks) ||
-        alloc(&reduce_counter, sizeof(unsigned)))
-      return -1;
-    e = cudaMemset(reduce_counter, 0, sizeof(unsigned));
-    if (e != cudaSuccess) return fail("cudaMemset", e);
+
     e = cudaMemset(dot_counter, 0, sizeof(unsigned));
     if (e != cudaSuccess) return fail("cudaMemset", e);
     return check("engine init");
@@ -1870,9 +1847,9 @@ class EngineImpl {
   // With gd, also the gradient dot products k_z_grad took (results[8..11)).
   void queue_energy(int nblk, const GradDots *gd = nullptr, int gblk = 0) {
     pre(kK_reduce_terms);
-    k_reduce_terms<<<kReduceBlocks, kReduceThreads, 0, stream>>>(
-        partials, nblk, g.dV, results, gd ? gd->partials : nullptr, gd ? gd->k : 0, gblk,
-        reduce_stage, reduce_counter);
+    k_reduce_terms<<<1, kReduceThreads, 0, stream>>>(partials, nblk, g.dV, results,
+                                                      gd ? gd->partials : nullptr,
+                                                      gd ? gd->k : 0, gblk);
     post(kK_reduce_terms);
     cudaMemcpyAsync(results_host, results, sizeof(double) * (gd ? 11 : 8), cudaMemcpyDeviceToHost,
                     stream);

@@ -66,7 +66,10 @@ extern "C" {
 #define DEFT_PC_FUNCTIONAL 1 /* the functional's preconditioned gradient (PreconditionedConjugateGradient) */
 #define DEFT_PC_DENSITY 2    /* diagonal M^-1 = n / (kT dV) in the density variable: the inverse of
                                 the ideal-gas curvature, zero on masked points (secant search,
-                                density variable only; an extension, not in the reference) */
+                                density variable only; an extension, not in the reference).  In
+                                the FP32 stage of the mixed form each search starts at the last
+                                accepted step and accepts |s| <= 0.5 |s0|; the FP64 form keeps
+                                the slope-ratio first step and 0.1 */
 
 typedef struct deft_ctx deft_ctx;
 typedef struct deft_grid deft_grid;
