@@ -35,6 +35,8 @@ KERNELS = {
     "Pz": ("z_r2c", "z_grad", "z_hvp_out"),
     "Pphi": ("z_phi_grad", "z_phi_energy", "z_hess", "z_jac"),
 }
+# tile widths that shape each axis's transforms (x, y, z)
+AXIS_PARAMS = (("Bxf", "Bxc"), ("By",), ("Pz", "Pphi"))
 AXIS_KERNELS = (
     ("x_fft", "x_conv_fwd", "x_conv_adj"),
     ("y_fft_1field", "y_fft_5fields"),
@@ -212,6 +214,42 @@ def tune(shape, precision=_lib.PRECISION_MIXED, device=0, repeats=4, trials=2, l
             b.set(tiles, radix)
             if log:
                 log(f"{shape} prec {precision}: axis {a} radix {best_o}")
+        if precision == _lib.PRECISION_MIXED:
+            # The register-resident transform (M = N/16 threads a line) fills
+            # a block only with enough lines per tile, which the Stockham
+            # tiles chosen above need not give: try it jointly with a sweep
+            # of that axis's tile widths.
+            for a in range(3):
+                if N[a] not in (32, 64, 128, 256):
+                    continue
+                reg = [16, N[a] // 16]
+                cur = [int(v) for v in radix[8 * a:8 * a + 8] if v]
+                if cur == reg:
+                    continue
+                cand_r = radix.copy()
+                cand_r[8 * a:8 * a + 8] = 0
+                cand_r[8 * a:8 * a + 2] = reg
+                base_c = cost(AXIS_KERNELS[a])
+                cand_t = tiles.copy()
+                for p in AXIS_PARAMS[a]:
+                    pi = PARAMS.index(p)
+                    best_v, best_pc = None, None
+                    for v in CANDIDATES:
+                        t2 = cand_t.copy()
+                        t2[pi] = v
+                        if not b.set(t2, cand_r):
+                            continue
+                        c = cost(KERNELS[p])
+                        if best_pc is None or c < best_pc:
+                            best_v, best_pc = v, c
+                    if best_v is not None:
+                        cand_t[pi] = best_v
+                if b.set(cand_t, cand_r) and cost(AXIS_KERNELS[a]) < base_c * 0.98:
+                    tiles, radix = cand_t, cand_r
+                    if log:
+                        log(f"{shape} prec {precision}: axis {a} register transform, tiles "
+                            f"{[int(v) for v in tiles]}")
+                b.set(tiles, radix)
         after = b.measure(repeats)
         return {
             "N": list(shape), "precision": int(precision),
