@@ -57,17 +57,14 @@ __device__ __forceinline__ float bf(const __nv_bfloat16 *w, size_t i) {
 // stages 128 lines (16-byte loads, eight in flight per thread) with row
 // stride N + 4 floats (16-byte rows; the eight rows one load instruction
 // touches fall in distinct banks).  Lane (lg = lane / 4,
-// mg = lane % 4) of warp w accumulates lines 32 (w mod 4) + lg + 8 r (r < 4)
-// and modes mg + 4 j (j < KB / 4): per z, four row values and KB / 4 table
-// entries feed 2 KB multiply-adds.  Warps 4-7 take the upper half of the z
-// range (256 threads: twice the warps per SM that the staged tile allows
-// with 128), and their sums are added through shared memory.  KB is Kz
-// rounded up to a multiple of 4.
+// mg = lane % 4) of warp w accumulates lines 32 w + lg + 8 r (r < 4) and
+// modes mg + 4 j (j < KB / 4): per z, four row values and KB / 4 table
+// entries feed 2 KB multiply-adds.  KB is Kz rounded up to a multiple of 4.
 constexpr int kMaxKz = 16;
 constexpr int kZfLines = 128;
 
 template <int KB>
-__global__ void __launch_bounds__(256) k_dft_z_fwd(const float *__restrict__ in,
+__global__ void __launch_bounds__(128) k_dft_z_fwd(const float *__restrict__ in,
                                                    float2 *__restrict__ out,
                                                    const float2 *__restrict__ E, int L, int N,
                                                    int Kz) {
@@ -89,7 +86,7 @@ __global__ void __launch_bounds__(256) k_dft_z_fwd(const float *__restrict__ in,
     *reinterpret_cast<float4 *>(tile + ll * S + 4 * q) = v;
   }
   __syncthreads();
-  const int lane = threadIdx.x & 31, w = (threadIdx.x >> 5) & 3, half = threadIdx.x >> 7;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int lg = lane >> 2, mg = lane & 3;
   float2 acc[4][J];
 #pragma unroll
@@ -97,9 +94,8 @@ __global__ void __launch_bounds__(256) k_dft_z_fwd(const float *__restrict__ in,
 #pragma unroll
     for (int j = 0; j < J; j++) acc[r][j] = make_float2(0.f, 0.f);
   const float *rows = tile + (32 * w + lg) * S;
-  const int zh = N >> 1, zb = half ? zh : 0, ze = half ? N : zh;
 #pragma unroll 2
-  for (int z = zb; z < ze; z++) {
+  for (int z = 0; z < N; z++) {
     float a[4];
 #pragma unroll
     for (int r = 0; r < 4; r++) a[r] = rows[8 * r * S + z];
@@ -117,17 +113,6 @@ __global__ void __launch_bounds__(256) k_dft_z_fwd(const float *__restrict__ in,
         acc[r][j].y += a[r] * e[j].y;
       }
   }
-  // the upper half's sums through the (no longer needed) tile
-  __syncthreads();
-  float2 *xs = reinterpret_cast<float2 *>(sm) + (threadIdx.x & 127) * (4 * J);
-  if (half) {
-#pragma unroll
-    for (int r = 0; r < 4; r++)
-#pragma unroll
-      for (int j = 0; j < J; j++) xs[r * J + j] = acc[r][j];
-  }
-  __syncthreads();
-  if (half) return;
 #pragma unroll
   for (int r = 0; r < 4; r++) {
     const int l = l0 + 32 * w + lg + 8 * r;
@@ -135,8 +120,7 @@ __global__ void __launch_bounds__(256) k_dft_z_fwd(const float *__restrict__ in,
 #pragma unroll
     for (int j = 0; j < J; j++) {
       const int k = mg + 4 * j;
-      const float2 u = xs[r * J + j];
-      if (k < Kz) out[(size_t)l * Kz + k] = make_float2(acc[r][j].x + u.x, acc[r][j].y + u.y);
+      if (k < Kz) out[(size_t)l * Kz + k] = acc[r][j];
     }
   }
 }
@@ -710,25 +694,22 @@ int check(deft_fno *f, const char *what) {
   return DEFT_OK;
 }
 
+size_t smem_z_fwd(int N, int Kz) {
+  return sizeof(float) * kZfLines * (N + 4) + sizeof(float2) * N * Kz;
+}
+
 // Kz rounded up to the register tile of the z transforms (4, 8, 12, 16).
 int kz_block(int Kz) { return (Kz + 3) / 4 * 4; }
-
-// Staged tile and table, or the upper half's sums if larger (small N).
-size_t smem_z_fwd(int N, int Kz) {
-  const size_t staged = sizeof(float) * kZfLines * (N + 4) + sizeof(float2) * N * Kz;
-  const size_t sums = sizeof(float2) * 128 * kz_block(Kz);
-  return staged > sums ? staged : sums;
-}
 
 void launch_z_fwd(deft_fno *f, const float *in, float2 *out, const float2 *E) {
   const int L = f->C * f->N * f->N;
   const dim3 grid((L + kZfLines - 1) / kZfLines);
   const size_t sm = smem_z_fwd(f->N, f->Kz);
   switch (kz_block(f->Kz)) {
-    case 4: k_dft_z_fwd<4><<<grid, 256, sm, f->stream>>>(in, out, E, L, f->N, f->Kz); break;
-    case 8: k_dft_z_fwd<8><<<grid, 256, sm, f->stream>>>(in, out, E, L, f->N, f->Kz); break;
-    case 12: k_dft_z_fwd<12><<<grid, 256, sm, f->stream>>>(in, out, E, L, f->N, f->Kz); break;
-    default: k_dft_z_fwd<16><<<grid, 256, sm, f->stream>>>(in, out, E, L, f->N, f->Kz); break;
+    case 4: k_dft_z_fwd<4><<<grid, 128, sm, f->stream>>>(in, out, E, L, f->N, f->Kz); break;
+    case 8: k_dft_z_fwd<8><<<grid, 128, sm, f->stream>>>(in, out, E, L, f->N, f->Kz); break;
+    case 12: k_dft_z_fwd<12><<<grid, 128, sm, f->stream>>>(in, out, E, L, f->N, f->Kz); break;
+    default: k_dft_z_fwd<16><<<grid, 128, sm, f->stream>>>(in, out, E, L, f->N, f->Kz); break;
   }
 }
 void launch_z_inv(deft_fno *f, const float2 *in, float *out, const float2 *G, int acc) {
