@@ -1,6 +1,6 @@
 """Learned warm start: host side of the Fourier neural operator in
 csrc/fno.cu (no reference counterpart; CG from the bulk density, the
-reference's only start, stays the fallback and the judge of convergence).
+reference's only start, stays the fallback and what decides convergence).
 
 * ``FourierOperator``: the network (create, parameters, save / load, one
   forward / backward pass, Adam training steps on device-resident samples,
