@@ -339,7 +339,7 @@ def run_ours(args, rank, world):
     # preconditioner, 1e-5 was the fastest of 1e-5, 3e-5, 3e-4 and the
     # relative rule on 30 held-out problems (python -m deft_gb300.warmstart
     # --count 256 --epochs 2 --held 30 --fp64-held 0 --switch 1e-5,3e-5,3e-4)
-    SWITCH = 1e-5 if PC == _lib.PC_DENSITY else 1e-4
+    SWITCH = args.switch if args.switch else (1e-5 if PC == _lib.PC_DENSITY else 1e-4)
 
     phases = {"network_s": [], "cg_s": []}
 
@@ -794,6 +794,9 @@ def main():
                     help="tuning file to register instead of the bundled one")
     ap.add_argument("--no-precond", action="store_true",
                     help="mixed solve without the density-variable preconditioner")
+    ap.add_argument("--switch", type=float, default=None,
+                    help="FP32-stage exit as a fraction of the bulk start's gradient norm "
+                         "(default 1e-5 with the preconditioner, 1e-4 without)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extra", action="store_true", help="skip cuFFT and batched sweep")
     ap.add_argument("--cpu-budget", type=float, default=20.0)
