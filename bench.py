@@ -12,9 +12,13 @@ Our arm (default): value = seconds per converged solve from the checked
 warm start (the Fourier-operator estimate, or the bulk density if the
 estimate is non-finite or has a higher energy) with the mixed evaluator
 (FP32 CG stage, then refinement on the FP64 gradient); the network's
-forward pass and the start's energy checks are inside the timed step.  The
+forward pass and the start's energy checks are inside the timed step.  A
+converged solve meets |grad F| < 1e-9 and has its profile within 1e-8 of
+the FP64 solution of the same problem (converged to |grad F| < 1e-12 before
+the timing): every timed step is checked and the run fails otherwise.  The
 plain FP64 solve from the bulk density of the same problems is timed beside
-it.  Also reported: per-kernel event timings of one profiled solve (roofline
+it, and so are the parts of the speed-up (FP64 with the density
+preconditioner, mixed from the bulk start).  Also reported: per-kernel event timings of one profiled solve (roofline
 of the dominant kernel, the whole-evaluation "conv HBM GB/s"), the same step
 end to end through the public API with host buffers, a cuFFT comparison of
 one 3-D transform, the batched sweep, and a CPU baseline (the oracle port,
@@ -24,8 +28,9 @@ The network is trained inside the run (--train-count solves of the same
 problem family, generated on the GPU) unless --weights names a weight file.
 
 --impl reference: the reference's CPU path (the plain-C restatement of it,
-since the reference sources are not present where this runs), bounded
-sample per step, scaled to the same metric.
+since the reference sources are not present where this runs): each step is
+one full converged solve of that step's problem on one core, the steps run
+concurrently on the host's cores.
 """
 import argparse
 import ctypes
@@ -46,14 +51,18 @@ sys.path.insert(0, ROOT)
 METRIC = "converged-solve s at 128\u00b3 (warm-start+mixed vs plain FP64 GPU); conv HBM GB/s"
 UNIT = "s"
 GTOL = 1e-9
+# The converged-solve target: |grad F| < 1e-9 and the density profile within
+# 1e-8 of the FP64 solution.  The mixed solve stops at |grad F| < 5e-10 (its
+# Newton refinement's final step then leaves the profile 3-4 orders of
+# magnitude inside the profile condition; at 1e-9 the worst of ten held-out
+# problems came to 3.7e-9), every timed step's profile is checked against
+# the FP64 solution of the same problem converged to |grad F| < 1e-12, and a
+# step outside 1e-8 fails the run.
+MIXED_GTOL = 5e-10
+PROFILE_TOL = 1e-8
+REF_GTOL = 1e-12
 HELD_SEED = 6
 TRAIN_SEED = 5
-# Energy+gradient evaluations of the plain FP64 solve from the bulk density
-# of held-out problems 0..15 at 128^3 (measured on GB300; the CPU port runs
-# the same CG), and the mean over 200 held-out problems for later ones.  The
-# reference arm scales each step's per-evaluation time by its problem's count.
-FP64_EVALS_128 = [149, 100, 104, 83, 40, 50, 157, 322, 360, 142, 101, 439, 38, 368, 65, 66]
-FP64_EVALS_MEAN_128 = 169.1
 HBM_FALLBACK_GBS = 6800.0
 
 
@@ -192,7 +201,8 @@ def kernel_profile(L, grid):
 
 def kernel_table(prof):
     total = sum(v[1] for v in prof.values()) or 1.0
-    return {k: {"launches": v[0], "ms_total": round(v[1], 3), "share": round(v[1] / total, 4),
+    return {k: {"launches": round(v[0], 2), "ms_total": round(v[1], 3),
+                "share": round(v[1] / total, 4),
                 "us_per_launch": round(1e3 * v[1] / v[0], 2)}
             for k, v in sorted(prof.items(), key=lambda kv: -kv[1][1])}
 
@@ -340,8 +350,30 @@ def run_ours(args, rank, world):
     # relative rule on 30 held-out problems (python -m deft_gb300.warmstart
     # --count 256 --epochs 2 --held 30 --fp64-held 0 --switch 1e-5,3e-5,3e-4)
     SWITCH = args.switch if args.switch else (1e-5 if PC == _lib.PC_DENSITY else 1e-4)
+    timed_idx = [args.warmup + k for k in range(args.steps)]
+
+    # The profile condition's reference: each timed problem solved in FP64
+    # (density preconditioner) to |grad F| < 1e-12, before any timing.
+    t0 = time.perf_counter()
+    refs, ref_stats = {}, []
+    for i in timed_idx:
+        sv.set_problem(probs[i], masks[i].data_ptr())
+        st, _ = sv.solve(FP64, bulks[i].data_ptr(), preconditioned=_lib.PC_DENSITY, gtol=REF_GTOL)
+        if not (st.converged and st.status == 0 and st.gnorm < REF_GTOL):
+            raise RuntimeError(f"FP64 reference solve of problem {i} did not converge "
+                               f"(status {st.status}, |grad| {st.gnorm:.3e})")
+        refs[i] = torch.empty_like(masks[0])
+        _lib.check(L.deft_cg_get_x(sv.cg[FP64], refs[i].data_ptr(), 1))
+        ref_stats.append((st.iter, st.evals))
+    ref_s = time.perf_counter() - t0
+    outs = {i: torch.empty_like(masks[0]) for i in timed_idx}  # each timed step's profile
+
+    def profile_errors(i, x):
+        d = float((x - refs[i]).abs().max())
+        return d, d / float(refs[i].abs().max())
 
     phases = {"network_s": [], "cg_s": []}
+    bulk_gn = {}
 
     def warm_step(i):
         s = probs[i]
@@ -349,22 +381,38 @@ def run_ours(args, rank, world):
         t0 = time.perf_counter()
         used, _, gb = net.initial_density(sv.fmt[MIXED], masks[i].data_ptr(), s.eta, s.nb,
                                           n_ws.data_ptr(), bulk_gnorm=True)
+        bulk_gn[i] = gb
         t1 = time.perf_counter()
-        st, _ = sv.solve(MIXED, n_ws.data_ptr(), refine_abs=SWITCH * gb, preconditioned=PC)
+        st, _ = sv.solve(MIXED, n_ws.data_ptr(), refine_abs=SWITCH * gb, preconditioned=PC,
+                         gtol=MIXED_GTOL)
+        if i in outs:
+            _lib.check(L.deft_cg_get_x(sv.cg[MIXED], outs[i].data_ptr(), 1))
         phases["network_s"].append(t1 - t0)
         phases["cg_s"].append(time.perf_counter() - t1)
         return st, used
 
-    def fp64_step(i):
+    def fp64_step(i, pc=_lib.PC_NONE):
         sv.set_problem(probs[i], masks[i].data_ptr())
-        st, _ = sv.solve(FP64, bulks[i].data_ptr())
+        st, _ = sv.solve(FP64, bulks[i].data_ptr(), preconditioned=pc)
+        if i in outs:
+            _lib.check(L.deft_cg_get_x(sv.cg[FP64], outs[i].data_ptr(), 1))
         return st, True
 
-    def timed(step, label):
-        for i in range(args.warmup):
-            st, _ = step(i)
+    def mixed_bulk_step(i):
+        sv.set_problem(probs[i], masks[i].data_ptr())
+        st, _ = sv.solve(MIXED, bulks[i].data_ptr(), refine_abs=SWITCH * bulk_gn[i],
+                         preconditioned=PC, gtol=MIXED_GTOL)
+        if i in outs:
+            _lib.check(L.deft_cg_get_x(sv.cg[MIXED], outs[i].data_ptr(), 1))
+        return st, True
+
+    def timed(step, label, warmup=True, clocked=True, gtol=GTOL):
+        if warmup:
+            for i in range(args.warmup):
+                step(i)
         clocks = Clocks(dev)
-        clocks.start()
+        if clocked:
+            clocks.start()
         barrier()
         torch.cuda.synchronize()
         _lib.check(L.deft_ctx_sync(sv.ctx))
@@ -373,12 +421,12 @@ def run_ours(args, rank, world):
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        stats = [step(args.warmup + k) for k in range(args.steps)]
+        stats = [step(i) for i in timed_idx]
         e1.record(stream)
         e1.synchronize()
         torch.cuda.synchronize()
         barrier()
-        ck = clocks.stop()
+        ck = clocks.stop() if clocked else None
         ms = e0.elapsed_time(e1)
         if world > 1:
             import torch.distributed as dist
@@ -388,54 +436,106 @@ def run_ours(args, rank, world):
         nl = (sum(v[0] for v in kernel_profile(L, sv.grid).values()) - launches0
               + L.deft_fno_launches(net.h) - fno0)
         bad = [k for k, (st, _) in enumerate(stats) if not (st.converged and st.status == 0
-                                                              and st.gnorm < GTOL)]
+                                                              and st.gnorm < gtol)]
         if bad:
             raise RuntimeError(f"{label}: steps {bad} did not converge")
-        return ms / args.steps, stats, ck, nl
+        errs = [profile_errors(i, outs[i]) for i in timed_idx]
+        return ms / args.steps, stats, ck, nl, errs
+
+    def err_summary(errs, gate):
+        worst_abs = max(e[0] for e in errs)
+        worst_rel = max(e[1] for e in errs)
+        out = {"max_abs_dn": worst_abs, "max_dn_rel_to_max_n": worst_rel,
+               "per_step_max_abs_dn": [float(f"{e[0]:.3e}") for e in errs],
+               "within_1e-8": bool(worst_abs <= PROFILE_TOL and worst_rel <= PROFILE_TOL)}
+        if gate and not out["within_1e-8"]:
+            raise RuntimeError(f"profile condition failed: max |dn| {worst_abs:.3e}, "
+                               f"relative {worst_rel:.3e} (limit {PROFILE_TOL:g})")
+        return out
 
     _lib.check(L.deft_grid_profile(sv.grid, 0))
-    ms_w, st_w, ck_w, nl_w = timed(warm_step, "warm start + mixed")
+    ms_w, st_w, ck_w, nl_w, err_w = timed(warm_step, "warm start + mixed", gtol=MIXED_GTOL)
+    prof_err_w = err_summary(err_w, gate=True)
     phase_means = {k: float(np.mean(v[-args.steps:])) for k, v in phases.items()}
-    ms_64, st_64, ck_64, nl_64 = timed(fp64_step, "plain FP64")
+    ms_64, st_64, ck_64, nl_64, err_64 = timed(fp64_step, "plain FP64")
+    prof_err_64 = err_summary(err_64, gate=False)
     avg = lambda sts, k: sum(getattr(x[0], k) for x in sts) / len(sts)  # noqa: E731
+    # the speed-up's parts: preconditioner (FP64 with it, from the bulk
+    # start), precision (mixed with it, from the bulk start), network
+    ms_pc, st_pc, _, _, err_pc = timed(lambda i: fp64_step(i, _lib.PC_DENSITY),
+                                       "FP64 + density preconditioner", clocked=False)
+    ms_mb, st_mb, _, _, err_mb = timed(mixed_bulk_step, "mixed from the bulk start",
+                                       warmup=False, clocked=False, gtol=MIXED_GTOL)
+    prof_err_mb = err_summary(err_mb, gate=True)
+    decomposition = {
+        "fp64_bulk_s": ms_64 / 1e3, "fp64_precond_bulk_s": ms_pc / 1e3,
+        "mixed_precond_bulk_s": ms_mb / 1e3, "warm_mixed_s": ms_w / 1e3,
+        "preconditioner_x": ms_64 / ms_pc, "precision_x": ms_pc / ms_mb,
+        "network_x": ms_mb / ms_w,
+        "fp64_precond_bulk": {"iters": avg(st_pc, "iter"), "evals": avg(st_pc, "evals"),
+                              "profile_vs_fp64_solution": err_summary(err_pc, gate=False)},
+        "mixed_precond_bulk": {"iters": avg(st_mb, "iter"), "evals": avg(st_mb, "evals"),
+                               "evals_fp64": avg(st_mb, "evals_fp64"), "hvps": avg(st_mb, "hvps"),
+                               "profile_vs_fp64_solution": prof_err_mb},
+        "note": "same held-out problems, CUDA-event timed like the headline: plain FP64 (no "
+                "preconditioner) / FP64 with the density preconditioner / mixed with it, both "
+                "from the bulk start / mixed from the checked warm start",
+    }
 
-    # one profiled headline step (per-kernel CUDA events; launches go out one by one)
-    # (NVTX range "warm_mixed_step": an ncu launch list of this one solve is
+    # Profiled passes (per-kernel CUDA events; launches go out one by one):
+    # the headline's timed problems again, for the kernel table, the roofline
+    # and the host time between kernels.  (NVTX range "warm_mixed_step"
+    # around the first: an ncu launch list of that one solve is
     # `ncu --nvtx --nvtx-include "warm_mixed_step/" --metrics gpu__time_duration.sum`)
     _lib.check(L.deft_grid_profile(sv.grid, 1))
     torch.cuda.nvtx.range_push("warm_mixed_step")
-    warm_step(args.warmup)
+    warm_step(timed_idx[0])
     torch.cuda.nvtx.range_pop()
+    for i in timed_idx[1:]:
+        warm_step(i)
     prof_w = kernel_profile(L, sv.grid)
     _lib.check(L.deft_grid_profile(sv.grid, 1))
-    fp64_step(args.warmup)
+    fp64_step(timed_idx[0])
     prof_64 = kernel_profile(L, sv.grid)
     _lib.check(L.deft_grid_profile(sv.grid, 0))
+    engine_ms_step = sum(v[1] for v in prof_w.values()) / len(timed_idx)
+    prof_w1 = {k: (v[0] / len(timed_idx), v[1] / len(timed_idx)) for k, v in prof_w.items()}
+    fwd_ms = network_forward_ms(L, net, masks[timed_idx[0]], probs[timed_idx[0]], n_ws, stream)
+    host_gap = {"timed_ms_per_step": ms_w, "engine_kernels_ms_per_step": engine_ms_step,
+                "network_forward_ms": fwd_ms,
+                "gap_ms_per_step": ms_w - engine_ms_step - fwd_ms,
+                "note": "timed step minus the summed per-kernel CUDA-event times of the same "
+                        "problems' solves (engine) and the wall time of the network's forward "
+                        "pass: the time the GPU waits on the host (line-search decisions, "
+                        "scalar reads); the forward pass's own launch gaps are not counted "
+                        "in it"}
 
     # end to end through the public API with host buffers: the problem's mask
     # goes in, the converged profile comes out, every step
     mask_host = [torch.tensor(s.mask.reshape(-1)).pin_memory() for s in probs]
-    out_host = torch.empty(probs[0].size, dtype=torch.float64).pin_memory()
+    out_host = {i: torch.empty(probs[0].size, dtype=torch.float64).pin_memory()
+                for i in timed_idx}
     mask_dev = torch.empty_like(masks[0])
-    K2 = args.steps  # the timed steps' problems
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for k in range(K2):
-        i = args.warmup + k
+    for i in timed_idx:
         s = probs[i]
         mask_dev.copy_(mask_host[i], non_blocking=True)
         torch.cuda.current_stream().synchronize()
         sv.set_problem(s, mask_dev.data_ptr())
         used, _, gb = net.initial_density(sv.fmt[MIXED], mask_dev.data_ptr(), s.eta, s.nb,
                                           n_ws.data_ptr(), bulk_gnorm=True)
-        st, _ = sv.solve(MIXED, n_ws.data_ptr(), refine_abs=SWITCH * gb, preconditioned=PC)
-        _lib.check(L.deft_cg_get_x(sv.cg[MIXED], out_host.data_ptr(), 0))
-    e2e_s = (time.perf_counter() - t0) / K2
+        st, _ = sv.solve(MIXED, n_ws.data_ptr(), refine_abs=SWITCH * gb, preconditioned=PC,
+                         gtol=MIXED_GTOL)
+        _lib.check(L.deft_cg_get_x(sv.cg[MIXED], out_host[i].data_ptr(), 0))
+    e2e_s = (time.perf_counter() - t0) / len(timed_idx)
+    err_e2e = [profile_errors(i, out_host[i].to(dd)) for i in timed_idx]
     e2e = {"value": e2e_s, "unit": UNIT, "h2d_bytes_per_step": 8 * probs[0].size,
            "d2h_bytes_per_step": 8 * probs[0].size,
            "api": "pinned host mask -> device, FourierOperator.initial_density "
                   "(deft_fno_initial_density), deft_cg_set_x + deft_cg_solve, deft_cg_get_x "
-                  "to a pinned host buffer"}
+                  "to a pinned host buffer",
+           "profile_vs_fp64_solution": err_summary(err_e2e, gate=True)}
 
     used_net = sum(1 for _, u in st_w if u)
     result = {
@@ -458,18 +558,33 @@ def run_ours(args, rank, world):
                     ("" if args.no_precond else " (density-variable diagonal preconditioner "
                      "n/(kT dV))") + ", Newton refinement on the FP64 gradient (FP32 stage "
                     f"left at {SWITCH:g} of the bulk start's gradient norm)",
+            "gtol_mixed": MIXED_GTOL,
+            "profile_condition": f"max |n - n_FP64| <= {PROFILE_TOL:g} (absolute and relative "
+                                 f"to max n) against the FP64 solution of the same problem "
+                                 f"converged to |grad F| < {REF_GTOL:g} (density-preconditioned "
+                                 f"FP64 CG, {ref_s:.1f} s for the {len(timed_idx)} problems, "
+                                 f"outside the timed region); checked on every timed step",
             "warm_mixed": {"solve_s": ms_w / 1e3, "iters": avg(st_w, "iter"),
                            "evals": avg(st_w, "evals"), "evals_fp64": avg(st_w, "evals_fp64"),
                            "hvps": avg(st_w, "hvps"), "network_used": used_net,
-                           "final_gnorm_fp64": st_w[-1][0].gnorm,
+                           "max_final_gnorm_fp64": max(x[0].gnorm for x in st_w),
+                           "profile_vs_fp64_solution": prof_err_w,
                            "host_wall_split_s": dict(phase_means,
                                                      note="host wall time per timed step: "
                                                           "checked warm start (network "
                                                           "forward + energy checks) and CG")},
             "fp64_bulk": {"solve_s": ms_64 / 1e3, "iters": avg(st_64, "iter"),
-                          "evals": avg(st_64, "evals"), "final_gnorm": st_64[-1][0].gnorm,
-                          "gpu_launches": nl_64},
+                          "evals": avg(st_64, "evals"), "max_final_gnorm":
+                              max(x[0].gnorm for x in st_64),
+                          "gpu_launches": nl_64,
+                          "profile_vs_fp64_solution": prof_err_64,
+                          "note": "plain FP64 CG stopped at |grad F| < 1e-9, the same rule "
+                                  "as the reference's drivers; its profile is not held to "
+                                  "the 1e-8 condition (reported), so this denominator is the "
+                                  "faster, looser solve"},
             "speedup_warm_mixed_vs_fp64": ms_64 / ms_w,
+            "decomposition": decomposition,
+            "host_gap": host_gap,
             "network": net_info,
             "tuning_entries_loaded": tuned,
             "cuda_graphs": "evaluations and Hessian-vector products replayed as graphs in the "
@@ -479,11 +594,11 @@ def run_ours(args, rank, world):
         "gpu_launches": nl_w,
         "clocks": ck_w,
         "clocks_fp64": ck_64,
-        "roofline": roofline(prof_w, N, True, peak, peak_kind),
+        "roofline": roofline(prof_w1, N, True, peak, peak_kind),
         "roofline_fp64": dict(roofline(prof_64, N, False, peak, peak_kind),
                               note="FP64 form: bound by the FP64 pipe (measured 1.0 TFLOP/s "
                                    "FMA on this GB300), not by HBM"),
-        "kernels": kernel_table(prof_w),
+        "kernels": kernel_table(prof_w1),
         "kernels_fp64": kernel_table(prof_64),
     }
     if not args.no_extra:
@@ -495,6 +610,24 @@ def run_ours(args, rank, world):
     net.close()
     sv.close()
     return result
+
+
+def network_forward_ms(L, net, mask, s, n_out, stream, reps=5):
+    """Wall time of the network's forward pass alone (deft_fno_warm_start on
+    the problem's mask, which runs on the network's own stream and
+    synchronises it before returning), median of `reps`, in ms."""
+    import torch
+    from deft_gb300 import _lib
+    times = []
+    for k in range(reps + 1):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        _lib.check(L.deft_fno_warm_start(net.h, mask.data_ptr(), s.eta, s.nb, 1e-3,
+                                         n_out.data_ptr()))
+        torch.cuda.synchronize()
+        if k:
+            times.append(1e3 * (time.perf_counter() - t0))
+    return float(statistics.median(times))
 
 
 def batched_sweep(count=64, seed=3):
@@ -548,28 +681,67 @@ def cpu_baseline(N, s, evals_per_solve, budget_s=20.0):
 # ---------------------------------------------------------------------------
 # reference arm
 
+def _port_warm(task):
+    """Worker warm-up: loads the oracle port and runs one evaluation."""
+    N, i = task
+    from oracle import oracle as O
+    s = held_out(N, i + 1)[i]
+    P = O.Problem(s.lat, s.shape, mu=s.mu, terms=O.HS | O.IDEAL | O.MU, mask=s.mask.reshape(-1))
+    P.energy_grad(s.n0.reshape(-1))
+    return i
+
+
+def _port_solve(task):
+    """One converged solve by the oracle port (the plain-C restatement of the
+    reference path: White Bear + ideal gas + mu + hard-wall constraint, the
+    same secant-search PR-CG from the bulk start as the plain FP64 GPU arm)
+    in a worker process on one core: (index, seconds, evaluations, iterations,
+    final |grad F|)."""
+    N, i, gtol = task
+    from oracle import oracle as O
+    s = held_out(N, i + 1)[i]
+    P = O.Problem(s.lat, s.shape, mu=s.mu, terms=O.HS | O.IDEAL | O.MU, mask=s.mask.reshape(-1))
+    n0 = s.n0.reshape(-1)
+    t0 = time.perf_counter()
+    _, info = P.cg_solve(n0, gtol=gtol, maxiter=20000)
+    return i, time.perf_counter() - t0, info["evals"], info["iters"], info["gnorm"]
+
+
 def run_reference(args, rank, world):
+    """The reference's CPU path on the host cores: every timed step is one
+    full converged solve (|grad F| < 1e-9) of that step's held-out problem by
+    the oracle port, single-threaded as the reference is; the steps run
+    concurrently, one per core, in a spawned process pool.  value = mean
+    seconds per solve.  Warm-up: one evaluation per worker."""
     if rank != 0:
         return None
+    import multiprocessing as mp
+    from oracle import oracle as O
+    O.build()
     N = args.N
-    probs = held_out(N, args.steps + args.warmup)
-
-    def evals_of(i):
-        if N == 128 and i < len(FP64_EVALS_128):
-            return FP64_EVALS_128[i]
-        return FP64_EVALS_MEAN_128
-
-    for i in range(args.warmup):
-        cpu_eval_seconds(probs[i], budget_s=0.0, max_evals=1)
-    samples = []
-    t0 = time.perf_counter()
-    for k in range(args.steps):
-        i = args.warmup + k
-        sec, _k = cpu_eval_seconds(probs[i], budget_s=0.0, max_evals=1)
-        samples.append(sec * evals_of(i))
-    evals = sum(evals_of(args.warmup + k) for k in range(args.steps)) / args.steps
-    wall = time.perf_counter() - t0
-    v = sum(samples) / len(samples)
+    timed_idx = [args.warmup + k for k in range(args.steps)]
+    cores = os.cpu_count() or 1
+    workers = max(1, min(len(timed_idx), cores))
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(workers) as pool:
+        pool.map(_port_warm, [(N, args.warmup)] * workers, chunksize=1)
+        t0 = time.perf_counter()
+        res = list(pool.imap_unordered(_port_solve, [(N, i, GTOL) for i in timed_idx],
+                                       chunksize=1))
+        wall = time.perf_counter() - t0
+    res.sort()
+    bad = [r[0] for r in res if not r[4] < GTOL]
+    if bad:
+        raise RuntimeError(f"oracle port solves of problems {bad} did not converge")
+    secs = [r[1] for r in res]
+    evals = [r[2] for r in res]
+    v = sum(secs) / len(secs)
+    s_per_eval = sum(secs) / sum(evals)
+    sample = (f"{len(res)} full converged solves (|grad F| < {GTOL:g}) of the timed held-out "
+              f"{N}^3 problems by the oracle port (plain-C restatement of the reference path, "
+              f"single-threaded like the reference), {workers} at a time on {workers} of "
+              f"{cores} host cores; mean {statistics.mean(evals):.1f} evaluations per solve, "
+              f"{s_per_eval:.3f} s per evaluation")
     return {
         "impl": "reference",
         "metric": METRIC,
@@ -578,19 +750,19 @@ def run_reference(args, rank, world):
         "n_gpus": world,
         "steps": args.steps,
         "warmup": args.warmup,
-        "ms_per_step": wall / args.steps * 1e3,
+        "ms_per_step": wall / len(res) * 1e3,
         "higher_is_better": False,
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic (seeded wall + solute problems, see config)",
-        "config": config(N, {"parallelism": "single thread (the reference has no threading)"}),
-        "cpu_baseline": {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
-                         "sample": f"per step: one energy+gradient evaluation of the step's "
-                                   f"held-out {N}^3 problem by the oracle port (plain-C "
-                                   f"restatement of the reference path), scaled by that "
-                                   f"problem's evaluation count for a converged FP64 solve "
-                                   f"(mean {evals:.1f})"},
+        "config": config(N, {"parallelism": f"one single-threaded solve per core, {workers} "
+                                            f"concurrent (the reference has no threading)",
+                             "per_step_s": [round(x, 2) for x in secs],
+                             "per_step_evals": evals,
+                             "wall_s_all_steps": wall}),
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": workers, "kind": "port",
+                         "sample": sample},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 

@@ -22,9 +22,11 @@
 // normalisation dV/V folded in.
 #include "fft_smem.cuh"
 #include "fmt_engine.h"
+#include "pencil_fft.cuh"
 #include "wb_phi.cuh"
 
 #include <cmath>
+#include <cstdlib>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -537,6 +539,191 @@ __global__ void DEFT_FFT_BOUNDS(RN) k_x_conv_adj(
     j += j0;
     if (j < J) out[(size_t)e * J + j] = res[idx];
   }
+}
+
+// ---------------------------------------------------------------------------
+// Pencil kernels (FP32, lengths 32/64/128/256): register-resident transforms
+// of 32 adjacent columns per W warps (pencil_fft.cuh), loading and storing
+// global memory directly in 256-byte rows.
+
+// FFT along y of nf complex fields in place.  Columns c = x NzH + kz (all x
+// planes back to back); element y of column c at x Ny NzH + y NzH + kz.
+// grid = (column groups, fields).
+template <int SIGN, int W>
+__global__ void __launch_bounds__(pencil_threads<W>())
+    k_y_pencil(float2 *data, Geom g, const float2 *__restrict__ tw) {
+  constexpr int G = pencil_groups<W>(), P = 16 / W;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, w = warp % W, grp = warp / W;
+  float2 *xs = reinterpret_cast<float2 *>(smem_raw) + grp * pencil_xs_elems<W>();
+  const int c = (blockIdx.x * G + grp) * 32 + lane;
+  const bool act = c < g.Nx * g.NzH;
+  int x, kz;
+  fdivmod(act ? c : 0, g.fNzH, x, kz);
+  float2 *base = data + (size_t)blockIdx.y * g.NC + (size_t)x * g.Ny * g.NzH + kz;
+  const int st = g.NzH;
+  float2 v[16];
+#pragma unroll
+  for (int m = 0; m < 16; m++) v[m] = act ? base[(w + W * m) * st] : make_float2(0.f, 0.f);
+  pencil_n2s<float, SIGN, W>(v, xs, w, lane, tw);
+  if (act) {
+#pragma unroll
+    for (int i = 0; i < P; i++)
+#pragma unroll
+      for (int k2 = 0; k2 < W; k2++) base[(w * P + i + 16 * k2) * st] = v[i * W + k2];
+  }
+}
+
+// Shared weight slots of the pencil convolutions: three FP32 weights (w3,
+// w2, wv; dV/V folded in) for each of a thread's 16 spectral slots,
+// thread-private and conflict-free.
+__device__ __forceinline__ float &pencil_wt(float *wts, int q, int a) {
+  return wts[(q * 3 + a) * blockDim.x + threadIdx.x];
+}
+
+// Weights at the 16 x-frequencies a thread holds of column (y, kz).
+template <int W>
+__device__ __forceinline__ void pencil_weights(float *wts, const Geom &g, int w, int y, int kz,
+                                               float R, float (&kc)[3]) {
+  const float yw = (float)wrapm(y, g.Ny), zf = (float)kz;
+#pragma unroll
+  for (int c = 0; c < 3; c++) kc[c] = g.Bmf[3 * c + 1] * yw + g.Bmf[3 * c + 2] * zf;
+#pragma unroll 1
+  for (int q = 0; q < 16; q++) {
+    const float xw = (float)wrapm(pencil_freq<W>(w, q), g.Nx);
+    const float kx = g.Bmf[0] * xw + kc[0], ky = g.Bmf[3] * xw + kc[1], kzz = g.Bmf[6] * xw + kc[2];
+    float a3, a2, av;
+    weights_at_f(kx * kx + ky * ky + kzz * kzz, R, (float)g.dr, (float)g.scale, a3, a2, av);
+    pencil_wt(wts, q, 0) = a3;
+    pencil_wt(wts, q, 1) = a2;
+    pencil_wt(wts, q, 2) = av;
+  }
+}
+
+// Forward convolution along x (pencil form of k_x_conv_fwd): x-FFT of n^,
+// times the five weights (w3, w2, i k_c wv), five inverse x-FFTs.  Columns
+// j = y NzH + kz < Ny NzH; element x at x Ny NzH + j.
+template <int W>
+__global__ void __launch_bounds__(pencil_threads<W>(), W >= 16 ? 1 : 2)
+    k_x_conv_fwd_pencil(const float2 *__restrict__ in, float2 *__restrict__ out5, Geom g,
+                        const float2 *__restrict__ tw, const LocalArgs *__restrict__ lap) {
+  constexpr int G = pencil_groups<W>();
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, w = warp % W, grp = warp / W;
+  float2 *xs = reinterpret_cast<float2 *>(smem_raw) + grp * pencil_xs_elems<W>();
+  float2 *spec = reinterpret_cast<float2 *>(smem_raw) + G * pencil_xs_elems<W>();
+  float *wts = reinterpret_cast<float *>(spec + 16 * pencil_threads<W>());
+  const int J = g.Ny * g.NzH;
+  const int j = (blockIdx.x * G + grp) * 32 + lane;
+  const bool act = j < J;
+  int y, kz;
+  fdivmod(act ? j : 0, g.fNzH, y, kz);
+  {
+    float2 v[16];
+    const float2 *src = in + j + w * J;
+    const int sW = W * J;
+#pragma unroll
+    for (int m = 0; m < 16; m++) v[m] = act ? src[m * sW] : make_float2(0.f, 0.f);
+    pencil_n2s<float, -1, W>(v, xs, w, lane, tw);
+    // the spectrum waits in thread-private shared slots while the five
+    // weighted copies are transformed back
+#pragma unroll
+    for (int q = 0; q < 16; q++) spec[q * blockDim.x + threadIdx.x] = v[q];
+  }
+  float kc[3];
+  pencil_weights<W>(wts, g, w, y, kz, (float)lap->R, kc);
+#pragma unroll 1
+  for (int a = 0; a < 5; a++) {
+    const float kca = a == 2 ? kc[0] : a == 3 ? kc[1] : kc[2];
+    const float bx = a == 2 ? g.Bmf[0] : a == 3 ? g.Bmf[3] : g.Bmf[6];
+    float2 u[16];
+#pragma unroll
+    for (int q = 0; q < 16; q++) {
+      const float2 v = spec[q * blockDim.x + threadIdx.x];
+      if (a < 2) {
+        const float wt = pencil_wt(wts, q, a);
+        u[q] = make_float2(v.x * wt, v.y * wt);
+      } else {
+        const float xw = (float)wrapm(pencil_freq<W>(w, q), g.Nx);
+        const float wk = (bx * xw + kca) * pencil_wt(wts, q, 2);
+        u[q] = make_float2(-v.y * wk, v.x * wk);  // times i wk
+      }
+    }
+    pencil_s2n<float, +1, W>(u, xs, w, lane, tw);
+    if (act) {
+      float2 *dst = out5 + (size_t)a * g.NC + j + w * J;
+      const int sW = W * J;
+#pragma unroll
+      for (int m = 0; m < 16; m++) dst[m * sW] = u[m];
+    }
+  }
+}
+
+// Adjoint convolution along x (pencil form of k_x_conv_adj): x-FFT of each
+// of the five partial spectra, times its adjoint weight (odd ones negated),
+// summed, one inverse x-FFT.
+template <int W>
+__global__ void __launch_bounds__(pencil_threads<W>(), W >= 16 ? 1 : 2)
+    k_x_conv_adj_pencil(const float2 *__restrict__ in5, float2 *__restrict__ out, Geom g,
+                        const float2 *__restrict__ tw, const LocalArgs *__restrict__ lap) {
+  constexpr int G = pencil_groups<W>();
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, w = warp % W, grp = warp / W;
+  float2 *xs = reinterpret_cast<float2 *>(smem_raw) + grp * pencil_xs_elems<W>();
+  float2 *sum = reinterpret_cast<float2 *>(smem_raw) + G * pencil_xs_elems<W>();
+  float *wts = reinterpret_cast<float *>(sum + 16 * pencil_threads<W>());
+  const int J = g.Ny * g.NzH;
+  const int j = (blockIdx.x * G + grp) * 32 + lane;
+  const bool act = j < J;
+  int y, kz;
+  fdivmod(act ? j : 0, g.fNzH, y, kz);
+  float kc[3];
+  pencil_weights<W>(wts, g, w, y, kz, (float)lap->R, kc);
+  // the weighted sum accumulates in thread-private shared slots
+#pragma unroll 1
+  for (int a = 0; a < 5; a++) {
+    float2 v[16];
+    const float2 *src = in5 + (size_t)a * g.NC + j + w * J;
+    const int sW = W * J;
+#pragma unroll
+    for (int m = 0; m < 16; m++) v[m] = act ? src[m * sW] : make_float2(0.f, 0.f);
+    pencil_n2s<float, -1, W>(v, xs, w, lane, tw);
+    const float kca = a == 2 ? kc[0] : a == 3 ? kc[1] : kc[2];
+    const float bx = a == 2 ? g.Bmf[0] : a == 3 ? g.Bmf[3] : g.Bmf[6];
+#pragma unroll
+    for (int q = 0; q < 16; q++) {
+      float2 o = a == 0 ? make_float2(0.f, 0.f) : sum[q * blockDim.x + threadIdx.x];
+      if (a < 2) {
+        const float wt = pencil_wt(wts, q, a);
+        o.x += v[q].x * wt;
+        o.y += v[q].y * wt;
+      } else {
+        const float xw = (float)wrapm(pencil_freq<W>(w, q), g.Nx);
+        const float wk = (bx * xw + kca) * pencil_wt(wts, q, 2);
+        o.x += v[q].y * wk;  // times -i wk
+        o.y -= v[q].x * wk;
+      }
+      sum[q * blockDim.x + threadIdx.x] = o;
+    }
+  }
+  float2 acc[16];
+#pragma unroll
+  for (int q = 0; q < 16; q++) acc[q] = sum[q * blockDim.x + threadIdx.x];
+  pencil_s2n<float, +1, W>(acc, xs, w, lane, tw);
+  if (act) {
+    float2 *dst = out + j + w * J;
+    const int sW = W * J;
+#pragma unroll
+    for (int m = 0; m < 16; m++) dst[m * sW] = acc[m];
+  }
+}
+
+// Shared memory of the pencil kernels: the exchange buffers, plus, for the
+// convolutions, a spectrum (or sum) slot and three weight slots per
+// frequency a thread holds.
+template <int W> constexpr size_t pencil_smem(bool conv) {
+  return sizeof(float2) * pencil_groups<W>() * pencil_xs_elems<W>() +
+         (conv ? (sizeof(float2) * 16 + sizeof(float) * 48) * pencil_threads<W>() : 0);
 }
 
 // Ideal-gas integrand kT n (ln(n/nQ) - 1) (src/IdealGas.cpp:68-72), 0 at
@@ -1568,6 +1755,21 @@ class EngineImpl {
       set_smem(k_z_jac<float, RN>, t32.smem_phi);
       set_smem(k_z_hvp_out<float, RN>, t32.smem_z);
     };
+    auto smemp = [&](auto wc) {
+      constexpr int W = decltype(wc)::value;
+      set_smem(k_y_pencil<-1, W>, pencil_smem<W>(false));
+      set_smem(k_y_pencil<+1, W>, pencil_smem<W>(false));
+      set_smem(k_x_conv_fwd_pencil<W>, pencil_smem<W>(true));
+      set_smem(k_x_conv_adj_pencil<W>, pencil_smem<W>(true));
+    };
+    smemp(std::integral_constant<int, 2>());
+    smemp(std::integral_constant<int, 4>());
+    smemp(std::integral_constant<int, 8>());
+    smemp(std::integral_constant<int, 16>());
+    {
+      const char *ev = getenv("DEFT_PENCIL");
+      pencil_on = !(ev && ev[0] == '0');
+    }
     smem32(std::integral_constant<int, 0>());
     smem32(std::integral_constant<int, 32>());
     smem32(std::integral_constant<int, 64>());
@@ -1686,11 +1888,47 @@ class EngineImpl {
       for (int i = 0; i < 8; i++) c->radix[a][i] = i < pl[a]->npass ? pl[a]->radix[i] : 0;
   }
 
+  // Pencil kernels for the FP32 x and y transforms of lengths 32..256
+  // (DEFT_PENCIL=0 in the environment at grid creation selects the
+  // shared-memory Stockham kernels instead).
+  bool pencil_on = true;
+  template <typename T> bool pencil(int axis) const {
+    return std::is_same<T, float>::value && pencil_on &&
+           pencil_w(axis == 0 ? g.Nx : axis == 1 ? g.Ny : g.Nz) > 0;
+  }
+  // Calls f(std::integral_constant<int, W>()) for the pencil width of length L.
+  template <typename F> static void with_w(int L, F &&f) {
+    switch (L) {
+      case 32: f(std::integral_constant<int, 2>()); break;
+      case 64: f(std::integral_constant<int, 4>()); break;
+      case 128: f(std::integral_constant<int, 8>()); break;
+      default: f(std::integral_constant<int, 16>()); break;
+    }
+  }
+
   template <typename T> void y_fft(typename Cplx<T>::type *data, int nf, int sign) {
     const Tiles &t = tl<T>();
     dim3 grid((g.NzH + t.By - 1) / t.By, g.Nx, nf);
     const int kid = kslot<T>(nf == 1 ? kK_y_fft1 : kK_y_fft5);
     pre(kid);
+    if constexpr (std::is_same<T, float>::value) {
+      if (pencil<T>(1)) {
+        with_w(g.Ny, [&](auto wc) {
+          constexpr int W = decltype(wc)::value;
+          const int cols = 32 * pencil_groups<W>();
+          const dim3 pg((g.Nx * g.NzH + cols - 1) / cols, nf);
+          const float2 *tw = reinterpret_cast<const float2 *>(plan<T>(1).tw);
+          if (sign < 0)
+            k_y_pencil<-1, W><<<pg, pencil_threads<W>(), pencil_smem<W>(false), stream>>>(
+                reinterpret_cast<float2 *>(data), g, tw);
+          else
+            k_y_pencil<+1, W><<<pg, pencil_threads<W>(), pencil_smem<W>(false), stream>>>(
+                reinterpret_cast<float2 *>(data), g, tw);
+        });
+        post(kid);
+        return;
+      }
+    }
     with_rn<T>(plan<T>(1), [&](auto rn) {
       constexpr int RN = decltype(rn)::value;
       if (sign < 0)
@@ -1701,6 +1939,27 @@ class EngineImpl {
     post(kid);
   }
   int x_tiles(int B) const { return (g.Ny * g.NzH + B - 1) / B; }
+
+  // Queues the adjoint x convolution: spec5 -> spec0.
+  template <typename T> void x_conv_adj() {
+    const Tiles &t = tl<T>();
+    if (pencil<T>(0)) {
+      with_w(g.Nx, [&](auto wc) {
+        constexpr int W = decltype(wc)::value;
+        const int cols = 32 * pencil_groups<W>();
+        k_x_conv_adj_pencil<W><<<(g.Ny * g.NzH + cols - 1) / cols, pencil_threads<W>(),
+                                 pencil_smem<W>(true), stream>>>(
+            reinterpret_cast<const float2 *>(spec5<T>()), reinterpret_cast<float2 *>(spec0<T>()),
+            g, reinterpret_cast<const float2 *>(plan<T>(0).tw), la_dev);
+      });
+      return;
+    }
+    with_rn<T>(plan<T>(0), [&](auto rn) {
+      k_x_conv_adj<T, decltype(rn)::value><<<x_tiles(t.Bxc), kThreads, t.smem_xc, stream>>>(
+          spec5<T>(), spec0<T>(), table<T>(0), table<T>(1), table<T>(2), g, plan<T>(0), t.fBxc,
+          t.f5Bxc, la_dev);
+    });
+  }
 
   // Queues z r2c, y FFT, x convolution and inverse y of n (the weight table
   // for f.R must be current: ensure_table runs outside any graph capture).
@@ -1714,11 +1973,22 @@ class EngineImpl {
     post(kslot<T>(kK_z_r2c));
     y_fft<T>(spec0<T>(), 1, -1);
     pre(kslot<T>(kK_x_conv_fwd));
-    with_rn<T>(plan<T>(0), [&](auto rn) {
-      k_x_conv_fwd<T, decltype(rn)::value><<<x_tiles(t.Bxf), kThreads, t.smem_xf, stream>>>(
-          spec0<T>(), spec5<T>(), table<T>(0), table<T>(1), table<T>(2), g, plan<T>(0), t.fBxf,
-          la_dev);
-    });
+    if (pencil<T>(0)) {
+      with_w(g.Nx, [&](auto wc) {
+        constexpr int W = decltype(wc)::value;
+        const int cols = 32 * pencil_groups<W>();
+        k_x_conv_fwd_pencil<W><<<(g.Ny * g.NzH + cols - 1) / cols, pencil_threads<W>(),
+                                 pencil_smem<W>(true), stream>>>(
+            reinterpret_cast<const float2 *>(spec0<T>()), reinterpret_cast<float2 *>(spec5<T>()),
+            g, reinterpret_cast<const float2 *>(plan<T>(0).tw), la_dev);
+      });
+    } else {
+      with_rn<T>(plan<T>(0), [&](auto rn) {
+        k_x_conv_fwd<T, decltype(rn)::value><<<x_tiles(t.Bxf), kThreads, t.smem_xf, stream>>>(
+            spec0<T>(), spec5<T>(), table<T>(0), table<T>(1), table<T>(2), g, plan<T>(0), t.fBxf,
+            la_dev);
+      });
+    }
     post(kslot<T>(kK_x_conv_fwd));
     y_fft<T>(spec5<T>(), 5, +1);
     return check("forward convolution");
@@ -1939,11 +2209,7 @@ class EngineImpl {
       if (grad) {
         y_fft<T>(spec5<T>(), 5, -1);
         pre(kslot<T>(kK_x_conv_adj));
-        with_rn<T>(plan<T>(0), [&](auto rn) {
-          k_x_conv_adj<T, decltype(rn)::value><<<x_tiles(t.Bxc), kThreads, t.smem_xc, stream>>>(
-              spec5<T>(), spec0<T>(), table<T>(0), table<T>(1), table<T>(2), g, plan<T>(0),
-              t.fBxc, t.f5Bxc, la_dev);
-        });
+        x_conv_adj<T>();
         post(kslot<T>(kK_x_conv_adj));
         y_fft<T>(spec0<T>(), 1, +1);
       }
@@ -2009,12 +2275,7 @@ class EngineImpl {
       post(kslot<float>(kK_z_jac));
       y_fft<float>(spec5<float>(), 5, -1);
       pre(kslot<float>(kK_x_conv_adj));
-      with_rn<float>(plan<float>(0), [&](auto rn) {
-        k_x_conv_adj<float, decltype(rn)::value><<<x_tiles(t32.Bxc), kThreads, t32.smem_xc,
-                                                   stream>>>(
-            spec5<float>(), spec0<float>(), table<float>(0), table<float>(1), table<float>(2), g,
-            plan<float>(0), t32.fBxc, t32.f5Bxc, la_dev);
-      });
+      x_conv_adj<float>();
       post(kslot<float>(kK_x_conv_adj));
       y_fft<float>(spec0<float>(), 1, +1);
     }
@@ -2270,21 +2531,24 @@ void Engine::profile_get(int i, const char **name, long long *launches, double *
 // forbids allocation once it has started.  This entry point takes its scratch
 // (spectra, weight table, twiddles, per-block partial energies) from one
 // file-scope device array of kNoAllocScratchBytes, which every GPU that loads
-// this library holds until the process exits.  Every call shares it and it
-// keeps the last call's contents; each call rewrites everything it reads, so
-// nothing has to start at zero.  Calls that overlap on the GPU (two streams,
-// or two host threads) race on the array.
+// this library holds until the process exits.  The array gets its device
+// memory when this library's GPU module is loaded on a device: under CUDA's
+// default lazy module loading that is the first call into the library on that
+// device (at once at start-up with CUDA_MODULE_LOADING=EAGER), so a caller
+// whose framework reserves the GPU's memory should make its first call before
+// the framework takes its pool.  Every call shares the array and it keeps the
+// last call's contents; each call rewrites everything it reads, so nothing
+// has to start at zero.  Calls that overlap on the GPU (two streams, or two
+// host threads) race on the array.  A call copies pageable host memory
+// (twiddles, parameters, results) and synchronises its stream, so it cannot
+// be made inside a CUDA stream capture.
 
 constexpr size_t kNoAllocScratchBytes = size_t(20) << 20;  // 20 MiB
 constexpr int kNoAllocMaxAxis = 256;
-constexpr int kNoAllocMaxDevices = 64;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
 namespace {
-std::mutex g_noalloc_mu;
-void *g_noalloc_ptr[kNoAllocMaxDevices] = {};
-
 size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 
 bool noalloc_fail(std::string *err, const std::string &m) {
@@ -2380,30 +2644,20 @@ int noalloc_energy_grad(const GridSpec &s, const FmtSpec &f, const double *n, co
     return 1;
   }
 
-  // ---- per-device set-up: the device address of the scratch array
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) {
-    noalloc_fail(err, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
-    return 2;
-  }
-  if (dev < 0 || dev >= kNoAllocMaxDevices) {
-    noalloc_fail(err, "device index out of range");
-    return 1;
-  }
+  // ---- the device address of the scratch array on the current device.
+  // Looked up on every call (cheap next to the synchronisation at the end),
+  // so the address is never stale: after a cudaDeviceReset the module is
+  // loaded again and the array gets a new address.
+  cudaError_t e = cudaSuccess;
   unsigned char *base = nullptr;
   {
-    std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (!g_noalloc_ptr[dev]) {
-      void *p = nullptr;
-      e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-      if (e != cudaSuccess || !p) {
-        noalloc_fail(err, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-        return 2;
-      }
-      g_noalloc_ptr[dev] = p;
+    void *p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) {
+      noalloc_fail(err, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+      return 2;
     }
-    base = static_cast<unsigned char *>(g_noalloc_ptr[dev]);
+    base = static_cast<unsigned char *>(p);
   }
   double2 *tw_x = reinterpret_cast<double2 *>(base + o_twx);
   double2 *tw_y = reinterpret_cast<double2 *>(base + o_twy);

@@ -267,16 +267,18 @@ class Solver:
             check(self.L.deft_fmt_set_params(f, ctypes.byref(p)))
             check(self.L.deft_fmt_set_mask(f, mask_ptr, 1))
 
-    def solve(self, precision, n0_ptr, refine_abs=0.0, preconditioned=_lib.PC_NONE):
+    def solve(self, precision, n0_ptr, refine_abs=0.0, preconditioned=_lib.PC_NONE, gtol=None,
+              maxiter=20000):
         """Solve from the device array n0_ptr; returns (CgStatus, seconds).
         refine_abs > 0 sets the mixed form's FP32-stage exit |grad| < refine_abs;
         preconditioned = PC_DENSITY runs the CG with the density-variable
-        diagonal preconditioner.
+        diagonal preconditioner; gtol overrides the solver's tolerance for
+        this solve.
         A minimiser that stops without converging (line search, iteration
         limit, non-finite values) is reported in CgStatus.status, not raised."""
         t0 = time.perf_counter()
-        cp = _lib.CgParams(_lib.LS_SECANT, self.gtol, 20000, 1.0, 0.0, 0.0, int(preconditioned),
-                           float(refine_abs))
+        cp = _lib.CgParams(_lib.LS_SECANT, self.gtol if gtol is None else float(gtol),
+                           int(maxiter), 1.0, 0.0, 0.0, int(preconditioned), float(refine_abs))
         check(self.L.deft_cg_set_params(self.cg[precision], ctypes.byref(cp)))
         check(self.L.deft_cg_set_x(self.cg[precision], n0_ptr, 1))
         st = _lib.CgStatus()

@@ -244,10 +244,15 @@ int deft_find_chemical_potential(double R, double kT, double nb, double *mu_out)
  * n, V, mask and grad_out are device pointers on the CURRENT device; lat, p,
  * E_out and terms_out are host pointers.  Work runs on `stream` (a
  * cudaStream_t, NULL = default stream) and is synchronised before return.
- * The first call on each device looks up the array's device address; make
- * that first call before any stream capture.  Every call shares the array
- * and overwrites it, so calls that overlap on the GPU (other streams or
- * host threads) race. */
+ * The array gets its device memory when the library's GPU module is loaded
+ * on a device: with CUDA's default lazy module loading, at the first call
+ * into the library on that device (with CUDA_MODULE_LOADING=EAGER, when the
+ * device's context is created).  A caller whose framework reserves the GPU's
+ * memory should therefore make its first call (any size) before the
+ * framework takes its pool.  The call copies pageable host memory and
+ * synchronises its stream, so it cannot be used inside a CUDA stream
+ * capture.  Every call shares the array and overwrites it, so calls that
+ * overlap on the GPU (other streams or host threads) race. */
 int deft_fmt_energy_grad_noalloc(const double lat[9], int Nx, int Ny, int Nz,
                                  const deft_fmt_params *p, const double *n, const double *V,
                                  const double *mask, double *E_out, double *grad_out,

@@ -24,13 +24,22 @@ def _slit(N=32, Nxy=8):
     return Slit(N=N, dx=0.2, eta=0.3, Nxy=Nxy, seed=1)
 
 
-@pytest.mark.parametrize("shape", [(8, 8, 32), (16, 12, 15), (48, 20, 10)])
-def test_mixed_energy_grad_vs_oracle(ctx, oracle_mod, shape):
+FCC = np.array([[0, 1.0, 1.0], [1.0, 0, 1.0], [1.0, 1.0, 0.0]])
+
+
+# Shapes with x and y lengths of 32..256 run the register-resident pencil
+# kernels for the x and y transforms; the others the shared-memory passes.
+@pytest.mark.parametrize("shape,lat_kind", [
+    ((8, 8, 32), "ortho"), ((16, 12, 15), "ortho"), ((48, 20, 10), "ortho"),
+    ((32, 32, 16), "ortho"), ((64, 32, 20), "ortho"), ((32, 128, 12), "ortho"),
+    ((256, 32, 8), "ortho"), ((32, 64, 24), "fcc"), ((64, 64, 64), "fcc")])
+def test_mixed_energy_grad_vs_oracle(ctx, oracle_mod, shape, lat_kind):
     from deft_gb300 import _lib
     from tests.capi import Fmt, Grid
     O = oracle_mod
     rng = np.random.default_rng(4)
-    lat = np.diag([0.2 * s for s in shape])
+    lat = np.diag([0.2 * s for s in shape]) if lat_kind == "ortho" else \
+        FCC * (0.15 * max(shape))
     nb = 0.3 / (4 * math.pi / 3)
     mu = O.find_mu(1.0, 1.0, nb)
     n = nb * (1 + 0.2 * rng.standard_normal(int(np.prod(shape))))
@@ -45,12 +54,14 @@ def test_mixed_energy_grad_vs_oracle(ctx, oracle_mod, shape):
     g.close()
 
 
-def test_hessian_vector_matches_fp64_gradient_difference(ctx, oracle_mod):
-    """H dx against (g(n + e dx) - g(n - e dx)) / 2e of the FP64 gradient."""
+@pytest.mark.parametrize("Nxy", [8, 32])
+def test_hessian_vector_matches_fp64_gradient_difference(ctx, oracle_mod, Nxy):
+    """H dx against (g(n + e dx) - g(n - e dx)) / 2e of the FP64 gradient
+    (Nxy = 32: pencil x and y transforms)."""
     from deft_gb300 import _lib
     from tests.capi import Fmt, Grid
     O = oracle_mod
-    s = _slit()
+    s = _slit(Nxy=Nxy)
     size = s.size
     mask = s.mask.reshape(-1)
     rng = np.random.default_rng(8)
@@ -72,11 +83,12 @@ def test_hessian_vector_matches_fp64_gradient_difference(ctx, oracle_mod):
     g.close()
 
 
-def test_mixed_solve_reaches_fp64_tolerance_and_profile(ctx, oracle_mod):
+@pytest.mark.parametrize("Nxy", [8, 32])
+def test_mixed_solve_reaches_fp64_tolerance_and_profile(ctx, oracle_mod, Nxy):
     from deft_gb300 import _lib
     from tests.capi import CG, Fmt, Grid
     O = oracle_mod
-    s = _slit()
+    s = _slit(Nxy=Nxy)
     mask = s.mask.reshape(-1)
     g = Grid(ctx, s.lat, s.shape)
     f = Fmt(g, mu=s.mu, terms=O.HS | O.IDEAL | O.MU | O.MASK, mask=mask,

@@ -135,12 +135,16 @@ def test_finite_difference_gradient(ctx, oracle_mod):
     g = _grid(ctx, lat, N)
     f = Fmt(g, R=P.R, kT=P.kT, mu=P.mu, terms=P.terms)
     E0, grad, _ = f.energy_grad(n)
-    d = grad / np.linalg.norm(grad)
+    # Direction n * grad (normalised): a step stays inside n > 0 up to
+    # eps = min(n / |d|), which is large, so the schedule can start where the
+    # central difference's O(eps^2) error dominates rounding and the
+    # convergence-rate rule has something to measure.
+    d = n * grad
+    d /= np.linalg.norm(d)
     lderiv = d @ grad
     eps_max = 1e-15 * abs(E0) / abs(lderiv) / 1e-15
     min_p = int(-math.floor(math.log10(eps_max) + 0.5))
-    # start no larger than a step that keeps every density positive
-    min_p = max(min_p, int(math.ceil(-math.log10(0.1 * n.min() / np.abs(d).max()))))
+    min_p = max(min_p, int(math.ceil(-math.log10(0.5 * np.min(n / np.abs(d))))))
     grads, best, mn = [], 1.0, 1e300
     for p in range(min_p, min_p + 8):
         eps = 10.0 ** (-p)
@@ -148,10 +152,11 @@ def test_finite_difference_gradient(ctx, oracle_mod):
         Em, _ = f.energy(n - eps * d)
         grads.append((Ep - Em) / (2 * eps))
         best = min(best, abs(grads[-1] / lderiv - 1))
-        if len(grads) > 1:
+        if len(grads) > 1 and grads[-1] != grads[-2]:
             diff = (grads[-2] - lderiv) * (-1 + 1 / 100.0) / (grads[-1] - grads[-2])
             mn = min(mn, abs(diff - 1))
-    assert (mn < 1e-3 and best < 1e-7) or best < 1e-10 or (mn < 1e-5 and best < 0.01)
+    # the reference's first pass branch: reasonable scaling and accuracy
+    assert mn < 1e-3 and best < 1e-7, (mn, best)
     f.close()
     g.close()
 

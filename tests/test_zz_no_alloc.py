@@ -22,7 +22,14 @@ G_TOL = 1e-9
 
 
 def _case(kind):
-    rng = np.random.default_rng(17 if kind == "slit" else 23)
+    rng = np.random.default_rng({"slit": 17, "fcc": 23, "local": 29}[kind])
+    if kind == "local":
+        # local terms only (no hard spheres): ideal gas, mu and V_ext
+        N = (12, 10, 14)
+        lat = np.diag([2.4, 2.0, 2.8])
+        n = 0.05 * (1 + 0.2 * rng.standard_normal(int(np.prod(N))))
+        V = 0.3 * rng.standard_normal(n.size)
+        return N, lat, 1.0, n, V, None
     if kind == "slit":
         N = (24, 20, 32)
         lat = np.diag([4.8, 4.0, 6.4])
@@ -75,9 +82,13 @@ def test_noalloc_matches_regular_entry_point_twice():
     _lib.check(L.deft_ctx_create(0, ctypes.byref(ctx)))
     stream = torch.cuda.current_stream()
     try:
-        for kind in ("slit", "fcc"):  # two calls in a row sharing the scratch array
+        # three calls in a row sharing the scratch array; the last has no
+        # hard-sphere term (the local-terms branch)
+        for kind in ("slit", "fcc", "local"):
             N, lat, R, n, V, mask = _case(kind)
-            terms = _lib.TERM_HS | _lib.TERM_IDEAL | _lib.TERM_MU
+            terms = _lib.TERM_IDEAL | _lib.TERM_MU
+            if kind != "local":
+                terms |= _lib.TERM_HS
             if V is not None:
                 terms |= _lib.TERM_VEXT
             if mask is not None:
@@ -123,3 +134,69 @@ def test_noalloc_rejects_oversized_grid():
                                        g.ctypes.data, None, None)
     assert s == _lib.ERR_ARG
     assert b"scratch" in L.deft_last_error()
+
+
+FIRST_CALL_CHILD = r"""
+import ctypes, json, sys
+import numpy as np
+import torch
+sys.path.insert(0, sys.argv[1])
+from deft_gb300 import _lib
+from tests.test_zz_no_alloc import _case
+free, total = torch.cuda.mem_get_info()
+hold = torch.empty(int(free * 0.9), dtype=torch.uint8, device="cuda")  # the framework's pool
+L = _lib.load()
+N, lat, R, n, V, mask = _case("fcc")
+terms = _lib.TERM_HS | _lib.TERM_IDEAL | _lib.TERM_MU | _lib.TERM_VEXT
+params = _lib.FmtParams(R, 1.0, -2.0, terms)
+lat9 = np.ascontiguousarray(lat.reshape(9), dtype=np.float64)
+nd = torch.tensor(n, dtype=torch.float64, device="cuda")
+Vd = torch.tensor(V, dtype=torch.float64, device="cuda")
+grad = torch.empty_like(nd)
+E = ctypes.c_double()
+torch.cuda.synchronize()
+s = L.deft_fmt_energy_grad_noalloc(lat9.ctypes.data, *N, ctypes.byref(params), nd.data_ptr(),
+                                   Vd.data_ptr(), None, ctypes.addressof(E), grad.data_ptr(),
+                                   None, None)
+out = {"status": s, "msg": L.deft_last_error().decode(), "E": E.value,
+       "grad": grad.cpu().numpy().tolist(), "held_gb": hold.numel() / 1e9}
+del hold
+torch.cuda.empty_cache()
+ctx = ctypes.c_void_p()
+_lib.check(L.deft_ctx_create(0, ctypes.byref(ctx)))
+g = ctypes.c_void_p()
+_lib.check(L.deft_grid_create(ctx, lat9.ctypes.data, *N, ctypes.byref(g)))
+f = ctypes.c_void_p()
+_lib.check(L.deft_fmt_create(g, ctypes.byref(params), ctypes.byref(f)))
+_lib.check(L.deft_fmt_set_vext(f, Vd.data_ptr(), 1))
+g2 = torch.empty_like(nd)
+E2 = ctypes.c_double()
+_lib.check(L.deft_fmt_energy_grad(f, nd.data_ptr(), 1, ctypes.addressof(E2), g2.data_ptr(), None))
+out["E_ref"] = E2.value
+out["grad_ref"] = g2.cpu().numpy().tolist()
+L.deft_fmt_destroy(f)
+L.deft_grid_destroy(g)
+L.deft_ctx_destroy(ctx)
+print(json.dumps(out))
+"""
+
+
+def test_noalloc_first_call_after_framework_reserved_memory():
+    """A fresh process whose framework (torch here) has taken 90 % of the
+    free device memory before its first call into the library: the first
+    call is the allocation-free entry point, which must still succeed (its
+    array comes with the library's module) and agree with the regular entry
+    point, called afterwards once the pool is released."""
+    import json
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([sys.executable, "-c", FIRST_CALL_CHILD, root], capture_output=True,
+                       text=True, timeout=300, cwd=root)
+    assert r.returncode == 0, r.stderr[-2000:]
+    out = json.loads(r.stdout.strip().splitlines()[-1])
+    assert out["status"] == 0, out["msg"]
+    assert abs(out["E"] / out["E_ref"] - 1) < E_TOL
+    g, g_ref = np.array(out["grad"]), np.array(out["grad_ref"])
+    assert np.abs(g - g_ref).max() <= G_TOL * np.abs(g_ref).max()
