@@ -136,6 +136,11 @@ def ref():
         L.ref_pcg.argtypes = [_dp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                               ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int, _dp,
                               _dp, _dp, ctypes.c_int, ctypes.c_double, _dp]
+        L.ref_pcg_precision.restype = ctypes.c_int
+        L.ref_pcg_precision.argtypes = [_dp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                        ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                        ctypes.c_int, ctypes.c_int, _dp, _dp, _dp, ctypes.c_int,
+                                        ctypes.c_double, ctypes.c_double, _dp]
         L.ref_fft_count.restype = ctypes.c_longlong
         L.ref_set_hs.argtypes = [ctypes.c_int]
         L.ref_new_minimize.restype = ctypes.c_int
@@ -331,6 +336,18 @@ class Problem:
         k = self._ref().ref_pcg(_ptr(self.lat), *self.N, self.R, self.kT, self.mu, self.terms,
                           int(bool(self.terms & VEFF)), _ptr(self.V), _ptr(self.mask), _ptr(x),
                           iters, step, _ptr(e))
+        return x, e[:k]
+
+    def ref_pcg_precision(self, x, iters, step, precision):
+        """Precision(precision, PreconditionedConjugateGradient(...)) of the
+        reference: (x after, energies after each improve_energy() call, the
+        last call being the one that returned false, if any)."""
+        x = np.array(x, dtype=np.float64).reshape(-1)
+        e = np.zeros(iters)
+        k = self._ref().ref_pcg_precision(_ptr(self.lat), *self.N, self.R, self.kT, self.mu,
+                                          self.terms, int(bool(self.terms & VEFF)), _ptr(self.V),
+                                          _ptr(self.mask), _ptr(x), iters, step, precision,
+                                          _ptr(e))
         return x, e[:k]
 
     def ref_cg(self, n, iters, step=0.1):

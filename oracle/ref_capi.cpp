@@ -313,6 +313,39 @@ double ref_homogeneous(double R, double kT, double mu, double nb) {
   return f(kT, nb);
 }
 
+// The stop rule of the paper drivers (papers/contact/figs/walls.cpp:104-110):
+// Precision(precision, PreconditionedConjugateGradient(f, gd, kT, &x,
+// QuadraticLineMinimizer, step)) (src/Precision.cpp:53-151 wrapped around
+// src/ConjugateGradient.cpp:115-160), improve_energy() called until it
+// returns false or `iters` calls; energies[] gets the energy after each
+// call.  Returns the number of calls made, the last one included.
+int ref_pcg_precision(const double *lat, int Nx, int Ny, int Nz, double R, double kT, double mu,
+                      int terms, int veff, const double *V, const double *mask,
+                      double *x_inout, int iters, double step, double precision,
+                      double *energies) {
+  GridDescription gd(make_lat(lat), Nx, Ny, Nz);
+  Functional f = make_sum(gd, R, mu, terms, V);
+  if (veff) f = OfEffectivePotential(f);
+  if (terms & REF_MASK) {
+    Grid m(gd);
+    for (int i = 0; i < gd.NxNyNz; i++) m[i] = mask[i];
+    f = constrain(m, f);
+  }
+  Grid x(gd);
+  for (int i = 0; i < gd.NxNyNz; i++) x[i] = x_inout[i];
+  Minimizer min = Precision(precision, PreconditionedConjugateGradient(f, gd, kT, &x,
+                                                                       QuadraticLineMinimizer,
+                                                                       step));
+  int i = 0;
+  for (; i < iters; i++) {
+    bool more = min.improve_energy(false);
+    energies[i] = min.energy();
+    if (!more) { i++; break; }
+  }
+  for (int j = 0; j < gd.NxNyNz; j++) x_inout[j] = x[j];
+  return i;
+}
+
 // Runs `iters` calls of ConjugateGradient(...).improve_energy()
 // (src/ConjugateGradient.cpp:59-108) with QuadraticLineMinimizer
 // (src/QuadraticLineMinimizer.cpp:27-198) on the constrained functional,

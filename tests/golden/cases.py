@@ -65,6 +65,24 @@ def cg_case():
     return P, n, 6, 0.1
 
 
+def precision_case():
+    """The stop rule of the paper drivers on the cg_case slit
+    (papers/contact/figs/walls.cpp:86-110): effective-potential variable
+    started at -kT ln((eta mask + 1e-4 eta) / (4 pi / 3)), precision =
+    |F_bulk(nb) x slit volume| x 1e-4, PreconditionedConjugateGradient with
+    QuadraticLineMinimizer at the default step 10.  Returns (problem, x0,
+    precision, step, iteration cap)."""
+    P, _, _, _ = cg_case()
+    P.terms |= O.VEFF
+    eta = 0.3
+    mask = P.mask
+    x0 = -P.kT * np.log((eta * mask + 1e-4 * eta) / (4 * math.pi / 3))
+    nb = eta / (4 * math.pi / 3)
+    dV = P.dvolume()
+    approx = O.lib().oracle_homogeneous(P.R, P.kT, P.mu, nb) * float(mask.sum()) * dV
+    return P, x0, abs(approx * 1e-4), 10.0, 100
+
+
 def veff_case():
     """The cg_case slit in the effective-potential variable, as
     papers/contact/figs/walls.cpp:86-101 sets it up: x = -kT ln n with the wall

@@ -19,7 +19,7 @@ sys.path.insert(0, ROOT)
 
 from oracle import oracle as O  # noqa: E402
 from tests.golden.cases import (CASES, HS_CASES, SAFT_CASES, WATER_SAFT, cg_case,  # noqa: E402
-                                make_case, saft_case, veff_case)
+                                make_case, precision_case, saft_case, veff_case)
 
 
 def main():
@@ -89,6 +89,15 @@ def main():
     x, e = P.ref_pcg(xv, iters, step=step)
     out["pcg_quadratic"] = {"energies": [float(v) for v in e], "iters": iters, "step": step}
     arrays["pcg_quadratic_x"] = x
+    # the drivers' Precision stop rule around PreconditionedConjugateGradient
+    P, x0, prec, step, cap = precision_case()
+    x, e = P.ref_pcg_precision(x0, cap, step, prec)
+    out["pcg_precision"] = {"energies": [float(v) for v in e], "calls": len(e),
+                            "precision": prec, "step": step}
+    # and with the precision 1e4 times tighter (more calls of the rule)
+    x, e = P.ref_pcg_precision(x0, cap, step, prec * 1e-4)
+    out["pcg_precision_tight"] = {"energies": [float(v) for v in e], "calls": len(e),
+                                  "precision": prec * 1e-4, "step": step}
     with open(os.path.join(HERE, "reference_values.json"), "w") as f:
         json.dump(out, f, indent=1, sort_keys=True)
     np.savez_compressed(os.path.join(HERE, "reference_fields.npz"), **arrays)

@@ -235,3 +235,35 @@ def test_full_size_energy_grad(ctx, oracle_mod, N):
     assert np.abs(grad - gr).max() <= G_TOL * np.abs(gr).max()
     f.close()
     g.close()
+
+
+def test_config1_slit_64_solve_matches_oracle(ctx, oracle_mod):
+    """The 64^3 hard-wall slit at its stated size (dx = 0.2, walls at z = 0
+    and z = 6.4, eta = 0.3, smoothed-noise start, seed 1): plain FP64 CG to
+    |grad F| < 1e-9.  The converged profile is within 1e-8 of the oracle's
+    1-D solution (1 x 1 x 64 grid, same cell volume, converged to 1e-13) and
+    the free energy within 1e-10 of 64 x 64 times the 1-D energy.  (F and the
+    gradient at the start are compared in test_full_size_energy_grad.)"""
+    from tests.capi import CG, Fmt
+    from deft_gb300.workloads import Slit
+    O = oracle_mod
+    s = Slit(N=64, dx=0.2, eta=0.3, seed=1)
+    assert abs(s.width - 6.4) < 1e-12
+    g = _grid(ctx, s.lat, s.shape)
+    f = Fmt(g, R=1.0, kT=1.0, mu=s.mu, terms=O.HS | O.IDEAL | O.MU | O.MASK,
+            mask=s.mask.reshape(-1))
+    cg = CG(f, gtol=1e-9, maxiter=5000, step=1.0)
+    cg.set_x(s.n0.reshape(-1))
+    code, st = cg.solve()
+    assert code == 0 and st.converged and st.gnorm < 1e-9
+    n = cg.get_x().reshape(s.shape)
+    E, _ = f.energy(n.reshape(-1))
+    P1 = O.Problem(np.diag([s.dx, s.dx, s.L]), (1, 1, s.shape[2]), mu=s.mu,
+                   terms=O.HS | O.IDEAL | O.MU, mask=s.mask[0, 0].copy())
+    x1, info = P1.cg_solve(np.where(s.mask[0, 0] > 0, s.nb, 0.0), gtol=1e-13, maxiter=20000)
+    assert info["gnorm"] < 1e-12
+    assert np.abs(n - x1[None, None, :]).max() < 1e-8
+    assert abs(E / (P1.energy(x1) * s.shape[0] * s.shape[1]) - 1) < E_TOL
+    cg.close()
+    f.close()
+    g.close()

@@ -151,3 +151,33 @@ def test_mixed_form_in_effective_potential_refines_in_fp64(oracle_mod):
         assert np.abs(n - no)[free].max() <= 1e-8 * no[free].max()
     finally:
         _close(cg, f, g, ctx)
+
+
+@pytest.mark.parametrize("key", ["pcg_precision", "pcg_precision_tight"])
+def test_precision_stop_rule_matches_reference(oracle_mod, golden, key):
+    """The drivers' stop rule, Precision(eps, PreconditionedConjugateGradient(
+    f, gd, kT, &x, QuadraticLineMinimizer)) (papers/contact/figs/walls.cpp:
+    104-110, src/Precision.cpp:53-151): the GPU minimiser with
+    deft_cg_params.precision = eps stops on the same improve_energy() call
+    as the reference build, with the same energies along the way."""
+    from tests.capi import CG
+    from tests.golden.cases import precision_case
+    vals, _ = golden
+    rec = vals[key]
+    P, x0, _, step, cap = precision_case()
+    ctx, g, f = _setup(P)
+    cg = CG(f, linesearch=_lib.LS_QUADRATIC_REF, step=step, preconditioned=1,
+            precision=rec["precision"])
+    try:
+        cg.set_x(x0)
+        e = []
+        for _ in range(cap):
+            s, st = cg.step()
+            assert s == 0
+            e.append(st.energy)
+            if st.converged:
+                break
+        assert len(e) == rec["calls"]
+        assert np.abs(np.array(e) / np.array(rec["energies"]) - 1).max() < 1e-10
+    finally:
+        _close(cg, f, g, ctx)

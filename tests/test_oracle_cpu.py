@@ -365,3 +365,46 @@ def test_oracle_new_api_minimize_matches_reference(oracle_mod, golden):
     assert np.abs(e[:m] / er[:m] - 1).max() < 1e-7
     xr = arrs["new_minimize_slit_x"]
     assert np.abs(x - xr).max() <= 1e-6 * xr.max()
+
+
+def precision_rule_stop(E0, energies, precision):
+    """Restatement of PrecisionMinimizer::improve_energy (src/Precision.cpp:
+    39-151) over a sequence of energies: the 1-based index of the
+    improve_energy() call that returns false (the inner minimiser assumed
+    not done), or None if the rule never stops."""
+    w, deltaE, log_avg = 0.1, 0.0, 0.0
+    dEdn = 0.0
+    old = E0
+    for k, new in enumerate(energies, start=1):
+        old_deltaE = deltaE
+        deltaE = old - new
+        dEdn = max(deltaE, old_deltaE)
+        nl = math.log(abs(deltaE / old_deltaE)) if (deltaE and old_deltaE) else 0.0
+        log_avg = (1 - w) * log_avg + w * nl
+        ratio = math.exp(log_avg)
+        guess = abs(max(dEdn, deltaE) / log_avg) if log_avg else math.inf
+        if ratio >= 1:
+            guess = precision + abs(new)
+        err = 2 * guess
+        if deltaE == 0 and old_deltaE == 0:
+            return k
+        if not err < precision:
+            old = new
+            continue
+        return k
+    return None
+
+
+@pytest.mark.parametrize("key", ["pcg_precision", "pcg_precision_tight"])
+def test_precision_rule_restatement_stops_where_the_reference_stops(oracle_mod, key):
+    """The drivers' Precision(eps, PreconditionedConjugateGradient(...)) stop
+    (papers/contact/figs/walls.cpp:104-110): the restated rule applied to the
+    reference's own energy sequence stops on the same call as the reference
+    build (tests/golden/reference_values.json)."""
+    from tests.golden.cases import precision_case
+    vals = json.load(open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden",
+                                       "reference_values.json")))
+    rec = vals[key]
+    P, x0, _, _, _ = precision_case()
+    E0, _, _ = P.energy_grad_pgrad(x0)
+    assert precision_rule_stop(E0, rec["energies"], rec["precision"]) == rec["calls"]
