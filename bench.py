@@ -815,15 +815,27 @@ def kernel_case(precision, N, problem="slit", evals=3, tuning=None):
         _lib.check(L.deft_fmt_energy_grad(f, n.data_ptr(), 1, ctypes.addressof(E), g.data_ptr(),
                                           None))
     prof = kernel_profile(L, grid)
+    hvp = {}
+    if precision == _lib.PRECISION_MIXED:
+        # the Newton refinement's Hessian-vector products
+        hv = torch.empty_like(n)
+        _lib.check(L.deft_grid_profile(grid, 1))
+        for _ in range(evals):
+            _lib.check(L.deft_fmt_hessian_vector(f, n.data_ptr(), g.data_ptr(), 1, hv.data_ptr()))
+        hvp = kernel_profile(L, grid)
     torch.cuda.synchronize()
     L.deft_fmt_destroy(f)
     L.deft_grid_destroy(grid)
     L.deft_ctx_destroy(ctx)
-    return {"kernel_case": "mixed" if precision else "fp64", "problem": problem, "N": N,
-            "evals": evals, "energy": E.value,
-            "wall_us_per_eval_call": round(1e6 * wall_eval, 1),
-            "kernel_us_per_eval": round(1e3 * sum(v[1] for v in prof.values()) / evals, 1),
-            "us_per_launch": {k: round(1e3 * v[1] / v[0], 2) for k, v in prof.items()}}
+    out = {"kernel_case": "mixed" if precision else "fp64", "problem": problem, "N": N,
+           "evals": evals, "energy": E.value,
+           "wall_us_per_eval_call": round(1e6 * wall_eval, 1),
+           "kernel_us_per_eval": round(1e3 * sum(v[1] for v in prof.values()) / evals, 1),
+           "us_per_launch": {k: round(1e3 * v[1] / v[0], 2) for k, v in prof.items()}}
+    if hvp:
+        out["hvp_kernel_us_per_product"] = round(1e3 * sum(v[1] for v in hvp.values()) / evals, 1)
+        out["hvp_us_per_launch"] = {k: round(1e3 * v[1] / v[0], 2) for k, v in hvp.items()}
+    return out
 
 
 def fno_case(N=128, reps=5):
@@ -856,6 +868,84 @@ def fno_case(N=128, reps=5):
     return {"fno_case": {"N": N, "channels": 16, "modes": 12, "layers": 4},
             "ms_per_forward": round(1e3 * statistics.median(times), 3),
             "launches_per_forward": launches // (reps + 2)}
+
+
+def solute_case(N=256, reps=5):
+    """The hard-sphere solute workload at 256^3 (dx = 0.1, eta = 0.35, centre
+    exclusion radius 3, smoothed-noise start with seed 2;
+    papers/contact/figs/sphere.cpp:90-105 geometry): plain FP64 solve and the
+    mixed solve (FP32 CG stage with the density preconditioner, Newton
+    refinement on the FP64 gradient), both from the same start and timed
+    with CUDA events, and the mixed form's errors against FP64: one
+    evaluation at the start (free energy, gradient) and the converged
+    profile against the FP64 solution converged to |grad F| < 1e-12."""
+    import torch
+    from deft_gb300 import _lib
+    from deft_gb300.warmstart import Solver
+    from deft_gb300.workloads import Solute
+    s = Solute(N=N, dx=0.1, eta=0.35, r_excl=3.0, seed=2)
+    dd = "cuda:0"
+    mask = torch.tensor(s.mask.reshape(-1), device=dd)
+    n0 = torch.tensor(s.n0.reshape(-1), device=dd)
+    sv = Solver(s.shape, s.lat, device=0, gtol=GTOL)
+    stream = torch.cuda.ExternalStream(sv.L.deft_ctx_stream(sv.ctx), device=dd)
+    MIXED, FP64 = _lib.PRECISION_MIXED, _lib.PRECISION_FP64
+    L = sv.L
+    try:
+        sv.set_problem(s, mask.data_ptr())
+        # one evaluation at the start in both forms
+        E = {}
+        g = {}
+        for prec in (FP64, MIXED):
+            e = ctypes.c_double()
+            g[prec] = torch.empty_like(n0)
+            _lib.check(L.deft_fmt_energy_grad(sv.fmt[prec], n0.data_ptr(), 1, ctypes.addressof(e),
+                                              g[prec].data_ptr(), None))
+            E[prec] = e.value
+        eval_err = {"dF_rel": abs(E[MIXED] / E[FP64] - 1),
+                    "max_dg_rel_to_max_g": float((g[MIXED] - g[FP64]).abs().max()
+                                                 / g[FP64].abs().max())}
+        # the FP64 solution to 1e-12 (the profile reference)
+        st, _ = sv.solve(FP64, n0.data_ptr(), preconditioned=_lib.PC_DENSITY, gtol=REF_GTOL)
+        if not (st.converged and st.gnorm < REF_GTOL):
+            raise RuntimeError("FP64 reference solve did not converge")
+        x_ref = torch.empty_like(n0)
+        _lib.check(L.deft_cg_get_x(sv.cg[FP64], x_ref.data_ptr(), 1))
+        x = torch.empty_like(n0)
+
+        def timed(prec, pc, gtol):
+            times, sts = [], []
+            for k in range(reps + 1):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                st, _ = sv.solve(prec, n0.data_ptr(), preconditioned=pc, gtol=gtol)
+                e1.record(stream)
+                e1.synchronize()
+                if k:
+                    times.append(e0.elapsed_time(e1) / 1e3)
+                    sts.append(st)
+            if not all(t.converged and t.status == 0 and t.gnorm < gtol for t in sts):
+                raise RuntimeError("solute solve did not converge")
+            _lib.check(L.deft_cg_get_x(sv.cg[prec], x.data_ptr(), 1))
+            d = float((x - x_ref).abs().max())
+            st = sts[-1]
+            return {"seconds": statistics.median(times), "iters": st.iter, "evals": st.evals,
+                    "evals_fp64": st.evals_fp64, "hvps": st.hvps, "gnorm": st.gnorm,
+                    "max_abs_dn_vs_fp64_solution": d,
+                    "max_dn_rel_to_max_n": d / float(x_ref.abs().max())}
+
+        fp64 = timed(FP64, _lib.PC_NONE, GTOL)
+        fp64_pc = timed(FP64, _lib.PC_DENSITY, GTOL)
+        mixed = timed(MIXED, _lib.PC_DENSITY, MIXED_GTOL)
+    finally:
+        sv.close()
+    return {"solute_case": f"White Bear + ideal gas + mu, {N}^3 periodic, dx = 0.1, eta = 0.35, "
+                           "hard-sphere solute (centre exclusion radius 3, n = 0 and frozen "
+                           "inside), smoothed-noise start (seed 2)",
+            "fp64_plain": fp64, "fp64_density_preconditioned": fp64_pc, "mixed": mixed,
+            "speedup_mixed_vs_fp64_plain": fp64["seconds"] / mixed["seconds"],
+            "mixed_single_evaluation_errors": eval_err,
+            "timing": f"median of {reps} solves from the start, CUDA events"}
 
 
 def saft_case(N=128, dx=0.2, evals=10, gtol=1e-11):
@@ -978,11 +1068,16 @@ def main():
     ap.add_argument("--case-problem", default="slit", choices=["slit", "solutes"])
     ap.add_argument("--saft-case", action="store_true",
                     help="only time the water SAFT workload (FP64) and exit")
+    ap.add_argument("--solute-case", action="store_true",
+                    help="only run the 256^3 hard-sphere solute workload (FP64 vs mixed) and exit")
     ap.add_argument("--fno-case", action="store_true",
                     help="only time the warm-start network's forward pass and exit")
     args = ap.parse_args()
     if args.saft_case:
         print(json.dumps(saft_case(args.N)))
+        return
+    if args.solute_case:
+        print(json.dumps(solute_case()))
         return
     if args.fno_case:
         print(json.dumps(fno_case(args.N)))
