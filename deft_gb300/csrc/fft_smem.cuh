@@ -16,6 +16,7 @@
 
 #include <cuda_runtime.h>
 
+#include "dfloat.cuh"
 #include "fastdiv.cuh"
 
 namespace deft {
@@ -23,6 +24,14 @@ namespace deft {
 template <typename T> struct Cplx;
 template <> struct Cplx<double> { using type = double2; };
 template <> struct Cplx<float> { using type = float2; };
+template <> struct Cplx<dfl> { using type = dfc; };
+
+// Read-only cached load of one complex value.
+template <typename C> __device__ __forceinline__ C ldg_c(const C *p) { return __ldg(p); }
+template <> __device__ __forceinline__ dfc ldg_c<dfc>(const dfc *p) {
+  const float4 v = __ldg(reinterpret_cast<const float4 *>(p));
+  return dfc{dfl(v.x, v.y), dfl(v.z, v.w)};
+}
 
 constexpr int kMaxPasses = 16;
 constexpr int kMaxRadix = 13;
@@ -118,7 +127,7 @@ template <int SIGN, typename T, typename C> __device__ __forceinline__ void dft5
 }
 
 template <int SIGN, typename C> __device__ __forceinline__ C tw_load(const C *tw, int t) {
-  C w = __ldg(&tw[t]);
+  C w = ldg_c(&tw[t]);
   if (SIGN > 0) w.y = -w.y;
   return w;
 }

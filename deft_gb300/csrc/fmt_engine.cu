@@ -23,6 +23,7 @@
 #include "fft_smem.cuh"
 #include "fmt_engine.h"
 #include "pencil_fft.cuh"
+#include "warp_fft.cuh"
 #include "wb_phi.cuh"
 
 #include <cmath>
@@ -38,7 +39,12 @@ namespace deft {
 namespace {
 
 constexpr int kThreads = 256;
-constexpr size_t kSmemBudget = 96 * 1024;
+
+// The FP64 form's transforms run in double-float arithmetic (dfloat.cuh);
+// its pointwise work (phi, ideal gas, local terms) and every reduction stay
+// FP64: Acc<T> is the type of that pointwise work.
+template <typename T> constexpr bool is_df = std::is_same<T, dfl>::value;
+template <typename T> using Acc = std::conditional_t<is_df<T>, double, T>;
 
 // ---------------------------------------------------------------------------
 // Device helpers
@@ -827,10 +833,11 @@ __global__ void __launch_bounds__(kThreads,
   const int Nz = g.Nz, P5 = 5 * P;
   const int p0 = blockIdx.x * P;
   C *res = z_load5_c2r<T, RN>(S5, A, Bf, g, pz, fP, f5P, p0);
-  T tacc[kNumTerms] = {0, 0, 0, 0, 0, 0};
+  using U = Acc<T>;
+  U tacc[kNumTerms] = {0, 0, 0, 0, 0, 0};
   const bool hs = la.terms & kTermHS;
-  const T inv_nQ = T(la.inv_nQ);
-  const T c = T(la.dV * la.kT);
+  const U inv_nQ = U(la.inv_nQ);
+  const U c = U(la.dV * la.kT);
   #pragma unroll 4
   for (int idx = threadIdx.x; idx < 2 * P * Nz; idx += blockDim.x) {
     int ll, z;
@@ -838,28 +845,28 @@ __global__ void __launch_bounds__(kThreads,
     const int line = 2 * p0 + ll;
     T *cell = reinterpret_cast<T *>(res + z * P5 + (ll >> 1)) + (ll & 1);  // field 0
     const int fstride = 2 * P;  // T elements between fields
-    T d[5] = {0, 0, 0, 0, 0};
+    U d[5] = {0, 0, 0, 0, 0};
     if (line < g.lines) {
       const size_t r = (size_t)line * Nz + z;
       if (hs) {
-        T phi[3];
-        wb_phi<T>(la.wr, cell[0], cell[fstride], cell[2 * fstride], cell[3 * fstride],
-                  cell[4 * fstride], phi, d);
+        U phi[3];
+        wb_phi<U>(la.wr, U(cell[0]), U(cell[fstride]), U(cell[2 * fstride]),
+                  U(cell[3 * fstride]), U(cell[4 * fstride]), phi, d);
         tacc[0] += phi[0];
         tacc[1] += phi[1];
         tacc[2] += phi[2];
       }
-      const T nv = T(n[r]);
-      if (la.terms & kTermIdeal) tacc[3] += ideal_energy_t<T>(nv, inv_nQ);
+      const U nv = U(n[r]);
+      if (la.terms & kTermIdeal) tacc[3] += ideal_energy_t<U>(nv, inv_nQ);
       if (la.terms & kTermMu) tacc[4] += nv;
-      if (la.terms & kTermVext) tacc[5] += T(V[r]) * nv;
+      if (la.terms & kTermVext) tacc[5] += U(V[r]) * nv;
     }
     if (GRAD) {
 #pragma unroll
-      for (int a = 0; a < 5; a++) cell[a * fstride] = c * d[a];
+      for (int a = 0; a < 5; a++) cell[a * fstride] = T(c * d[a]);
     }
   }
-  block_reduce_terms<T>(tacc, la, red, partials);
+  block_reduce_terms<U>(tacc, la, red, partials);
   if (!GRAD) return;
   __syncthreads();
   z_r2c_store5<T, RN>(res, res == A ? Bf : A, S5, g, pz, fP, f2P, f5P, p0);
@@ -883,7 +890,8 @@ __global__ void DEFT_FFT_BOUNDS(RN) k_z_grad(const typename Cplx<T>::type *__res
   const int p0 = blockIdx.x * P;
   const bool hs = la.terms & kTermHS;
   const C *res = nullptr;
-  T dacc[3] = {0, 0, 0};
+  using U = Acc<T>;
+  U dacc[3] = {0, 0, 0};
   if (hs) {
     pack_c2r<T>(in, buf0, g, p0, P);
     res = fft_tile<T, +1, RN>(buf0, buf1, fP, pz);
@@ -895,27 +903,27 @@ __global__ void DEFT_FFT_BOUNDS(RN) k_z_grad(const typename Cplx<T>::type *__res
     const int line = 2 * p0 + ll;
     if (line >= g.lines) continue;
     const size_t r = (size_t)line * g.Nz + z;
-    T conv = 0;
+    U conv = 0;
     if (hs) {
       const C v = res[z * P + (ll >> 1)];
-      conv = (ll & 1) ? v.y : v.x;
+      conv = U((ll & 1) ? v.y : v.x);
     }
-    T loc = 0;
-    const T nv = T(n[r]);
-    if (la.terms & kTermIdeal) loc += T(la.kT) * wb_log<T>(nv * T(la.inv_nQ));
-    if (la.terms & kTermMu) loc += T(la.mu);
-    if (la.terms & kTermVext) loc += T(V[r]);
-    T gr = conv + T(la.dV) * loc;
+    U loc = 0;
+    const U nv = U(n[r]);
+    if (la.terms & kTermIdeal) loc += U(la.kT) * wb_log<U>(nv * U(la.inv_nQ));
+    if (la.terms & kTermMu) loc += U(la.mu);
+    if (la.terms & kTermVext) loc += U(V[r]);
+    U gr = conv + U(la.dV) * loc;
     if (la.terms & kTermMask) {
-      const T m = T(mask[r]);
-      gr = m == T(0) ? T(0) : m * gr;
+      const U m = U(mask[r]);
+      gr = m == U(0) ? U(0) : m * gr;
     }
     grad[r] = double(gr);
-    // per-thread sums in T (a dozen terms; FP32 products of the FP32
+    // per-thread sums in U (a dozen terms; FP32 products of the FP32
     // gradient), the block and grid sums in FP64
 #pragma unroll
     for (int i = 0; i < 3; i++)
-      if (i < gd.k) dacc[i] += gr * (gd.b[i] ? T(gd.b[i][r]) : gr);
+      if (i < gd.k) dacc[i] += gr * (gd.b[i] ? U(gd.b[i][r]) : gr);
   }
   if (gd.k > 0) {
     __shared__ double dred[32 * 3];
@@ -1064,6 +1072,345 @@ __global__ void DEFT_FFT_BOUNDS(RN) k_z_hvp_out(
     __shared__ double red[32];
     double pqd[1] = {double(pq[0])};
     finish_dots<1>(pqd, red, dpart, counter, dout);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Warp kernels for the FP32 z transforms (Nz = 32 E, E = 1, 2, 4, 8): one
+// warp per pair of z-lines (lines 2p and 2p+1 transformed as one complex
+// line), kZWarps warps a block, the transforms of warp_fft.cuh.  A warp
+// reads and writes its pair's lines (real, or two contiguous half spectra)
+// in contiguous runs; shared memory only stages the half spectra for the
+// Hermitian packing (one buffer per warp, no block barrier in the
+// transforms).
+
+constexpr int kZWarps = 8;
+// One staging buffer per warp (one-field kernels) or five (the five-field
+// kernels stage all fields before transforming, so their loads overlap).
+template <int E> constexpr size_t zwarp_smem(int nf = 1) {
+  return sizeof(float2) * kZWarps * nf * warp_buf_elems<E>();
+}
+
+// Lines of pair p present: 2, 1 (odd line count) or 0; half-spectrum
+// values of the pair to read or write.
+__device__ __forceinline__ int zwarp_nvalid(int l0, const Geom &g) {
+  return l0 + 1 < g.lines ? 2 * g.NzH : (l0 < g.lines ? g.NzH : 0);
+}
+
+// The five fields' half spectra of the warp's pair, staged together (five
+// buffers), packed and transformed back along z (lane-natural order).
+template <int E>
+__device__ __forceinline__ void warp_load5_c2r(const float2 *__restrict__ S5, const Geom &g,
+                                               int l0, int nvalid, float2 *wb, int lane,
+                                               const float2 *__restrict__ tw, float2 (&v)[5][E]) {
+  constexpr int NzH = 16 * E + 1, B = warp_buf_elems<E>();
+#pragma unroll
+  for (int a = 0; a < 5; a++)
+    warp_stage_load<E>(S5 + (size_t)a * g.NC + (size_t)l0 * NzH, nvalid, wb + a * B, lane);
+  __syncwarp();
+#pragma unroll
+  for (int a = 0; a < 5; a++) warp_pack<E>(wb + a * B, lane, v[a]);
+  __syncwarp();
+  float2 w[4];
+  warp_stage_tw<+1, E>(tw, lane, w);
+#pragma unroll
+  for (int a = 0; a < 5; a++) warp_s2n<+1, E>(v[a], lane, tw, w);
+}
+
+// Forward z transforms of the five fields and their Hermitian split into
+// the half spectra of the pair's lines.
+template <int E>
+__device__ __forceinline__ void warp_r2c_store5(float2 (&v)[5][E], float2 *S5, const Geom &g,
+                                                int l0, int nvalid, float2 *wb, int lane,
+                                                const float2 *__restrict__ tw) {
+  constexpr int NzH = 16 * E + 1, B = warp_buf_elems<E>();
+  float2 w[4];
+  warp_stage_tw<-1, E>(tw, lane, w);
+#pragma unroll
+  for (int a = 0; a < 5; a++) warp_n2s<-1, E>(v[a], lane, tw, w);
+#pragma unroll
+  for (int a = 0; a < 5; a++)
+    warp_unpack_store<E>(v[a], lane, 1.0f, wb + a * B, S5 + (size_t)a * g.NC + (size_t)l0 * NzH,
+                         nvalid);
+}
+
+template <int E>
+__global__ void __launch_bounds__(32 * kZWarps)
+    k_z_r2c_warp(const double *__restrict__ in, float2 *__restrict__ out, Geom g,
+                 const float2 *__restrict__ tw, float s) {
+  constexpr int N = 32 * E, NzH = N / 2 + 1;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  float2 *wb = reinterpret_cast<float2 *>(smem_raw) + warp * warp_buf_elems<E>();
+  const int l0 = 2 * (blockIdx.x * kZWarps + warp);
+  float2 w[4];
+  warp_stage_tw<-1, E>(tw, lane, w);
+  const bool a0 = l0 < g.lines, a1 = l0 + 1 < g.lines;
+  float2 v[E];
+#pragma unroll
+  for (int m = 0; m < E; m++) {
+    const size_t r = (size_t)l0 * N + lane + 32 * m;
+    v[m] = make_float2(a0 ? float(in[r]) : 0.f, a1 ? float(in[r + N]) : 0.f);
+  }
+  warp_n2s<-1, E>(v, lane, tw, w);
+  warp_unpack_store<E>(v, lane, s, wb, out + (size_t)l0 * NzH, zwarp_nvalid(l0, g));
+}
+
+// Warp form of k_z_grad: c2r of the adjoint sum, + local gradient terms,
+// masked, optional dot products of the new gradient.
+template <int E>
+__global__ void __launch_bounds__(32 * kZWarps)
+    k_z_grad_warp(const float2 *__restrict__ in, const double *__restrict__ n,
+                  const double *__restrict__ V, const double *__restrict__ mask,
+                  double *__restrict__ grad, Geom g, const float2 *__restrict__ tw,
+                  const LocalArgs *__restrict__ lap, GradDots gd) {
+  constexpr int N = 32 * E, NzH = N / 2 + 1;
+  const LocalArgs la = *lap;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  float2 *wb = reinterpret_cast<float2 *>(smem_raw) + warp * warp_buf_elems<E>();
+  const int l0 = 2 * (blockIdx.x * kZWarps + warp);
+  const bool hs = la.terms & kTermHS;
+  float2 v[E];
+  if (hs) {
+    float2 w[4];
+    warp_stage_tw<+1, E>(tw, lane, w);
+    warp_load_pack<E>(in + (size_t)l0 * NzH, zwarp_nvalid(l0, g), wb, lane, v);
+    warp_s2n<+1, E>(v, lane, tw, w);
+  } else {
+#pragma unroll
+    for (int m = 0; m < E; m++) v[m] = make_float2(0.f, 0.f);
+  }
+  float dacc[3] = {0, 0, 0};
+#pragma unroll
+  for (int half = 0; half < 2; half++) {
+    const int line = l0 + half;
+    if (line >= g.lines) continue;
+#pragma unroll
+    for (int m = 0; m < E; m++) {
+      const size_t r = (size_t)line * N + lane + 32 * m;
+      const float conv = half ? v[m].y : v[m].x;
+      float loc = 0;
+      const float nv = float(n[r]);
+      if (la.terms & kTermIdeal) loc += float(la.kT) * wb_log<float>(nv * float(la.inv_nQ));
+      if (la.terms & kTermMu) loc += float(la.mu);
+      if (la.terms & kTermVext) loc += float(V[r]);
+      float gr = conv + float(la.dV) * loc;
+      if (la.terms & kTermMask) {
+        const float mk = float(mask[r]);
+        gr = mk == 0.f ? 0.f : mk * gr;
+      }
+      grad[r] = double(gr);
+#pragma unroll
+      for (int i = 0; i < 3; i++)
+        if (i < gd.k) dacc[i] += gr * (gd.b[i] ? float(gd.b[i][r]) : gr);
+    }
+  }
+  if (gd.k > 0) {
+    __shared__ double dred[32 * 3];
+    double dsum[3] = {double(dacc[0]), double(dacc[1]), double(dacc[2])};
+    block_reduce<3>(dsum, dred);
+    if (threadIdx.x == 0)
+      for (int i = 0; i < 3; i++) gd.partials[(size_t)blockIdx.x * 3 + i] = dsum[i];
+  }
+}
+
+// Warp form of k_z_hvp_out: c2r of the adjoint sum plus the ideal-gas
+// curvature dV kT/n dx, masked, and dx.out by the last block.
+template <int E>
+__global__ void __launch_bounds__(32 * kZWarps)
+    k_z_hvp_out_warp(const float2 *__restrict__ in, const double *__restrict__ dx,
+                     const float *__restrict__ hloc, const double *__restrict__ mask,
+                     double *__restrict__ out, Geom g, const float2 *__restrict__ tw,
+                     const LocalArgs *__restrict__ lap, double *dpart, unsigned int *counter,
+                     double *dout) {
+  constexpr int N = 32 * E, NzH = N / 2 + 1;
+  const LocalArgs la = *lap;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  float2 *wb = reinterpret_cast<float2 *>(smem_raw) + warp * warp_buf_elems<E>();
+  const int l0 = 2 * (blockIdx.x * kZWarps + warp);
+  const bool hs = la.terms & kTermHS;
+  float2 v[E];
+  if (hs) {
+    float2 w[4];
+    warp_stage_tw<+1, E>(tw, lane, w);
+    warp_load_pack<E>(in + (size_t)l0 * NzH, zwarp_nvalid(l0, g), wb, lane, v);
+    warp_s2n<+1, E>(v, lane, tw, w);
+  } else {
+#pragma unroll
+    for (int m = 0; m < E; m++) v[m] = make_float2(0.f, 0.f);
+  }
+  float pq = 0;
+#pragma unroll
+  for (int half = 0; half < 2; half++) {
+    const int line = l0 + half;
+    if (line >= g.lines) continue;
+#pragma unroll
+    for (int m = 0; m < E; m++) {
+      const size_t r = (size_t)line * N + lane + 32 * m;
+      const float conv = half ? v[m].y : v[m].x;
+      const float dxt = float(dx[r]);
+      float o = conv + float(la.dV) * hloc[r] * dxt;
+      if (la.terms & kTermMask) {
+        const float mk = float(mask[r]);
+        o = mk == 0.f ? 0.f : mk * o;
+      }
+      out[r] = double(o);
+      pq += dxt * o;
+    }
+  }
+  if (dout) {
+    __shared__ double red[32];
+    double pqd[1] = {double(pq)};
+    finish_dots<1>(pqd, red, dpart, counter, dout);
+  }
+}
+
+// Warp form of k_z_phi: c2r of the five weighted densities of the pair, phi
+// and the local energy terms at its 2N points, per-block energies, and
+// (GRAD) r2c of the five partials dV kT dphi/dn_a in place.
+template <bool GRAD, int E>
+__global__ void __launch_bounds__(32 * kZWarps)
+    k_z_phi_warp(float2 *S5, const double *__restrict__ n, const double *__restrict__ V, Geom g,
+                 const float2 *__restrict__ tw, const LocalArgs *__restrict__ lap,
+                 double *partials) {
+  constexpr int N = 32 * E;
+  const LocalArgs la = *lap;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ double red[32 * kNumTerms];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  float2 *wb = reinterpret_cast<float2 *>(smem_raw) + warp * 5 * warp_buf_elems<E>();
+  const int l0 = 2 * (blockIdx.x * kZWarps + warp);
+  const int nvalid = zwarp_nvalid(l0, g);
+  const bool hs = la.terms & kTermHS;
+  float2 v[5][E];
+  if (hs) warp_load5_c2r<E>(S5, g, l0, nvalid, wb, lane, tw, v);
+  float tacc[kNumTerms] = {0, 0, 0, 0, 0, 0};
+  const float inv_nQ = float(la.inv_nQ);
+  const float c = float(la.dV * la.kT);
+#pragma unroll
+  for (int half = 0; half < 2; half++) {
+    const int line = l0 + half;
+    const bool act = line < g.lines;
+#pragma unroll
+    for (int m = 0; m < E; m++) {
+      float d[5] = {0, 0, 0, 0, 0};
+      if (act) {
+        const size_t r = (size_t)line * N + lane + 32 * m;
+        if (hs) {
+          float f[5];
+#pragma unroll
+          for (int a = 0; a < 5; a++) f[a] = half ? v[a][m].y : v[a][m].x;
+          float phi[3];
+          wb_phi<float>(la.wr, f[0], f[1], f[2], f[3], f[4], phi, d);
+          tacc[0] += phi[0];
+          tacc[1] += phi[1];
+          tacc[2] += phi[2];
+        }
+        const float nv = float(n[r]);
+        if (la.terms & kTermIdeal) tacc[3] += ideal_energy_t<float>(nv, inv_nQ);
+        if (la.terms & kTermMu) tacc[4] += nv;
+        if (la.terms & kTermVext) tacc[5] += float(V[r]) * nv;
+      }
+      if (GRAD && hs) {
+#pragma unroll
+        for (int a = 0; a < 5; a++) {
+          if (half) v[a][m].y = c * d[a];
+          else v[a][m].x = c * d[a];
+        }
+      }
+    }
+  }
+  block_reduce_terms<float>(tacc, la, red, partials);
+  if (!GRAD || !hs) return;
+  warp_r2c_store5<E>(v, S5, g, l0, nvalid, wb, lane, tw);
+}
+
+// Warp form of k_z_jac: c2r of the five weighted perturbations, dP = dV kT
+// J dw with the stored Hessian blocks, r2c of dP in place.
+template <int E>
+__global__ void __launch_bounds__(32 * kZWarps)
+    k_z_jac_warp(float2 *S5, Geom g, const float2 *__restrict__ tw,
+                 const LocalArgs *__restrict__ lap, const float *__restrict__ hess) {
+  constexpr int N = 32 * E;
+  const float cc = float(lap->dV * lap->kT);
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  float2 *wb = reinterpret_cast<float2 *>(smem_raw) + warp * 5 * warp_buf_elems<E>();
+  const int l0 = 2 * (blockIdx.x * kZWarps + warp);
+  const int nvalid = zwarp_nvalid(l0, g);
+  float2 v[5][E];
+  warp_load5_c2r<E>(S5, g, l0, nvalid, wb, lane, tw, v);
+#pragma unroll
+  for (int half = 0; half < 2; half++) {
+    const int line = l0 + half;
+    const bool act = line < g.lines;
+#pragma unroll
+    for (int m = 0; m < E; m++) {
+      float o[5] = {0, 0, 0, 0, 0};
+      if (act) {
+        const size_t r = (size_t)line * N + lane + 32 * m;
+        float h[kHessPacked];
+#pragma unroll
+        for (int k = 0; k < kHessPacked; k++) h[k] = hess[(size_t)k * g.NR + r];
+        float dd[5];
+#pragma unroll
+        for (int a = 0; a < 5; a++) dd[a] = half ? v[a][m].y : v[a][m].x;
+        o[0] = h[0] * dd[0] + h[1] * dd[1] + h[2] * dd[2] + h[3] * dd[3] + h[4] * dd[4];
+        o[1] = h[1] * dd[0] + h[5] * dd[1] + h[6] * dd[2] + h[7] * dd[3] + h[8] * dd[4];
+        o[2] = h[2] * dd[0] + h[6] * dd[1] + h[9] * dd[2];
+        o[3] = h[3] * dd[0] + h[7] * dd[1] + h[9] * dd[3];
+        o[4] = h[4] * dd[0] + h[8] * dd[1] + h[9] * dd[4];
+      }
+#pragma unroll
+      for (int a = 0; a < 5; a++) {
+        if (half) v[a][m].y = cc * o[a];
+        else v[a][m].x = cc * o[a];
+      }
+    }
+  }
+  warp_r2c_store5<E>(v, S5, g, l0, nvalid, wb, lane, tw);
+}
+
+// Warp form of k_z_hess: c2r of the five weighted densities, the packed
+// Hessian blocks of phi and the ideal-gas curvature kT/n in FP32.
+template <int E>
+__global__ void __launch_bounds__(32 * kZWarps)
+    k_z_hess_warp(const float2 *__restrict__ S5, const double *__restrict__ n, Geom g,
+                  const float2 *__restrict__ tw, const LocalArgs *__restrict__ lap,
+                  float *__restrict__ hess, float *__restrict__ hloc) {
+  constexpr int N = 32 * E;
+  const LocalArgs la = *lap;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  float2 *wb = reinterpret_cast<float2 *>(smem_raw) + warp * 5 * warp_buf_elems<E>();
+  const int l0 = 2 * (blockIdx.x * kZWarps + warp);
+  const bool hs = la.terms & kTermHS;
+  float2 v[5][E];
+  if (hs) warp_load5_c2r<E>(S5, g, l0, zwarp_nvalid(l0, g), wb, lane, tw, v);
+#pragma unroll
+  for (int half = 0; half < 2; half++) {
+    const int line = l0 + half;
+    if (line >= g.lines) continue;
+#pragma unroll
+    for (int m = 0; m < E; m++) {
+      const size_t r = (size_t)line * N + lane + 32 * m;
+      float h[kHessPacked];
+      if (hs) {
+        float f[5];
+#pragma unroll
+        for (int a = 0; a < 5; a++) f[a] = half ? v[a][m].y : v[a][m].x;
+        wb_hess<float>(la.wr, f[0], f[1], f[2], f[3], f[4], h);
+      } else {
+#pragma unroll
+        for (int k = 0; k < kHessPacked; k++) h[k] = 0.f;
+      }
+#pragma unroll
+      for (int k = 0; k < kHessPacked; k++) hess[(size_t)k * g.NR + r] = h[k];
+      const double nv = n[r];
+      hloc[r] = (la.terms & kTermIdeal) && nv > 0 ? float(la.kT / nv) : 0.0f;
+    }
   }
 }
 
@@ -1568,6 +1915,13 @@ class EngineImpl {
   float2 *tw_xf = nullptr, *tw_yf = nullptr, *tw_zf = nullptr;
   float *w3f = nullptr, *w2f = nullptr, *wvf = nullptr;
   double table_Rf = -1;
+  // the FP64 form's double-float transforms (DEFT_FP64_TRANSFORMS=fp64 in
+  // the environment at grid creation keeps FP64 arithmetic instead)
+  bool df_on = true;
+  FftPlan pxd{}, pyd{}, pzd{};
+  dfc *tw_xd = nullptr, *tw_yd = nullptr, *tw_zd = nullptr;
+  dfl *w3d = nullptr, *w2d = nullptr, *wvd = nullptr;
+  double table_Rd = -1;
   float *hess = nullptr, *hloc = nullptr;  // Newton refinement: Hessian blocks
   double *partials = nullptr;
   int max_blocks = 0;
@@ -1595,6 +1949,12 @@ class EngineImpl {
     cudaFree(tw_xf);
     cudaFree(tw_yf);
     cudaFree(tw_zf);
+    cudaFree(tw_xd);
+    cudaFree(tw_yd);
+    cudaFree(tw_zd);
+    cudaFree(w3d);
+    cudaFree(w2d);
+    cudaFree(wvd);
     cudaFree(w3f);
     cudaFree(w2f);
     cudaFree(wvf);
@@ -1633,32 +1993,47 @@ class EngineImpl {
     return 0;
   }
 
-  int make_plan(int n, FftPlan &p, double2 **tw, FftPlan &pf, float2 **twf) {
+  int make_plan(int n, FftPlan &p, double2 **tw, FftPlan &pf, float2 **twf, FftPlan &pd,
+                dfc **twd) {
     if (!factorize(n, p)) {
       err = "grid size " + std::to_string(n) + " has a prime factor above 13";
       return -1;
     }
     plan_fill_ns(p);
     pf = p;
+    pd = p;
     std::vector<double2> h(n);
     std::vector<float2> hf(n);
+    std::vector<dfc> hd(n);
     const long double twopi = 6.283185307179586476925286766559005768L;
+    // double-float roots: hi the float nearest the root, lo the float
+    // nearest what is left (both from the long-double value)
+    auto split = [](long double v) {
+      const float hi = (float)v;
+      return dfl(hi, (float)(v - (long double)hi));
+    };
     for (int t = 0; t < n; t++) {
       const long double a = twopi * (long double)t / (long double)n;
       h[t] = make_double2((double)cosl(a), (double)-sinl(a));
       hf[t] = make_float2((float)cosl(a), (float)-sinl(a));
+      hd[t] = dfc{split(cosl(a)), split(-sinl(a))};
     }
-    if (alloc(tw, sizeof(double2) * n) || alloc(twf, sizeof(float2) * n)) return -1;
+    if (alloc(tw, sizeof(double2) * n) || alloc(twf, sizeof(float2) * n) ||
+        alloc(twd, sizeof(dfc) * n))
+      return -1;
     cudaError_t e = cudaMemcpy(*tw, h.data(), sizeof(double2) * n, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(*twf, hf.data(), sizeof(float2) * n, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(*twd, hd.data(), sizeof(dfc) * n, cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return fail("twiddle upload", e);
     p.tw = *tw;
     pf.tw = *twf;
+    pd.tw = *twd;
     return 0;
   }
 
   template <typename T> const FftPlan &plan(int axis) const {
     if constexpr (std::is_same<T, float>::value) return axis == 0 ? pxf : axis == 1 ? pyf : pzf;
+    else if constexpr (is_df<T>) return axis == 0 ? pxd : axis == 1 ? pyd : pzd;
     else return axis == 0 ? px : axis == 1 ? py : pz;
   }
   template <typename T> typename Cplx<T>::type *spec0() {
@@ -1669,6 +2044,7 @@ class EngineImpl {
   }
   template <typename T> const T *table(int which) const {
     if constexpr (std::is_same<T, float>::value) return which == 0 ? w3f : which == 1 ? w2f : wvf;
+    else if constexpr (is_df<T>) return which == 0 ? w3d : which == 1 ? w2d : wvd;
     else return which == 0 ? w3 : which == 1 ? w2 : wv;
   }
 
@@ -1716,8 +2092,9 @@ class EngineImpl {
       for (int j = 0; j < 3; j++) g.Bm[3 * i + j] = 2 * M_PI * inv[3 * j + i];
     geom_finish(g);
 
-    if (make_plan(s.Nx, px, &tw_x, pxf, &tw_xf) || make_plan(s.Ny, py, &tw_y, pyf, &tw_yf) ||
-        make_plan(s.Nz, pz, &tw_z, pzf, &tw_zf))
+    if (make_plan(s.Nx, px, &tw_x, pxf, &tw_xf, pxd, &tw_xd) ||
+        make_plan(s.Ny, py, &tw_y, pyf, &tw_yf, pyd, &tw_yd) ||
+        make_plan(s.Nz, pz, &tw_z, pzf, &tw_zf, pzd, &tw_zd))
       return -1;
 
     const size_t cs = sizeof(double2);
@@ -1740,6 +2117,18 @@ class EngineImpl {
     set_smem(k_z_phi<double, false>, t64.smem_phi);
     set_smem(k_z_phi<double, true>, t64.smem_phi);
     set_smem(k_z_grad<double>, t64.smem_z);
+    set_smem(k_z_r2c<dfl>, t64.smem_z);
+    set_smem(k_y_fft<dfl, -1>, t64.smem_y);
+    set_smem(k_y_fft<dfl, +1>, t64.smem_y);
+    set_smem(k_x_conv_fwd<dfl>, t64.smem_xf);
+    set_smem(k_x_conv_adj<dfl>, t64.smem_xc);
+    set_smem(k_z_phi<dfl, false>, t64.smem_phi);
+    set_smem(k_z_phi<dfl, true>, t64.smem_phi);
+    set_smem(k_z_grad<dfl>, t64.smem_z);
+    {
+      const char *ev = getenv("DEFT_FP64_TRANSFORMS");
+      df_on = !(ev && !strcmp(ev, "fp64"));
+    }
     // every FP32 instantiation (shared-memory passes and register lengths)
     auto smem32 = [&](auto rn) {
       constexpr int RN = decltype(rn)::value;
@@ -1766,9 +2155,25 @@ class EngineImpl {
     smemp(std::integral_constant<int, 4>());
     smemp(std::integral_constant<int, 8>());
     smemp(std::integral_constant<int, 16>());
+    auto smemw = [&](auto ec) {
+      constexpr int E = decltype(ec)::value;
+      set_smem(k_z_r2c_warp<E>, zwarp_smem<E>());
+      set_smem(k_z_grad_warp<E>, zwarp_smem<E>());
+      set_smem(k_z_hvp_out_warp<E>, zwarp_smem<E>());
+      set_smem(k_z_phi_warp<true, E>, zwarp_smem<E>(5));
+      set_smem(k_z_phi_warp<false, E>, zwarp_smem<E>(5));
+      set_smem(k_z_jac_warp<E>, zwarp_smem<E>(5));
+      set_smem(k_z_hess_warp<E>, zwarp_smem<E>(5));
+    };
+    smemw(std::integral_constant<int, 1>());
+    smemw(std::integral_constant<int, 2>());
+    smemw(std::integral_constant<int, 4>());
+    smemw(std::integral_constant<int, 8>());
     {
       const char *ev = getenv("DEFT_PENCIL");
       pencil_on = !(ev && ev[0] == '0');
+      ev = getenv("DEFT_ZWARP");
+      if (ev) zwarp_mask = atoi(ev) & 3;
     }
     smem32(std::integral_constant<int, 0>());
     smem32(std::integral_constant<int, 32>());
@@ -1783,6 +2188,7 @@ class EngineImpl {
     const int mb32 = (pairs + t32.Pphi - 1) / t32.Pphi;
     if (max_blocks < mb32) max_blocks = mb32;
     if (max_blocks < 1024) max_blocks = 1024;
+    if (max_blocks < zwarp_blocks()) max_blocks = zwarp_blocks();
     if (alloc(&partials, sizeof(double) * kNumTerms * max_blocks)) return -1;
     if (alloc(&results, sizeof(double) * 16) || alloc(&la_dev, sizeof(LocalArgs))) return -1;
     cudaError_t e = cudaMallocHost((void **)&results_host, sizeof(double) * 16);
@@ -1816,6 +2222,15 @@ class EngineImpl {
       k_weight_table<float><<<nb, kThreads, 0, stream>>>(g, R, w3f, w2f, wvf);
       post(kslot<float>(kK_weight_table));
       table_Rf = R;
+    } else if constexpr (is_df<T>) {
+      if (R == table_Rd) return 0;
+      if (!w3d && (alloc(&w3d, sizeof(dfl) * g.NC) || alloc(&w2d, sizeof(dfl) * g.NC) ||
+                   alloc(&wvd, sizeof(dfl) * g.NC)))
+        return -1;
+      pre(kK_weight_table);
+      k_weight_table<dfl><<<nb, kThreads, 0, stream>>>(g, R, w3d, w2d, wvd);
+      post(kK_weight_table);
+      table_Rd = R;
     } else {
       if (R == table_R) return 0;
       pre(kK_weight_table);
@@ -1870,6 +2285,13 @@ class EngineImpl {
       px = np[0];
       py = np[1];
       pz = np[2];
+      // the double-float plans share the FP64 radix orders (own twiddles)
+      FftPlan *pd[3] = {&pxd, &pyd, &pzd};
+      for (int a = 0; a < 3; a++) {
+        const void *tw = pd[a]->tw;
+        *pd[a] = np[a];
+        pd[a]->tw = tw;
+      }
     }
     return 0;
   }
@@ -1905,6 +2327,26 @@ class EngineImpl {
       default: f(std::integral_constant<int, 16>()); break;
     }
   }
+
+  const float2 *twz32() const { return reinterpret_cast<const float2 *>(pzf.tw); }
+  // Warp kernels for the FP32 z transforms (Nz = 32 E), under the pencil
+  // switch and DEFT_ZWARP at grid creation: bit 0 the one-field kernels
+  // (r2c, gradient, Hessian-vector output), bit 1 the five-field ones (phi,
+  // Hessian blocks, Jacobian product).
+  int zwarp_mask = 1;
+  template <typename T> bool zwarp(int nf = 1) const {
+    return std::is_same<T, float>::value && pencil_on && pencil_w(g.Nz) > 0 &&
+           (zwarp_mask & (nf == 1 ? 1 : 2));
+  }
+  template <typename F> static void with_e(int L, F &&f) {
+    switch (L) {
+      case 32: f(std::integral_constant<int, 1>()); break;
+      case 64: f(std::integral_constant<int, 2>()); break;
+      case 128: f(std::integral_constant<int, 4>()); break;
+      default: f(std::integral_constant<int, 8>()); break;
+    }
+  }
+  int zwarp_blocks() const { return (((g.lines + 1) / 2) + kZWarps - 1) / kZWarps; }
 
   template <typename T> void y_fft(typename Cplx<T>::type *data, int nf, int sign) {
     const Tiles &t = tl<T>();
@@ -1966,10 +2408,18 @@ class EngineImpl {
   template <typename T> int forward_weighted(const FmtSpec &f, const double *n) {
     const Tiles &t = tl<T>();
     pre(kslot<T>(kK_z_r2c));
-    with_rn<T>(plan<T>(2), [&](auto rn) {
-      k_z_r2c<T, decltype(rn)::value><<<dim3(pairs_tiles(t.Pz), 1), kThreads, t.smem_z, stream>>>(
-          n, spec0<T>(), g, plan<T>(2), t.fPz, T(1));
-    });
+    if (zwarp<T>()) {
+      with_e(g.Nz, [&](auto ec) {
+        constexpr int E = decltype(ec)::value;
+        k_z_r2c_warp<E><<<zwarp_blocks(), 32 * kZWarps, zwarp_smem<E>(), stream>>>(
+            n, reinterpret_cast<float2 *>(spec0<T>()), g, twz32(), 1.0f);
+      });
+    } else {
+      with_rn<T>(plan<T>(2), [&](auto rn) {
+        k_z_r2c<T, decltype(rn)::value><<<dim3(pairs_tiles(t.Pz), 1), kThreads, t.smem_z,
+                                          stream>>>(n, spec0<T>(), g, plan<T>(2), t.fPz, T(1));
+      });
+    }
     post(kslot<T>(kK_z_r2c));
     y_fft<T>(spec0<T>(), 1, -1);
     pre(kslot<T>(kK_x_conv_fwd));
@@ -2154,7 +2604,8 @@ class EngineImpl {
            const double *const *db = nullptr, double *dots_host = nullptr) {
     if ((f.terms & kTermHS) && ensure_table<T>(f.R)) return -1;
     if (upload_args(f)) return -1;
-    const GraphKey key = graph_key(grad ? 1 : 0, sizeof(T), f, n, V, mask, grad, kd, da, db);
+    const GraphKey key =
+        graph_key(grad ? 1 : 0, is_df<T> ? 9 : (int)sizeof(T), f, n, V, mask, grad, kd, da, db);
     // dot products of the new gradient ride on the kernel that writes it
     bool fused = grad && kd > 0;
     GradDots gd{};
@@ -2195,15 +2646,29 @@ class EngineImpl {
       if (forward_weighted<T>(f, n)) return -1;
       nblk = pairs_tiles(t.Pphi);
       pre(kslot<T>(grad ? kK_z_phi_grad : kK_z_phi_energy));
-      with_rn<T>(plan<T>(2), [&](auto rn) {
-        constexpr int RN = decltype(rn)::value;
-        if (grad)
-          k_z_phi<T, true, RN><<<nblk, kThreads, t.smem_phi, stream>>>(
-              spec5<T>(), n, V, g, plan<T>(2), t.fPphi, t.f2Pphi, t.f5Pphi, la_dev, partials);
-        else
-          k_z_phi<T, false, RN><<<nblk, kThreads, t.smem_phi, stream>>>(
-              spec5<T>(), n, V, g, plan<T>(2), t.fPphi, t.f2Pphi, t.f5Pphi, la_dev, partials);
-      });
+      if (zwarp<T>(5)) {
+        nblk = zwarp_blocks();
+        with_e(g.Nz, [&](auto ec) {
+          constexpr int E = decltype(ec)::value;
+          float2 *s5 = reinterpret_cast<float2 *>(spec5<T>());
+          if (grad)
+            k_z_phi_warp<true, E><<<nblk, 32 * kZWarps, zwarp_smem<E>(5), stream>>>(
+                s5, n, V, g, twz32(), la_dev, partials);
+          else
+            k_z_phi_warp<false, E><<<nblk, 32 * kZWarps, zwarp_smem<E>(5), stream>>>(
+                s5, n, V, g, twz32(), la_dev, partials);
+        });
+      } else {
+        with_rn<T>(plan<T>(2), [&](auto rn) {
+          constexpr int RN = decltype(rn)::value;
+          if (grad)
+            k_z_phi<T, true, RN><<<nblk, kThreads, t.smem_phi, stream>>>(
+                spec5<T>(), n, V, g, plan<T>(2), t.fPphi, t.f2Pphi, t.f5Pphi, la_dev, partials);
+          else
+            k_z_phi<T, false, RN><<<nblk, kThreads, t.smem_phi, stream>>>(
+                spec5<T>(), n, V, g, plan<T>(2), t.fPphi, t.f2Pphi, t.f5Pphi, la_dev, partials);
+        });
+      }
       post(kslot<T>(grad ? kK_z_phi_grad : kK_z_phi_energy));
       if (check("phi")) return -1;
       if (grad) {
@@ -2216,19 +2681,30 @@ class EngineImpl {
     } else {
       nblk = 4 * 152;
       pre(kslot<T>(kK_local_energy));
-      k_local_energy<T><<<nblk, kThreads, 0, stream>>>(n, V, g, la_dev, partials);
+      k_local_energy<Acc<T>><<<nblk, kThreads, 0, stream>>>(n, V, g, la_dev, partials);
       post(kslot<T>(kK_local_energy));
     }
+    int gblk = pairs_tiles(t.Pz);
     if (grad) {
       pre(kslot<T>(kK_z_grad));
-      with_rn<T>(plan<T>(2), [&](auto rn) {
-        k_z_grad<T, decltype(rn)::value><<<pairs_tiles(t.Pz), kThreads, t.smem_z, stream>>>(
-            spec0<T>(), n, V, mask, grad, g, plan<T>(2), t.fPz, la_dev, gd ? *gd : GradDots{});
-      });
+      if (zwarp<T>()) {
+        gblk = zwarp_blocks();
+        with_e(g.Nz, [&](auto ec) {
+          constexpr int E = decltype(ec)::value;
+          k_z_grad_warp<E><<<gblk, 32 * kZWarps, zwarp_smem<E>(), stream>>>(
+              reinterpret_cast<const float2 *>(spec0<T>()), n, V, mask, grad, g, twz32(), la_dev,
+              gd ? *gd : GradDots{});
+        });
+      } else {
+        with_rn<T>(plan<T>(2), [&](auto rn) {
+          k_z_grad<T, decltype(rn)::value><<<pairs_tiles(t.Pz), kThreads, t.smem_z, stream>>>(
+              spec0<T>(), n, V, mask, grad, g, plan<T>(2), t.fPz, la_dev, gd ? *gd : GradDots{});
+        });
+      }
       post(kslot<T>(kK_z_grad));
     }
     if (check("gradient")) return -1;
-    queue_energy(nblk, grad ? gd : nullptr, pairs_tiles(t.Pz));
+    queue_energy(nblk, grad ? gd : nullptr, gblk);
     return check("energy reduction");
   }
   int hess_setup(const FmtSpec &f, const double *n) {
@@ -2240,12 +2716,20 @@ class EngineImpl {
       if (ensure_table<float>(f.R) || forward_weighted<float>(f, n)) return -1;
     }
     pre(kslot<float>(kK_z_hess));
-    with_rn<float>(plan<float>(2), [&](auto rn) {
-      k_z_hess<float, decltype(rn)::value><<<pairs_tiles(t32.Pphi), kThreads, t32.smem_phi,
-                                             stream>>>(spec5<float>(), n, g, plan<float>(2),
-                                                       t32.fPphi, t32.f5Pphi, la_dev, hess,
-                                                       hloc);
-    });
+    if (zwarp<float>(5)) {
+      with_e(g.Nz, [&](auto ec) {
+        constexpr int E = decltype(ec)::value;
+        k_z_hess_warp<E><<<zwarp_blocks(), 32 * kZWarps, zwarp_smem<E>(5), stream>>>(
+            reinterpret_cast<const float2 *>(spec5<float>()), n, g, twz32(), la_dev, hess, hloc);
+      });
+    } else {
+      with_rn<float>(plan<float>(2), [&](auto rn) {
+        k_z_hess<float, decltype(rn)::value><<<pairs_tiles(t32.Pphi), kThreads, t32.smem_phi,
+                                               stream>>>(spec5<float>(), n, g, plan<float>(2),
+                                                         t32.fPphi, t32.f5Pphi, la_dev, hess,
+                                                         hloc);
+      });
+    }
     post(kslot<float>(kK_z_hess));
     return check("hessian blocks");
   }
@@ -2266,12 +2750,20 @@ class EngineImpl {
     if (f.terms & kTermHS) {
       if (forward_weighted<float>(f, dx)) return -1;
       pre(kslot<float>(kK_z_jac));
-      with_rn<float>(plan<float>(2), [&](auto rn) {
-        k_z_jac<float, decltype(rn)::value><<<pairs_tiles(t32.Pphi), kThreads, t32.smem_phi,
-                                              stream>>>(spec5<float>(), g, plan<float>(2),
-                                                        t32.fPphi, t32.f2Pphi, t32.f5Pphi,
-                                                        la_dev, hess);
-      });
+      if (zwarp<float>(5)) {
+        with_e(g.Nz, [&](auto ec) {
+          constexpr int E = decltype(ec)::value;
+          k_z_jac_warp<E><<<zwarp_blocks(), 32 * kZWarps, zwarp_smem<E>(5), stream>>>(
+              reinterpret_cast<float2 *>(spec5<float>()), g, twz32(), la_dev, hess);
+        });
+      } else {
+        with_rn<float>(plan<float>(2), [&](auto rn) {
+          k_z_jac<float, decltype(rn)::value><<<pairs_tiles(t32.Pphi), kThreads, t32.smem_phi,
+                                                stream>>>(spec5<float>(), g, plan<float>(2),
+                                                          t32.fPphi, t32.f2Pphi, t32.f5Pphi,
+                                                          la_dev, hess);
+        });
+      }
       post(kslot<float>(kK_z_jac));
       y_fft<float>(spec5<float>(), 5, -1);
       pre(kslot<float>(kK_x_conv_adj));
@@ -2280,13 +2772,22 @@ class EngineImpl {
       y_fft<float>(spec0<float>(), 1, +1);
     }
     pre(kslot<float>(kK_z_hvp_out));
-    with_rn<float>(plan<float>(2), [&](auto rn) {
-      k_z_hvp_out<float, decltype(rn)::value><<<pairs_tiles(t32.Pz), kThreads, t32.smem_z,
-                                                stream>>>(spec0<float>(), dx, hloc, mask, out, g,
-                                                          plan<float>(2), t32.fPz, la_dev,
-                                                          grad_partials, dot_counter,
-                                                          with_dot ? results : nullptr);
-    });
+    if (zwarp<float>()) {
+      with_e(g.Nz, [&](auto ec) {
+        constexpr int E = decltype(ec)::value;
+        k_z_hvp_out_warp<E><<<zwarp_blocks(), 32 * kZWarps, zwarp_smem<E>(), stream>>>(
+            reinterpret_cast<const float2 *>(spec0<float>()), dx, hloc, mask, out, g, twz32(),
+            la_dev, grad_partials, dot_counter, with_dot ? results : nullptr);
+      });
+    } else {
+      with_rn<float>(plan<float>(2), [&](auto rn) {
+        k_z_hvp_out<float, decltype(rn)::value><<<pairs_tiles(t32.Pz), kThreads, t32.smem_z,
+                                                  stream>>>(spec0<float>(), dx, hloc, mask, out,
+                                                            g, plan<float>(2), t32.fPz, la_dev,
+                                                            grad_partials, dot_counter,
+                                                            with_dot ? results : nullptr);
+      });
+    }
     post(kslot<float>(kK_z_hvp_out));
     return check("hessian-vector product");
   }
@@ -2297,6 +2798,7 @@ class EngineImpl {
                double *dots_host = nullptr) {
     if (f.precision == kPrecisionMixed)
       return eval<float>(f, n, V, mask, grad, E_host, terms_host, kd, da, db, dots_host);
+    if (df_on) return eval<dfl>(f, n, V, mask, grad, E_host, terms_host, kd, da, db, dots_host);
     return eval<double>(f, n, V, mask, grad, E_host, terms_host, kd, da, db, dots_host);
   }
 };
