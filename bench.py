@@ -24,8 +24,11 @@ end to end through the public API with host buffers, a cuFFT comparison of
 one 3-D transform, the batched sweep, and a CPU baseline (the oracle port,
 one core, on a bounded sample).
 
-The network is trained inside the run (--train-count solves of the same
-problem family, generated on the GPU) unless --weights names a weight file.
+The network is the bundled one (deft_gb300/weights/fno_wb128_2000.bf16:
+trained by `python -m deft_gb300.warmstart --count 2000 --epochs 3` on 2000
+converged solves of the same problem family, training seed 5, disjoint from
+the held-out seed), or the one --weights names, or, with --weights train (or
+no bundled file), trained inside the run on --train-count solves.
 
 --impl reference: the reference's CPU path (the plain-C restatement of it,
 since the reference sources are not present where this runs): each step is
@@ -64,6 +67,7 @@ REF_GTOL = 1e-12
 HELD_SEED = 6
 TRAIN_SEED = 5
 HBM_FALLBACK_GBS = 6800.0
+BUNDLED_WEIGHTS = os.path.join(ROOT, "deft_gb300", "weights", "fno_wb128_2000.bf16")
 
 
 def measured_peaks():
@@ -249,9 +253,15 @@ def get_network(args, N, dev, log):
     solves of the same family (training seed, disjoint from the held-out seed)."""
     from deft_gb300.warmstart import FourierOperator, make_dataset, train
     from deft_gb300.workloads import walls_solutes_set
-    if args.weights:
+    if args.weights != "train":
         net = FourierOperator.load(args.weights, device=dev)
-        return net, {"source": args.weights}
+        bundled = os.path.basename(args.weights) == os.path.basename(BUNDLED_WEIGHTS)
+        return net, {"source": os.path.relpath(args.weights, ROOT),
+                     "trained_on": "2000 converged solves (mixed, refined on the FP64 gradient "
+                                   "to |grad F| < 1e-9) of seeded wall + solute problems, "
+                                   f"training seed {TRAIN_SEED}, 3 epochs (python -m "
+                                   "deft_gb300.warmstart --count 2000 --epochs 3)"
+                     if bundled else "given with --weights"}
     t0 = time.perf_counter()
     ds = make_dataset(walls_solutes_set(args.train_count, TRAIN_SEED, N=N), device=dev,
                       workers=args.train_workers)
@@ -1047,7 +1057,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--N", type=int, default=128)
-    ap.add_argument("--weights", default=None, help="warm-start network weight file")
+    ap.add_argument("--weights", default=None,
+                    help="warm-start network weight file (default: the bundled 2000-solve "
+                         "network when present), or 'train' to train one in the run on "
+                         "--train-count solves")
     ap.add_argument("--train-count", type=int, default=256)
     ap.add_argument("--train-epochs", type=int, default=2)
     ap.add_argument("--train-workers", type=int, default=8,
@@ -1073,6 +1086,8 @@ def main():
     ap.add_argument("--fno-case", action="store_true",
                     help="only time the warm-start network's forward pass and exit")
     args = ap.parse_args()
+    if args.weights is None:
+        args.weights = BUNDLED_WEIGHTS if os.path.exists(BUNDLED_WEIGHTS) else "train"
     if args.saft_case:
         print(json.dumps(saft_case(args.N)))
         return
