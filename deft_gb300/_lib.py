@@ -34,7 +34,7 @@ EXPORTS = (
     "deft_find_chemical_potential",
     "deft_fmt_energy_grad_noalloc", "deft_noalloc_scratch_bytes",
     "deft_cg_create", "deft_cg_destroy", "deft_cg_set_params", "deft_cg_set_x", "deft_cg_get_x", "deft_cg_x_device",
-    "deft_cg_step", "deft_cg_solve", "deft_cg_checkpoint", "deft_cg_restore", "deft_batch_solve",
+    "deft_cg_step", "deft_cg_solve", "deft_cg_checkpoint", "deft_cg_restore", "deft_cg_set_log", "deft_batch_solve",
     "deft_fno_create", "deft_fno_destroy", "deft_fno_param_count", "deft_fno_get_params",
     "deft_fno_set_params", "deft_fno_eval", "deft_fno_adam", "deft_fno_train_step",
     "deft_fno_warm_start", "deft_fno_initial_density", "deft_fno_launches",
@@ -146,6 +146,7 @@ def load():
         "deft_cg_solve": (ctypes.c_int, [_vp, ctypes.POINTER(CgStatus)]),
         "deft_cg_checkpoint": (ctypes.c_int, [_vp, ctypes.c_char_p]),
         "deft_cg_restore": (ctypes.c_int, [_vp, ctypes.c_char_p]),
+        "deft_cg_set_log": (ctypes.c_int, [_vp, ctypes.c_char_p]),
         "deft_fno_create": (ctypes.c_int, [ctypes.c_int] * 5 + [ctypes.c_ulonglong, _pp]),
         "deft_fno_destroy": (ctypes.c_int, [_vp]),
         "deft_fno_param_count": (ctypes.c_size_t, [_vp]),

@@ -46,6 +46,10 @@ struct deft_fmt {
   double *s_buf = nullptr, *s_grad = nullptr;     // DEFT_TERM_SAFT only
   deft::SaftParams saft{};
   bool saft_set = false;
+  // per-term energies of the last evaluation (the reference keeps them as
+  // last_energy, src/Functional.h:223): the six fused terms, then the SAFT
+  // association and dispersion terms
+  double last_terms[deft::kNumTerms + 2] = {0, 0, 0, 0, 0, 0, 0, 0};
 };
 
 struct deft_cg {
@@ -79,6 +83,7 @@ struct deft_cg {
   double g0norm = -1;
   bool last_eval_mixed = false;          // c->g / c->E came from the FP32 evaluator
   double *q = nullptr, *dxv = nullptr;  // refinement work vectors
+  FILE *log = nullptr;                  // per-step JSONL records (deft_cg_set_log)
 };
 
 namespace {
@@ -549,7 +554,11 @@ int density_eval(deft_fmt *f, const deft::FmtSpec &spec_in, const double *n, dou
                  double *E, double *terms) {
   deft::FmtSpec spec = spec_in;
   spec.terms &= ~DEFT_TERM_SAFT;
-  if (int s = density_eval_fmt(f, spec, n, grad, E, terms)) return s;
+  double tl[deft::kNumTerms];
+  if (int s = density_eval_fmt(f, spec, n, grad, E, tl)) return s;
+  memcpy(f->last_terms, tl, sizeof(tl));
+  f->last_terms[deft::kNumTerms] = f->last_terms[deft::kNumTerms + 1] = 0;
+  if (terms) memcpy(terms, tl, sizeof(tl));
   if (!has_saft(f)) return DEFT_OK;
   Engine *e = f->grid->eng;
   if (!f->s_buf) {
@@ -568,6 +577,8 @@ int density_eval(deft_fmt *f, const deft::FmtSpec &spec_in, const double *n, dou
   if (grad && deft::add_masked(e, f->s_grad, (spec.terms & DEFT_TERM_MASK) ? f->mask : nullptr, grad))
     return set_err(DEFT_ERR_CUDA, "SAFT: gradient sum");
   *E += t2[0] + t2[1];
+  f->last_terms[deft::kNumTerms] = t2[0];
+  f->last_terms[deft::kNumTerms + 1] = t2[1];
   return DEFT_OK;
 }
 
@@ -910,7 +921,18 @@ int deft_cg_destroy(deft_cg *c) {
   cudaFree(c->pg);
   cudaFree(c->q);
   cudaFree(c->dxv);
+  if (c->log) fclose(c->log);
   delete c;
+  return DEFT_OK;
+}
+
+int deft_cg_set_log(deft_cg *c, const char *path) {
+  if (!c) return set_err(DEFT_ERR_ARG, "NULL argument");
+  if (c->log) fclose(c->log);
+  c->log = nullptr;
+  if (!path) return DEFT_OK;
+  c->log = fopen(path, "a");
+  if (!c->log) return set_err(DEFT_ERR_ARG, std::string("cannot open log file ") + path);
   return DEFT_OK;
 }
 
@@ -1562,6 +1584,31 @@ int step_newapi(deft_cg *c, bool *more) {
   return DEFT_OK;
 }
 
+// One JSON line per deft_cg_step: what the reference prints per iteration
+// (print_info / print_iteration, src/Minimizer.cpp:20-25 and
+// src/Functional.cpp:281-316: iteration, energy, gradient norm, the energy
+// of each term of the last evaluation) plus the minimiser's step and the
+// evaluation counters.
+void cg_log_step(deft_cg *c, const deft_cg_status *st) {
+  static const char *names[deft::kNumTerms + 2] = {"hs_phi3", "hs_phi1", "hs_phi2", "ideal_gas",
+                                                   "chemical_potential", "external_potential",
+                                                   "saft_association", "saft_dispersion"};
+  const double step = c->p.linesearch == DEFT_LS_SECANT    ? c->alpha
+                      : c->p.linesearch == DEFT_LS_NEW_API ? c->nm_step
+                                                           : c->step;
+  fprintf(c->log,
+          "{\"iter\": %d, \"energy\": %.17g, \"gnorm\": %.17g, \"step\": %.17g, "
+          "\"evals\": %d, \"evals_fp64\": %d, \"hvps\": %d, \"stage\": %d, "
+          "\"converged\": %d, \"status\": %d, \"terms\": {",
+          st->iter, st->energy, st->gnorm, step, st->evals, st->evals_fp64, st->hvps, st->stage,
+          st->converged, st->status);
+  const int nt = has_saft(c->f) ? deft::kNumTerms + 2 : deft::kNumTerms;
+  for (int i = 0; i < nt; i++)
+    fprintf(c->log, "%s\"%s\": %.17g", i ? ", " : "", names[i], c->f->last_terms[i]);
+  fprintf(c->log, "}}\n");
+  fflush(c->log);
+}
+
 }  // namespace
 
 int deft_cg_step(deft_cg *c, deft_cg_status *st) {
@@ -1650,6 +1697,7 @@ int deft_cg_step(deft_cg *c, deft_cg_status *st) {
   st->evals_fp64 = c->evals_fp64;
   st->hvps = c->hvps;
   st->stage = c->stage;
+  if (c->log) cg_log_step(c, st);
   return status;
 }
 

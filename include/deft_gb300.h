@@ -286,6 +286,15 @@ int deft_cg_solve(deft_cg *cg, deft_cg_status *st);
  * settings continues the run bit-identically. */
 int deft_cg_checkpoint(deft_cg *cg, const char *path);
 int deft_cg_restore(deft_cg *cg, const char *path);
+/* Per-iteration log, the machine-readable form of what the reference prints
+ * per iteration (MinimizerInterface::print_info, src/Minimizer.cpp:20-25,
+ * and Functional::print_iteration / print_summary,
+ * src/Functional.cpp:281-316): from the next deft_cg_step on, each step
+ * appends one JSON line to `path` (iteration, energy, gradient norm, line
+ * step, evaluation counters, stage, status, and the energy of each term of
+ * the last evaluation).  NULL stops logging; the file is closed by the next
+ * call or by deft_cg_destroy. */
+int deft_cg_set_log(deft_cg *cg, const char *path);
 
 /* ---- contact values (src/ContactDensity.cpp, src/haskell/WhiteBear.hs:68-137) ----
  * The step after the solve in the reference's papers

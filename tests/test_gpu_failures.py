@@ -131,3 +131,45 @@ def test_checkpoint_resume_is_bit_identical(tmp_path, precision, linesearch, pre
         _close(c2, f2, g2)
     finally:
         _close(f, g, ctx)
+
+
+@pytest.mark.parametrize("precision,linesearch", [(0, _lib.LS_SECANT), (1, _lib.LS_SECANT),
+                                                  (0, _lib.LS_QUADRATIC_REF)])
+def test_per_iteration_log(tmp_path, precision, linesearch):
+    """deft_cg_set_log: one JSON line per deft_cg_step with the step's
+    iteration, energy, gradient norm and counters as deft_cg_status reports
+    them, and the energies of the terms of the last evaluation; NULL stops
+    the log, a path that cannot be opened is an argument error."""
+    import json
+    from tests.capi import CG
+    s, ctx, g, f = _problem(precision)
+    path = os.path.join(tmp_path, "cg.jsonl")
+    try:
+        cg = CG(f, linesearch=linesearch, gtol=1e-9, maxiter=400,
+                step=1.0 if linesearch == _lib.LS_SECANT else 0.1)
+        cg.set_x(s.n0.reshape(-1))
+        _lib.check(f.L.deft_cg_set_log(cg.h, path.encode()))
+        seen = []
+        for _ in range(400):
+            code, st = cg.step()
+            assert code == 0
+            seen.append((st.iter, st.energy, st.gnorm, st.evals, st.converged))
+            if st.converged:
+                break
+        _lib.check(f.L.deft_cg_set_log(cg.h, None))
+        cg.step()  # not logged
+        recs = [json.loads(line) for line in open(path)]
+        assert len(recs) == len(seen)
+        for r, (it, E, gn, ev, conv) in zip(recs, seen):
+            assert (r["iter"], r["evals"], r["converged"]) == (it, ev, conv)
+            assert r["energy"] == E and r["gnorm"] == gn
+            assert set(r["terms"]) == {"hs_phi3", "hs_phi1", "hs_phi2", "ideal_gas",
+                                       "chemical_potential", "external_potential"}
+            assert all(np.isfinite(v) for v in r["terms"].values())
+        assert recs[-1]["converged"] == 1
+        # the terms of the last evaluation add up to an energy near the final one
+        assert abs(sum(recs[-1]["terms"].values()) / recs[-1]["energy"] - 1) < 1e-6
+        assert f.L.deft_cg_set_log(cg.h, str(tmp_path).encode()) == _lib.ERR_ARG
+        cg.close()
+    finally:
+        _close(f, g, ctx)
