@@ -16,7 +16,8 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libdeft_gb300.so")
 
-SOURCES = ["fmt_engine.cu", "deft_capi.cu", "batch.cu", "fno.cu", "contact.cu", "tensor.cu", "saft.cu"]
+SOURCES = ["fmt_engine.cu", "deft_capi.cu", "batch.cu", "fno.cu", "contact.cu", "tensor.cu", "saft.cu",
+           "devcg.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
          "--expt-relaxed-constexpr", "-I" + os.path.join(ROOT, "include")]

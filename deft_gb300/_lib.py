@@ -10,7 +10,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libdeft_gb300.so")
 
 OK = 0
-ERR_ARG, ERR_CUDA, ERR_NAN, ERR_LINESEARCH, ERR_MAXITER, ERR_NOMEM = 1, 2, 3, 4, 5, 6
+ERR_ARG, ERR_CUDA, ERR_NAN, ERR_LINESEARCH, ERR_MAXITER, ERR_NOMEM, ERR_TIMEOUT = 1, 2, 3, 4, 5, 6, 7
 TERM_HS, TERM_IDEAL, TERM_MU, TERM_VEXT, TERM_MASK, TERM_VEFF, TERM_SAFT = 1, 2, 4, 8, 16, 32, 64
 NTERMS = 6
 LS_SECANT, LS_QUADRATIC_REF, LS_NEW_API = 0, 1, 2
@@ -34,7 +34,7 @@ EXPORTS = (
     "deft_find_chemical_potential",
     "deft_fmt_energy_grad_noalloc", "deft_noalloc_scratch_bytes",
     "deft_cg_create", "deft_cg_destroy", "deft_cg_set_params", "deft_cg_set_x", "deft_cg_get_x", "deft_cg_x_device",
-    "deft_cg_step", "deft_cg_solve", "deft_cg_checkpoint", "deft_cg_restore", "deft_cg_set_log", "deft_batch_solve",
+    "deft_cg_step", "deft_cg_solve", "deft_cg_solve_device", "deft_cg_checkpoint", "deft_cg_restore", "deft_cg_set_log", "deft_batch_solve",
     "deft_fno_create", "deft_fno_destroy", "deft_fno_param_count", "deft_fno_get_params",
     "deft_fno_set_params", "deft_fno_eval", "deft_fno_adam", "deft_fno_train_step",
     "deft_fno_warm_start", "deft_fno_initial_density", "deft_fno_launches",
@@ -60,7 +60,7 @@ class CgParams(ctypes.Structure):
                 ("step", ctypes.c_double), ("precision", ctypes.c_double),
                 ("refine_rel", ctypes.c_double), ("preconditioned", ctypes.c_int),
                 ("refine_abs", ctypes.c_double), ("relative_precision", ctypes.c_double),
-                ("miniter", ctypes.c_int)]
+                ("miniter", ctypes.c_int), ("device_loops", ctypes.c_int)]
 
 
 class CgStatus(ctypes.Structure):
@@ -144,6 +144,7 @@ def load():
         "deft_cg_x_device": (_vp, [_vp]),
         "deft_cg_step": (ctypes.c_int, [_vp, ctypes.POINTER(CgStatus)]),
         "deft_cg_solve": (ctypes.c_int, [_vp, ctypes.POINTER(CgStatus)]),
+        "deft_cg_solve_device": (ctypes.c_int, [_vp, ctypes.POINTER(CgStatus)]),
         "deft_cg_checkpoint": (ctypes.c_int, [_vp, ctypes.c_char_p]),
         "deft_cg_restore": (ctypes.c_int, [_vp, ctypes.c_char_p]),
         "deft_cg_set_log": (ctypes.c_int, [_vp, ctypes.c_char_p]),

@@ -5,6 +5,7 @@
 // scalars (energies and dot products) come back.
 #include "../../include/deft_gb300.h"
 #include "contact.h"
+#include "devcg.h"
 #include "fmt_engine.h"
 #include "saft.h"
 #include "tensor.h"
@@ -84,6 +85,11 @@ struct deft_cg {
   bool last_eval_mixed = false;          // c->g / c->E came from the FP32 evaluator
   double *q = nullptr, *dxv = nullptr;  // refinement work vectors
   FILE *log = nullptr;                  // per-step JSONL records (deft_cg_set_log)
+  // device-driven solve (deft_cg_solve_device): its graph and what it bakes in
+  deft::DcgGraph *dgraph = nullptr;
+  int dkey_terms = -1, dkey_hs = -1, dkey_prec = -1;
+  double dkey_kT = 0;
+  const double *dkey_V = nullptr, *dkey_mask = nullptr;
 };
 
 namespace {
@@ -922,6 +928,7 @@ int deft_cg_destroy(deft_cg *c) {
   cudaFree(c->q);
   cudaFree(c->dxv);
   if (c->log) fclose(c->log);
+  deft::dcg_free(c->dgraph);
   delete c;
   return DEFT_OK;
 }
@@ -1708,6 +1715,97 @@ int deft_cg_solve(deft_cg *c, deft_cg_status *st) {
     if (s) return s;
     if (st->converged) return DEFT_OK;
   }
+}
+
+int deft_cg_solve_device(deft_cg *c, deft_cg_status *st) {
+  if (!c || !st) return set_err(DEFT_ERR_ARG, "NULL argument");
+  deft_fmt *f = c->f;
+  cudaSetDevice(f->grid->ctx->device);
+  if (int s = check_terms(f)) return s;
+  if (c->p.linesearch != DEFT_LS_SECANT || c->p.preconditioned != DEFT_PC_DENSITY)
+    return set_err(DEFT_ERR_ARG, "device-driven solves use DEFT_LS_SECANT with DEFT_PC_DENSITY");
+  if (c->p.precision > 0)
+    return set_err(DEFT_ERR_ARG, "device-driven solves stop on gtol (no Precision rule)");
+  if ((f->p.terms & (DEFT_TERM_VEFF | DEFT_TERM_SAFT)) || is_tensor(f))
+    return set_err(DEFT_ERR_ARG,
+                   "device-driven solves take the fused functionals in the density variable");
+  const size_t bytes = sizeof(double) * nr(f->grid);
+  if (!c->q) {
+    cudaError_t ce = cudaMalloc((void **)&c->q, bytes);
+    if (ce == cudaSuccess) ce = cudaMalloc((void **)&c->dxv, bytes);
+    if (ce != cudaSuccess) return cuda_err(ce, "cudaMalloc");
+  }
+  const deft::FmtSpec spec = spec_of(f);
+  const double *V = (spec.terms & DEFT_TERM_VEXT) ? f->V : nullptr;
+  const double *mask = (spec.terms & DEFT_TERM_MASK) ? f->mask : nullptr;
+  if (c->dgraph && (c->dkey_terms != spec.terms || c->dkey_hs != spec.hs ||
+                    c->dkey_prec != spec.precision || c->dkey_kT != spec.kT ||
+                    c->dkey_V != V || c->dkey_mask != mask)) {
+    deft::dcg_free(c->dgraph);
+    c->dgraph = nullptr;
+  }
+  Engine *e = f->grid->eng;
+  deft::DcgConfig cf;
+  cf.mixed = spec.precision == deft::kPrecisionMixed;
+  cf.gtol = c->p.gtol;
+  cf.refine_rel = c->p.refine_rel;
+  cf.refine_abs = c->p.refine_abs;
+  cf.step = c->p.step;
+  cf.maxiter = c->p.maxiter;
+  cf.max_loops = c->p.device_loops > 0 ? c->p.device_loops
+                 : c->p.maxiter > 0    ? 64 * c->p.maxiter + 64
+                                       : 20000;
+  if (!c->dgraph) {
+    if (e->dev_prepare(spec)) return eng_err(e);
+    deft::DcgProblem p;
+    p.eng = e;
+    p.spec = spec;
+    p.v = {c->x, c->g, c->d, c->gold, c->pg, c->q, c->dxv, V, mask};
+    p.cfg = cf;
+    std::string err;
+    c->dgraph = deft::dcg_build(&p, 1, &err);
+    if (!c->dgraph) return set_err(DEFT_ERR_CUDA, err);
+    c->dkey_terms = spec.terms;
+    c->dkey_hs = spec.hs;
+    c->dkey_prec = spec.precision;
+    c->dkey_kT = spec.kT;
+    c->dkey_V = V;
+    c->dkey_mask = mask;
+  }
+  deft::dcg_set_config(c->dgraph, 0, cf, spec);
+  deft::DcgOutcome o;
+  std::string err;
+  if (int s = deft::dcg_run(c->dgraph, f->grid->ctx->stream, &o, &err)) return set_err(s, err);
+  // the host minimiser restarts its directions from here
+  c->iter = o.iter;
+  c->evals = o.evals;
+  c->evals_fp64 = o.evals_fp64;
+  c->hvps = o.hvps;
+  c->stage = o.stage;
+  c->done = o.converged != 0;
+  c->have_g = false;
+  c->e_valid = false;
+  c->slope_ok = false;
+  c->goldsqr = 0;
+  c->pgoldsqr = 0;
+  c->last_eval_mixed = false;
+  st->iter = o.iter;
+  st->evals = o.evals;
+  st->energy = o.energy;
+  st->gnorm = o.gnorm;
+  st->converged = o.converged;
+  st->status = o.status;
+  st->evals_fp64 = o.evals_fp64;
+  st->hvps = o.hvps;
+  st->stage = o.stage;
+  if (o.status) {
+    static const char *what[] = {"", "", "", "energy or gradient is not finite",
+                                 "line search found no acceptable step",
+                                 "CG iteration limit reached", "",
+                                 "device-driven solve used up its loop budget"};
+    return set_err(o.status, o.status < 8 ? what[o.status] : "device-driven solve failed");
+  }
+  return DEFT_OK;
 }
 
 }  // extern "C"

@@ -2571,9 +2571,11 @@ class EngineImpl {
                                                       gd ? gd->partials : nullptr,
                                                       gd ? gd->k : 0, gblk);
     post(kK_reduce_terms);
-    cudaMemcpyAsync(results_host, results, sizeof(double) * (gd ? 11 : 8), cudaMemcpyDeviceToHost,
-                    stream);
+    if (!dev_only)
+      cudaMemcpyAsync(results_host, results, sizeof(double) * (gd ? 11 : 8),
+                      cudaMemcpyDeviceToHost, stream);
   }
+  bool dev_only = false;  // leave the results in device memory (device-driven solves)
 
   int finish_energy(double *E_host, double *terms_host, int kd = 0, double *dots_host = nullptr) {
     cudaError_t e = cudaStreamSynchronize(stream);
@@ -2948,6 +2950,46 @@ int Engine::scal_add_dot(double beta, double *d, double alpha, const double *g, 
   e.post(kK_scal_add);
   return e.read_results(1, out_host, "scal_add_dot");
 }
+
+int Engine::dev_prepare(const FmtSpec &f) {
+  EngineImpl &e = *impl_;
+  if (f.terms & kTermHS) {
+    if (e.ensure_table<float>(f.R)) return -1;
+    if (e.df_on ? e.ensure_table<dfl>(f.R) : e.ensure_table<double>(f.R)) return -1;
+  }
+  if (e.upload_args(f)) return -1;
+  if (!e.hess && (e.alloc(&e.hess, sizeof(float) * kHessPacked * (size_t)e.g.NR) ||
+                  e.alloc(&e.hloc, sizeof(float) * (size_t)e.g.NR)))
+    return -1;
+  const cudaError_t r = cudaStreamSynchronize(e.stream);
+  return r == cudaSuccess ? 0 : e.fail("device-driven set-up", r);
+}
+
+int Engine::dev_eval(const FmtSpec &f, const double *n, const double *V, const double *mask,
+                     double *grad, int kd, const double *const *db) {
+  EngineImpl &e = *impl_;
+  GradDots gd{};
+  for (int i = 0; i < kd; i++) gd.b[i] = db[i] == grad ? nullptr : db[i];
+  gd.k = kd;
+  gd.partials = e.grad_partials;
+  const GradDots *pg = grad && kd > 0 ? &gd : nullptr;
+  e.dev_only = true;
+  int r;
+  if (f.precision == kPrecisionMixed) r = e.eval_launch<float>(f, n, V, mask, grad, pg);
+  else if (e.df_on) r = e.eval_launch<dfl>(f, n, V, mask, grad, pg);
+  else r = e.eval_launch<double>(f, n, V, mask, grad, pg);
+  e.dev_only = false;
+  return r;
+}
+
+int Engine::dev_hess_setup(const FmtSpec &f, const double *n) { return impl_->hess_setup(f, n); }
+
+int Engine::dev_hvp(const FmtSpec &f, const double *dx, const double *mask, double *out) {
+  return impl_->hvp_launch(f, dx, mask, out, true);
+}
+
+double *Engine::dev_results() const { return impl_->results; }
+int Engine::vector_blocks() const { return impl_->dot_blocks; }
 
 int Engine::newton_update(const FmtSpec &f, const double *n, double alpha, const double *p,
                           const double *q, double *dx, double *r, const double *mask, double *z,

@@ -170,6 +170,24 @@ class Engine {
 
   const char *last_error() const;
 
+  // Device-driven solves (devcg.cu).  These only queue kernels: their scalar
+  // results stay in device memory, so the sequences can be captured into the
+  // bodies of conditional graph nodes.  dev_prepare (weight tables of both
+  // forms, parameters, Hessian buffers) runs first, outside any capture.
+  int dev_prepare(const FmtSpec &f);
+  // Energy and gradient in f's precision, with the dot products grad.db[i]
+  // (i < kd <= 3; db[i] == grad: |grad|^2) taken by the gradient kernel:
+  // energy at dev_results()[6], terms at [0..6), dots at [8..8+kd).
+  int dev_eval(const FmtSpec &f, const double *n, const double *V, const double *mask,
+               double *grad, int kd, const double *const *db);
+  int dev_hess_setup(const FmtSpec &f, const double *n);
+  // out = H dx (FP32 transforms), dx.out at dev_results()[0].
+  int dev_hvp(const FmtSpec &f, const double *dx, const double *mask, double *out);
+  double *dev_results() const;
+  // Blocks of the FP64 vector kernels (a multiple of the SM count, at most
+  // one block per 256 points).
+  int vector_blocks() const;
+
  private:
   explicit Engine(EngineImpl *impl);
   EngineImpl *impl_;

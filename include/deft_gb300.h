@@ -32,6 +32,7 @@ extern "C" {
 #define DEFT_ERR_LINESEARCH 4  /* line search found no acceptable step */
 #define DEFT_ERR_MAXITER 5     /* iteration limit reached before the tolerance */
 #define DEFT_ERR_NOMEM 6       /* device allocation failed */
+#define DEFT_ERR_TIMEOUT 7     /* a device-driven solve used up its loop budget */
 
 /* Terms of the composed functional. */
 #define DEFT_TERM_HS 1     /* HardSpheresWBnotensor(R), src/HardSpheres.cpp:137-159 */
@@ -120,6 +121,8 @@ typedef struct {
   double relative_precision; /* DEFT_LS_NEW_API: Minimize::set_relative_precision
                                 (0 = the constructor's 1e-15) */
   int miniter;               /* DEFT_LS_NEW_API: Minimize::set_miniter (0 = the constructor's 6) */
+  int device_loops; /* deft_cg_solve_device: budget of device loop passes (one evaluation or
+                       Hessian-vector product each); 0 = 64 per maxiter, 20000 without one */
 } deft_cg_params;
 
 typedef struct {
@@ -279,6 +282,20 @@ double *deft_cg_x_device(deft_cg *cg);
 int deft_cg_step(deft_cg *cg, deft_cg_status *st);
 /* improve_energy() until converged, an error, or maxiter. */
 int deft_cg_solve(deft_cg *cg, deft_cg_status *st);
+/* The same minimisation driven from the device (no reference counterpart:
+ * the reference's loop is `while (min.improve_energy())`, e.g.
+ * papers/contact/figs/walls.cpp:104-110): one CUDA graph launch runs the
+ * whole solve, every line-search, direction and stop decision taken by a
+ * kernel from scalars in device memory, so the host waits once.  For
+ * DEFT_LS_SECANT with DEFT_PC_DENSITY, without the Precision rule, on the
+ * fused functionals (no DEFT_TERM_VEFF / SAFT, no tensor kinds): FP64 form
+ * (the secant CG to gtol) or mixed form (FP32 stage, then Newton steps on
+ * the FP64 gradient).  Starts from the current x (deft_cg_set_x); the loop
+ * budget (device_loops) ends a solve that has not converged with
+ * DEFT_ERR_TIMEOUT.  The graph is built on the
+ * first call and reused while the functional's terms, kT and fields stay
+ * the same.  Afterwards the host minimiser restarts its directions. */
+int deft_cg_solve_device(deft_cg *cg, deft_cg_status *st);
 /* Checkpoint / resume (no reference counterpart): `path` gets the
  * minimiser's vectors (x, direction, previous gradient, gradient[, pgrad]) as
  * raw little-endian FP64 and `path`.json a header with the grid shape and

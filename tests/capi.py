@@ -115,11 +115,11 @@ class Fmt:
 class CG:
     def __init__(self, fmt, linesearch=_lib.LS_SECANT, gtol=1e-9, maxiter=0, step=1.0,
                  precision=0.0, refine_rel=0.0, preconditioned=0, refine_abs=0.0,
-                 relative_precision=0.0, miniter=0):
+                 relative_precision=0.0, miniter=0, device_loops=0):
         self.L = fmt.L
         self.size = fmt.grid.size
         p = _lib.CgParams(linesearch, gtol, maxiter, step, precision, refine_rel, preconditioned,
-                          refine_abs, relative_precision, miniter)
+                          refine_abs, relative_precision, miniter, device_loops)
         h = ctypes.c_void_p()
         check(self.L.deft_cg_create(fmt.h, ctypes.byref(p), ctypes.byref(h)))
         self.h = h
@@ -140,6 +140,10 @@ class CG:
 
     def solve(self):
         s = self.L.deft_cg_solve(self.h, ctypes.byref(self.st))
+        return s, self.st
+
+    def solve_device(self):
+        s = self.L.deft_cg_solve_device(self.h, ctypes.byref(self.st))
         return s, self.st
 
     def close(self):
