@@ -89,7 +89,7 @@ struct deft_cg {
   deft::DcgGraph *dgraph = nullptr;
   int dkey_terms = -1, dkey_hs = -1, dkey_prec = -1;
   double dkey_kT = 0;
-  const double *dkey_V = nullptr, *dkey_mask = nullptr;
+  const double *dkey_V = nullptr, *dkey_mask = nullptr, *dkey_pg = nullptr;
 };
 
 namespace {
@@ -1717,10 +1717,12 @@ int deft_cg_solve(deft_cg *c, deft_cg_status *st) {
   }
 }
 
-int deft_cg_solve_device(deft_cg *c, deft_cg_status *st) {
-  if (!c || !st) return set_err(DEFT_ERR_ARG, "NULL argument");
+namespace {
+
+// Checks that cg can run device-driven, allocates its Newton vectors and
+// fills the problem (engine, spec, vectors, settings) and key fields.
+int device_problem(deft_cg *c, deft::DcgProblem *p) {
   deft_fmt *f = c->f;
-  cudaSetDevice(f->grid->ctx->device);
   if (int s = check_terms(f)) return s;
   if (c->p.linesearch != DEFT_LS_SECANT || c->p.preconditioned != DEFT_PC_DENSITY)
     return set_err(DEFT_ERR_ARG, "device-driven solves use DEFT_LS_SECANT with DEFT_PC_DENSITY");
@@ -1738,14 +1740,8 @@ int deft_cg_solve_device(deft_cg *c, deft_cg_status *st) {
   const deft::FmtSpec spec = spec_of(f);
   const double *V = (spec.terms & DEFT_TERM_VEXT) ? f->V : nullptr;
   const double *mask = (spec.terms & DEFT_TERM_MASK) ? f->mask : nullptr;
-  if (c->dgraph && (c->dkey_terms != spec.terms || c->dkey_hs != spec.hs ||
-                    c->dkey_prec != spec.precision || c->dkey_kT != spec.kT ||
-                    c->dkey_V != V || c->dkey_mask != mask)) {
-    deft::dcg_free(c->dgraph);
-    c->dgraph = nullptr;
-  }
   Engine *e = f->grid->eng;
-  deft::DcgConfig cf;
+  deft::DcgConfig &cf = p->cfg;
   cf.mixed = spec.precision == deft::kPrecisionMixed;
   cf.gtol = c->p.gtol;
   cf.refine_rel = c->p.refine_rel;
@@ -1755,28 +1751,15 @@ int deft_cg_solve_device(deft_cg *c, deft_cg_status *st) {
   cf.max_loops = c->p.device_loops > 0 ? c->p.device_loops
                  : c->p.maxiter > 0    ? 64 * c->p.maxiter + 64
                                        : 20000;
-  if (!c->dgraph) {
-    if (e->dev_prepare(spec)) return eng_err(e);
-    deft::DcgProblem p;
-    p.eng = e;
-    p.spec = spec;
-    p.v = {c->x, c->g, c->d, c->gold, c->pg, c->q, c->dxv, V, mask};
-    p.cfg = cf;
-    std::string err;
-    c->dgraph = deft::dcg_build(&p, 1, &err);
-    if (!c->dgraph) return set_err(DEFT_ERR_CUDA, err);
-    c->dkey_terms = spec.terms;
-    c->dkey_hs = spec.hs;
-    c->dkey_prec = spec.precision;
-    c->dkey_kT = spec.kT;
-    c->dkey_V = V;
-    c->dkey_mask = mask;
-  }
-  deft::dcg_set_config(c->dgraph, 0, cf, spec);
-  deft::DcgOutcome o;
-  std::string err;
-  if (int s = deft::dcg_run(c->dgraph, f->grid->ctx->stream, &o, &err)) return set_err(s, err);
-  // the host minimiser restarts its directions from here
+  p->eng = e;
+  p->spec = spec;
+  p->v = {c->x, c->g, c->d, c->gold, c->pg, c->q, c->dxv, V, mask};
+  return DEFT_OK;
+}
+
+// Copies a device-driven outcome into the minimiser (which restarts its
+// directions from there) and the status record.
+int device_outcome(deft_cg *c, const deft::DcgOutcome &o, deft_cg_status *st) {
   c->iter = o.iter;
   c->evals = o.evals;
   c->evals_fp64 = o.evals_fp64;
@@ -1806,6 +1789,101 @@ int deft_cg_solve_device(deft_cg *c, deft_cg_status *st) {
     return set_err(o.status, o.status < 8 ? what[o.status] : "device-driven solve failed");
   }
   return DEFT_OK;
+}
+
+}  // namespace
+
+int deft_cg_solve_device(deft_cg *c, deft_cg_status *st) {
+  if (!c || !st) return set_err(DEFT_ERR_ARG, "NULL argument");
+  deft_fmt *f = c->f;
+  cudaSetDevice(f->grid->ctx->device);
+  deft::DcgProblem p;
+  if (int s = device_problem(c, &p)) return s;
+  const deft::FmtSpec &spec = p.spec;
+  if (c->dgraph && (c->dkey_terms != spec.terms || c->dkey_hs != spec.hs ||
+                    c->dkey_prec != spec.precision || c->dkey_kT != spec.kT ||
+                    c->dkey_V != p.v.V || c->dkey_mask != p.v.mask || c->dkey_pg != p.v.pg)) {
+    deft::dcg_free(c->dgraph);
+    c->dgraph = nullptr;
+  }
+  if (!c->dgraph) {
+    if (p.eng->dev_prepare(spec)) return eng_err(p.eng);
+    std::string err;
+    c->dgraph = deft::dcg_build(&p, 1, &err);
+    if (!c->dgraph) return set_err(DEFT_ERR_CUDA, err);
+    c->dkey_terms = spec.terms;
+    c->dkey_hs = spec.hs;
+    c->dkey_prec = spec.precision;
+    c->dkey_kT = spec.kT;
+    c->dkey_V = p.v.V;
+    c->dkey_mask = p.v.mask;
+    c->dkey_pg = p.v.pg;
+  }
+  deft::dcg_set_config(c->dgraph, 0, p.cfg, spec);
+  deft::DcgOutcome o;
+  std::string err;
+  if (int s = deft::dcg_run(c->dgraph, f->grid->ctx->stream, &o, &err)) return set_err(s, err);
+  return device_outcome(c, o, st);
+}
+
+int deft_batch_solve_device(int device, int count, const deft_batch_problem *probs,
+                            const deft_cg_params *cgp, deft_cg_status *status_out) {
+  if (count < 0 || (count && (!probs || !cgp || !status_out)))
+    return set_err(DEFT_ERR_ARG, "NULL argument");
+  if (count == 0) return DEFT_OK;
+  deft_ctx *ctx = nullptr;
+  if (int s = deft_ctx_create(device, &ctx)) return s;
+  std::vector<deft_grid *> grids(count, nullptr);
+  std::vector<deft_fmt *> fmts(count, nullptr);
+  std::vector<deft_cg *> cgs(count, nullptr);
+  std::vector<deft::DcgProblem> pr(count);
+  deft::DcgGraph *gr = nullptr;
+  int s = DEFT_OK;
+  for (int i = 0; i < count && !s; i++) {
+    const deft_batch_problem &p = probs[i];
+    memset(&status_out[i], 0, sizeof(deft_cg_status));
+    s = deft_grid_create(ctx, p.lat, p.N[0], p.N[1], p.N[2], &grids[i]);
+    deft_fmt_params fp{};
+    fp.functional = p.functional;
+    fp.R = p.R;
+    fp.kT = p.kT;
+    fp.mu = p.mu;
+    fp.terms = p.terms;
+    fp.precision = p.precision;
+    if (!s) s = deft_fmt_create(grids[i], &fp, &fmts[i]);
+    if (!s && p.mask) s = deft_fmt_set_mask(fmts[i], p.mask, 0);
+    if (!s && p.V) s = deft_fmt_set_vext(fmts[i], p.V, 0);
+    if (!s) s = deft_cg_create(fmts[i], cgp, &cgs[i]);
+    if (!s) s = deft_cg_set_x(cgs[i], p.n_init, 0);
+    if (!s) s = device_problem(cgs[i], &pr[i]);
+    if (!s && pr[i].eng->dev_prepare(pr[i].spec)) s = eng_err(pr[i].eng);
+    if (s) g_err = "problem " + std::to_string(i) + ": " + g_err;
+  }
+  std::string err;
+  if (!s) {
+    gr = deft::dcg_build(pr.data(), count, &err);
+    if (!gr) s = set_err(DEFT_ERR_CUDA, err);
+  }
+  std::vector<deft::DcgOutcome> out(count);
+  if (!s && (s = deft::dcg_run(gr, ctx->stream, out.data(), &err))) set_err(s, err);
+  int first = DEFT_OK;
+  for (int i = 0; i < count && !s; i++) {
+    const int r = device_outcome(cgs[i], out[i], &status_out[i]);
+    if (r && !first) {
+      first = r;
+      g_err = "problem " + std::to_string(i) + ": " + g_err;
+    }
+    if (probs[i].n_out && deft_cg_get_x(cgs[i], probs[i].n_out, 0) && !first)
+      first = DEFT_ERR_CUDA;
+  }
+  deft::dcg_free(gr);
+  for (int i = 0; i < count; i++) {
+    deft_cg_destroy(cgs[i]);
+    deft_fmt_destroy(fmts[i]);
+    deft_grid_destroy(grids[i]);
+  }
+  deft_ctx_destroy(ctx);
+  return s ? s : first;
 }
 
 }  // extern "C"

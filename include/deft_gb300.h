@@ -363,6 +363,14 @@ typedef struct {
 /* Returns DEFT_OK or the first error; status_out[i] holds problem i's result. */
 int deft_batch_solve(int device, int count, const deft_batch_problem *problems,
                      const deft_batch_params *params, deft_cg_status *status_out);
+/* The same batch as one launch: every problem gets its own grid and
+ * minimiser, and one CUDA graph holds their device-driven solves
+ * (deft_cg_solve_device) as independent conditional WHILE nodes, so all of
+ * them run concurrently from a single cudaGraphLaunch and the host waits
+ * once.  cg must be DEFT_LS_SECANT with DEFT_PC_DENSITY (no Precision rule);
+ * n_out gets each converged profile; status_out[i] each outcome. */
+int deft_batch_solve_device(int device, int count, const deft_batch_problem *problems,
+                            const deft_cg_params *cg, deft_cg_status *status_out);
 
 /* ---- learned warm start ----
  * A 3-D Fourier neural operator (no reference counterpart) that maps a

@@ -150,9 +150,12 @@ class CG:
         self.L.deft_cg_destroy(self.h)
 
 
-def batch_solve(problems, precision=0, workers=4, gtol=1e-9, device=0):
-    """Runs deft_batch_solve on workloads.Slit-like problems (host arrays);
-    returns (status code, list of CgStatus, list of converged profiles)."""
+def batch_solve(problems, precision=0, workers=4, gtol=1e-9, device=0, preconditioned=0,
+                device_driven=False):
+    """Runs deft_batch_solve (or, device_driven, deft_batch_solve_device with
+    the density preconditioner) on workloads.Slit-like problems (host
+    arrays); returns (status code, list of CgStatus, list of converged
+    profiles)."""
     keep = []
     arr = (_lib.BatchProblem * len(problems))()
     outs = []
@@ -174,7 +177,13 @@ def batch_solve(problems, precision=0, workers=4, gtol=1e-9, device=0):
         p.V = None
         p.n_init = n0.ctypes.data
         p.n_out = out.ctypes.data
-    bp = _lib.BatchParams(workers, _lib.CgParams(_lib.LS_SECANT, gtol, 20000, 1.0, 0.0, 0.0))
     st = (_lib.CgStatus * len(problems))()
-    code = _lib.load().deft_batch_solve(device, len(problems), arr, ctypes.byref(bp), st)
+    if device_driven:
+        cp = _lib.CgParams(_lib.LS_SECANT, gtol, 20000, 1.0, 0.0, 0.0, _lib.PC_DENSITY)
+        code = _lib.load().deft_batch_solve_device(device, len(problems), arr, ctypes.byref(cp),
+                                                   st)
+    else:
+        bp = _lib.BatchParams(workers, _lib.CgParams(_lib.LS_SECANT, gtol, 20000, 1.0, 0.0, 0.0,
+                                                     preconditioned))
+        code = _lib.load().deft_batch_solve(device, len(problems), arr, ctypes.byref(bp), st)
     return code, list(st), outs
