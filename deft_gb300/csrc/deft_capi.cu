@@ -1034,7 +1034,8 @@ int cg_eval_dots(deft_cg *c, const deft::FmtSpec &spec, int k, const double *con
     return e->dots(k, a, b, out) ? eng_err(e) : DEFT_OK;
   }
   double E;
-  if (e->energy_grad_dots(spec, c->x, c->f->V, c->f->mask, c->g, &E, k, a, b, out))
+  if (e->energy_grad_dots(spec, c->x, c->f->V, c->f->mask, c->g, &E, k, a, b, out,
+                         c->f->last_terms))
     return eng_err(e);
   if (c->pg && c->p.preconditioned != DEFT_PC_DENSITY && e->copy(c->g, c->pg)) return eng_err(e);
   c->evals++;

@@ -56,7 +56,13 @@ struct DcgState {
   // results of the vector kernels' reductions, and their block counter
   double red[2];
   unsigned int counter;
+  // executions of each launch sequence (kSeq*), for the launch accounting
+  int runs[10];
 };
+
+// Launch sequences of one solve's graph, counted per execution.
+enum DcgSeq { kSeqLoop, kSeqTrial, kSeqDirection, kSeqOuter, kSeqBacktrack, kSeqSetup,
+              kSeqProduct, kSeqUpdate, kSeqPUpdate, kSeqApply, kNumSeq };
 
 // ---------------------------------------------------------------------------
 // Reductions: per-block sums in a fixed order, summed by the last block to
@@ -227,8 +233,13 @@ __device__ void stage_end(DcgState *st) {
   }
 }
 
-__global__ void k_dcg_begin(const DcgState *st, cudaGraphConditionalHandle h_sw) {
-  if (threadIdx.x == 0) cudaGraphSetConditional(h_sw, st->mode < kModeDone ? st->mode : 3);
+__global__ void k_dcg_begin(DcgState *st, cudaGraphConditionalHandle h_sw) {
+  if (threadIdx.x) return;
+  const int m = st->mode;
+  if (m == kModeStage) st->runs[kSeqTrial]++;
+  else if (m == kModeNewtonOuter) st->runs[kSeqOuter]++;
+  else if (m == kModeNewtonInner) st->runs[kSeqProduct]++;
+  cudaGraphSetConditional(h_sw, m < kModeDone ? m : 3);
 }
 
 // After the stage's evaluation at x = x0 + at d: the secant search's step
@@ -256,6 +267,7 @@ __global__ void k_dcg_decide_stage(DcgState *st, const double *__restrict__ res,
       if (gn < st->thr) stage_end(st);
       else dir = 1;
     }
+    st->runs[kSeqDirection] += dir;
     cudaGraphSetConditional(h_dir, dir);
     return;
   }
@@ -282,6 +294,7 @@ __global__ void k_dcg_decide_stage(DcgState *st, const double *__restrict__ res,
     } else {
       dir = 1;
     }
+    st->runs[kSeqDirection] += dir;
     cudaGraphSetConditional(h_dir, dir);
     return;
   } else if (s < 0 && E <= st->E0 + etol) {
@@ -413,6 +426,8 @@ __global__ void k_dcg_decide_outer(DcgState *st, const double *__restrict__ res,
       }
     }
   }
+  st->runs[kSeqBacktrack] += bt;
+  st->runs[kSeqSetup] += setup;
   cudaGraphSetConditional(h_bt, bt);
   cudaGraphSetConditional(h_setup, setup);
 }
@@ -446,10 +461,12 @@ __global__ void k_dcg_decide_product(DcgState *st, const double *__restrict__ re
   if (!(pq > 0)) {
     // no positive curvature along p: keep the step so far
     finish_inner(st);
+    st->runs[kSeqApply]++;
     cudaGraphSetConditional(h_upd, 0);
     cudaGraphSetConditional(h_apply, 1);
   } else {
     st->alpha_n = st->rz / pq;
+    st->runs[kSeqUpdate]++;
     cudaGraphSetConditional(h_upd, 1);
     cudaGraphSetConditional(h_apply, 0);
   }
@@ -463,11 +480,13 @@ __global__ void k_dcg_decide_update(DcgState *st, cudaGraphConditionalHandle h_p
   st->inner_k++;
   if (sqrt(rr) < st->tol_in || st->inner_k >= 400 || !(rz > 0)) {
     finish_inner(st);
+    st->runs[kSeqApply]++;
     cudaGraphSetConditional(h_pupd, 0);
     cudaGraphSetConditional(h_apply, 1);
   } else {
     st->beta_n = rz / st->rz;
     st->rz = rz;
+    st->runs[kSeqPUpdate]++;
     cudaGraphSetConditional(h_pupd, 1);
   }
 }
@@ -534,8 +553,9 @@ struct Builder {
     for (unsigned i = 0; i < size; i++) bodies[i] = p.conditional.phGraph_out[i];
     return true;
   }
-  bool handle(cudaGraphConditionalHandle *h, unsigned def) {
-    const cudaError_t r = cudaGraphConditionalHandleCreate(h, top, def, cudaGraphCondAssignDefault);
+  // A handle belongs to the graph that holds its conditional node.
+  bool handle(cudaGraph_t g, cudaGraphConditionalHandle *h, unsigned def) {
+    const cudaError_t r = cudaGraphConditionalHandleCreate(h, g, def, cudaGraphCondAssignDefault);
     return r == cudaSuccess || fail("conditional handle", r);
   }
 };
@@ -544,10 +564,27 @@ struct Solve {
   DcgProblem p;
   DcgState *st = nullptr;     // device
   double *partials = nullptr;  // device, 2 per vector block
+  // launches per execution of each sequence, per engine accounting slot
+  std::vector<long long> seq[kNumSeq];
 };
 
 bool add_solve(Builder &b, Solve &sv) {
   Engine *e = sv.p.eng;
+  const int slots = e->launch_slots(), ctl = e->control_slot();
+  std::vector<long long> before(slots), after(slots);
+  for (auto &q : sv.seq) q.assign(slots, 0);
+  // captures one sequence: its engine launches (taken out of the engine's
+  // counters again) and `own` solver kernels go to sv.seq[k]
+  auto cap = [&](int k, int own, cudaGraph_t g, const std::vector<cudaGraphNode_t> &deps,
+                 auto fn, std::vector<cudaGraphNode_t> *sinks) {
+    e->launch_counts(before.data());
+    const bool ok = b.capture(e->stream(), g, deps, fn, sinks);
+    e->launch_counts(after.data());
+    e->launch_set(before.data());
+    for (int i = 0; i < slots; i++) sv.seq[k][i] += after[i] - before[i];
+    sv.seq[k][ctl] += own;
+    return ok;
+  };
   const DcgVectors &v = sv.p.v;
   cudaStream_t s = e->stream();
   const Geom &g = e->geom();
@@ -564,22 +601,22 @@ bool add_solve(Builder &b, Solve &sv) {
   f32.precision = kPrecisionMixed;
   const double *mask = v.mask;
 
+  // each handle is created on the graph that holds its conditional node,
+  // before the kernels that set it are captured
   cudaGraphConditionalHandle h_run, h_sw, h_dir, h_bt, h_setup, h_upd, h_pupd, h_apply;
-  if (!b.handle(&h_run, 1) || !b.handle(&h_sw, 0) || !b.handle(&h_dir, 0) ||
-      !b.handle(&h_bt, 0) || !b.handle(&h_setup, 0) || !b.handle(&h_upd, 0) ||
-      !b.handle(&h_pupd, 0) || !b.handle(&h_apply, 0))
-    return false;
   cudaGraphNode_t wnode, snode, n;
   cudaGraph_t wbody, sb[3], ib;
   std::vector<cudaGraphNode_t> sinks, none;
+  if (!b.handle(b.top, &h_run, 1)) return false;
   if (!b.cond(b.top, none, h_run, cudaGraphCondTypeWhile, 1, &wnode, &wbody)) return false;
-  if (!b.capture(s, wbody, none, [&] {
+  if (!b.handle(wbody, &h_sw, 0)) return false;
+  if (!cap(kSeqLoop, 1, wbody, none, [&] {
         k_dcg_begin<<<1, 32, 0, s>>>(st, h_sw);
         return true;
       }, &sinks))
     return false;
   if (!b.cond(wbody, sinks, h_sw, cudaGraphCondTypeSwitch, 3, &snode, sb)) return false;
-  if (!b.capture(s, wbody, {snode}, [&] {
+  if (!cap(kSeqLoop, 1, wbody, {snode}, [&] {
         k_dcg_end<<<1, 32, 0, s>>>(st, h_run);
         return true;
       }, nullptr))
@@ -587,7 +624,8 @@ bool add_solve(Builder &b, Solve &sv) {
 
   // 0: line-search trial
   const double *db3[3] = {v.d, v.g, v.gold};
-  if (!b.capture(s, sb[0], none, [&] {
+  if (!b.handle(sb[0], &h_dir, 0)) return false;
+  if (!cap(kSeqTrial, 2, sb[0], none, [&] {
         k_dcg_move<<<nb, kThreads, 0, s>>>(&st->coef, v.x, v.d, N);
         if (e->dev_eval(stage, v.x, v.V, mask, v.g, 3, db3)) return false;
         k_dcg_decide_stage<<<1, 32, 0, s>>>(st, res, h_dir);
@@ -595,7 +633,7 @@ bool add_solve(Builder &b, Solve &sv) {
       }, &sinks))
     return false;
   if (!b.cond(sb[0], sinks, h_dir, cudaGraphCondTypeIf, 1, &n, &ib)) return false;
-  if (!b.capture(s, ib, none, [&] {
+  if (!cap(kSeqDirection, 3, ib, none, [&] {
         k_dcg_precond_dots<<<nb, kThreads, 0, s>>>(st, v.x, v.g, mask, v.gold, inv_c, v.pg, N,
                                                    part);
         k_dcg_decide_direction<<<1, 32, 0, s>>>(st);
@@ -617,7 +655,8 @@ bool add_solve(Builder &b, Solve &sv) {
   // r in gold, z in g (the FP64 gradient is evaluated again after the
   // step), p in d, q, dx.
   const double *db1[1] = {v.g};
-  if (!b.capture(s, sb[1], none, [&] {
+  if (!b.handle(sb[1], &h_bt, 0) || !b.handle(sb[1], &h_setup, 0)) return false;
+  if (!cap(kSeqOuter, 2, sb[1], none, [&] {
         k_dcg_move<<<nb, kThreads, 0, s>>>(&st->coef, v.x, v.d, N);
         if (e->dev_eval(f64, v.x, v.V, mask, v.g, 1, db1)) return false;
         k_dcg_decide_outer<<<1, 32, 0, s>>>(st, res, h_bt, h_setup);
@@ -626,13 +665,13 @@ bool add_solve(Builder &b, Solve &sv) {
     return false;
   cudaGraphNode_t nbt;
   if (!b.cond(sb[1], sinks, h_bt, cudaGraphCondTypeIf, 1, &nbt, &ib)) return false;
-  if (!b.capture(s, ib, none, [&] {
+  if (!cap(kSeqBacktrack, 1, ib, none, [&] {
         k_dcg_move<<<nb, kThreads, 0, s>>>(&st->coef_dx, v.x, v.dx, N);
         return true;
       }, nullptr))
     return false;
   if (!b.cond(sb[1], {nbt}, h_setup, cudaGraphCondTypeIf, 1, &n, &ib)) return false;
-  if (!b.capture(s, ib, none, [&] {
+  if (!cap(kSeqSetup, 2, ib, none, [&] {
         if (e->dev_hess_setup(f32, v.x)) return false;
         k_dcg_newton_init<<<nb, kThreads, 0, s>>>(st, v.g, v.x, mask, inv_c, v.gold, v.d, v.dx,
                                                   N, part);
@@ -642,7 +681,8 @@ bool add_solve(Builder &b, Solve &sv) {
     return false;
 
   // 2: one product of the linear CG
-  if (!b.capture(s, sb[2], none, [&] {
+  if (!b.handle(sb[2], &h_upd, 0) || !b.handle(sb[2], &h_apply, 0)) return false;
+  if (!cap(kSeqProduct, 1, sb[2], none, [&] {
         if (e->dev_hvp(f32, v.d, mask, v.q)) return false;
         k_dcg_decide_product<<<1, 32, 0, s>>>(st, res, h_upd, h_apply);
         return true;
@@ -650,7 +690,8 @@ bool add_solve(Builder &b, Solve &sv) {
     return false;
   cudaGraphNode_t nupd;
   if (!b.cond(sb[2], sinks, h_upd, cudaGraphCondTypeIf, 1, &nupd, &ib)) return false;
-  if (!b.capture(s, ib, none, [&] {
+  if (!b.handle(ib, &h_pupd, 0)) return false;
+  if (!cap(kSeqUpdate, 2, ib, none, [&] {
         k_dcg_newton_update<<<nb, kThreads, 0, s>>>(st, v.d, v.q, v.dx, v.gold, v.x, mask, inv_c,
                                                     v.g, N, part);
         k_dcg_decide_update<<<1, 32, 0, s>>>(st, h_pupd, h_apply);
@@ -659,13 +700,13 @@ bool add_solve(Builder &b, Solve &sv) {
     return false;
   cudaGraph_t pb;
   if (!b.cond(ib, sinks, h_pupd, cudaGraphCondTypeIf, 1, &n, &pb)) return false;
-  if (!b.capture(s, pb, none, [&] {
+  if (!cap(kSeqPUpdate, 1, pb, none, [&] {
         k_dcg_p_update<<<nb, kThreads, 0, s>>>(st, v.d, v.g, N);
         return true;
       }, nullptr))
     return false;
   if (!b.cond(sb[2], {nupd}, h_apply, cudaGraphCondTypeIf, 1, &n, &ib)) return false;
-  if (!b.capture(s, ib, none, [&] {
+  if (!cap(kSeqApply, 1, ib, none, [&] {
         k_dcg_move<<<nb, kThreads, 0, s>>>(&st->coef_dx, v.x, v.dx, N);
         return true;
       }, nullptr))
@@ -752,9 +793,14 @@ DcgGraph *dcg_build(const DcgProblem *p, int count, std::string *err) {
       return nullptr;
     }
   }
-  r = cudaGraphInstantiate(&gr->exec, gr->graph, 0);
+  cudaGraphInstantiateParams ip = {};
+  r = cudaGraphInstantiateWithParams(&gr->exec, gr->graph, &ip);
   if (r != cudaSuccess) {
-    b.fail("instantiate", r);
+    cudaGraphNodeType t = cudaGraphNodeTypeCount;
+    if (ip.errNode_out) cudaGraphNodeGetType(ip.errNode_out, &t);
+    b.fail(("instantiate (result " + std::to_string((int)ip.result_out) + ", node type " +
+            std::to_string((int)t) + ")").c_str(),
+           r);
     dcg_free(gr);
     return nullptr;
   }
@@ -786,8 +832,10 @@ int dcg_run(DcgGraph *gr, cudaStream_t stream, DcgOutcome *out, std::string *err
   if (r == cudaSuccess) r = cudaStreamSynchronize(stream);
   if (r != cudaSuccess) return fail("solve", r);
   for (int i = 0; i < count; i++) {
-    const DcgState &s = gr->host[i];
+    DcgState &s = gr->host[i];
     DcgOutcome &o = out[i];
+    s.runs[kSeqLoop] = s.loops;
+    for (int k = 0; k < kNumSeq; k++) gr->solves[i].p.eng->launch_add(gr->solves[i].seq[k].data(), s.runs[k]);
     o.status = s.status;
     o.converged = s.converged;
     o.stage = s.mixed && s.evals_fp64 > 0 ? 1 : 0;

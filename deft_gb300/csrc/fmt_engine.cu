@@ -1825,13 +1825,13 @@ enum KernelId {
   kK_z_r2c, kK_z_c2r, kK_y_fft1, kK_y_fft5, kK_x_fft, kK_x_conv_fwd, kK_x_conv_adj, kK_z_phi_grad,
   kK_z_phi_energy, kK_z_grad, kK_local_energy, kK_reduce_terms, kK_dots, kK_axpy, kK_scal_add,
   kK_weight_table, kK_z_hess, kK_z_jac, kK_z_hvp_out, kK_veff_density, kK_veff_grad,
-  kK_diag_precond, kK_precond_dots, kK_newton_update, kNumKernels
+  kK_diag_precond, kK_precond_dots, kK_newton_update, kK_device_control, kNumKernels
 };
 const char *const kKernelNames[kNumKernels] = {
     "z_r2c", "z_c2r", "y_fft_1field", "y_fft_5fields", "x_fft", "x_conv_fwd", "x_conv_adj", "z_phi_grad",
     "z_phi_energy", "z_grad", "local_energy", "reduce_terms", "dots", "axpy", "scal_add",
     "weight_table", "z_hess", "z_jac", "z_hvp_out", "veff_density", "veff_grad",
-    "diag_precond", "precond_dots", "newton_update"};
+    "diag_precond", "precond_dots", "newton_update", "device_control"};
 
 // Calls f(std::integral_constant<int, RN>()) with RN = the plan's length
 // when it is an FP32 plan marked for the register-resident transform, else
@@ -2869,9 +2869,10 @@ int Engine::energy(const FmtSpec &f, const double *n, const double *V, const dou
 
 int Engine::energy_grad_dots(const FmtSpec &f, const double *n, const double *V,
                              const double *mask, double *grad, double *E_host, int k,
-                             const double *const *a, const double *const *b, double *dots_host) {
-  if (k < 1 || k > 3) return impl_->eval_any(f, n, V, mask, grad, E_host, nullptr);
-  return impl_->eval_any(f, n, V, mask, grad, E_host, nullptr, k, a, b, dots_host);
+                             const double *const *a, const double *const *b, double *dots_host,
+                             double *terms_host) {
+  if (k < 1 || k > 3) return impl_->eval_any(f, n, V, mask, grad, E_host, terms_host);
+  return impl_->eval_any(f, n, V, mask, grad, E_host, terms_host, k, a, b, dots_host);
 }
 
 int Engine::energy_grad(const FmtSpec &f, const double *n, const double *V, const double *mask,
@@ -2989,6 +2990,17 @@ int Engine::dev_hvp(const FmtSpec &f, const double *dx, const double *mask, doub
 }
 
 double *Engine::dev_results() const { return impl_->results; }
+int Engine::launch_slots() const { return kNumSlots; }
+int Engine::control_slot() const { return kK_device_control; }
+void Engine::launch_counts(long long *out) const {
+  memcpy(out, impl_->launches, sizeof(long long) * kNumSlots);
+}
+void Engine::launch_set(const long long *in) {
+  memcpy(impl_->launches, in, sizeof(long long) * kNumSlots);
+}
+void Engine::launch_add(const long long *delta, long long times) {
+  for (int i = 0; i < kNumSlots; i++) impl_->launches[i] += delta[i] * times;
+}
 int Engine::vector_blocks() const { return impl_->dot_blocks; }
 
 int Engine::newton_update(const FmtSpec &f, const double *n, double alpha, const double *p,

@@ -117,7 +117,8 @@ class Engine {
   // and a single synchronisation.
   int energy_grad_dots(const FmtSpec &f, const double *n, const double *V, const double *mask,
                        double *grad, double *E_host, int k, const double *const *a,
-                       const double *const *b, double *dots_host);
+                       const double *const *b, double *dots_host,
+                       double *terms_host = nullptr);
 
   // Newton refinement of the mixed form: hess_setup stores, at the point n,
   // the packed second derivatives of phi (FP32, from FP32 weighted
@@ -187,6 +188,15 @@ class Engine {
   // Blocks of the FP64 vector kernels (a multiple of the SM count, at most
   // one block per 256 points).
   int vector_blocks() const;
+  // Launch accounting of graphs built elsewhere: per-kind counters
+  // (launch_slots() of them; control_slot() counts the device-driven
+  // solver's own kernels), read, reset after a capture, and advanced by a
+  // sequence's counts times its executions.
+  int launch_slots() const;
+  int control_slot() const;
+  void launch_counts(long long *out) const;
+  void launch_set(const long long *in);
+  void launch_add(const long long *delta, long long times);
 
  private:
   explicit Engine(EngineImpl *impl);

@@ -113,7 +113,7 @@ def test_device_driven_solve_refuses_unsupported_settings():
     s = _problems()[0]
     ctx, g, f = _setup(s, _lib.PRECISION_MIXED)
     try:
-        for kw in (dict(linesearch=_lib.LS_QUADRATIC_REF, preconditioned=_lib.PC_DENSITY),
+        for kw in (dict(linesearch=_lib.LS_QUADRATIC_REF, preconditioned=_lib.PC_NONE),
                    dict(linesearch=_lib.LS_SECANT, preconditioned=_lib.PC_NONE),
                    dict(linesearch=_lib.LS_SECANT, preconditioned=_lib.PC_DENSITY,
                         precision=1e-6)):
