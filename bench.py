@@ -355,6 +355,9 @@ def run_ours(args, rank, world):
     n_ws = torch.empty_like(masks[0])
     MIXED, FP64 = _lib.PRECISION_MIXED, _lib.PRECISION_FP64
     PC = _lib.PC_NONE if args.no_precond else _lib.PC_DENSITY
+    # mixed solves driven from the device (one graph launch each) unless
+    # --host-driven; the device-driven minimiser needs the preconditioner
+    DEVICE = PC == _lib.PC_DENSITY and not args.host_driven
     # FP32 stage exit |grad| < SWITCH x the bulk start's |grad|: with the
     # preconditioner, 1e-5 was the fastest of 1e-5, 3e-5, 3e-4 and the
     # relative rule on 30 held-out problems (python -m deft_gb300.warmstart
@@ -394,7 +397,7 @@ def run_ours(args, rank, world):
         bulk_gn[i] = gb
         t1 = time.perf_counter()
         st, _ = sv.solve(MIXED, n_ws.data_ptr(), refine_abs=SWITCH * gb, preconditioned=PC,
-                         gtol=MIXED_GTOL)
+                         gtol=MIXED_GTOL, device=DEVICE)
         if i in outs:
             _lib.check(L.deft_cg_get_x(sv.cg[MIXED], outs[i].data_ptr(), 1))
         phases["network_s"].append(t1 - t0)
@@ -411,7 +414,7 @@ def run_ours(args, rank, world):
     def mixed_bulk_step(i):
         sv.set_problem(probs[i], masks[i].data_ptr())
         st, _ = sv.solve(MIXED, bulks[i].data_ptr(), refine_abs=SWITCH * bulk_gn[i],
-                         preconditioned=PC, gtol=MIXED_GTOL)
+                         preconditioned=PC, gtol=MIXED_GTOL, device=DEVICE)
         if i in outs:
             _lib.check(L.deft_cg_get_x(sv.cg[MIXED], outs[i].data_ptr(), 1))
         return st, True
@@ -536,7 +539,7 @@ def run_ours(args, rank, world):
         used, _, gb = net.initial_density(sv.fmt[MIXED], mask_dev.data_ptr(), s.eta, s.nb,
                                           n_ws.data_ptr(), bulk_gnorm=True)
         st, _ = sv.solve(MIXED, n_ws.data_ptr(), refine_abs=SWITCH * gb, preconditioned=PC,
-                         gtol=MIXED_GTOL)
+                         gtol=MIXED_GTOL, device=DEVICE)
         _lib.check(L.deft_cg_get_x(sv.cg[MIXED], out_host[i].data_ptr(), 0))
     e2e_s = (time.perf_counter() - t0) / len(timed_idx)
     err_e2e = [profile_errors(i, out_host[i].to(dd)) for i in timed_idx]
@@ -567,7 +570,10 @@ def run_ours(args, rank, world):
             "form": "checked learned warm start, FP32 CG stage" +
                     ("" if args.no_precond else " (density-variable diagonal preconditioner "
                      "n/(kT dV))") + ", Newton refinement on the FP64 gradient (FP32 stage "
-                    f"left at {SWITCH:g} of the bulk start's gradient norm)",
+                    f"left at {SWITCH:g} of the bulk start's gradient norm); "
+                    + ("device-driven: each solve is one CUDA graph launch (conditional "
+                       "WHILE/SWITCH/IF nodes, every decision in a kernel)" if DEVICE
+                       else "host-driven (one graph replay and sync per evaluation)"),
             "gtol_mixed": MIXED_GTOL,
             "profile_condition": f"max |n - n_FP64| <= {PROFILE_TOL:g} (absolute and relative "
                                  f"to max n) against the FP64 solution of the same problem "
@@ -1081,6 +1087,9 @@ def main():
     ap.add_argument("--case-problem", default="slit", choices=["slit", "solutes"])
     ap.add_argument("--saft-case", action="store_true",
                     help="only time the water SAFT workload (FP64) and exit")
+    ap.add_argument("--host-driven", action="store_true",
+                    help="run the mixed solves host-driven (deft_cg_solve) instead of "
+                         "device-driven (deft_cg_solve_device)")
     ap.add_argument("--solute-case", action="store_true",
                     help="only run the 256^3 hard-sphere solute workload (FP64 vs mixed) and exit")
     ap.add_argument("--fno-case", action="store_true",

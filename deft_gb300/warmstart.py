@@ -268,12 +268,13 @@ class Solver:
             check(self.L.deft_fmt_set_mask(f, mask_ptr, 1))
 
     def solve(self, precision, n0_ptr, refine_abs=0.0, preconditioned=_lib.PC_NONE, gtol=None,
-              maxiter=20000):
+              maxiter=20000, device=False):
         """Solve from the device array n0_ptr; returns (CgStatus, seconds).
         refine_abs > 0 sets the mixed form's FP32-stage exit |grad| < refine_abs;
         preconditioned = PC_DENSITY runs the CG with the density-variable
         diagonal preconditioner; gtol overrides the solver's tolerance for
-        this solve.
+        this solve; device = True runs it device-driven (deft_cg_solve_device,
+        one graph launch; needs preconditioned = PC_DENSITY).
         A minimiser that stops without converging (line search, iteration
         limit, non-finite values) is reported in CgStatus.status, not raised."""
         t0 = time.perf_counter()
@@ -282,8 +283,10 @@ class Solver:
         check(self.L.deft_cg_set_params(self.cg[precision], ctypes.byref(cp)))
         check(self.L.deft_cg_set_x(self.cg[precision], n0_ptr, 1))
         st = _lib.CgStatus()
-        code = self.L.deft_cg_solve(self.cg[precision], ctypes.byref(st))
-        if code not in (_lib.OK, _lib.ERR_LINESEARCH, _lib.ERR_MAXITER, _lib.ERR_NAN):
+        solve = self.L.deft_cg_solve_device if device else self.L.deft_cg_solve
+        code = solve(self.cg[precision], ctypes.byref(st))
+        if code not in (_lib.OK, _lib.ERR_LINESEARCH, _lib.ERR_MAXITER, _lib.ERR_NAN,
+                        _lib.ERR_TIMEOUT):
             check(code)
         st.status = code
         return st, time.perf_counter() - t0
