@@ -355,9 +355,10 @@ def run_ours(args, rank, world):
     n_ws = torch.empty_like(masks[0])
     MIXED, FP64 = _lib.PRECISION_MIXED, _lib.PRECISION_FP64
     PC = _lib.PC_NONE if args.no_precond else _lib.PC_DENSITY
-    # mixed solves driven from the device (one graph launch each) unless
-    # --host-driven; the device-driven minimiser needs the preconditioner
-    DEVICE = PC == _lib.PC_DENSITY and not args.host_driven
+    # mixed solves driven from the host (one graph replay and sync per
+    # evaluation; measured 0.3 ms per solve faster at 128^3 than the
+    # device-driven graph) unless --device-driven (needs the preconditioner)
+    DEVICE = PC == _lib.PC_DENSITY and args.device_driven
     # FP32 stage exit |grad| < SWITCH x the bulk start's |grad|: with the
     # preconditioner, 1e-5 was the fastest of 1e-5, 3e-5, 3e-4 and the
     # relative rule on 30 held-out problems (python -m deft_gb300.warmstart
@@ -388,7 +389,7 @@ def run_ours(args, rank, world):
     phases = {"network_s": [], "cg_s": []}
     bulk_gn = {}
 
-    def warm_step(i):
+    def warm_step(i, device=None):
         s = probs[i]
         sv.set_problem(s, masks[i].data_ptr())
         t0 = time.perf_counter()
@@ -397,7 +398,8 @@ def run_ours(args, rank, world):
         bulk_gn[i] = gb
         t1 = time.perf_counter()
         st, _ = sv.solve(MIXED, n_ws.data_ptr(), refine_abs=SWITCH * gb, preconditioned=PC,
-                         gtol=MIXED_GTOL, device=DEVICE)
+                         gtol=MIXED_GTOL,
+                         device=DEVICE if device is None else device)
         if i in outs:
             _lib.check(L.deft_cg_get_x(sv.cg[MIXED], outs[i].data_ptr(), 1))
         phases["network_s"].append(t1 - t0)
@@ -502,10 +504,10 @@ def run_ours(args, rank, world):
     # `ncu --nvtx --nvtx-include "warm_mixed_step/" --metrics gpu__time_duration.sum`)
     _lib.check(L.deft_grid_profile(sv.grid, 1))
     torch.cuda.nvtx.range_push("warm_mixed_step")
-    warm_step(timed_idx[0])
+    warm_step(timed_idx[0], device=False)
     torch.cuda.nvtx.range_pop()
     for i in timed_idx[1:]:
-        warm_step(i)
+        warm_step(i, device=False)
     prof_w = kernel_profile(L, sv.grid)
     _lib.check(L.deft_grid_profile(sv.grid, 1))
     fp64_step(timed_idx[0])
@@ -648,24 +650,39 @@ def network_forward_ms(L, net, mask, s, n_out, stream, reps=5):
 
 def batched_sweep(count=64, seed=3):
     """The batched sweep (64 slits, eta in [0.05, 0.45], grids from
-    {32,48,64,96,128}^3, dx = 0.2, slit widths 3-10): mixed form, solved by
-    deft_batch_solve with 8 concurrent streams, against the same problems one
-    after another on one stream."""
+    {32,48,64,96,128}^3, dx = 0.2, slit widths 3-10): mixed form with the
+    density preconditioner, solved (1) as one graph launch of 64
+    device-driven solves (deft_batch_solve_device; the time includes each
+    problem's grid set-up and the graph's capture), (2) by deft_batch_solve
+    on 8 host threads and streams, (3) one after another on one stream.  The
+    device batch's profiles are checked against the 8-stream ones."""
+    import numpy as np
     from deft_gb300.warmstart import solve_batch
     from deft_gb300.workloads import batch_sweep
     probs = batch_sweep(count=count, seed=seed)
-    solve_batch(probs[:8], workers=8)  # warm-up: plans, tables, graphs
+    PCD = _lib.PC_DENSITY
+    solve_batch(probs[:8], workers=8, preconditioned=PCD)  # warm-up: module, plans
+    solve_batch(probs[:8], preconditioned=PCD, device_driven=True)
     t0 = time.perf_counter()
-    code, st, _ = solve_batch(probs, workers=8)
+    code_d, st_d, x_d = solve_batch(probs, preconditioned=PCD, device_driven=True)
+    t_dev = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    code, st, x_h = solve_batch(probs, workers=8, preconditioned=PCD)
     t_conc = time.perf_counter() - t0
     t0 = time.perf_counter()
-    code1, _, _ = solve_batch(probs, workers=1)
+    code1, _, _ = solve_batch(probs, workers=1, preconditioned=PCD)
     t_seq = time.perf_counter() - t0
     conv = sum(1 for x in st if x.converged and x.gnorm < GTOL)
-    return {"problems": count, "converged": conv, "status": code or code1,
-            "seconds_8_streams": t_conc, "seconds_1_stream": t_seq,
-            "solves_per_s": count / t_conc, "grid_points": int(sum(p.size for p in probs)),
-            "form": "mixed (FP32 CG stage + FP64-residual Newton refinement), |grad F|<1e-9"}
+    conv_d = sum(1 for x in st_d if x.converged and x.gnorm < GTOL)
+    dn = max(float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)) for a, b in zip(x_d, x_h))
+    return {"problems": count, "converged_device": conv_d, "converged_8_streams": conv,
+            "status": code_d or code or code1,
+            "seconds_one_launch": t_dev, "seconds_8_streams": t_conc, "seconds_1_stream": t_seq,
+            "solves_per_s": count / t_dev, "solves_per_s_8_streams": count / t_conc,
+            "max_profile_rel_diff_device_vs_streams": dn,
+            "grid_points": int(sum(p.size for p in probs)),
+            "form": "mixed (FP32 CG stage + FP64-residual Newton refinement), density "
+                    "preconditioner, |grad F|<1e-9"}
 
 
 def cpu_eval_seconds(s, budget_s, max_evals=8):
@@ -1087,9 +1104,9 @@ def main():
     ap.add_argument("--case-problem", default="slit", choices=["slit", "solutes"])
     ap.add_argument("--saft-case", action="store_true",
                     help="only time the water SAFT workload (FP64) and exit")
-    ap.add_argument("--host-driven", action="store_true",
-                    help="run the mixed solves host-driven (deft_cg_solve) instead of "
-                         "device-driven (deft_cg_solve_device)")
+    ap.add_argument("--device-driven", action="store_true",
+                    help="run the timed mixed solves device-driven (deft_cg_solve_device, one "
+                         "graph launch each) instead of host-driven (deft_cg_solve)")
     ap.add_argument("--solute-case", action="store_true",
                     help="only run the 256^3 hard-sphere solute workload (FP64 vs mixed) and exit")
     ap.add_argument("--fno-case", action="store_true",

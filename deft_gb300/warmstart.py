@@ -139,9 +139,11 @@ class FourierOperator:
 
 
 def solve_batch(problems, precision=_lib.PRECISION_MIXED, workers=8, gtol=1e-9, maxiter=20000,
-                device=0):
+                device=0, preconditioned=_lib.PC_NONE, device_driven=False):
     """Converged solves of problems with .lat/.shape/.R/.kT/.mu/.mask/.n0
-    through deft_batch_solve; returns (status, [CgStatus], [profiles])."""
+    through deft_batch_solve (`workers` host threads and streams) or, with
+    device_driven, deft_batch_solve_device (one graph launch for all; needs
+    preconditioned = PC_DENSITY); returns (status, [CgStatus], [profiles])."""
     keep, outs = [], []
     arr = (_lib.BatchProblem * len(problems))()
     for k, s in enumerate(problems):
@@ -162,9 +164,14 @@ def solve_batch(problems, precision=_lib.PRECISION_MIXED, workers=8, gtol=1e-9, 
         p.V = None
         p.n_init = n0.ctypes.data
         p.n_out = out.ctypes.data
-    bp = _lib.BatchParams(workers, _lib.CgParams(_lib.LS_SECANT, gtol, maxiter, 1.0, 0.0, 0.0))
+    cp = _lib.CgParams(_lib.LS_SECANT, gtol, maxiter, 1.0, 0.0, 0.0, int(preconditioned))
     st = (_lib.CgStatus * len(problems))()
-    code = _lib.load().deft_batch_solve(device, len(problems), arr, ctypes.byref(bp), st)
+    if device_driven:
+        code = _lib.load().deft_batch_solve_device(device, len(problems), arr, ctypes.byref(cp),
+                                                   st)
+    else:
+        bp = _lib.BatchParams(workers, cp)
+        code = _lib.load().deft_batch_solve(device, len(problems), arr, ctypes.byref(bp), st)
     return code, list(st), outs
 
 
