@@ -657,6 +657,7 @@ def batched_sweep(count=64, seed=3):
     on 8 host threads and streams, (3) one after another on one stream.  The
     device batch's profiles are checked against the 8-stream ones."""
     import numpy as np
+    from deft_gb300 import _lib
     from deft_gb300.warmstart import solve_batch
     from deft_gb300.workloads import batch_sweep
     probs = batch_sweep(count=count, seed=seed)
