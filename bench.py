@@ -667,6 +667,8 @@ def batched_sweep(count=64, seed=3):
     t0 = time.perf_counter()
     code_d, st_d, x_d = solve_batch(probs, preconditioned=PCD, device_driven=True)
     t_dev = time.perf_counter() - t0
+    phases = np.zeros(3)
+    _lib.check(_lib.load().deft_batch_device_times(phases.ctypes.data))
     t0 = time.perf_counter()
     code, st, x_h = solve_batch(probs, workers=8, preconditioned=PCD)
     t_conc = time.perf_counter() - t0
@@ -678,7 +680,10 @@ def batched_sweep(count=64, seed=3):
     dn = max(float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)) for a, b in zip(x_d, x_h))
     return {"problems": count, "converged_device": conv_d, "converged_8_streams": conv,
             "status": code_d or code or code1,
-            "seconds_one_launch": t_dev, "seconds_8_streams": t_conc, "seconds_1_stream": t_seq,
+            "seconds_one_launch": t_dev,
+            "one_launch_phases_s": {"set_up": float(phases[0]), "graph_build": float(phases[1]),
+                                    "solve": float(phases[2])},
+            "seconds_8_streams": t_conc, "seconds_1_stream": t_seq,
             "solves_per_s": count / t_dev, "solves_per_s_8_streams": count / t_conc,
             "max_profile_rel_diff_device_vs_streams": dn,
             "grid_points": int(sum(p.size for p in probs)),

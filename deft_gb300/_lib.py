@@ -35,7 +35,7 @@ EXPORTS = (
     "deft_fmt_energy_grad_noalloc", "deft_noalloc_scratch_bytes",
     "deft_cg_create", "deft_cg_destroy", "deft_cg_set_params", "deft_cg_set_x", "deft_cg_get_x", "deft_cg_x_device",
     "deft_cg_step", "deft_cg_solve", "deft_cg_solve_device", "deft_cg_checkpoint", "deft_cg_restore", "deft_cg_set_log", "deft_batch_solve",
-    "deft_batch_solve_device",
+    "deft_batch_solve_device", "deft_batch_device_times",
     "deft_fno_create", "deft_fno_destroy", "deft_fno_param_count", "deft_fno_get_params",
     "deft_fno_set_params", "deft_fno_eval", "deft_fno_adam", "deft_fno_train_step",
     "deft_fno_warm_start", "deft_fno_initial_density", "deft_fno_launches",
@@ -167,6 +167,7 @@ def load():
                                                     _dp, _dp]),
         "deft_batch_solve": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.POINTER(BatchProblem),
                                             ctypes.POINTER(BatchParams), ctypes.POINTER(CgStatus)]),
+        "deft_batch_device_times": (ctypes.c_int, [_dp]),
         "deft_batch_solve_device": (ctypes.c_int, [ctypes.c_int, ctypes.c_int,
                                                    ctypes.POINTER(BatchProblem),
                                                    ctypes.POINTER(CgParams),

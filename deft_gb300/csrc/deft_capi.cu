@@ -11,6 +11,7 @@
 #include "tensor.h"
 
 #include <cfloat>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -1827,11 +1828,21 @@ int deft_cg_solve_device(deft_cg *c, deft_cg_status *st) {
   return device_outcome(c, o, st);
 }
 
+static thread_local double g_batch_times[3] = {0, 0, 0};
+
+int deft_batch_device_times(double seconds[3]) {
+  if (!seconds) return set_err(DEFT_ERR_ARG, "NULL argument");
+  memcpy(seconds, g_batch_times, sizeof(g_batch_times));
+  return DEFT_OK;
+}
+
 int deft_batch_solve_device(int device, int count, const deft_batch_problem *probs,
                             const deft_cg_params *cgp, deft_cg_status *status_out) {
   if (count < 0 || (count && (!probs || !cgp || !status_out)))
     return set_err(DEFT_ERR_ARG, "NULL argument");
   if (count == 0) return DEFT_OK;
+  using clk = std::chrono::steady_clock;
+  const auto t0 = clk::now();
   deft_ctx *ctx = nullptr;
   if (int s = deft_ctx_create(device, &ctx)) return s;
   std::vector<deft_grid *> grids(count, nullptr);
@@ -1861,12 +1872,18 @@ int deft_batch_solve_device(int device, int count, const deft_batch_problem *pro
     if (s) g_err = "problem " + std::to_string(i) + ": " + g_err;
   }
   std::string err;
+  const auto t1 = clk::now();
   if (!s) {
     gr = deft::dcg_build(pr.data(), count, &err);
     if (!gr) s = set_err(DEFT_ERR_CUDA, err);
   }
+  const auto t2 = clk::now();
   std::vector<deft::DcgOutcome> out(count);
   if (!s && (s = deft::dcg_run(gr, ctx->stream, out.data(), &err))) set_err(s, err);
+  const auto t3 = clk::now();
+  g_batch_times[0] = std::chrono::duration<double>(t1 - t0).count();
+  g_batch_times[1] = std::chrono::duration<double>(t2 - t1).count();
+  g_batch_times[2] = std::chrono::duration<double>(t3 - t2).count();
   int first = DEFT_OK;
   for (int i = 0; i < count && !s; i++) {
     const int r = device_outcome(cgs[i], out[i], &status_out[i]);

@@ -371,6 +371,10 @@ int deft_batch_solve(int device, int count, const deft_batch_problem *problems,
  * n_out gets each converged profile; status_out[i] each outcome. */
 int deft_batch_solve_device(int device, int count, const deft_batch_problem *problems,
                             const deft_cg_params *cg, deft_cg_status *status_out);
+/* Wall seconds of the calling thread's last deft_batch_solve_device: set-up
+ * (grids, tables, minimisers), graph construction, and the solve (upload of
+ * the states, the one launch, the wait). */
+int deft_batch_device_times(double seconds[3]);
 
 /* ---- learned warm start ----
  * A 3-D Fourier neural operator (no reference counterpart) that maps a
