@@ -63,7 +63,26 @@ __device__ __forceinline__ dfl operator*(dfl a, dfl b) {
 }
 __device__ __forceinline__ dfl &operator+=(dfl &a, dfl b) { return a = a + b; }
 __device__ __forceinline__ dfl &operator-=(dfl &a, dfl b) { return a = a - b; }
+__device__ __forceinline__ dfl &operator*=(dfl &a, dfl b) { return a = a * b; }
 __device__ __forceinline__ bool operator==(dfl a, dfl b) { return a.hi == b.hi && a.lo == b.lo; }
+__device__ __forceinline__ bool operator<(dfl a, dfl b) {
+  return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo);
+}
+__device__ __forceinline__ dfl fabs(dfl a) { return a.hi < 0.f ? -a : a; }
+// Quotient by one correction step (the long division of Dekker 1971):
+// q1 = a.hi / b.hi in FP32, the remainder r = a - q1 b in double-float,
+// q = q1 + r.hi / b.hi; relative error about 2^-44.
+__device__ __forceinline__ dfl operator/(dfl a, dfl b) {
+  const float rb = 1.0f / b.hi;
+  const float q1 = a.hi * rb;
+  const dfl r = a - dfl(q1, 0.f) * b;
+  const float q2 = r.hi * rb;
+  const dfl q = df_fast_two_sum(q1, q2);
+  // a second correction for the last bits
+  const dfl r2 = a - q * b;
+  return q + dfl(r2.hi * rb, 0.f);
+}
+__device__ __forceinline__ double to_double(dfl a) { return (double)a.hi + (double)a.lo; }
 
 // Complex double-float: 16 bytes, the size of a double2, so the FP64 form's
 // tiles and spectra keep their shapes.

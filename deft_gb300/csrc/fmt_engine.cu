@@ -833,11 +833,13 @@ __global__ void __launch_bounds__(kThreads,
   const int Nz = g.Nz, P5 = 5 * P;
   const int p0 = blockIdx.x * P;
   C *res = z_load5_c2r<T, RN>(S5, A, Bf, g, pz, fP, f5P, p0);
+  // Phi and its partials in T (double-float in the FP64 form: FP64 only for
+  // its log), the energy sums and the local terms in U
   using U = Acc<T>;
   U tacc[kNumTerms] = {0, 0, 0, 0, 0, 0};
   const bool hs = la.terms & kTermHS;
   const U inv_nQ = U(la.inv_nQ);
-  const U c = U(la.dV * la.kT);
+  const T c = T(la.dV * la.kT);
   #pragma unroll 4
   for (int idx = threadIdx.x; idx < 2 * P * Nz; idx += blockDim.x) {
     int ll, z;
@@ -845,16 +847,16 @@ __global__ void __launch_bounds__(kThreads,
     const int line = 2 * p0 + ll;
     T *cell = reinterpret_cast<T *>(res + z * P5 + (ll >> 1)) + (ll & 1);  // field 0
     const int fstride = 2 * P;  // T elements between fields
-    U d[5] = {0, 0, 0, 0, 0};
+    T d[5] = {0, 0, 0, 0, 0};
     if (line < g.lines) {
       const size_t r = (size_t)line * Nz + z;
       if (hs) {
-        U phi[3];
-        wb_phi<U>(la.wr, U(cell[0]), U(cell[fstride]), U(cell[2 * fstride]),
-                  U(cell[3 * fstride]), U(cell[4 * fstride]), phi, d);
-        tacc[0] += phi[0];
-        tacc[1] += phi[1];
-        tacc[2] += phi[2];
+        T phi[3];
+        wb_phi<T>(la.wr, cell[0], cell[fstride], cell[2 * fstride], cell[3 * fstride],
+                  cell[4 * fstride], phi, d);
+        tacc[0] += U(phi[0]);
+        tacc[1] += U(phi[1]);
+        tacc[2] += U(phi[2]);
       }
       const U nv = U(n[r]);
       if (la.terms & kTermIdeal) tacc[3] += ideal_energy_t<U>(nv, inv_nQ);
@@ -863,7 +865,7 @@ __global__ void __launch_bounds__(kThreads,
     }
     if (GRAD) {
 #pragma unroll
-      for (int a = 0; a < 5; a++) cell[a * fstride] = T(c * d[a]);
+      for (int a = 0; a < 5; a++) cell[a * fstride] = c * d[a];
     }
   }
   block_reduce_terms<U>(tacc, la, red, partials);

@@ -26,6 +26,8 @@
 
 #include <cuda_runtime.h>
 
+#include "dfloat.cuh"
+
 namespace deft {
 
 template <typename T> struct WbConst;
@@ -33,6 +35,13 @@ template <> struct WbConst<double> {
   static constexpr double series_below = 1e-2;  // S
   static constexpr int series_terms = 14;
   static constexpr double m2_below = 0.1;       // P2, P3
+  static constexpr int m2_terms = 20;
+};
+// The FP64 form's double-float Phi: about 46 bits, the FP64 thresholds.
+template <> struct WbConst<dfl> {
+  static constexpr double series_below = 1e-2;
+  static constexpr int series_terms = 14;
+  static constexpr double m2_below = 0.1;
   static constexpr int m2_terms = 20;
 };
 template <> struct WbConst<float> {
@@ -53,6 +62,8 @@ constexpr int kHsTarazona = 4;
 template <typename T> __device__ __forceinline__ T wb_log(T x);
 template <> __device__ __forceinline__ double wb_log<double>(double x) { return log(x); }
 template <> __device__ __forceinline__ float wb_log<float>(float x) { return logf(x); }
+// double-float log through the FP64 log (one FP64 log per point)
+template <> __device__ __forceinline__ dfl wb_log<dfl>(dfl x) { return dfl(log(to_double(x))); }
 
 // S, S', S'' at e; l = ln(1 - e) (computed once by the caller).
 template <typename T>
