@@ -814,9 +814,22 @@ __device__ void z_r2c_store5(typename Cplx<T>::type *res, typename Cplx<T>::type
 #ifndef DEFT_Z_PHI_MIN_BLOCKS
 #define DEFT_Z_PHI_MIN_BLOCKS 5
 #endif
+// The FP64 form's Phi: FP64 (0) or double-float arithmetic (1).  Double-float
+// Phi needs 255 registers a thread (one block per SM) and measured 987 us
+// against 741 us at 128^3; capped at 128 registers it spills 1.7 KB.
+#ifndef DEFT_DF_PHI
+#define DEFT_DF_PHI 0
+#endif
+#ifndef DEFT_Z_PHI_DF_MIN_BLOCKS
+#define DEFT_Z_PHI_DF_MIN_BLOCKS 0
+#endif
+template <typename T> using PhiT = std::conditional_t<is_df<T> && !DEFT_DF_PHI, double, T>;
 template <typename T, bool GRAD, int RN = 0>
 __global__ void __launch_bounds__(kThreads,
-                                  RN > 0 ? 2 : (sizeof(T) == 4 ? DEFT_Z_PHI_MIN_BLOCKS : 0))
+                                  RN > 0 ? 2
+                                         : (sizeof(T) == 4 ? DEFT_Z_PHI_MIN_BLOCKS
+                                                           : (is_df<T> ? DEFT_Z_PHI_DF_MIN_BLOCKS
+                                                                       : 0)))
     k_z_phi(typename Cplx<T>::type *S5,
                                                     const double *__restrict__ n,
                                                     const double *__restrict__ V, Geom g,
@@ -836,10 +849,11 @@ __global__ void __launch_bounds__(kThreads,
   // Phi and its partials in T (double-float in the FP64 form: FP64 only for
   // its log), the energy sums and the local terms in U
   using U = Acc<T>;
+  using Q = PhiT<T>;
   U tacc[kNumTerms] = {0, 0, 0, 0, 0, 0};
   const bool hs = la.terms & kTermHS;
   const U inv_nQ = U(la.inv_nQ);
-  const T c = T(la.dV * la.kT);
+  const Q c = Q(la.dV * la.kT);
   #pragma unroll 4
   for (int idx = threadIdx.x; idx < 2 * P * Nz; idx += blockDim.x) {
     int ll, z;
@@ -847,13 +861,13 @@ __global__ void __launch_bounds__(kThreads,
     const int line = 2 * p0 + ll;
     T *cell = reinterpret_cast<T *>(res + z * P5 + (ll >> 1)) + (ll & 1);  // field 0
     const int fstride = 2 * P;  // T elements between fields
-    T d[5] = {0, 0, 0, 0, 0};
+    Q d[5] = {0, 0, 0, 0, 0};
     if (line < g.lines) {
       const size_t r = (size_t)line * Nz + z;
       if (hs) {
-        T phi[3];
-        wb_phi<T>(la.wr, cell[0], cell[fstride], cell[2 * fstride], cell[3 * fstride],
-                  cell[4 * fstride], phi, d);
+        Q phi[3];
+        wb_phi<Q>(la.wr, Q(cell[0]), Q(cell[fstride]), Q(cell[2 * fstride]),
+                  Q(cell[3 * fstride]), Q(cell[4 * fstride]), phi, d);
         tacc[0] += U(phi[0]);
         tacc[1] += U(phi[1]);
         tacc[2] += U(phi[2]);
@@ -865,7 +879,7 @@ __global__ void __launch_bounds__(kThreads,
     }
     if (GRAD) {
 #pragma unroll
-      for (int a = 0; a < 5; a++) cell[a * fstride] = c * d[a];
+      for (int a = 0; a < 5; a++) cell[a * fstride] = T(c * d[a]);
     }
   }
   block_reduce_terms<U>(tacc, la, red, partials);
