@@ -992,9 +992,12 @@ def saft_case(N=128, dx=0.2, evals=10, gtol=1e-11):
     src/water-constants.cpp:22-40; atomic units): N^3 grid of spacing dx bohr,
     liquid density 4.9388942e-3 bohr^-3 around a hard-sphere solute whose
     centre-exclusion radius is 3 Angstrom = 5.669 bohr (the density inside it
-    floored at 1e-5 of the liquid's), mu of the homogeneous liquid.  Times
-    FP64 energy+gradient evaluations with CUDA events and one converged solve
-    (density-preconditioned CG to |grad F| < gtol)."""
+    floored at 1e-5 of the liquid's), mu of the homogeneous liquid.  In the
+    FP64 form and in the mixed form (every transform in FP32, refinement by
+    FP64 CG): energy+gradient evaluations timed with CUDA events, the mixed
+    evaluation's errors against FP64, and one converged solve each
+    (density-preconditioned CG to |grad F| < gtol) with the two profiles
+    compared."""
     import torch
     from deft_gb300 import _lib
     L = _lib.load()
@@ -1003,9 +1006,10 @@ def saft_case(N=128, dx=0.2, evals=10, gtol=1e-11):
     sp = np.array([1400.0 * kB, 0.0381876 * (3.03420 * ang) ** 3, 250.0 * kB, 1.78890, 0.353])
     terms = _lib.TERM_HS | _lib.TERM_IDEAL | _lib.TERM_MU | _lib.TERM_SAFT
 
-    def fmt(grid, mu, mask=None):
+    def fmt(grid, mu, mask=None, precision=0):
         h = ctypes.c_void_p()
-        p = _lib.FmtParams(R, kT, mu, terms | (_lib.TERM_MASK if mask is not None else 0), 0, 0)
+        p = _lib.FmtParams(R, kT, mu, terms | (_lib.TERM_MASK if mask is not None else 0),
+                           precision, 0)
         _lib.check(L.deft_fmt_create(grid, ctypes.byref(p), ctypes.byref(h)))
         _lib.check(L.deft_fmt_set_saft(h, sp.ctypes.data))
         if mask is not None:
@@ -1041,43 +1045,58 @@ def saft_case(N=128, dx=0.2, evals=10, gtol=1e-11):
     mask_h = (r > 3 * ang).astype(np.float64).reshape(-1)
     mask = torch.tensor(mask_h, device="cuda:0")
     n0 = torch.tensor(np.where(mask_h > 0, nl, 1e-5 * nl), device="cuda:0")
-    f = fmt(grid, mu, mask)
-    gbuf = torch.empty_like(n0)
-    for _ in range(3):
-        _lib.check(L.deft_fmt_energy_grad(f, n0.data_ptr(), 1, ctypes.addressof(E), gbuf.data_ptr(),
-                                          None))
     stream = torch.cuda.ExternalStream(L.deft_ctx_stream(ctx))
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(evals):
-        _lib.check(L.deft_fmt_energy_grad(f, n0.data_ptr(), 1, ctypes.addressof(E), gbuf.data_ptr(),
-                                          None))
-    e1.record(stream)
-    e1.synchronize()
-    ms_eval = e0.elapsed_time(e1) / evals
-    cp = _lib.CgParams(_lib.LS_SECANT, gtol, 20000, 1.0, 0.0, 0.0, _lib.PC_DENSITY, 0.0)
-    h = ctypes.c_void_p()
-    _lib.check(L.deft_cg_create(f, ctypes.byref(cp), ctypes.byref(h)))
-    cg = h
-    _lib.check(L.deft_cg_set_x(cg, n0.data_ptr(), 1))
-    st = _lib.CgStatus()
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    code = L.deft_cg_solve(cg, ctypes.byref(st))
-    torch.cuda.synchronize()
-    t_solve = time.perf_counter() - t0
-    L.deft_cg_destroy(cg)
-    L.deft_fmt_destroy(f)
+    out = {}
+    res = {}
+    for prec, name in ((0, "fp64"), (1, "mixed")):
+        f = fmt(grid, mu, mask, prec)
+        gbuf = torch.empty_like(n0)
+        for _ in range(3):
+            _lib.check(L.deft_fmt_energy_grad(f, n0.data_ptr(), 1, ctypes.addressof(E),
+                                              gbuf.data_ptr(), None))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(evals):
+            _lib.check(L.deft_fmt_energy_grad(f, n0.data_ptr(), 1, ctypes.addressof(E),
+                                              gbuf.data_ptr(), None))
+        e1.record(stream)
+        e1.synchronize()
+        ms_eval = e0.elapsed_time(e1) / evals
+        E0 = E.value
+        cp = _lib.CgParams(_lib.LS_SECANT, gtol, 20000, 1.0, 0.0, 0.0, _lib.PC_DENSITY, 0.0)
+        h = ctypes.c_void_p()
+        _lib.check(L.deft_cg_create(f, ctypes.byref(cp), ctypes.byref(h)))
+        cg = h
+        _lib.check(L.deft_cg_set_x(cg, n0.data_ptr(), 1))
+        st = _lib.CgStatus()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        code = L.deft_cg_solve(cg, ctypes.byref(st))
+        torch.cuda.synchronize()
+        t_solve = time.perf_counter() - t0
+        xs = torch.empty_like(n0)
+        _lib.check(L.deft_cg_get_x(cg, xs.data_ptr(), 1))
+        res[name] = (E0, gbuf.clone(), xs)
+        L.deft_cg_destroy(cg)
+        L.deft_fmt_destroy(f)
+        out[name] = {"ms_per_energy_grad": ms_eval,
+                     "solve": {"status": code, "converged": bool(st.converged),
+                               "seconds": t_solve, "iters": st.iter, "evals": st.evals,
+                               "evals_fp64": st.evals_fp64, "gnorm": st.gnorm, "gtol": gtol,
+                               "energy_hartree": st.energy}}
     L.deft_grid_destroy(grid)
     L.deft_ctx_destroy(ctx)
-    return {"saft_case": "water SAFT (WaterSaft, hughes_water_prop) FP64, hard-sphere solute "
-                          "of exclusion radius 3 Angstrom in liquid water",
-            "N": N, "dx_bohr": dx, "mu_hartree": mu, "ms_per_energy_grad": ms_eval,
-            "solve": {"status": code, "converged": bool(st.converged), "seconds": t_solve,
-                      "iters": st.iter, "evals": st.evals, "gnorm": st.gnorm, "gtol": gtol,
-                      "energy_hartree": st.energy, "form": "FP64 secant CG with the density "
-                                                          "preconditioner"}}
-
+    (Ed, gd, xd), (Em, gm, xm) = res["fp64"], res["mixed"]
+    out["mixed"]["evaluation_errors_vs_fp64"] = {
+        "dF_rel": abs(Em / Ed - 1),
+        "max_dg_rel_to_max_g": float((gm - gd).abs().max() / gd.abs().max())}
+    out["mixed"]["profile_vs_fp64_solve"] = float((xm - xd).abs().max() / xd.abs().max())
+    return {"saft_case": "water SAFT (WaterSaft, hughes_water_prop), hard-sphere solute "
+                         "of exclusion radius 3 Angstrom in liquid water; FP64 and mixed "
+                         "(transforms in FP32, refinement by FP64 CG)",
+            "N": N, "dx_bohr": dx, "mu_hartree": mu, **out,
+            "speedup_mixed_vs_fp64_solve": out["fp64"]["solve"]["seconds"]
+            / out["mixed"]["solve"]["seconds"]}
 
 def main():
     ap = argparse.ArgumentParser()

@@ -1430,6 +1430,20 @@ __global__ void __launch_bounds__(32 * kZWarps)
   }
 }
 
+// Complex field conversions between the FP32 work spectra and FP64 spectra.
+__global__ void k_c_f2d(const float2 *__restrict__ in, double2 *__restrict__ out, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float2 v = in[i];
+    out[i] = make_double2(v.x, v.y);
+  }
+}
+__global__ void k_c_d2f(const double2 *__restrict__ in, float2 *__restrict__ out, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double2 v = in[i];
+    out[i] = make_float2((float)v.x, (float)v.y);
+  }
+}
+
 // Energy partials of the local terms only (no hard spheres).
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_local_energy(const double *__restrict__ n,
@@ -2134,6 +2148,9 @@ class EngineImpl {
     set_smem(k_z_phi<double, true>, t64.smem_phi);
     set_smem(k_z_grad<double>, t64.smem_z);
     set_smem(k_z_r2c<dfl>, t64.smem_z);
+    set_smem(k_x_fft<float, -1>, t32.smem_x2);
+    set_smem(k_x_fft<float, +1>, t32.smem_x2);
+    set_smem(k_z_c2r<float>, t32.smem_z);
     set_smem(k_y_fft<dfl, -1>, t64.smem_y);
     set_smem(k_y_fft<dfl, +1>, t64.smem_y);
     set_smem(k_x_conv_fwd<dfl>, t64.smem_xf);
@@ -2421,7 +2438,8 @@ class EngineImpl {
 
   // Queues z r2c, y FFT, x convolution and inverse y of n (the weight table
   // for f.R must be current: ensure_table runs outside any graph capture).
-  template <typename T> int forward_weighted(const FmtSpec &f, const double *n) {
+  // Real field -> half spectra along z, into S0 (in T).
+  template <typename T> void z_r2c_spec0(const double *n) {
     const Tiles &t = tl<T>();
     pre(kslot<T>(kK_z_r2c));
     if (zwarp<T>()) {
@@ -2437,6 +2455,11 @@ class EngineImpl {
       });
     }
     post(kslot<T>(kK_z_r2c));
+  }
+
+  template <typename T> int forward_weighted(const FmtSpec &f, const double *n) {
+    const Tiles &t = tl<T>();
+    z_r2c_spec0<T>(n);
     y_fft<T>(spec0<T>(), 1, -1);
     pre(kslot<T>(kK_x_conv_fwd));
     if (pencil<T>(0)) {
@@ -2839,8 +2862,20 @@ cudaStream_t Engine::stream() const { return impl_->stream; }
 size_t Engine::scratch_bytes() const { return impl_->bytes; }
 const char *Engine::last_error() const { return impl_->err.c_str(); }
 
-int Engine::fft(const double *in, double2 *out) {
+int Engine::fft(const double *in, double2 *out, bool f32) {
   EngineImpl &e = *impl_;
+  if (f32) {
+    // FP32 transforms (mixed form): z, y, x in the work spectrum, then FP64 out
+    float2 *w = reinterpret_cast<float2 *>(e.S0);
+    e.z_r2c_spec0<float>(in);
+    e.y_fft<float>(w, 1, -1);
+    e.pre(kslot<float>(kK_x_fft));
+    k_x_fft<float, -1><<<e.x_tiles(e.t32.Bx), kThreads, e.t32.smem_x2, e.stream>>>(
+        w, e.g, e.pxf, e.t32.fBx, (float)e.g.dV);
+    e.post(kslot<float>(kK_x_fft));
+    k_c_f2d<<<e.dot_blocks, kThreads, 0, e.stream>>>(w, out, e.g.NC);
+    return e.check("fft");
+  }
   e.pre(kK_z_r2c);
     k_z_r2c<double><<<dim3(e.pairs_tiles(e.t64.Pz), 1), kThreads, e.t64.smem_z, e.stream>>>(
       in, out, e.g, e.pz, e.t64.fPz, 1.0);
@@ -2853,8 +2888,22 @@ int Engine::fft(const double *in, double2 *out) {
   return e.check("fft");
 }
 
-int Engine::ifft(const double2 *in, double *out) {
+int Engine::ifft(const double2 *in, double *out, bool f32) {
   EngineImpl &e = *impl_;
+  if (f32) {
+    float2 *w = reinterpret_cast<float2 *>(e.S0);
+    k_c_d2f<<<e.dot_blocks, kThreads, 0, e.stream>>>(in, w, e.g.NC);
+    e.pre(kslot<float>(kK_x_fft));
+    k_x_fft<float, +1><<<e.x_tiles(e.t32.Bx), kThreads, e.t32.smem_x2, e.stream>>>(
+        w, e.g, e.pxf, e.t32.fBx, 1.0f);
+    e.post(kslot<float>(kK_x_fft));
+    e.y_fft<float>(w, 1, +1);
+    e.pre(kslot<float>(kK_z_c2r));
+    k_z_c2r<float><<<dim3(e.pairs_tiles(e.t32.Pz), 1), kThreads, e.t32.smem_z, e.stream>>>(
+        w, out, e.g, e.pzf, e.t32.fPz, 1.0 / e.g.vol);
+    e.post(kslot<float>(kK_z_c2r));
+    return e.check("ifft");
+  }
   cudaMemcpyAsync(e.S0, in, sizeof(double2) * e.g.NC, cudaMemcpyDeviceToDevice, e.stream);
   e.pre(kK_x_fft);
     k_x_fft<double, +1><<<e.x_tiles(e.t64.Bx), kThreads, e.t64.smem_x2, e.stream>>>(
@@ -2870,6 +2919,15 @@ int Engine::ifft(const double2 *in, double *out) {
 
 int Engine::weighted(const FmtSpec &f, const double *n, double *out5) {
   EngineImpl &e = *impl_;
+  if (f.precision == kPrecisionMixed) {
+    if (e.upload_args(f) || e.ensure_table<float>(f.R) || e.forward_weighted<float>(f, n))
+      return -1;
+    e.pre(kslot<float>(kK_z_c2r));
+    k_z_c2r<float><<<dim3(e.pairs_tiles(e.t32.Pz), 5), kThreads, e.t32.smem_z, e.stream>>>(
+        e.spec5<float>(), out5, e.g, e.pzf, e.t32.fPz, 1.0);
+    e.post(kslot<float>(kK_z_c2r));
+    return e.check("weighted");
+  }
   if (e.ensure_table<double>(f.R) || e.forward_weighted<double>(f, n)) return -1;
   e.pre(kK_z_c2r);
     k_z_c2r<double><<<dim3(e.pairs_tiles(e.t64.Pz), 5), kThreads, e.t64.smem_z, e.stream>>>(

@@ -98,10 +98,11 @@ class Engine {
 
   // fft(gd, v): r2c x dV (src/Grid.cpp:470-478); ifft: c2r x 1/V
   // (src/ReciprocalGrid.cpp:42-66).  out of fft / in of ifft: NC complex.
-  int fft(const double *in, double2 *out);
-  int ifft(const double2 *in, double *out);
+  // f32: the transforms in FP32 (the mixed form), FP64 in and out.
+  int fft(const double *in, double2 *out, bool f32 = false);
+  int ifft(const double2 *in, double *out, bool f32 = false);
 
-  // n3, n2, n2x, n2y, n2z (5*NR reals).
+  // n3, n2, n2x, n2y, n2z (5*NR reals), in f's precision.
   int weighted(const FmtSpec &f, const double *n, double *out5);
 
   // Energy (terms_host gets the 6 per-term energies, may be null).

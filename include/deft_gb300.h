@@ -49,7 +49,8 @@ extern "C" {
 #define DEFT_TERM_SAFT 64 /* water SAFT association + dispersion terms (src/haskell/WaterSaft.hs:
                              35-104; src/WaterSaftFast.cpp), parameters from deft_fmt_set_saft;
                              with DEFT_TERM_HS (White Bear), IDEAL and MU this is WaterSaft(...).
-                             FP64 only */
+                             In the mixed form its transforms run in FP32 and the minimiser's
+                             refinement is FP64 CG */
 
 /* Number of per-term energies: phi3, phi1, phi2 (src/HardSpheres.cpp:156),
  * ideal gas, chemical potential, external potential. */
