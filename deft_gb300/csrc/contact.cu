@@ -111,13 +111,13 @@ int contact_values(Engine *e, const FmtSpec &f, int which, const double *n, doub
     double2 *spec = reinterpret_cast<double2 *>(scratch);
     double2 *acc = spec + NC;
     double *num = reinterpret_cast<double *>(acc + NC);
-    if (e->fft(n, spec)) return fail("fft");
+    if (e->fft(n, spec, Engine::kArithDF)) return fail("fft");
     cm::k_weight_apply<<<blocks_for(NC), kThreads, 0, s>>>(9, g, f.R, 0.0, spec, acc, 0, 1);
-    if (e->ifft(acc, num)) return fail("ifft");
+    if (e->ifft(acc, num, Engine::kArithDF)) return fail("ifft");
     k_contact_finish<<<blocks_for(NR), kThreads, 0, s>>>(which, num, nullptr, NR, out);
   } else {
     double *w = scratch;
-    if (e->weighted(f64, n, w)) return fail("weighted densities");
+    if (e->weighted(f64, n, w, Engine::kArithDF)) return fail("weighted densities");
     if (which != DEFT_CONTACT_GSIGMA_A) {
       k_contact_point<<<blocks_for(NR), kThreads, 0, s>>>(which, f.hs, f.R, w, NR, out);
     } else {
@@ -126,13 +126,13 @@ int contact_values(Engine *e, const FmtSpec &f, int which, const double *n, doub
       double2 *acc = spec + NC;
       for (int a = 0; a < 8; a++) {
         k_contact_source<<<blocks_for(NR), kThreads, 0, s>>>(a, f.hs, f.R, w, NR, src);
-        if (e->fft(src, spec)) return fail("fft");
+        if (e->fft(src, spec, Engine::kArithDF)) return fail("fft");
         cm::k_weight_apply<<<blocks_for(NC), kThreads, 0, s>>>(a, g, f.R, 0.0, spec, acc, 0, a == 0);
       }
-      if (e->ifft(acc, num)) return fail("ifft");
-      if (e->fft(n, spec)) return fail("fft");
+      if (e->ifft(acc, num, Engine::kArithDF)) return fail("ifft");
+      if (e->fft(n, spec, Engine::kArithDF)) return fail("fft");
       cm::k_weight_apply<<<blocks_for(NC), kThreads, 0, s>>>(8, g, f.R, 0.0, spec, acc, 0, 1);
-      if (e->ifft(acc, den)) return fail("ifft");
+      if (e->ifft(acc, den, Engine::kArithDF)) return fail("ifft");
       k_contact_finish<<<blocks_for(NR), kThreads, 0, s>>>(which, num, den, NR, out);
     }
   }

@@ -711,7 +711,8 @@ int deft_fmt_weighted(deft_fmt *f, const double *n, int on_device, double *out5)
   }
   const double *dens;
   if (int s = fmt_density(f, spec_of(f), src, &dens)) return s;
-  if (g->eng->weighted(spec_of(f), dens, dst)) return eng_err(g->eng);
+  // FP64 transforms whatever the functional's precision
+  if (g->eng->weighted(fp64_of(spec_of(f)), dens, dst)) return eng_err(g->eng);
   if (!on_device) {
     cudaError_t e = cudaMemcpyAsync(out5, dst, 5 * sizeof(double) * nr(g), cudaMemcpyDeviceToHost,
                                     g->ctx->stream);

@@ -1443,6 +1443,19 @@ __global__ void k_c_d2f(const double2 *__restrict__ in, float2 *__restrict__ out
     out[i] = make_float2((float)v.x, (float)v.y);
   }
 }
+// ... and between double-float and FP64 spectra.
+__global__ void k_c_df2d(const dfc *__restrict__ in, double2 *__restrict__ out, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const dfc v = in[i];
+    out[i] = make_double2(double(v.x), double(v.y));
+  }
+}
+__global__ void k_c_d2df(const double2 *__restrict__ in, dfc *__restrict__ out, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double2 v = in[i];
+    out[i] = dfc{dfl(v.x), dfl(v.y)};
+  }
+}
 
 // Energy partials of the local terms only (no hard spheres).
 template <typename T>
@@ -2148,6 +2161,9 @@ class EngineImpl {
     set_smem(k_z_phi<double, true>, t64.smem_phi);
     set_smem(k_z_grad<double>, t64.smem_z);
     set_smem(k_z_r2c<dfl>, t64.smem_z);
+    set_smem(k_x_fft<dfl, -1>, t64.smem_x2);
+    set_smem(k_x_fft<dfl, +1>, t64.smem_x2);
+    set_smem(k_z_c2r<dfl>, t64.smem_z);
     set_smem(k_x_fft<float, -1>, t32.smem_x2);
     set_smem(k_x_fft<float, +1>, t32.smem_x2);
     set_smem(k_z_c2r<float>, t32.smem_z);
@@ -2862,9 +2878,9 @@ cudaStream_t Engine::stream() const { return impl_->stream; }
 size_t Engine::scratch_bytes() const { return impl_->bytes; }
 const char *Engine::last_error() const { return impl_->err.c_str(); }
 
-int Engine::fft(const double *in, double2 *out, bool f32) {
+int Engine::fft(const double *in, double2 *out, Arith a) {
   EngineImpl &e = *impl_;
-  if (f32) {
+  if (a == kArithFP32) {
     // FP32 transforms (mixed form): z, y, x in the work spectrum, then FP64 out
     float2 *w = reinterpret_cast<float2 *>(e.S0);
     e.z_r2c_spec0<float>(in);
@@ -2874,6 +2890,18 @@ int Engine::fft(const double *in, double2 *out, bool f32) {
         w, e.g, e.pxf, e.t32.fBx, (float)e.g.dV);
     e.post(kslot<float>(kK_x_fft));
     k_c_f2d<<<e.dot_blocks, kThreads, 0, e.stream>>>(w, out, e.g.NC);
+    return e.check("fft");
+  }
+  if (a == kArithDF && e.df_on) {
+    // double-float transforms, FP64 out
+    dfc *w = reinterpret_cast<dfc *>(e.S0);
+    e.z_r2c_spec0<dfl>(in);
+    e.y_fft<dfl>(w, 1, -1);
+    e.pre(kK_x_fft);
+    k_x_fft<dfl, -1><<<e.x_tiles(e.t64.Bx), kThreads, e.t64.smem_x2, e.stream>>>(
+        w, e.g, e.pxd, e.t64.fBx, dfl(e.g.dV));
+    e.post(kK_x_fft);
+    k_c_df2d<<<e.dot_blocks, kThreads, 0, e.stream>>>(w, out, e.g.NC);
     return e.check("fft");
   }
   e.pre(kK_z_r2c);
@@ -2888,9 +2916,9 @@ int Engine::fft(const double *in, double2 *out, bool f32) {
   return e.check("fft");
 }
 
-int Engine::ifft(const double2 *in, double *out, bool f32) {
+int Engine::ifft(const double2 *in, double *out, Arith a) {
   EngineImpl &e = *impl_;
-  if (f32) {
+  if (a == kArithFP32) {
     float2 *w = reinterpret_cast<float2 *>(e.S0);
     k_c_d2f<<<e.dot_blocks, kThreads, 0, e.stream>>>(in, w, e.g.NC);
     e.pre(kslot<float>(kK_x_fft));
@@ -2902,6 +2930,20 @@ int Engine::ifft(const double2 *in, double *out, bool f32) {
     k_z_c2r<float><<<dim3(e.pairs_tiles(e.t32.Pz), 1), kThreads, e.t32.smem_z, e.stream>>>(
         w, out, e.g, e.pzf, e.t32.fPz, 1.0 / e.g.vol);
     e.post(kslot<float>(kK_z_c2r));
+    return e.check("ifft");
+  }
+  if (a == kArithDF && e.df_on) {
+    dfc *w = reinterpret_cast<dfc *>(e.S0);
+    k_c_d2df<<<e.dot_blocks, kThreads, 0, e.stream>>>(in, w, e.g.NC);
+    e.pre(kK_x_fft);
+    k_x_fft<dfl, +1><<<e.x_tiles(e.t64.Bx), kThreads, e.t64.smem_x2, e.stream>>>(
+        w, e.g, e.pxd, e.t64.fBx, dfl(1));
+    e.post(kK_x_fft);
+    e.y_fft<dfl>(w, 1, +1);
+    e.pre(kK_z_c2r);
+    k_z_c2r<dfl><<<dim3(e.pairs_tiles(e.t64.Pz), 1), kThreads, e.t64.smem_z, e.stream>>>(
+        w, out, e.g, e.pzd, e.t64.fPz, 1.0 / e.g.vol);
+    e.post(kK_z_c2r);
     return e.check("ifft");
   }
   cudaMemcpyAsync(e.S0, in, sizeof(double2) * e.g.NC, cudaMemcpyDeviceToDevice, e.stream);
@@ -2917,7 +2959,7 @@ int Engine::ifft(const double2 *in, double *out, bool f32) {
   return e.check("ifft");
 }
 
-int Engine::weighted(const FmtSpec &f, const double *n, double *out5) {
+int Engine::weighted(const FmtSpec &f, const double *n, double *out5, Arith a) {
   EngineImpl &e = *impl_;
   if (f.precision == kPrecisionMixed) {
     if (e.upload_args(f) || e.ensure_table<float>(f.R) || e.forward_weighted<float>(f, n))
@@ -2926,6 +2968,14 @@ int Engine::weighted(const FmtSpec &f, const double *n, double *out5) {
     k_z_c2r<float><<<dim3(e.pairs_tiles(e.t32.Pz), 5), kThreads, e.t32.smem_z, e.stream>>>(
         e.spec5<float>(), out5, e.g, e.pzf, e.t32.fPz, 1.0);
     e.post(kslot<float>(kK_z_c2r));
+    return e.check("weighted");
+  }
+  if (a == kArithDF && e.df_on) {
+    if (e.upload_args(f) || e.ensure_table<dfl>(f.R) || e.forward_weighted<dfl>(f, n)) return -1;
+    e.pre(kK_z_c2r);
+    k_z_c2r<dfl><<<dim3(e.pairs_tiles(e.t64.Pz), 5), kThreads, e.t64.smem_z, e.stream>>>(
+        e.spec5<dfl>(), out5, e.g, e.pzd, e.t64.fPz, 1.0);
+    e.post(kK_z_c2r);
     return e.check("weighted");
   }
   if (e.ensure_table<double>(f.R) || e.forward_weighted<double>(f, n)) return -1;

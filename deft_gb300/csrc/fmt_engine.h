@@ -98,12 +98,16 @@ class Engine {
 
   // fft(gd, v): r2c x dV (src/Grid.cpp:470-478); ifft: c2r x 1/V
   // (src/ReciprocalGrid.cpp:42-66).  out of fft / in of ifft: NC complex.
-  // f32: the transforms in FP32 (the mixed form), FP64 in and out.
-  int fft(const double *in, double2 *out, bool f32 = false);
-  int ifft(const double2 *in, double *out, bool f32 = false);
+  // Arithmetic of the transforms (FP64 in and out in every case):
+  // kArithFP64 FP64 butterflies, kArithDF double-float (FP64 if the engine's
+  // double-float transforms are off), kArithFP32 FP32 (the mixed form).
+  enum Arith { kArithFP64 = 0, kArithDF = 1, kArithFP32 = 2 };
+  int fft(const double *in, double2 *out, Arith a = kArithFP64);
+  int ifft(const double2 *in, double *out, Arith a = kArithFP64);
 
-  // n3, n2, n2x, n2y, n2z (5*NR reals), in f's precision.
-  int weighted(const FmtSpec &f, const double *n, double *out5);
+  // n3, n2, n2x, n2y, n2z (5*NR reals): FP32 transforms when f is mixed,
+  // else those of `a`.
+  int weighted(const FmtSpec &f, const double *n, double *out5, Arith a = kArithFP64);
 
   // Energy (terms_host gets the 6 per-term energies, may be null).
   // V, mask may be null when the corresponding term flag is off.

@@ -181,43 +181,44 @@ int saft_terms(Engine *e, const FmtSpec &f, const SaftParams &sp, const double *
     return -1;
   };
   // the mixed form runs every transform in FP32 (pointwise work stays FP64)
-  const bool f32 = f.precision == kPrecisionMixed;
+  const Engine::Arith arith =
+      f.precision == kPrecisionMixed ? Engine::kArithFP32 : Engine::kArithDF;
   FmtSpec fw = f;
   fw.hs = kHsWhiteBear;
-  if (e->weighted(fw, n, w)) return fail("weighted densities");
+  if (e->weighted(fw, n, w, arith)) return fail("weighted densities");
   for (int a = 0; a < 8; a++) {
     k_saft_source<<<rb, kThreads, 0, s>>>(a, R, w, NR, t);
-    if (e->fft(t, spec, f32)) return fail("fft");
+    if (e->fft(t, spec, arith)) return fail("fft");
     cm::k_weight_apply<<<cb, kThreads, 0, s>>>(a, g, R, 0.0, spec, acc, 0, a == 0);
   }
-  if (e->ifft(acc, A, f32)) return fail("ifft");
-  if (e->fft(n, spec, f32)) return fail("fft");
+  if (e->ifft(acc, A, arith)) return fail("ifft");
+  if (e->fft(n, spec, arith)) return fail("fft");
   cm::k_weight_apply<<<cb, kThreads, 0, s>>>(8, g, R, 0.0, spec, acc, 0, 1);
-  if (e->ifft(acc, D2, f32)) return fail("ifft");
+  if (e->ifft(acc, D2, arith)) return fail("ifft");
   cm::k_weight_apply<<<cb, kThreads, 0, s>>>(10, g, R, gs, spec, acc, 0, 1);
-  if (e->ifft(acc, Eg, f32)) return fail("ifft");
+  if (e->ifft(acc, Eg, arith)) return fail("ifft");
   k_saft_point<<<kBlocks, kThreads, 0, s>>>(sp, R, f.kT, n, A, D2, Eg, NR, grad != nullptr, lA, lD,
                                             lE, expl, partials);
   k_saft_sum<<<1, 32, 0, s>>>(partials, kBlocks, g.dV, sums);
   if (grad) {
     // adjoint of gSigmaA's eight convolutions, through the source Jacobian
     double2 *specA = acc;  // spectrum of lA, kept while the eight adjoints are formed
-    if (e->fft(lA, specA, f32)) return fail("fft");
+    if (e->fft(lA, specA, arith)) return fail("fft");
     for (int a = 0; a < 8; a++) {
       cm::k_weight_apply<<<cb, kThreads, 0, s>>>(a, g, R, 0.0, specA, spec, 1, 1);
-      if (e->ifft(spec, t, f32)) return fail("ifft");
+      if (e->ifft(spec, t, arith)) return fail("ifft");
       k_saft_jac<<<rb, kThreads, 0, s>>>(a, R, w, t, NR, lw);
     }
     // weighted-density adjoints (step, shell, vector shells), shell_2R, Gaussian
     for (int b = 0; b < 5; b++) {
-      if (e->fft(lw + (size_t)b * NR, spec, f32)) return fail("fft");
+      if (e->fft(lw + (size_t)b * NR, spec, arith)) return fail("fft");
       cm::k_weight_apply<<<cb, kThreads, 0, s>>>(11 + b, g, R, 0.0, spec, acc, 1, b == 0);
     }
-    if (e->fft(lD, spec, f32)) return fail("fft");
+    if (e->fft(lD, spec, arith)) return fail("fft");
     cm::k_weight_apply<<<cb, kThreads, 0, s>>>(8, g, R, 0.0, spec, acc, 1, 0);
-    if (e->fft(lE, spec, f32)) return fail("fft");
+    if (e->fft(lE, spec, arith)) return fail("fft");
     cm::k_weight_apply<<<cb, kThreads, 0, s>>>(10, g, R, gs, spec, acc, 1, 0);
-    if (e->ifft(acc, t, f32)) return fail("ifft");
+    if (e->ifft(acc, t, arith)) return fail("ifft");
     k_saft_grad<<<rb, kThreads, 0, s>>>(g.dV, expl, t, NR, grad);
   }
   cudaError_t ce = cudaMemcpyAsync(terms2, sums, 2 * sizeof(double), cudaMemcpyDeviceToHost, s);

@@ -201,20 +201,20 @@ int tensor_hs(Engine *e, const FmtSpec &f, const double *n, double *scratch, dou
   };
   const int kind = f.hs == kHsTarazona ? 1 : 0;
   const int cblocks = (NC + kThreads - 1) / kThreads < 4096 ? (NC + kThreads - 1) / kThreads : 4096;
-  if (e->fft(n, Nk)) return fail("fft");
+  if (e->fft(n, Nk, Engine::kArithDF)) return fail("fft");
   for (int a = 0; a < 11; a++) {
     k_tensor_weight<<<cblocks, kThreads, 0, s>>>(a, g, f.R, Nk, tmp, 0, 1);
-    if (e->ifft(tmp, w + (size_t)a * NR)) return fail("ifft");
+    if (e->ifft(tmp, w + (size_t)a * NR, Engine::kArithDF)) return fail("ifft");
   }
   k_tensor_phi<<<kBlocks, kThreads, 0, s>>>(kind, f.R, f.kT, g.dV, w, NR, grad ? part : nullptr,
                                             partials);
   k_tensor_sum<<<1, 32, 0, s>>>(partials, kBlocks, g.dV, sums);
   if (grad) {
     for (int a = 0; a < 11; a++) {
-      if (e->fft(part + (size_t)a * NR, tmp)) return fail("fft");
+      if (e->fft(part + (size_t)a * NR, tmp, Engine::kArithDF)) return fail("fft");
       k_tensor_weight<<<cblocks, kThreads, 0, s>>>(a, g, f.R, tmp, acc, 1, a == 0);
     }
-    if (e->ifft(acc, grad)) return fail("ifft");
+    if (e->ifft(acc, grad, Engine::kArithDF)) return fail("ifft");
   }
   cudaError_t ce = cudaMemcpyAsync(terms3, sums, 3 * sizeof(double), cudaMemcpyDeviceToHost, s);
   if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);
