@@ -442,8 +442,6 @@ static int check_fmt_params(const deft_fmt_params *p) {
     return set_err(DEFT_ERR_ARG, "unknown precision");
   if (p->functional < DEFT_HS_WB_NOTENSOR || p->functional > DEFT_HS_TARAZONA)
     return set_err(DEFT_ERR_ARG, "unknown hard-sphere functional");
-  if (p->functional >= DEFT_HS_WB_TENSOR && p->precision != DEFT_PRECISION_FP64)
-    return set_err(DEFT_ERR_ARG, "the tensor functionals evaluate in FP64 only");
   if ((p->terms & DEFT_TERM_SAFT) && p->functional != DEFT_HS_WB_NOTENSOR)
     return set_err(DEFT_ERR_ARG, "the SAFT terms go with the White Bear functional");
   return DEFT_OK;
@@ -1650,7 +1648,7 @@ int deft_cg_step(deft_cg *c, deft_cg_status *st) {
           if (!status && (c->done || st->gnorm < thr || c->iter > 0 && !c->have_g)) {
             c->stage = 1;
             c->done = false;
-            if ((c->f->p.terms & DEFT_TERM_VEFF) || has_saft(c->f)) {
+            if ((c->f->p.terms & DEFT_TERM_VEFF) || has_saft(c->f) || is_tensor(c->f)) {
               // refinement by FP64 CG (the Newton step works in the density
               // variable): restart the conjugate directions
               c->have_g = false;
@@ -1658,9 +1656,9 @@ int deft_cg_step(deft_cg *c, deft_cg_status *st) {
               c->pgoldsqr = 0;
             }
           }
-        } else if ((c->f->p.terms & DEFT_TERM_VEFF) || has_saft(c->f)) {
+        } else if ((c->f->p.terms & DEFT_TERM_VEFF) || has_saft(c->f) || is_tensor(c->f)) {
           // the refinement by FP64 CG (the Newton step's Hessian covers the
-          // hard spheres and the ideal gas, in the density variable)
+          // vector White Bear kinds and the ideal gas, in the density variable)
           status = step_secant(c, st, fp64_of(spec), c->p.gtol);
         } else {
           status = step_newton(c, st, spec);

@@ -200,21 +200,24 @@ int tensor_hs(Engine *e, const FmtSpec &f, const double *n, double *scratch, dou
     return -1;
   };
   const int kind = f.hs == kHsTarazona ? 1 : 0;
+  // the mixed form runs the transforms in FP32 (Phi and its partials FP64)
+  const Engine::Arith arith =
+      f.precision == kPrecisionMixed ? Engine::kArithFP32 : Engine::kArithDF;
   const int cblocks = (NC + kThreads - 1) / kThreads < 4096 ? (NC + kThreads - 1) / kThreads : 4096;
-  if (e->fft(n, Nk, Engine::kArithDF)) return fail("fft");
+  if (e->fft(n, Nk, arith)) return fail("fft");
   for (int a = 0; a < 11; a++) {
     k_tensor_weight<<<cblocks, kThreads, 0, s>>>(a, g, f.R, Nk, tmp, 0, 1);
-    if (e->ifft(tmp, w + (size_t)a * NR, Engine::kArithDF)) return fail("ifft");
+    if (e->ifft(tmp, w + (size_t)a * NR, arith)) return fail("ifft");
   }
   k_tensor_phi<<<kBlocks, kThreads, 0, s>>>(kind, f.R, f.kT, g.dV, w, NR, grad ? part : nullptr,
                                             partials);
   k_tensor_sum<<<1, 32, 0, s>>>(partials, kBlocks, g.dV, sums);
   if (grad) {
     for (int a = 0; a < 11; a++) {
-      if (e->fft(part + (size_t)a * NR, tmp, Engine::kArithDF)) return fail("fft");
+      if (e->fft(part + (size_t)a * NR, tmp, arith)) return fail("fft");
       k_tensor_weight<<<cblocks, kThreads, 0, s>>>(a, g, f.R, tmp, acc, 1, a == 0);
     }
-    if (e->ifft(acc, grad, Engine::kArithDF)) return fail("ifft");
+    if (e->ifft(acc, grad, arith)) return fail("ifft");
   }
   cudaError_t ce = cudaMemcpyAsync(terms3, sums, 3 * sizeof(double), cudaMemcpyDeviceToHost, s);
   if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);

@@ -85,14 +85,16 @@ typedef struct deft_cg deft_cg;
 
 /* Hard-sphere functional (deft_fmt_params.functional).  The first three share
  * the weighted densities n3, n2, n2v and differ in their phi2, phi3
- * prefactors; the tensor ones add the six tensor weighted densities. */
+ * prefactors; the tensor ones add the six tensor weighted densities (their
+ * mixed form runs the eleven convolutions in FP32, and the minimiser's
+ * refinement is FP64 CG instead of Newton steps). */
 #define DEFT_HS_WB_NOTENSOR 0 /* HardSpheresWBnotensor, src/HardSpheres.cpp:137-159 */
 #define DEFT_HS_RF 1          /* HardSpheresRF (Rosenfeld), src/HardSpheres.cpp:69-88 */
 #define DEFT_HS_WB_MARK2 2    /* WhiteBearMarkII (whitebear_m2, src/haskell/WhiteBear.hs:140-159),
                                  vector third term */
 #define DEFT_HS_WB_TENSOR 3   /* HardSpheresWB: White Bear with the tensor third term,
-                                 src/HardSpheres.cpp:30-61,113-135 (FP64 only) */
-#define DEFT_HS_TARAZONA 4    /* HardSpheresTarazona, src/HardSpheres.cpp:90-111 (FP64 only) */
+                                 src/HardSpheres.cpp:30-61,113-135 */
+#define DEFT_HS_TARAZONA 4    /* HardSpheresTarazona, src/HardSpheres.cpp:90-111 */
 
 typedef struct {
   double R;   /* hard-sphere radius */

@@ -145,39 +145,47 @@ def test_unknown_functional_is_refused(ctx):
     g.close()
 
 
+@pytest.mark.parametrize("precision", [0, 1])
 @pytest.mark.parametrize("name,hs", [("cubic12", 3), ("ortho_odd", 3), ("fcc12", 3),
                                      ("cubic12", 4), ("fcc12", 4)])
-def test_tensor_fp64_matches_reference_golden(ctx, oracle_mod, golden, name, hs):
+def test_tensor_matches_reference_golden(ctx, oracle_mod, golden, name, hs, precision):
+    """The compiled HardSpheresWB / HardSpheresTarazona energy, per-term
+    energies and gradient: FP64 form to 1e-10 / 1e-9; mixed form (eleven
+    convolutions in FP32) to 1e-6 / 1e-4 of the largest entry."""
     from tests.capi import Fmt, Grid
     from tests.golden.cases import make_case
     vals, arrs = golden
     P, n = make_case(name, hs)
     g = Grid(ctx, P.lat.reshape(3, 3), P.N)
-    f = Fmt(g, R=P.R, kT=P.kT, mu=P.mu, terms=P.terms, V=P.V, mask=P.mask, functional=hs)
+    f = Fmt(g, R=P.R, kT=P.kT, mu=P.mu, terms=P.terms, V=P.V, mask=P.mask, functional=hs,
+            precision=precision)
     E, grad, terms = f.energy_grad(n)
     ref = vals[f"{name}_hs{hs}"]
-    assert abs(E / ref["E"] - 1) < 1e-10
+    e_tol, g_tol = (1e-10, 1e-9) if precision == 0 else (1e-6, 1e-4)
+    assert abs(E / ref["E"] - 1) < e_tol
     tr = np.array(ref["terms"])
-    assert np.abs(terms[:len(tr)] - tr).max() <= 1e-10 * np.abs(tr).max()
+    assert np.abs(terms[:len(tr)] - tr).max() <= e_tol * np.abs(tr).max()
     gr = arrs[f"{name}_hs{hs}_grad"]
-    assert np.abs(grad - gr).max() <= 1e-9 * np.abs(gr).max()
+    assert np.abs(grad - gr).max() <= g_tol * np.abs(gr).max()
     E2, _ = f.energy(n)
-    assert abs(E2 / E - 1) < 1e-14
+    assert abs(E2 / E - 1) < (1e-14 if precision == 0 else 1e-6)
     f.close()
     g.close()
 
 
+@pytest.mark.parametrize("precision", [0, 1])
 @pytest.mark.parametrize("hs", [_lib.HS_WB_TENSOR, _lib.HS_TARAZONA])
-def test_tensor_secant_solve_matches_oracle_profile(ctx, oracle_mod, hs):
-    """FP64 CG with the tensor functional on the slit, to |grad| < 1e-10:
-    the profile equals the oracle's 1-D solve of the same functional."""
+def test_tensor_secant_solve_matches_oracle_profile(ctx, oracle_mod, hs, precision):
+    """CG with the tensor functional on the slit, to |grad| < 1e-10 (the
+    mixed form: FP32 stage, then FP64 CG): the profile equals the oracle's
+    1-D solve of the same functional."""
     from tests.capi import CG, Fmt, Grid
     O = oracle_mod
     s = _slit()
     mask = s.mask.reshape(-1)
     terms = O.HS | O.IDEAL | O.MU | O.MASK
     g = Grid(ctx, s.lat, s.shape)
-    f = Fmt(g, mu=s.mu, terms=terms, mask=mask, functional=hs)
+    f = Fmt(g, mu=s.mu, terms=terms, mask=mask, functional=hs, precision=precision)
     cg = CG(f, gtol=1e-10, maxiter=5000, step=1.0, preconditioned=_lib.PC_DENSITY)
     cg.set_x(s.n0.reshape(-1))
     code, st = cg.solve()
@@ -193,11 +201,17 @@ def test_tensor_secant_solve_matches_oracle_profile(ctx, oracle_mod, hs):
     g.close()
 
 
-def test_tensor_functionals_refuse_the_mixed_form(ctx):
+def test_tensor_functionals_have_no_hessian_vector_product(ctx):
+    """The Newton step's FP32 Hessian covers the vector kinds only: the
+    tensor kinds' mixed form refines by FP64 CG, and the product is refused."""
     import ctypes
-    from tests.capi import Grid
+    from tests.capi import Fmt, Grid
     g = Grid(ctx, np.diag([2.4, 2.4, 2.4]), (12, 12, 12))
-    p = _lib.FmtParams(1.0, 1.0, 0.0, 7, _lib.PRECISION_MIXED, _lib.HS_WB_TENSOR)
-    h = ctypes.c_void_p()
-    assert g.L.deft_fmt_create(g.h, ctypes.byref(p), ctypes.byref(h)) == _lib.ERR_ARG
+    f = Fmt(g, R=1.0, kT=1.0, mu=0.0, terms=7, precision=_lib.PRECISION_MIXED,
+            functional=_lib.HS_WB_TENSOR)
+    n = np.full(12 ** 3, 0.05)
+    out = np.empty_like(n)
+    assert f.L.deft_fmt_hessian_vector(f.h, n.ctypes.data, n.ctypes.data, 0,
+                                       out.ctypes.data) == _lib.ERR_ARG
+    f.close()
     g.close()
