@@ -55,14 +55,16 @@ __device__ void a1_terms(double eta, double lam, double eps, double o[5]) {
                 L3 * (g1 * xl + eta * (g2 * xl * xe + g1 * xel)));    // d2 a1 / d eta d lambda
 }
 
-// Source field a of gSigmaA (White Bear partials).
-__global__ void k_saft_source(int a, double R, const double *__restrict__ w, int NR,
-                              double *__restrict__ src) {
+// The eight source fields of gSigmaA (White Bear partials, computed once
+// per point): src + a NR, a < 8.
+__global__ void k_saft_sources(double R, const double *__restrict__ w, int NR,
+                               double *__restrict__ src) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < NR; i += gridDim.x * blockDim.x) {
     const double v[3] = {w[2 * (size_t)NR + i], w[3 * (size_t)NR + i], w[4 * (size_t)NR + i]};
     const cm::Partials p = cm::partials(kHsWhiteBear, R, w[i], w[(size_t)NR + i],
                                         v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
-    src[i] = cm::gsa_source(a, p, v, R);
+#pragma unroll
+    for (int a = 0; a < 8; a++) src[(size_t)a * NR + i] = cm::gsa_source(a, p, v, R);
   }
 }
 
@@ -129,21 +131,24 @@ __global__ void k_saft_sum(const double *__restrict__ partials, int nblk, double
   }
 }
 
-// lw[b] (+)= t * d(source a)/d(w_b): the adjoint of gSigmaA's numerator
-// through its source fields into the five weighted densities.
-__global__ void k_saft_jac(int a, double R, const double *__restrict__ w,
-                           const double *__restrict__ t, int NR, double *__restrict__ lw) {
+// lw[b] = sum_a t_a d(source a)/d(w_b) (t_a = t + a NR): the adjoint of
+// gSigmaA's numerator through its source fields into the five weighted
+// densities, the partials and their derivatives computed once per point.
+__global__ void k_saft_jacs(double R, const double *__restrict__ w,
+                            const double *__restrict__ t, int NR, double *__restrict__ lw) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < NR; i += gridDim.x * blockDim.x) {
     const double v[3] = {w[2 * (size_t)NR + i], w[3 * (size_t)NR + i], w[4 * (size_t)NR + i]};
-    double D[6][3], J[5];
+    double D[6][3];
     const cm::Partials p = cm::partials(kHsWhiteBear, R, w[i], w[(size_t)NR + i],
                                         v[0] * v[0] + v[1] * v[1] + v[2] * v[2], D);
-    cm::gsa_jacobian(a, p, D, v, R, J);
-    const double ti = t[i];
-    for (int b = 0; b < 5; b++) {
-      double *o = lw + (size_t)b * NR + i;
-      *o = (a == 0 ? 0.0 : *o) + ti * J[b];
+    double acc[5] = {0, 0, 0, 0, 0};
+    for (int a = 0; a < 8; a++) {
+      double J[5];
+      cm::gsa_jacobian(a, p, D, v, R, J);
+      const double ti = t[(size_t)a * NR + i];
+      for (int b = 0; b < 5; b++) acc[b] += ti * J[b];
     }
+    for (int b = 0; b < 5; b++) lw[(size_t)b * NR + i] = acc[b];
   }
 }
 
@@ -161,9 +166,9 @@ int blocks_for(int n) {
 }  // namespace
 
 size_t saft_scratch_doubles(const Geom &g) {
-  // w (5), A, D2, Eg, src/t, lA, lD, lE, expl (8), lw (5) real fields; two
-  // spectra; block partials and sums
-  return 18 * (size_t)g.NR + 4 * (size_t)g.NC + 2 * kBlocks + 2;
+  // w (5), A, D2, Eg, the eight source / adjoint fields t, lA, lD, lE, expl,
+  // lw (5) real fields; two spectra; block partials and sums
+  return 25 * (size_t)g.NR + 4 * (size_t)g.NC + 2 * kBlocks + 2;
 }
 
 int saft_terms(Engine *e, const FmtSpec &f, const SaftParams &sp, const double *n,
@@ -172,7 +177,7 @@ int saft_terms(Engine *e, const FmtSpec &f, const SaftParams &sp, const double *
   cudaStream_t s = e->stream();
   const int NR = g.NR, NC = g.NC, rb = blocks_for(NR), cb = blocks_for(NC);
   double *w = scratch, *A = w + 5 * (size_t)NR, *D2 = A + NR, *Eg = D2 + NR, *t = Eg + NR;
-  double *lA = t + NR, *lD = lA + NR, *lE = lD + NR, *expl = lE + NR, *lw = expl + NR;
+  double *lA = t + 8 * (size_t)NR, *lD = lA + NR, *lE = lD + NR, *expl = lE + NR, *lw = expl + NR;
   double2 *spec = reinterpret_cast<double2 *>(lw + 5 * (size_t)NR), *acc = spec + NC;
   double *partials = reinterpret_cast<double *>(acc + NC), *sums = partials + 2 * kBlocks;
   const double R = f.R, gs = 2 * sp.length_scaling * sp.lambda_d * R;
@@ -186,9 +191,9 @@ int saft_terms(Engine *e, const FmtSpec &f, const SaftParams &sp, const double *
   FmtSpec fw = f;
   fw.hs = kHsWhiteBear;
   if (e->weighted(fw, n, w, arith)) return fail("weighted densities");
+  k_saft_sources<<<rb, kThreads, 0, s>>>(R, w, NR, t);
   for (int a = 0; a < 8; a++) {
-    k_saft_source<<<rb, kThreads, 0, s>>>(a, R, w, NR, t);
-    if (e->fft(t, spec, arith)) return fail("fft");
+    if (e->fft(t + (size_t)a * NR, spec, arith)) return fail("fft");
     cm::k_weight_apply<<<cb, kThreads, 0, s>>>(a, g, R, 0.0, spec, acc, 0, a == 0);
   }
   if (e->ifft(acc, A, arith)) return fail("ifft");
@@ -206,9 +211,9 @@ int saft_terms(Engine *e, const FmtSpec &f, const SaftParams &sp, const double *
     if (e->fft(lA, specA, arith)) return fail("fft");
     for (int a = 0; a < 8; a++) {
       cm::k_weight_apply<<<cb, kThreads, 0, s>>>(a, g, R, 0.0, specA, spec, 1, 1);
-      if (e->ifft(spec, t, arith)) return fail("ifft");
-      k_saft_jac<<<rb, kThreads, 0, s>>>(a, R, w, t, NR, lw);
+      if (e->ifft(spec, t + (size_t)a * NR, arith)) return fail("ifft");
     }
+    k_saft_jacs<<<rb, kThreads, 0, s>>>(R, w, t, NR, lw);
     // weighted-density adjoints (step, shell, vector shells), shell_2R, Gaussian
     for (int b = 0; b < 5; b++) {
       if (e->fft(lw + (size_t)b * NR, spec, arith)) return fail("fft");
