@@ -211,6 +211,64 @@ __global__ void k_dft_axis(const float2 *__restrict__ in, float2 *__restrict__ o
   }
 }
 
+// The same contraction with MT consecutive outputs m per thread: each input
+// value is loaded once per thread and feeds MT multiply-adds, so the input
+// is read ceil(Mout / MT) times instead of Mout times.  Thread t handles
+// i = t mod inner (consecutive threads: consecutive i, coalesced), output
+// tile (t / inner) mod tiles, and o.
+template <int MT>
+__global__ void k_dft_axis_tile(const float2 *__restrict__ in, float2 *__restrict__ out,
+                                const float2 *__restrict__ E, int outer, int Nin, int Mout,
+                                int inner) {
+  extern __shared__ float sm[];
+  float2 *Es = reinterpret_cast<float2 *>(sm);  // [Mout][Nin]
+  for (int i = threadIdx.x; i < Mout * Nin; i += blockDim.x) Es[i] = E[i];
+  __syncthreads();
+  const int tiles = (Mout + MT - 1) / MT;
+  const long long total = (long long)outer * tiles * inner;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(t % inner);
+    const long long r = t / inner;
+    const int m0 = (int)(r % tiles) * MT;
+    const int o = (int)(r / tiles);
+    const float2 *src = in + (size_t)o * Nin * inner + i;
+    float re[MT], im[MT];
+#pragma unroll
+    for (int u = 0; u < MT; u++) re[u] = im[u] = 0.f;
+    int n = 0;
+    for (; n + 4 <= Nin; n += 4) {
+      float2 a[4];
+#pragma unroll
+      for (int v = 0; v < 4; v++) a[v] = src[(size_t)(n + v) * inner];
+#pragma unroll
+      for (int v = 0; v < 4; v++) {
+#pragma unroll
+        for (int u = 0; u < MT; u++) {
+          const int m = m0 + u < Mout ? m0 + u : Mout - 1;
+          const float2 b = Es[m * Nin + n + v];
+          re[u] += a[v].x * b.x - a[v].y * b.y;
+          im[u] += a[v].x * b.y + a[v].y * b.x;
+        }
+      }
+    }
+    for (; n < Nin; n++) {
+      const float2 a = src[(size_t)n * inner];
+#pragma unroll
+      for (int u = 0; u < MT; u++) {
+        const int m = m0 + u < Mout ? m0 + u : Mout - 1;
+        const float2 b = Es[m * Nin + n];
+        re[u] += a.x * b.x - a.y * b.y;
+        im[u] += a.x * b.y + a.y * b.x;
+      }
+    }
+    float2 *dst = out + ((size_t)o * Mout + m0) * inner + i;
+#pragma unroll
+    for (int u = 0; u < MT; u++)
+      if (m0 + u < Mout) dst[(size_t)u * inner] = make_float2(re[u], im[u]);
+  }
+}
+
 // Spectral mixing U[o][k] = sum_i W[i][o][k] V[i][k]  (W bf16 complex).
 __global__ void k_spec_mix(const float2 *__restrict__ V, const __nv_bfloat16 *__restrict__ W,
                            float2 *__restrict__ U, int C, int K) {
@@ -722,11 +780,23 @@ void launch_z_inv(deft_fno *f, const float2 *in, float *out, const float2 *G, in
     default: k_dft_z_inv<16><<<grid, 128, 0, f->stream>>>(in, out, G, L, f->N, f->Kz, acc); break;
   }
 }
+// Output tile per thread: the widest of 16, 8, 4, 2 that still leaves about
+// 48K threads (the input is then read Mout / MT times from L2).
 void launch_axis(deft_fno *f, const float2 *in, float2 *out, const float2 *E, int outer, int Nin,
                  int Mout, int inner) {
-  const long long total = (long long)outer * Mout * inner;
-  k_dft_axis<<<grid_for(total), kT, sizeof(float2) * Mout * Nin, f->stream>>>(in, out, E, outer,
-                                                                              Nin, Mout, inner);
+  const size_t sm = sizeof(float2) * Mout * Nin;
+  const long long lines = (long long)outer * inner;
+  int mt = 16;
+  while (mt > 1 && lines * ((Mout + mt - 1) / mt) < 48 * 1024) mt /= 2;
+  if (mt > Mout) mt = Mout >= 16 ? 16 : Mout >= 8 ? 8 : Mout >= 4 ? 4 : Mout >= 2 ? 2 : 1;
+  const long long total = lines * ((Mout + mt - 1) / mt);
+  switch (mt) {
+    case 16: k_dft_axis_tile<16><<<grid_for(total), kT, sm, f->stream>>>(in, out, E, outer, Nin, Mout, inner); break;
+    case 8: k_dft_axis_tile<8><<<grid_for(total), kT, sm, f->stream>>>(in, out, E, outer, Nin, Mout, inner); break;
+    case 4: k_dft_axis_tile<4><<<grid_for(total), kT, sm, f->stream>>>(in, out, E, outer, Nin, Mout, inner); break;
+    case 2: k_dft_axis_tile<2><<<grid_for(total), kT, sm, f->stream>>>(in, out, E, outer, Nin, Mout, inner); break;
+    default: k_dft_axis<<<grid_for(lines * Mout), kT, sm, f->stream>>>(in, out, E, outer, Nin, Mout, inner); break;
+  }
 }
 
 // Forward through the spectral part of layer l: S (in zbuf) = Finv(W F h).
@@ -939,8 +1009,14 @@ int deft_fno_create(int device, int N, int channels, int modes, int layers, unsi
   cudaFuncSetAttribute(k_dft_z_fwd<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)zf);
   cudaFuncSetAttribute(k_dft_z_fwd<12>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)zf);
   cudaFuncSetAttribute(k_dft_z_fwd<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)zf);
-  cudaFuncSetAttribute(k_dft_axis, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)(sizeof(float2) * 2 * modes * N));
+  {
+    const int ax = (int)(sizeof(float2) * 2 * modes * N);
+    cudaFuncSetAttribute(k_dft_axis, cudaFuncAttributeMaxDynamicSharedMemorySize, ax);
+    cudaFuncSetAttribute(k_dft_axis_tile<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, ax);
+    cudaFuncSetAttribute(k_dft_axis_tile<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, ax);
+    cudaFuncSetAttribute(k_dft_axis_tile<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, ax);
+    cudaFuncSetAttribute(k_dft_axis_tile<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, ax);
+  }
   k_to_bf16<<<grid_for((long long)off), kT, 0, f->stream>>>(f->p, f->pb, (long long)off);
   if (check(f, "fno create")) {
     deft_fno_destroy(f);
