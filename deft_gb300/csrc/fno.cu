@@ -211,61 +211,50 @@ __global__ void k_dft_axis(const float2 *__restrict__ in, float2 *__restrict__ o
   }
 }
 
-// The same contraction with MT consecutive outputs m per thread: each input
-// value is loaded once per thread and feeds MT multiply-adds, so the input
-// is read ceil(Mout / MT) times instead of Mout times.  Thread t handles
-// i = t mod inner (consecutive threads: consecutive i, coalesced), output
-// tile (t / inner) mod tiles, and o.
+// The same contraction by slabs: a block takes one o and IC consecutive i,
+// stages in[o][0..Nin)[i0..i0+IC) in shared memory (one coalesced read of
+// the input), and thread (il = t mod IC, mg = t / IC) computes the outputs
+// m = mg, mg + G, ... (G = blockDim / IC, at most MT of them) from it; the
+// table E is read through the read-only cache.
 template <int MT>
-__global__ void k_dft_axis_tile(const float2 *__restrict__ in, float2 *__restrict__ out,
-                                const float2 *__restrict__ E, int outer, int Nin, int Mout,
-                                int inner) {
+__global__ void k_dft_axis_slab(const float2 *__restrict__ in, float2 *__restrict__ out,
+                                const float2 *__restrict__ E, int Nin, int Mout, int inner,
+                                int IC) {
   extern __shared__ float sm[];
-  float2 *Es = reinterpret_cast<float2 *>(sm);  // [Mout][Nin]
-  for (int i = threadIdx.x; i < Mout * Nin; i += blockDim.x) Es[i] = E[i];
+  float2 *slab = reinterpret_cast<float2 *>(sm);  // [Nin][IC]
+  const int chunks = (inner + IC - 1) / IC;
+  const int o = blockIdx.x / chunks;
+  const int i0 = (blockIdx.x - o * chunks) * IC;
+  const int ic = inner - i0 < IC ? inner - i0 : IC;
+  const float2 *src = in + (size_t)o * Nin * inner + i0;
+  for (int k = threadIdx.x; k < Nin * IC; k += blockDim.x) {
+    const int n = k / IC, il = k - n * IC;
+    slab[k] = il < ic ? src[(size_t)n * inner + il] : make_float2(0.f, 0.f);
+  }
   __syncthreads();
-  const int tiles = (Mout + MT - 1) / MT;
-  const long long total = (long long)outer * tiles * inner;
-  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
-       t += (long long)gridDim.x * blockDim.x) {
-    const int i = (int)(t % inner);
-    const long long r = t / inner;
-    const int m0 = (int)(r % tiles) * MT;
-    const int o = (int)(r / tiles);
-    const float2 *src = in + (size_t)o * Nin * inner + i;
-    float re[MT], im[MT];
+  const int G = blockDim.x / IC;
+  const int il = threadIdx.x % IC, mg = threadIdx.x / IC;
+  if (mg >= G || il >= ic) return;
+  float re[MT], im[MT];
 #pragma unroll
-    for (int u = 0; u < MT; u++) re[u] = im[u] = 0.f;
-    int n = 0;
-    for (; n + 4 <= Nin; n += 4) {
-      float2 a[4];
+  for (int u = 0; u < MT; u++) re[u] = im[u] = 0.f;
+  for (int n = 0; n < Nin; n++) {
+    const float2 a = slab[n * IC + il];
 #pragma unroll
-      for (int v = 0; v < 4; v++) a[v] = src[(size_t)(n + v) * inner];
-#pragma unroll
-      for (int v = 0; v < 4; v++) {
-#pragma unroll
-        for (int u = 0; u < MT; u++) {
-          const int m = m0 + u < Mout ? m0 + u : Mout - 1;
-          const float2 b = Es[m * Nin + n + v];
-          re[u] += a[v].x * b.x - a[v].y * b.y;
-          im[u] += a[v].x * b.y + a[v].y * b.x;
-        }
-      }
-    }
-    for (; n < Nin; n++) {
-      const float2 a = src[(size_t)n * inner];
-#pragma unroll
-      for (int u = 0; u < MT; u++) {
-        const int m = m0 + u < Mout ? m0 + u : Mout - 1;
-        const float2 b = Es[m * Nin + n];
+    for (int u = 0; u < MT; u++) {
+      const int m = mg + u * G;
+      if (m < Mout) {
+        const float2 b = __ldg(&E[(size_t)m * Nin + n]);
         re[u] += a.x * b.x - a.y * b.y;
         im[u] += a.x * b.y + a.y * b.x;
       }
     }
-    float2 *dst = out + ((size_t)o * Mout + m0) * inner + i;
+  }
+  float2 *dst = out + (size_t)o * Mout * inner + i0 + il;
 #pragma unroll
-    for (int u = 0; u < MT; u++)
-      if (m0 + u < Mout) dst[(size_t)u * inner] = make_float2(re[u], im[u]);
+  for (int u = 0; u < MT; u++) {
+    const int m = mg + u * G;
+    if (m < Mout) dst[(size_t)m * inner] = make_float2(re[u], im[u]);
   }
 }
 
@@ -780,23 +769,30 @@ void launch_z_inv(deft_fno *f, const float2 *in, float *out, const float2 *G, in
     default: k_dft_z_inv<16><<<grid, 128, 0, f->stream>>>(in, out, G, L, f->N, f->Kz, acc); break;
   }
 }
-// Output tile per thread: the widest of 16, 8, 4, 2 that still leaves about
-// 48K threads (the input is then read Mout / MT times from L2).
+// Slab kernel: IC = inner (at most 32) i per block, else 32; 256 threads
+// minus the remainder; MT = outputs per thread, rounded up to 1, 2, 4, 8 or
+// 16.  Nin x IC complex values of shared memory (32 KB at Nin = 128).
 void launch_axis(deft_fno *f, const float2 *in, float2 *out, const float2 *E, int outer, int Nin,
                  int Mout, int inner) {
-  const size_t sm = sizeof(float2) * Mout * Nin;
-  const long long lines = (long long)outer * inner;
-  int mt = 16;
-  while (mt > 1 && lines * ((Mout + mt - 1) / mt) < 48 * 1024) mt /= 2;
-  if (mt > Mout) mt = Mout >= 16 ? 16 : Mout >= 8 ? 8 : Mout >= 4 ? 4 : Mout >= 2 ? 2 : 1;
-  const long long total = lines * ((Mout + mt - 1) / mt);
-  switch (mt) {
-    case 16: k_dft_axis_tile<16><<<grid_for(total), kT, sm, f->stream>>>(in, out, E, outer, Nin, Mout, inner); break;
-    case 8: k_dft_axis_tile<8><<<grid_for(total), kT, sm, f->stream>>>(in, out, E, outer, Nin, Mout, inner); break;
-    case 4: k_dft_axis_tile<4><<<grid_for(total), kT, sm, f->stream>>>(in, out, E, outer, Nin, Mout, inner); break;
-    case 2: k_dft_axis_tile<2><<<grid_for(total), kT, sm, f->stream>>>(in, out, E, outer, Nin, Mout, inner); break;
-    default: k_dft_axis<<<grid_for(lines * Mout), kT, sm, f->stream>>>(in, out, E, outer, Nin, Mout, inner); break;
-  }
+  const int IC = inner <= 32 ? inner : 32;
+  const int G = 256 / IC;
+  const int threads = G * IC;
+  const int need = (Mout + G - 1) / G;
+  const int blocks = outer * ((inner + IC - 1) / IC);
+  const size_t sm = sizeof(float2) * (size_t)Nin * IC;
+  if (need <= 1)
+    k_dft_axis_slab<1><<<blocks, threads, sm, f->stream>>>(in, out, E, Nin, Mout, inner, IC);
+  else if (need <= 2)
+    k_dft_axis_slab<2><<<blocks, threads, sm, f->stream>>>(in, out, E, Nin, Mout, inner, IC);
+  else if (need <= 4)
+    k_dft_axis_slab<4><<<blocks, threads, sm, f->stream>>>(in, out, E, Nin, Mout, inner, IC);
+  else if (need <= 8)
+    k_dft_axis_slab<8><<<blocks, threads, sm, f->stream>>>(in, out, E, Nin, Mout, inner, IC);
+  else if (need <= 16)
+    k_dft_axis_slab<16><<<blocks, threads, sm, f->stream>>>(in, out, E, Nin, Mout, inner, IC);
+  else
+    k_dft_axis<<<grid_for((long long)outer * Mout * inner), kT, sizeof(float2) * Mout * Nin,
+                 f->stream>>>(in, out, E, outer, Nin, Mout, inner);
 }
 
 // Forward through the spectral part of layer l: S (in zbuf) = Finv(W F h).
@@ -1012,10 +1008,12 @@ int deft_fno_create(int device, int N, int channels, int modes, int layers, unsi
   {
     const int ax = (int)(sizeof(float2) * 2 * modes * N);
     cudaFuncSetAttribute(k_dft_axis, cudaFuncAttributeMaxDynamicSharedMemorySize, ax);
-    cudaFuncSetAttribute(k_dft_axis_tile<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, ax);
-    cudaFuncSetAttribute(k_dft_axis_tile<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, ax);
-    cudaFuncSetAttribute(k_dft_axis_tile<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, ax);
-    cudaFuncSetAttribute(k_dft_axis_tile<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, ax);
+    const int slab = (int)(sizeof(float2) * N * 32);
+    cudaFuncSetAttribute(k_dft_axis_slab<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, slab);
+    cudaFuncSetAttribute(k_dft_axis_slab<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, slab);
+    cudaFuncSetAttribute(k_dft_axis_slab<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, slab);
+    cudaFuncSetAttribute(k_dft_axis_slab<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, slab);
+    cudaFuncSetAttribute(k_dft_axis_slab<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, slab);
   }
   k_to_bf16<<<grid_for((long long)off), kT, 0, f->stream>>>(f->p, f->pb, (long long)off);
   if (check(f, "fno create")) {
