@@ -211,53 +211,6 @@ __global__ void k_dft_axis(const float2 *__restrict__ in, float2 *__restrict__ o
   }
 }
 
-// The same contraction by slabs: a block takes one o and IC consecutive i,
-// stages in[o][0..Nin)[i0..i0+IC) in shared memory (one coalesced read of
-// the input), and thread (il = t mod IC, mg = t / IC) computes the outputs
-// m = mg, mg + G, ... (G = blockDim / IC, at most MT of them) from it; the
-// table E is read through the read-only cache.
-template <int MT>
-__global__ void k_dft_axis_slab(const float2 *__restrict__ in, float2 *__restrict__ out,
-                                const float2 *__restrict__ E, int Nin, int Mout, int inner,
-                                int IC) {
-  extern __shared__ float sm[];
-  float2 *slab = reinterpret_cast<float2 *>(sm);  // [Nin][IC]
-  const int chunks = (inner + IC - 1) / IC;
-  const int o = blockIdx.x / chunks;
-  const int i0 = (blockIdx.x - o * chunks) * IC;
-  const int ic = inner - i0 < IC ? inner - i0 : IC;
-  const float2 *src = in + (size_t)o * Nin * inner + i0;
-  for (int k = threadIdx.x; k < Nin * IC; k += blockDim.x) {
-    const int n = k / IC, il = k - n * IC;
-    slab[k] = il < ic ? src[(size_t)n * inner + il] : make_float2(0.f, 0.f);
-  }
-  __syncthreads();
-  const int G = blockDim.x / IC;
-  const int il = threadIdx.x % IC, mg = threadIdx.x / IC;
-  if (mg >= G || il >= ic) return;
-  float re[MT], im[MT];
-#pragma unroll
-  for (int u = 0; u < MT; u++) re[u] = im[u] = 0.f;
-  for (int n = 0; n < Nin; n++) {
-    const float2 a = slab[n * IC + il];
-#pragma unroll
-    for (int u = 0; u < MT; u++) {
-      const int m = mg + u * G;
-      if (m < Mout) {
-        const float2 b = __ldg(&E[(size_t)m * Nin + n]);
-        re[u] += a.x * b.x - a.y * b.y;
-        im[u] += a.x * b.y + a.y * b.x;
-      }
-    }
-  }
-  float2 *dst = out + (size_t)o * Mout * inner + i0 + il;
-#pragma unroll
-  for (int u = 0; u < MT; u++) {
-    const int m = mg + u * G;
-    if (m < Mout) dst[(size_t)m * inner] = make_float2(re[u], im[u]);
-  }
-}
-
 // Spectral mixing U[o][k] = sum_i W[i][o][k] V[i][k]  (W bf16 complex).
 __global__ void k_spec_mix(const float2 *__restrict__ V, const __nv_bfloat16 *__restrict__ W,
                            float2 *__restrict__ U, int C, int K) {
@@ -769,30 +722,11 @@ void launch_z_inv(deft_fno *f, const float2 *in, float *out, const float2 *G, in
     default: k_dft_z_inv<16><<<grid, 128, 0, f->stream>>>(in, out, G, L, f->N, f->Kz, acc); break;
   }
 }
-// Slab kernel: IC = inner (at most 32) i per block, else 32; 256 threads
-// minus the remainder; MT = outputs per thread, rounded up to 1, 2, 4, 8 or
-// 16.  Nin x IC complex values of shared memory (32 KB at Nin = 128).
 void launch_axis(deft_fno *f, const float2 *in, float2 *out, const float2 *E, int outer, int Nin,
                  int Mout, int inner) {
-  const int IC = inner <= 32 ? inner : 32;
-  const int G = 256 / IC;
-  const int threads = G * IC;
-  const int need = (Mout + G - 1) / G;
-  const int blocks = outer * ((inner + IC - 1) / IC);
-  const size_t sm = sizeof(float2) * (size_t)Nin * IC;
-  if (need <= 1)
-    k_dft_axis_slab<1><<<blocks, threads, sm, f->stream>>>(in, out, E, Nin, Mout, inner, IC);
-  else if (need <= 2)
-    k_dft_axis_slab<2><<<blocks, threads, sm, f->stream>>>(in, out, E, Nin, Mout, inner, IC);
-  else if (need <= 4)
-    k_dft_axis_slab<4><<<blocks, threads, sm, f->stream>>>(in, out, E, Nin, Mout, inner, IC);
-  else if (need <= 8)
-    k_dft_axis_slab<8><<<blocks, threads, sm, f->stream>>>(in, out, E, Nin, Mout, inner, IC);
-  else if (need <= 16)
-    k_dft_axis_slab<16><<<blocks, threads, sm, f->stream>>>(in, out, E, Nin, Mout, inner, IC);
-  else
-    k_dft_axis<<<grid_for((long long)outer * Mout * inner), kT, sizeof(float2) * Mout * Nin,
-                 f->stream>>>(in, out, E, outer, Nin, Mout, inner);
+  const long long total = (long long)outer * Mout * inner;
+  k_dft_axis<<<grid_for(total), kT, sizeof(float2) * Mout * Nin, f->stream>>>(in, out, E, outer,
+                                                                              Nin, Mout, inner);
 }
 
 // Forward through the spectral part of layer l: S (in zbuf) = Finv(W F h).
@@ -1005,16 +939,8 @@ int deft_fno_create(int device, int N, int channels, int modes, int layers, unsi
   cudaFuncSetAttribute(k_dft_z_fwd<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)zf);
   cudaFuncSetAttribute(k_dft_z_fwd<12>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)zf);
   cudaFuncSetAttribute(k_dft_z_fwd<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)zf);
-  {
-    const int ax = (int)(sizeof(float2) * 2 * modes * N);
-    cudaFuncSetAttribute(k_dft_axis, cudaFuncAttributeMaxDynamicSharedMemorySize, ax);
-    const int slab = (int)(sizeof(float2) * N * 32);
-    cudaFuncSetAttribute(k_dft_axis_slab<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, slab);
-    cudaFuncSetAttribute(k_dft_axis_slab<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, slab);
-    cudaFuncSetAttribute(k_dft_axis_slab<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, slab);
-    cudaFuncSetAttribute(k_dft_axis_slab<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, slab);
-    cudaFuncSetAttribute(k_dft_axis_slab<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, slab);
-  }
+  cudaFuncSetAttribute(k_dft_axis, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)(sizeof(float2) * 2 * modes * N));
   k_to_bf16<<<grid_for((long long)off), kT, 0, f->stream>>>(f->p, f->pb, (long long)off);
   if (check(f, "fno create")) {
     deft_fno_destroy(f);
