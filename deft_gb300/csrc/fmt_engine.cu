@@ -1535,11 +1535,17 @@ __global__ void k_reduce_terms_mb(const double *partials, int nblk, double dV, d
     last = atomicAdd(counter, 1u) == gridDim.x - 1;
   }
   __syncthreads();
-  if (!last || threadIdx.x) return;
+  if (!last) return;
   __threadfence();
+  // the block sums, loaded in parallel, added in block order by thread 0
+  __shared__ double l1[kReduceBlocks * 9];
+  for (int k = threadIdx.x; k < (int)gridDim.x * 9; k += blockDim.x)
+    l1[k] = ((volatile double *)level1)[k];
+  __syncthreads();
+  if (threadIdx.x) return;
   double s[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
   for (int b = 0; b < (int)gridDim.x; b++)
-    for (int t = 0; t < 9; t++) s[t] += ((volatile double *)level1)[(size_t)b * 9 + t];
+    for (int t = 0; t < 9; t++) s[t] += l1[b * 9 + t];
   double E = 0;
   for (int t = 0; t < kNumTerms; t++) {
     out[t] = s[t] * dV;
