@@ -1508,54 +1508,6 @@ __global__ void k_reduce_terms(const double *partials, int nblk, double dV, doub
   }
 }
 
-// The same sums over kReduceBlocks blocks: block b adds a contiguous run of
-// the per-block partials (energy terms and gradient dots), the last block to
-// finish adds the kReduceBlocks runs in order (deterministic, one launch, no
-// block serialises over thousands of partials).
-constexpr int kReduceBlocks = 16;
-__global__ void k_reduce_terms_mb(const double *partials, int nblk, double dV, double *out,
-                                  const double *dpart, int dk, int dblk, double *level1,
-                                  unsigned int *counter) {
-  __shared__ double red[32 * 9];
-  __shared__ bool last;
-  double acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-  const int ce = (nblk + gridDim.x - 1) / gridDim.x, cd = (dblk + gridDim.x - 1) / gridDim.x;
-  const int e0 = blockIdx.x * ce, e1 = min(nblk, e0 + ce);
-  for (int b = e0 + threadIdx.x; b < e1; b += blockDim.x)
-    for (int t = 0; t < kNumTerms; t++) acc[t] += partials[(size_t)b * kNumTerms + t];
-  if (dk > 0) {
-    const int d0 = blockIdx.x * cd, d1 = min(dblk, d0 + cd);
-    for (int b = d0 + threadIdx.x; b < d1; b += blockDim.x)
-      for (int t = 0; t < 3; t++) acc[6 + t] += dpart[(size_t)b * 3 + t];
-  }
-  block_reduce<9>(acc, red);
-  if (threadIdx.x == 0) {
-    for (int t = 0; t < 9; t++) level1[(size_t)blockIdx.x * 9 + t] = acc[t];
-    __threadfence();
-    last = atomicAdd(counter, 1u) == gridDim.x - 1;
-  }
-  __syncthreads();
-  if (!last) return;
-  __threadfence();
-  // the block sums, loaded in parallel, added in block order by thread 0
-  __shared__ double l1[kReduceBlocks * 9];
-  for (int k = threadIdx.x; k < (int)gridDim.x * 9; k += blockDim.x)
-    l1[k] = ((volatile double *)level1)[k];
-  __syncthreads();
-  if (threadIdx.x) return;
-  double s[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-  for (int b = 0; b < (int)gridDim.x; b++)
-    for (int t = 0; t < 9; t++) s[t] += l1[b * 9 + t];
-  double E = 0;
-  for (int t = 0; t < kNumTerms; t++) {
-    out[t] = s[t] * dV;
-    E += out[t];
-  }
-  out[kNumTerms] = E;
-  for (int t = 0; t < dk; t++) out[8 + t] = s[6 + t];
-  *counter = 0;
-}
-
 // Up to three dot products in one pass; the last block to finish reduces the
 // per-block partials in a fixed order (deterministic).
 __global__ void k_dots(int k, const double *a0, const double *b0, const double *a1,
@@ -2021,8 +1973,6 @@ class EngineImpl {
   double *dot_partials = nullptr;
   double *grad_partials = nullptr;  // k_z_grad's dot-product block sums
   unsigned int *dot_counter = nullptr;
-  double *red_level1 = nullptr;        // k_reduce_terms_mb's per-block sums
-  unsigned int *red_counter = nullptr;
   int dot_blocks = 0;
   Tiles t64, t32;  // launch shapes of the FP64 and the FP32 kernels
   template <typename T> const Tiles &tl() const { return sizeof(T) == 4 ? t32 : t64; }
@@ -2065,8 +2015,6 @@ class EngineImpl {
     cudaFree(dot_partials);
     cudaFree(grad_partials);
     cudaFree(dot_counter);
-    cudaFree(red_level1);
-    cudaFree(red_counter);
     cudaFreeHost(results_host);
   }
 
@@ -2303,14 +2251,10 @@ class EngineImpl {
     if (dot_blocks < 1) dot_blocks = 1;
     if (alloc(&dot_partials, sizeof(double) * 3 * dot_blocks) || alloc(&dot_counter, sizeof(unsigned)))
       return -1;
-    if (alloc(&red_level1, sizeof(double) * 9 * kReduceBlocks) ||
-        alloc(&red_counter, sizeof(unsigned)))
-      return -1;
     // one slot triple per gradient block at any pair-tile width
     if (alloc(&grad_partials, sizeof(double) * 3 * (size_t)(pairs > 0 ? pairs : 1))) return -1;
 
     e = cudaMemset(dot_counter, 0, sizeof(unsigned));
-    if (e == cudaSuccess) e = cudaMemset(red_counter, 0, sizeof(unsigned));
     if (e != cudaSuccess) return fail("cudaMemset", e);
     return check("engine init");
   }
@@ -2678,9 +2622,9 @@ class EngineImpl {
   // With gd, also the gradient dot products k_z_grad took (results[8..11)).
   void queue_energy(int nblk, const GradDots *gd = nullptr, int gblk = 0) {
     pre(kK_reduce_terms);
-    k_reduce_terms_mb<<<kReduceBlocks, kReduceThreads, 0, stream>>>(
-        partials, nblk, g.dV, results, gd ? gd->partials : nullptr, gd ? gd->k : 0, gblk,
-        red_level1, red_counter);
+    k_reduce_terms<<<1, kReduceThreads, 0, stream>>>(partials, nblk, g.dV, results,
+                                                      gd ? gd->partials : nullptr,
+                                                      gd ? gd->k : 0, gblk);
     post(kK_reduce_terms);
     if (!dev_only)
       cudaMemcpyAsync(results_host, results, sizeof(double) * (gd ? 11 : 8),
