@@ -238,10 +238,19 @@ def roofline(prof, N, fp32, peak, peak_kind):
                 traffic = json.load(fh).get(f"{'fp32' if fp32 else 'fp64'}_{N}_{dom}")
         except Exception:
             traffic = None
+    # every kernel of the evaluation and the Hessian-vector product with its
+    # algorithmic bytes per launch against its mean event time
+    by_kernel = {}
+    for k, (nl, ms) in sorted(prof.items(), key=lambda kv: -kv[1][1]):
+        if k in ab and nl:
+            us = 1e3 * ms / nl
+            gbs = ab[k] / (us * 1e-6) / 1e9
+            by_kernel[k] = {"us_per_launch": round(us, 2), "alg_MB": round(ab[k] / 1e6, 1),
+                            "GB_s": round(gbs, 1), "frac": round(gbs / peak, 3)}
     return {
         "bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
         "frac": achieved / peak, "traffic": traffic, "alg_bytes_per_launch": ab[dom],
-        "avg_launch_ms": dom_ms,
+        "avg_launch_ms": dom_ms, "by_kernel": by_kernel,
         "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
         else "fallback 6.8 TB/s",
         "conv_hbm_gbs": conv_gbs, "conv_frac": conv_gbs / peak if conv_gbs else None,
