@@ -1101,6 +1101,10 @@ __global__ void DEFT_FFT_BOUNDS(RN) k_z_hvp_out(
 // transforms).
 
 constexpr int kZWarps = 8;
+// Resident blocks asked of the five-field warp kernels (0: ptxas's choice).
+#ifndef DEFT_ZWARP5_MIN_BLOCKS
+#define DEFT_ZWARP5_MIN_BLOCKS 0
+#endif
 // One staging buffer per warp (one-field kernels) or five (the five-field
 // kernels stage all fields before transforming, so their loads overlap).
 template <int E> constexpr size_t zwarp_smem(int nf = 1) {
@@ -1287,7 +1291,7 @@ __global__ void __launch_bounds__(32 * kZWarps)
 // and the local energy terms at its 2N points, per-block energies, and
 // (GRAD) r2c of the five partials dV kT dphi/dn_a in place.
 template <bool GRAD, int E>
-__global__ void __launch_bounds__(32 * kZWarps)
+__global__ void __launch_bounds__(32 * kZWarps, DEFT_ZWARP5_MIN_BLOCKS)
     k_z_phi_warp(float2 *S5, const double *__restrict__ n, const double *__restrict__ V, Geom g,
                  const float2 *__restrict__ tw, const LocalArgs *__restrict__ lap,
                  double *partials) {
@@ -1346,7 +1350,7 @@ __global__ void __launch_bounds__(32 * kZWarps)
 // Warp form of k_z_jac: c2r of the five weighted perturbations, dP = dV kT
 // J dw with the stored Hessian blocks, r2c of dP in place.
 template <int E>
-__global__ void __launch_bounds__(32 * kZWarps)
+__global__ void __launch_bounds__(32 * kZWarps, DEFT_ZWARP5_MIN_BLOCKS)
     k_z_jac_warp(float2 *S5, Geom g, const float2 *__restrict__ tw,
                  const LocalArgs *__restrict__ lap, const float *__restrict__ hess) {
   constexpr int N = 32 * E;
@@ -1392,7 +1396,7 @@ __global__ void __launch_bounds__(32 * kZWarps)
 // Warp form of k_z_hess: c2r of the five weighted densities, the packed
 // Hessian blocks of phi and the ideal-gas curvature kT/n in FP32.
 template <int E>
-__global__ void __launch_bounds__(32 * kZWarps)
+__global__ void __launch_bounds__(32 * kZWarps, DEFT_ZWARP5_MIN_BLOCKS)
     k_z_hess_warp(const float2 *__restrict__ S5, const double *__restrict__ n, Geom g,
                   const float2 *__restrict__ tw, const LocalArgs *__restrict__ lap,
                   float *__restrict__ hess, float *__restrict__ hloc) {
