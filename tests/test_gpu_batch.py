@@ -36,12 +36,13 @@ def test_batch_matches_individual_solves(precision):
 
 def test_device_batch_matches_individual_solves():
     """deft_batch_solve_device: the whole batch as one graph launch of
-    device-driven solves (mixed form, density preconditioner); every
-    problem converges and matches its own host-driven solve to 1e-8."""
+    device-driven solves (mixed form, density preconditioner) over the
+    sweep's grid mix, 32^3 to 128^3; every problem converges and matches its
+    own host-driven solve to 1e-8."""
     from deft_gb300 import _lib
     from deft_gb300.workloads import batch_sweep
     from tests.capi import CG, Ctx, Fmt, Grid, batch_solve
-    probs = batch_sweep(count=6, seed=7, sizes=(32, 48, 64))
+    probs = batch_sweep(count=6, seed=7, sizes=(32, 48, 64, 96, 128))
     code, st, outs = batch_solve(probs, precision=1, gtol=5e-10, device_driven=True)
     assert code == 0, _lib.load().deft_last_error()
     ctx = Ctx(0)
