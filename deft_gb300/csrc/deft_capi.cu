@@ -14,9 +14,11 @@
 #include <chrono>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <type_traits>
 #include <utility>
 #include <vector>
 
@@ -52,6 +54,7 @@ struct deft_fmt {
   // last_energy, src/Functional.h:223): the six fused terms, then the SAFT
   // association and dispersion terms
   double last_terms[deft::kNumTerms + 2] = {0, 0, 0, 0, 0, 0, 0, 0};
+  unsigned fields_version = 0;  // bumped when V or the mask is set
 };
 
 struct deft_cg {
@@ -91,6 +94,13 @@ struct deft_cg {
   int dkey_terms = -1, dkey_hs = -1, dkey_prec = -1;
   double dkey_kT = 0;
   const double *dkey_V = nullptr, *dkey_mask = nullptr, *dkey_pg = nullptr;
+  // FP32 copies of the vectors for the mixed form's FP32 stage (f32_stage):
+  // while f32_live they hold the state and the FP64 vectors but x are
+  // stale; x is brought up to date after every step
+  float *x32 = nullptr, *g32 = nullptr, *d32 = nullptr, *gold32 = nullptr, *pg32 = nullptr;
+  float *V32 = nullptr, *mask32 = nullptr;
+  bool f32_live = false;
+  unsigned f32_fields = ~0u;  // the functional's fields_version V32, mask32 were made from
 };
 
 namespace {
@@ -488,11 +498,13 @@ int deft_fmt_set_params(deft_fmt *f, const deft_fmt_params *p) {
 
 int deft_fmt_set_vext(deft_fmt *f, const double *V, int on_device) {
   if (!f) return set_err(DEFT_ERR_ARG, "fmt is NULL");
+  f->fields_version++;
   return set_field(f, &f->V, V, on_device);
 }
 
 int deft_fmt_set_mask(deft_fmt *f, const double *mask, int on_device) {
   if (!f) return set_err(DEFT_ERR_ARG, "fmt is NULL");
+  f->fields_version++;
   return set_field(f, &f->mask, mask, on_device);
 }
 
@@ -926,6 +938,7 @@ int deft_cg_destroy(deft_cg *c) {
   cudaFree(c->pg);
   cudaFree(c->q);
   cudaFree(c->dxv);
+  for (float *v : {c->x32, c->g32, c->d32, c->gold32, c->pg32, c->V32, c->mask32}) cudaFree(v);
   if (c->log) fclose(c->log);
   deft::dcg_free(c->dgraph);
   delete c;
@@ -966,6 +979,7 @@ static void cg_reset(deft_cg *c) {
   c->nm_step = 0.1;  // the new API's Minimize() constructor state
   c->nm_oldgradsqr = 1.0;
   c->nm_deltaE = c->nm_dEdn = c->nm_log_avg = c->nm_err = 0;
+  c->f32_live = false;
   const size_t bytes = sizeof(double) * nr(c->f->grid);
   cudaMemsetAsync(c->d, 0, bytes, c->f->grid->ctx->stream);
   cudaMemsetAsync(c->gold, 0, bytes, c->f->grid->ctx->stream);
@@ -1083,23 +1097,167 @@ bool fast_stage(const deft_cg *c, const deft::FmtSpec &spec) {
   return spec.precision != deft::kPrecisionFP64 && c->p.preconditioned == DEFT_PC_DENSITY;
 }
 
+// (C++ linkage: overloads and templates inside the C API's block)
+extern "C++" {
+
+// The secant CG's vectors in their storage type: FP64, or the FP32 copies
+// the mixed form's FP32 stage runs on (f32_stage).
+template <typename V> struct CgVec;
+template <> struct CgVec<double> {
+  static double *&x(deft_cg *c) { return c->x; }
+  static double *&g(deft_cg *c) { return c->g; }
+  static double *&d(deft_cg *c) { return c->d; }
+  static double *&gold(deft_cg *c) { return c->gold; }
+  static double *&pg(deft_cg *c) { return c->pg; }
+};
+template <> struct CgVec<float> {
+  static float *&x(deft_cg *c) { return c->x32; }
+  static float *&g(deft_cg *c) { return c->g32; }
+  static float *&d(deft_cg *c) { return c->d32; }
+  static float *&gold(deft_cg *c) { return c->gold32; }
+  static float *&pg(deft_cg *c) { return c->pg32; }
+};
+
+// g = grad F(x), E, and the products g.b[i] (k <= 3) in one launch sequence.
+int cg_eval_gdots(deft_cg *c, const deft::FmtSpec &spec, int k, const double *const *b,
+                  double *out) {
+  const double *a[3] = {c->g, c->g, c->g};
+  return cg_eval_dots(c, spec, k, a, b, out);
+}
+int cg_eval_gdots(deft_cg *c, const deft::FmtSpec &spec, int k, const float *const *b,
+                  double *out) {
+  Engine *e = eng_of(c);
+  double E;
+  if (e->eval32(spec, c->x32, c->f->V ? c->V32 : nullptr, c->f->mask ? c->mask32 : nullptr,
+                c->g32, &E, c->f->last_terms, k, b, out))
+    return eng_err(e);
+  c->evals++;
+  c->last_eval_mixed = true;
+  c->E = E;
+  c->e_cache = E;
+  c->e_valid = true;
+  c->have_g = true;
+  return DEFT_OK;
+}
+
+int cg_axpy(deft_cg *c, double a, const float *v) {
+  if (eng_of(c)->axpy32(a, v, c->x32)) return eng_err(eng_of(c));
+  c->e_valid = false;
+  c->have_g = false;
+  return DEFT_OK;
+}
+
+int v_scal_add(Engine *e, double beta, double *d, double alpha, const double *g) {
+  return e->scal_add(beta, d, alpha, g);
+}
+int v_scal_add(Engine *e, double beta, float *d, double alpha, const float *g) {
+  return e->scal_add32(beta, d, alpha, g);
+}
+int v_scal_add_dot(Engine *e, double beta, double *d, double alpha, const double *g,
+                   const double *h, double *out) {
+  return e->scal_add_dot(beta, d, alpha, g, h, out);
+}
+int v_scal_add_dot(Engine *e, double beta, float *d, double alpha, const float *g,
+                   const float *h, double *out) {
+  return e->scal_add_dot32(beta, d, alpha, g, h, out);
+}
+int v_copy(Engine *e, const double *src, double *dst) { return e->copy(src, dst); }
+int v_copy(Engine *e, const float *src, float *dst) { return e->copy32(src, dst); }
+
+// pg = M^-1 g (M^-1 = n / (kT dV) on the active points) with pg.g, pg.g_old.
+int cg_precond_dots(deft_cg *c, const deft::FmtSpec &spec, const double *, double *o) {
+  return eng_of(c)->precond_dots(spec, c->x, c->g, active_mask(c->f), c->pg, c->gold, o)
+             ? eng_err(eng_of(c))
+             : DEFT_OK;
+}
+int cg_precond_dots(deft_cg *c, const deft::FmtSpec &spec, const float *, double *o) {
+  const float *mask = active_mask(c->f) ? c->mask32 : nullptr;
+  return eng_of(c)->precond_dots32(spec, c->x32, c->g32, mask, c->pg32, c->gold32, o)
+             ? eng_err(eng_of(c))
+             : DEFT_OK;
+}
+
+#ifndef DEFT_F32_VECTORS
+#define DEFT_F32_VECTORS 1
+#endif
+
+// Whether the FP32 stage of the mixed form keeps its vectors in FP32: the
+// secant CG with the density preconditioner on the plain White Bear kinds
+// (no effective-potential variable, tensor or SAFT terms) where the
+// engine's FP32 gradient kernels take FP32 vectors.  FP32 vectors halve the
+// vector traffic and spare the gradient kernels the FP64 conversions (the
+// FP64 pipe runs at 1/64 of the FP32 rate on sm_103a); the stage's
+// iterates are FP32-evaluated anyway and x only has to reach the switch to
+// the FP64 Newton refinement.  DEFT_F32_VECTORS=0 in the environment keeps
+// FP64 vectors.
+bool f32_stage(deft_cg *c, const deft::FmtSpec &spec) {
+  static const bool on = [] {
+    const char *ev = getenv("DEFT_F32_VECTORS");
+    return ev ? atoi(ev) != 0 : DEFT_F32_VECTORS != 0;
+  }();
+  return on && spec.precision == deft::kPrecisionMixed && c->pg &&
+         c->p.preconditioned == DEFT_PC_DENSITY && !(c->f->p.terms & DEFT_TERM_VEFF) &&
+         !is_tensor(c->f) && !has_saft(c->f) && eng_of(c)->f32_vectors_ok(spec);
+}
+
+// Makes the FP32 vectors current: allocates them, converts V and the mask
+// when they changed, and the state vectors when the FP64 ones hold it.
+int f32_enter(deft_cg *c) {
+  Engine *e = eng_of(c);
+  const size_t n = nr(c->f->grid);
+  if (!c->x32) {
+    for (float **v : {&c->x32, &c->g32, &c->d32, &c->gold32, &c->pg32, &c->V32, &c->mask32}) {
+      cudaError_t ce = cudaMalloc((void **)v, sizeof(float) * n);
+      if (ce != cudaSuccess) {
+        *v = nullptr;
+        return cuda_err(ce, "cudaMalloc");
+      }
+    }
+  }
+  if (c->f32_fields != c->f->fields_version) {
+    if ((c->f->V && e->to_f32(c->f->V, c->V32)) || (c->f->mask && e->to_f32(c->f->mask, c->mask32)))
+      return eng_err(e);
+    c->f32_fields = c->f->fields_version;
+  }
+  if (!c->f32_live) {
+    if (e->to_f32(c->x, c->x32) || e->to_f32(c->g, c->g32) || e->to_f32(c->d, c->d32) ||
+        e->to_f32(c->gold, c->gold32) || e->to_f32(c->pg, c->pg32))
+      return eng_err(e);
+    c->f32_live = true;
+  }
+  return DEFT_OK;
+}
+
+// Hands the state back to the FP64 vectors (exact: FP32 -> FP64 -> FP32
+// round-trips).
+int f32_leave(deft_cg *c) {
+  if (!c->f32_live) return DEFT_OK;
+  Engine *e = eng_of(c);
+  if (e->to_f64(c->x32, c->x) || e->to_f64(c->g32, c->g) || e->to_f64(c->d32, c->d) ||
+      e->to_f64(c->gold32, c->gold) || e->to_f64(c->pg32, c->pg))
+    return eng_err(e);
+  c->f32_live = false;
+  return DEFT_OK;
+}
+
 // Bracketing secant search on s(a) = grad(x + a d).d from s(0) = s0 < 0,
 // accepting |s| <= c2 |s0| (c2 = 0.1 but in fast_stage) with no energy rise
 // beyond rounding.  Leaves x, g, E, gg, ggold at the accepted point.
+template <typename V>
 int secant_search(deft_cg *c, const deft::FmtSpec &spec, double E0, double s0) {
+  using CV = CgVec<V>;
   const double c2 = fast_stage(c, spec) ? DEFT_SECANT_C2_MIXED : 0.1;
   double lo = 0, s_lo = s0, hi = -1, s_hi = 0, plo = 0, s_plo = s0;
   double a = c->alpha, at = 0;
   // energies only guard against rises; FP32 sums carry ~1e-7 relative noise
   const double etol = (spec.precision == deft::kPrecisionFP64 ? 1e-12 : 1e-6) * std::fabs(E0);
   for (int it = 0; it < 40; it++) {
-    if (int st = cg_axpy(c, a - at, c->d)) return st;
+    if (int st = cg_axpy(c, a - at, CV::d(c))) return st;
     at = a;
     double o[3];
     {
-      const double *da[3] = {c->g, c->g, c->g};
-      const double *db[3] = {c->d, c->g, c->gold};
-      if (int st = cg_eval_dots(c, spec, 3, da, db, o)) return st;
+      const V *db[3] = {CV::d(c), CV::g(c), CV::gold(c)};
+      if (int st = cg_eval_gdots(c, spec, 3, db, o)) return st;
     }
     const double s = o[0], gg = o[1], ggold = o[2];
     const double E = c->E;
@@ -1143,16 +1301,17 @@ int secant_search(deft_cg *c, const deft::FmtSpec &spec, double E0, double s0) {
     a = an;
   }
   // return to the start point
-  cg_axpy(c, -at, c->d);
+  cg_axpy(c, -at, CV::d(c));
   return set_err(DEFT_ERR_LINESEARCH, "secant line search did not converge in 40 evaluations");
 }
 
+template <typename V>
 int step_secant(deft_cg *c, deft_cg_status *st, const deft::FmtSpec &spec, double gtol) {
+  using CV = CgVec<V>;
   if (!c->have_g) {
-    const double *a[2] = {c->g, c->g};
-    const double *b[2] = {c->g, c->gold};
+    const V *b[2] = {CV::g(c), CV::gold(c)};
     double o[2];
-    if (int s = cg_eval_dots(c, spec, 2, a, b, o)) return s;
+    if (int s = cg_eval_gdots(c, spec, 2, b, o)) return s;
     c->gg = o[0];
     c->ggold = o[1];
   }
@@ -1165,19 +1324,21 @@ int step_secant(deft_cg *c, deft_cg_status *st, const deft::FmtSpec &spec, doubl
     return DEFT_OK;
   }
   Engine *e = eng_of(c);
+  V *pgv = CV::pg(c);
   double beta = 0, pgg = 0;
-  if (c->pg) {
+  if (pgv) {
     // Preconditioned Polak-Ribiere (src/ConjugateGradient.cpp:115-160):
     // beta = pg.(g - g_old) / (pg_old.g_old), d = -pg + beta d
     double o[2];
     if (c->p.preconditioned == DEFT_PC_DENSITY) {
       // pg = M^-1 g, M^-1 = n / (kT dV), formed with its two dot products
-      if (e->precond_dots(spec, c->x, c->g, active_mask(c->f), c->pg, c->gold, o))
-        return eng_err(e);
-    } else {
+      if (int s = cg_precond_dots(c, spec, pgv, o)) return s;
+    } else if constexpr (std::is_same_v<V, double>) {
       const double *a[2] = {c->pg, c->pg};
       const double *b[2] = {c->g, c->gold};
       if (e->dots(2, a, b, o)) return eng_err(e);
+    } else {
+      return set_err(DEFT_ERR_ARG, "FP32 vectors need the density preconditioner");
     }
     pgg = o[0];
     if (c->pgoldsqr != 0) {
@@ -1197,25 +1358,26 @@ int step_secant(deft_cg *c, deft_cg_status *st, const deft::FmtSpec &spec, doubl
   double s0;
   const bool known = c->slope_ok && c->have_g && c->s_acc_evals == c->evals;
   c->slope_ok = false;
+  V *dv = CV::d(c);
   if (known || beta == 0) {
-    if (e->scal_add(beta, c->d, -1.0, c->pg ? c->pg : c->g)) return eng_err(e);
-    s0 = -(c->pg ? pgg : c->gg) + (beta != 0 ? beta * c->s_acc : 0.0);
-  } else if (e->scal_add_dot(beta, c->d, -1.0, c->pg ? c->pg : c->g, c->g, &s0)) {
+    if (v_scal_add(e, beta, dv, -1.0, pgv ? pgv : CV::g(c))) return eng_err(e);
+    s0 = -(pgv ? pgg : c->gg) + (beta != 0 ? beta * c->s_acc : 0.0);
+  } else if (v_scal_add_dot(e, beta, dv, -1.0, pgv ? pgv : CV::g(c), CV::g(c), &s0)) {
     return eng_err(e);
   }
-  if (!(s0 < 0) && c->pg && beta != 0) {
+  if (!(s0 < 0) && pgv && beta != 0) {
     // not downhill: the preconditioned steepest direction
-    if (e->scal_add(0.0, c->d, -1.0, c->pg)) return eng_err(e);
+    if (v_scal_add(e, 0.0, dv, -1.0, pgv)) return eng_err(e);
     beta = 0;
     s0 = -pgg;
   }
   if (!(s0 < 0)) {
-    if (e->scal_add(0.0, c->d, -1.0, c->g)) return eng_err(e);
+    if (v_scal_add(e, 0.0, dv, -1.0, CV::g(c))) return eng_err(e);
     s0 = -c->gg;
   }
   c->pgoldsqr = pgg;
   // g_old = g by exchanging the buffers: the next evaluation writes g
-  std::swap(c->g, c->gold);
+  std::swap(CV::g(c), CV::gold(c));
   c->goldsqr = c->gg;
   // First trial step: the last accepted step rescaled by the slope ratio
   // (equal first-order decrease), except in the FP32 stage of the mixed form
@@ -1229,23 +1391,38 @@ int step_secant(deft_cg *c, deft_cg_status *st, const deft::FmtSpec &spec, doubl
   c->s_prev = s0;
   c->iter++;
   const double E0 = c->E;
-  int ls = secant_search(c, spec, E0, s0);
+  int ls = secant_search<V>(c, spec, E0, s0);
   if (ls == DEFT_ERR_LINESEARCH && beta != 0) {
     // The search failed along the conjugate direction (x is back at the
     // start point, whose gradient is in gold): retry once along steepest
     // descent, which cannot drive a vanishing density negative.
-    if (e->copy(c->gold, c->g)) return eng_err(e);
+    if (v_copy(e, CV::gold(c), CV::g(c))) return eng_err(e);
     c->E = E0;
-    if (e->scal_add(0.0, c->d, -1.0, c->g)) return eng_err(e);
+    if (v_scal_add(e, 0.0, dv, -1.0, CV::g(c))) return eng_err(e);
     s0 = -c->goldsqr;
     c->s_prev = s0;
-    ls = secant_search(c, spec, E0, s0);
+    ls = secant_search<V>(c, spec, E0, s0);
   }
   if (ls) return ls;
   st->gnorm = std::sqrt(c->gg);
   if (st->gnorm < gtol) c->done = true;
   return DEFT_OK;
 }
+
+// The FP32 stage's step: on FP32 vectors where f32_stage allows, with x
+// brought back to FP64 after the step.
+int step_stage0(deft_cg *c, deft_cg_status *st, const deft::FmtSpec &spec, double gtol) {
+  if (!f32_stage(c, spec)) {
+    if (int s = f32_leave(c)) return s;
+    return step_secant<double>(c, st, spec, gtol);
+  }
+  if (int s = f32_enter(c)) return s;
+  const int status = step_secant<float>(c, st, spec, gtol);
+  if (eng_of(c)->to_f64(c->x32, c->x)) return eng_err(eng_of(c));
+  return status;
+}
+
+}  // extern "C++"
 
 // One Newton refinement step of the mixed form.  The residual is the FP64
 // gradient g; the step solves H dx = -g by linear CG whose Hessian-vector
@@ -1643,9 +1820,10 @@ int deft_cg_step(deft_cg *c, deft_cg_status *st) {
           const double thr = std::fmax(
               c->p.refine_abs > 0 ? c->p.refine_abs : (c->g0norm > 0 ? rel * c->g0norm : 0.0),
               c->p.gtol);
-          status = step_secant(c, st, spec, thr);
+          status = step_stage0(c, st, spec, thr);
           if (status == DEFT_ERR_LINESEARCH) status = DEFT_OK;
           if (!status && (c->done || st->gnorm < thr || c->iter > 0 && !c->have_g)) {
+            status = f32_leave(c);
             c->stage = 1;
             c->done = false;
             if ((c->f->p.terms & DEFT_TERM_VEFF) || has_saft(c->f) || is_tensor(c->f)) {
@@ -1659,13 +1837,13 @@ int deft_cg_step(deft_cg *c, deft_cg_status *st) {
         } else if ((c->f->p.terms & DEFT_TERM_VEFF) || has_saft(c->f) || is_tensor(c->f)) {
           // the refinement by FP64 CG (the Newton step's Hessian covers the
           // vector White Bear kinds and the ideal gas, in the density variable)
-          status = step_secant(c, st, fp64_of(spec), c->p.gtol);
+          status = step_secant<double>(c, st, fp64_of(spec), c->p.gtol);
         } else {
           status = step_newton(c, st, spec);
         }
         more = !c->done;
       } else if (c->p.linesearch == DEFT_LS_SECANT) {
-        status = step_secant(c, st, spec, c->p.gtol);
+        status = step_secant<double>(c, st, spec, c->p.gtol);
         more = !c->done;
       } else if (c->p.linesearch == DEFT_LS_NEW_API) {
         status = step_newapi(c, &more);
@@ -1801,6 +1979,7 @@ int deft_cg_solve_device(deft_cg *c, deft_cg_status *st) {
   cudaSetDevice(f->grid->ctx->device);
   deft::DcgProblem p;
   if (int s = device_problem(c, &p)) return s;
+  c->f32_live = false;  // the device solve runs on the FP64 vectors from x
   const deft::FmtSpec &spec = p.spec;
   if (c->dgraph && (c->dkey_terms != spec.terms || c->dkey_hs != spec.hs ||
                     c->dkey_prec != spec.precision || c->dkey_kT != spec.kT ||
@@ -1984,6 +2163,7 @@ int deft_cg_checkpoint(deft_cg *c, const char *path) {
   cudaSetDevice(g->ctx->device);
   if (int s = sync(g->ctx)) return s;
   const size_t n = nr(g);
+  if (int s = f32_leave(c)) return s;
   std::vector<double> host(n);
   FILE *fb = std::fopen(path, "wb");
   if (!fb) return set_err(DEFT_ERR_ARG, std::string("cannot write ") + path);
@@ -2062,6 +2242,7 @@ int deft_cg_restore(deft_cg *c, const char *path) {
     else if (sc.i) *sc.i = (int)v;
     else *sc.b = v != 0;
   }
+  c->f32_live = false;  // the FP64 vectors hold the restored state
   return DEFT_OK;
 }
 

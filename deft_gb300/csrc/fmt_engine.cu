@@ -127,6 +127,10 @@ __device__ __forceinline__ bool precond_active(double m, double nv) {
   const unsigned long long nb = (unsigned long long)__double_as_longlong(nv);
   return (mb << 1) != 0 && nb - 1ull < 0x7FF0000000000000ull;
 }
+__device__ __forceinline__ bool precond_active(float m, float nv) {
+  const unsigned mb = __float_as_uint(m), nb = __float_as_uint(nv);
+  return (mb << 1) != 0 && nb - 1u < 0x7F800000u;
+}
 
 // Deterministic block reduction of K doubles; thread 0 gets the sums.
 template <int K>
@@ -389,11 +393,14 @@ struct LocalArgs {
 // kernel that writes the gradient (b[i] == nullptr: the gradient itself);
 // per-block sums go to partials[3 * block + i] and k_reduce_terms adds them
 // up in block order.
-struct GradDots {
-  const double *b[3];
+// R is the type of the real fields (FP64, or FP32 in the mixed form's FP32
+// stage on FP32 vectors).
+template <typename R> struct GradDotsT {
+  const R *b[3];
   int k;
   double *partials;
 };
+using GradDots = GradDotsT<double>;
 
 // Last-block reduction of per-block dot products (defined with k_dots).
 template <int K>
@@ -824,15 +831,15 @@ __device__ void z_r2c_store5(typename Cplx<T>::type *res, typename Cplx<T>::type
 #define DEFT_Z_PHI_DF_MIN_BLOCKS 0
 #endif
 template <typename T> using PhiT = std::conditional_t<is_df<T> && !DEFT_DF_PHI, double, T>;
-template <typename T, bool GRAD, int RN = 0>
+template <typename T, bool GRAD, int RN = 0, typename R = double>
 __global__ void __launch_bounds__(kThreads,
                                   RN > 0 ? 2
                                          : (sizeof(T) == 4 ? DEFT_Z_PHI_MIN_BLOCKS
                                                            : (is_df<T> ? DEFT_Z_PHI_DF_MIN_BLOCKS
                                                                        : 0)))
     k_z_phi(typename Cplx<T>::type *S5,
-                                                    const double *__restrict__ n,
-                                                    const double *__restrict__ V, Geom g,
+                                                    const R *__restrict__ n,
+                                                    const R *__restrict__ V, Geom g,
                                                     FftPlan pz, FastDiv fP, FastDiv f2P,
                                                     FastDiv f5P, const LocalArgs *__restrict__ lap,
                                                     double *partials) {
@@ -1154,9 +1161,9 @@ __device__ __forceinline__ void warp_r2c_store5(float2 (&v)[5][E], float2 *S5, c
                          nvalid);
 }
 
-template <int E>
+template <int E, typename R = double>
 __global__ void __launch_bounds__(32 * kZWarps)
-    k_z_r2c_warp(const double *__restrict__ in, float2 *__restrict__ out, Geom g,
+    k_z_r2c_warp(const R *__restrict__ in, float2 *__restrict__ out, Geom g,
                  const float2 *__restrict__ tw, float s) {
   constexpr int N = 32 * E, NzH = N / 2 + 1;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -1178,12 +1185,12 @@ __global__ void __launch_bounds__(32 * kZWarps)
 
 // Warp form of k_z_grad: c2r of the adjoint sum, + local gradient terms,
 // masked, optional dot products of the new gradient.
-template <int E>
+template <int E, typename R = double>
 __global__ void __launch_bounds__(32 * kZWarps)
-    k_z_grad_warp(const float2 *__restrict__ in, const double *__restrict__ n,
-                  const double *__restrict__ V, const double *__restrict__ mask,
-                  double *__restrict__ grad, Geom g, const float2 *__restrict__ tw,
-                  const LocalArgs *__restrict__ lap, GradDots gd) {
+    k_z_grad_warp(const float2 *__restrict__ in, const R *__restrict__ n,
+                  const R *__restrict__ V, const R *__restrict__ mask,
+                  R *__restrict__ grad, Geom g, const float2 *__restrict__ tw,
+                  const LocalArgs *__restrict__ lap, GradDotsT<R> gd) {
   constexpr int N = 32 * E, NzH = N / 2 + 1;
   const LocalArgs la = *lap;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -1220,7 +1227,7 @@ __global__ void __launch_bounds__(32 * kZWarps)
         const float mk = float(mask[r]);
         gr = mk == 0.f ? 0.f : mk * gr;
       }
-      grad[r] = double(gr);
+      grad[r] = R(gr);
 #pragma unroll
       for (int i = 0; i < 3; i++)
         if (i < gd.k) dacc[i] += gr * (gd.b[i] ? float(gd.b[i][r]) : gr);
@@ -1611,6 +1618,59 @@ __global__ void k_precond_dots(const double *__restrict__ n, const double *__res
     acc[1] += zv * h[i];
   }
   finish_dots<2>(acc, red, partials, counter, out);
+}
+
+// FP32-vector forms for the mixed form's FP32 stage: z = g n / (kT dV) on
+// the active points (mask != 0, n > 0) with (z.g, z.h) summed in FP64;
+// d = alpha g + beta d; y += alpha x; conversions.
+__global__ void k_precond_dots32(const float *__restrict__ n, const float *__restrict__ g,
+                                 const float *__restrict__ mask, const float *__restrict__ h,
+                                 float inv_c, float *__restrict__ z, int N, double *partials,
+                                 unsigned int *counter, double *out) {
+  __shared__ double red[32 * 2];
+  float acc[2] = {0, 0};
+  #pragma unroll 4
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+    const float m = mask ? mask[i] : 1.0f;
+    const float nv = n[i], gv = g[i];
+    const float zv = precond_active(m, nv) ? gv * nv * inv_c : 0.0f;
+    z[i] = zv;
+    acc[0] += zv * gv;
+    acc[1] += zv * h[i];
+  }
+  double accd[2] = {acc[0], acc[1]};
+  finish_dots<2>(accd, red, partials, counter, out);
+}
+__global__ void k_scal_add32(float beta, float *__restrict__ d, float alpha,
+                             const float *__restrict__ g, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    d[i] = alpha * g[i] + beta * d[i];
+}
+__global__ void k_scal_add_dot32(float beta, float *__restrict__ d, float alpha,
+                                 const float *__restrict__ g, const float *__restrict__ h, int N,
+                                 double *partials, unsigned int *counter, double *out) {
+  __shared__ double red[32];
+  float acc = 0;
+  #pragma unroll 4
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+    const float dv = alpha * g[i] + beta * d[i];
+    d[i] = dv;
+    acc += h[i] * dv;
+  }
+  double accd[1] = {acc};
+  finish_dots<1>(accd, red, partials, counter, out);
+}
+__global__ void k_axpy32(float alpha, const float *__restrict__ x, float *__restrict__ y, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    y[i] += alpha * x[i];
+}
+__global__ void k_to_f32(const double *__restrict__ a, float *__restrict__ b, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    b[i] = (float)a[i];
+}
+__global__ void k_to_f64(const float *__restrict__ a, double *__restrict__ b, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    b[i] = (double)a[i];
 }
 
 // One update of the Newton step's preconditioned linear CG in one pass:
@@ -2192,6 +2252,8 @@ class EngineImpl {
       set_smem(k_x_conv_adj<float, RN>, t32.smem_xc);
       set_smem(k_z_phi<float, false, RN>, t32.smem_phi);
       set_smem(k_z_phi<float, true, RN>, t32.smem_phi);
+      set_smem(k_z_phi<float, false, RN, float>, t32.smem_phi);
+      set_smem(k_z_phi<float, true, RN, float>, t32.smem_phi);
       set_smem(k_z_grad<float, RN>, t32.smem_z);
       set_smem(k_z_hess<float, RN>, t32.smem_phi);
       set_smem(k_z_jac<float, RN>, t32.smem_phi);
@@ -2212,6 +2274,8 @@ class EngineImpl {
       constexpr int E = decltype(ec)::value;
       set_smem(k_z_r2c_warp<E>, zwarp_smem<E>());
       set_smem(k_z_grad_warp<E>, zwarp_smem<E>());
+      set_smem(k_z_r2c_warp<E, float>, zwarp_smem<E>());
+      set_smem(k_z_grad_warp<E, float>, zwarp_smem<E>());
       set_smem(k_z_hvp_out_warp<E>, zwarp_smem<E>());
       set_smem(k_z_phi_warp<true, E>, zwarp_smem<E>(5));
       set_smem(k_z_phi_warp<false, E>, zwarp_smem<E>(5));
@@ -2459,16 +2523,17 @@ class EngineImpl {
   // Queues z r2c, y FFT, x convolution and inverse y of n (the weight table
   // for f.R must be current: ensure_table runs outside any graph capture).
   // Real field -> half spectra along z, into S0 (in T).
-  template <typename T> void z_r2c_spec0(const double *n) {
+  // (R = float: FP32 input, warp kernels only; see f32_vectors_ok.)
+  template <typename T, typename R = double> void z_r2c_spec0(const R *n) {
     const Tiles &t = tl<T>();
     pre(kslot<T>(kK_z_r2c));
     if (zwarp<T>()) {
       with_e(g.Nz, [&](auto ec) {
         constexpr int E = decltype(ec)::value;
-        k_z_r2c_warp<E><<<zwarp_blocks(), 32 * kZWarps, zwarp_smem<E>(), stream>>>(
+        k_z_r2c_warp<E, R><<<zwarp_blocks(), 32 * kZWarps, zwarp_smem<E>(), stream>>>(
             n, reinterpret_cast<float2 *>(spec0<T>()), g, twz32(), 1.0f);
       });
-    } else {
+    } else if constexpr (std::is_same<R, double>::value) {
       with_rn<T>(plan<T>(2), [&](auto rn) {
         k_z_r2c<T, decltype(rn)::value><<<dim3(pairs_tiles(t.Pz), 1), kThreads, t.smem_z,
                                           stream>>>(n, spec0<T>(), g, plan<T>(2), t.fPz, T(1));
@@ -2477,9 +2542,9 @@ class EngineImpl {
     post(kslot<T>(kK_z_r2c));
   }
 
-  template <typename T> int forward_weighted(const FmtSpec &f, const double *n) {
+  template <typename T, typename R = double> int forward_weighted(const FmtSpec &f, const R *n) {
     const Tiles &t = tl<T>();
-    z_r2c_spec0<T>(n);
+    z_r2c_spec0<T, R>(n);
     y_fft<T>(spec0<T>(), 1, -1);
     pre(kslot<T>(kK_x_conv_fwd));
     if (pencil<T>(0)) {
@@ -2624,14 +2689,13 @@ class EngineImpl {
   // Queues the fixed-order reduction of the energy partials and the copy of
   // the results to the pinned host block.
   // With gd, also the gradient dot products k_z_grad took (results[8..11)).
-  void queue_energy(int nblk, const GradDots *gd = nullptr, int gblk = 0) {
+  void queue_energy(int nblk, int dk = 0, const double *dpart = nullptr, int gblk = 0) {
     pre(kK_reduce_terms);
-    k_reduce_terms<<<1, kReduceThreads, 0, stream>>>(partials, nblk, g.dV, results,
-                                                      gd ? gd->partials : nullptr,
-                                                      gd ? gd->k : 0, gblk);
+    k_reduce_terms<<<1, kReduceThreads, 0, stream>>>(partials, nblk, g.dV, results, dpart, dk,
+                                                      gblk);
     post(kK_reduce_terms);
     if (!dev_only)
-      cudaMemcpyAsync(results_host, results, sizeof(double) * (gd ? 11 : 8),
+      cudaMemcpyAsync(results_host, results, sizeof(double) * (dk ? 11 : 8),
                       cudaMemcpyDeviceToHost, stream);
   }
   bool dev_only = false;  // leave the results in device memory (device-driven solves)
@@ -2685,6 +2749,33 @@ class EngineImpl {
     return finish_energy(E_host, terms_host, kd, dots_host);
   }
 
+  // eval<float> on FP32 vectors (f32_vectors_ok(f)): n, V, mask, grad and
+  // the dot vectors db[i] (db[i] == grad: |grad|^2) in FP32.
+  int eval32(const FmtSpec &f, const float *n, const float *V, const float *mask, float *grad,
+             double *E_host, double *terms_host, int kd, const float *const *db,
+             double *dots_host) {
+    if (!f32_vectors_ok(f)) {
+      err = "FP32 vectors: not for this functional or grid";
+      return -1;
+    }
+    if (ensure_table<float>(f.R) || upload_args(f)) return -1;
+    const double *ka[3] = {nullptr, nullptr, nullptr}, *kb[3] = {nullptr, nullptr, nullptr};
+    GradDotsT<float> gd{};
+    for (int i = 0; i < kd; i++) {
+      gd.b[i] = db[i] == grad ? nullptr : db[i];
+      ka[i] = reinterpret_cast<const double *>(grad);
+      kb[i] = reinterpret_cast<const double *>(db[i]);
+    }
+    gd.k = kd;
+    gd.partials = grad_partials;
+    const GraphKey key = graph_key(5, 4, f, n, V, mask, grad, kd, ka, kb);
+    if (run_graphed(key, [&] {
+          return eval_launch<float, float>(f, n, V, mask, grad, kd > 0 ? &gd : nullptr);
+        }))
+      return -1;
+    return finish_energy(E_host, terms_host, kd, dots_host);
+  }
+
   // Queues k_dots for kd <= 3 pairs into results[slot..] and its copy to the
   // pinned host block.
   void queue_dots(int kd, const double *const *a, const double *const *b, int slot) {
@@ -2698,35 +2789,44 @@ class EngineImpl {
                     cudaMemcpyDeviceToHost, stream);
   }
 
-  template <typename T>
-  int eval_launch(const FmtSpec &f, const double *n, const double *V, const double *mask,
-                  double *grad, const GradDots *gd = nullptr) {
+  // R = float: n, V, mask, the gradient and the dot vectors in FP32 (the
+  // mixed form's FP32 stage on FP32 vectors; hard spheres on, warp z
+  // kernels for the one-field transforms and the Stockham Phi kernel: the
+  // cases f32_vectors_ok admits).
+  template <typename T, typename R = double>
+  int eval_launch(const FmtSpec &f, const R *n, const R *V, const R *mask, R *grad,
+                  const GradDotsT<R> *gd = nullptr) {
+    constexpr bool r64 = std::is_same<R, double>::value;
     const Tiles &t = tl<T>();
     int nblk;
     if (f.terms & kTermHS) {
-      if (forward_weighted<T>(f, n)) return -1;
+      if (forward_weighted<T, R>(f, n)) return -1;
       nblk = pairs_tiles(t.Pphi);
       pre(kslot<T>(grad ? kK_z_phi_grad : kK_z_phi_energy));
-      if (zwarp<T>(5)) {
-        nblk = zwarp_blocks();
-        with_e(g.Nz, [&](auto ec) {
-          constexpr int E = decltype(ec)::value;
-          float2 *s5 = reinterpret_cast<float2 *>(spec5<T>());
-          if (grad)
-            k_z_phi_warp<true, E><<<nblk, 32 * kZWarps, zwarp_smem<E>(5), stream>>>(
-                s5, n, V, g, twz32(), la_dev, partials);
-          else
-            k_z_phi_warp<false, E><<<nblk, 32 * kZWarps, zwarp_smem<E>(5), stream>>>(
-                s5, n, V, g, twz32(), la_dev, partials);
-        });
+      bool warp5 = false;
+      if constexpr (r64) warp5 = zwarp<T>(5);
+      if (warp5) {
+        if constexpr (r64) {
+          nblk = zwarp_blocks();
+          with_e(g.Nz, [&](auto ec) {
+            constexpr int E = decltype(ec)::value;
+            float2 *s5 = reinterpret_cast<float2 *>(spec5<T>());
+            if (grad)
+              k_z_phi_warp<true, E><<<nblk, 32 * kZWarps, zwarp_smem<E>(5), stream>>>(
+                  s5, n, V, g, twz32(), la_dev, partials);
+            else
+              k_z_phi_warp<false, E><<<nblk, 32 * kZWarps, zwarp_smem<E>(5), stream>>>(
+                  s5, n, V, g, twz32(), la_dev, partials);
+          });
+        }
       } else {
         with_rn<T>(plan<T>(2), [&](auto rn) {
           constexpr int RN = decltype(rn)::value;
           if (grad)
-            k_z_phi<T, true, RN><<<nblk, kThreads, t.smem_phi, stream>>>(
+            k_z_phi<T, true, RN, R><<<nblk, kThreads, t.smem_phi, stream>>>(
                 spec5<T>(), n, V, g, plan<T>(2), t.fPphi, t.f2Pphi, t.f5Pphi, la_dev, partials);
           else
-            k_z_phi<T, false, RN><<<nblk, kThreads, t.smem_phi, stream>>>(
+            k_z_phi<T, false, RN, R><<<nblk, kThreads, t.smem_phi, stream>>>(
                 spec5<T>(), n, V, g, plan<T>(2), t.fPphi, t.f2Pphi, t.f5Pphi, la_dev, partials);
         });
       }
@@ -2741,9 +2841,14 @@ class EngineImpl {
       }
     } else {
       nblk = 4 * 152;
-      pre(kslot<T>(kK_local_energy));
-      k_local_energy<Acc<T>><<<nblk, kThreads, 0, stream>>>(n, V, g, la_dev, partials);
-      post(kslot<T>(kK_local_energy));
+      if constexpr (r64) {
+        pre(kslot<T>(kK_local_energy));
+        k_local_energy<Acc<T>><<<nblk, kThreads, 0, stream>>>(n, V, g, la_dev, partials);
+        post(kslot<T>(kK_local_energy));
+      } else {
+        err = "FP32 vectors need the hard-sphere term";
+        return -1;
+      }
     }
     int gblk = pairs_tiles(t.Pz);
     if (grad) {
@@ -2752,22 +2857,33 @@ class EngineImpl {
         gblk = zwarp_blocks();
         with_e(g.Nz, [&](auto ec) {
           constexpr int E = decltype(ec)::value;
-          k_z_grad_warp<E><<<gblk, 32 * kZWarps, zwarp_smem<E>(), stream>>>(
+          k_z_grad_warp<E, R><<<gblk, 32 * kZWarps, zwarp_smem<E>(), stream>>>(
               reinterpret_cast<const float2 *>(spec0<T>()), n, V, mask, grad, g, twz32(), la_dev,
-              gd ? *gd : GradDots{});
+              gd ? *gd : GradDotsT<R>{});
         });
-      } else {
+      } else if constexpr (r64) {
         with_rn<T>(plan<T>(2), [&](auto rn) {
           k_z_grad<T, decltype(rn)::value><<<pairs_tiles(t.Pz), kThreads, t.smem_z, stream>>>(
               spec0<T>(), n, V, mask, grad, g, plan<T>(2), t.fPz, la_dev, gd ? *gd : GradDots{});
         });
+      } else {
+        err = "FP32 vectors need the warp z transforms";
+        return -1;
       }
       post(kslot<T>(kK_z_grad));
     }
     if (check("gradient")) return -1;
-    queue_energy(nblk, grad ? gd : nullptr, gblk);
+    queue_energy(nblk, grad && gd ? gd->k : 0, grad && gd ? gd->partials : nullptr, gblk);
     return check("energy reduction");
   }
+
+  // Whether eval32 can run spec f: mixed form with the hard-sphere term, the
+  // one-field warp z transforms on, the five-field ones off.
+  bool f32_vectors_ok(const FmtSpec &f) const {
+    return f.precision == kPrecisionMixed && (f.terms & kTermHS) && zwarp<float>() &&
+           !zwarp<float>(5);
+  }
+
   int hess_setup(const FmtSpec &f, const double *n) {
     if (!hess && (alloc(&hess, sizeof(float) * kHessPacked * (size_t)g.NR) ||
                   alloc(&hloc, sizeof(float) * (size_t)g.NR)))
@@ -3057,6 +3173,72 @@ int Engine::diag_precond(const FmtSpec &f, const double *n, const double *r, con
                                                           e.g.NR);
   e.post(kK_diag_precond);
   return e.check("diag_precond");
+}
+
+bool Engine::f32_vectors_ok(const FmtSpec &f) const { return impl_->f32_vectors_ok(f); }
+
+int Engine::eval32(const FmtSpec &f, const float *n, const float *V, const float *mask,
+                   float *grad, double *E_host, double *terms_host, int kd,
+                   const float *const *db, double *dots_host) {
+  return impl_->eval32(f, n, V, mask, grad, E_host, terms_host, kd, db, dots_host);
+}
+
+int Engine::scal_add_dot32(double beta, float *d, double alpha, const float *g, const float *h,
+                           double *out_host) {
+  EngineImpl &e = *impl_;
+  e.pre(kslot<float>(kK_scal_add));
+  k_scal_add_dot32<<<e.dot_blocks, kThreads, 0, e.stream>>>(
+      (float)beta, d, (float)alpha, g, h, e.g.NR, e.dot_partials, e.dot_counter, e.results);
+  e.post(kslot<float>(kK_scal_add));
+  return e.read_results(1, out_host, "scal_add_dot");
+}
+
+int Engine::copy32(const float *src, float *dst) {
+  EngineImpl &e = *impl_;
+  cudaError_t err =
+      cudaMemcpyAsync(dst, src, sizeof(float) * e.g.NR, cudaMemcpyDeviceToDevice, e.stream);
+  return err != cudaSuccess ? e.fail("copy", err) : 0;
+}
+
+int Engine::precond_dots32(const FmtSpec &f, const float *n, const float *g, const float *mask,
+                           float *z, const float *h, double *out_host) {
+  EngineImpl &e = *impl_;
+  e.pre(kslot<float>(kK_precond_dots));
+  k_precond_dots32<<<e.dot_blocks, kThreads, 0, e.stream>>>(
+      n, g, mask, h, (float)(1.0 / (f.kT * e.g.dV)), z, e.g.NR, e.dot_partials, e.dot_counter,
+      e.results);
+  e.post(kslot<float>(kK_precond_dots));
+  return e.read_results(2, out_host, "precond_dots");
+}
+
+int Engine::scal_add32(double beta, float *d, double alpha, const float *g) {
+  EngineImpl &e = *impl_;
+  e.pre(kslot<float>(kK_scal_add));
+  k_scal_add32<<<e.dot_blocks, kThreads, 0, e.stream>>>((float)beta, d, (float)alpha, g, e.g.NR);
+  e.post(kslot<float>(kK_scal_add));
+  return e.check("scal_add");
+}
+
+int Engine::axpy32(double alpha, const float *x, float *y) {
+  EngineImpl &e = *impl_;
+  e.pre(kslot<float>(kK_axpy));
+  k_axpy32<<<e.dot_blocks, kThreads, 0, e.stream>>>((float)alpha, x, y, e.g.NR);
+  e.post(kslot<float>(kK_axpy));
+  return e.check("axpy");
+}
+
+int Engine::to_f32(const double *a, float *b, long long n) {
+  EngineImpl &e = *impl_;
+  if (n < 0) n = e.g.NR;
+  k_to_f32<<<e.dot_blocks, kThreads, 0, e.stream>>>(a, b, (int)n);
+  return e.check("to_f32");
+}
+
+int Engine::to_f64(const float *a, double *b, long long n) {
+  EngineImpl &e = *impl_;
+  if (n < 0) n = e.g.NR;
+  k_to_f64<<<e.dot_blocks, kThreads, 0, e.stream>>>(a, b, (int)n);
+  return e.check("to_f64");
 }
 
 int Engine::precond_dots(const FmtSpec &f, const double *n, const double *g, const double *mask,

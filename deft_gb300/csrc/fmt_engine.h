@@ -153,6 +153,26 @@ class Engine {
   int scal_add_dot(double beta, double *d, double alpha, const double *g, const double *h,
                    double *out_host);
 
+  // The mixed form's FP32 stage on FP32 vectors.  f32_vectors_ok: whether
+  // eval32 runs spec f here (mixed, hard spheres on, Nz = 32, 64, 128 or
+  // 256 with the warp z transforms).  eval32: energy + gradient of the FP32
+  // density n (V, mask FP32, may be null), the gradient in FP32, and the
+  // dot products grad.db[i] (FP32 vectors; db[i] == grad: |grad|^2) summed
+  // in FP64.  The vector kernels take FP32 vectors and FP64 coefficients.
+  bool f32_vectors_ok(const FmtSpec &f) const;
+  int eval32(const FmtSpec &f, const float *n, const float *V, const float *mask, float *grad,
+             double *E_host, double *terms_host, int kd, const float *const *db,
+             double *dots_host);
+  int precond_dots32(const FmtSpec &f, const float *n, const float *g, const float *mask,
+                     float *z, const float *h, double *out_host);
+  int scal_add32(double beta, float *d, double alpha, const float *g);  // d = alpha g + beta d
+  int scal_add_dot32(double beta, float *d, double alpha, const float *g, const float *h,
+                     double *out_host);                                 // ... and h.d
+  int copy32(const float *src, float *dst);
+  int axpy32(double alpha, const float *x, float *y);                   // y += alpha x
+  int to_f32(const double *a, float *b, long long n = -1);              // n = -1: NR
+  int to_f64(const float *a, double *b, long long n = -1);
+
   // Vector kernels (NR-long device vectors).
   // out_host[i] = a_i . b_i for i < k (k <= 3), one pass, one sync.
   int dots(int k, const double *const *a, const double *const *b, double *out_host);
