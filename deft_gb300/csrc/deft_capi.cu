@@ -99,6 +99,7 @@ struct deft_cg {
   // stale; x is brought up to date after every step
   float *x32 = nullptr, *g32 = nullptr, *d32 = nullptr, *gold32 = nullptr, *pg32 = nullptr;
   float *V32 = nullptr, *mask32 = nullptr;
+  float *q32 = nullptr, *dx32 = nullptr;  // the Newton step's linear CG on FP32 vectors
   bool f32_live = false;
   unsigned f32_fields = ~0u;  // the functional's fields_version V32, mask32 were made from
 };
@@ -938,7 +939,8 @@ int deft_cg_destroy(deft_cg *c) {
   cudaFree(c->pg);
   cudaFree(c->q);
   cudaFree(c->dxv);
-  for (float *v : {c->x32, c->g32, c->d32, c->gold32, c->pg32, c->V32, c->mask32}) cudaFree(v);
+  for (float *v : {c->x32, c->g32, c->d32, c->gold32, c->pg32, c->V32, c->mask32, c->q32, c->dx32})
+    cudaFree(v);
   if (c->log) fclose(c->log);
   deft::dcg_free(c->dgraph);
   delete c;
@@ -1190,23 +1192,34 @@ int cg_precond_dots(deft_cg *c, const deft::FmtSpec &spec, const float *, double
 // iterates are FP32-evaluated anyway and x only has to reach the switch to
 // the FP64 Newton refinement.  DEFT_F32_VECTORS=0 in the environment keeps
 // FP64 vectors.
-bool f32_stage(deft_cg *c, const deft::FmtSpec &spec) {
+bool f32_switch() {
   static const bool on = [] {
     const char *ev = getenv("DEFT_F32_VECTORS");
     return ev ? atoi(ev) != 0 : DEFT_F32_VECTORS != 0;
   }();
-  return on && spec.precision == deft::kPrecisionMixed && c->pg &&
+  return on;
+}
+bool f32_stage(deft_cg *c, const deft::FmtSpec &spec) {
+  return f32_switch() && spec.precision == deft::kPrecisionMixed && c->pg &&
          c->p.preconditioned == DEFT_PC_DENSITY && !(c->f->p.terms & DEFT_TERM_VEFF) &&
          !is_tensor(c->f) && !has_saft(c->f) && eng_of(c)->f32_vectors_ok(spec);
 }
 
-// Makes the FP32 vectors current: allocates them, converts V and the mask
-// when they changed, and the state vectors when the FP64 ones hold it.
-int f32_enter(deft_cg *c) {
+// Whether the Newton refinement's linear CG keeps its vectors in FP32
+// (same switch and engine condition as f32_stage; any preconditioner).
+bool f32_newton(deft_cg *c, const deft::FmtSpec &spec) {
+  return f32_switch() && spec.precision == deft::kPrecisionMixed &&
+         !(c->f->p.terms & DEFT_TERM_VEFF) && !is_tensor(c->f) && !has_saft(c->f) &&
+         eng_of(c)->f32_vectors_ok(spec);
+}
+
+// Allocates the FP32 vectors and converts V and the mask when they changed.
+int f32_buffers(deft_cg *c) {
   Engine *e = eng_of(c);
   const size_t n = nr(c->f->grid);
   if (!c->x32) {
-    for (float **v : {&c->x32, &c->g32, &c->d32, &c->gold32, &c->pg32, &c->V32, &c->mask32}) {
+    for (float **v : {&c->x32, &c->g32, &c->d32, &c->gold32, &c->pg32, &c->V32, &c->mask32,
+                      &c->q32, &c->dx32}) {
       cudaError_t ce = cudaMalloc((void **)v, sizeof(float) * n);
       if (ce != cudaSuccess) {
         *v = nullptr;
@@ -1219,6 +1232,14 @@ int f32_enter(deft_cg *c) {
       return eng_err(e);
     c->f32_fields = c->f->fields_version;
   }
+  return DEFT_OK;
+}
+
+// Makes the FP32 vectors current: buffers and fields, and the state
+// vectors when the FP64 ones hold the state.
+int f32_enter(deft_cg *c) {
+  Engine *e = eng_of(c);
+  if (int s = f32_buffers(c)) return s;
   if (!c->f32_live) {
     if (e->to_f32(c->x, c->x32) || e->to_f32(c->g, c->g32) || e->to_f32(c->d, c->d32) ||
         e->to_f32(c->gold, c->gold32) || e->to_f32(c->pg, c->pg32))
@@ -1457,34 +1478,68 @@ int step_newton(deft_cg *c, deft_cg_status *st, const deft::FmtSpec &spec) {
   if (e->hess_setup(spec, c->x)) return eng_err(e);
   // Preconditioned linear CG on H dx = -g with M^-1 = n / (kT dV) (the
   // inverse ideal-gas curvature, which spans orders of magnitude between
-  // walls, contacts and bulk): r = -g (in gold), z (in pg or g), p = z (in d)
-  double *r = c->gold, *p = c->d, *q = c->q, *dx = c->dxv;
-  double *z = c->g;  // the FP64 gradient is re-evaluated after the step
-  if (e->scal_add(0.0, r, -1.0, c->g)) return eng_err(e);
-  if (e->diag_precond(spec, c->x, r, active_mask(c->f), z) || e->copy(z, p)) return eng_err(e);
-  c->have_g = false;
-  if (cudaMemsetAsync(dx, 0, bytes, stream) != cudaSuccess) return set_err(DEFT_ERR_CUDA, "memset");
-  double rz;
-  {
-    const double *a[1] = {r};
-    const double *b[1] = {z};
-    if (e->dots(1, a, b, &rz)) return eng_err(e);
-  }
+  // walls, contacts and bulk).  The products run through the FP32 FFTs, so
+  // where the engine takes FP32 vectors (f32_newton) the CG's vectors are
+  // FP32 too: the step only has to solve to 1e-5 of |g|, far above FP32
+  // rounding, and the FP64 gradient at x + dx decides what is accepted.
   const double tol = std::fmax(1e-5 * st->gnorm, 0.05 * c->p.gtol);
-  for (int k = 0; k < 400 && rz > 0; k++) {
-    double pq;  // p.q, taken by the product's last kernel
-    if (e->hvp(spec, p, c->f->mask, q, &pq)) return eng_err(e);
-    c->hvps++;
-    if (!(pq > 0)) break;  // no positive curvature along p: keep the step so far
-    const double alpha = rz / pq;
-    // dx += alpha p, r -= alpha q, z = M^-1 r, (r.r, r.z) in one pass
-    double o[2];
-    if (e->newton_update(spec, c->x, alpha, p, q, dx, r, active_mask(c->f), z, o))
-      return eng_err(e);
-    if (std::sqrt(o[0]) < tol) break;
-    if (e->scal_add(o[1] / rz, p, 1.0, z)) return eng_err(e);
-    rz = o[1];
+  if (f32_newton(c, spec)) {
+    if (int s = f32_leave(c)) return s;
+    if (int s = f32_buffers(c)) return s;
+    // r = -g (gold32), z (g32), p = z (d32), q (q32), dx (dx32), n (x32)
+    float *r = c->gold32, *p = c->d32, *q = c->q32, *dx = c->dx32, *z = c->g32, *n = c->x32;
+    const float *mask = c->f->mask ? c->mask32 : nullptr;
+    const float *amask = active_mask(c->f) ? c->mask32 : nullptr;
+    if (e->to_f32(c->x, n) || e->to_f32(c->g, r, -1, -1.0)) return eng_err(e);
+    double rz;
+    if (e->diag_precond_dot32(spec, n, r, amask, z, &rz) || e->copy32(z, p)) return eng_err(e);
+    c->have_g = false;
+    if (cudaMemsetAsync(dx, 0, sizeof(float) * nr(c->f->grid), stream) != cudaSuccess)
+      return set_err(DEFT_ERR_CUDA, "memset");
+    for (int k = 0; k < 400 && rz > 0; k++) {
+      double pq;
+      if (e->hvp32(spec, p, mask, q, &pq)) return eng_err(e);
+      c->hvps++;
+      if (!(pq > 0)) break;
+      const double alpha = rz / pq;
+      double o[2];
+      if (e->newton_update32(spec, n, alpha, p, q, dx, r, amask, z, o)) return eng_err(e);
+      if (std::sqrt(o[0]) < tol) break;
+      if (e->scal_add32(o[1] / rz, p, 1.0, z)) return eng_err(e);
+      rz = o[1];
+    }
+    if (e->to_f64(dx, c->dxv)) return eng_err(e);
+  } else {
+    // r = -g (in gold), z (in pg or g), p = z (in d)
+    double *r = c->gold, *p = c->d, *q = c->q, *dx = c->dxv;
+    double *z = c->g;  // the FP64 gradient is re-evaluated after the step
+    if (e->scal_add(0.0, r, -1.0, c->g)) return eng_err(e);
+    if (e->diag_precond(spec, c->x, r, active_mask(c->f), z) || e->copy(z, p)) return eng_err(e);
+    c->have_g = false;
+    if (cudaMemsetAsync(dx, 0, bytes, stream) != cudaSuccess)
+      return set_err(DEFT_ERR_CUDA, "memset");
+    double rz;
+    {
+      const double *a[1] = {r};
+      const double *b[1] = {z};
+      if (e->dots(1, a, b, &rz)) return eng_err(e);
+    }
+    for (int k = 0; k < 400 && rz > 0; k++) {
+      double pq;  // p.q, taken by the product's last kernel
+      if (e->hvp(spec, p, c->f->mask, q, &pq)) return eng_err(e);
+      c->hvps++;
+      if (!(pq > 0)) break;  // no positive curvature along p: keep the step so far
+      const double alpha = rz / pq;
+      // dx += alpha p, r -= alpha q, z = M^-1 r, (r.r, r.z) in one pass
+      double o[2];
+      if (e->newton_update(spec, c->x, alpha, p, q, dx, r, active_mask(c->f), z, o))
+        return eng_err(e);
+      if (std::sqrt(o[0]) < tol) break;
+      if (e->scal_add(o[1] / rz, p, 1.0, z)) return eng_err(e);
+      rz = o[1];
+    }
   }
+  const double *dx = c->dxv;
   const double E0 = c->E;
   double scale = 1.0;
   for (int bt = 0; bt < 6; bt++) {

@@ -1243,12 +1243,13 @@ __global__ void __launch_bounds__(32 * kZWarps)
 }
 
 // Warp form of k_z_hvp_out: c2r of the adjoint sum plus the ideal-gas
-// curvature dV kT/n dx, masked, and dx.out by the last block.
-template <int E>
+// curvature dV kT/n dx, masked, and dx.out by the last block (dx, mask and
+// out in R: FP64, or FP32 for the Newton step's linear CG on FP32 vectors).
+template <int E, typename R = double>
 __global__ void __launch_bounds__(32 * kZWarps)
-    k_z_hvp_out_warp(const float2 *__restrict__ in, const double *__restrict__ dx,
-                     const float *__restrict__ hloc, const double *__restrict__ mask,
-                     double *__restrict__ out, Geom g, const float2 *__restrict__ tw,
+    k_z_hvp_out_warp(const float2 *__restrict__ in, const R *__restrict__ dx,
+                     const float *__restrict__ hloc, const R *__restrict__ mask,
+                     R *__restrict__ out, Geom g, const float2 *__restrict__ tw,
                      const LocalArgs *__restrict__ lap, double *dpart, unsigned int *counter,
                      double *dout) {
   constexpr int N = 32 * E, NzH = N / 2 + 1;
@@ -1283,7 +1284,7 @@ __global__ void __launch_bounds__(32 * kZWarps)
         const float mk = float(mask[r]);
         o = mk == 0.f ? 0.f : mk * o;
       }
-      out[r] = double(o);
+      out[r] = R(o);
       pq += dxt * o;
     }
   }
@@ -1671,6 +1672,54 @@ __global__ void k_to_f32(const double *__restrict__ a, float *__restrict__ b, in
 __global__ void k_to_f64(const float *__restrict__ a, double *__restrict__ b, int n) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
     b[i] = (double)a[i];
+}
+__global__ void k_to_f32_scaled(const double *__restrict__ a, double s, float *__restrict__ b,
+                                int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    b[i] = (float)(s * a[i]);
+}
+// The Newton step's linear CG on FP32 vectors: z = M^-1 r with r.z, and
+// the fused update of k_newton_update (per-thread FP32 sums, FP64 across
+// threads and blocks in a fixed order).
+__global__ void k_diag_precond_dot32(const float *__restrict__ n, const float *__restrict__ r,
+                                     const float *__restrict__ mask, float inv_c,
+                                     float *__restrict__ z, int N, double *partials,
+                                     unsigned int *counter, double *out) {
+  __shared__ double red[32];
+  float acc = 0;
+  #pragma unroll 4
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+    const float m = mask ? mask[i] : 1.0f;
+    const float nv = n[i], rv = r[i];
+    const float zv = precond_active(m, nv) ? rv * nv * inv_c : 0.0f;
+    z[i] = zv;
+    acc += rv * zv;
+  }
+  double accd[1] = {acc};
+  finish_dots<1>(accd, red, partials, counter, out);
+}
+__global__ void k_newton_update32(float alpha, const float *__restrict__ p,
+                                  const float *__restrict__ q, float *__restrict__ dx,
+                                  float *__restrict__ r, const float *__restrict__ n,
+                                  const float *__restrict__ mask, float inv_c,
+                                  float *__restrict__ z, int N, double *partials,
+                                  unsigned int *counter, double *out) {
+  __shared__ double red[32 * 2];
+  float acc[2] = {0, 0};
+  #pragma unroll 4
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+    dx[i] += alpha * p[i];
+    const float rv = r[i] - alpha * q[i];
+    r[i] = rv;
+    const float m = mask ? mask[i] : 1.0f;
+    const float nv = n[i];
+    const float zv = precond_active(m, nv) ? rv * nv * inv_c : 0.0f;
+    z[i] = zv;
+    acc[0] += rv * rv;
+    acc[1] += rv * zv;
+  }
+  double accd[2] = {acc[0], acc[1]};
+  finish_dots<2>(accd, red, partials, counter, out);
 }
 
 // One update of the Newton step's preconditioned linear CG in one pass:
@@ -2277,6 +2326,7 @@ class EngineImpl {
       set_smem(k_z_r2c_warp<E, float>, zwarp_smem<E>());
       set_smem(k_z_grad_warp<E, float>, zwarp_smem<E>());
       set_smem(k_z_hvp_out_warp<E>, zwarp_smem<E>());
+      set_smem(k_z_hvp_out_warp<E, float>, zwarp_smem<E>());
       set_smem(k_z_phi_warp<true, E>, zwarp_smem<E>(5));
       set_smem(k_z_phi_warp<false, E>, zwarp_smem<E>(5));
       set_smem(k_z_jac_warp<E>, zwarp_smem<E>(5));
@@ -2912,20 +2962,27 @@ class EngineImpl {
   }
 
   // With pq_host, also dx.out (taken by the output kernel) read back.
-  int hvp(const FmtSpec &f, const double *dx, const double *mask, double *out,
-          double *pq_host = nullptr) {
+  // R = float: FP32 vectors (f32_vectors_ok).
+  template <typename R>
+  int hvp(const FmtSpec &f, const R *dx, const R *mask, R *out, double *pq_host = nullptr) {
+    constexpr bool r64 = std::is_same<R, double>::value;
+    if (!r64 && !f32_vectors_ok(f)) {
+      err = "FP32 vectors: not for this functional or grid";
+      return -1;
+    }
     if ((f.terms & kTermHS) && ensure_table<float>(f.R)) return -1;
     if (upload_args(f)) return -1;
-    const GraphKey key = graph_key(pq_host ? 3 : 2, 4, f, dx, mask, out, hess);
-    if (run_graphed(key, [&] { return hvp_launch(f, dx, mask, out, pq_host != nullptr); }))
+    const GraphKey key = graph_key(r64 ? (pq_host ? 3 : 2) : (pq_host ? 7 : 6), 4, f, dx, mask,
+                                   out, hess);
+    if (run_graphed(key, [&] { return hvp_launch<R>(f, dx, mask, out, pq_host != nullptr); }))
       return -1;
     return pq_host ? read_results(1, pq_host, "hessian-vector product") : 0;
   }
 
-  int hvp_launch(const FmtSpec &f, const double *dx, const double *mask, double *out,
-                 bool with_dot = false) {
+  template <typename R = double>
+  int hvp_launch(const FmtSpec &f, const R *dx, const R *mask, R *out, bool with_dot = false) {
     if (f.terms & kTermHS) {
-      if (forward_weighted<float>(f, dx)) return -1;
+      if (forward_weighted<float, R>(f, dx)) return -1;
       pre(kslot<float>(kK_z_jac));
       if (zwarp<float>(5)) {
         with_e(g.Nz, [&](auto ec) {
@@ -2952,10 +3009,13 @@ class EngineImpl {
     if (zwarp<float>()) {
       with_e(g.Nz, [&](auto ec) {
         constexpr int E = decltype(ec)::value;
-        k_z_hvp_out_warp<E><<<zwarp_blocks(), 32 * kZWarps, zwarp_smem<E>(), stream>>>(
+        k_z_hvp_out_warp<E, R><<<zwarp_blocks(), 32 * kZWarps, zwarp_smem<E>(), stream>>>(
             reinterpret_cast<const float2 *>(spec0<float>()), dx, hloc, mask, out, g, twz32(),
             la_dev, grad_partials, dot_counter, with_dot ? results : nullptr);
       });
+    } else if constexpr (!std::is_same<R, double>::value) {
+      err = "FP32 vectors need the warp z transforms";
+      return -1;
     } else {
       with_rn<float>(plan<float>(2), [&](auto rn) {
         k_z_hvp_out<float, decltype(rn)::value><<<pairs_tiles(t32.Pz), kThreads, t32.smem_z,
@@ -3128,7 +3188,35 @@ int Engine::hess_setup(const FmtSpec &f, const double *n) { return impl_->hess_s
 
 int Engine::hvp(const FmtSpec &f, const double *dx, const double *mask, double *out,
                 double *pq_host) {
-  return impl_->hvp(f, dx, mask, out, pq_host);
+  return impl_->hvp<double>(f, dx, mask, out, pq_host);
+}
+
+int Engine::hvp32(const FmtSpec &f, const float *dx, const float *mask, float *out,
+                  double *pq_host) {
+  return impl_->hvp<float>(f, dx, mask, out, pq_host);
+}
+
+int Engine::diag_precond_dot32(const FmtSpec &f, const float *n, const float *r,
+                               const float *mask, float *z, double *rz_host) {
+  EngineImpl &e = *impl_;
+  e.pre(kslot<float>(kK_diag_precond));
+  k_diag_precond_dot32<<<e.dot_blocks, kThreads, 0, e.stream>>>(
+      n, r, mask, (float)(1.0 / (f.kT * e.g.dV)), z, e.g.NR, e.dot_partials, e.dot_counter,
+      e.results);
+  e.post(kslot<float>(kK_diag_precond));
+  return e.read_results(1, rz_host, "diag_precond");
+}
+
+int Engine::newton_update32(const FmtSpec &f, const float *n, double alpha, const float *p,
+                            const float *q, float *dx, float *r, const float *mask, float *z,
+                            double *out_host) {
+  EngineImpl &e = *impl_;
+  e.pre(kslot<float>(kK_newton_update));
+  k_newton_update32<<<e.dot_blocks, kThreads, 0, e.stream>>>(
+      (float)alpha, p, q, dx, r, n, mask, (float)(1.0 / (f.kT * e.g.dV)), z, e.g.NR,
+      e.dot_partials, e.dot_counter, e.results);
+  e.post(kslot<float>(kK_newton_update));
+  return e.read_results(2, out_host, "newton_update");
 }
 
 int Engine::dots(int k, const double *const *a, const double *const *b, double *out_host) {
@@ -3227,10 +3315,13 @@ int Engine::axpy32(double alpha, const float *x, float *y) {
   return e.check("axpy");
 }
 
-int Engine::to_f32(const double *a, float *b, long long n) {
+int Engine::to_f32(const double *a, float *b, long long n, double scale) {
   EngineImpl &e = *impl_;
   if (n < 0) n = e.g.NR;
-  k_to_f32<<<e.dot_blocks, kThreads, 0, e.stream>>>(a, b, (int)n);
+  if (scale == 1.0)
+    k_to_f32<<<e.dot_blocks, kThreads, 0, e.stream>>>(a, b, (int)n);
+  else
+    k_to_f32_scaled<<<e.dot_blocks, kThreads, 0, e.stream>>>(a, scale, b, (int)n);
   return e.check("to_f32");
 }
 

@@ -170,7 +170,15 @@ class Engine {
                      double *out_host);                                 // ... and h.d
   int copy32(const float *src, float *dst);
   int axpy32(double alpha, const float *x, float *y);                   // y += alpha x
-  int to_f32(const double *a, float *b, long long n = -1);              // n = -1: NR
+  int to_f32(const double *a, float *b, long long n = -1, double scale = 1.0);  // b = scale a
+  // The Newton step's linear CG on FP32 vectors (f32_vectors_ok): H dx
+  // with dx.out; z = M^-1 r with r.z; the fused update of newton_update.
+  int hvp32(const FmtSpec &f, const float *dx, const float *mask, float *out, double *pq_host);
+  int diag_precond_dot32(const FmtSpec &f, const float *n, const float *r, const float *mask,
+                         float *z, double *rz_host);
+  int newton_update32(const FmtSpec &f, const float *n, double alpha, const float *p,
+                      const float *q, float *dx, float *r, const float *mask, float *z,
+                      double *out_host);
   int to_f64(const float *a, double *b, long long n = -1);
 
   // Vector kernels (NR-long device vectors).

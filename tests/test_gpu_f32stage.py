@@ -1,7 +1,8 @@
-"""The mixed form's FP32 stage on FP32 vectors (the secant CG with the density
-preconditioner, on grids whose z lines the warp transforms take: Nz = 32,
-64, 128, 256).  The stage's preconditioner, direction and step kernels run
-on FP32 vectors (their launches are counted under the FP32 kinds, none
+"""The mixed form on FP32 vectors (on grids whose z lines the warp transforms
+take: Nz = 32, 64, 128, 256): the FP32 stage (the secant CG with the
+density preconditioner) and the Newton refinement's linear CG keep their
+vectors in FP32.  Their preconditioner, direction, step and update kernels
+run on FP32 vectors (their launches are counted under the FP32 kinds, none
 under the FP64 ones), the solve meets the FP64 gradient tolerance at the
 profile of a tightly converged FP64 solve, and a run checkpointed inside
 the FP32 stage and restored into a fresh minimiser continues
@@ -66,6 +67,7 @@ def test_fp32_stage_on_fp32_vectors_meets_fp64_tolerance(k):
         n = _launches(g.L, g)
         assert n["precond_dots_f32"] > 0 and n["axpy_f32"] > 0
         assert n["precond_dots"] == 0  # no FP64-vector stage ran
+        assert n["newton_update_f32"] > 0 and n["newton_update"] == 0
         # the stop test is the FP64 gradient: check it independently
         _, g64, _ = f64.energy_grad(x)
         assert np.linalg.norm(g64) < gtol
