@@ -14,7 +14,7 @@ ERR_ARG, ERR_CUDA, ERR_NAN, ERR_LINESEARCH, ERR_MAXITER, ERR_NOMEM, ERR_TIMEOUT 
 TERM_HS, TERM_IDEAL, TERM_MU, TERM_VEXT, TERM_MASK, TERM_VEFF, TERM_SAFT = 1, 2, 4, 8, 16, 32, 64
 NTERMS = 6
 LS_SECANT, LS_QUADRATIC_REF, LS_NEW_API = 0, 1, 2
-PC_NONE, PC_FUNCTIONAL, PC_DENSITY = 0, 1, 2
+PC_NONE, PC_FUNCTIONAL, PC_DENSITY, PC_STRUCTURE = 0, 1, 2, 3
 HS_WB_NOTENSOR, HS_RF, HS_WB_MARK2, HS_WB_TENSOR, HS_TARAZONA = 0, 1, 2, 3, 4
 CONTACT_GSIGMA_S, CONTACT_GSIGMA_A, CONTACT_GROSS, CONTACT_YUWU, CONTACT_YUWU_S = 0, 1, 2, 3, 4
 
@@ -30,7 +30,7 @@ EXPORTS = (
     "deft_fmt_create", "deft_fmt_destroy", "deft_fmt_set_params", "deft_fmt_set_vext",
     "deft_fmt_set_mask", "deft_fmt_energy", "deft_fmt_energy_grad", "deft_fmt_energy_grad_pgrad",
     "deft_fmt_weighted", "deft_fmt_contact", "deft_fmt_set_saft",
-    "deft_fmt_hessian_vector",
+    "deft_fmt_hessian_vector", "deft_fmt_precondition",
     "deft_find_chemical_potential",
     "deft_fmt_energy_grad_noalloc", "deft_noalloc_scratch_bytes",
     "deft_cg_create", "deft_cg_destroy", "deft_cg_set_params", "deft_cg_set_x", "deft_cg_get_x", "deft_cg_x_device",
@@ -131,6 +131,7 @@ def load():
         "deft_fmt_contact": (ctypes.c_int, [_vp, _dp, ctypes.c_int, ctypes.c_int, _dp]),
         "deft_fmt_set_saft": (ctypes.c_int, [_vp, _dp]),
         "deft_fmt_hessian_vector": (ctypes.c_int, [_vp, _dp, _dp, ctypes.c_int, _dp]),
+        "deft_fmt_precondition": (ctypes.c_int, [_vp, _dp, _dp, ctypes.c_int, _dp, _dp]),
         "deft_find_chemical_potential": (ctypes.c_int, [ctypes.c_double, ctypes.c_double,
                                                         ctypes.c_double, _dp]),
         "deft_fmt_energy_grad_noalloc": (ctypes.c_int, [_dp, ctypes.c_int, ctypes.c_int,

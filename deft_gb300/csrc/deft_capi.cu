@@ -787,6 +787,35 @@ int deft_fmt_hessian_vector(deft_fmt *f, const double *n, const double *dx, int 
   return sync(g->ctx);
 }
 
+int deft_fmt_precondition(deft_fmt *f, const double *n, const double *r, int on_device, double *z,
+                          double *bulk_out) {
+  if (!f || !n || !r || !z) return set_err(DEFT_ERR_ARG, "NULL argument");
+  if (int s = check_terms(f)) return s;
+  const deft::FmtSpec spec = spec_of(f);
+  if ((f->p.terms & DEFT_TERM_VEFF) || is_tensor(f) || has_saft(f) ||
+      !f->grid->eng->structure_ok(spec))
+    return set_err(DEFT_ERR_ARG,
+                   "the structure preconditioner needs the White Bear, Rosenfeld or mark II "
+                   "hard-sphere and ideal-gas terms in the density variable (no tensor or SAFT "
+                   "terms) and Nz = 32, 64, 128 or 256");
+  deft_grid *g = f->grid;
+  cudaSetDevice(g->ctx->device);
+  const double *ns, *rs;
+  if (int s = stage_in(g, n, on_device, g->in_buf, &ns)) return s;
+  if (int s = stage_in(g, r, on_device, g->out_buf, &rs)) return s;
+  double *dst = on_device ? z : f->g_buf;
+  const double *mask = (spec.terms & DEFT_TERM_MASK) ? f->mask : nullptr;
+  double o3[3];
+  if (g->eng->pc_apply(spec, ns, rs, mask, dst, rs, nullptr, o3)) return eng_err(g->eng);
+  if (bulk_out) *bulk_out = g->eng->bulk_density(spec);
+  if (!on_device) {
+    cudaError_t e = cudaMemcpyAsync(z, dst, sizeof(double) * nr(g), cudaMemcpyDeviceToHost,
+                                    g->ctx->stream);
+    if (e != cudaSuccess) return cuda_err(e, "device-to-host copy");
+  }
+  return sync(g->ctx);
+}
+
 int deft_find_chemical_potential(double R, double kT, double nb, double *mu_out) {
   if (!mu_out || !(R > 0) || !(kT > 0) || !(nb > 0))
     return set_err(DEFT_ERR_ARG, "R, kT and nb must be positive");
@@ -872,12 +901,19 @@ static int check_cg_params(const deft_fmt *f, const deft_cg_params *p) {
   if (p->linesearch != DEFT_LS_SECANT && p->linesearch != DEFT_LS_QUADRATIC_REF &&
       p->linesearch != DEFT_LS_NEW_API)
     return set_err(DEFT_ERR_ARG, "unknown line search");
-  if (p->preconditioned < DEFT_PC_NONE || p->preconditioned > DEFT_PC_DENSITY)
+  if (p->preconditioned < DEFT_PC_NONE || p->preconditioned > DEFT_PC_STRUCTURE)
     return set_err(DEFT_ERR_ARG, "unknown preconditioner");
-  if (p->preconditioned == DEFT_PC_DENSITY &&
+  if (p->preconditioned >= DEFT_PC_DENSITY &&
       (p->linesearch != DEFT_LS_SECANT || (f->p.terms & DEFT_TERM_VEFF)))
     return set_err(DEFT_ERR_ARG,
-                   "the density preconditioner needs the secant search and the density variable");
+                   "the density and structure preconditioners need the secant search and the "
+                   "density variable");
+  if (p->preconditioned == DEFT_PC_STRUCTURE &&
+      (is_tensor(f) || has_saft(f) || !f->grid->eng->structure_ok(spec_of(f))))
+    return set_err(DEFT_ERR_ARG,
+                   "the structure preconditioner needs the White Bear, Rosenfeld or mark II "
+                   "hard-sphere and ideal-gas terms (no tensor or SAFT terms) and Nz = 32, 64, "
+                   "128 or 256");
   return DEFT_OK;
 }
 
@@ -1022,11 +1058,16 @@ const double *active_mask(const deft_fmt *f) {
   return (f->p.terms & DEFT_TERM_MASK) ? f->mask : nullptr;
 }
 
-// (With DEFT_PC_DENSITY, pg is formed where the step uses it, together with
-// its dot products: step_secant.)
+// With the density or structure preconditioner, pg is formed where the step
+// uses it, together with its dot products (step_secant).
+bool pg_in_step(const deft_cg *c) {
+  return c->pg && (c->p.preconditioned == DEFT_PC_DENSITY ||
+                   c->p.preconditioned == DEFT_PC_STRUCTURE);
+}
+
 int cg_eval(deft_cg *c, const deft::FmtSpec &spec) {
   double E;
-  const bool pcd = c->pg && c->p.preconditioned == DEFT_PC_DENSITY;
+  const bool pcd = pg_in_step(c);
   if (int s = fmt_eval(c->f, spec, c->x, c->g, pcd ? nullptr : c->pg, &E, nullptr)) return s;
   c->evals++;
   if (spec.precision == deft::kPrecisionFP64) c->evals_fp64++;
@@ -1052,7 +1093,7 @@ int cg_eval_dots(deft_cg *c, const deft::FmtSpec &spec, int k, const double *con
   if (e->energy_grad_dots(spec, c->x, c->f->V, c->f->mask, c->g, &E, k, a, b, out,
                          c->f->last_terms))
     return eng_err(e);
-  if (c->pg && c->p.preconditioned != DEFT_PC_DENSITY && e->copy(c->g, c->pg)) return eng_err(e);
+  if (c->pg && !pg_in_step(c) && e->copy(c->g, c->pg)) return eng_err(e);
   c->evals++;
   if (spec.precision == deft::kPrecisionFP64) c->evals_fp64++;
   c->last_eval_mixed = spec.precision != deft::kPrecisionFP64;
@@ -1096,7 +1137,7 @@ int cg_axpy(deft_cg *c, double a, const double *v) {
 // The FP32 stage of the mixed form under the density preconditioner: first
 // trial at the last accepted step, acceptance at DEFT_SECANT_C2_MIXED.
 bool fast_stage(const deft_cg *c, const deft::FmtSpec &spec) {
-  return spec.precision != deft::kPrecisionFP64 && c->p.preconditioned == DEFT_PC_DENSITY;
+  return spec.precision != deft::kPrecisionFP64 && pg_in_step(c);
 }
 
 // (C++ linkage: overloads and templates inside the C API's block)
@@ -1166,17 +1207,34 @@ int v_scal_add_dot(Engine *e, double beta, float *d, double alpha, const float *
 int v_copy(Engine *e, const double *src, double *dst) { return e->copy(src, dst); }
 int v_copy(Engine *e, const float *src, float *dst) { return e->copy32(src, dst); }
 
-// pg = M^-1 g (M^-1 = n / (kT dV) on the active points) with pg.g, pg.g_old.
+// pg = M^-1 g with pg.g, pg.g_old: the density preconditioner
+// (M^-1 = n / (kT dV) on the active points) or the structure one.
 int cg_precond_dots(deft_cg *c, const deft::FmtSpec &spec, const double *, double *o) {
-  return eng_of(c)->precond_dots(spec, c->x, c->g, active_mask(c->f), c->pg, c->gold, o)
-             ? eng_err(eng_of(c))
-             : DEFT_OK;
+  Engine *e = eng_of(c);
+  if (c->p.preconditioned == DEFT_PC_STRUCTURE) {
+    double o3[3];
+    if (e->pc_apply(spec, c->x, c->g, active_mask(c->f), c->pg, c->g, c->gold, o3))
+      return eng_err(e);
+    o[0] = o3[0];
+    o[1] = o3[1];
+    return DEFT_OK;
+  }
+  return e->precond_dots(spec, c->x, c->g, active_mask(c->f), c->pg, c->gold, o) ? eng_err(e)
+                                                                                 : DEFT_OK;
 }
 int cg_precond_dots(deft_cg *c, const deft::FmtSpec &spec, const float *, double *o) {
+  Engine *e = eng_of(c);
   const float *mask = active_mask(c->f) ? c->mask32 : nullptr;
-  return eng_of(c)->precond_dots32(spec, c->x32, c->g32, mask, c->pg32, c->gold32, o)
-             ? eng_err(eng_of(c))
-             : DEFT_OK;
+  if (c->p.preconditioned == DEFT_PC_STRUCTURE) {
+    double o3[3];
+    if (e->pc_apply32(spec, c->x32, c->g32, mask, c->pg32, c->g32, c->gold32, o3))
+      return eng_err(e);
+    o[0] = o3[0];
+    o[1] = o3[1];
+    return DEFT_OK;
+  }
+  return e->precond_dots32(spec, c->x32, c->g32, mask, c->pg32, c->gold32, o) ? eng_err(e)
+                                                                             : DEFT_OK;
 }
 
 #ifndef DEFT_F32_VECTORS
@@ -1201,7 +1259,7 @@ bool f32_switch() {
 }
 bool f32_stage(deft_cg *c, const deft::FmtSpec &spec) {
   return f32_switch() && spec.precision == deft::kPrecisionMixed && c->pg &&
-         c->p.preconditioned == DEFT_PC_DENSITY && !(c->f->p.terms & DEFT_TERM_VEFF) &&
+         pg_in_step(c) && !(c->f->p.terms & DEFT_TERM_VEFF) &&
          !is_tensor(c->f) && !has_saft(c->f) && eng_of(c)->f32_vectors_ok(spec);
 }
 
@@ -1351,8 +1409,8 @@ int step_secant(deft_cg *c, deft_cg_status *st, const deft::FmtSpec &spec, doubl
     // Preconditioned Polak-Ribiere (src/ConjugateGradient.cpp:115-160):
     // beta = pg.(g - g_old) / (pg_old.g_old), d = -pg + beta d
     double o[2];
-    if (c->p.preconditioned == DEFT_PC_DENSITY) {
-      // pg = M^-1 g, M^-1 = n / (kT dV), formed with its two dot products
+    if (pg_in_step(c)) {
+      // pg = M^-1 g, formed with its two dot products
       if (int s = cg_precond_dots(c, spec, pgv, o)) return s;
     } else if constexpr (std::is_same_v<V, double>) {
       const double *a[2] = {c->pg, c->pg};
@@ -1483,6 +1541,9 @@ int step_newton(deft_cg *c, deft_cg_status *st, const deft::FmtSpec &spec) {
   // FP32 too: the step only has to solve to 1e-5 of |g|, far above FP32
   // rounding, and the FP64 gradient at x + dx decides what is accepted.
   const double tol = std::fmax(1e-5 * st->gnorm, 0.05 * c->p.gtol);
+  // the linear CG's preconditioner: the structure one if the minimiser uses
+  // it, else the inverse ideal-gas curvature
+  const bool spc = c->p.preconditioned == DEFT_PC_STRUCTURE;
   if (f32_newton(c, spec)) {
     if (int s = f32_leave(c)) return s;
     if (int s = f32_buffers(c)) return s;
@@ -1491,8 +1552,12 @@ int step_newton(deft_cg *c, deft_cg_status *st, const deft::FmtSpec &spec) {
     const float *mask = c->f->mask ? c->mask32 : nullptr;
     const float *amask = active_mask(c->f) ? c->mask32 : nullptr;
     if (e->to_f32(c->x, n) || e->to_f32(c->g, r, -1, -1.0)) return eng_err(e);
-    double rz;
-    if (e->diag_precond_dot32(spec, n, r, amask, z, &rz) || e->copy32(z, p)) return eng_err(e);
+    double rz, o3[3];
+    if (spc ? e->pc_apply32(spec, n, r, amask, z, r, nullptr, o3)
+            : e->diag_precond_dot32(spec, n, r, amask, z, o3))
+      return eng_err(e);
+    rz = o3[0];
+    if (e->copy32(z, p)) return eng_err(e);
     c->have_g = false;
     if (cudaMemsetAsync(dx, 0, sizeof(float) * nr(c->f->grid), stream) != cudaSuccess)
       return set_err(DEFT_ERR_CUDA, "memset");
@@ -1502,11 +1567,23 @@ int step_newton(deft_cg *c, deft_cg_status *st, const deft::FmtSpec &spec) {
       c->hvps++;
       if (!(pq > 0)) break;
       const double alpha = rz / pq;
-      double o[2];
-      if (e->newton_update32(spec, n, alpha, p, q, dx, r, amask, z, o)) return eng_err(e);
-      if (std::sqrt(o[0]) < tol) break;
-      if (e->scal_add32(o[1] / rz, p, 1.0, z)) return eng_err(e);
-      rz = o[1];
+      double rr, rzn;
+      if (spc) {
+        // dx += alpha p, r -= alpha q; z = M^-1 r with r.z and r.r
+        if (e->newton_step32(alpha, p, q, dx, r) ||
+            e->pc_apply32(spec, n, r, amask, z, r, nullptr, o3))
+          return eng_err(e);
+        rr = o3[2];
+        rzn = o3[0];
+      } else {
+        double o[2];
+        if (e->newton_update32(spec, n, alpha, p, q, dx, r, amask, z, o)) return eng_err(e);
+        rr = o[0];
+        rzn = o[1];
+      }
+      if (std::sqrt(rr) < tol) break;
+      if (e->scal_add32(rzn / rz, p, 1.0, z)) return eng_err(e);
+      rz = rzn;
     }
     if (e->to_f64(dx, c->dxv)) return eng_err(e);
   } else {
@@ -1514,29 +1591,44 @@ int step_newton(deft_cg *c, deft_cg_status *st, const deft::FmtSpec &spec) {
     double *r = c->gold, *p = c->d, *q = c->q, *dx = c->dxv;
     double *z = c->g;  // the FP64 gradient is re-evaluated after the step
     if (e->scal_add(0.0, r, -1.0, c->g)) return eng_err(e);
-    if (e->diag_precond(spec, c->x, r, active_mask(c->f), z) || e->copy(z, p)) return eng_err(e);
-    c->have_g = false;
-    if (cudaMemsetAsync(dx, 0, bytes, stream) != cudaSuccess)
-      return set_err(DEFT_ERR_CUDA, "memset");
-    double rz;
-    {
+    double rz, o3[3];
+    if (spc) {
+      if (e->pc_apply(spec, c->x, r, active_mask(c->f), z, r, nullptr, o3)) return eng_err(e);
+      rz = o3[0];
+    } else {
+      if (e->diag_precond(spec, c->x, r, active_mask(c->f), z)) return eng_err(e);
       const double *a[1] = {r};
       const double *b[1] = {z};
       if (e->dots(1, a, b, &rz)) return eng_err(e);
     }
+    if (e->copy(z, p)) return eng_err(e);
+    c->have_g = false;
+    if (cudaMemsetAsync(dx, 0, bytes, stream) != cudaSuccess)
+      return set_err(DEFT_ERR_CUDA, "memset");
     for (int k = 0; k < 400 && rz > 0; k++) {
       double pq;  // p.q, taken by the product's last kernel
       if (e->hvp(spec, p, c->f->mask, q, &pq)) return eng_err(e);
       c->hvps++;
       if (!(pq > 0)) break;  // no positive curvature along p: keep the step so far
       const double alpha = rz / pq;
-      // dx += alpha p, r -= alpha q, z = M^-1 r, (r.r, r.z) in one pass
-      double o[2];
-      if (e->newton_update(spec, c->x, alpha, p, q, dx, r, active_mask(c->f), z, o))
-        return eng_err(e);
-      if (std::sqrt(o[0]) < tol) break;
-      if (e->scal_add(o[1] / rz, p, 1.0, z)) return eng_err(e);
-      rz = o[1];
+      double rr, rzn;
+      if (spc) {
+        if (e->newton_step(alpha, p, q, dx, r) ||
+            e->pc_apply(spec, c->x, r, active_mask(c->f), z, r, nullptr, o3))
+          return eng_err(e);
+        rr = o3[2];
+        rzn = o3[0];
+      } else {
+        // dx += alpha p, r -= alpha q, z = M^-1 r, (r.r, r.z) in one pass
+        double o[2];
+        if (e->newton_update(spec, c->x, alpha, p, q, dx, r, active_mask(c->f), z, o))
+          return eng_err(e);
+        rr = o[0];
+        rzn = o[1];
+      }
+      if (std::sqrt(rr) < tol) break;
+      if (e->scal_add(rzn / rz, p, 1.0, z)) return eng_err(e);
+      rz = rzn;
     }
   }
   const double *dx = c->dxv;

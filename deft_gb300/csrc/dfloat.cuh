@@ -82,7 +82,7 @@ __device__ __forceinline__ dfl operator/(dfl a, dfl b) {
   const dfl r2 = a - q * b;
   return q + dfl(r2.hi * rb, 0.f);
 }
-__device__ __forceinline__ double to_double(dfl a) { return (double)a.hi + (double)a.lo; }
+__host__ __device__ __forceinline__ double to_double(dfl a) { return (double)a.hi + (double)a.lo; }
 
 // Complex double-float: 16 bytes, the size of a double2, so the FP64 form's
 // tiles and spectra keep their shapes.

@@ -387,7 +387,76 @@ struct LocalArgs {
   double R, kT, mu, nQ, inv_nQ, dV;
   WbRadius wr;
   int terms;
+  // Bulk structure-factor preconditioner: 1/nb of the bulk density in
+  // equilibrium at mu, and the bulk Hessian per kT dV at |k|,
+  //   H(k) = 1/nb + h33 w3^2 + 2 h32 w3 w2 + h22 w2^2 + hvv k^2 wv^2,
+  // with h the Hessian of phi at the bulk weighted densities (0: off).
+  float pc_inv_nb, pc_h33, pc_h32x2, pc_h22, pc_hvv, pc_inv_kTdV;
 };
+
+// The bulk density nb in equilibrium with the chemical-potential term of f
+// (its integrand is mu n, so kT ln(nb/nQ) + kT dphi/dn_a w_a(0) = -mu;
+// w3(0) = 4 pi R^3 / 3,
+// w2(0) = 4 pi R^2; monotone in nb, solved by Newton's method safeguarded by
+// bisection on the packing fraction) and the bulk Hessian coefficients of
+// LocalArgs.  Only for the White Bear / Rosenfeld / mark II kinds with the
+// ideal gas on; otherwise the coefficients stay 0 (preconditioner off).
+// Returns nb (0 when off).
+double bulk_structure(const FmtSpec &f, double nQ, WbRadius wr, LocalArgs &la) {
+  if (!(f.terms & kTermHS) || !(f.terms & kTermIdeal) || f.hs > kHsMarkII || !(f.R > 0) ||
+      !(f.kT > 0))
+    return 0.0;
+  const double w30 = 4 * M_PI * f.R * f.R * f.R / 3, w20 = 4 * M_PI * f.R * f.R;
+  const double target = ((f.terms & kTermMu) ? -f.mu : 0.0) / f.kT;
+  auto mu_of = [&](double nb, double *dmu) {
+    double phi[3], d[5], h[10];
+    wb_phi<double>(wr, nb * w30, nb * w20, 0.0, 0.0, 0.0, phi, d);
+    wb_hess<double>(wr, nb * w30, nb * w20, 0.0, 0.0, 0.0, h);
+    *dmu = 1 / nb + h[0] * w30 * w30 + 2 * h[1] * w30 * w20 + h[5] * w20 * w20;
+    return log(nb / nQ) + d[0] * w30 + d[1] * w20;
+  };
+  double lo = 1e-12 / w30, hi = 0.999 / w30, nb = 0.3 / w30;
+  for (int it = 0; it < 200; it++) {
+    double dmu;
+    const double r = mu_of(nb, &dmu) - target;
+    if (r > 0) hi = nb;
+    else lo = nb;
+    double nn = nb - r / dmu;
+    if (!(nn > lo && nn < hi)) nn = 0.5 * (lo + hi);
+    if (std::fabs(nn - nb) <= 1e-15 * nb) {
+      nb = nn;
+      break;
+    }
+    nb = nn;
+  }
+  double h[10];
+  wb_hess<double>(wr, nb * w30, nb * w20, 0.0, 0.0, 0.0, h);
+  la.pc_inv_nb = (float)(1 / nb);
+  la.pc_h33 = (float)h[0];
+  la.pc_h32x2 = (float)(2 * h[1]);
+  la.pc_h22 = (float)h[5];
+  la.pc_hvv = (float)h[9];
+  la.pc_inv_kTdV = (float)(1 / (f.kT * la.dV));
+  return nb;
+}
+
+// The structure preconditioner M^-1 r = s F^-1[ P(k) F[s r] ] with
+// s = sqrt(n / nb) on the active points (0 elsewhere) and P = 1 / H_b(k),
+// the inverse bulk Hessian (kT dV H(k) of LocalArgs, analytic weights at
+// |k| with the smearing of the convolutions); scale = 1/N for the
+// unnormalised transforms.  In a uniform fluid at nb M is the Hessian
+// itself; at large k, P -> nb / (kT dV), the density preconditioner.
+__device__ __forceinline__ float pc_point_scale(float m, float nv, float inv_nb) {
+  return precond_active(m, nv) ? sqrtf(nv * inv_nb) : 0.0f;
+}
+__device__ __forceinline__ float pc_mult(float k2, const LocalArgs &la, float dr, float scale) {
+  float w3, w2, wv;
+  weights_at_f(k2, (float)la.R, dr, 1.0f, w3, w2, wv);
+  float h = la.pc_inv_nb + la.pc_h33 * w3 * w3 + la.pc_h32x2 * w3 * w2 + la.pc_h22 * w2 * w2 +
+            la.pc_hvv * k2 * wv * wv;
+  h = fmaxf(h, 1e-3f * la.pc_inv_nb);
+  return scale * la.pc_inv_kTdV / h;
+}
 
 // Dot products of the new gradient with up to k <= 3 vectors, taken by the
 // kernel that writes the gradient (b[i] == nullptr: the gradient itself);
@@ -728,6 +797,62 @@ __global__ void __launch_bounds__(pencil_threads<W>(), W >= 16 ? 1 : 2)
     const int sW = W * J;
 #pragma unroll
     for (int m = 0; m < 16; m++) dst[m * sW] = acc[m];
+  }
+}
+
+// The structure preconditioner along x, in place on one field: x-FFT, times
+// P(k) / N, inverse x-FFT (columns as in k_x_conv_fwd_pencil).
+template <int W>
+__global__ void __launch_bounds__(pencil_threads<W>())
+    k_x_pc_pencil(float2 *data, Geom g, const float2 *__restrict__ tw,
+                  const LocalArgs *__restrict__ lap) {
+  constexpr int G = pencil_groups<W>();
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const LocalArgs la = *lap;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, w = warp % W, grp = warp / W;
+  float2 *xs = reinterpret_cast<float2 *>(smem_raw) + grp * pencil_xs_elems<W>();
+  const int J = g.Ny * g.NzH;
+  const int j = (blockIdx.x * G + grp) * 32 + lane;
+  const bool act = j < J;
+  int y, kz;
+  fdivmod(act ? j : 0, g.fNzH, y, kz);
+  float2 v[16];
+  float2 *col = data + j + w * J;
+  const int sW = W * J;
+#pragma unroll
+  for (int m = 0; m < 16; m++) v[m] = act ? col[m * sW] : make_float2(0.f, 0.f);
+  pencil_n2s<float, -1, W>(v, xs, w, lane, tw);
+  const float yw = (float)wrapm(y, g.Ny), zf = (float)kz;
+  float kc[3];
+#pragma unroll
+  for (int c = 0; c < 3; c++) kc[c] = g.Bmf[3 * c + 1] * yw + g.Bmf[3 * c + 2] * zf;
+#pragma unroll
+  for (int q = 0; q < 16; q++) {
+    const float xw = (float)wrapm(pencil_freq<W>(w, q), g.Nx);
+    const float kx = g.Bmf[0] * xw + kc[0], ky = g.Bmf[3] * xw + kc[1], kzz = g.Bmf[6] * xw + kc[2];
+    const float p = pc_mult(kx * kx + ky * ky + kzz * kzz, la, (float)g.dr, (float)g.scale);
+    v[q] = make_float2(v[q].x * p, v[q].y * p);
+  }
+  pencil_s2n<float, +1, W>(v, xs, w, lane, tw);
+  if (act) {
+#pragma unroll
+    for (int m = 0; m < 16; m++) col[m * sW] = v[m];
+  }
+}
+
+// The same multiplication on an x-transformed spectrum (layout x Ny NzH +
+// y NzH + kz), for grids whose x length the pencil kernels do not take.
+__global__ void k_pc_mult(float2 *data, Geom g, const LocalArgs *__restrict__ lap) {
+  const LocalArgs la = *lap;
+  const int J = g.Ny * g.NzH;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < g.NC; i += gridDim.x * blockDim.x) {
+    const int x = i / J, j = i - x * J;
+    int y, z;
+    fdivmod(j, g.fNzH, y, z);
+    const float kx = kcomp_t<float>(g, 0, x, y, z), ky = kcomp_t<float>(g, 1, x, y, z),
+                kz = kcomp_t<float>(g, 2, x, y, z);
+    const float p = pc_mult(kx * kx + ky * ky + kz * kz, la, (float)g.dr, (float)g.scale);
+    data[i] = make_float2(data[i].x * p, data[i].y * p);
   }
 }
 
@@ -1295,6 +1420,81 @@ __global__ void __launch_bounds__(32 * kZWarps)
   }
 }
 
+// The structure preconditioner along z, into the spectrum: r2c of s r
+// (s = sqrt(n / nb) on the active points).
+template <int E, typename R>
+__global__ void __launch_bounds__(32 * kZWarps)
+    k_pc_in_warp(const R *__restrict__ rv, const R *__restrict__ n, const R *__restrict__ mask,
+                 float2 *__restrict__ out, Geom g, const float2 *__restrict__ tw,
+                 const LocalArgs *__restrict__ lap) {
+  constexpr int N = 32 * E, NzH = N / 2 + 1;
+  const float inv_nb = lap->pc_inv_nb;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  float2 *wb = reinterpret_cast<float2 *>(smem_raw) + warp * warp_buf_elems<E>();
+  const int l0 = 2 * (blockIdx.x * kZWarps + warp);
+  float2 w[4];
+  warp_stage_tw<-1, E>(tw, lane, w);
+  const bool a0 = l0 < g.lines, a1 = l0 + 1 < g.lines;
+  float2 v[E];
+#pragma unroll
+  for (int m = 0; m < E; m++) {
+    const size_t r = (size_t)l0 * N + lane + 32 * m;
+    float u0 = 0.f, u1 = 0.f;
+    if (a0) u0 = pc_point_scale(mask ? float(mask[r]) : 1.f, float(n[r]), inv_nb) * float(rv[r]);
+    if (a1)
+      u1 = pc_point_scale(mask ? float(mask[r + N]) : 1.f, float(n[r + N]), inv_nb) *
+           float(rv[r + N]);
+    v[m] = make_float2(u0, u1);
+  }
+  warp_n2s<-1, E>(v, lane, tw, w);
+  warp_unpack_store<E>(v, lane, 1.0f, wb, out + (size_t)l0 * NzH, zwarp_nvalid(l0, g));
+}
+
+// ... and out of it: z = s c2r, with the sums z.a, z.b (b may be null) and
+// a.a, reduced by the last block into out[0..3).
+template <int E, typename R>
+__global__ void __launch_bounds__(32 * kZWarps)
+    k_pc_out_warp(const float2 *__restrict__ in, const R *__restrict__ n,
+                  const R *__restrict__ mask, R *__restrict__ z, const R *__restrict__ a,
+                  const R *__restrict__ b, Geom g, const float2 *__restrict__ tw,
+                  const LocalArgs *__restrict__ lap, double *partials, unsigned int *counter,
+                  double *out) {
+  constexpr int N = 32 * E, NzH = N / 2 + 1;
+  const float inv_nb = lap->pc_inv_nb;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  float2 *wb = reinterpret_cast<float2 *>(smem_raw) + warp * warp_buf_elems<E>();
+  const int l0 = 2 * (blockIdx.x * kZWarps + warp);
+  float2 v[E];
+  {
+    float2 w[4];
+    warp_stage_tw<+1, E>(tw, lane, w);
+    warp_load_pack<E>(in + (size_t)l0 * NzH, zwarp_nvalid(l0, g), wb, lane, v);
+    warp_s2n<+1, E>(v, lane, tw, w);
+  }
+  float acc[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+  for (int half = 0; half < 2; half++) {
+    const int line = l0 + half;
+    if (line >= g.lines) continue;
+#pragma unroll
+    for (int m = 0; m < E; m++) {
+      const size_t r = (size_t)line * N + lane + 32 * m;
+      const float s = pc_point_scale(mask ? float(mask[r]) : 1.f, float(n[r]), inv_nb);
+      const float zv = s * (half ? v[m].y : v[m].x);
+      z[r] = R(zv);
+      const float av = float(a[r]);
+      acc[0] += zv * av;
+      if (b) acc[1] += zv * float(b[r]);
+      acc[2] += av * av;
+    }
+  }
+  __shared__ double red[32 * 3];
+  double accd[3] = {acc[0], acc[1], acc[2]};
+  finish_dots<3>(accd, red, partials, counter, out);
+}
+
 // Warp form of k_z_phi: c2r of the five weighted densities of the pair, phi
 // and the local energy terms at its 2N points, per-block energies, and
 // (GRAD) r2c of the five partials dV kT dphi/dn_a in place.
@@ -1678,6 +1878,17 @@ __global__ void k_to_f32_scaled(const double *__restrict__ a, double s, float *_
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
     b[i] = (float)(s * a[i]);
 }
+// The Newton step's linear CG update without the preconditioner (which the
+// structure preconditioner applies afterwards): dx += alpha p, r -= alpha q.
+template <typename R>
+__global__ void k_newton_step(R alpha, const R *__restrict__ p, const R *__restrict__ q,
+                              R *__restrict__ dx, R *__restrict__ r, int N) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+    dx[i] += alpha * p[i];
+    r[i] -= alpha * q[i];
+  }
+}
+
 // The Newton step's linear CG on FP32 vectors: z = M^-1 r with r.z, and
 // the fused update of k_newton_update (per-thread FP32 sums, FP64 across
 // threads and blocks in a fixed order).
@@ -1981,13 +2192,14 @@ enum KernelId {
   kK_z_r2c, kK_z_c2r, kK_y_fft1, kK_y_fft5, kK_x_fft, kK_x_conv_fwd, kK_x_conv_adj, kK_z_phi_grad,
   kK_z_phi_energy, kK_z_grad, kK_local_energy, kK_reduce_terms, kK_dots, kK_axpy, kK_scal_add,
   kK_weight_table, kK_z_hess, kK_z_jac, kK_z_hvp_out, kK_veff_density, kK_veff_grad,
-  kK_diag_precond, kK_precond_dots, kK_newton_update, kK_device_control, kNumKernels
+  kK_diag_precond, kK_precond_dots, kK_newton_update, kK_device_control, kK_struct_pc,
+  kNumKernels
 };
 const char *const kKernelNames[kNumKernels] = {
     "z_r2c", "z_c2r", "y_fft_1field", "y_fft_5fields", "x_fft", "x_conv_fwd", "x_conv_adj", "z_phi_grad",
     "z_phi_energy", "z_grad", "local_energy", "reduce_terms", "dots", "axpy", "scal_add",
     "weight_table", "z_hess", "z_jac", "z_hvp_out", "veff_density", "veff_grad",
-    "diag_precond", "precond_dots", "newton_update", "device_control"};
+    "diag_precond", "precond_dots", "newton_update", "device_control", "struct_pc"};
 
 // Calls f(std::integral_constant<int, RN>()) with RN = the plan's length
 // when it is an FP32 plan marked for the register-resident transform, else
@@ -2314,6 +2526,7 @@ class EngineImpl {
       set_smem(k_y_pencil<+1, W>, pencil_smem<W>(false));
       set_smem(k_x_conv_fwd_pencil<W>, pencil_smem<W>(true));
       set_smem(k_x_conv_adj_pencil<W>, pencil_smem<W>(true));
+      set_smem(k_x_pc_pencil<W>, pencil_smem<W>(false));
     };
     smemp(std::integral_constant<int, 2>());
     smemp(std::integral_constant<int, 4>());
@@ -2327,6 +2540,10 @@ class EngineImpl {
       set_smem(k_z_grad_warp<E, float>, zwarp_smem<E>());
       set_smem(k_z_hvp_out_warp<E>, zwarp_smem<E>());
       set_smem(k_z_hvp_out_warp<E, float>, zwarp_smem<E>());
+      set_smem(k_pc_in_warp<E, float>, zwarp_smem<E>());
+      set_smem(k_pc_in_warp<E, double>, zwarp_smem<E>());
+      set_smem(k_pc_out_warp<E, float>, zwarp_smem<E>());
+      set_smem(k_pc_out_warp<E, double>, zwarp_smem<E>());
       set_smem(k_z_phi_warp<true, E>, zwarp_smem<E>(5));
       set_smem(k_z_phi_warp<false, E>, zwarp_smem<E>(5));
       set_smem(k_z_jac_warp<E>, zwarp_smem<E>(5));
@@ -2631,8 +2848,32 @@ class EngineImpl {
     la.wr.inv_4piR2 = 1.0 / (4 * M_PI * f.R * f.R);
     la.wr.kind = f.hs;
     la.terms = f.terms;
+    if (f.terms & kTermHS) {
+      // the bulk solve runs once per (mu, kT, R, kind)
+      if (!(pc_key_valid && pc_key.mu == f.mu && pc_key.kT == f.kT && pc_key.R == f.R &&
+            pc_key.hs == f.hs && pc_key.terms == f.terms && pc_key.dV == g.dV)) {
+        pc_la = la;
+        pc_nb = bulk_structure(f, la.nQ, la.wr, pc_la);
+        pc_key = PcKey{f.mu, f.kT, f.R, g.dV, f.hs, f.terms};
+        pc_key_valid = true;
+      }
+      la.pc_inv_nb = pc_la.pc_inv_nb;
+      la.pc_h33 = pc_la.pc_h33;
+      la.pc_h32x2 = pc_la.pc_h32x2;
+      la.pc_h22 = pc_la.pc_h22;
+      la.pc_hvv = pc_la.pc_hvv;
+      la.pc_inv_kTdV = pc_la.pc_inv_kTdV;
+    }
     return la;
   }
+  struct PcKey {
+    double mu, kT, R, dV;
+    int hs, terms;
+  };
+  mutable PcKey pc_key{};
+  mutable LocalArgs pc_la{};
+  mutable double pc_nb = 0;
+  mutable bool pc_key_valid = false;
 
   // Device copy of the functional parameters the kernels read; uploaded on
   // the stream (before any graph launch that reads it) when they change.
@@ -2932,6 +3173,78 @@ class EngineImpl {
   bool f32_vectors_ok(const FmtSpec &f) const {
     return f.precision == kPrecisionMixed && (f.terms & kTermHS) && zwarp<float>() &&
            !zwarp<float>(5);
+  }
+
+  // The structure preconditioner (DEFT_PC_STRUCTURE): White Bear kinds with
+  // the ideal gas, Nz that the warp z transforms take.
+  bool structure_ok(const FmtSpec &f) const {
+    return (f.terms & kTermHS) && (f.terms & kTermIdeal) && f.hs <= kHsMarkII && zwarp<float>();
+  }
+  // z = M^-1 r and (z.a, z.b, a.a) read back (b may be null); R = double or
+  // float vectors, FP32 transforms either way.
+  template <typename R>
+  int pc_apply(const FmtSpec &f, const R *n, const R *r, const R *mask, R *z, const R *a,
+               const R *b, double *out_host) {
+    if (!structure_ok(f)) {
+      err = "structure preconditioner: needs the hard-sphere (White Bear, Rosenfeld or mark II) "
+            "and ideal-gas terms and Nz = 32, 64, 128 or 256";
+      return -1;
+    }
+    if (upload_args(f)) return -1;
+    if (!(la_last.pc_inv_nb > 0)) {
+      err = "structure preconditioner: no bulk density for these parameters";
+      return -1;
+    }
+    const double *da[1] = {reinterpret_cast<const double *>(a)};
+    const double *db[1] = {reinterpret_cast<const double *>(b)};
+    const GraphKey key =
+        graph_key(std::is_same<R, double>::value ? 10 : 11, 4, f, n, r, mask, z, 1, da, db);
+    if (run_graphed(key, [&] { return pc_launch<R>(n, r, mask, z, a, b); })) return -1;
+    return read_results(3, out_host, "structure preconditioner");
+  }
+  template <typename R>
+  int pc_launch(const R *n, const R *r, const R *mask, R *z, const R *a, const R *b) {
+    float2 *w = reinterpret_cast<float2 *>(spec0<float>());
+    pre(kslot<float>(kK_struct_pc));
+    with_e(g.Nz, [&](auto ec) {
+      constexpr int E = decltype(ec)::value;
+      k_pc_in_warp<E, R><<<zwarp_blocks(), 32 * kZWarps, zwarp_smem<E>(), stream>>>(
+          r, n, mask, w, g, twz32(), la_dev);
+    });
+    post(kslot<float>(kK_struct_pc));
+    y_fft<float>(w, 1, -1);
+    if (pencil<float>(0)) {
+      pre(kslot<float>(kK_struct_pc));
+      with_w(g.Nx, [&](auto wc) {
+        constexpr int W = decltype(wc)::value;
+        const int cols = 32 * pencil_groups<W>();
+        k_x_pc_pencil<W><<<(g.Ny * g.NzH + cols - 1) / cols, pencil_threads<W>(),
+                           pencil_smem<W>(false), stream>>>(
+            w, g, reinterpret_cast<const float2 *>(plan<float>(0).tw), la_dev);
+      });
+      post(kslot<float>(kK_struct_pc));
+    } else {
+      pre(kslot<float>(kK_x_fft));
+      k_x_fft<float, -1><<<x_tiles(t32.Bx), kThreads, t32.smem_x2, stream>>>(w, g, pxf, t32.fBx,
+                                                                             1.0f);
+      post(kslot<float>(kK_x_fft));
+      pre(kslot<float>(kK_struct_pc));
+      k_pc_mult<<<dot_blocks, kThreads, 0, stream>>>(w, g, la_dev);
+      post(kslot<float>(kK_struct_pc));
+      pre(kslot<float>(kK_x_fft));
+      k_x_fft<float, +1><<<x_tiles(t32.Bx), kThreads, t32.smem_x2, stream>>>(w, g, pxf, t32.fBx,
+                                                                             1.0f);
+      post(kslot<float>(kK_x_fft));
+    }
+    y_fft<float>(w, 1, +1);
+    pre(kslot<float>(kK_struct_pc));
+    with_e(g.Nz, [&](auto ec) {
+      constexpr int E = decltype(ec)::value;
+      k_pc_out_warp<E, R><<<zwarp_blocks(), 32 * kZWarps, zwarp_smem<E>(), stream>>>(
+          w, n, mask, z, a, b, g, twz32(), la_dev, grad_partials, dot_counter, results);
+    });
+    post(kslot<float>(kK_struct_pc));
+    return check("structure preconditioner");
   }
 
   int hess_setup(const FmtSpec &f, const double *n) {
@@ -3264,6 +3577,39 @@ int Engine::diag_precond(const FmtSpec &f, const double *n, const double *r, con
 }
 
 bool Engine::f32_vectors_ok(const FmtSpec &f) const { return impl_->f32_vectors_ok(f); }
+
+bool Engine::structure_ok(const FmtSpec &f) const { return impl_->structure_ok(f); }
+
+double Engine::bulk_density(const FmtSpec &f) const {
+  impl_->local_args(f);
+  return impl_->pc_nb;
+}
+
+int Engine::pc_apply(const FmtSpec &f, const double *n, const double *r, const double *mask,
+                     double *z, const double *a, const double *b, double *out_host) {
+  return impl_->pc_apply<double>(f, n, r, mask, z, a, b, out_host);
+}
+
+int Engine::pc_apply32(const FmtSpec &f, const float *n, const float *r, const float *mask,
+                       float *z, const float *a, const float *b, double *out_host) {
+  return impl_->pc_apply<float>(f, n, r, mask, z, a, b, out_host);
+}
+
+int Engine::newton_step(double alpha, const double *p, const double *q, double *dx, double *r) {
+  EngineImpl &e = *impl_;
+  e.pre(kK_newton_update);
+  k_newton_step<double><<<e.dot_blocks, kThreads, 0, e.stream>>>(alpha, p, q, dx, r, e.g.NR);
+  e.post(kK_newton_update);
+  return e.check("newton_step");
+}
+
+int Engine::newton_step32(double alpha, const float *p, const float *q, float *dx, float *r) {
+  EngineImpl &e = *impl_;
+  e.pre(kslot<float>(kK_newton_update));
+  k_newton_step<float><<<e.dot_blocks, kThreads, 0, e.stream>>>((float)alpha, p, q, dx, r, e.g.NR);
+  e.post(kslot<float>(kK_newton_update));
+  return e.check("newton_step");
+}
 
 int Engine::eval32(const FmtSpec &f, const float *n, const float *V, const float *mask,
                    float *grad, double *E_host, double *terms_host, int kd,

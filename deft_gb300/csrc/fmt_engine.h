@@ -171,6 +171,21 @@ class Engine {
   int copy32(const float *src, float *dst);
   int axpy32(double alpha, const float *x, float *y);                   // y += alpha x
   int to_f32(const double *a, float *b, long long n = -1, double scale = 1.0);  // b = scale a
+  // The bulk structure-factor preconditioner (DEFT_PC_STRUCTURE):
+  // z = s F^-1[F[s r] / H_b(k)], s = sqrt(n / nb) on the active points
+  // (mask != 0, n > 0), H_b the Hessian of the uniform fluid at the bulk
+  // density nb in equilibrium at mu; FP32 transforms.  out_host[3] =
+  // (z.a, z.b, a.a) (b may be null).  structure_ok: hard spheres (White
+  // Bear, Rosenfeld, mark II) + ideal gas, Nz = 32, 64, 128 or 256.
+  bool structure_ok(const FmtSpec &f) const;
+  double bulk_density(const FmtSpec &f) const;  // the n_b the preconditioner uses (0: none)
+  int pc_apply(const FmtSpec &f, const double *n, const double *r, const double *mask, double *z,
+               const double *a, const double *b, double *out_host);
+  int pc_apply32(const FmtSpec &f, const float *n, const float *r, const float *mask, float *z,
+                 const float *a, const float *b, double *out_host);
+  // dx += alpha p, r -= alpha q (the linear CG step before a pc_apply).
+  int newton_step(double alpha, const double *p, const double *q, double *dx, double *r);
+  int newton_step32(double alpha, const float *p, const float *q, float *dx, float *r);
   // The Newton step's linear CG on FP32 vectors (f32_vectors_ok): H dx
   // with dx.out; z = M^-1 r with r.z; the fused update of newton_update.
   int hvp32(const FmtSpec &f, const float *dx, const float *mask, float *out, double *pq_host);

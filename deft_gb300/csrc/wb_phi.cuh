@@ -59,16 +59,16 @@ constexpr int kHsMarkII = 2;
 constexpr int kHsWhiteBearTensor = 3;
 constexpr int kHsTarazona = 4;
 
-template <typename T> __device__ __forceinline__ T wb_log(T x);
-template <> __device__ __forceinline__ double wb_log<double>(double x) { return log(x); }
-template <> __device__ __forceinline__ float wb_log<float>(float x) { return logf(x); }
+template <typename T> __host__ __device__ __forceinline__ T wb_log(T x);
+template <> __host__ __device__ __forceinline__ double wb_log<double>(double x) { return log(x); }
+template <> __host__ __device__ __forceinline__ float wb_log<float>(float x) { return logf(x); }
 // double-float log through the FP64 log (one FP64 log per point)
-template <> __device__ __forceinline__ dfl wb_log<dfl>(dfl x) { return dfl(log(to_double(x))); }
+template <> __host__ __device__ __forceinline__ dfl wb_log<dfl>(dfl x) { return dfl(log(to_double(x))); }
 
 // S, S', S'' at e; l = ln(1 - e) (computed once by the caller).
 template <typename T>
-__device__ __forceinline__ void wb_S(T e, T l, T &S, T &dS, T &d2S) {
-  if (fabs(e) < WbConst<T>::series_below) {
+__host__ __device__ __forceinline__ void wb_S(T e, T l, T &S, T &dS, T &d2S) {
+  if ((e < T(0) ? -e : e) < T(WbConst<T>::series_below)) {
     T s = T(1.5), ds = T(0), d2s = T(0);
     T pm2 = T(1), pm1 = T(1);  // e^(j-2) (from j = 2), e^(j-1)
 #pragma unroll
@@ -101,8 +101,8 @@ __device__ __forceinline__ void wb_S(T e, T l, T &S, T &dS, T &d2S) {
 // P2, P3 of the mark II functional and their first two derivatives;
 // l = ln(1 - e).
 template <typename T>
-__device__ __forceinline__ void m2_P(T e, T l, T P2[3], T P3[3]) {
-  if (fabs(e) < WbConst<T>::m2_below) {
+__host__ __device__ __forceinline__ void m2_P(T e, T l, T P2[3], T P3[3]) {
+  if ((e < T(0) ? -e : e) < T(WbConst<T>::m2_below)) {
     T p2 = T(0), dp2 = T(0), d2p2 = T(0), p3 = T(0), dp3 = T(0), d2p3 = T(0);
     T ekm3 = T(0);  // e^(k-3): read from k = 3 on, after the first shift
     T ekm2 = T(1), ekm1 = e, ek = e * e;  // e^(k-2), e^(k-1), e^k at k = 2
@@ -154,7 +154,7 @@ __device__ __forceinline__ void m2_P(T e, T l, T P2[3], T P3[3]) {
 // f2, f3 of the kind and their first two derivatives at e = n3
 // (u = 1/(1-e), l = ln(1-e)).
 template <typename T>
-__device__ __forceinline__ void hs_coeffs(int kind, T e, T u, T l, T f2[3], T f3[3]) {
+__host__ __device__ __forceinline__ void hs_coeffs(int kind, T e, T u, T l, T f2[3], T f3[3]) {
   const T u2 = u * u;
   if (kind == kHsMarkII) {
     T P2[3], P3[3];
@@ -194,7 +194,7 @@ struct WbRadius {
 
 // phi = (phi3, phi1, phi2); d = d phi / d(n3, n2, vx, vy, vz).
 template <typename T>
-__device__ __forceinline__ void wb_phi(const WbRadius &r, T n3, T n2, T vx, T vy, T vz, T phi[3],
+__host__ __device__ __forceinline__ void wb_phi(const WbRadius &r, T n3, T n2, T vx, T vy, T vz, T phi[3],
                                        T d[5]) {
   const T a1 = T(r.inv_4piR2), a2 = T(r.inv_4piR);
   const T v2 = vx * vx + vy * vy + vz * vz;
@@ -220,7 +220,7 @@ __device__ __forceinline__ void wb_phi(const WbRadius &r, T n3, T n2, T vx, T vy
 // layout constants below.  The v-v block is c * identity.
 constexpr int kHessPacked = 10;  // h33 h32 h3x h3y h3z h22 h2x h2y h2z hvv
 template <typename T>
-__device__ __forceinline__ void wb_hess(const WbRadius &r, T n3, T n2, T vx, T vy, T vz, T h[10]) {
+__host__ __device__ __forceinline__ void wb_hess(const WbRadius &r, T n3, T n2, T vx, T vy, T vz, T h[10]) {
   const T a1 = T(r.inv_4piR2), a2 = T(r.inv_4piR);
   const T v2 = vx * vx + vy * vy + vz * vz;
   const T u = T(1) / (T(1) - n3);

@@ -72,6 +72,16 @@ extern "C" {
                                 the FP32 stage of the mixed form each search starts at the last
                                 accepted step and accepts |s| <= 0.5 |s0|; the FP64 form keeps
                                 the slope-ratio first step and 0.1 */
+#define DEFT_PC_STRUCTURE 3  /* bulk structure-factor preconditioner (an extension, not in the
+                                reference): M^-1 r = s F^-1[F[s r] / H_b(k)], s = sqrt(n / n_b)
+                                on the free points (0 where masked or n <= 0), H_b(k) the
+                                Hessian of the uniform fluid at the bulk density n_b in
+                                equilibrium at mu (analytic weights, FP32 transforms).  In a
+                                uniform fluid M is the Hessian; at large k it is the density
+                                preconditioner.  Used by the secant CG and by the mixed
+                                form's Newton refinement.  Secant search, density variable,
+                                hard-sphere (White Bear, Rosenfeld, mark II) and ideal-gas
+                                terms, no tensor or SAFT terms, Nz = 32, 64, 128 or 256 */
 
 typedef struct deft_ctx deft_ctx;
 typedef struct deft_grid deft_grid;
@@ -235,6 +245,12 @@ int deft_fmt_weighted(deft_fmt *f, const double *n, int on_device, double *out5)
  * refinement (no reference counterpart; the reference has no Hessian). */
 int deft_fmt_hessian_vector(deft_fmt *f, const double *n, const double *dx, int on_device,
                             double *out);
+/* The structure preconditioner of DEFT_PC_STRUCTURE at density n applied to
+ * r: z = M^-1 r (no reference counterpart).  Fills bulk_out (may be NULL)
+ * with the bulk density n_b in equilibrium at the functional's mu that it
+ * uses.  Same requirements as DEFT_PC_STRUCTURE. */
+int deft_fmt_precondition(deft_fmt *f, const double *n, const double *r, int on_device,
+                          double *z, double *bulk_out);
 /* find_chemical_potential(OfEffectivePotential(HS(R)+IdealGas()), kT, nb)
  * (src/equation-of-state.cpp:189-192): the mu that makes nb the bulk density. */
 int deft_find_chemical_potential(double R, double kT, double nb, double *mu_out);
