@@ -380,7 +380,10 @@ def run_ours(args, rank, world):
     # preconditioner, 1e-5 was the fastest of 1e-5, 3e-5, 3e-4 and the
     # relative rule on 30 held-out problems (python -m deft_gb300.warmstart
     # --count 256 --epochs 2 --held 30 --fp64-held 0 --switch 1e-5,3e-5,3e-4)
-    SWITCH = args.switch if args.switch else (1e-4 if PC == _lib.PC_NONE else 1e-5)
+    # (structure preconditioner: 3e-6 against 1e-5 and 3e-5 in one call on
+    # 20 held-out problems, 15.0 / 15.3 / 16.1 ms, fewer FP64 evaluations)
+    SWITCH = args.switch if args.switch else {_lib.PC_NONE: 1e-4, _lib.PC_DENSITY: 1e-5,
+                                              _lib.PC_STRUCTURE: 3e-6}[PC]
     timed_idx = [args.warmup + k for k in range(args.steps)]
 
     # The profile condition's reference: each timed problem solved in FP64

@@ -1540,7 +1540,11 @@ int step_newton(deft_cg *c, deft_cg_status *st, const deft::FmtSpec &spec) {
   // where the engine takes FP32 vectors (f32_newton) the CG's vectors are
   // FP32 too: the step only has to solve to 1e-5 of |g|, far above FP32
   // rounding, and the FP64 gradient at x + dx decides what is accepted.
-  const double tol = std::fmax(1e-5 * st->gnorm, 0.05 * c->p.gtol);
+  static const double rtol = [] {
+    const char *ev = getenv("DEFT_NEWTON_RTOL");
+    return ev && atof(ev) > 0 ? atof(ev) : 1e-5;
+  }();
+  const double tol = std::fmax(rtol * st->gnorm, 0.05 * c->p.gtol);
   // the linear CG's preconditioner: the structure one if the minimiser uses
   // it, else the inverse ideal-gas curvature
   const bool spc = c->p.preconditioned == DEFT_PC_STRUCTURE;

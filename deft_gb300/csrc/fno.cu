@@ -314,6 +314,84 @@ __global__ void __launch_bounds__(256) k_layer_pw(const float *__restrict__ h,
   }
 }
 
+// Inference form of the layer output (no backward pass needs z): the
+// z-synthesis of the spectral part fused into the pointwise layer.
+// spec[o][r] = sum_k Re[A[o][line][k] G[z][k]] is formed in registers from
+// the line's Kz coefficients instead of being written and read back as a
+// full C x N^3 field.  A block takes 4 z-lines per pass (two consecutive z
+// per thread, so a line is two warps and its coefficients are read as
+// broadcasts), the synthesis table transposed to [k][z] in shared memory
+// (conflict-free 16-byte reads), the pointwise weights in shared memory.
+template <int C>
+__global__ void __launch_bounds__(256) k_layer_synth_pw(const float2 *__restrict__ A,
+                                                        const float2 *__restrict__ G,
+                                                        const float *__restrict__ h,
+                                                        float *__restrict__ hn,
+                                                        const __nv_bfloat16 *__restrict__ Wp,
+                                                        const __nv_bfloat16 *__restrict__ b, int N,
+                                                        int Kz, int act) {
+  extern __shared__ __align__(16) float sm[];
+  float *Ws = sm;                                                // [C][C]
+  float *bs = Ws + C * C;                                        // [C] (padded to 4)
+  float2 *Gs = reinterpret_cast<float2 *>(bs + ((C + 3) & ~3));  // [Kz][N]
+  float2 *As = Gs + (size_t)Kz * N;                              // [4 lines][C][Kz]
+  for (int i = threadIdx.x; i < C * C; i += blockDim.x) Ws[i] = bf(Wp, i);
+  for (int i = threadIdx.x; i < C; i += blockDim.x) bs[i] = bf(b, i);
+  for (int i = threadIdx.x; i < Kz * N; i += blockDim.x) {
+    const int k = i / N, z = i - k * N;
+    Gs[i] = G[(size_t)z * Kz + k];
+  }
+  const int half = N >> 1;                 // threads per line
+  const int lines = N * N;                 // z-lines per channel
+  const long long NR = (long long)lines * N;
+  const int lpb = blockDim.x / half;       // lines per pass (4 at N = 128)
+  const int tl = threadIdx.x / half, zp = threadIdx.x - tl * half;
+  const int z0 = 2 * zp;
+  for (int l0 = blockIdx.x * lpb; l0 < lines; l0 += gridDim.x * lpb) {
+    __syncthreads();  // previous pass's readers of As are done (and the tables are in)
+    for (int i = threadIdx.x; i < lpb * C * Kz; i += blockDim.x) {
+      const int ll = i / (C * Kz), rem = i - ll * C * Kz;
+      const int c = rem / Kz, k = rem - c * Kz;
+      const int line = l0 + ll;
+      As[i] = line < lines ? A[((size_t)c * lines + line) * Kz + k] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    const int line = l0 + tl;
+    if (line >= lines || tl >= lpb) continue;
+    const float2 *a = As + (size_t)tl * C * Kz;
+    float2 spec[C];
+#pragma unroll
+    for (int c = 0; c < C; c++) spec[c] = make_float2(0.f, 0.f);
+    for (int k = 0; k < Kz; k++) {
+      const float4 g = *reinterpret_cast<const float4 *>(Gs + (size_t)k * N + z0);
+#pragma unroll
+      for (int c = 0; c < C; c++) {
+        const float2 ac = a[c * Kz + k];
+        spec[c].x += ac.x * g.x - ac.y * g.y;
+        spec[c].y += ac.x * g.z - ac.y * g.w;
+      }
+    }
+    const size_t r = (size_t)line * N + z0;
+    float2 hv[C];
+#pragma unroll
+    for (int i = 0; i < C; i++) hv[i] = *reinterpret_cast<const float2 *>(h + (size_t)i * NR + r);
+#pragma unroll
+    for (int o = 0; o < C; o++) {
+      float2 acc = spec[o];
+      acc.x += bs[o];
+      acc.y += bs[o];
+#pragma unroll
+      for (int i = 0; i < C; i++) {
+        const float w = Ws[o * C + i];
+        acc.x += w * hv[i].x;
+        acc.y += w * hv[i].y;
+      }
+      if (act) acc = make_float2(gelu(acc.x), gelu(acc.y));
+      *reinterpret_cast<float2 *>(hn + (size_t)o * NR + r) = acc;
+    }
+  }
+}
+
 // Deterministic block reduction of K floats into partial[block][K].
 template <int K>
 __device__ void block_sum_store(float (&v)[K], float *partial) {
@@ -729,7 +807,8 @@ void launch_axis(deft_fno *f, const float2 *in, float2 *out, const float2 *E, in
                                                                               Nin, Mout, inner);
 }
 
-// Forward through the spectral part of layer l: S (in zbuf) = Finv(W F h).
+// Forward through the spectral part of layer l: S (in zbuf) = Finv(W F h);
+// without zout, stops before the z synthesis (its coefficients in f->A).
 void spectral_fwd(deft_fno *f, int l, const float *hin, float *zout) {
   const int C = f->C, N = f->N;
   launch_z_fwd(f, hin, f->A, f->Ezf);                               // [C N N Kz]
@@ -739,7 +818,28 @@ void spectral_fwd(deft_fno *f, int l, const float *hin, float *zout) {
                                                               f->K);
   launch_axis(f, f->S, f->B, f->Exi, C, f->Kx, N, f->Ky * f->Kz);   // [C N Ky Kz]
   launch_axis(f, f->B, f->A, f->Eyi, C * N, f->Ky, N, f->Kz);       // [C N N Kz]
-  launch_z_inv(f, f->A, zout, f->Gzi, 0);
+  if (zout) launch_z_inv(f, f->A, zout, f->Gzi, 0);
+}
+
+// The inference layer: synthesis of f->A fused into the pointwise layer.
+template <int C>
+void launch_layer_synth_pw(deft_fno *f, int l) {
+  const int N = f->N, half = N / 2, lpb = 256 / half;
+  const size_t sm = sizeof(float) * (C * C + ((C + 3) & ~3)) +
+                    sizeof(float2) * ((size_t)f->Kz * N + (size_t)lpb * C * f->Kz);
+  if (sm > 48 * 1024)
+    cudaFuncSetAttribute(k_layer_synth_pw<C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)sm);
+  int sms = 0, dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int lines = N * N;
+  int grid = 4 * (sms > 0 ? sms : 148);
+  const int need = (lines + lpb - 1) / lpb;
+  if (grid > need) grid = need;
+  k_layer_synth_pw<C><<<grid, 256, sm, f->stream>>>(f->A, f->Gzi, f->h[l], f->h[l + 1],
+                                                    f->pb + f->oWp[l], f->pb + f->ob[l], N, f->Kz,
+                                                    l < f->L - 1 ? 1 : 0);
 }
 
 // Adjoint of spectral_fwd for upstream zbar: adds K^T zbar to hin_bar and
@@ -785,11 +885,19 @@ int forward(deft_fno *f, float eta, bool train) {
   k_lift<<<grid_for(f->NR), kT, 0, f->stream>>>(f->mask, eta, f->pb + f->oP, f->pb + f->op, f->h[0],
                                                C, f->NR);
   for (int l = 0; l < f->L; l++) {
+    if (!train) {
+      // inference: no z field for a backward pass; one launch fewer per layer
+      spectral_fwd(f, l, f->h[l], nullptr);
+      f->launches--;
+      if (C == 16) launch_layer_synth_pw<16>(f, l);
+      else if (C == 8) launch_layer_synth_pw<8>(f, l);
+      else launch_layer_synth_pw<4>(f, l);
+      continue;
+    }
     spectral_fwd(f, l, f->h[l], f->z[l]);
-    const int sz = train ? 1 : 0;
-    if (C == 16) launch_layer_pw<16>(f, l, sz);
-    else if (C == 8) launch_layer_pw<8>(f, l, sz);
-    else launch_layer_pw<4>(f, l, sz);
+    if (C == 16) launch_layer_pw<16>(f, l, 1);
+    else if (C == 8) launch_layer_pw<8>(f, l, 1);
+    else launch_layer_pw<4>(f, l, 1);
   }
   return check(f, "fno forward");
 }

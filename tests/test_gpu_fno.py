@@ -63,6 +63,30 @@ def test_forward_and_gradient_match_fp64_restatement(N, C, m, L):
         net.close()
 
 
+@pytest.mark.parametrize("N,C,m,L", [(12, 4, 3, 2), (16, 16, 4, 4), (20, 8, 5, 3),
+                                     (32, 16, 12, 4)])
+def test_inference_layers_match_training_forward(N, C, m, L):
+    """Inference (no gradient asked) fuses the z synthesis into the pointwise
+    layer; its output equals the training forward's (separate synthesis,
+    stored z) and the FP64 restatement's to FP32 accumulation error."""
+    net = _net(N, C, m, L)
+    try:
+        rng = np.random.default_rng(N + 7 * C)
+        p = (net.get_params() + 0.05 * rng.standard_normal(net.nparam)).astype(np.float32)
+        net.set_params(p)
+        mask, target = _sample(N, seed=N + 1)
+        eta = 0.31
+        y_inf, loss_inf, _ = net.eval(mask, eta, target, want_grad=False)
+        y_tr, loss_tr, _ = net.eval(mask, eta, target, want_grad=True)
+        _, y_r, _ = ref.loss_and_grad(p, mask, eta, target, N, C, m, L)
+        scale = max(1.0, float(np.max(np.abs(y_r))))
+        assert np.max(np.abs(y_inf - y_tr)) <= 1e-5 * scale
+        assert np.max(np.abs(y_inf - y_r)) <= 2e-5 * scale
+        assert abs(loss_inf - loss_tr) <= 1e-5 * loss_tr
+    finally:
+        net.close()
+
+
 def test_eval_is_deterministic_and_device_inputs_agree():
     import torch
     N, C, m, L = 16, 8, 4, 2
