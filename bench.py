@@ -935,6 +935,53 @@ def fno_case(N=128, reps=5):
             "launches_per_forward": launches // (reps + 2)}
 
 
+def pc_case(N=128, reps=20):
+    """The structure preconditioner (DEFT_PC_STRUCTURE) applied to a
+    gradient-sized vector on a held-out N^3 wall + solute problem at its bulk
+    start: `reps` applications through deft_fmt_precondition on device
+    buffers (FP64 vectors, FP32 transforms), timed with CUDA events on the
+    library's stream after warm-up; per-application kernel events from the
+    grid's profile."""
+    import torch
+    from deft_gb300 import _lib
+    from deft_gb300.warmstart import Solver
+    L = _lib.load()
+    s = held_out(N, 1)[0]
+    sv = Solver(s.shape, s.lat, device=0, gtol=GTOL)
+    try:
+        mask = torch.tensor(s.mask.reshape(-1), device="cuda:0")
+        sv.set_problem(s, mask.data_ptr())
+        h = sv.fmt[_lib.PRECISION_MIXED]
+        n = torch.tensor(s.n0.reshape(-1), device="cuda:0")
+        r = torch.randn(n.numel(), dtype=torch.float64, device="cuda:0",
+                        generator=torch.Generator(device="cuda:0").manual_seed(1)) * mask
+        z = torch.empty_like(n)
+        stream = torch.cuda.ExternalStream(L.deft_ctx_stream(sv.ctx), device="cuda:0")
+        nb = ctypes.c_double()
+        for _ in range(3):
+            _lib.check(L.deft_fmt_precondition(h, n.data_ptr(), r.data_ptr(), 1, z.data_ptr(),
+                                               ctypes.addressof(nb)))
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            _lib.check(L.deft_fmt_precondition(h, n.data_ptr(), r.data_ptr(), 1, z.data_ptr(),
+                                               None))
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        _lib.check(L.deft_grid_profile(sv.grid, 1))
+        _lib.check(L.deft_fmt_precondition(h, n.data_ptr(), r.data_ptr(), 1, z.data_ptr(), None))
+        prof = kernel_profile(L, sv.grid)
+        _lib.check(L.deft_grid_profile(sv.grid, 0))
+    finally:
+        sv.close()
+    return {"pc_case": {"N": N, "eta": s.eta, "bulk_density": nb.value},
+            "us_per_application": round(1e3 * ms, 2),
+            "kernels_us": {k: round(1e3 * v[1] / v[0], 2) for k, v in prof.items()},
+            "launches": {k: v[0] for k, v in prof.items()}}
+
+
 def solute_case(N=256, reps=5):
     """The hard-sphere solute workload at 256^3 (dx = 0.1, eta = 0.35, centre
     exclusion radius 3, smoothed-noise start with seed 2;
@@ -1168,6 +1215,8 @@ def main():
                     help="only run the 256^3 hard-sphere solute workload (FP64 vs mixed) and exit")
     ap.add_argument("--fno-case", action="store_true",
                     help="only time the warm-start network's forward pass and exit")
+    ap.add_argument("--pc-case", action="store_true",
+                    help="only time the structure preconditioner's application and exit")
     args = ap.parse_args()
     if args.weights is None:
         args.weights = BUNDLED_WEIGHTS if os.path.exists(BUNDLED_WEIGHTS) else "train"
@@ -1179,6 +1228,9 @@ def main():
         return
     if args.fno_case:
         print(json.dumps(fno_case(args.N)))
+        return
+    if args.pc_case:
+        print(json.dumps(pc_case(args.N)))
         return
     if args.kernel_case:
         print(json.dumps(kernel_case(1 if args.kernel_case == "mixed" else 0, args.N,

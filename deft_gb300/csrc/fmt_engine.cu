@@ -801,14 +801,14 @@ __global__ void __launch_bounds__(pencil_threads<W>(), W >= 16 ? 1 : 2)
 }
 
 // The structure preconditioner along x, in place on one field: x-FFT, times
-// P(k) / N, inverse x-FFT (columns as in k_x_conv_fwd_pencil).
+// P(k) / N from the table P (layout x Ny NzH + y NzH + kz, k_pc_table),
+// inverse x-FFT (columns as in k_x_conv_fwd_pencil).
 template <int W>
 __global__ void __launch_bounds__(pencil_threads<W>())
     k_x_pc_pencil(float2 *data, Geom g, const float2 *__restrict__ tw,
-                  const LocalArgs *__restrict__ lap) {
+                  const float *__restrict__ P) {
   constexpr int G = pencil_groups<W>();
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const LocalArgs la = *lap;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, w = warp % W, grp = warp / W;
   float2 *xs = reinterpret_cast<float2 *>(smem_raw) + grp * pencil_xs_elems<W>();
   const int J = g.Ny * g.NzH;
@@ -822,15 +822,11 @@ __global__ void __launch_bounds__(pencil_threads<W>())
 #pragma unroll
   for (int m = 0; m < 16; m++) v[m] = act ? col[m * sW] : make_float2(0.f, 0.f);
   pencil_n2s<float, -1, W>(v, xs, w, lane, tw);
-  const float yw = (float)wrapm(y, g.Ny), zf = (float)kz;
-  float kc[3];
-#pragma unroll
-  for (int c = 0; c < 3; c++) kc[c] = g.Bmf[3 * c + 1] * yw + g.Bmf[3 * c + 2] * zf;
+  (void)y;
+  (void)kz;
 #pragma unroll
   for (int q = 0; q < 16; q++) {
-    const float xw = (float)wrapm(pencil_freq<W>(w, q), g.Nx);
-    const float kx = g.Bmf[0] * xw + kc[0], ky = g.Bmf[3] * xw + kc[1], kzz = g.Bmf[6] * xw + kc[2];
-    const float p = pc_mult(kx * kx + ky * ky + kzz * kzz, la, (float)g.dr, (float)g.scale);
+    const float p = act ? __ldg(P + (size_t)pencil_freq<W>(w, q) * J + j) : 0.f;
     v[q] = make_float2(v[q].x * p, v[q].y * p);
   }
   pencil_s2n<float, +1, W>(v, xs, w, lane, tw);
@@ -840,9 +836,19 @@ __global__ void __launch_bounds__(pencil_threads<W>())
   }
 }
 
-// The same multiplication on an x-transformed spectrum (layout x Ny NzH +
-// y NzH + kz), for grids whose x length the pencil kernels do not take.
-__global__ void k_pc_mult(float2 *data, Geom g, const LocalArgs *__restrict__ lap) {
+// The same multiplication on an x-transformed spectrum, for grids whose x
+// length the pencil kernels do not take.
+__global__ void k_pc_mult(float2 *data, const float *__restrict__ P, int NC) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < NC; i += gridDim.x * blockDim.x) {
+    const float p = P[i];
+    data[i] = make_float2(data[i].x * p, data[i].y * p);
+  }
+}
+
+// The preconditioner's multiplier P(k) / N at every k of the half spectrum
+// (layout x Ny NzH + y NzH + kz), made once per set of functional
+// parameters (the bulk density and Hessian of LocalArgs).
+__global__ void k_pc_table(float *__restrict__ P, Geom g, const LocalArgs *__restrict__ lap) {
   const LocalArgs la = *lap;
   const int J = g.Ny * g.NzH;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < g.NC; i += gridDim.x * blockDim.x) {
@@ -851,8 +857,7 @@ __global__ void k_pc_mult(float2 *data, Geom g, const LocalArgs *__restrict__ la
     fdivmod(j, g.fNzH, y, z);
     const float kx = kcomp_t<float>(g, 0, x, y, z), ky = kcomp_t<float>(g, 1, x, y, z),
                 kz = kcomp_t<float>(g, 2, x, y, z);
-    const float p = pc_mult(kx * kx + ky * ky + kz * kz, la, (float)g.dr, (float)g.scale);
-    data[i] = make_float2(data[i].x * p, data[i].y * p);
+    P[i] = pc_mult(kx * kx + ky * ky + kz * kz, la, (float)g.dr, (float)g.scale);
   }
 }
 
@@ -2327,6 +2332,7 @@ class EngineImpl {
     cudaFree(w2f);
     cudaFree(wvf);
     cudaFree(hess);
+    cudaFree(pc_table);
     clear_graphs();
     cudaFree(la_dev);
     cudaFree(hloc);
@@ -3195,6 +3201,16 @@ class EngineImpl {
       err = "structure preconditioner: no bulk density for these parameters";
       return -1;
     }
+    // the multiplier table, (re)made on the stream when the parameters change
+    if (!pc_table && alloc(&pc_table, sizeof(float) * (size_t)g.NC)) return -1;
+    if (!pc_table_valid || memcmp(&pc_table_la, &la_last, sizeof(LocalArgs))) {
+      pre(kslot<float>(kK_struct_pc));
+      k_pc_table<<<dot_blocks, kThreads, 0, stream>>>(pc_table, g, la_dev);
+      post(kslot<float>(kK_struct_pc));
+      if (check("structure preconditioner table")) return -1;
+      pc_table_la = la_last;
+      pc_table_valid = true;
+    }
     const double *da[1] = {reinterpret_cast<const double *>(a)};
     const double *db[1] = {reinterpret_cast<const double *>(b)};
     const GraphKey key =
@@ -3220,7 +3236,7 @@ class EngineImpl {
         const int cols = 32 * pencil_groups<W>();
         k_x_pc_pencil<W><<<(g.Ny * g.NzH + cols - 1) / cols, pencil_threads<W>(),
                            pencil_smem<W>(false), stream>>>(
-            w, g, reinterpret_cast<const float2 *>(plan<float>(0).tw), la_dev);
+            w, g, reinterpret_cast<const float2 *>(plan<float>(0).tw), pc_table);
       });
       post(kslot<float>(kK_struct_pc));
     } else {
@@ -3229,7 +3245,7 @@ class EngineImpl {
                                                                              1.0f);
       post(kslot<float>(kK_x_fft));
       pre(kslot<float>(kK_struct_pc));
-      k_pc_mult<<<dot_blocks, kThreads, 0, stream>>>(w, g, la_dev);
+      k_pc_mult<<<dot_blocks, kThreads, 0, stream>>>(w, pc_table, g.NC);
       post(kslot<float>(kK_struct_pc));
       pre(kslot<float>(kK_x_fft));
       k_x_fft<float, +1><<<x_tiles(t32.Bx), kThreads, t32.smem_x2, stream>>>(w, g, pxf, t32.fBx,
@@ -3246,6 +3262,10 @@ class EngineImpl {
     post(kslot<float>(kK_struct_pc));
     return check("structure preconditioner");
   }
+
+  float *pc_table = nullptr;  // P(k) / N of the structure preconditioner
+  LocalArgs pc_table_la{};    // the parameters it was made for
+  bool pc_table_valid = false;
 
   int hess_setup(const FmtSpec &f, const double *n) {
     if (!hess && (alloc(&hess, sizeof(float) * kHessPacked * (size_t)g.NR) ||

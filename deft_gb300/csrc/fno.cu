@@ -179,13 +179,14 @@ __global__ void k_dft_axis(const float2 *__restrict__ in, float2 *__restrict__ o
   float2 *Es = reinterpret_cast<float2 *>(sm);  // [Mout][Nin]
   for (int i = threadIdx.x; i < Mout * Nin; i += blockDim.x) Es[i] = E[i];
   __syncthreads();
-  const long long total = (long long)outer * Mout * inner;
-  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
-       t += (long long)gridDim.x * blockDim.x) {
-    const int i = (int)(t % inner);
-    const long long r = t / inner;
-    const int m = (int)(r % Mout);
-    const int o = (int)(r / Mout);
+  // 32-bit index arithmetic (the network's tensors hold < 2^31 entries; a
+  // 64-bit division costs several times a 32-bit one)
+  const int total = outer * Mout * inner;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+    const int r = t / inner;
+    const int i = t - r * inner;
+    const int o = r / Mout;
+    const int m = r - o * Mout;
     const float2 *src = in + (size_t)o * Nin * inner + i;
     const float2 *e = Es + m * Nin;
     float re = 0.f, im = 0.f;
@@ -208,6 +209,77 @@ __global__ void k_dft_axis(const float2 *__restrict__ in, float2 *__restrict__ o
       im += a.x * b.y + a.y * b.x;
     }
     out[t] = make_float2(re, im);
+  }
+}
+
+// The same contraction by tiles: a tile is (o, IC consecutive i), its
+// Nin x IC inputs staged in shared memory with the whole table E (rows
+// padded by one entry against bank conflicts), staged once per block; a
+// thread forms four outputs m = 4 g .. 4 g + 3 of one column i, so each
+// staged input feeds four complex multiply-adds.  For the y contractions
+// (inner = Kz) a tile is a whole contiguous slab; S tiles go through a block
+// at once when one leaves threads idle.
+constexpr int kAxMR = 4;
+__global__ void __launch_bounds__(256) k_dft_tile(const float2 *__restrict__ in,
+                                                  float2 *__restrict__ out,
+                                                  const float2 *__restrict__ E, int outer,
+                                                  int Nin, int Mout, int inner, int IC, int S) {
+  extern __shared__ __align__(16) float2 smt[];
+  const int ES = Nin + 1;
+  float2 *Es = smt;             // [Mout][Nin + 1]
+  float2 *Tb = Es + Mout * ES;  // S x [Nin][IC]
+  for (int i = threadIdx.x; i < Mout * Nin; i += blockDim.x) {
+    const int m = i / Nin, n = i - m * Nin;
+    Es[m * ES + n] = E[i];
+  }
+  const int nch = (inner + IC - 1) / IC;
+  const int tiles = outer * nch;
+  const int groups = (Mout + kAxMR - 1) / kAxMR;
+  const int per = groups * IC;  // work items of one tile
+  for (int t0 = blockIdx.x * S; t0 < tiles; t0 += gridDim.x * S) {
+    __syncthreads();  // the previous batch's readers are done (and E is in)
+    for (int idx = threadIdx.x; idx < S * Nin * IC; idx += blockDim.x) {
+      const int s = idx / (Nin * IC), rem = idx - s * Nin * IC;
+      const int n = rem / IC, j = rem - n * IC;
+      const int tile = t0 + s;
+      float2 v = make_float2(0.f, 0.f);
+      if (tile < tiles) {
+        const int o = tile / nch, i0 = (tile - o * nch) * IC;
+        if (i0 + j < inner) v = in[((size_t)o * Nin + n) * inner + i0 + j];
+      }
+      Tb[idx] = v;
+    }
+    __syncthreads();
+    for (int w = threadIdx.x; w < S * per; w += blockDim.x) {
+      const int s = w / per, idx = w - s * per;
+      const int tile = t0 + s;
+      if (tile >= tiles) continue;
+      const int o = tile / nch, i0 = (tile - o * nch) * IC;
+      const int ic = inner - i0 < IC ? inner - i0 : IC;
+      const float2 *T = Tb + (size_t)s * Nin * IC;
+      const int g = idx / IC, j = idx - g * IC;
+      if (j >= ic) continue;
+      float re[kAxMR], im[kAxMR];
+#pragma unroll
+      for (int r = 0; r < kAxMR; r++) re[r] = im[r] = 0.f;
+      const float2 *e0 = Es + (size_t)(g * kAxMR) * ES;
+      for (int n = 0; n < Nin; n++) {
+        const float2 a = T[n * IC + j];
+#pragma unroll
+        for (int r = 0; r < kAxMR; r++) {
+          if (g * kAxMR + r < Mout) {
+            const float2 b = e0[r * ES + n];
+            re[r] += a.x * b.x - a.y * b.y;
+            im[r] += a.x * b.y + a.y * b.x;
+          }
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < kAxMR; r++) {
+        const int m = g * kAxMR + r;
+        if (m < Mout) out[((size_t)o * Mout + m) * inner + i0 + j] = make_float2(re[r], im[r]);
+      }
+    }
   }
 }
 
@@ -321,7 +393,9 @@ __global__ void __launch_bounds__(256) k_layer_pw(const float *__restrict__ h,
 // full C x N^3 field.  A block takes 4 z-lines per pass (two consecutive z
 // per thread, so a line is two warps and its coefficients are read as
 // broadcasts), the synthesis table transposed to [k][z] in shared memory
-// (conflict-free 16-byte reads), the pointwise weights in shared memory.
+// (conflict-free 16-byte reads), the line's coefficients as [k][c] (two
+// channels per 16-byte broadcast read), the pointwise weights in shared
+// memory (four per 16-byte broadcast read).
 template <int C>
 __global__ void __launch_bounds__(256) k_layer_synth_pw(const float2 *__restrict__ A,
                                                         const float2 *__restrict__ G,
@@ -334,7 +408,7 @@ __global__ void __launch_bounds__(256) k_layer_synth_pw(const float2 *__restrict
   float *Ws = sm;                                                // [C][C]
   float *bs = Ws + C * C;                                        // [C] (padded to 4)
   float2 *Gs = reinterpret_cast<float2 *>(bs + ((C + 3) & ~3));  // [Kz][N]
-  float2 *As = Gs + (size_t)Kz * N;                              // [4 lines][C][Kz]
+  float2 *As = Gs + (size_t)Kz * N;                              // [4 lines][Kz][C]
   for (int i = threadIdx.x; i < C * C; i += blockDim.x) Ws[i] = bf(Wp, i);
   for (int i = threadIdx.x; i < C; i += blockDim.x) bs[i] = bf(b, i);
   for (int i = threadIdx.x; i < Kz * N; i += blockDim.x) {
@@ -353,7 +427,8 @@ __global__ void __launch_bounds__(256) k_layer_synth_pw(const float2 *__restrict
       const int ll = i / (C * Kz), rem = i - ll * C * Kz;
       const int c = rem / Kz, k = rem - c * Kz;
       const int line = l0 + ll;
-      As[i] = line < lines ? A[((size_t)c * lines + line) * Kz + k] : make_float2(0.f, 0.f);
+      As[(size_t)ll * C * Kz + k * C + c] =
+          line < lines ? A[((size_t)c * lines + line) * Kz + k] : make_float2(0.f, 0.f);
     }
     __syncthreads();
     const int line = l0 + tl;
@@ -364,11 +439,14 @@ __global__ void __launch_bounds__(256) k_layer_synth_pw(const float2 *__restrict
     for (int c = 0; c < C; c++) spec[c] = make_float2(0.f, 0.f);
     for (int k = 0; k < Kz; k++) {
       const float4 g = *reinterpret_cast<const float4 *>(Gs + (size_t)k * N + z0);
+      const float4 *ak = reinterpret_cast<const float4 *>(a + k * C);
 #pragma unroll
-      for (int c = 0; c < C; c++) {
-        const float2 ac = a[c * Kz + k];
-        spec[c].x += ac.x * g.x - ac.y * g.y;
-        spec[c].y += ac.x * g.z - ac.y * g.w;
+      for (int c2 = 0; c2 < C / 2; c2++) {
+        const float4 ac = ak[c2];  // channels 2 c2, 2 c2 + 1
+        spec[2 * c2].x += ac.x * g.x - ac.y * g.y;
+        spec[2 * c2].y += ac.x * g.z - ac.y * g.w;
+        spec[2 * c2 + 1].x += ac.z * g.x - ac.w * g.y;
+        spec[2 * c2 + 1].y += ac.z * g.z - ac.w * g.w;
       }
     }
     const size_t r = (size_t)line * N + z0;
@@ -380,11 +458,14 @@ __global__ void __launch_bounds__(256) k_layer_synth_pw(const float2 *__restrict
       float2 acc = spec[o];
       acc.x += bs[o];
       acc.y += bs[o];
+      const float4 *wr = reinterpret_cast<const float4 *>(Ws + o * C);
 #pragma unroll
-      for (int i = 0; i < C; i++) {
-        const float w = Ws[o * C + i];
-        acc.x += w * hv[i].x;
-        acc.y += w * hv[i].y;
+      for (int i4 = 0; i4 < C / 4; i4++) {
+        const float4 w = wr[i4];
+        acc.x += w.x * hv[4 * i4].x + w.y * hv[4 * i4 + 1].x + w.z * hv[4 * i4 + 2].x +
+                 w.w * hv[4 * i4 + 3].x;
+        acc.y += w.x * hv[4 * i4].y + w.y * hv[4 * i4 + 1].y + w.z * hv[4 * i4 + 2].y +
+                 w.w * hv[4 * i4 + 3].y;
       }
       if (act) acc = make_float2(gelu(acc.x), gelu(acc.y));
       *reinterpret_cast<float2 *>(hn + (size_t)o * NR + r) = acc;
@@ -802,6 +883,29 @@ void launch_z_inv(deft_fno *f, const float2 *in, float *out, const float2 *G, in
 }
 void launch_axis(deft_fno *f, const float2 *in, float2 *out, const float2 *E, int outer, int Nin,
                  int Mout, int inner) {
+  // tiles of up to 32 columns (a whole slab when inner <= 32) while they fit
+  const int IC = inner < 32 ? inner : 32;
+  const size_t sm = sizeof(float2) * ((size_t)Mout * (Nin + 1) + (size_t)Nin * IC);
+  if (sm <= 96 * 1024) {
+    int sms = 0, dev = 0;
+    cudaGetDevice(&dev);
+    static bool attr[64] = {};  // the shared-memory cap, set once per device
+    if (dev < 0 || dev >= 64 || !attr[dev]) {
+      cudaFuncSetAttribute(k_dft_tile, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024);
+      if (dev >= 0 && dev < 64) attr[dev] = true;
+    }
+    // tiles per block pass: fill the 256 threads when a tile has few items
+    const int per = ((Mout + kAxMR - 1) / kAxMR) * IC;
+    int S = per >= 256 ? 1 : 256 / per;
+    while (S > 1 && sm + sizeof(float2) * (size_t)(S - 1) * Nin * IC > 96 * 1024) S--;
+    const size_t sm2 = sm + sizeof(float2) * (size_t)(S - 1) * Nin * IC;
+    const int tiles = (outer * ((inner + IC - 1) / IC) + S - 1) / S;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    int grid = 2 * (sms > 0 ? sms : 148);
+    if (grid > tiles) grid = tiles;
+    k_dft_tile<<<grid, 256, sm2, f->stream>>>(in, out, E, outer, Nin, Mout, inner, IC, S);
+    return;
+  }
   const long long total = (long long)outer * Mout * inner;
   k_dft_axis<<<grid_for(total), kT, sizeof(float2) * Mout * Nin, f->stream>>>(in, out, E, outer,
                                                                               Nin, Mout, inner);
