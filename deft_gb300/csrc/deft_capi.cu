@@ -101,6 +101,8 @@ struct deft_cg {
   float *V32 = nullptr, *mask32 = nullptr;
   float *q32 = nullptr, *dx32 = nullptr;  // the Newton step's linear CG on FP32 vectors
   bool f32_live = false;
+  bool x_stale = false;   // x lags x32 (brought up to date by x64_sync)
+  bool in_solve = false;  // inside deft_cg_solve: x is synced once at the end
   unsigned f32_fields = ~0u;  // the functional's fields_version V32, mask32 were made from
 };
 
@@ -1018,6 +1020,7 @@ static void cg_reset(deft_cg *c) {
   c->nm_oldgradsqr = 1.0;
   c->nm_deltaE = c->nm_dEdn = c->nm_log_avg = c->nm_err = 0;
   c->f32_live = false;
+  c->x_stale = false;
   const size_t bytes = sizeof(double) * nr(c->f->grid);
   cudaMemsetAsync(c->d, 0, bytes, c->f->grid->ctx->stream);
   cudaMemsetAsync(c->gold, 0, bytes, c->f->grid->ctx->stream);
@@ -1035,10 +1038,19 @@ int deft_cg_set_x(deft_cg *c, const double *n, int on_device) {
   return sync(g->ctx);
 }
 
+// Brings the FP64 iterate up to date with the FP32 stage's (x_stale).
+static int x64_sync(deft_cg *c) {
+  if (!c->x_stale) return DEFT_OK;
+  if (c->f->grid->eng->to_f64(c->x32, c->x)) return eng_err(c->f->grid->eng);
+  c->x_stale = false;
+  return DEFT_OK;
+}
+
 int deft_cg_get_x(deft_cg *c, double *n, int on_device) {
   if (!c || !n) return set_err(DEFT_ERR_ARG, "NULL argument");
   deft_grid *g = c->f->grid;
   cudaSetDevice(g->ctx->device);
+  if (int s = x64_sync(c)) return s;
   cudaError_t e = cudaMemcpyAsync(n, c->x, sizeof(double) * nr(g),
                                   on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
                                   g->ctx->stream);
@@ -1046,7 +1058,10 @@ int deft_cg_get_x(deft_cg *c, double *n, int on_device) {
   return sync(g->ctx);
 }
 
-double *deft_cg_x_device(deft_cg *c) { return c ? c->x : nullptr; }
+double *deft_cg_x_device(deft_cg *c) {
+  if (!c || x64_sync(c)) return nullptr;
+  return c->x;
+}
 
 namespace {
 
@@ -1107,6 +1122,7 @@ int cg_eval_dots(deft_cg *c, const deft::FmtSpec &spec, int k, const double *con
 // Minimizer::energy() (src/Minimizer.h:52), cached while x is unchanged.
 int cg_energy(deft_cg *c, double *E) {
   if (!c->e_valid) {
+    if (int s = x64_sync(c)) return s;
     const deft::FmtSpec spec = spec_of(c->f);
     if (int s = fmt_eval(c->f, spec, c->x, nullptr, nullptr, &c->e_cache, nullptr)) return s;
     c->evals++;
@@ -1310,12 +1326,13 @@ int f32_enter(deft_cg *c) {
 // Hands the state back to the FP64 vectors (exact: FP32 -> FP64 -> FP32
 // round-trips).
 int f32_leave(deft_cg *c) {
-  if (!c->f32_live) return DEFT_OK;
+  if (!c->f32_live) return x64_sync(c);
   Engine *e = eng_of(c);
   if (e->to_f64(c->x32, c->x) || e->to_f64(c->g32, c->g) || e->to_f64(c->d32, c->d) ||
       e->to_f64(c->gold32, c->gold) || e->to_f64(c->pg32, c->pg))
     return eng_err(e);
   c->f32_live = false;
+  c->x_stale = false;
   return DEFT_OK;
 }
 
@@ -1497,7 +1514,10 @@ int step_stage0(deft_cg *c, deft_cg_status *st, const deft::FmtSpec &spec, doubl
   }
   if (int s = f32_enter(c)) return s;
   const int status = step_secant<float>(c, st, spec, gtol);
-  if (eng_of(c)->to_f64(c->x32, c->x)) return eng_err(eng_of(c));
+  // x follows at the end of a public step (deft_cg_solve: at the end of the solve)
+  c->x_stale = true;
+  if (!c->in_solve)
+    if (int s = x64_sync(c)) return s;
   return status;
 }
 
@@ -2041,11 +2061,15 @@ int deft_cg_step(deft_cg *c, deft_cg_status *st) {
 
 int deft_cg_solve(deft_cg *c, deft_cg_status *st) {
   if (!c || !st) return set_err(DEFT_ERR_ARG, "NULL argument");
+  c->in_solve = true;
+  int s;
   for (;;) {
-    int s = deft_cg_step(c, st);
-    if (s) return s;
-    if (st->converged) return DEFT_OK;
+    s = deft_cg_step(c, st);
+    if (s || st->converged) break;
   }
+  c->in_solve = false;
+  const int sx = x64_sync(c);
+  return s ? s : sx;
 }
 
 namespace {
@@ -2128,6 +2152,7 @@ int deft_cg_solve_device(deft_cg *c, deft_cg_status *st) {
   if (!c || !st) return set_err(DEFT_ERR_ARG, "NULL argument");
   deft_fmt *f = c->f;
   cudaSetDevice(f->grid->ctx->device);
+  if (int s = x64_sync(c)) return s;
   deft::DcgProblem p;
   if (int s = device_problem(c, &p)) return s;
   c->f32_live = false;  // the device solve runs on the FP64 vectors from x
@@ -2394,6 +2419,7 @@ int deft_cg_restore(deft_cg *c, const char *path) {
     else *sc.b = v != 0;
   }
   c->f32_live = false;  // the FP64 vectors hold the restored state
+  c->x_stale = false;
   return DEFT_OK;
 }
 

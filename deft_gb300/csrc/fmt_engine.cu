@@ -1828,15 +1828,49 @@ __global__ void k_precond_dots(const double *__restrict__ n, const double *__res
 
 // FP32-vector forms for the mixed form's FP32 stage: z = g n / (kT dV) on
 // the active points (mask != 0, n > 0) with (z.g, z.h) summed in FP64;
-// d = alpha g + beta d; y += alpha x; conversions.
+// d = alpha g + beta d; y += alpha x; conversions.  Four elements per
+// thread and step (16-byte accesses; the vectors come from cudaMalloc),
+// a scalar tail when the length is not a multiple of 4; per-thread sums in
+// FP32, FP64 across threads and blocks.
+#define DEFT_V4_LOOP(n)                                                              \
+  const int n4_ = (n) >> 2;                                                           \
+  const int tid_ = blockIdx.x * blockDim.x + threadIdx.x, nth_ = gridDim.x * blockDim.x; \
+  for (int i4 = tid_; i4 < n4_; i4 += nth_)
+#define DEFT_V4_TAIL(n) for (int i = 4 * n4_ + tid_; i < (n); i += nth_)
+
+__device__ __forceinline__ float f4c(const float4 &v, int c) {
+  return c == 0 ? v.x : c == 1 ? v.y : c == 2 ? v.z : v.w;
+}
+__device__ __forceinline__ void f4s(float4 &v, int c, float x) {
+  if (c == 0) v.x = x;
+  else if (c == 1) v.y = x;
+  else if (c == 2) v.z = x;
+  else v.w = x;
+}
+
 __global__ void k_precond_dots32(const float *__restrict__ n, const float *__restrict__ g,
                                  const float *__restrict__ mask, const float *__restrict__ h,
                                  float inv_c, float *__restrict__ z, int N, double *partials,
                                  unsigned int *counter, double *out) {
   __shared__ double red[32 * 2];
   float acc[2] = {0, 0};
-  #pragma unroll 4
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+  DEFT_V4_LOOP(N) {
+    const float4 nv = reinterpret_cast<const float4 *>(n)[i4];
+    const float4 gv = reinterpret_cast<const float4 *>(g)[i4];
+    const float4 hv = reinterpret_cast<const float4 *>(h)[i4];
+    const float4 mv = mask ? reinterpret_cast<const float4 *>(mask)[i4] : make_float4(1, 1, 1, 1);
+    float4 zv;
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+      const float zc =
+          precond_active(f4c(mv, c), f4c(nv, c)) ? f4c(gv, c) * f4c(nv, c) * inv_c : 0.0f;
+      f4s(zv, c, zc);
+      acc[0] += zc * f4c(gv, c);
+      acc[1] += zc * f4c(hv, c);
+    }
+    reinterpret_cast<float4 *>(z)[i4] = zv;
+  }
+  DEFT_V4_TAIL(N) {
     const float m = mask ? mask[i] : 1.0f;
     const float nv = n[i], gv = g[i];
     const float zv = precond_active(m, nv) ? gv * nv * inv_c : 0.0f;
@@ -1849,16 +1883,34 @@ __global__ void k_precond_dots32(const float *__restrict__ n, const float *__res
 }
 __global__ void k_scal_add32(float beta, float *__restrict__ d, float alpha,
                              const float *__restrict__ g, int n) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-    d[i] = alpha * g[i] + beta * d[i];
+  DEFT_V4_LOOP(n) {
+    const float4 a = reinterpret_cast<const float4 *>(g)[i4];
+    float4 b = reinterpret_cast<float4 *>(d)[i4];
+    b.x = alpha * a.x + beta * b.x;
+    b.y = alpha * a.y + beta * b.y;
+    b.z = alpha * a.z + beta * b.z;
+    b.w = alpha * a.w + beta * b.w;
+    reinterpret_cast<float4 *>(d)[i4] = b;
+  }
+  DEFT_V4_TAIL(n) d[i] = alpha * g[i] + beta * d[i];
 }
 __global__ void k_scal_add_dot32(float beta, float *__restrict__ d, float alpha,
                                  const float *__restrict__ g, const float *__restrict__ h, int N,
                                  double *partials, unsigned int *counter, double *out) {
   __shared__ double red[32];
   float acc = 0;
-  #pragma unroll 4
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+  DEFT_V4_LOOP(N) {
+    const float4 a = reinterpret_cast<const float4 *>(g)[i4];
+    const float4 hv = reinterpret_cast<const float4 *>(h)[i4];
+    float4 b = reinterpret_cast<float4 *>(d)[i4];
+    b.x = alpha * a.x + beta * b.x;
+    b.y = alpha * a.y + beta * b.y;
+    b.z = alpha * a.z + beta * b.z;
+    b.w = alpha * a.w + beta * b.w;
+    reinterpret_cast<float4 *>(d)[i4] = b;
+    acc += hv.x * b.x + hv.y * b.y + hv.z * b.z + hv.w * b.w;
+  }
+  DEFT_V4_TAIL(N) {
     const float dv = alpha * g[i] + beta * d[i];
     d[i] = dv;
     acc += h[i] * dv;
@@ -1867,33 +1919,43 @@ __global__ void k_scal_add_dot32(float beta, float *__restrict__ d, float alpha,
   finish_dots<1>(accd, red, partials, counter, out);
 }
 __global__ void k_axpy32(float alpha, const float *__restrict__ x, float *__restrict__ y, int n) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-    y[i] += alpha * x[i];
+  DEFT_V4_LOOP(n) {
+    const float4 a = reinterpret_cast<const float4 *>(x)[i4];
+    float4 b = reinterpret_cast<float4 *>(y)[i4];
+    b.x += alpha * a.x;
+    b.y += alpha * a.y;
+    b.z += alpha * a.z;
+    b.w += alpha * a.w;
+    reinterpret_cast<float4 *>(y)[i4] = b;
+  }
+  DEFT_V4_TAIL(n) y[i] += alpha * x[i];
 }
 __global__ void k_to_f32(const double *__restrict__ a, float *__restrict__ b, int n) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-    b[i] = (float)a[i];
+  DEFT_V4_LOOP(n) {
+    const double2 u = reinterpret_cast<const double2 *>(a)[2 * i4];
+    const double2 v = reinterpret_cast<const double2 *>(a)[2 * i4 + 1];
+    reinterpret_cast<float4 *>(b)[i4] = make_float4((float)u.x, (float)u.y, (float)v.x, (float)v.y);
+  }
+  DEFT_V4_TAIL(n) b[i] = (float)a[i];
 }
 __global__ void k_to_f64(const float *__restrict__ a, double *__restrict__ b, int n) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-    b[i] = (double)a[i];
+  DEFT_V4_LOOP(n) {
+    const float4 u = reinterpret_cast<const float4 *>(a)[i4];
+    reinterpret_cast<double2 *>(b)[2 * i4] = make_double2(u.x, u.y);
+    reinterpret_cast<double2 *>(b)[2 * i4 + 1] = make_double2(u.z, u.w);
+  }
+  DEFT_V4_TAIL(n) b[i] = (double)a[i];
 }
 __global__ void k_to_f32_scaled(const double *__restrict__ a, double s, float *__restrict__ b,
                                 int n) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-    b[i] = (float)(s * a[i]);
-}
-// The Newton step's linear CG update without the preconditioner (which the
-// structure preconditioner applies afterwards): dx += alpha p, r -= alpha q.
-template <typename R>
-__global__ void k_newton_step(R alpha, const R *__restrict__ p, const R *__restrict__ q,
-                              R *__restrict__ dx, R *__restrict__ r, int N) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
-    dx[i] += alpha * p[i];
-    r[i] -= alpha * q[i];
+  DEFT_V4_LOOP(n) {
+    const double2 u = reinterpret_cast<const double2 *>(a)[2 * i4];
+    const double2 v = reinterpret_cast<const double2 *>(a)[2 * i4 + 1];
+    reinterpret_cast<float4 *>(b)[i4] =
+        make_float4((float)(s * u.x), (float)(s * u.y), (float)(s * v.x), (float)(s * v.y));
   }
+  DEFT_V4_TAIL(n) b[i] = (float)(s * a[i]);
 }
-
 // The Newton step's linear CG on FP32 vectors: z = M^-1 r with r.z, and
 // the fused update of k_newton_update (per-thread FP32 sums, FP64 across
 // threads and blocks in a fixed order).
@@ -1903,8 +1965,21 @@ __global__ void k_diag_precond_dot32(const float *__restrict__ n, const float *_
                                      unsigned int *counter, double *out) {
   __shared__ double red[32];
   float acc = 0;
-  #pragma unroll 4
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+  DEFT_V4_LOOP(N) {
+    const float4 nv = reinterpret_cast<const float4 *>(n)[i4];
+    const float4 rv = reinterpret_cast<const float4 *>(r)[i4];
+    const float4 mv = mask ? reinterpret_cast<const float4 *>(mask)[i4] : make_float4(1, 1, 1, 1);
+    float4 zv;
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+      const float zc =
+          precond_active(f4c(mv, c), f4c(nv, c)) ? f4c(rv, c) * f4c(nv, c) * inv_c : 0.0f;
+      f4s(zv, c, zc);
+      acc += f4c(rv, c) * zc;
+    }
+    reinterpret_cast<float4 *>(z)[i4] = zv;
+  }
+  DEFT_V4_TAIL(N) {
     const float m = mask ? mask[i] : 1.0f;
     const float nv = n[i], rv = r[i];
     const float zv = precond_active(m, nv) ? rv * nv * inv_c : 0.0f;
@@ -1922,8 +1997,29 @@ __global__ void k_newton_update32(float alpha, const float *__restrict__ p,
                                   unsigned int *counter, double *out) {
   __shared__ double red[32 * 2];
   float acc[2] = {0, 0};
-  #pragma unroll 4
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+  DEFT_V4_LOOP(N) {
+    const float4 pv = reinterpret_cast<const float4 *>(p)[i4];
+    const float4 qv = reinterpret_cast<const float4 *>(q)[i4];
+    const float4 nv = reinterpret_cast<const float4 *>(n)[i4];
+    const float4 mv = mask ? reinterpret_cast<const float4 *>(mask)[i4] : make_float4(1, 1, 1, 1);
+    float4 dv = reinterpret_cast<float4 *>(dx)[i4];
+    float4 rv = reinterpret_cast<float4 *>(r)[i4];
+    float4 zv;
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+      f4s(dv, c, f4c(dv, c) + alpha * f4c(pv, c));
+      const float rc = f4c(rv, c) - alpha * f4c(qv, c);
+      f4s(rv, c, rc);
+      const float zc = precond_active(f4c(mv, c), f4c(nv, c)) ? rc * f4c(nv, c) * inv_c : 0.0f;
+      f4s(zv, c, zc);
+      acc[0] += rc * rc;
+      acc[1] += rc * zc;
+    }
+    reinterpret_cast<float4 *>(dx)[i4] = dv;
+    reinterpret_cast<float4 *>(r)[i4] = rv;
+    reinterpret_cast<float4 *>(z)[i4] = zv;
+  }
+  DEFT_V4_TAIL(N) {
     dx[i] += alpha * p[i];
     const float rv = r[i] - alpha * q[i];
     r[i] = rv;
@@ -1936,6 +2032,43 @@ __global__ void k_newton_update32(float alpha, const float *__restrict__ p,
   }
   double accd[2] = {acc[0], acc[1]};
   finish_dots<2>(accd, red, partials, counter, out);
+}
+// The linear CG update before a structure-preconditioner application:
+// dx += alpha p, r -= alpha q.
+__global__ void k_newton_step32(float alpha, const float *__restrict__ p,
+                                const float *__restrict__ q, float *__restrict__ dx,
+                                float *__restrict__ r, int N) {
+  DEFT_V4_LOOP(N) {
+    const float4 pv = reinterpret_cast<const float4 *>(p)[i4];
+    const float4 qv = reinterpret_cast<const float4 *>(q)[i4];
+    float4 dv = reinterpret_cast<float4 *>(dx)[i4];
+    float4 rv = reinterpret_cast<float4 *>(r)[i4];
+    dv.x += alpha * pv.x;
+    dv.y += alpha * pv.y;
+    dv.z += alpha * pv.z;
+    dv.w += alpha * pv.w;
+    rv.x -= alpha * qv.x;
+    rv.y -= alpha * qv.y;
+    rv.z -= alpha * qv.z;
+    rv.w -= alpha * qv.w;
+    reinterpret_cast<float4 *>(dx)[i4] = dv;
+    reinterpret_cast<float4 *>(r)[i4] = rv;
+  }
+  DEFT_V4_TAIL(N) {
+    dx[i] += alpha * p[i];
+    r[i] -= alpha * q[i];
+  }
+}
+#undef DEFT_V4_LOOP
+#undef DEFT_V4_TAIL
+// ... and its FP64-vector form.
+__global__ void k_newton_step64(double alpha, const double *__restrict__ p,
+                                const double *__restrict__ q, double *__restrict__ dx,
+                                double *__restrict__ r, int N) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+    dx[i] += alpha * p[i];
+    r[i] -= alpha * q[i];
+  }
 }
 
 // One update of the Newton step's preconditioned linear CG in one pass:
@@ -3618,7 +3751,7 @@ int Engine::pc_apply32(const FmtSpec &f, const float *n, const float *r, const f
 int Engine::newton_step(double alpha, const double *p, const double *q, double *dx, double *r) {
   EngineImpl &e = *impl_;
   e.pre(kK_newton_update);
-  k_newton_step<double><<<e.dot_blocks, kThreads, 0, e.stream>>>(alpha, p, q, dx, r, e.g.NR);
+  k_newton_step64<<<e.dot_blocks, kThreads, 0, e.stream>>>(alpha, p, q, dx, r, e.g.NR);
   e.post(kK_newton_update);
   return e.check("newton_step");
 }
@@ -3626,7 +3759,7 @@ int Engine::newton_step(double alpha, const double *p, const double *q, double *
 int Engine::newton_step32(double alpha, const float *p, const float *q, float *dx, float *r) {
   EngineImpl &e = *impl_;
   e.pre(kslot<float>(kK_newton_update));
-  k_newton_step<float><<<e.dot_blocks, kThreads, 0, e.stream>>>((float)alpha, p, q, dx, r, e.g.NR);
+  k_newton_step32<<<e.dot_blocks, kThreads, 0, e.stream>>>((float)alpha, p, q, dx, r, e.g.NR);
   e.post(kslot<float>(kK_newton_update));
   return e.check("newton_step");
 }
