@@ -375,7 +375,7 @@ def run_ours(args, rank, world):
     # mixed solves driven from the host (one graph replay and sync per
     # evaluation; measured 0.3 ms per solve faster at 128^3 than the
     # device-driven graph) unless --device-driven (needs the preconditioner)
-    DEVICE = PC == _lib.PC_DENSITY and args.device_driven
+    DEVICE = PC in (_lib.PC_DENSITY, _lib.PC_STRUCTURE) and args.device_driven
     # FP32 stage exit |grad| < SWITCH x the bulk start's |grad|: with the
     # preconditioner, 1e-5 was the fastest of 1e-5, 3e-5, 3e-4 and the
     # relative rule on 30 held-out problems (python -m deft_gb300.warmstart

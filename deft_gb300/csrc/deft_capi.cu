@@ -94,6 +94,7 @@ struct deft_cg {
   int dkey_terms = -1, dkey_hs = -1, dkey_prec = -1;
   double dkey_kT = 0;
   const double *dkey_V = nullptr, *dkey_mask = nullptr, *dkey_pg = nullptr;
+  int dkey_pc = -1;
   // FP32 copies of the vectors for the mixed form's FP32 stage (f32_stage):
   // while f32_live they hold the state and the FP64 vectors but x are
   // stale; x is brought up to date after every step
@@ -2079,8 +2080,10 @@ namespace {
 int device_problem(deft_cg *c, deft::DcgProblem *p) {
   deft_fmt *f = c->f;
   if (int s = check_terms(f)) return s;
-  if (c->p.linesearch != DEFT_LS_SECANT || c->p.preconditioned != DEFT_PC_DENSITY)
-    return set_err(DEFT_ERR_ARG, "device-driven solves use DEFT_LS_SECANT with DEFT_PC_DENSITY");
+  if (c->p.linesearch != DEFT_LS_SECANT || (c->p.preconditioned != DEFT_PC_DENSITY &&
+                                            c->p.preconditioned != DEFT_PC_STRUCTURE))
+    return set_err(DEFT_ERR_ARG, "device-driven solves use DEFT_LS_SECANT with DEFT_PC_DENSITY "
+                                 "or DEFT_PC_STRUCTURE");
   if (c->p.precision > 0)
     return set_err(DEFT_ERR_ARG, "device-driven solves stop on gtol (no Precision rule)");
   if ((f->p.terms & (DEFT_TERM_VEFF | DEFT_TERM_SAFT)) || is_tensor(f))
@@ -2098,6 +2101,7 @@ int device_problem(deft_cg *c, deft::DcgProblem *p) {
   Engine *e = f->grid->eng;
   deft::DcgConfig &cf = p->cfg;
   cf.mixed = spec.precision == deft::kPrecisionMixed;
+  cf.structure = c->p.preconditioned == DEFT_PC_STRUCTURE ? 1 : 0;
   cf.gtol = c->p.gtol;
   cf.refine_rel = c->p.refine_rel;
   cf.refine_abs = c->p.refine_abs;
@@ -2159,12 +2163,13 @@ int deft_cg_solve_device(deft_cg *c, deft_cg_status *st) {
   const deft::FmtSpec &spec = p.spec;
   if (c->dgraph && (c->dkey_terms != spec.terms || c->dkey_hs != spec.hs ||
                     c->dkey_prec != spec.precision || c->dkey_kT != spec.kT ||
-                    c->dkey_V != p.v.V || c->dkey_mask != p.v.mask || c->dkey_pg != p.v.pg)) {
+                    c->dkey_V != p.v.V || c->dkey_mask != p.v.mask || c->dkey_pg != p.v.pg ||
+                    c->dkey_pc != p.cfg.structure)) {
     deft::dcg_free(c->dgraph);
     c->dgraph = nullptr;
   }
   if (!c->dgraph) {
-    if (p.eng->dev_prepare(spec)) return eng_err(p.eng);
+    if (p.eng->dev_prepare(spec, p.cfg.structure != 0)) return eng_err(p.eng);
     std::string err;
     c->dgraph = deft::dcg_build(&p, 1, &err);
     if (!c->dgraph) return set_err(DEFT_ERR_CUDA, err);
@@ -2175,6 +2180,7 @@ int deft_cg_solve_device(deft_cg *c, deft_cg_status *st) {
     c->dkey_V = p.v.V;
     c->dkey_mask = p.v.mask;
     c->dkey_pg = p.v.pg;
+    c->dkey_pc = p.cfg.structure;
   }
   deft::dcg_set_config(c->dgraph, 0, p.cfg, spec);
   deft::DcgOutcome o;
@@ -2223,7 +2229,7 @@ int deft_batch_solve_device(int device, int count, const deft_batch_problem *pro
     if (!s) s = deft_cg_create(fmts[i], cgp, &cgs[i]);
     if (!s) s = deft_cg_set_x(cgs[i], p.n_init, 0);
     if (!s) s = device_problem(cgs[i], &pr[i]);
-    if (!s && pr[i].eng->dev_prepare(pr[i].spec)) s = eng_err(pr[i].eng);
+    if (!s && pr[i].eng->dev_prepare(pr[i].spec, pr[i].cfg.structure != 0)) s = eng_err(pr[i].eng);
     if (s) g_err = "problem " + std::to_string(i) + ": " + g_err;
   }
   std::string err;

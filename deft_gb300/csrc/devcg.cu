@@ -9,8 +9,9 @@
 //      (FP32 in the mixed form) with g.d, g.g, g.g_old from the gradient
 //      kernel, then the search's decision; after an accepted trial the
 //      IF body forms the next direction (density preconditioner
-//      z = g n/(kT dV) with z.g and z.g_old in one pass, Polak-Ribiere beta
-//      from those, d = beta d - z, g_old = g)
+//      z = g n/(kT dV) with z.g and z.g_old in one pass, or the structure
+//      preconditioner's launches and their sums; Polak-Ribiere beta from
+//      those, d = beta d - z, g_old = g)
 //   1  FP64 energy + gradient (mixed form only): accepts or halves the last
 //      Newton step, stops at |g| < gtol, else (IF) stores the FP32 Hessian
 //      blocks at x and starts the step's linear CG (r = -g, z = M^-1 r,
@@ -204,6 +205,38 @@ __global__ void k_dcg_newton_update(DcgState *st, const double *__restrict__ p,
     acc[1] += rv * zv;
   }
   finish_to_state<2>(acc, partials, st);
+}
+
+// The structure preconditioner's forms: its sums (z.a, z.b, a.a at
+// res[0..3)) into st->red; the linear CG's start without z (r = -g,
+// dx = 0) and, after the preconditioner, p = z with r.z; the update without
+// z (dx += alpha p, r -= alpha q).
+__global__ void k_dcg_take(DcgState *st, const double *__restrict__ res, int i0, int i1) {
+  if (threadIdx.x || blockIdx.x) return;
+  st->red[0] = res[i0];
+  st->red[1] = res[i1];
+}
+__global__ void k_dcg_newton_init_s(const double *__restrict__ g, double *__restrict__ r,
+                                    double *__restrict__ dx, int N) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+    r[i] = -g[i];
+    dx[i] = 0.0;
+  }
+}
+__global__ void k_dcg_pcopy_take(DcgState *st, const double *__restrict__ res,
+                                 double *__restrict__ p, const double *__restrict__ z, int N) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) st->red[0] = res[0];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x)
+    p[i] = z[i];
+}
+__global__ void k_dcg_newton_step(const DcgState *__restrict__ st, const double *__restrict__ p,
+                                  const double *__restrict__ q, double *__restrict__ dx,
+                                  double *__restrict__ r, int N) {
+  const double alpha = st->alpha_n;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+    dx[i] += alpha * p[i];
+    r[i] -= alpha * q[i];
+  }
 }
 
 // p = z + beta p.
@@ -633,9 +666,15 @@ bool add_solve(Builder &b, Solve &sv) {
       }, &sinks))
     return false;
   if (!b.cond(sb[0], sinks, h_dir, cudaGraphCondTypeIf, 1, &n, &ib)) return false;
-  if (!cap(kSeqDirection, 3, ib, none, [&] {
-        k_dcg_precond_dots<<<nb, kThreads, 0, s>>>(st, v.x, v.g, mask, v.gold, inv_c, v.pg, N,
-                                                   part);
+  const bool spc = sv.p.cfg.structure != 0;
+  if (!cap(kSeqDirection, spc ? 3 : 3, ib, none, [&] {
+        if (spc) {
+          if (e->dev_pc(stage, v.x, v.g, mask, v.pg, v.g, v.gold)) return false;
+          k_dcg_take<<<1, 32, 0, s>>>(st, res, 0, 1);
+        } else {
+          k_dcg_precond_dots<<<nb, kThreads, 0, s>>>(st, v.x, v.g, mask, v.gold, inv_c, v.pg, N,
+                                                     part);
+        }
         k_dcg_decide_direction<<<1, 32, 0, s>>>(st);
         k_dcg_direction<<<nb, kThreads, 0, s>>>(st, v.d, v.pg, v.g, v.gold, N);
         return true;
@@ -671,10 +710,16 @@ bool add_solve(Builder &b, Solve &sv) {
       }, nullptr))
     return false;
   if (!b.cond(sb[1], {nbt}, h_setup, cudaGraphCondTypeIf, 1, &n, &ib)) return false;
-  if (!cap(kSeqSetup, 2, ib, none, [&] {
+  if (!cap(kSeqSetup, spc ? 3 : 2, ib, none, [&] {
         if (e->dev_hess_setup(f32, v.x)) return false;
-        k_dcg_newton_init<<<nb, kThreads, 0, s>>>(st, v.g, v.x, mask, inv_c, v.gold, v.d, v.dx,
-                                                  N, part);
+        if (spc) {
+          k_dcg_newton_init_s<<<nb, kThreads, 0, s>>>(v.g, v.gold, v.dx, N);
+          if (e->dev_pc(f32, v.x, v.gold, mask, v.g, v.gold, nullptr)) return false;
+          k_dcg_pcopy_take<<<nb, kThreads, 0, s>>>(st, res, v.d, v.g, N);
+        } else {
+          k_dcg_newton_init<<<nb, kThreads, 0, s>>>(st, v.g, v.x, mask, inv_c, v.gold, v.d,
+                                                    v.dx, N, part);
+        }
         k_dcg_decide_init<<<1, 32, 0, s>>>(st);
         return true;
       }, nullptr))
@@ -691,9 +736,16 @@ bool add_solve(Builder &b, Solve &sv) {
   cudaGraphNode_t nupd;
   if (!b.cond(sb[2], sinks, h_upd, cudaGraphCondTypeIf, 1, &nupd, &ib)) return false;
   if (!b.handle(ib, &h_pupd, 0)) return false;
-  if (!cap(kSeqUpdate, 2, ib, none, [&] {
-        k_dcg_newton_update<<<nb, kThreads, 0, s>>>(st, v.d, v.q, v.dx, v.gold, v.x, mask, inv_c,
-                                                    v.g, N, part);
+  if (!cap(kSeqUpdate, spc ? 3 : 2, ib, none, [&] {
+        if (spc) {
+          // r.r and r.z from the preconditioner's sums (a.a at res[2], z.a at res[0])
+          k_dcg_newton_step<<<nb, kThreads, 0, s>>>(st, v.d, v.q, v.dx, v.gold, N);
+          if (e->dev_pc(f32, v.x, v.gold, mask, v.g, v.gold, nullptr)) return false;
+          k_dcg_take<<<1, 32, 0, s>>>(st, res, 2, 0);
+        } else {
+          k_dcg_newton_update<<<nb, kThreads, 0, s>>>(st, v.d, v.q, v.dx, v.gold, v.x, mask,
+                                                      inv_c, v.g, N, part);
+        }
         k_dcg_decide_update<<<1, 32, 0, s>>>(st, h_pupd, h_apply);
         return true;
       }, &sinks))
@@ -815,7 +867,7 @@ int dcg_run(DcgGraph *gr, cudaStream_t stream, DcgOutcome *out, std::string *err
   };
   for (int i = 0; i < count; i++) {
     Solve &sv = gr->solves[i];
-    if (sv.p.eng->dev_prepare(sv.p.spec)) {
+    if (sv.p.eng->dev_prepare(sv.p.spec, sv.p.cfg.structure != 0)) {
       if (err) *err = sv.p.eng->last_error();
       return DEFT_ERR_CUDA;
     }

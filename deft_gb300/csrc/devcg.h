@@ -27,6 +27,7 @@ struct DcgConfig {
   int maxiter;        // 0: no limit
   int max_loops;      // evaluations + products budget of the device loop
   int mixed;          // 1: FP32 stage + Newton refinement on the FP64 gradient
+  int structure = 0;  // 1: the structure preconditioner (else the density one)
 };
 
 struct DcgOutcome {
@@ -45,7 +46,8 @@ struct DcgProblem {
 // One executable graph for a list of solves (one WHILE node each).
 struct DcgGraph;
 
-// Builds the graph; every problem's engine must have run dev_prepare.  The
+// Builds the graph; every problem's engine must have run dev_prepare (with
+// the structure preconditioner's table when cfg.structure).  The
 // problems' engines may share a stream or not; capture uses each engine's
 // own stream.  Returns null and sets *err on failure.
 DcgGraph *dcg_build(const DcgProblem *p, int count, std::string *err);

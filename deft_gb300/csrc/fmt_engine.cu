@@ -3329,12 +3329,26 @@ class EngineImpl {
             "and ideal-gas terms and Nz = 32, 64, 128 or 256";
       return -1;
     }
-    if (upload_args(f)) return -1;
+    if (upload_args(f) || pc_prepare(f)) return -1;
+    const double *da[1] = {reinterpret_cast<const double *>(a)};
+    const double *db[1] = {reinterpret_cast<const double *>(b)};
+    const GraphKey key =
+        graph_key(std::is_same<R, double>::value ? 10 : 11, 4, f, n, r, mask, z, 1, da, db);
+    if (run_graphed(key, [&] { return pc_launch<R>(n, r, mask, z, a, b); })) return -1;
+    return read_results(3, out_host, "structure preconditioner");
+  }
+  // The multiplier table, (re)made on the stream when the parameters change
+  // (after upload_args(f)).
+  int pc_prepare(const FmtSpec &f) {
+    if (!structure_ok(f)) {
+      err = "structure preconditioner: needs the hard-sphere (White Bear, Rosenfeld or mark II) "
+            "and ideal-gas terms and Nz = 32, 64, 128 or 256";
+      return -1;
+    }
     if (!(la_last.pc_inv_nb > 0)) {
       err = "structure preconditioner: no bulk density for these parameters";
       return -1;
     }
-    // the multiplier table, (re)made on the stream when the parameters change
     if (!pc_table && alloc(&pc_table, sizeof(float) * (size_t)g.NC)) return -1;
     if (!pc_table_valid || memcmp(&pc_table_la, &la_last, sizeof(LocalArgs))) {
       pre(kslot<float>(kK_struct_pc));
@@ -3344,13 +3358,9 @@ class EngineImpl {
       pc_table_la = la_last;
       pc_table_valid = true;
     }
-    const double *da[1] = {reinterpret_cast<const double *>(a)};
-    const double *db[1] = {reinterpret_cast<const double *>(b)};
-    const GraphKey key =
-        graph_key(std::is_same<R, double>::value ? 10 : 11, 4, f, n, r, mask, z, 1, da, db);
-    if (run_graphed(key, [&] { return pc_launch<R>(n, r, mask, z, a, b); })) return -1;
-    return read_results(3, out_host, "structure preconditioner");
+    return 0;
   }
+
   template <typename R>
   int pc_launch(const R *n, const R *r, const R *mask, R *z, const R *a, const R *b) {
     float2 *w = reinterpret_cast<float2 *>(spec0<float>());
@@ -3852,13 +3862,14 @@ int Engine::scal_add_dot(double beta, double *d, double alpha, const double *g, 
   return e.read_results(1, out_host, "scal_add_dot");
 }
 
-int Engine::dev_prepare(const FmtSpec &f) {
+int Engine::dev_prepare(const FmtSpec &f, bool structure) {
   EngineImpl &e = *impl_;
   if (f.terms & kTermHS) {
     if (e.ensure_table<float>(f.R)) return -1;
     if (e.df_on ? e.ensure_table<dfl>(f.R) : e.ensure_table<double>(f.R)) return -1;
   }
   if (e.upload_args(f)) return -1;
+  if (structure && e.pc_prepare(f)) return -1;
   if (!e.hess && (e.alloc(&e.hess, sizeof(float) * kHessPacked * (size_t)e.g.NR) ||
                   e.alloc(&e.hloc, sizeof(float) * (size_t)e.g.NR)))
     return -1;
@@ -3884,6 +3895,11 @@ int Engine::dev_eval(const FmtSpec &f, const double *n, const double *V, const d
 }
 
 int Engine::dev_hess_setup(const FmtSpec &f, const double *n) { return impl_->hess_setup(f, n); }
+
+int Engine::dev_pc(const FmtSpec &, const double *n, const double *r, const double *mask,
+                   double *z, const double *a, const double *b) {
+  return impl_->pc_launch<double>(n, r, mask, z, a, b);
+}
 
 int Engine::dev_hvp(const FmtSpec &f, const double *dx, const double *mask, double *out) {
   return impl_->hvp_launch(f, dx, mask, out, true);

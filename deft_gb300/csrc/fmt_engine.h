@@ -223,7 +223,7 @@ class Engine {
   // results stay in device memory, so the sequences can be captured into the
   // bodies of conditional graph nodes.  dev_prepare (weight tables of both
   // forms, parameters, Hessian buffers) runs first, outside any capture.
-  int dev_prepare(const FmtSpec &f);
+  int dev_prepare(const FmtSpec &f, bool structure = false);
   // Energy and gradient in f's precision, with the dot products grad.db[i]
   // (i < kd <= 3; db[i] == grad: |grad|^2) taken by the gradient kernel:
   // energy at dev_results()[6], terms at [0..6), dots at [8..8+kd).
@@ -232,6 +232,10 @@ class Engine {
   int dev_hess_setup(const FmtSpec &f, const double *n);
   // out = H dx (FP32 transforms), dx.out at dev_results()[0].
   int dev_hvp(const FmtSpec &f, const double *dx, const double *mask, double *out);
+  // The structure preconditioner's launches (its table made by dev_prepare):
+  // z = M^-1 r with (z.a, z.b, a.a) at dev_results()[0..3).
+  int dev_pc(const FmtSpec &f, const double *n, const double *r, const double *mask, double *z,
+             const double *a, const double *b);
   double *dev_results() const;
   // Blocks of the FP64 vector kernels (a multiple of the SM count, at most
   // one block per 256 points).

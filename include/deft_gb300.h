@@ -306,7 +306,8 @@ int deft_cg_solve(deft_cg *cg, deft_cg_status *st);
  * papers/contact/figs/walls.cpp:104-110): one CUDA graph launch runs the
  * whole solve, every line-search, direction and stop decision taken by a
  * kernel from scalars in device memory, so the host waits once.  For
- * DEFT_LS_SECANT with DEFT_PC_DENSITY, without the Precision rule, on the
+ * DEFT_LS_SECANT with DEFT_PC_DENSITY or DEFT_PC_STRUCTURE, without the
+ * Precision rule, on the
  * fused functionals (no DEFT_TERM_VEFF / SAFT, no tensor kinds): FP64 form
  * (the secant CG to gtol) or mixed form (FP32 stage, then Newton steps on
  * the FP64 gradient).  Starts from the current x (deft_cg_set_x); the loop
@@ -386,7 +387,8 @@ int deft_batch_solve(int device, int count, const deft_batch_problem *problems,
  * minimiser, and one CUDA graph holds their device-driven solves
  * (deft_cg_solve_device) as independent conditional WHILE nodes, so all of
  * them run concurrently from a single cudaGraphLaunch and the host waits
- * once.  cg must be DEFT_LS_SECANT with DEFT_PC_DENSITY (no Precision rule);
+ * once.  cg must be DEFT_LS_SECANT with DEFT_PC_DENSITY or DEFT_PC_STRUCTURE
+ * (no Precision rule);
  * n_out gets each converged profile; status_out[i] each outcome. */
 int deft_batch_solve_device(int device, int count, const deft_batch_problem *problems,
                             const deft_cg_params *cg, deft_cg_status *status_out);

@@ -9,6 +9,8 @@ M^-1 r = s F^-1[F[s r] / H_b(k)], s = sqrt(n / n_b) on the free points.
 - Solves with it, FP64 and mixed, converge to the FP64 solution at
   |grad F| < 1e-12 within 1e-8 of the density scale and take fewer
   evaluations than with the density preconditioner from the same start.
+- The device-driven solve (one graph launch) with it follows the
+  host-driven one.
 - Unsupported settings are refused."""
 import ctypes
 
@@ -155,13 +157,44 @@ def test_structure_preconditioner_refuses_unsupported_settings():
         q = _lib.CgParams(_lib.LS_QUADRATIC_REF, 1e-9, 0, 0.1, 0.0, 0.0, _lib.PC_STRUCTURE, 0.0,
                           0.0, 0, 0)
         assert f.L.deft_cg_create(f.h, ctypes.byref(q), ctypes.byref(h)) == _lib.ERR_ARG
-        # device-driven solves take the density preconditioner only
-        cg = CG(f, gtol=1e-9, step=1.0, preconditioned=_lib.PC_STRUCTURE)
-        cg.set_x(s.n0.reshape(-1))
-        code, _ = cg.solve_device()
-        assert code == _lib.ERR_ARG
-        cg.close()
         f.close()
         g.close()
     finally:
         ctx.close()
+
+
+@pytest.mark.parametrize("precision", [_lib.PRECISION_MIXED, _lib.PRECISION_FP64])
+def test_device_driven_structure_preconditioned_solve(precision):
+    from tests.capi import CG, Ctx, Fmt, Grid
+    s = _problem(1)
+    mask = s.mask.reshape(-1)
+    ctx = Ctx(0)
+    g = Grid(ctx, s.lat, s.shape)
+    f = Fmt(g, R=s.R, kT=s.kT, mu=s.mu, terms=TERMS, mask=mask, precision=precision)
+    try:
+        gtol = 3e-10 if precision == _lib.PRECISION_MIXED else 1e-9
+        kw = dict(gtol=gtol, maxiter=3000, step=1.0, preconditioned=_lib.PC_STRUCTURE)
+        host = CG(f, **kw)
+        host.set_x(s.n0.reshape(-1))
+        code, st_h = host.solve()
+        assert code == 0 and st_h.converged
+        it_h, ev_h, x_h = st_h.iter, st_h.evals, host.get_x()
+        host.close()
+        dev = CG(f, **kw)
+        for rep in range(2):  # the second call replays the same graph
+            dev.set_x(s.n0.reshape(-1))
+            code, st_d = dev.solve_device()
+            assert code == 0, _lib.load().deft_last_error()
+            assert st_d.converged and st_d.gnorm < gtol
+            x_d = dev.get_x()
+            if rep == 0:
+                first = x_d.copy()
+            else:
+                assert np.array_equal(x_d, first)
+        dev.close()
+        assert abs(st_d.iter - it_h) <= max(2, it_h // 5)
+        assert abs(st_d.evals - ev_h) <= max(4, ev_h // 5)
+        assert np.abs(x_d - x_h).max() <= 1e-8 * float(np.abs(x_h).max())
+    finally:
+        for o in (f, g, ctx):
+            o.close()
