@@ -972,7 +972,7 @@ __global__ void __launch_bounds__(kThreads,
                                                     const R *__restrict__ V, Geom g,
                                                     FftPlan pz, FastDiv fP, FastDiv f2P,
                                                     FastDiv f5P, const LocalArgs *__restrict__ lap,
-                                                    double *partials) {
+                                                    double *partials, double *__restrict__ lnq) {
   const LocalArgs la = *lap;
   const int P = (int)fP.d;
   using C = typename Cplx<T>::type;
@@ -1010,7 +1010,14 @@ __global__ void __launch_bounds__(kThreads,
         tacc[2] += U(phi[2]);
       }
       const U nv = U(n[r]);
-      if (la.terms & kTermIdeal) tacc[3] += ideal_energy_t<U>(nv, inv_nQ);
+      if (la.terms & kTermIdeal) {
+        // ln(n/nQ) once: the ideal-gas energy here, kept (lnq) for the
+        // gradient kernel of the same evaluation (FP64 forms: an FP64 log
+        // costs about 25 operations of GB300's narrow FP64 pipe)
+        const U lg = wb_log<U>(nv * inv_nQ);
+        tacc[3] += nv == U(0) ? U(0) : nv * (lg - U(1));
+        if (lnq) lnq[r] = double(lg);
+      }
       if (la.terms & kTermMu) tacc[4] += nv;
       if (la.terms & kTermVext) tacc[5] += U(V[r]) * nv;
     }
@@ -1033,7 +1040,8 @@ __global__ void DEFT_FFT_BOUNDS(RN) k_z_grad(const typename Cplx<T>::type *__res
                                                      const double *__restrict__ mask,
                                                      double *__restrict__ grad, Geom g, FftPlan pz,
                                                      FastDiv fP, const LocalArgs *__restrict__ lap,
-                                                     GradDots gd) {
+                                                     GradDots gd,
+                                                     const double *__restrict__ lnq) {
   const LocalArgs la = *lap;
   const int P = (int)fP.d;
   using C = typename Cplx<T>::type;
@@ -1062,8 +1070,8 @@ __global__ void DEFT_FFT_BOUNDS(RN) k_z_grad(const typename Cplx<T>::type *__res
       conv = U((ll & 1) ? v.y : v.x);
     }
     U loc = 0;
-    const U nv = U(n[r]);
-    if (la.terms & kTermIdeal) loc += U(la.kT) * wb_log<U>(nv * U(la.inv_nQ));
+    if (la.terms & kTermIdeal)
+      loc += U(la.kT) * (lnq ? U(lnq[r]) : wb_log<U>(U(n[r]) * U(la.inv_nQ)));
     if (la.terms & kTermMu) loc += U(la.mu);
     if (la.terms & kTermVext) loc += U(V[r]);
     U gr = conv + U(la.dV) * loc;
@@ -2466,6 +2474,7 @@ class EngineImpl {
     cudaFree(wvf);
     cudaFree(hess);
     cudaFree(pc_table);
+    cudaFree(lnq);
     clear_graphs();
     cudaFree(la_dev);
     cudaFree(hloc);
@@ -3158,6 +3167,7 @@ class EngineImpl {
            double *E_host, double *terms_host, int kd = 0, const double *const *da = nullptr,
            const double *const *db = nullptr, double *dots_host = nullptr) {
     if ((f.terms & kTermHS) && ensure_table<T>(f.R)) return -1;
+    if (sizeof(T) != 4 && grad && (f.terms & kTermHS) && ensure_lnq()) return -1;
     if (upload_args(f)) return -1;
     const GraphKey key =
         graph_key(grad ? 1 : 0, is_df<T> ? 9 : (int)sizeof(T), f, n, V, mask, grad, kd, da, db);
@@ -3254,10 +3264,12 @@ class EngineImpl {
           constexpr int RN = decltype(rn)::value;
           if (grad)
             k_z_phi<T, true, RN, R><<<nblk, kThreads, t.smem_phi, stream>>>(
-                spec5<T>(), n, V, g, plan<T>(2), t.fPphi, t.f2Pphi, t.f5Pphi, la_dev, partials);
+                spec5<T>(), n, V, g, plan<T>(2), t.fPphi, t.f2Pphi, t.f5Pphi, la_dev, partials,
+                lnq_for<T>(f));
           else
             k_z_phi<T, false, RN, R><<<nblk, kThreads, t.smem_phi, stream>>>(
-                spec5<T>(), n, V, g, plan<T>(2), t.fPphi, t.f2Pphi, t.f5Pphi, la_dev, partials);
+                spec5<T>(), n, V, g, plan<T>(2), t.fPphi, t.f2Pphi, t.f5Pphi, la_dev, partials,
+                nullptr);
         });
       }
       post(kslot<T>(grad ? kK_z_phi_grad : kK_z_phi_energy));
@@ -3294,7 +3306,8 @@ class EngineImpl {
       } else if constexpr (r64) {
         with_rn<T>(plan<T>(2), [&](auto rn) {
           k_z_grad<T, decltype(rn)::value><<<pairs_tiles(t.Pz), kThreads, t.smem_z, stream>>>(
-              spec0<T>(), n, V, mask, grad, g, plan<T>(2), t.fPz, la_dev, gd ? *gd : GradDots{});
+              spec0<T>(), n, V, mask, grad, g, plan<T>(2), t.fPz, la_dev, gd ? *gd : GradDots{},
+              (f.terms & kTermHS) ? lnq_for<T>(f) : nullptr);
         });
       } else {
         err = "FP32 vectors need the warp z transforms";
@@ -3406,6 +3419,13 @@ class EngineImpl {
     return check("structure preconditioner");
   }
 
+  // ln(n/nQ) of the FP64 forms' last Phi pass, for their gradient kernel
+  // (allocated outside graph capture: ensure_lnq)
+  double *lnq = nullptr;
+  int ensure_lnq() { return lnq ? 0 : alloc(&lnq, sizeof(double) * (size_t)g.NR); }
+  template <typename T> double *lnq_for(const FmtSpec &f) const {
+    return (sizeof(T) != 4 && (f.terms & kTermIdeal)) ? lnq : nullptr;
+  }
   float *pc_table = nullptr;  // P(k) / N of the structure preconditioner
   LocalArgs pc_table_la{};    // the parameters it was made for
   bool pc_table_valid = false;
@@ -3869,6 +3889,7 @@ int Engine::dev_prepare(const FmtSpec &f, bool structure) {
     if (e.df_on ? e.ensure_table<dfl>(f.R) : e.ensure_table<double>(f.R)) return -1;
   }
   if (e.upload_args(f)) return -1;
+  if ((f.terms & kTermHS) && e.ensure_lnq()) return -1;
   if (structure && e.pc_prepare(f)) return -1;
   if (!e.hess && (e.alloc(&e.hess, sizeof(float) * kHessPacked * (size_t)e.g.NR) ||
                   e.alloc(&e.hloc, sizeof(float) * (size_t)e.g.NR)))
@@ -4206,7 +4227,7 @@ int noalloc_energy_grad(const GridSpec &s, const FmtSpec &f, const double *n, co
         S0, S5, w3, w2, wv, g, px, t.fBxf, la_dev);
     k_y_fft<double, +1><<<ygrid5, kThreads, t.smem_y, stream>>>(S5, g, py, t.fBy);
     k_z_phi<double, true><<<nblk_phi, kThreads, t.smem_phi, stream>>>(
-        S5, n, V, g, pz, t.fPphi, t.f2Pphi, t.f5Pphi, la_dev, partials);
+        S5, n, V, g, pz, t.fPphi, t.f2Pphi, t.f5Pphi, la_dev, partials, nullptr);
     k_y_fft<double, -1><<<ygrid5, kThreads, t.smem_y, stream>>>(S5, g, py, t.fBy);
     k_x_conv_adj<double><<<xt, kThreads, t.smem_xc, stream>>>(S5, S0, w3, w2, wv, g, px, t.fBxc,
                                                               t.f5Bxc, la_dev);
@@ -4215,7 +4236,7 @@ int noalloc_energy_grad(const GridSpec &s, const FmtSpec &f, const double *n, co
     k_local_energy<double><<<nblk, kThreads, 0, stream>>>(n, V, g, la_dev, partials);
   }
   k_z_grad<double><<<ptiles_z, kThreads, t.smem_z, stream>>>(S0, n, V, mask, grad, g, pz, t.fPz,
-                                                             la_dev, GradDots{});
+                                                             la_dev, GradDots{}, nullptr);
   k_reduce_terms<<<1, kReduceThreads, 0, stream>>>(partials, nblk, g.dV, results);
   double res[8];
   e = cudaGetLastError();
