@@ -1336,6 +1336,30 @@ __global__ void __launch_bounds__(32 * kZWarps)
   float2 *wb = reinterpret_cast<float2 *>(smem_raw) + warp * warp_buf_elems<E>();
   const int l0 = 2 * (blockIdx.x * kZWarps + warp);
   const bool hs = la.terms & kTermHS;
+  // the pointwise inputs (and the local gradient terms) first, so their
+  // loads are in flight while the line is transformed
+  float loc[2][E], mk[2][E], bv[3][2][E];
+#pragma unroll
+  for (int half = 0; half < 2; half++) {
+    const bool ok = l0 + half < g.lines;
+#pragma unroll
+    for (int m = 0; m < E; m++) {
+      const size_t r = (size_t)(l0 + half) * N + lane + 32 * m;
+      float lc = 0, mv = 1;
+      if (ok) {
+        if (la.terms & kTermIdeal)
+          lc += float(la.kT) * wb_log<float>(float(n[r]) * float(la.inv_nQ));
+        if (la.terms & kTermMu) lc += float(la.mu);
+        if (la.terms & kTermVext) lc += float(V[r]);
+        if (la.terms & kTermMask) mv = float(mask[r]);
+      }
+      loc[half][m] = lc;
+      mk[half][m] = mv;
+#pragma unroll
+      for (int i = 0; i < 3; i++)
+        bv[i][half][m] = (ok && i < gd.k && gd.b[i]) ? float(gd.b[i][r]) : 0.f;
+    }
+  }
   float2 v[E];
   if (hs) {
     float2 w[4];
@@ -1355,20 +1379,12 @@ __global__ void __launch_bounds__(32 * kZWarps)
     for (int m = 0; m < E; m++) {
       const size_t r = (size_t)line * N + lane + 32 * m;
       const float conv = half ? v[m].y : v[m].x;
-      float loc = 0;
-      const float nv = float(n[r]);
-      if (la.terms & kTermIdeal) loc += float(la.kT) * wb_log<float>(nv * float(la.inv_nQ));
-      if (la.terms & kTermMu) loc += float(la.mu);
-      if (la.terms & kTermVext) loc += float(V[r]);
-      float gr = conv + float(la.dV) * loc;
-      if (la.terms & kTermMask) {
-        const float mk = float(mask[r]);
-        gr = mk == 0.f ? 0.f : mk * gr;
-      }
+      float gr = conv + float(la.dV) * loc[half][m];
+      if (la.terms & kTermMask) gr = mk[half][m] == 0.f ? 0.f : mk[half][m] * gr;
       grad[r] = R(gr);
 #pragma unroll
       for (int i = 0; i < 3; i++)
-        if (i < gd.k) dacc[i] += gr * (gd.b[i] ? float(gd.b[i][r]) : gr);
+        if (i < gd.k) dacc[i] += gr * (gd.b[i] ? bv[i][half][m] : gr);
     }
   }
   if (gd.k > 0) {

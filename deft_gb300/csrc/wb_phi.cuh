@@ -46,7 +46,7 @@ template <> struct WbConst<dfl> {
 };
 template <> struct WbConst<float> {
   static constexpr float series_below = 0.3f;
-  static constexpr int series_terms = 18;
+  static constexpr int series_terms = 14;  // truncation below FP32 rounding at e < 0.3
   static constexpr float m2_below = 0.5f;
   static constexpr int m2_terms = 30;
 };
