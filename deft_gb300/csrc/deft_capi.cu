@@ -1146,13 +1146,21 @@ int cg_axpy(deft_cg *c, double a, const double *v) {
 // only has to reach the switch to the Newton refinement; with its first
 // trial at the last accepted step, 0.5 accepts most first trials (one
 // evaluation per iteration) and saved about 30 % of the evaluations of
-// 48^3 wall + solute problems against 0.1.
+// 48^3 wall + solute problems against 0.1.  With the structure
+// preconditioner the directions are closer to Newton steps and a stricter
+// search pays: 0.3 took 20 held-out 128^3 solves from 14.3 to 13.9 ms
+// (12.7 iterations against 15.4; 0.1, 0.2, 0.7: 14.3, 14.3, 14.8 ms).
+// DEFT_SECANT_C2 in the environment overrides both.
 #ifndef DEFT_SECANT_C2_MIXED
 #define DEFT_SECANT_C2_MIXED 0.5
 #endif
+#ifndef DEFT_SECANT_C2_STRUCTURE
+#define DEFT_SECANT_C2_STRUCTURE 0.3
+#endif
 
-// The FP32 stage of the mixed form under the density preconditioner: first
-// trial at the last accepted step, acceptance at DEFT_SECANT_C2_MIXED.
+// The FP32 stage of the mixed form under the density or structure
+// preconditioner: first trial at the last accepted step, acceptance at
+// DEFT_SECANT_C2_MIXED / DEFT_SECANT_C2_STRUCTURE.
 bool fast_stage(const deft_cg *c, const deft::FmtSpec &spec) {
   return spec.precision != deft::kPrecisionFP64 && pg_in_step(c);
 }
@@ -1343,7 +1351,14 @@ int f32_leave(deft_cg *c) {
 template <typename V>
 int secant_search(deft_cg *c, const deft::FmtSpec &spec, double E0, double s0) {
   using CV = CgVec<V>;
-  const double c2 = fast_stage(c, spec) ? DEFT_SECANT_C2_MIXED : 0.1;
+  static const double c2_env = [] {
+    const char *ev = getenv("DEFT_SECANT_C2");
+    return ev && atof(ev) > 0 && atof(ev) < 1 ? atof(ev) : 0.0;
+  }();
+  const double c2_fast = c2_env > 0 ? c2_env
+                         : c->p.preconditioned == DEFT_PC_STRUCTURE ? DEFT_SECANT_C2_STRUCTURE
+                                                                    : DEFT_SECANT_C2_MIXED;
+  const double c2 = fast_stage(c, spec) ? c2_fast : 0.1;
   double lo = 0, s_lo = s0, hi = -1, s_hi = 0, plo = 0, s_plo = s0;
   double a = c->alpha, at = 0;
   // energies only guard against rises; FP32 sums carry ~1e-7 relative noise

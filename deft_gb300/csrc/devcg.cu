@@ -778,7 +778,9 @@ DcgState initial_state(const DcgConfig &c) {
   // the mixed form's FP32 stage: first trial at the last accepted step,
   // acceptance at half the start slope, energy rises below FP32 rounding
   s.fast = c.mixed;
-  s.c2 = c.mixed ? 0.5 : 0.1;
+  // (the host-driven minimiser's values: 0.3 with the structure
+  // preconditioner, 0.5 with the density one)
+  s.c2 = c.mixed ? (c.structure ? 0.3 : 0.5) : 0.1;
   s.etol_rel = c.mixed ? 1e-6 : 1e-12;
   s.alpha = c.step > 0 ? c.step : 1.0;
   s.mode = kModeStage;
