@@ -1727,7 +1727,22 @@ __global__ void k_reduce_terms(const double *partials, int nblk, double dV, doub
                                const double *dpart = nullptr, int dk = 0, int dblk = 0) {
   __shared__ double red[32 * kNumTerms];
   double acc[kNumTerms] = {0, 0, 0, 0, 0, 0};
-  for (int b = threadIdx.x; b < nblk; b += blockDim.x)
+  // four blocks' partials in flight per thread and step (one block is
+  // latency-bound on these loads), then the remainder; a fixed order
+  int b = threadIdx.x;
+  for (; b + 3 * (int)blockDim.x < nblk; b += 4 * blockDim.x) {
+    double v[4][kNumTerms];
+#pragma unroll
+    for (int u = 0; u < 4; u++)
+#pragma unroll
+      for (int t = 0; t < kNumTerms; t++)
+        v[u][t] = partials[(size_t)(b + u * blockDim.x) * kNumTerms + t];
+#pragma unroll
+    for (int u = 0; u < 4; u++)
+#pragma unroll
+      for (int t = 0; t < kNumTerms; t++) acc[t] += v[u][t];
+  }
+  for (; b < nblk; b += blockDim.x)
     for (int t = 0; t < kNumTerms; t++) acc[t] += partials[(size_t)b * kNumTerms + t];
   block_reduce<kNumTerms>(acc, red);
   if (threadIdx.x == 0) {
@@ -1741,8 +1756,20 @@ __global__ void k_reduce_terms(const double *partials, int nblk, double dV, doub
   if (dk > 0) {
     __syncthreads();
     double d[3] = {0, 0, 0};
-    for (int b = threadIdx.x; b < dblk; b += blockDim.x)
-      for (int t = 0; t < 3; t++) d[t] += dpart[(size_t)b * 3 + t];
+    int b2 = threadIdx.x;
+    for (; b2 + 3 * (int)blockDim.x < dblk; b2 += 4 * blockDim.x) {
+      double v[4][3];
+#pragma unroll
+      for (int u = 0; u < 4; u++)
+#pragma unroll
+        for (int t = 0; t < 3; t++) v[u][t] = dpart[(size_t)(b2 + u * blockDim.x) * 3 + t];
+#pragma unroll
+      for (int u = 0; u < 4; u++)
+#pragma unroll
+        for (int t = 0; t < 3; t++) d[t] += v[u][t];
+    }
+    for (; b2 < dblk; b2 += blockDim.x)
+      for (int t = 0; t < 3; t++) d[t] += dpart[(size_t)b2 * 3 + t];
     block_reduce<3>(d, red);
     if (threadIdx.x == 0)
       for (int t = 0; t < dk; t++) out[8 + t] = d[t];
