@@ -31,7 +31,7 @@ EXPORTS = (
     "deft_fmt_set_mask", "deft_fmt_energy", "deft_fmt_energy_grad", "deft_fmt_energy_grad_pgrad",
     "deft_fmt_weighted", "deft_fmt_contact", "deft_fmt_set_saft",
     "deft_fmt_hessian_vector", "deft_fmt_precondition",
-    "deft_find_chemical_potential",
+    "deft_find_chemical_potential", "deft_bulk_density",
     "deft_fmt_energy_grad_noalloc", "deft_noalloc_scratch_bytes",
     "deft_cg_create", "deft_cg_destroy", "deft_cg_set_params", "deft_cg_set_x", "deft_cg_get_x", "deft_cg_x_device",
     "deft_cg_step", "deft_cg_solve", "deft_cg_solve_device", "deft_cg_checkpoint", "deft_cg_restore", "deft_cg_set_log", "deft_batch_solve",
@@ -134,6 +134,8 @@ def load():
         "deft_fmt_precondition": (ctypes.c_int, [_vp, _dp, _dp, ctypes.c_int, _dp, _dp]),
         "deft_find_chemical_potential": (ctypes.c_int, [ctypes.c_double, ctypes.c_double,
                                                         ctypes.c_double, _dp]),
+        "deft_bulk_density": (ctypes.c_int, [ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                             ctypes.c_int, _dp]),
         "deft_fmt_energy_grad_noalloc": (ctypes.c_int, [_dp, ctypes.c_int, ctypes.c_int,
                                                          ctypes.c_int, ctypes.POINTER(FmtParams),
                                                          _dp, _dp, _dp, _dp, _dp, _dp, _vp]),

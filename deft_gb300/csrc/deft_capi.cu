@@ -819,6 +819,15 @@ int deft_fmt_precondition(deft_fmt *f, const double *n, const double *r, int on_
   return sync(g->ctx);
 }
 
+int deft_bulk_density(double R, double kT, double mu, int functional, double *nb_out) {
+  if (!nb_out || !(R > 0) || !(kT > 0) || !std::isfinite(mu) || functional < 0 || functional > 2)
+    return set_err(DEFT_ERR_ARG, "R, kT > 0, finite mu and a White Bear, Rosenfeld or mark II kind");
+  const double nb = deft::bulk_density(R, kT, mu, functional);
+  if (!(nb > 0)) return set_err(DEFT_ERR_ARG, "no bulk density for these parameters");
+  *nb_out = nb;
+  return DEFT_OK;
+}
+
 int deft_find_chemical_potential(double R, double kT, double nb, double *mu_out) {
   if (!mu_out || !(R > 0) || !(kT > 0) || !(nb > 0))
     return set_err(DEFT_ERR_ARG, "R, kT and nb must be positive");

@@ -440,6 +440,27 @@ double bulk_structure(const FmtSpec &f, double nQ, WbRadius wr, LocalArgs &la) {
   return nb;
 }
 
+double nQ_of(double kT);
+
+// The bulk density in equilibrium at mu for the hard-sphere kind hs with the
+// ideal gas (0 when none is found or the kind has no closed bulk form).
+double bulk_density_of(double R, double kT, double mu, int hs) {
+  FmtSpec f;
+  f.R = R;
+  f.kT = kT;
+  f.mu = mu;
+  f.terms = kTermHS | kTermIdeal | kTermMu;
+  f.hs = hs;
+  LocalArgs la;
+  memset(&la, 0, sizeof(la));
+  la.dV = 1.0;
+  WbRadius wr;
+  wr.inv_4piR = 1.0 / (4 * M_PI * R);
+  wr.inv_4piR2 = 1.0 / (4 * M_PI * R * R);
+  wr.kind = hs;
+  return bulk_structure(f, nQ_of(kT), wr, la);
+}
+
 // The structure preconditioner M^-1 r = s F^-1[ P(k) F[s r] ] with
 // s = sqrt(n / nb) on the active points (0 elsewhere) and P = 1 / H_b(k),
 // the inverse bulk Hessian (kT dV H(k) of LocalArgs, analytic weights at
@@ -2275,6 +2296,10 @@ void set_smem(K kernel, size_t bytes) {
 }
 
 }  // namespace
+
+double bulk_density(double R, double kT, double mu, int hs) {
+  return bulk_density_of(R, kT, mu, hs);
+}
 
 // Tile widths and shared-memory sizes of every kernel for one precision
 // (cs = bytes of one complex element).

@@ -73,6 +73,11 @@ struct TileChoice {
   int radix[3][8] = {};  // axes x, y, z
 };
 
+// The bulk density in equilibrium with the chemical-potential term mu
+// (integrand mu n) for hard-sphere kind hs (White Bear, Rosenfeld, mark II)
+// plus the ideal gas; 0 when there is none.  Host code.
+double bulk_density(double R, double kT, double mu, int hs);
+
 class EngineImpl;
 
 class Engine {

@@ -254,6 +254,12 @@ int deft_fmt_precondition(deft_fmt *f, const double *n, const double *r, int on_
 /* find_chemical_potential(OfEffectivePotential(HS(R)+IdealGas()), kT, nb)
  * (src/equation-of-state.cpp:189-192): the mu that makes nb the bulk density. */
 int deft_find_chemical_potential(double R, double kT, double nb, double *mu_out);
+/* Its inverse (no reference counterpart; host only): the bulk density n_b in
+ * equilibrium with the chemical-potential term mu of hard spheres of kind
+ * `functional` (DEFT_HS_*: White Bear, Rosenfeld, mark II) plus the ideal gas
+ * (the n_b the structure preconditioner uses).  DEFT_ERR_ARG when there is
+ * none. */
+int deft_bulk_density(double R, double kT, double mu, int functional, double *nb_out);
 
 /* Energy and gradient with NO device allocation (no counterpart in the
  * reference).  Meant for callers that cannot call cudaMalloc: a host

@@ -73,6 +73,34 @@ def test_find_chemical_potential_matches_oracle(oracle_mod, eta):
     assert abs(chemical_potential(1.0, 1.0, nb) / ref - 1) < 1e-13
 
 
+@pytest.mark.parametrize("eta", [0.05, 0.2, 0.3, 0.45])
+@pytest.mark.parametrize("kind", [0, 1, 2])
+def test_bulk_density_inverts_the_chemical_potential(eta, kind):
+    """deft_bulk_density (the structure preconditioner's n_b) against closed
+    forms of the bulk chemical potential: White Bear and mark II give the
+    Carnahan-Starling mu_ex (the reference's find_chemical_potential for
+    White Bear), Rosenfeld the Percus-Yevick compressibility route,
+    beta mu_ex = -ln(1-eta) + (14 eta - 13 eta^2 + 5 eta^3) / (2 (1-eta)^3)."""
+    from deft_gb300 import _lib
+    from deft_gb300.workloads import chemical_potential
+    L = _lib.load()
+    R, kT = 1.0, 1.0
+    nb = eta / (4 * math.pi / 3)
+    if kind == 1:
+        x = 18.01528 * 1822.8885 * kT / (2 * math.pi)
+        nQ = x * math.sqrt(x)
+        mu_ex = -math.log(1 - eta) + (14 * eta - 13 * eta ** 2 + 5 * eta ** 3) / (2 * (1 - eta) ** 3)
+        mu = -kT * (math.log(nb / nQ) + mu_ex)
+    else:
+        mu = chemical_potential(R, kT, nb)
+    out = ctypes.c_double()
+    assert L.deft_bulk_density(R, kT, mu, kind, ctypes.addressof(out)) == 0
+    assert abs(out.value / nb - 1) < 1e-12
+    # no solution for the tensor kinds; bad arguments refused
+    assert L.deft_bulk_density(R, kT, mu, 3, ctypes.addressof(out)) == _lib.ERR_ARG
+    assert L.deft_bulk_density(-1.0, kT, mu, kind, ctypes.addressof(out)) == _lib.ERR_ARG
+
+
 def test_grid_size_from_dx_rule():
     """GridDescription(lat, dx): N = 1 + int(e/100 + |a|/dx) (src/GridDescription.cpp:27-29);
     L = 12.8, dx = 0.2 gives 65, not 64."""
