@@ -677,7 +677,8 @@ def network_forward_ms(L, net, mask, s, n_out, stream, reps=5):
 def batched_sweep(count=64, seed=3):
     """The batched sweep (64 slits, eta in [0.05, 0.45], grids from
     {32,48,64,96,128}^3, dx = 0.2, slit widths 3-10): mixed form with the
-    density preconditioner, solved (1) as one graph launch of 64
+    structure preconditioner (the density one on the 48^3 and 96^3 grids,
+    which it does not take), solved (1) as one graph launch of 64
     device-driven solves (deft_batch_solve_device; the time includes each
     problem's grid set-up and the graph's capture), (2) by deft_batch_solve
     on 8 host threads and streams, (3) one after another on one stream.  The
@@ -687,7 +688,7 @@ def batched_sweep(count=64, seed=3):
     from deft_gb300.warmstart import solve_batch
     from deft_gb300.workloads import batch_sweep
     probs = batch_sweep(count=count, seed=seed)
-    PCD = _lib.PC_DENSITY
+    PCD = _lib.PC_STRUCTURE
     solve_batch(probs[:8], workers=8, preconditioned=PCD)  # warm-up: module, plans
     solve_batch(probs[:8], preconditioned=PCD, device_driven=True)
     t0 = time.perf_counter()
@@ -713,8 +714,8 @@ def batched_sweep(count=64, seed=3):
             "solves_per_s": count / t_dev, "solves_per_s_8_streams": count / t_conc,
             "max_profile_rel_diff_device_vs_streams": dn,
             "grid_points": int(sum(p.size for p in probs)),
-            "form": "mixed (FP32 CG stage + FP64-residual Newton refinement), density "
-                    "preconditioner, |grad F|<1e-9"}
+            "form": "mixed (FP32 CG stage + FP64-residual Newton refinement), structure "
+                    "preconditioner (density on 48^3 and 96^3), |grad F|<1e-9"}
 
 
 def cpu_eval_seconds(s, budget_s, max_evals=8):

@@ -68,7 +68,15 @@ int solve_one(Worker &w, const deft_batch_problem &p, const deft_cg_params &cgp,
   deft_cg *cg = nullptr;
   if (!s && p.mask) s = deft_fmt_set_mask(f, p.mask, 0);
   if (!s && p.V) s = deft_fmt_set_vext(f, p.V, 0);
-  if (!s) s = deft_cg_create(f, &cgp, &cg);
+  if (!s) {
+    s = deft_cg_create(f, &cgp, &cg);
+    if (s == DEFT_ERR_ARG && cgp.preconditioned == DEFT_PC_STRUCTURE) {
+      // a grid or functional the structure preconditioner does not take
+      deft_cg_params c2 = cgp;
+      c2.preconditioned = DEFT_PC_DENSITY;
+      s = deft_cg_create(f, &c2, &cg);
+    }
+  }
   if (!s) s = deft_cg_set_x(cg, p.n_init, 0);
   if (!s) s = deft_cg_solve(cg, st);
   if (!s && p.n_out) s = deft_cg_get_x(cg, p.n_out, 0);

@@ -2250,7 +2250,15 @@ int deft_batch_solve_device(int device, int count, const deft_batch_problem *pro
     if (!s) s = deft_fmt_create(grids[i], &fp, &fmts[i]);
     if (!s && p.mask) s = deft_fmt_set_mask(fmts[i], p.mask, 0);
     if (!s && p.V) s = deft_fmt_set_vext(fmts[i], p.V, 0);
-    if (!s) s = deft_cg_create(fmts[i], cgp, &cgs[i]);
+    if (!s) {
+      s = deft_cg_create(fmts[i], cgp, &cgs[i]);
+      if (s == DEFT_ERR_ARG && cgp->preconditioned == DEFT_PC_STRUCTURE) {
+        // a grid or functional the structure preconditioner does not take
+        deft_cg_params c2 = *cgp;
+        c2.preconditioned = DEFT_PC_DENSITY;
+        s = deft_cg_create(fmts[i], &c2, &cgs[i]);
+      }
+    }
     if (!s) s = deft_cg_set_x(cgs[i], p.n_init, 0);
     if (!s) s = device_problem(cgs[i], &pr[i]);
     if (!s && pr[i].eng->dev_prepare(pr[i].spec, pr[i].cfg.structure != 0)) s = eng_err(pr[i].eng);

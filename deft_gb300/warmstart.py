@@ -143,7 +143,9 @@ def solve_batch(problems, precision=_lib.PRECISION_MIXED, workers=8, gtol=1e-9, 
     """Converged solves of problems with .lat/.shape/.R/.kT/.mu/.mask/.n0
     through deft_batch_solve (`workers` host threads and streams) or, with
     device_driven, deft_batch_solve_device (one graph launch for all; needs
-    preconditioned = PC_DENSITY); returns (status, [CgStatus], [profiles])."""
+    preconditioned = PC_DENSITY or PC_STRUCTURE, the latter falling back to
+    the former on grids it does not take); returns (status, [CgStatus],
+    [profiles])."""
     keep, outs = [], []
     arr = (_lib.BatchProblem * len(problems))()
     for k, s in enumerate(problems):

@@ -386,7 +386,11 @@ typedef struct {
   deft_cg_params cg;    /* minimiser settings for every problem */
 } deft_batch_params;
 
-/* Returns DEFT_OK or the first error; status_out[i] holds problem i's result. */
+/* Returns DEFT_OK or the first error; status_out[i] holds problem i's result.
+ * With cg.preconditioned = DEFT_PC_STRUCTURE, problems whose grid or
+ * functional that preconditioner does not take (Nz not 32, 64, 128 or 256;
+ * tensor or SAFT terms) use DEFT_PC_DENSITY (here and in
+ * deft_batch_solve_device). */
 int deft_batch_solve(int device, int count, const deft_batch_problem *problems,
                      const deft_batch_params *params, deft_cg_status *status_out);
 /* The same batch as one launch: every problem gets its own grid and

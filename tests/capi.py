@@ -153,7 +153,8 @@ class CG:
 def batch_solve(problems, precision=0, workers=4, gtol=1e-9, device=0, preconditioned=0,
                 device_driven=False):
     """Runs deft_batch_solve (or, device_driven, deft_batch_solve_device with
-    the density preconditioner) on workloads.Slit-like problems (host
+    the density preconditioner, or the structure one when asked) on
+    workloads.Slit-like problems (host
     arrays); returns (status code, list of CgStatus, list of converged
     profiles)."""
     keep = []
@@ -179,7 +180,8 @@ def batch_solve(problems, precision=0, workers=4, gtol=1e-9, device=0, precondit
         p.n_out = out.ctypes.data
     st = (_lib.CgStatus * len(problems))()
     if device_driven:
-        cp = _lib.CgParams(_lib.LS_SECANT, gtol, 20000, 1.0, 0.0, 0.0, _lib.PC_DENSITY)
+        pc = preconditioned if preconditioned == _lib.PC_STRUCTURE else _lib.PC_DENSITY
+        cp = _lib.CgParams(_lib.LS_SECANT, gtol, 20000, 1.0, 0.0, 0.0, pc)
         code = _lib.load().deft_batch_solve_device(device, len(problems), arr, ctypes.byref(cp),
                                                    st)
     else:

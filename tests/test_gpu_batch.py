@@ -61,3 +61,34 @@ def test_device_batch_matches_individual_solves():
         f.close()
         g.close()
     ctx.close()
+
+
+def test_device_batch_with_the_structure_preconditioner():
+    """deft_batch_solve_device with DEFT_PC_STRUCTURE over the 32^3-128^3
+    mix: the 48^3 and 96^3 problems (no warp z transform) fall back to the
+    density preconditioner; every problem converges and matches its own
+    host-driven solve with the same preconditioner to 1e-8."""
+    from deft_gb300 import _lib
+    from deft_gb300.workloads import batch_sweep
+    from tests.capi import CG, Ctx, Fmt, Grid, batch_solve
+    probs = batch_sweep(count=6, seed=11, sizes=(32, 48, 64, 96, 128))
+    code, st, outs = batch_solve(probs, precision=1, gtol=3e-10, device_driven=True,
+                                 preconditioned=_lib.PC_STRUCTURE)
+    assert code == 0, _lib.load().deft_last_error()
+    ctx = Ctx(0)
+    for s, stat, out in zip(probs, st, outs):
+        assert stat.converged and stat.gnorm < 3e-10 and stat.status == 0
+        g = Grid(ctx, s.lat, s.shape)
+        f = Fmt(g, mu=s.mu, terms=1 | 2 | 4 | 16, mask=s.mask.reshape(-1), precision=1)
+        pc = _lib.PC_STRUCTURE if s.shape[2] in (32, 64, 128, 256) else _lib.PC_DENSITY
+        cg = CG(f, gtol=3e-10, maxiter=20000, preconditioned=pc)
+        cg.set_x(s.n0.reshape(-1))
+        c2, st2 = cg.solve()
+        assert c2 == 0 and st2.converged
+        ref = cg.get_x()
+        assert np.abs(out - ref).max() < 1e-8
+        assert np.all(out[s.mask.reshape(-1) == 0] == 0)
+        cg.close()
+        f.close()
+        g.close()
+    ctx.close()
