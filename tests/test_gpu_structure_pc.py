@@ -198,3 +198,51 @@ def test_device_driven_structure_preconditioned_solve(precision):
     finally:
         for o in (f, g, ctx):
             o.close()
+
+
+@pytest.mark.parametrize("kind", [1, 2])
+def test_structure_preconditioned_mixed_solve_other_kinds_and_vext(kind):
+    """The mixed form on FP32 vectors with the structure preconditioner for
+    the Rosenfeld and mark II kinds, with an external potential on the free
+    points (a soft attraction to the walls): converges to the FP64 solution
+    of the same functional within 1e-8 of the density scale, and its bulk
+    density is the one deft_bulk_density gives."""
+    from tests.capi import CG, Ctx, Fmt, Grid
+    s = _problem(0)
+    mask = s.mask.reshape(-1)
+    ctx = Ctx(0)
+    g = Grid(ctx, s.lat, s.shape)
+    z = np.arange(s.shape[2]) * s.dx
+    V = np.broadcast_to(-0.3 * np.exp(-((z - 1.0) / 0.6) ** 2), s.shape).reshape(-1).copy()
+    terms = TERMS | _lib.TERM_VEXT
+    f = Fmt(g, R=s.R, kT=s.kT, mu=s.mu, terms=terms, mask=mask, V=V,
+            precision=_lib.PRECISION_MIXED, functional=kind)
+    f64 = Fmt(g, R=s.R, kT=s.kT, mu=s.mu, terms=terms, mask=mask, V=V, functional=kind)
+    try:
+        nb_api = ctypes.c_double()
+        _lib.check(f.L.deft_bulk_density(s.R, s.kT, s.mu, kind, ctypes.addressof(nb_api)))
+        r = np.ones(g.size) * mask
+        zz = np.empty(g.size)
+        nb_pc = ctypes.c_double()
+        _lib.check(f.L.deft_fmt_precondition(f.h, s.n0.reshape(-1).ctypes.data, r.ctypes.data, 0,
+                                             zz.ctypes.data, ctypes.addressof(nb_pc)))
+        assert nb_pc.value == nb_api.value
+        cg = CG(f, gtol=3e-10, maxiter=3000, step=1.0, preconditioned=_lib.PC_STRUCTURE)
+        cg.set_x(s.n0.reshape(-1))
+        code, st = cg.solve()
+        assert code == 0, _lib.load().deft_last_error()
+        assert st.converged and st.stage == 1
+        x = cg.get_x()
+        cg.close()
+        _, g64, _ = f64.energy_grad(x)
+        assert np.linalg.norm(g64) < 3e-10
+        ref = CG(f64, gtol=1e-12, maxiter=5000, step=1.0, preconditioned=_lib.PC_DENSITY)
+        ref.set_x(s.n0.reshape(-1))
+        code, st_r = ref.solve()
+        assert code == 0 and st_r.converged
+        x_ref = ref.get_x()
+        ref.close()
+        assert np.abs(x - x_ref).max() <= 1e-8 * float(np.abs(x_ref).max())
+    finally:
+        for o in (f64, f, g, ctx):
+            o.close()
