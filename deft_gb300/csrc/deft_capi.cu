@@ -94,7 +94,7 @@ struct deft_cg {
   int dkey_terms = -1, dkey_hs = -1, dkey_prec = -1;
   double dkey_kT = 0;
   const double *dkey_V = nullptr, *dkey_mask = nullptr, *dkey_pg = nullptr;
-  int dkey_pc = -1;
+  int dkey_pc = -1, dkey_f32 = -1;
   // FP32 copies of the vectors for the mixed form's FP32 stage (f32_stage):
   // while f32_live they hold the state and the FP64 vectors but x are
   // stale; x is brought up to date after every step
@@ -987,8 +987,7 @@ int deft_cg_destroy(deft_cg *c) {
   cudaFree(c->pg);
   cudaFree(c->q);
   cudaFree(c->dxv);
-  for (float *v : {c->x32, c->g32, c->d32, c->gold32, c->pg32, c->V32, c->mask32, c->q32, c->dx32})
-    cudaFree(v);
+  cudaFree(c->x32);  // the block holding all nine FP32 vectors
   if (c->log) fclose(c->log);
   deft::dcg_free(c->dgraph);
   delete c;
@@ -1310,14 +1309,15 @@ int f32_buffers(deft_cg *c) {
   Engine *e = eng_of(c);
   const size_t n = nr(c->f->grid);
   if (!c->x32) {
-    for (float **v : {&c->x32, &c->g32, &c->d32, &c->gold32, &c->pg32, &c->V32, &c->mask32,
-                      &c->q32, &c->dx32}) {
-      cudaError_t ce = cudaMalloc((void **)v, sizeof(float) * n);
-      if (ce != cudaSuccess) {
-        *v = nullptr;
-        return cuda_err(ce, "cudaMalloc");
-      }
-    }
+    // one allocation for the nine vectors (each 256-byte aligned): a batch
+    // of minimisers pays one cudaMalloc each instead of nine
+    const size_t stride = (n + 63) / 64 * 64;
+    float *block = nullptr;
+    cudaError_t ce = cudaMalloc((void **)&block, sizeof(float) * stride * 9);
+    if (ce != cudaSuccess) return cuda_err(ce, "cudaMalloc");
+    float **vs[9] = {&c->x32, &c->g32, &c->d32, &c->gold32, &c->pg32, &c->V32, &c->mask32,
+                     &c->q32, &c->dx32};
+    for (int i = 0; i < 9; i++) *vs[i] = block + stride * i;
   }
   if (c->f32_fields != c->f->fields_version) {
     if ((c->f->V && e->to_f32(c->f->V, c->V32)) || (c->f->mask && e->to_f32(c->f->mask, c->mask32)))
@@ -2137,6 +2137,21 @@ int device_problem(deft_cg *c, deft::DcgProblem *p) {
   p->eng = e;
   p->spec = spec;
   p->v = {c->x, c->g, c->d, c->gold, c->pg, c->q, c->dxv, V, mask};
+  // the mixed form's FP32 stage on FP32 vectors where the host-driven one
+  // would use them
+  cf.f32 = 0;
+  if (cf.mixed && f32_stage(c, spec)) {
+    if (int s = f32_buffers(c)) return s;
+    c->f32_live = false;
+    p->v.x32 = c->x32;
+    p->v.g32 = c->g32;
+    p->v.d32 = c->d32;
+    p->v.gold32 = c->gold32;
+    p->v.pg32 = c->pg32;
+    p->v.V32 = c->V32;
+    p->v.mask32 = c->mask32;
+    cf.f32 = 1;
+  }
   return DEFT_OK;
 }
 
@@ -2188,7 +2203,7 @@ int deft_cg_solve_device(deft_cg *c, deft_cg_status *st) {
   if (c->dgraph && (c->dkey_terms != spec.terms || c->dkey_hs != spec.hs ||
                     c->dkey_prec != spec.precision || c->dkey_kT != spec.kT ||
                     c->dkey_V != p.v.V || c->dkey_mask != p.v.mask || c->dkey_pg != p.v.pg ||
-                    c->dkey_pc != p.cfg.structure)) {
+                    c->dkey_pc != p.cfg.structure || c->dkey_f32 != p.cfg.f32)) {
     deft::dcg_free(c->dgraph);
     c->dgraph = nullptr;
   }
@@ -2205,6 +2220,7 @@ int deft_cg_solve_device(deft_cg *c, deft_cg_status *st) {
     c->dkey_mask = p.v.mask;
     c->dkey_pg = p.v.pg;
     c->dkey_pc = p.cfg.structure;
+    c->dkey_f32 = p.cfg.f32;
   }
   deft::dcg_set_config(c->dgraph, 0, p.cfg, spec);
   deft::DcgOutcome o;

@@ -53,6 +53,7 @@ struct DcgState {
   double pgoldsqr, s_acc, s_prev, beta, coef;
   // Newton refinement
   int inner_k, bt, stepped;
+  int x_pending;  // the FP32 stage's x32 is to be copied into x (f32)
   double E_before, scale, rz, tol_in, alpha_n, beta_n, coef_dx;
   // results of the vector kernels' reductions, and their block counter
   double red[2];
@@ -239,6 +240,54 @@ __global__ void k_dcg_newton_step(const DcgState *__restrict__ st, const double 
   }
 }
 
+// The FP32 stage on FP32 vectors (cfg.f32): x32 += coef d32; the density
+// preconditioner with its sums; the direction; and, on entering the Newton
+// refinement, x = x32 (once: the flag is cleared by the next kernel).
+__global__ void k_dcg_move32(const double *__restrict__ coef, float *__restrict__ x,
+                             const float *__restrict__ v, int N) {
+  const float c = (float)*coef;
+  if (*coef == 0.0) return;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x)
+    x[i] += c * v[i];
+}
+__global__ void k_dcg_precond_dots32(DcgState *st, const float *__restrict__ n,
+                                     const float *__restrict__ g, const float *__restrict__ mask,
+                                     const float *__restrict__ gold, float inv_c,
+                                     float *__restrict__ z, int N, double *partials) {
+  float acc[2] = {0, 0};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+    const float m = mask ? mask[i] : 1.0f;
+    const float nv = n[i], gv = g[i];
+    const float zv = (m != 0.0f && nv > 0.0f) ? gv * nv * inv_c : 0.0f;
+    z[i] = zv;
+    acc[0] += zv * gv;
+    acc[1] += zv * gold[i];
+  }
+  double accd[2] = {acc[0], acc[1]};
+  finish_to_state<2>(accd, partials, st);
+}
+__global__ void k_dcg_direction32(const DcgState *__restrict__ st, float *__restrict__ d,
+                                  const float *__restrict__ z, const float *__restrict__ g,
+                                  float *__restrict__ gold, int N) {
+  const float beta = (float)st->beta;
+  const float *v = st->plain ? g : z;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+    const float gv = g[i];
+    d[i] = -1.0f * v[i] + beta * d[i];
+    gold[i] = gv;
+  }
+}
+__global__ void k_dcg_sync_x(const DcgState *__restrict__ st, const float *__restrict__ x32,
+                             double *__restrict__ x, int N) {
+  if (!st->x_pending) return;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x)
+    x[i] = (double)x32[i];
+}
+__global__ void k_dcg_clear_pending(DcgState *st) {
+  if (threadIdx.x || blockIdx.x) return;
+  st->x_pending = 0;
+}
+
 // p = z + beta p.
 __global__ void k_dcg_p_update(const DcgState *__restrict__ st, double *__restrict__ p,
                                const double *__restrict__ z, int N) {
@@ -260,6 +309,7 @@ __device__ void stage_end(DcgState *st) {
   if (st->mixed) {
     st->mode = kModeNewtonOuter;
     st->stepped = 0;
+    st->x_pending = 1;  // (read only when the stage ran on FP32 vectors)
   } else {
     st->mode = kModeDone;
     st->converged = 1;
@@ -655,20 +705,35 @@ bool add_solve(Builder &b, Solve &sv) {
       }, nullptr))
     return false;
 
-  // 0: line-search trial
+  // 0: line-search trial (on the FP32 vectors with cfg.f32)
+  const bool v32 = sv.p.cfg.f32 != 0;
   const double *db3[3] = {v.d, v.g, v.gold};
+  const float *db3f[3] = {v.d32, v.g32, v.gold32};
+  const float *mask32 = mask ? v.mask32 : nullptr;
   if (!b.handle(sb[0], &h_dir, 0)) return false;
   if (!cap(kSeqTrial, 2, sb[0], none, [&] {
-        k_dcg_move<<<nb, kThreads, 0, s>>>(&st->coef, v.x, v.d, N);
-        if (e->dev_eval(stage, v.x, v.V, mask, v.g, 3, db3)) return false;
+        if (v32) {
+          k_dcg_move32<<<nb, kThreads, 0, s>>>(&st->coef, v.x32, v.d32, N);
+          if (e->dev_eval32(stage, v.x32, v.V ? v.V32 : nullptr, mask32, v.g32, 3, db3f))
+            return false;
+        } else {
+          k_dcg_move<<<nb, kThreads, 0, s>>>(&st->coef, v.x, v.d, N);
+          if (e->dev_eval(stage, v.x, v.V, mask, v.g, 3, db3)) return false;
+        }
         k_dcg_decide_stage<<<1, 32, 0, s>>>(st, res, h_dir);
         return true;
       }, &sinks))
     return false;
   if (!b.cond(sb[0], sinks, h_dir, cudaGraphCondTypeIf, 1, &n, &ib)) return false;
   const bool spc = sv.p.cfg.structure != 0;
-  if (!cap(kSeqDirection, spc ? 3 : 3, ib, none, [&] {
-        if (spc) {
+  if (!cap(kSeqDirection, 3, ib, none, [&] {
+        if (v32 && spc) {
+          if (e->dev_pc32(stage, v.x32, v.g32, mask32, v.pg32, v.g32, v.gold32)) return false;
+          k_dcg_take<<<1, 32, 0, s>>>(st, res, 0, 1);
+        } else if (v32) {
+          k_dcg_precond_dots32<<<nb, kThreads, 0, s>>>(st, v.x32, v.g32, mask32, v.gold32,
+                                                       (float)inv_c, v.pg32, N, part);
+        } else if (spc) {
           if (e->dev_pc(stage, v.x, v.g, mask, v.pg, v.g, v.gold)) return false;
           k_dcg_take<<<1, 32, 0, s>>>(st, res, 0, 1);
         } else {
@@ -676,7 +741,10 @@ bool add_solve(Builder &b, Solve &sv) {
                                                      part);
         }
         k_dcg_decide_direction<<<1, 32, 0, s>>>(st);
-        k_dcg_direction<<<nb, kThreads, 0, s>>>(st, v.d, v.pg, v.g, v.gold, N);
+        if (v32)
+          k_dcg_direction32<<<nb, kThreads, 0, s>>>(st, v.d32, v.pg32, v.g32, v.gold32, N);
+        else
+          k_dcg_direction<<<nb, kThreads, 0, s>>>(st, v.d, v.pg, v.g, v.gold, N);
         return true;
       }, nullptr))
     return false;
@@ -695,7 +763,12 @@ bool add_solve(Builder &b, Solve &sv) {
   // step), p in d, q, dx.
   const double *db1[1] = {v.g};
   if (!b.handle(sb[1], &h_bt, 0) || !b.handle(sb[1], &h_setup, 0)) return false;
-  if (!cap(kSeqOuter, 2, sb[1], none, [&] {
+  if (!cap(kSeqOuter, v32 ? 4 : 2, sb[1], none, [&] {
+        if (v32) {
+          // entering the refinement: x from the FP32 stage's x32 (once)
+          k_dcg_sync_x<<<nb, kThreads, 0, s>>>(st, v.x32, v.x, N);
+          k_dcg_clear_pending<<<1, 32, 0, s>>>(st);
+        }
         k_dcg_move<<<nb, kThreads, 0, s>>>(&st->coef, v.x, v.d, N);
         if (e->dev_eval(f64, v.x, v.V, mask, v.g, 1, db1)) return false;
         k_dcg_decide_outer<<<1, 32, 0, s>>>(st, res, h_bt, h_setup);
@@ -873,6 +946,18 @@ int dcg_run(DcgGraph *gr, cudaStream_t stream, DcgOutcome *out, std::string *err
       if (err) *err = sv.p.eng->last_error();
       return DEFT_ERR_CUDA;
     }
+    if (sv.p.cfg.f32) {
+      // the FP32 stage starts from x with no previous direction (d = 0:
+      // the first direction is beta d - z with beta = 0)
+      const size_t bytes = sizeof(float) * (size_t)sv.p.eng->geom().NR;
+      if (sv.p.eng->to_f32(sv.p.v.x, sv.p.v.x32)) {
+        if (err) *err = sv.p.eng->last_error();
+        return DEFT_ERR_CUDA;
+      }
+      const cudaError_t r0 = cudaMemsetAsync(sv.p.v.d32, 0, bytes, stream);
+      const cudaError_t r1 = cudaMemsetAsync(sv.p.v.gold32, 0, bytes, stream);
+      if (r0 != cudaSuccess || r1 != cudaSuccess) return fail("FP32 vectors", r0 ? r0 : r1);
+    }
     gr->host[i] = initial_state(sv.p.cfg);
     const cudaError_t r = cudaMemcpyAsync(sv.st, &gr->host[i], sizeof(DcgState),
                                           cudaMemcpyHostToDevice, stream);
@@ -885,6 +970,16 @@ int dcg_run(DcgGraph *gr, cudaStream_t stream, DcgOutcome *out, std::string *err
                         stream);
   if (r == cudaSuccess) r = cudaStreamSynchronize(stream);
   if (r != cudaSuccess) return fail("solve", r);
+  for (int i = 0; i < count; i++) {
+    // a solve that ended in its FP32 stage leaves x in x32
+    const Solve &sv = gr->solves[i];
+    if (sv.p.cfg.f32 && gr->host[i].mixed && gr->host[i].evals_fp64 == 0 &&
+        sv.p.eng->to_f64(sv.p.v.x32, sv.p.v.x)) {
+      if (err) *err = sv.p.eng->last_error();
+      return DEFT_ERR_CUDA;
+    }
+  }
+  if (cudaStreamSynchronize(stream) != cudaSuccess) return fail("solve", cudaGetLastError());
   for (int i = 0; i < count; i++) {
     DcgState &s = gr->host[i];
     DcgOutcome &o = out[i];

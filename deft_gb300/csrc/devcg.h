@@ -13,10 +13,14 @@
 
 namespace deft {
 
-// Device vectors of one solve (NR doubles each; V and mask may be null).
+// Device vectors of one solve (NR doubles each; V and mask may be null),
+// and, for the mixed form's FP32 stage on FP32 vectors (cfg.f32), their
+// FP32 copies (NR floats each).
 struct DcgVectors {
   double *x, *g, *d, *gold, *pg, *q, *dx;
   const double *V, *mask;
+  float *x32 = nullptr, *g32 = nullptr, *d32 = nullptr, *gold32 = nullptr, *pg32 = nullptr;
+  const float *V32 = nullptr, *mask32 = nullptr;
 };
 
 struct DcgConfig {
@@ -28,6 +32,7 @@ struct DcgConfig {
   int max_loops;      // evaluations + products budget of the device loop
   int mixed;          // 1: FP32 stage + Newton refinement on the FP64 gradient
   int structure = 0;  // 1: the structure preconditioner (else the density one)
+  int f32 = 0;        // 1: the FP32 stage on the FP32 vectors of DcgVectors
 };
 
 struct DcgOutcome {

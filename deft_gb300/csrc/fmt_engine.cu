@@ -3990,6 +3990,28 @@ int Engine::dev_pc(const FmtSpec &, const double *n, const double *r, const doub
   return impl_->pc_launch<double>(n, r, mask, z, a, b);
 }
 
+int Engine::dev_pc32(const FmtSpec &, const float *n, const float *r, const float *mask, float *z,
+                     const float *a, const float *b) {
+  return impl_->pc_launch<float>(n, r, mask, z, a, b);
+}
+
+int Engine::dev_eval32(const FmtSpec &f, const float *n, const float *V, const float *mask,
+                       float *grad, int kd, const float *const *db) {
+  EngineImpl &e = *impl_;
+  if (!e.f32_vectors_ok(f)) {
+    e.err = "FP32 vectors: not for this functional or grid";
+    return -1;
+  }
+  GradDotsT<float> gd{};
+  for (int i = 0; i < kd; i++) gd.b[i] = db[i] == grad ? nullptr : db[i];
+  gd.k = kd;
+  gd.partials = e.grad_partials;
+  e.dev_only = true;
+  const int r = e.eval_launch<float, float>(f, n, V, mask, grad, kd > 0 ? &gd : nullptr);
+  e.dev_only = false;
+  return r;
+}
+
 int Engine::dev_hvp(const FmtSpec &f, const double *dx, const double *mask, double *out) {
   return impl_->hvp_launch(f, dx, mask, out, true);
 }

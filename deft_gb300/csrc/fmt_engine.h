@@ -241,6 +241,13 @@ class Engine {
   // z = M^-1 r with (z.a, z.b, a.a) at dev_results()[0..3).
   int dev_pc(const FmtSpec &f, const double *n, const double *r, const double *mask, double *z,
              const double *a, const double *b);
+  // ... and their FP32-vector forms (f32_vectors_ok): the mixed form's
+  // evaluation with the dots of the new gradient, the structure
+  // preconditioner.
+  int dev_eval32(const FmtSpec &f, const float *n, const float *V, const float *mask,
+                 float *grad, int kd, const float *const *db);
+  int dev_pc32(const FmtSpec &f, const float *n, const float *r, const float *mask, float *z,
+               const float *a, const float *b);
   double *dev_results() const;
   // Blocks of the FP64 vector kernels (a multiple of the SM count, at most
   // one block per 256 points).
