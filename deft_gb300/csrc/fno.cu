@@ -1346,18 +1346,31 @@ int deft_fno_adam(deft_fno *f, float lr) {
 
 // Warm start for the minimiser: n = nb max(y, floor_rel) on free points,
 // 0 where mask == 0.  mask and n_out are DEVICE pointers of N^3 doubles.
-int deft_fno_warm_start(deft_fno *f, const double *mask_dev, double eta, double nb,
-                        double floor_rel, double *n_out_dev) {
-  if (!f || !mask_dev || !n_out_dev) return DEFT_ERR_ARG;
-  cudaSetDevice(f->device);
-  const int C = f->C;
+}  // extern "C"
+
+namespace {
+
+// The warm start's launches on the network's stream, not waited for.
+int warm_start_queue(deft_fno *f, const double *mask_dev, double eta, double nb,
+                     double floor_rel, double *n_out_dev) {
   k_d2f<<<grid_for(f->NR), kT, 0, f->stream>>>(mask_dev, f->mask, f->NR, 1.f);
   f->launches += 2;  // this and the density below
   if (int s = forward(f, (float)eta, false)) return s;
   project(f, nullptr, nullptr, nullptr, nullptr);
   k_density<<<grid_for(f->NR), kT, 0, f->stream>>>(f->y, mask_dev, nb, floor_rel, n_out_dev,
                                                    f->NR);
-  if (int s = check(f, "warm start")) return s;
+  return check(f, "warm start");
+}
+
+}  // namespace
+
+extern "C" {
+
+int deft_fno_warm_start(deft_fno *f, const double *mask_dev, double eta, double nb,
+                        double floor_rel, double *n_out_dev) {
+  if (!f || !mask_dev || !n_out_dev) return DEFT_ERR_ARG;
+  cudaSetDevice(f->device);
+  if (int s = warm_start_queue(f, mask_dev, eta, nb, floor_rel, n_out_dev)) return s;
   return cudaStreamSynchronize(f->stream) == cudaSuccess ? DEFT_OK : DEFT_ERR_CUDA;
 }
 
@@ -1379,7 +1392,10 @@ int deft_fno_initial_density(deft_fno *f, deft_fmt *fmt, const double *mask_dev,
   }
   k_bulk<<<grid_for(f->NR), kT, 0, f->stream>>>(mask_dev, nb, f->bulk, f->NR);
   f->launches++;
-  if (int s = deft_fno_warm_start(f, mask_dev, eta, nb, floor_rel, n_out_dev)) return s;
+  if (cudaStreamSynchronize(f->stream) != cudaSuccess) return check(f, "bulk start");
+  // the network runs on its own stream while the bulk start is evaluated on
+  // the functional's (the forward pass is latency-bound and leaves room)
+  if (int s = warm_start_queue(f, mask_dev, eta, nb, floor_rel, n_out_dev)) return s;
   double E0 = 0, E1 = 0;
   if (gnorm_bulk_out) {
     // energy and gradient of the bulk start (gradient in the buffer's upper half)
@@ -1397,6 +1413,7 @@ int deft_fno_initial_density(deft_fno *f, deft_fmt *fmt, const double *mask_dev,
   } else if (int s = deft_fmt_energy(fmt, f->bulk, 1, &E0, nullptr)) {
     return s;
   }
+  if (cudaStreamSynchronize(f->stream) != cudaSuccess) return check(f, "warm start");
   const int s1 = deft_fmt_energy(fmt, n_out_dev, 1, &E1, nullptr);
   const bool use = s1 == DEFT_OK && std::isfinite(E1) && E1 <= E0;
   if (!use) {
