@@ -901,7 +901,17 @@ void launch_axis(deft_fno *f, const float2 *in, float2 *out, const float2 *E, in
     const size_t sm2 = sm + sizeof(float2) * (size_t)(S - 1) * Nin * IC;
     const int tiles = (outer * ((inner + IC - 1) / IC) + S - 1) / S;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    int grid = 2 * (sms > 0 ? sms : 148);
+    // as many resident blocks as shared memory and registers allow: the
+    // staging loads of one pass are not overlapped with its multiply-adds,
+    // so other resident blocks hide them
+    int bps = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_dft_tile, 256, sm2) !=
+            cudaSuccess ||
+        bps < 1) {
+      cudaGetLastError();  // the query's own error, if any, is not the launch's
+      bps = 2;
+    }
+    int grid = bps * (sms > 0 ? sms : 148);
     if (grid > tiles) grid = tiles;
     k_dft_tile<<<grid, 256, sm2, f->stream>>>(in, out, E, outer, Nin, Mout, inner, IC, S);
     return;
