@@ -213,28 +213,36 @@ __global__ void k_dft_axis(const float2 *__restrict__ in, float2 *__restrict__ o
 }
 
 // The same contraction by tiles: a tile is (o, IC consecutive i), its
-// Nin x IC inputs staged in shared memory with the whole table E (rows
-// padded by one entry against bank conflicts), staged once per block; a
-// thread forms four outputs m = 4 g .. 4 g + 3 of one column i, so each
-// staged input feeds four complex multiply-adds.  For the y contractions
-// (inner = Kz) a tile is a whole contiguous slab; S tiles go through a block
-// at once when one leaves threads idle.
+// Nin x IC inputs staged in shared memory with the whole table E, staged
+// once per block n-major ([n][m], Mout padded with zero rows to a multiple
+// of four); a thread forms four outputs m = 4 g .. 4 g + 3 of one column i,
+// so per n it reads one staged input and its four table entries as two
+// 16-byte words and does sixteen fused multiply-adds.  For the y
+// contractions (inner = Kz) a tile is a whole contiguous slab; S tiles go
+// through a block at once when one leaves threads idle.
 constexpr int kAxMR = 4;
+__host__ __device__ constexpr int ax_rows(int Mout) { return (Mout + kAxMR - 1) / kAxMR * kAxMR; }
+__device__ __forceinline__ void cmac(float &re, float &im, float2 a, float bx, float by) {
+  re = fmaf(a.x, bx, re);
+  re = fmaf(-a.y, by, re);
+  im = fmaf(a.x, by, im);
+  im = fmaf(a.y, bx, im);
+}
 __global__ void __launch_bounds__(256) k_dft_tile(const float2 *__restrict__ in,
                                                   float2 *__restrict__ out,
                                                   const float2 *__restrict__ E, int outer,
                                                   int Nin, int Mout, int inner, int IC, int S) {
   extern __shared__ __align__(16) float2 smt[];
-  const int ES = Nin + 1;
-  float2 *Es = smt;             // [Mout][Nin + 1]
-  float2 *Tb = Es + Mout * ES;  // S x [Nin][IC]
-  for (int i = threadIdx.x; i < Mout * Nin; i += blockDim.x) {
-    const int m = i / Nin, n = i - m * Nin;
-    Es[m * ES + n] = E[i];
+  const int MS = ax_rows(Mout);
+  float2 *Es = smt;             // [Nin][MS]
+  float2 *Tb = Es + Nin * MS;   // S x [Nin][IC]
+  for (int i = threadIdx.x; i < Nin * MS; i += blockDim.x) {
+    const int n = i / MS, m = i - n * MS;
+    Es[i] = m < Mout ? E[m * Nin + n] : make_float2(0.f, 0.f);
   }
   const int nch = (inner + IC - 1) / IC;
   const int tiles = outer * nch;
-  const int groups = (Mout + kAxMR - 1) / kAxMR;
+  const int groups = MS / kAxMR;
   const int per = groups * IC;  // work items of one tile
   for (int t0 = blockIdx.x * S; t0 < tiles; t0 += gridDim.x * S) {
     __syncthreads();  // the previous batch's readers are done (and E is in)
@@ -256,23 +264,24 @@ __global__ void __launch_bounds__(256) k_dft_tile(const float2 *__restrict__ in,
       if (tile >= tiles) continue;
       const int o = tile / nch, i0 = (tile - o * nch) * IC;
       const int ic = inner - i0 < IC ? inner - i0 : IC;
-      const float2 *T = Tb + (size_t)s * Nin * IC;
       const int g = idx / IC, j = idx - g * IC;
       if (j >= ic) continue;
+      const float2 *pa = Tb + (size_t)s * Nin * IC + j;
+      // the group's four table entries of row n: two 16-byte words (MS and
+      // 4 g are multiples of four float2, the array is 16-byte aligned)
+      const float4 *pe = reinterpret_cast<const float4 *>(Es + g * kAxMR);
+      const int ES4 = MS / 2;
       float re[kAxMR], im[kAxMR];
 #pragma unroll
       for (int r = 0; r < kAxMR; r++) re[r] = im[r] = 0.f;
-      const float2 *e0 = Es + (size_t)(g * kAxMR) * ES;
+#pragma unroll 4
       for (int n = 0; n < Nin; n++) {
-        const float2 a = T[n * IC + j];
-#pragma unroll
-        for (int r = 0; r < kAxMR; r++) {
-          if (g * kAxMR + r < Mout) {
-            const float2 b = e0[r * ES + n];
-            re[r] += a.x * b.x - a.y * b.y;
-            im[r] += a.x * b.y + a.y * b.x;
-          }
-        }
+        const float2 a = pa[n * IC];
+        const float4 b01 = pe[n * ES4], b23 = pe[n * ES4 + 1];
+        cmac(re[0], im[0], a, b01.x, b01.y);
+        cmac(re[1], im[1], a, b01.z, b01.w);
+        cmac(re[2], im[2], a, b23.x, b23.y);
+        cmac(re[3], im[3], a, b23.z, b23.w);
       }
 #pragma unroll
       for (int r = 0; r < kAxMR; r++) {
@@ -885,7 +894,7 @@ void launch_axis(deft_fno *f, const float2 *in, float2 *out, const float2 *E, in
                  int Mout, int inner) {
   // tiles of up to 32 columns (a whole slab when inner <= 32) while they fit
   const int IC = inner < 32 ? inner : 32;
-  const size_t sm = sizeof(float2) * ((size_t)Mout * (Nin + 1) + (size_t)Nin * IC);
+  const size_t sm = sizeof(float2) * ((size_t)ax_rows(Mout) * Nin + (size_t)Nin * IC);
   if (sm <= 96 * 1024) {
     int sms = 0, dev = 0;
     cudaGetDevice(&dev);
@@ -895,7 +904,7 @@ void launch_axis(deft_fno *f, const float2 *in, float2 *out, const float2 *E, in
       if (dev >= 0 && dev < 64) attr[dev] = true;
     }
     // tiles per block pass: fill the 256 threads when a tile has few items
-    const int per = ((Mout + kAxMR - 1) / kAxMR) * IC;
+    const int per = (ax_rows(Mout) / kAxMR) * IC;
     int S = per >= 256 ? 1 : 256 / per;
     while (S > 1 && sm + sizeof(float2) * (size_t)(S - 1) * Nin * IC > 96 * 1024) S--;
     const size_t sm2 = sm + sizeof(float2) * (size_t)(S - 1) * Nin * IC;
