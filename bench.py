@@ -336,6 +336,19 @@ def cufft_comparison(N, dev):
             "cufft_ms": cu, "max_rel_diff": err, "note": "cuFFT timed only as a comparison"}
 
 
+def max_over_ranks(ms, world, device):
+    """A barrier-bracketed step time reduced to its maximum over the ranks
+    (each rank an independent replica on its own GPU: the only exchange is
+    this scalar); with one rank ms is returned unchanged."""
+    if world <= 1:
+        return ms
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(ms)], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def run_ours(args, rank, world):
     import torch
     from deft_gb300 import _lib, autotune
@@ -462,12 +475,7 @@ def run_ours(args, rank, world):
         torch.cuda.synchronize()
         barrier()
         ck = clocks.stop() if clocked else None
-        ms = e0.elapsed_time(e1)
-        if world > 1:
-            import torch.distributed as dist
-            t = torch.tensor([ms], device=dd)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
+        ms = max_over_ranks(e0.elapsed_time(e1), world, dd)
         nl = (sum(v[0] for v in kernel_profile(L, sv.grid).values()) - launches0
               + L.deft_fno_launches(net.h) - fno0)
         bad = [k for k, (st, _) in enumerate(stats) if not (st.converged and st.status == 0
