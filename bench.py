@@ -162,14 +162,16 @@ class Clocks:
 # ---------------------------------------------------------------------------
 # our arm
 
-def alg_bytes(N, fp32):
+def alg_bytes(N, fp32, vec_bytes=8):
     """Algorithmic bytes per launch of each kernel: the compulsory field reads
     and writes of the stage (nothing for the analytic weights).  Real fields
-    at the boundary (n, mask, gradient) are FP64 (R = 8 N^3); spectra are
-    C = 16 N^2 (N/2+1) in the FP64 form and 8 N^2 (N/2+1) in the mixed form."""
+    at the boundary (n, mask, gradient) are R = vec_bytes N^3: FP64 (8) in
+    general, FP32 (4) on the FP32 vectors of the mixed form's CG stages;
+    spectra are C = 16 N^2 (N/2+1) in the FP64 form and 8 N^2 (N/2+1) in the
+    mixed form."""
     NR = N ** 3
     NC = N * N * (N // 2 + 1)
-    R, C = 8 * NR, (8 if fp32 else 16) * NC
+    R, C = vec_bytes * NR, (8 if fp32 else 16) * NC
     return {
         "z_r2c": R + C,
         "y_fft_1field": 2 * C,
@@ -179,7 +181,7 @@ def alg_bytes(N, fp32):
         "z_phi_energy": 5 * C + R,
         "x_conv_adj": 5 * C + C,
         "z_grad": C + 3 * R,
-        "z_hess": 5 * C + R + 44 * NR,
+        "z_hess": 5 * C + 8 * NR + 44 * NR,  # set up at the FP64 iterate
         "z_jac": 5 * C + 40 * NR + 5 * C,
         "z_hvp_out": C + 4 * NR + 3 * R,
         "eval_model": 4 * R + 24 * C,  # one energy+gradient evaluation
@@ -190,8 +192,16 @@ CONV_KERNELS = ("z_r2c", "y_fft_1field", "y_fft_5fields", "x_conv_fwd", "z_phi_g
                 "z_phi_energy", "x_conv_adj", "z_grad")
 
 
-CONV_KERNELS = ("z_r2c", "y_fft_1field", "y_fft_5fields", "x_conv_fwd", "z_phi_grad",
-                "z_phi_energy", "x_conv_adj", "z_grad")
+def f32_vectors(N, pc_none):
+    """Whether the mixed solves keep their CG vectors in FP32 (the library's
+    rule: a preconditioned secant CG, hard spheres on, Nz = 32, 64, 128 or
+    256, and DEFT_F32_VECTORS not set to 0)."""
+    ev = os.environ.get("DEFT_F32_VECTORS")
+    try:
+        on = int(ev) != 0 if ev else True
+    except ValueError:
+        on = False
+    return on and not pc_none and N in (32, 64, 128, 256)
 
 
 def kernel_profile(L, grid):
@@ -225,9 +235,9 @@ def by_precision(prof, fp32):
     return out
 
 
-def roofline(prof, N, fp32, peak, peak_kind):
+def roofline(prof, N, fp32, peak, peak_kind, vec_bytes=8):
     prof = by_precision(prof, fp32)
-    ab = alg_bytes(N, fp32)
+    ab = alg_bytes(N, fp32, vec_bytes)
     dom = max((k for k in prof if k in ab), key=lambda k: prof[k][1])
     dom_ms = prof[dom][1] / prof[dom][0]
     achieved = ab[dom] / (dom_ms * 1e-3) / 1e9
@@ -646,7 +656,11 @@ def run_ours(args, rank, world):
         "gpu_launches": nl_w,
         "clocks": ck_w,
         "clocks_fp64": ck_64,
-        "roofline": roofline(prof_w1, N, True, peak, peak_kind),
+        # the profiled solve's FP32 launches run on FP32 vectors, all but the
+        # warm start's two checks (bulk start and estimate, FP64 at their
+        # boundary) and the Hessian set-up at the FP64 iterate
+        "roofline": roofline(prof_w1, N, True, peak, peak_kind,
+                             vec_bytes=4 if f32_vectors(N, PC == _lib.PC_NONE) else 8),
         "roofline_fp64": dict(roofline(prof_64, N, False, peak, peak_kind),
                               note="FP64 form: bound by the FP64 pipe (measured 1.0 TFLOP/s "
                                    "FMA on this GB300), not by HBM"),

@@ -1275,7 +1275,7 @@ int cg_precond_dots(deft_cg *c, const deft::FmtSpec &spec, const float *, double
 #endif
 
 // Whether the FP32 stage of the mixed form keeps its vectors in FP32: the
-// secant CG with the density preconditioner on the plain White Bear kinds
+// secant CG with the density or structure preconditioner on the plain kinds
 // (no effective-potential variable, tensor or SAFT terms) where the
 // engine's FP32 gradient kernels take FP32 vectors.  FP32 vectors halve the
 // vector traffic and spare the gradient kernels the FP64 conversions (the
