@@ -848,7 +848,11 @@ def run_reference(args, rank, world):
                                             f"concurrent (the reference has no threading)",
                              "per_step_s": [round(x, 2) for x in secs],
                              "per_step_evals": evals,
-                             "wall_s_all_steps": wall}),
+                             "wall_s_all_steps": wall,
+                             "value_vs_ms_per_step": "value is the mean time of one "
+                             "single-threaded solve (the metric's latency); ms_per_step is the "
+                             "wall time of all timed steps over their count, the solves "
+                             "running concurrently"}),
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": workers, "kind": "port",
                          "sample": sample},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
